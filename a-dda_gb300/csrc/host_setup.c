@@ -1,0 +1,178 @@
+/* host_setup.c - host-side inputs of the DDA hot path: particle lattice, incident plane wave, polarisabilities.
+ *
+ * These are the data the reference's C host hands to the FFT matvec and the iterative solver. They are restated here
+ * so that a caller without the reference host (the tests, bench.py, other front ends) can build the same inputs:
+ *   adda_gb300_fit_box          <- FitBox / FitBox_yz + InitShape sizing    src/make_particle.c:1283-1308, 1912-1919
+ *   adda_gb300_make_particle    <- MakeParticle box loop                    src/make_particle.c:1984-2230
+ *   adda_gb300_rotation         <- InitRotation (zyz Euler angles)          src/crosssec.c:82-139
+ *   adda_gb300_plane_wave       <- GenerateB, free-space plane wave         src/GenerateB.c:324-328
+ *   adda_gb300_polarizability   <- CoupleConstant (CM, LDR, RRC, DGF)        src/calculator.c:100-262
+ * All functions are pure host code: no GPU is touched.
+ */
+#include "adda_gb300.h"
+
+#include <complex.h>
+#include <math.h>
+#include <string.h>
+
+#define TWO_PI_D 6.283185307179586476925286766559
+#define FOUR_PI_D 12.566370614359172953850573533118
+
+int adda_gb300_fit_box(int shape, const double *pars, int boxX, int *boxY, int *boxZ)
+{
+	double yx = 1, zx = 1;
+	switch (shape) {
+		case ADDA_SHAPE_SPHERE: break;
+		case ADDA_SHAPE_ELLIPSOID:
+		case ADDA_SHAPE_BOX:
+			if (pars) { yx = pars[0]; zx = pars[1]; }
+			break;
+		default: return ADDA_GB300_EINVAL;
+	}
+	if (boxX < 1 || boxX % 2) return ADDA_GB300_EINVAL;
+	/* FitBox_yz with jagged=1: 2*floor((size+1)/2) */
+	*boxY = 2 * (int)floor((yx * boxX + 1) / 2);
+	*boxZ = 2 * (int)floor((zx * boxX + 1) / 2);
+	if (*boxY < 2) *boxY = 2;
+	if (*boxZ < 2) *boxZ = 2;
+	return ADDA_GB300_OK;
+}
+
+size_t adda_gb300_make_particle(int shape, const double *pars, int boxX, int boxY, int boxZ, uint16_t *position,
+	uint8_t *material)
+{
+	double invsqY = 1, invsqZ = 1, haspY = 0.5, haspZ = 0.5;
+	if (shape == ADDA_SHAPE_ELLIPSOID && pars) {
+		invsqY = 1 / (pars[0] * pars[0]);
+		invsqZ = 1 / (pars[1] * pars[1]);
+	}
+	if (shape == ADDA_SHAPE_BOX && pars) {
+		haspY = pars[0] / 2;
+		haspZ = pars[1] / 2;
+	}
+	size_t idx = 0;
+	/* loop order z, y, x (x fastest), as in the reference: dipoles on one x-line are consecutive */
+	for (int k = 0; k < boxZ; k++)
+		for (int j = 0; j < boxY; j++)
+			for (int i = 0; i < boxX; i++) {
+				/* jagged=1: centre of cell relative to the box centre, scaled by boxX */
+				double xr = (i - boxX / 2 + 0.5) / boxX;
+				double yr = (j - boxY / 2 + 0.5) / boxX;
+				double zr = (k - boxZ / 2 + 0.5) / boxX;
+				int in = 0;
+				switch (shape) {
+					case ADDA_SHAPE_SPHERE: in = (xr * xr + yr * yr + zr * zr <= 0.25); break;
+					case ADDA_SHAPE_ELLIPSOID: in = (xr * xr + yr * yr * invsqY + zr * zr * invsqZ <= 0.25); break;
+					case ADDA_SHAPE_BOX: in = (fabs(yr) <= haspY && fabs(zr) <= haspZ); break;
+					default: return 0;
+				}
+				if (!in) continue;
+				if (position) {
+					position[3 * idx] = (uint16_t)i;
+					position[3 * idx + 1] = (uint16_t)j;
+					position[3 * idx + 2] = (uint16_t)k;
+				}
+				if (material) material[idx] = 0;
+				idx++;
+			}
+	return idx;
+}
+
+void adda_gb300_rotation(double alpha_deg, double beta_deg, double gamma_deg, double prop[3], double incPolY[3],
+	double incPolX[3])
+{
+	/* laboratory frame: prop_0=(0,0,1), incPolY_0=(0,1,0), incPolX_0=(1,0,0) (param.c:1988-1989, 2116-2119) */
+	const double d2r = TWO_PI_D / 360;
+	double a = alpha_deg * d2r, b = beta_deg * d2r, g = gamma_deg * d2r;
+	double ca = cos(a), sa = sin(a), cb = cos(b), sb = sin(b), cg = cos(g), sg = sin(g);
+	double m[3][3] = {
+		{ca * cb * cg - sa * sg, sa * cb * cg + ca * sg, -sb * cg},
+		{-ca * cb * sg - sa * cg, -sa * cb * sg + ca * cg, sb * sg},
+		{ca * sb, sa * sb, cb}};
+	for (int i = 0; i < 3; i++) {
+		prop[i] = m[i][2];
+		incPolY[i] = m[i][1];
+		incPolX[i] = m[i][0];
+	}
+}
+
+void adda_gb300_plane_wave(size_t ndip, const uint16_t *position, int boxX, int boxY, int boxZ, double gridspace,
+	double wavenum, const double prop[3], const double pol[3], double *einc)
+{
+	const double cX = (boxX - 1) / 2.0, cY = (boxY - 1) / 2.0, cZ = (boxZ - 1) / 2.0;
+	for (size_t i = 0; i < ndip; i++) {
+		double r0 = (position[3 * i] - cX) * gridspace;
+		double r1 = (position[3 * i + 1] - cY) * gridspace;
+		double r2 = (position[3 * i + 2] - cZ) * gridspace;
+		double ph = wavenum * (r0 * prop[0] + r1 * prop[1] + r2 * prop[2]);
+		double c = cos(ph), s = sin(ph);
+		for (int a = 0; a < 3; a++) {
+			einc[6 * i + 2 * a] = c * pol[a];
+			einc[6 * i + 2 * a + 1] = s * pol[a];
+		}
+	}
+}
+
+/* polCM, polM, polMplusRR, pol3coef: src/calculator.c:100-132 */
+static double complex pol_cm(double complex m, double dipvol)
+{
+	double complex m2 = m * m;
+	return (3 / FOUR_PI_D) * dipvol * (m2 - 1) / (m2 + 2);
+}
+
+static double complex pol_m(double complex M, double complex m, double dipvol)
+{
+	double complex cm = pol_cm(m, dipvol);
+	return cm / (1 - (cm / dipvol) * M);
+}
+
+static double complex pol_rr(double complex M, double complex m, double kd, double dipvol)
+{
+	return pol_m(M + I * 2 * kd * kd * kd / 3, m, dipvol);
+}
+
+int adda_gb300_polarizability(int relation, double m_re, double m_im, double kd, double gridspace,
+	const double prop[3], const double incPol[3], int avgpol, double cc[6])
+{
+	const double dipvol = gridspace * gridspace * gridspace;
+	const double complex m = m_re + I * m_im;
+	double complex r;
+	switch (relation) {
+		case ADDA_POL_CM: r = pol_cm(m, dipvol); break;
+		case ADDA_POL_RRC: r = pol_rr(0, m, kd, dipvol); break;
+		case ADDA_POL_DGF: r = pol_rr(1.6119919540164696407169668466385 * kd * kd, m, kd, dipvol); break;
+		case ADDA_POL_LDR: {
+			/* LDR coefficients b1,b2,b3 (const.h:234-236); S = sum_i prop_i^2 e_i^2, or its average */
+			const double b1 = 1.8915316, b2 = -0.1648469, b3 = 1.7700004;
+			double S;
+			if (avgpol) S = 0.5 * (1 - (prop[0] * prop[0] * prop[0] * prop[0] + prop[1] * prop[1] * prop[1] * prop[1]
+				+ prop[2] * prop[2] * prop[2] * prop[2]));
+			else S = prop[0] * prop[0] * incPol[0] * incPol[0] + prop[1] * prop[1] * incPol[1] * incPol[1]
+				+ prop[2] * prop[2] * incPol[2] * incPol[2];
+			r = pol_rr((b1 + (b2 + b3 * S) * m * m) * kd * kd, m, kd, dipvol);
+			break;
+		}
+		default: return ADDA_GB300_EINVAL;
+	}
+	for (int a = 0; a < 3; a++) {
+		cc[2 * a] = creal(r);
+		cc[2 * a + 1] = cimag(r);
+	}
+	return ADDA_GB300_OK;
+}
+
+int adda_gb300_fft_fit(int x, int divis)
+{
+	if (x < 1 || divis < 1) return ADDA_GB300_EINVAL;
+	for (;; x++) {
+		if (x % 2 || x % divis) continue;
+		int y = x;
+		while (y % 2 == 0) y /= 2;
+		while (y % 3 == 0) y /= 3;
+		while (y % 5 == 0) y /= 5;
+		while (y % 7 == 0) y /= 7;
+		if (y % 11 == 0) y /= 11;
+		else if (y % 13 == 0) y /= 13;
+		if (y == 1) return x;
+	}
+}

@@ -1,0 +1,152 @@
+/* adda_gb300.h - C ABI of the GB300-native DDA hot path (FFT-accelerated interaction matvec + Krylov solve).
+ *
+ * Plain C: pointers, sizes, status codes; no C++ or torch types. One context holds one particle lattice on one GPU
+ * (device-resident interaction matrix, work buffers and solver state for up to nrhs_max right-hand sides).
+ *
+ * Conventions shared with the reference (ADDA 1.3b6):
+ *   - complex vectors are interleaved (re,im) doubles, dipole-major [dipole][3], length 3*ndip complex per RHS
+ *     (the reference's doublecomplex argvec/resultvec, src/matvec.c:128); several RHS are stacked back to back;
+ *   - position[] holds (x,y,z) lattice indices of the non-void dipoles in the box, in the reference's order
+ *     (z outermost, x innermost; src/make_particle.c:1984); material[] indexes the per-material tables;
+ *   - cc are polarisabilities per material and component (the reference's cc[MAX_NMAT][3], src/vars.h); the
+ *     library takes their square roots itself (InitCC, src/calculator.c:266-289).
+ * Every entry point returns ADDA_GB300_OK (0) or a status code; adda_gb300_last_error() describes the last failure.
+ * Entry points are not reentrant on one context; different contexts may be used from different threads.
+ */
+#ifndef ADDA_GB300_H
+#define ADDA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes; negative = API/runtime error, positive = solver outcome (the reference's LogError/LogWarning cases) */
+#define ADDA_GB300_OK 0
+#define ADDA_GB300_EINVAL (-1)      /* bad argument (the reference's LogError on inconsistent input) */
+#define ADDA_GB300_ECUDA (-2)       /* CUDA runtime error or no usable GPU */
+#define ADDA_GB300_ENOMEM (-3)      /* device allocation failed */
+#define ADDA_GB300_ESTATE (-4)      /* call out of order (e.g. matvec before init_dmatrix) */
+#define ADDA_GB300_EBREAKDOWN 1     /* Krylov breakdown (iterative.c:684,697,960) */
+#define ADDA_GB300_ESTAGNATION 2    /* residual stagnated > mc iterations (iterative.c:1509) */
+#define ADDA_GB300_EMAXITER 3       /* maxiter reached without convergence (iterative.c:1507, a warning there) */
+
+enum adda_gb300_shape { ADDA_SHAPE_SPHERE = 0, ADDA_SHAPE_ELLIPSOID = 1, ADDA_SHAPE_BOX = 2 };
+enum adda_gb300_pol { ADDA_POL_LDR = 0, ADDA_POL_CM = 1, ADDA_POL_RRC = 2, ADDA_POL_DGF = 3 };
+enum adda_gb300_iter { ADDA_ITER_QMR_CS = 0, ADDA_ITER_BICGSTAB = 1 };
+/* arithmetic of a matvec / solve. FP64: everything in double. FP32: complex-float FFTs, D-matrix and vectors.
+ * MIXED (solve only): FP32 Krylov inner solves inside an FP64 iterative-refinement loop whose residual is
+ * recomputed with the FP64 matvec (the reference's ResidualNorm2, iterative.c:322-338). */
+enum adda_gb300_prec { ADDA_PREC_FP64 = 0, ADDA_PREC_FP32 = 1, ADDA_PREC_MIXED = 2 };
+enum adda_gb300_init_field { ADDA_IF_AUTO = 0, ADDA_IF_ZERO = 1, ADDA_IF_INC = 2 };
+
+typedef struct adda_gb300_ctx adda_gb300_ctx;
+
+/* The particle lattice: replaces the globals the reference sets in ParSetup/MakeParticle (comm.c:481-535,
+ * make_particle.c:2185-2230) and reads in InitDmatrix/MatVec. */
+typedef struct {
+	int boxX, boxY, boxZ;        /* computational box; boxX,boxY,boxZ >= 1 */
+	int gridX, gridY, gridZ;     /* padded FFT grid; 0 = fftFit(2*box) as ParSetup does (comm.c:489-491) */
+	size_t ndip;                 /* non-void dipoles */
+	const uint16_t *position;    /* [ndip][3], sorted z-major then y then x (the reference's order) */
+	const uint8_t *material;     /* [ndip] material index, or NULL (all 0) */
+	double gridspace;            /* lattice spacing d (lambda/dpl) */
+	double wavenum;              /* k = 2*pi/lambda */
+	int nrhs_max;                /* right-hand sides solved together (>=1) */
+	int device;                  /* CUDA device ordinal */
+} adda_gb300_problem;
+
+typedef struct {
+	int method;                  /* enum adda_gb300_iter (-iter) */
+	int precision;               /* ADDA_PREC_FP64 or ADDA_PREC_MIXED */
+	double eps;                  /* relative residual target (-eps e => 10^-e) */
+	int maxiter;                 /* -maxiter */
+	int init_field;              /* enum adda_gb300_init_field (-init_field) */
+	int check_every;             /* iterations between host convergence checks (CUDA graph length); 0 = default */
+	double inner_eps;            /* MIXED: relative tolerance of each FP32 inner solve; 0 = default */
+	int max_refine;              /* MIXED: maximum outer refinement steps; 0 = default */
+} adda_gb300_solve_params;
+
+typedef struct {
+	int niter;                   /* Krylov iterations (reference: IterativeSolver's return value) */
+	int status;                  /* ADDA_GB300_OK or solver outcome code */
+	double resid;                /* final relative residual; MIXED: the FP64 recomputed one */
+	int refinements;             /* MIXED: outer steps; FP64: 0 */
+	int matvecs_fp64, matvecs_fp32;
+} adda_gb300_rhs_stats;
+
+/* ---- particle-side inputs (host code, no GPU) --------------------------------------------------------------- */
+
+/* fftFit, src/fft.c:528-562: smallest even size >= x, divisible by divis, with prime factors 2,3,5,7 (+ one 11|13) */
+int adda_gb300_fft_fit(int x, int divis);
+/* boxY/boxZ from boxX and the shape's aspect ratios: InitShape sizing, src/make_particle.c:1283-1308,1912-1919.
+ * pars: ellipsoid/box aspect ratios (y/x, z/x), or NULL for a sphere/cube. */
+int adda_gb300_fit_box(int shape, const double *pars, int boxX, int *boxY, int *boxZ);
+/* MakeParticle's box loop, src/make_particle.c:1984-2230. Returns ndip; position/material may be NULL to count. */
+size_t adda_gb300_make_particle(int shape, const double *pars, int boxX, int boxY, int boxZ, uint16_t *position,
+	uint8_t *material);
+/* InitRotation, src/crosssec.c:82-139 (zyz Euler angles in degrees): propagation and the two polarisations */
+void adda_gb300_rotation(double alpha_deg, double beta_deg, double gamma_deg, double prop[3], double incPolY[3],
+	double incPolX[3]);
+/* GenerateB, free-space plane wave, src/GenerateB.c:324-328: einc[i] = pol * exp(i k r_i.prop) */
+void adda_gb300_plane_wave(size_t ndip, const uint16_t *position, int boxX, int boxY, int boxZ, double gridspace,
+	double wavenum, const double prop[3], const double pol[3], double *einc);
+/* CoupleConstant, src/calculator.c:170-262 (CM, RRC, DGF, LDR [avgpol]); cc = 3 identical complex values */
+int adda_gb300_polarizability(int relation, double m_re, double m_im, double kd, double gridspace,
+	const double prop[3], const double incPol[3], int avgpol, double cc[6]);
+
+/* ---- device context ------------------------------------------------------------------------------------------ */
+
+/* ParSetup + allocation half of InitDmatrix (comm.c:481-535, fft.c:1164-1209): validates the lattice, uploads it
+ * and allocates every device buffer. Fails with ADDA_GB300_ECUDA when no GPU is usable. */
+int adda_gb300_create(const adda_gb300_problem *p, adda_gb300_ctx **out);
+/* Free_FFT_Dmat, src/fft.c:1420-1493 */
+int adda_gb300_destroy(adda_gb300_ctx *ctx);
+/* grid actually used (after fftFit) */
+int adda_gb300_get_grid(const adda_gb300_ctx *ctx, int grid[3]);
+
+/* InitDmatrix, src/fft.c:918-1416: Green's tensor (point dipoles, interaction.c:290-331) and its FFT, computed in
+ * FP64 on the GPU, kept in the reduced (y<=gY/2, z<=gZ/2) layout plus an FP32 copy. */
+int adda_gb300_init_dmatrix(adda_gb300_ctx *ctx);
+/* copy the FP64 D matrix to the host: layout [x][z<gZ/2+1][y<gY/2+1][6] complex (fft.c:144-150) */
+size_t adda_gb300_dmatrix_len(const adda_gb300_ctx *ctx);
+int adda_gb300_get_dmatrix(adda_gb300_ctx *ctx, double *out);
+
+/* InitCC, src/calculator.c:266-289, for right-hand side rhs: cc per material [nmat][3] complex */
+int adda_gb300_set_cc(adda_gb300_ctx *ctx, int rhs, int nmat, const double *cc);
+/* per-dipole polarisabilities [ndip][3] complex for right-hand side rhs (inhomogeneous media) */
+int adda_gb300_set_cc_dipole(adda_gb300_ctx *ctx, int rhs, const double *cc);
+
+/* MatVec, src/matvec.c:128-425, for nrhs stacked vectors in HOST memory: resultvec = argvec + S.D.S.argvec,
+ * S = diag(sqrt(cc)); her != 0 applies the Hermitian transpose; inprod (may be NULL) receives |resultvec_r|^2 per
+ * RHS. prec = ADDA_PREC_FP64 or ADDA_PREC_FP32 (the FP32 path rounds the inputs to complex float). */
+int adda_gb300_matvec(adda_gb300_ctx *ctx, int prec, int nrhs, const double *argvec, double *resultvec,
+	double *inprod, int her);
+/* same, on DEVICE buffers (double2 for FP64, float2 for FP32) on the context's stream; no host synchronisation */
+int adda_gb300_matvec_device(adda_gb300_ctx *ctx, int prec, int nrhs, const void *d_argvec, void *d_resultvec,
+	double *d_inprod, int her);
+
+/* IterativeSolver, src/iterative.c:1398-1530, for nrhs right-hand sides at once. einc: incident fields
+ * [nrhs][ndip][3] (host). On return xvec (may be NULL) holds the solution x and pvec (may be NULL) the polarisations
+ * S.x; both also stay on the device for adda_gb300_cross_sections. stats: one entry per RHS (may be NULL).
+ * resid_hist (may be NULL): [nrhs][hist_cap] relative residuals RE_000, RE_001, ... (iterative.c:69,301). */
+int adda_gb300_solve(adda_gb300_ctx *ctx, const adda_gb300_solve_params *sp, int nrhs, const double *einc,
+	double *xvec, double *pvec, adda_gb300_rhs_stats *stats, double *resid_hist, int hist_cap);
+
+/* ExtCross (plane wave) and AbsCross (Draine), src/crosssec.c:811-917, in FP64 on the device from the
+ * polarisations left by the last solve: prop/incpol per RHS [nrhs][3]; cext/cabs per RHS. */
+int adda_gb300_cross_sections(adda_gb300_ctx *ctx, int nrhs, const double *prop, const double *incpol,
+	double *cext, double *cabs);
+
+/* last error message of the calling thread */
+const char *adda_gb300_last_error(void);
+/* number of kernels this library has launched in the calling process (for launch accounting) */
+uint64_t adda_gb300_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,593 @@
+/* adda_oracle.c - CPU restatement of ADDA's FFT-accelerated DDA matvec, D-matrix, Krylov solvers and cross sections.
+ *
+ * TEST INFRASTRUCTURE (oracle): the checker for the GPU product and the timed CPU baseline, nothing else. Every
+ * function names the reference code it restates (ADDA 1.3b6, paths relative to the reference project). The data
+ * layouts follow the reference's own where the reference fixes them (the reduced D layout of fft.c:144-150); the
+ * rest is organised for clarity and OpenMP parallelism.
+ */
+#include "adda_oracle.h"
+#include "cfft.h"
+
+#include <complex.h>
+#include <math.h>
+#include <omp.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef double complex cplx;
+
+#define OR_MAXMAT 256
+
+struct or_ctx {
+	int bX, bY, bZ, gX, gY, gZ;
+	size_t n;            // number of non-void dipoles
+	uint16_t *pos;       // [n][3] grid coordinates
+	uint8_t *mat;        // [n] material index
+	double gridspace, k;
+	size_t DsY, DsZ;     // reduced D sizes (fft.c:955-963)
+	cplx *D;             // [gX][DsZ][DsY][6]
+	int per_dip, nmat;
+	cplx cc[OR_MAXMAT][3], ccs[OR_MAXMAT][3];
+	cplx *ccd, *ccsd;    // per-dipole [n][3] (cc and its root)
+	cfft_plan px, py, pz;
+	cplx *X;             // expanded grid after the X transform: [3][bZ][bY][gX]
+	int nthreads;
+};
+
+/* fftFit, src/fft.c:528-562 (FFTW3 branch, weird_nprocs=false): smallest even x' >= x divisible by divis whose prime
+ * factors are 2,3,5,7 and at most one factor of 11 or 13 */
+int or_fftfit(int x, int divis)
+{
+	for (;; x++) {
+		if (x % 2 || x % divis) continue;
+		int y = x;
+		while (y % 2 == 0) y /= 2;
+		while (y % 3 == 0) y /= 3;
+		while (y % 5 == 0) y /= 5;
+		while (y % 7 == 0) y /= 7;
+		if (y % 11 == 0) y /= 11;
+		else if (y % 13 == 0) y /= 13;
+		if (y == 1) return x;
+	}
+}
+
+or_ctx *or_create(int bX, int bY, int bZ, int gX, int gY, int gZ, size_t n, const uint16_t *position,
+	const uint8_t *material, double gridspace, double wavenum, int nthreads)
+{
+	or_ctx *c = calloc(1, sizeof(*c));
+	c->bX = bX; c->bY = bY; c->bZ = bZ;
+	c->gX = gX; c->gY = gY; c->gZ = gZ;
+	c->n = n;
+	c->pos = malloc(sizeof(uint16_t) * 3 * n);
+	c->mat = malloc(n ? n : 1);
+	memcpy(c->pos, position, sizeof(uint16_t) * 3 * n);
+	if (material) memcpy(c->mat, material, n);
+	else memset(c->mat, 0, n);
+	c->gridspace = gridspace;
+	c->k = wavenum;
+	c->nthreads = nthreads > 0 ? nthreads : omp_get_max_threads();
+	cfft_plan_init(&c->px, gX);
+	cfft_plan_init(&c->py, gY);
+	cfft_plan_init(&c->pz, gZ);
+	c->X = malloc(sizeof(cplx) * 3 * (size_t)bZ * bY * gX);
+	return c;
+}
+
+void or_free(or_ctx *c)
+{
+	if (!c) return;
+	cfft_plan_free(&c->px);
+	cfft_plan_free(&c->py);
+	cfft_plan_free(&c->pz);
+	free(c->pos); free(c->mat); free(c->D); free(c->X); free(c->ccd); free(c->ccsd);
+	free(c);
+}
+
+/* Point-dipole Green's tensor for integer offset (i,j,k) in units of the lattice spacing:
+ * InterParams + InterTerm_core + InterTerm_poi, src/interaction.c:159-181, 290-331 (non-SSE3 branch).
+ * Component order xx,xy,xz,yy,yz,zz. */
+static void green_poi(const or_ctx *c, int i, int j, int k, cplx g[6])
+{
+	double q[3] = {i, j, k};
+	double rn = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+	double invrn = 1.0 / rn;
+	for (int a = 0; a < 3; a++) q[a] *= invrn;
+	double rr = rn * c->gridspace;
+	double invr3 = 1 / (rr * rr * rr);
+	double kr = c->k * rr, kr2 = kr * kr;
+	double qm[6] = {q[0] * q[0], q[0] * q[1], q[0] * q[2], q[1] * q[1], q[1] * q[2], q[2] * q[2]};
+	double t1 = 3 - kr2, t2 = -3 * kr, t3 = kr2 - 1;
+	cplx ev = invr3 * (cos(kr) + I * sin(kr));
+	for (int a = 0; a < 6; a++) {
+		if (a == 0 || a == 3 || a == 5) g[a] = ((t1 * qm[a] + t3) + I * (kr + t2 * qm[a])) * ev;
+		else g[a] = (t1 + I * t2) * qm[a] * ev;
+	}
+}
+
+size_t or_dmatrix_len(const or_ctx *c)
+{
+	return (size_t)c->gX * c->DsZ * c->DsY * 6;
+}
+
+/* InitDmatrix, src/fft.c:918-1322 (sequential, reduced_FFT): D = -FFT(G)/Ngrid, stored for y<=gY/2, z<=gZ/2 only;
+ * the remaining octants follow from the reflection symmetries of G (components xy,yz odd in y; xz,yz odd in z). */
+void or_init_dmatrix(or_ctx *c)
+{
+	const int bX = c->bX, bY = c->bY, bZ = c->bZ, gX = c->gX, gY = c->gY, gZ = c->gZ;
+	c->DsY = gY / 2 + 1;
+	c->DsZ = gZ / 2 + 1;
+	free(c->D);
+	c->D = calloc(or_dmatrix_len(c), sizeof(cplx));
+	const double invN = 1.0 / (gX * ((double)gY * gZ));
+	const size_t lines = (size_t)bZ * bY;
+	cplx *G = calloc(6 * lines * gX, sizeof(cplx)); // [comp][k][j][x mod gX]
+	#pragma omp parallel for num_threads(c->nthreads) schedule(dynamic)
+	for (int k = 0; k < bZ; k++)
+		for (int j = 0; j < bY; j++)
+			for (int i = 1 - bX; i < bX; i++) {
+				if (!i && !j && !k) continue;
+				cplx g[6];
+				green_poi(c, i, j, k, g);
+				size_t idx = ((size_t)k * bY + j) * gX + (i < 0 ? i + gX : i);
+				for (int a = 0; a < 6; a++) G[a * lines * gX + idx] = g[a];
+			}
+	for (int a = 0; a < 6; a++) {
+		cplx *Ga = G + a * lines * gX;
+		const double sy = (a == 1 || a == 4) ? -1 : 1, sz = (a == 2 || a == 4) ? -1 : 1;
+		#pragma omp parallel num_threads(c->nthreads)
+		{
+			cplx *work = malloc(sizeof(cplx) * (gX > gY ? (gX > gZ ? gX : gZ) : (gY > gZ ? gY : gZ)));
+			cplx *s = malloc(sizeof(cplx) * (size_t)gY * gZ); // [y][z]
+			#pragma omp for
+			for (size_t l = 0; l < lines; l++) cfft_exec(&c->px, Ga + l * gX, work, -1);
+			#pragma omp for
+			for (int x = 0; x < gX; x++) {
+				memset(s, 0, sizeof(cplx) * (size_t)gY * gZ);
+				for (int j = 0; j < bY; j++)
+					for (int k = 0; k < bZ; k++) s[(size_t)j * gZ + k] = Ga[((size_t)k * bY + j) * gX + x];
+				for (int j = 1; j < bY; j++) // mirror along y (fft.c:1276-1282)
+					for (int k = 0; k < bZ; k++) s[(size_t)(gY - j) * gZ + k] = sy * s[(size_t)j * gZ + k];
+				for (int j = 1 - bY; j < bY; j++) { // mirror along z (fft.c:1283-1289)
+					size_t row = (size_t)(j < 0 ? j + gY : j) * gZ;
+					for (int k = 1; k < bZ; k++) s[row + gZ - k] = sz * s[row + k];
+				}
+				for (int y = 0; y < gY; y++) cfft_exec(&c->pz, s + (size_t)y * gZ, work, -1);
+				cfft_exec_strided(&c->py, s, gZ, 1, (size_t)gZ, -1);
+				for (size_t z = 0; z < c->DsZ; z++)
+					for (size_t y = 0; y < c->DsY; y++)
+						c->D[(((size_t)x * c->DsZ + z) * c->DsY + y) * 6 + a] = -invN * s[y * gZ + z];
+			}
+			free(work);
+			free(s);
+		}
+	}
+	free(G);
+}
+
+void or_get_dmatrix(const or_ctx *c, double *out)
+{
+	memcpy(out, c->D, sizeof(cplx) * or_dmatrix_len(c));
+}
+
+/* InitCC, src/calculator.c:266-289: cc_sqrt = csqrt(cc) */
+void or_set_cc_mat(or_ctx *c, int nmat, const double *cc)
+{
+	const cplx *in = (const cplx *)cc;
+	c->per_dip = 0;
+	c->nmat = nmat;
+	for (int m = 0; m < nmat && m < OR_MAXMAT; m++)
+		for (int a = 0; a < 3; a++) {
+			c->cc[m][a] = in[3 * m + a];
+			c->ccs[m][a] = csqrt(in[3 * m + a]);
+		}
+}
+
+void or_set_cc_dip(or_ctx *c, const double *cc)
+{
+	const cplx *in = (const cplx *)cc;
+	c->per_dip = 1;
+	free(c->ccd); free(c->ccsd);
+	c->ccd = malloc(sizeof(cplx) * 3 * c->n);
+	c->ccsd = malloc(sizeof(cplx) * 3 * c->n);
+	for (size_t i = 0; i < 3 * c->n; i++) {
+		c->ccd[i] = in[i];
+		c->ccsd[i] = csqrt(in[i]);
+	}
+}
+
+static inline cplx ccs_of(const or_ctx *c, size_t i, int a)
+{
+	return c->per_dip ? c->ccsd[3 * i + a] : c->ccs[c->mat[i]][a];
+}
+
+static inline cplx cc_of(const or_ctx *c, size_t i, int a)
+{
+	return c->per_dip ? c->ccd[3 * i + a] : c->cc[c->mat[i]][a];
+}
+
+/* MatVec, src/matvec.c:128-425 (FFT mode, sequential): y = x + S.D.S.x with S = diag(cc_sqrt); her => A^H via
+ * conjugation of input and output. inprod (if not NULL) receives |y|^2. */
+void or_matvec(or_ctx *c, const double *argv, double *resv, double *inprod, int her)
+{
+	const cplx *arg = (const cplx *)argv;
+	cplx *res = (cplx *)resv;
+	const int bY = c->bY, bZ = c->bZ, gX = c->gX, gY = c->gY, gZ = c->gZ;
+	const size_t plane = (size_t)bZ * bY * gX;
+	const size_t DsY = c->DsY, DsZ = c->DsZ;
+	cplx *X = c->X;
+	memset(X, 0, sizeof(cplx) * 3 * plane);
+	// scatter S.x onto the expanded grid (matvec.c:205-212)
+	for (size_t i = 0; i < c->n; i++) {
+		size_t idx = ((size_t)c->pos[3 * i + 2] * bY + c->pos[3 * i + 1]) * gX + c->pos[3 * i];
+		for (int a = 0; a < 3; a++) {
+			cplx v = arg[3 * i + a];
+			if (her) v = conj(v);
+			X[a * plane + idx] = ccs_of(c, i, a) * v;
+		}
+	}
+	#pragma omp parallel num_threads(c->nthreads)
+	{
+		int gmax = gX > gY ? (gX > gZ ? gX : gZ) : (gY > gZ ? gY : gZ);
+		cplx *work = malloc(sizeof(cplx) * gmax);
+		cplx *col = malloc(sizeof(cplx) * 3 * gY);
+		cplx *s = malloc(sizeof(cplx) * 3 * (size_t)gY * gZ); // [comp][y][z]
+		#pragma omp for
+		for (size_t l = 0; l < 3 * (size_t)bZ * bY; l++) cfft_exec(&c->px, X + l * gX, work, -1);
+		#pragma omp for schedule(dynamic)
+		for (int x = 0; x < gX; x++) {
+			memset(s, 0, sizeof(cplx) * 3 * (size_t)gY * gZ);
+			for (int a = 0; a < 3; a++)
+				for (int y = 0; y < bY; y++)
+					for (int z = 0; z < bZ; z++)
+						s[((size_t)a * gY + y) * gZ + z] = X[a * plane + ((size_t)z * bY + y) * gX + x];
+			for (int a = 0; a < 3; a++)
+				for (int y = 0; y < bY; y++) cfft_exec(&c->pz, s + ((size_t)a * gY + y) * gZ, work, -1);
+			for (int z = 0; z < gZ; z++) {
+				for (int a = 0; a < 3; a++) {
+					cplx *ln = col + a * gY;
+					for (int y = 0; y < gY; y++) ln[y] = s[((size_t)a * gY + y) * gZ + z];
+					cfft_exec(&c->py, ln, work, -1);
+				}
+				// D~.X~ with the reduced-FFT sign flips (matvec.c:271-305)
+				for (int y = 0; y < gY; y++) {
+					size_t yy = (size_t)y < DsY ? (size_t)y : (size_t)(gY - y);
+					size_t zz = (size_t)z < DsZ ? (size_t)z : (size_t)(gZ - z);
+					const cplx *f = c->D + (((size_t)x * DsZ + zz) * DsY + yy) * 6;
+					cplx m[6] = {f[0], f[1], f[2], f[3], f[4], f[5]};
+					if ((size_t)y >= DsY) {
+						m[1] = -m[1];
+						if ((size_t)z >= DsZ) m[2] = -m[2];
+						else m[4] = -m[4];
+					}
+					else if ((size_t)z >= DsZ) {
+						m[2] = -m[2];
+						m[4] = -m[4];
+					}
+					cplx v0 = col[y], v1 = col[gY + y], v2 = col[2 * gY + y];
+					col[y] = m[0] * v0 + m[1] * v1 + m[2] * v2;
+					col[gY + y] = m[1] * v0 + m[3] * v1 + m[4] * v2;
+					col[2 * gY + y] = m[2] * v0 + m[4] * v1 + m[5] * v2;
+				}
+				for (int a = 0; a < 3; a++) {
+					cplx *ln = col + a * gY;
+					cfft_exec(&c->py, ln, work, 1);
+					for (int y = 0; y < bY; y++) s[((size_t)a * gY + y) * gZ + z] = ln[y];
+				}
+			}
+			for (int a = 0; a < 3; a++)
+				for (int y = 0; y < bY; y++) cfft_exec(&c->pz, s + ((size_t)a * gY + y) * gZ, work, 1);
+			for (int a = 0; a < 3; a++)
+				for (int y = 0; y < bY; y++)
+					for (int z = 0; z < bZ; z++)
+						X[a * plane + ((size_t)z * bY + y) * gX + x] = s[((size_t)a * gY + y) * gZ + z];
+		}
+		#pragma omp for
+		for (size_t l = 0; l < 3 * (size_t)bZ * bY; l++) cfft_exec(&c->px, X + l * gX, work, 1);
+		free(work); free(col); free(s);
+	}
+	// gather y = x + S.X (matvec.c:352-364)
+	double sum = 0;
+	for (size_t i = 0; i < c->n; i++) {
+		size_t idx = ((size_t)c->pos[3 * i + 2] * bY + c->pos[3 * i + 1]) * gX + c->pos[3 * i];
+		for (int a = 0; a < 3; a++) {
+			cplx v = arg[3 * i + a];
+			if (her) v = conj(v);
+			cplx r = v + ccs_of(c, i, a) * X[a * plane + idx];
+			sum += creal(r) * creal(r) + cimag(r) * cimag(r);
+			res[3 * i + a] = her ? conj(r) : r;
+		}
+	}
+	if (inprod) *inprod = sum;
+}
+
+/* ---------------- BLAS-1 restated from src/linalg.c ---------------- */
+
+static double nnorm2(const cplx *a, size_t n)
+{
+	double s = 0;
+	for (size_t i = 0; i < n; i++) s += creal(a[i]) * creal(a[i]) + cimag(a[i]) * cimag(a[i]);
+	return s;
+}
+
+static cplx ndot(const cplx *a, const cplx *b, size_t n) // sum a*conj(b), linalg.c:75-88
+{
+	cplx s = 0;
+	for (size_t i = 0; i < n; i++) s += a[i] * conj(b[i]);
+	return s;
+}
+
+static cplx ndot_conj(const cplx *a, const cplx *b, size_t n) // sum a*b, linalg.c:92-105
+{
+	cplx s = 0;
+	for (size_t i = 0; i < n; i++) s += a[i] * b[i];
+	return s;
+}
+
+/* ---------------- iterative solvers, src/iterative.c ---------------- */
+
+typedef struct {
+	or_ctx *c;
+	size_t n;                 // 3*N
+	cplx *x, *r, *p, *Av, *v1, *v2, *v3;
+	double inprodR, inprodRp1, epsB;
+	int niter, counter, matvec_ready, complete;
+} solver;
+
+static void mv(solver *s, const cplx *in, cplx *out, double *ipr)
+{
+	or_matvec(s->c, (const double *)in, (double *)out, ipr, 0);
+}
+
+/* QMR_CS, src/iterative.c:898-1032 (Freund 1992). Returns OR_OK or OR_EBREAKDOWN. */
+typedef struct {
+	double c_old, c_new, om_old, om_new;
+	cplx beta, tautilda, s_old, s_new;
+	cplx *v, *vt, *pn, *po;
+} qmr_state;
+
+static void qmr_init(solver *s, qmr_state *q)
+{
+	const size_t n = s->n;
+	q->v = s->v1; q->vt = s->v2; q->pn = s->p; q->po = s->v3;
+	q->om_old = 0.0;
+	q->beta = csqrt(ndot_conj(s->r, s->r, n));
+	q->om_new = sqrt(s->inprodR) / cabs(q->beta);
+	cplx t = 1 / q->beta;
+	for (size_t i = 0; i < n; i++) q->v[i] = t * s->r[i];
+	q->tautilda = q->om_new * q->beta;
+	q->c_new = q->c_old = 1.0;
+	q->s_new = q->s_old = 0.0;
+}
+
+static int qmr_iter(solver *s, qmr_state *q)
+{
+	const size_t n = s->n;
+	if (1 / (q->om_new * q->om_new) < 1e-10) return OR_EBREAKDOWN;
+	if (s->niter == 1 && s->matvec_ready) {
+		cplx t = 1 / q->beta;
+		for (size_t i = 0; i < n; i++) s->Av[i] *= t;
+	}
+	else mv(s, q->v, s->Av, NULL);
+	cplx alpha = ndot_conj(q->v, s->Av, n);
+	cplx ma = -alpha;
+	if (s->niter == 1) for (size_t i = 0; i < n; i++) q->vt[i] = ma * q->v[i] + s->Av[i];
+	else {
+		cplx mb = -q->beta;
+		for (size_t i = 0; i < n; i++) q->vt[i] = mb * q->vt[i] + ma * q->v[i] + s->Av[i];
+	}
+	cplx theta = conj(q->s_old) * q->om_old * q->beta;
+	cplx eta = q->c_old * q->c_new * q->om_old * q->beta;
+	eta += alpha * conj(q->s_new) * q->om_new;
+	cplx zetat = q->c_new * q->om_new * alpha - q->s_new * q->c_old * q->om_old * q->beta;
+	q->om_old = q->om_new;
+	double b0 = 0, b1 = 0, b2 = 0; // nDotProdSelf_conj_Norm2, linalg.c:127-145
+	for (size_t i = 0; i < n; i++) {
+		b0 += creal(q->vt[i]) * creal(q->vt[i]);
+		b1 += cimag(q->vt[i]) * cimag(q->vt[i]);
+		b2 += creal(q->vt[i]) * cimag(q->vt[i]);
+	}
+	double nrm = b0 + b1;
+	q->beta = csqrt(b0 - b1 + I * 2 * b2);
+	q->om_new = sqrt(nrm) / cabs(q->beta);
+	double zt2 = creal(zetat) * creal(zetat) + cimag(zetat) * cimag(zetat);
+	double zabs = sqrt(zt2 + nrm);
+	double zt = sqrt(zt2);
+	cplx zeta = (zt < 1e-40) ? (cplx)zabs : (zabs / zt) * zetat;
+	q->c_old = q->c_new;
+	q->c_new = zt / zabs;
+	q->s_old = q->s_new;
+	q->s_new = q->om_new * q->beta / zeta;
+	cplx t4 = 1 / zeta;
+	if (s->niter == 1) for (size_t i = 0; i < n; i++) q->pn[i] = t4 * q->v[i];
+	else {
+		cplx t2 = -eta * t4;
+		if (s->niter == 2) for (size_t i = 0; i < n; i++) q->po[i] = t2 * q->pn[i] + t4 * q->v[i];
+		else {
+			cplx t1 = -theta * t4;
+			for (size_t i = 0; i < n; i++) q->po[i] = t1 * q->po[i] + t2 * q->pn[i] + t4 * q->v[i];
+		}
+		cplx *tmp = q->po; q->po = q->pn; q->pn = tmp;
+	}
+	cplx tau = q->c_new * q->tautilda;
+	q->tautilda = -q->s_new * q->tautilda;
+	for (size_t i = 0; i < n; i++) s->x[i] += tau * q->pn[i];
+	cplx ib = 1 / q->beta;
+	for (size_t i = 0; i < n; i++) q->vt[i] *= ib;
+	cplx *tmp = q->v; q->v = q->vt; q->vt = tmp;
+	double sa2 = creal(q->s_new) * creal(q->s_new) + cimag(q->s_new) * cimag(q->s_new);
+	cplx t1 = (q->c_new / q->om_new) * q->tautilda;
+	double sum = 0;
+	for (size_t i = 0; i < n; i++) {
+		s->r[i] = sa2 * s->r[i] + t1 * q->v[i];
+		sum += creal(s->r[i]) * creal(s->r[i]) + cimag(s->r[i]) * cimag(s->r[i]);
+	}
+	s->inprodRp1 = sum;
+	return OR_OK;
+}
+
+/* BiCGStab, src/iterative.c:640-724 */
+typedef struct {
+	cplx ro_old, omega, alpha;
+	cplx *v, *sv, *rt;
+} bcgs_state;
+
+static int bcgs_iter(solver *s, bcgs_state *b)
+{
+	const size_t n = s->n;
+	cplx ro_new = ndot(s->r, b->rt, n);
+	if (s->niter == 1) memcpy(s->p, s->r, sizeof(cplx) * n);
+	else {
+		cplx t1 = ro_new * b->alpha, t2 = b->ro_old * b->omega;
+		if (cabs(t2) / cabs(t1) < 1e-10) return OR_EBREAKDOWN;
+		cplx beta = t1 / t2;
+		cplx mbo = -beta * b->omega;
+		for (size_t i = 0; i < n; i++) s->p[i] = beta * s->p[i] + mbo * b->v[i] + s->r[i];
+	}
+	if (s->niter == 1 && s->matvec_ready) memcpy(b->v, s->Av, sizeof(cplx) * n);
+	else mv(s, s->p, b->v, NULL);
+	cplx t1 = ndot(b->v, b->rt, n);
+	if (cabs(t1) / cabs(ro_new) < 1e-10) return OR_EBREAKDOWN;
+	b->alpha = ro_new / t1;
+	cplx ma = -b->alpha;
+	double sum = 0;
+	for (size_t i = 0; i < n; i++) {
+		b->sv[i] = ma * b->v[i] + s->r[i];
+		sum += creal(b->sv[i]) * creal(b->sv[i]) + cimag(b->sv[i]) * cimag(b->sv[i]);
+	}
+	s->inprodRp1 = sum;
+	if (s->inprodRp1 < s->epsB) {
+		for (size_t i = 0; i < n; i++) s->x[i] += b->alpha * s->p[i];
+		s->complete = 0;
+	}
+	else {
+		double den;
+		mv(s, b->sv, s->Av, &den);
+		b->omega = ndot(b->sv, s->Av, n) / den;
+		for (size_t i = 0; i < n; i++) s->x[i] += b->alpha * s->p[i] + b->omega * b->sv[i];
+		cplx mo = -b->omega;
+		sum = 0;
+		for (size_t i = 0; i < n; i++) {
+			s->r[i] = mo * s->Av[i] + b->sv[i];
+			sum += creal(s->r[i]) * creal(s->r[i]) + cimag(s->r[i]) * cimag(s->r[i]);
+		}
+		s->inprodRp1 = sum;
+		b->ro_old = ro_new;
+	}
+	return OR_OK;
+}
+
+/* IterativeSolver, src/iterative.c:1398-1530 with CalcInitField (:1342-1394) and ProgressReport (:282-318).
+ * einc: incident field [N][3]; xvec receives x, pvec the polarisations S.x; resid_hist[0..] the relative residuals
+ * RE_000, RE_001, ... (at most hist_cap values). Returns a status code; *niter_out = iterations performed. */
+int or_solve(or_ctx *c, int method, const double *einc, double eps, int maxiter, int init_field,
+	double *xvec, double *pvec, double *resid_hist, int hist_cap, int *niter_out)
+{
+	solver S;
+	memset(&S, 0, sizeof(S));
+	S.c = c;
+	S.n = 3 * c->n;
+	const size_t n = S.n;
+	const cplx *E = (const cplx *)einc;
+	S.x = (cplx *)xvec;
+	cplx *b = (cplx *)pvec;
+	S.r = malloc(sizeof(cplx) * n);
+	S.p = malloc(sizeof(cplx) * n);
+	S.Av = malloc(sizeof(cplx) * n);
+	S.v1 = malloc(sizeof(cplx) * n);
+	S.v2 = malloc(sizeof(cplx) * n);
+	S.v3 = malloc(sizeof(cplx) * n);
+	// b = S.Einc (nMult_mat)
+	for (size_t i = 0; i < c->n; i++)
+		for (int a = 0; a < 3; a++) b[3 * i + a] = ccs_of(c, i, a) * E[3 * i + a];
+	double temp = nnorm2(b, n);
+	double resid_scale = 1 / temp;
+	S.epsB = eps * eps * temp;
+	if (init_field == OR_IF_ZERO) {
+		memset(S.x, 0, sizeof(cplx) * n);
+		memcpy(S.r, b, sizeof(cplx) * n);
+		S.inprodR = temp;
+	}
+	else {
+		mv(&S, b, S.Av, NULL);
+		double ip = 0;
+		for (size_t i = 0; i < n; i++) {
+			S.r[i] = b[i] - S.Av[i];
+			ip += creal(S.r[i]) * creal(S.r[i]) + cimag(S.r[i]) * cimag(S.r[i]);
+		}
+		S.inprodR = ip;
+		if (init_field == OR_IF_AUTO && temp < S.inprodR) {
+			memset(S.x, 0, sizeof(cplx) * n);
+			memcpy(S.r, b, sizeof(cplx) * n);
+			S.inprodR = temp;
+			S.matvec_ready = 1;
+		}
+		else memcpy(S.x, b, sizeof(cplx) * n);
+	}
+	int nh = 0;
+	if (nh < hist_cap) resid_hist[nh++] = sqrt(resid_scale * S.inprodR);
+	S.niter = 1;
+	S.counter = 0;
+	const int mc = 50000; // QMR_CS and BiCGStab stagnation limits are 50000 and 30000 (iterative.c:118-125)
+	const int mcm = (method == OR_BICGSTAB) ? 30000 : mc;
+	qmr_state q;
+	bcgs_state bs;
+	if (method == OR_QMR_CS) qmr_init(&S, &q);
+	else {
+		bs.v = S.v1; bs.sv = S.v2; bs.rt = S.v3;
+		memcpy(bs.rt, S.r, sizeof(cplx) * n);
+	}
+	int status = OR_OK;
+	while (S.inprodR > S.epsB && S.niter <= maxiter && S.counter <= mcm) {
+		S.complete = 1;
+		status = (method == OR_QMR_CS) ? qmr_iter(&S, &q) : bcgs_iter(&S, &bs);
+		if (status != OR_OK) break;
+		if (S.inprodRp1 <= S.inprodR) {
+			S.inprodR = S.inprodRp1;
+			S.counter = 0;
+		}
+		else S.counter++;
+		if (nh < hist_cap) resid_hist[nh++] = sqrt(resid_scale * S.inprodRp1);
+		S.niter++;
+	}
+	if (status == OR_OK && S.inprodR > S.epsB) status = (S.niter > maxiter) ? OR_EMAXITER : OR_ESTAGNATION;
+	for (size_t i = 0; i < c->n; i++)
+		for (int a = 0; a < 3; a++) b[3 * i + a] = ccs_of(c, i, a) * S.x[3 * i + a];
+	if (niter_out) *niter_out = S.niter - 1;
+	free(S.r); free(S.p); free(S.Av); free(S.v1); free(S.v2); free(S.v3);
+	return status;
+}
+
+/* ExtCross (plane wave, free space) via CalcFieldFree, src/crosssec.c:506-596, 811-822; AbsCross (Draine),
+ * src/crosssec.c:852-917. Positions are taken relative to the first dipole of the box, whose centre is at
+ * box_origin = -gridspace*((boxX-1)/2, (boxY-1)/2, (boxZ-1)/2) (make_particle.c:2305-2308). */
+void or_cross(or_ctx *c, const double *pvec, const double prop[3], const double incpol[3], double *cext,
+	double *cabs)
+{
+	const cplx *P = (const cplx *)pvec;
+	const double kd = c->k * c->gridspace;
+	cplx sum[3] = {0, 0, 0};
+	for (size_t j = 0; j < c->n; j++) {
+		double ph = -kd * (prop[0] * c->pos[3 * j] + prop[1] * c->pos[3 * j + 1] + prop[2] * c->pos[3 * j + 2]);
+		cplx a = cos(ph) + I * sin(ph);
+		for (int i = 0; i < 3; i++) sum[i] += P[3 * j + i] * a;
+	}
+	cplx dpr = sum[0] * prop[0] + sum[1] * prop[1] + sum[2] * prop[2];
+	cplx tb[3];
+	for (int i = 0; i < 3; i++) tb[i] = sum[i] - dpr * prop[i];
+	double r0[3] = {-c->gridspace * (c->bX - 1) / 2.0, -c->gridspace * (c->bY - 1) / 2.0,
+		-c->gridspace * (c->bZ - 1) / 2.0};
+	double ph0 = -c->k * (r0[0] * prop[0] + r0[1] * prop[1] + r0[2] * prop[2]);
+	cplx amp = -I * (cos(ph0) + I * sin(ph0)) * (c->k * c->k * c->k);
+	double s = 0;
+	for (int i = 0; i < 3; i++) s += creal(amp * tb[i] * incpol[i]);
+	*cext = s * 4 * M_PI / (c->k * c->k);
+	const double t1 = 2 * c->k * c->k * c->k / 3;
+	double sa = 0;
+	for (size_t j = 0; j < c->n; j++)
+		for (int i = 0; i < 3; i++) {
+			double mult = -cimag(1 / cc_of(c, j, i)) - t1;
+			cplx p = P[3 * j + i];
+			sa += mult * (creal(p) * creal(p) + cimag(p) * cimag(p));
+		}
+	*cabs = 4 * M_PI * c->k * sa;
+}

@@ -1,0 +1,43 @@
+/* adda_oracle.h - CPU restatement of ADDA's FFT-accelerated DDA hot path (double precision).
+ *
+ * TEST INFRASTRUCTURE (oracle). Used only by tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg,
+ * always as the checker or the timed CPU baseline, never as part of the GPU product.
+ *
+ * What is restated (reference = ADDA 1.3b6, paths relative to the reference project):
+ *   or_init_dmatrix  <- InitDmatrix              src/fft.c:918-1416 (point-dipole term, reduced FFT)
+ *   or_matvec        <- MatVec                   src/matvec.c:128-425
+ *   or_solve         <- IterativeSolver          src/iterative.c:1398-1530, QMR_CS :898-1032, BiCGStab :640-724
+ *   or_cross         <- ExtCross / AbsCross      src/crosssec.c:811-917 (plane wave, free space, Draine)
+ * Complex vectors are interleaved (re,im) doubles, dipole-major [dipole][3], like the reference's doublecomplex.
+ */
+#ifndef ADDA_ORACLE_H
+#define ADDA_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+typedef struct or_ctx or_ctx;
+
+/* iterative methods and initial-field modes, same meaning as -iter and -init_field */
+enum { OR_QMR_CS = 0, OR_BICGSTAB = 1 };
+enum { OR_IF_AUTO = 0, OR_IF_ZERO = 1, OR_IF_INC = 2 };
+/* solver status codes */
+enum { OR_OK = 0, OR_EBREAKDOWN = 1, OR_ESTAGNATION = 2, OR_EMAXITER = 3 };
+
+int or_fftfit(int x, int divis);
+or_ctx *or_create(int boxX, int boxY, int boxZ, int gridX, int gridY, int gridZ, size_t nvoid,
+	const uint16_t *position, const uint8_t *material, double gridspace, double wavenum, int nthreads);
+void or_free(or_ctx *c);
+void or_init_dmatrix(or_ctx *c);
+size_t or_dmatrix_len(const or_ctx *c);        // complex elements, layout [x][z<DsizeZ][y<DsizeY][6]
+void or_get_dmatrix(const or_ctx *c, double *out);
+/* coupling constants: cc (not its root) per material [nmat][3] or per dipole [N][3]; cc_sqrt=csqrt(cc) */
+void or_set_cc_mat(or_ctx *c, int nmat, const double *cc);
+void or_set_cc_dip(or_ctx *c, const double *cc);
+void or_matvec(or_ctx *c, const double *argvec, double *resultvec, double *inprod, int her);
+int or_solve(or_ctx *c, int method, const double *einc, double eps, int maxiter, int init_field,
+	double *xvec, double *pvec, double *resid_hist, int hist_cap, int *niter_out);
+void or_cross(or_ctx *c, const double *pvec, const double prop[3], const double incpol[3], double *cext,
+	double *cabs);
+
+#endif

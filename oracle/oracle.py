@@ -1,0 +1,146 @@
+"""ctypes front end of the C oracle (liboracle.so) and of the reference build under oracle/_ref.
+
+TEST INFRASTRUCTURE: imported only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg, as the
+checker or the timed CPU baseline. The GPU product never imports this module.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_BIN = os.path.join(HERE, "_ref", "adda")
+
+QMR_CS, BICGSTAB = 0, 1
+IF_AUTO, IF_ZERO, IF_INC = 0, 1, 2
+STATUS = {0: "ok", 1: "breakdown", 2: "stagnation", 3: "maxiter"}
+
+_lib = None
+
+
+def build(force=False):
+    """Compile liboracle.so (and, when the reference sources are present, the reference build)."""
+    if force or not os.path.exists(LIB_PATH):
+        subprocess.run(["make", "-s", "-C", HERE, "lib"], check=True)
+    return LIB_PATH
+
+
+def build_reference(ref_src="/root/reference/src"):
+    """Compile the unmodified reference sequential build with the FFTW-subset shim into oracle/_ref/adda."""
+    if not os.path.isdir(ref_src):
+        return None
+    subprocess.run(["make", "-s", "-C", HERE, "ref", "REF_SRC=" + ref_src, "-j8"], check=True)
+    return REF_BIN
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        c_p, c_d, c_i, c_sz = ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_size_t
+        L.or_fftfit.argtypes = [c_i, c_i]
+        L.or_fftfit.restype = c_i
+        L.or_create.argtypes = [c_i] * 6 + [c_sz, c_p, c_p, c_d, c_d, c_i]
+        L.or_create.restype = c_p
+        L.or_free.argtypes = [c_p]
+        L.or_init_dmatrix.argtypes = [c_p]
+        L.or_dmatrix_len.argtypes = [c_p]
+        L.or_dmatrix_len.restype = c_sz
+        L.or_get_dmatrix.argtypes = [c_p, c_p]
+        L.or_set_cc_mat.argtypes = [c_p, c_i, c_p]
+        L.or_set_cc_dip.argtypes = [c_p, c_p]
+        L.or_matvec.argtypes = [c_p, c_p, c_p, c_p, c_i]
+        L.or_solve.argtypes = [c_p, c_i, c_p, c_d, c_i, c_i, c_p, c_p, c_p, c_i, c_p]
+        L.or_solve.restype = c_i
+        L.or_cross.argtypes = [c_p, c_p, c_p, c_p, c_p, c_p]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Oracle:
+    """One particle lattice on the CPU: D matrix, matvec, QMR_CS/BiCGStab and Cext/Cabs in double precision."""
+
+    def __init__(self, box, grid, position, material, gridspace, wavenum, nthreads=0):
+        self.L = lib()
+        self.position = np.ascontiguousarray(position, dtype=np.uint16).reshape(-1, 3)
+        self.material = np.ascontiguousarray(material if material is not None
+                                             else np.zeros(len(self.position)), dtype=np.uint8)
+        self.n = len(self.position)
+        self.box, self.grid = tuple(box), tuple(grid)
+        self.h = self.L.or_create(*box, *grid, self.n, _ptr(self.position), _ptr(self.material),
+                                  gridspace, wavenum, nthreads)
+        self.L.or_init_dmatrix(self.h)
+
+    def close(self):
+        if self.h:
+            self.L.or_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def dmatrix(self):
+        n = self.L.or_dmatrix_len(self.h)
+        out = np.empty(n, dtype=np.complex128)
+        self.L.or_get_dmatrix(self.h, _ptr(out))
+        return out
+
+    def set_cc(self, cc):
+        """cc: complex [nmat,3] per material or [ndip,3] per dipole (flag by shape)."""
+        cc = np.ascontiguousarray(cc, dtype=np.complex128)
+        if cc.ndim == 2 and cc.shape[0] == self.n and cc.shape[0] > 255:
+            self.L.or_set_cc_dip(self.h, _ptr(cc))
+        else:
+            self.L.or_set_cc_mat(self.h, cc.shape[0], _ptr(cc))
+
+    def set_cc_dipole(self, cc):
+        cc = np.ascontiguousarray(cc, dtype=np.complex128).reshape(self.n, 3)
+        self.L.or_set_cc_dip(self.h, _ptr(cc))
+
+    def matvec(self, x, her=False):
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        y = np.empty_like(x)
+        ip = ctypes.c_double(0)
+        self.L.or_matvec(self.h, _ptr(x), _ptr(y), ctypes.byref(ip), int(her))
+        return y, ip.value
+
+    def solve(self, einc, method=QMR_CS, eps=1e-5, maxiter=100000, init_field=IF_AUTO, hist_cap=100000):
+        einc = np.ascontiguousarray(einc, dtype=np.complex128)
+        x = np.empty_like(einc)
+        p = np.empty_like(einc)
+        hist = np.zeros(hist_cap)
+        nit = ctypes.c_int(0)
+        st = self.L.or_solve(self.h, method, _ptr(einc), eps, maxiter, init_field, _ptr(x), _ptr(p), _ptr(hist),
+                             hist_cap, ctypes.byref(nit))
+        return dict(status=st, niter=nit.value, x=x, p=p, resid=hist[:min(nit.value + 1, hist_cap)])
+
+    def cross(self, pvec, prop, incpol):
+        pvec = np.ascontiguousarray(pvec, dtype=np.complex128)
+        prop = np.ascontiguousarray(prop, dtype=np.float64)
+        incpol = np.ascontiguousarray(incpol, dtype=np.float64)
+        ce, ca = ctypes.c_double(0), ctypes.c_double(0)
+        self.L.or_cross(self.h, _ptr(pvec), _ptr(prop), _ptr(incpol), ctypes.byref(ce), ctypes.byref(ca))
+        return ce.value, ca.value
+
+
+def fftfit(x, divis=1):
+    return lib().or_fftfit(x, divis)
+
+
+def run_reference(args, workdir):
+    """Run the reference build (oracle/_ref/adda) with a command line; returns (stdout, run directory)."""
+    os.makedirs(workdir, exist_ok=True)
+    rundir = os.path.join(workdir, "run")
+    out = subprocess.run([REF_BIN] + list(args) + ["-dir", rundir], cwd=workdir, capture_output=True, text=True,
+                         check=True)
+    return out.stdout, rundir
