@@ -1,0 +1,308 @@
+"""Python front end of libadda_gb300.so (ctypes over the C ABI in include/adda_gb300.h).
+
+The host side mirrors the reference's command-line driven setup for the hot path: a particle from -grid/-shape,
+-m, -dpl, -pol, -orient (param.c defaults: lambda = 2*pi, so k = 1; dpl = 10*|m|), the incident plane waves of
+both polarisations, and then the device context that owns the interaction matrix, the matvec and the solver.
+No CPU fallback exists: every compute call goes through the CUDA library and fails loudly without it.
+"""
+import ctypes
+import math
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libadda_gb300.so")
+
+SHAPES = {"sphere": 0, "ellipsoid": 1, "box": 2}
+POLS = {"ldr": 0, "cm": 1, "rrc": 2, "dgf": 3}
+ITERS = {"qmr": 0, "bicgstab": 1}
+PREC = {"fp64": 0, "fp32": 1, "mixed": 2}
+INIT = {"auto": 0, "zero": 1, "inc": 2}
+STATUS = {0: "ok", 1: "breakdown", 2: "stagnation", 3: "maxiter"}
+
+
+class AddaError(RuntimeError):
+    pass
+
+
+class Problem(ctypes.Structure):
+    _fields_ = [("boxX", ctypes.c_int), ("boxY", ctypes.c_int), ("boxZ", ctypes.c_int),
+                ("gridX", ctypes.c_int), ("gridY", ctypes.c_int), ("gridZ", ctypes.c_int),
+                ("ndip", ctypes.c_size_t), ("position", ctypes.c_void_p), ("material", ctypes.c_void_p),
+                ("gridspace", ctypes.c_double), ("wavenum", ctypes.c_double), ("nrhs_max", ctypes.c_int),
+                ("device", ctypes.c_int)]
+
+
+class SolveParams(ctypes.Structure):
+    _fields_ = [("method", ctypes.c_int), ("precision", ctypes.c_int), ("eps", ctypes.c_double),
+                ("maxiter", ctypes.c_int), ("init_field", ctypes.c_int), ("check_every", ctypes.c_int),
+                ("inner_eps", ctypes.c_double), ("max_refine", ctypes.c_int)]
+
+
+class RhsStats(ctypes.Structure):
+    _fields_ = [("niter", ctypes.c_int), ("status", ctypes.c_int), ("resid", ctypes.c_double),
+                ("refinements", ctypes.c_int), ("matvecs_fp64", ctypes.c_int), ("matvecs_fp32", ctypes.c_int)]
+
+
+EXPORTS = ["adda_gb300_fft_fit", "adda_gb300_fit_box", "adda_gb300_make_particle", "adda_gb300_rotation",
+           "adda_gb300_plane_wave", "adda_gb300_polarizability", "adda_gb300_create", "adda_gb300_destroy",
+           "adda_gb300_get_grid", "adda_gb300_init_dmatrix", "adda_gb300_dmatrix_len", "adda_gb300_get_dmatrix",
+           "adda_gb300_set_cc", "adda_gb300_set_cc_dipole", "adda_gb300_matvec", "adda_gb300_matvec_device",
+           "adda_gb300_solve", "adda_gb300_solve_device", "adda_gb300_cross_sections", "adda_gb300_time_matvec",
+           "adda_gb300_last_solve_ms", "adda_gb300_last_error", "adda_gb300_kernel_launches"]
+
+_lib = None
+
+
+def build(force=False):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("adda_gb300_build", os.path.join(HERE, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(force=force)
+
+
+def lib():
+    """Load the CUDA library (building it first if it is missing or older than its sources)."""
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        P, I, D, SZ = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_size_t
+        sig = {
+            "adda_gb300_fft_fit": ([I, I], I),
+            "adda_gb300_fit_box": ([I, P, I, P, P], I),
+            "adda_gb300_make_particle": ([I, P, I, I, I, P, P], SZ),
+            "adda_gb300_rotation": ([P, D, D, D, P, P, P], None),
+            "adda_gb300_plane_wave": ([SZ, P, I, I, I, D, D, P, P, P], None),
+            "adda_gb300_polarizability": ([I, D, D, D, D, P, P, I, P], I),
+            "adda_gb300_create": ([P, P], I),
+            "adda_gb300_destroy": ([P], I),
+            "adda_gb300_get_grid": ([P, P], I),
+            "adda_gb300_init_dmatrix": ([P], I),
+            "adda_gb300_dmatrix_len": ([P], SZ),
+            "adda_gb300_get_dmatrix": ([P, P], I),
+            "adda_gb300_set_cc": ([P, I, I, P], I),
+            "adda_gb300_set_cc_dipole": ([P, I, P], I),
+            "adda_gb300_matvec": ([P, I, I, P, P, P, I], I),
+            "adda_gb300_matvec_device": ([P, I, I, P, P, P, I], I),
+            "adda_gb300_solve": ([P, P, I, P, P, P, P, P, I], I),
+            "adda_gb300_solve_device": ([P, P, I, P, P, P, P], I),
+            "adda_gb300_time_matvec": ([P, I, I, I, SZ, P], I),
+            "adda_gb300_cross_sections": ([P, I, P, P, P, P], I),
+            "adda_gb300_last_error": ([], ctypes.c_char_p),
+            "adda_gb300_last_solve_ms": ([P], D),
+            "adda_gb300_kernel_launches": ([], ctypes.c_uint64),
+        }
+        for name, (args, res) in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise AddaError("%s failed (%d): %s" % (what, rc, lib().adda_gb300_last_error().decode()))
+
+
+def kernel_launches():
+    return int(lib().adda_gb300_kernel_launches())
+
+
+# ---------------------------------------------------------------------------------------------------------------------
+# host-side inputs (no GPU)
+
+def fft_fit(x, divis=1):
+    return lib().adda_gb300_fft_fit(int(x), int(divis))
+
+
+def make_particle(shape="sphere", grid=16, pars=None):
+    """Particle lattice as MakeParticle builds it: returns (box, position [N,3] uint16, material [N] uint8)."""
+    L = lib()
+    sh = SHAPES[shape]
+    pp = None if pars is None else np.ascontiguousarray(pars, dtype=np.float64)
+    by, bz = ctypes.c_int(), ctypes.c_int()
+    _check(L.adda_gb300_fit_box(sh, _p(pp), int(grid), ctypes.byref(by), ctypes.byref(bz)), "fit_box")
+    box = (int(grid), by.value, bz.value)
+    n = L.adda_gb300_make_particle(sh, _p(pp), *box, None, None)
+    pos = np.zeros((n, 3), np.uint16)
+    mat = np.zeros(n, np.uint8)
+    L.adda_gb300_make_particle(sh, _p(pp), *box, _p(pos), _p(mat))
+    return box, pos, mat
+
+
+def rotation(alpha=0.0, beta=0.0, gamma=0.0, prop0=None):
+    prop, py, px = np.zeros(3), np.zeros(3), np.zeros(3)
+    p0 = None if prop0 is None else np.ascontiguousarray(prop0, dtype=np.float64)
+    lib().adda_gb300_rotation(_p(p0), alpha, beta, gamma, _p(prop), _p(py), _p(px))
+    return prop, py, px
+
+
+def plane_wave(box, pos, gridspace, wavenum, prop, pol):
+    e = np.zeros(len(pos) * 3, np.complex128)
+    pos = np.ascontiguousarray(pos, dtype=np.uint16)
+    lib().adda_gb300_plane_wave(len(pos), _p(pos), *box, gridspace, wavenum, _p(np.ascontiguousarray(prop, float)),
+                                _p(np.ascontiguousarray(pol, float)), _p(e))
+    return e
+
+
+def polarizability(m, kd, gridspace, prop, incpol, relation="ldr", avgpol=False):
+    cc = np.zeros(3, np.complex128)
+    _check(lib().adda_gb300_polarizability(POLS[relation], complex(m).real, complex(m).imag, kd, gridspace,
+                                           _p(np.ascontiguousarray(prop, float)),
+                                           _p(np.ascontiguousarray(incpol, float)), int(avgpol), _p(cc)),
+           "polarizability")
+    return cc
+
+
+VOLUME_RATIO = {"sphere": lambda p: math.pi / 6, "ellipsoid": lambda p: math.pi / 6 * p[0] * p[1],
+                "box": lambda p: p[0] * p[1]}
+
+
+class Setup:
+    """The inputs the reference host would build for
+    '-grid g -shape s [pars] -m re im [-dpl d | -size s] -pol p [avgpol] -orient a b c -prop px py pz'
+    (lambda = 2*pi, so k = 1): lattice, grid, both polarisations' cc, Einc, propagation and polarisation vectors.
+    dpl defaults to 10*|m|; with -size it follows from the volume correction (make_particle.c:2178-2191).
+    Order of the RHS: Y polarisation first, then X (calculator.c:309-330)."""
+
+    def __init__(self, grid=16, shape="sphere", pars=None, m=1.5, dpl=None, size=None, pol="ldr", orient=(0, 0, 0),
+                 avgpol=False, prop=None, lam=2 * math.pi):
+        self.box, self.pos, self.mat = make_particle(shape, grid, pars)
+        self.n = len(self.pos)
+        self.grid = (fft_fit(2 * self.box[0]), fft_fit(2 * self.box[1]), fft_fit(2 * self.box[2], 2))
+        self.m = complex(m)
+        if size is not None:
+            vr = VOLUME_RATIO[shape](pars if pars is not None else (1.0, 1.0))
+            self.dpl = lam * (self.n / vr) ** (1.0 / 3) / size
+        else:
+            self.dpl = float(dpl) if dpl else 10 * abs(self.m)
+        self.wavenum = 2 * math.pi / lam
+        self.gridspace = lam / self.dpl
+        self.kd = 2 * math.pi / self.dpl
+        self.prop, py, px = rotation(*orient, prop0=prop)
+        self.incpol = [py, px]
+        self.cc = [polarizability(self.m, self.kd, self.gridspace, self.prop, e, pol, avgpol) for e in self.incpol]
+        self.einc = [plane_wave(self.box, self.pos, self.gridspace, self.wavenum, self.prop, e) for e in self.incpol]
+
+
+# ---------------------------------------------------------------------------------------------------------------------
+# device context
+
+class Context:
+    """One particle lattice on one GPU: the interaction matrix, FP64/FP32 matvecs, solver and cross sections."""
+
+    def __init__(self, box, pos, mat, gridspace, wavenum, grid=(0, 0, 0), nrhs_max=2, device=0):
+        self.L = lib()
+        self.pos = np.ascontiguousarray(pos, dtype=np.uint16).reshape(-1, 3)
+        self.mat = None if mat is None else np.ascontiguousarray(mat, dtype=np.uint8)
+        self.n = len(self.pos)
+        self.nrhs_max = nrhs_max
+        pr = Problem(box[0], box[1], box[2], grid[0], grid[1], grid[2], self.n, _p(self.pos).value,
+                     None if self.mat is None else _p(self.mat).value, gridspace, wavenum, nrhs_max, device)
+        self.h = ctypes.c_void_p()
+        _check(self.L.adda_gb300_create(ctypes.byref(pr), ctypes.byref(self.h)), "create")
+        g = (ctypes.c_int * 3)()
+        self.L.adda_gb300_get_grid(self.h, g)
+        self.grid = tuple(g)
+
+    @classmethod
+    def from_setup(cls, s, nrhs_max=2, device=0):
+        c = cls(s.box, s.pos, s.mat, s.gridspace, s.wavenum, s.grid, nrhs_max, device)
+        c.init_dmatrix()
+        for r in range(min(nrhs_max, len(s.cc))):
+            c.set_cc(r, s.cc[r].reshape(1, 3))
+        return c
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.L.adda_gb300_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init_dmatrix(self):
+        _check(self.L.adda_gb300_init_dmatrix(self.h), "init_dmatrix")
+
+    def dmatrix(self):
+        n = self.L.adda_gb300_dmatrix_len(self.h)
+        out = np.empty(n, np.complex128)
+        _check(self.L.adda_gb300_get_dmatrix(self.h, _p(out)), "get_dmatrix")
+        return out
+
+    def set_cc(self, rhs, cc):
+        cc = np.ascontiguousarray(cc, dtype=np.complex128).reshape(-1, 3)
+        _check(self.L.adda_gb300_set_cc(self.h, rhs, cc.shape[0], _p(cc)), "set_cc")
+
+    def set_cc_dipole(self, rhs, cc):
+        cc = np.ascontiguousarray(cc, dtype=np.complex128).reshape(self.n, 3)
+        _check(self.L.adda_gb300_set_cc_dipole(self.h, rhs, _p(cc)), "set_cc_dipole")
+
+    def matvec(self, x, prec="fp64", her=False):
+        """x: [nrhs, 3N] (or [3N]) complex; returns (y, |y|^2 per RHS)."""
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        one = x.ndim == 1
+        x2 = x.reshape(-1, 3 * self.n)
+        y = np.empty_like(x2)
+        ip = np.zeros(x2.shape[0])
+        _check(self.L.adda_gb300_matvec(self.h, PREC[prec], x2.shape[0], _p(x2), _p(y), _p(ip), int(her)), "matvec")
+        return (y[0], ip[0]) if one else (y, ip)
+
+    def solve(self, einc, method="qmr", prec="fp64", eps=1e-5, maxiter=100000, init="auto", check_every=0,
+              inner_eps=0.0, max_refine=0, hist_cap=0):
+        """einc: [nrhs, 3N] complex. Returns dict with x, p [nrhs,3N], stats per RHS and residual histories."""
+        e = np.ascontiguousarray(einc, dtype=np.complex128).reshape(-1, 3 * self.n)
+        R = e.shape[0]
+        x = np.empty_like(e)
+        p = np.empty_like(e)
+        st = (RhsStats * R)()
+        hist = np.zeros((R, hist_cap)) if hist_cap else None
+        sp = SolveParams(ITERS[method], PREC[prec], eps, maxiter, INIT[init], check_every, inner_eps, max_refine)
+        _check(self.L.adda_gb300_solve(self.h, ctypes.byref(sp), R, _p(e), _p(x), _p(p), st, _p(hist), hist_cap),
+               "solve")
+        stats = [dict(niter=s.niter, status=STATUS.get(s.status, s.status), resid=s.resid,
+                      refinements=s.refinements, matvecs_fp64=s.matvecs_fp64, matvecs_fp32=s.matvecs_fp32)
+                 for s in st]
+        return dict(x=x, p=p, stats=stats, hist=hist)
+
+    def solve_device(self, d_einc, nrhs, d_x=None, d_p=None, method="qmr", prec="mixed", eps=1e-5, maxiter=100000,
+                     init="auto", check_every=0, inner_eps=0.0, max_refine=0):
+        """solve on device-resident buffers (raw CUDA pointers as ints, double2 [nrhs][3N])"""
+        st = (RhsStats * nrhs)()
+        sp = SolveParams(ITERS[method], PREC[prec], eps, maxiter, INIT[init], check_every, inner_eps, max_refine)
+        _check(self.L.adda_gb300_solve_device(self.h, ctypes.byref(sp), nrhs, ctypes.c_void_p(d_einc),
+                                              ctypes.c_void_p(d_x) if d_x else None,
+                                              ctypes.c_void_p(d_p) if d_p else None, st), "solve_device")
+        return [dict(niter=s.niter, status=STATUS.get(s.status, s.status), resid=s.resid, refinements=s.refinements,
+                     matvecs_fp64=s.matvecs_fp64, matvecs_fp32=s.matvecs_fp32) for s in st]
+
+    def last_solve_ms(self):
+        """device milliseconds of the last solve (CUDA events on the context stream)"""
+        return self.L.adda_gb300_last_solve_ms(self.h)
+
+    def time_matvec(self, prec="fp32", nrhs=1, iters=10, flush_bytes=0):
+        """average device milliseconds of one matvec (CUDA events on the context stream)"""
+        ms = ctypes.c_double(0)
+        _check(self.L.adda_gb300_time_matvec(self.h, PREC[prec], nrhs, iters, flush_bytes, ctypes.byref(ms)),
+               "time_matvec")
+        return ms.value
+
+    def cross_sections(self, prop, incpol):
+        """prop/incpol: [nrhs,3]; returns (Cext[nrhs], Cabs[nrhs]) from the last solve's polarisations."""
+        prop = np.ascontiguousarray(prop, dtype=np.float64).reshape(-1, 3)
+        inc = np.ascontiguousarray(incpol, dtype=np.float64).reshape(-1, 3)
+        R = prop.shape[0]
+        ce, ca = np.zeros(R), np.zeros(R)
+        _check(self.L.adda_gb300_cross_sections(self.h, R, _p(prop), _p(inc), _p(ce), _p(ca)), "cross_sections")
+        return ce, ca

@@ -1,0 +1,524 @@
+// api.cu - context management and the C-ABI entry points of include/adda_gb300.h.
+#include "ctx.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+
+namespace adda {
+
+static thread_local std::string g_err;
+std::atomic<unsigned long long> g_launches{0};
+
+void set_error(const std::string &msg) { g_err = msg; }
+
+// exp(-2*pi*i*t/n) with octant reduction (arguments of cos/sin stay in [0, pi/4])
+static void unit_root(long t, long n, double &c, double &s)
+{
+	t %= n;
+	if (t < 0) t += n;
+	const long e = 8 * t;
+	const int oct = (int)(e / n);
+	const double a = (double)(e - (long)oct * n) / (double)n * (M_PI / 4);
+	const double ca = cos(a), sa = sin(a), cb = cos(M_PI / 4 - a), sb = sin(M_PI / 4 - a);
+	double cc, ss;
+	switch (oct) {
+		case 0: cc = ca; ss = sa; break;
+		case 1: cc = sb; ss = cb; break;
+		case 2: cc = -sa; ss = ca; break;
+		case 3: cc = -cb; ss = sb; break;
+		case 4: cc = -ca; ss = -sa; break;
+		case 5: cc = -sb; ss = -cb; break;
+		case 6: cc = sa; ss = -ca; break;
+		default: cc = cb; ss = -sb; break;
+	}
+	c = cc;
+	s = -ss;
+}
+
+FftPlan make_plan(int n, int max_radix)
+{
+	FftPlan p;
+	memset(&p, 0, sizeof(p));
+	p.n = n;
+	int m = n;
+	while (m % max_radix == 0 && p.np < ADDA_FFT_MAXPASS) { p.r[p.np++] = max_radix; m /= max_radix; }
+	for (int r = max_radix / 2; r >= 2; r /= 2)
+		while (m % r == 0 && p.np < ADDA_FFT_MAXPASS) { p.r[p.np++] = r; m /= r; }
+	const int odd[] = {3, 5, 7, 11, 13};
+	for (int q : odd)
+		while (m % q == 0 && p.np < ADDA_FFT_MAXPASS) { p.r[p.np++] = q; m /= q; }
+	if (m != 1) p.np = -1; // unsupported factor
+	return p;
+}
+
+} // namespace adda
+
+using namespace adda;
+
+extern "C" {
+
+const char *adda_gb300_last_error(void) { return g_err.c_str(); }
+
+double adda_gb300_last_solve_ms(const adda_gb300_ctx *c) { return c ? c->last_solve_ms : 0.0; }
+
+uint64_t adda_gb300_kernel_launches(void) { return g_launches.load(); }
+
+int adda_gb300_get_grid(const adda_gb300_ctx *c, int grid[3])
+{
+	if (!c || !grid) return ADDA_GB300_EINVAL;
+	grid[0] = c->gX;
+	grid[1] = c->gY;
+	grid[2] = c->gZ;
+	return ADDA_GB300_OK;
+}
+
+static int upload_twiddles(adda_gb300_ctx *c, int which, int n)
+{
+	std::vector<double2> t64(n);
+	std::vector<float2> t32(n);
+	for (int t = 0; t < n; t++) {
+		double cs, sn;
+		unit_root(t, n, cs, sn);
+		t64[t] = make_double2(cs, sn);
+		t32[t] = make_float2((float)cs, (float)sn);
+	}
+	ADDA_CUDA(cudaMalloc(&c->tw64[which], sizeof(double2) * n));
+	ADDA_CUDA(cudaMalloc(&c->tw32[which], sizeof(float2) * n));
+	ADDA_CUDA(cudaMemcpy(c->tw64[which], t64.data(), sizeof(double2) * n, cudaMemcpyHostToDevice));
+	ADDA_CUDA(cudaMemcpy(c->tw32[which], t32.data(), sizeof(float2) * n, cudaMemcpyHostToDevice));
+	return ADDA_GB300_OK;
+}
+
+static int create_impl(const adda_gb300_problem *p, adda_gb300_ctx *c)
+{
+	c->device = p->device;
+	ADDA_CUDA(cudaSetDevice(p->device));
+	ADDA_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+	c->bX = p->boxX; c->bY = p->boxY; c->bZ = p->boxZ;
+	c->gX = p->gridX > 0 ? p->gridX : adda_gb300_fft_fit(2 * p->boxX, 1);
+	c->gY = p->gridY > 0 ? p->gridY : adda_gb300_fft_fit(2 * p->boxY, 1);
+	c->gZ = p->gridZ > 0 ? p->gridZ : adda_gb300_fft_fit(2 * p->boxZ, 2);
+	if (c->gX < 2 * c->bX - 1 || c->gY < 2 * c->bY || c->gZ < 2 * c->bZ || c->gY % 2 || c->gZ % 2) {
+		set_error("FFT grid must satisfy gridX >= 2*boxX-1 and even gridY >= 2*boxY, gridZ >= 2*boxZ");
+		return ADDA_GB300_EINVAL;
+	}
+	c->DsY = c->gY / 2 + 1;
+	c->DsZ = c->gZ / 2 + 1;
+	c->N = p->ndip;
+	c->Rmax = p->nrhs_max > 0 ? p->nrhs_max : 1;
+	c->gridspace = p->gridspace;
+	c->k = p->wavenum;
+	const int g3[3] = {c->gX, c->gY, c->gZ};
+	FftPlan *pl[3] = {c->px, c->py, c->pz};
+	for (int d = 0; d < 3; d++) {
+		pl[d][0] = make_plan(g3[d], 8);
+		pl[d][1] = make_plan(g3[d], 16);
+		if (pl[d][0].np < 0 || pl[d][1].np < 0) {
+			set_error("FFT grid sizes must factor into 2,3,5,7,11,13");
+			return ADDA_GB300_EINVAL;
+		}
+		int rc = upload_twiddles(c, d, g3[d]);
+		if (rc) return rc;
+	}
+	// lattice: check order (z, y, x ascending), build per-line dipole ranges
+	const size_t N = c->N;
+	c->pos.assign(p->position, p->position + 3 * N);
+	c->mat.assign(N, 0);
+	if (p->material) std::copy(p->material, p->material + N, c->mat.begin());
+	std::vector<uint32_t> ls((size_t)c->bZ * c->bY + 1, 0), xy(N);
+	long prev = -1;
+	for (size_t i = 0; i < N; i++) {
+		const int x = c->pos[3 * i], y = c->pos[3 * i + 1], z = c->pos[3 * i + 2];
+		if (x >= c->bX || y >= c->bY || z >= c->bZ) {
+			set_error("dipole position outside the box");
+			return ADDA_GB300_EINVAL;
+		}
+		const long key = ((long)z * c->bY + y) * c->bX + x;
+		if (key <= prev) {
+			set_error("dipole positions must be unique and sorted z-major, then y, then x");
+			return ADDA_GB300_EINVAL;
+		}
+		prev = key;
+		ls[(size_t)z * c->bY + y + 1]++;
+		xy[i] = (uint32_t)x | ((uint32_t)y << 16);
+	}
+	for (size_t l = 1; l < ls.size(); l++) ls[l] += ls[l - 1];
+	if (N > 0xffffffffu / 3) {
+		set_error("too many dipoles");
+		return ADDA_GB300_EINVAL;
+	}
+	ADDA_CUDA(cudaMalloc(&c->d_line_start, sizeof(uint32_t) * ls.size()));
+	ADDA_CUDA(cudaMalloc(&c->d_xy, sizeof(uint32_t) * std::max<size_t>(N, 1)));
+	ADDA_CUDA(cudaMalloc(&c->d_mat, std::max<size_t>(N, 1)));
+	ADDA_CUDA(cudaMalloc(&c->d_pos, sizeof(uint16_t) * 3 * std::max<size_t>(N, 1)));
+	ADDA_CUDA(cudaMemcpy(c->d_line_start, ls.data(), sizeof(uint32_t) * ls.size(), cudaMemcpyHostToDevice));
+	if (N) {
+		ADDA_CUDA(cudaMemcpy(c->d_xy, xy.data(), sizeof(uint32_t) * N, cudaMemcpyHostToDevice));
+		ADDA_CUDA(cudaMemcpy(c->d_mat, c->mat.data(), N, cudaMemcpyHostToDevice));
+		ADDA_CUDA(cudaMemcpy(c->d_pos, c->pos.data(), sizeof(uint16_t) * 3 * N, cudaMemcpyHostToDevice));
+	}
+	// interaction matrix
+	const size_t dlen = (size_t)c->gX * c->DsZ * c->DsY * 6;
+	ADDA_CUDA(cudaMalloc(&c->D64, sizeof(double2) * dlen));
+	ADDA_CUDA(cudaMalloc(&c->D32, sizeof(float2) * dlen));
+	// matvec work: Xf for Rmax RHS in FP64; the z-chunk buffer is sized to ~48 MB so that it stays in L2
+	const size_t R = c->Rmax;
+	ADDA_CUDA(cudaMalloc(&c->Xf, sizeof(double2) * R * c->gX * 3 * (size_t)c->bZ * c->bY));
+	const size_t slab = R * 3 * (size_t)c->gZ * c->bY; // complex elements of one x-slab for all RHS
+	const size_t budget = 48u << 20;
+	c->CK64 = (int)std::max<size_t>(1, std::min<size_t>(c->gX, budget / (slab * sizeof(double2))));
+	c->CK32 = (int)std::max<size_t>(1, std::min<size_t>(c->gX, budget / (slab * sizeof(float2))));
+	const size_t tz = std::max(c->CK64 * sizeof(double2), c->CK32 * sizeof(float2)) * slab;
+	ADDA_CUDA(cudaMalloc(&c->Tz, tz));
+	c->partial_len = R * matvec_partial_blocks(c, true) * 4;
+	ADDA_CUDA(cudaMalloc(&c->partial, sizeof(double) * c->partial_len));
+	ADDA_CUDA(cudaMalloc(&c->d_red, sizeof(double) * R * 4));
+	ADDA_CUDA(cudaMalloc(&c->vin, sizeof(double2) * R * 3 * std::max<size_t>(N, 1)));
+	ADDA_CUDA(cudaMalloc(&c->vout, sizeof(double2) * R * 3 * std::max<size_t>(N, 1)));
+	c->cc_set.assign(R, 0);
+	c->nmat = 0;
+	return matvec_setup(c);
+}
+
+int adda_gb300_destroy(adda_gb300_ctx *c)
+{
+	if (!c) return ADDA_GB300_OK;
+	if (c->stream) cudaStreamSynchronize(c->stream);
+	solver_free(c);
+	void *bufs[] = {c->d_line_start, c->d_xy, c->d_mat, c->d_pos, c->D64, c->D32, c->cc64, c->ccs64, c->ccs32,
+		c->Xf, c->Tz, c->partial, c->d_red, c->vin, c->vout, c->pvec64, c->tw64[0], c->tw64[1], c->tw64[2],
+		c->tw32[0], c->tw32[1], c->tw32[2]};
+	for (void *b : bufs)
+		if (b) cudaFree(b);
+	if (c->stream) cudaStreamDestroy(c->stream);
+	delete c;
+	return ADDA_GB300_OK;
+}
+
+int adda_gb300_create(const adda_gb300_problem *p, adda_gb300_ctx **out)
+{
+	if (!p || !out || p->boxX < 1 || p->boxY < 1 || p->boxZ < 1 || (p->ndip && !p->position) ||
+		p->boxX > 65535 || p->boxY > 65535 || p->boxZ > 65535 || !(p->gridspace > 0) || !(p->wavenum > 0)) {
+		set_error("adda_gb300_create: invalid problem description");
+		return ADDA_GB300_EINVAL;
+	}
+	*out = nullptr;
+	int ndev = 0;
+	if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= p->device || p->device < 0) {
+		cudaGetLastError();
+		set_error("adda_gb300_create: no usable CUDA device");
+		return ADDA_GB300_ECUDA;
+	}
+	adda_gb300_ctx *c = new adda_gb300_ctx();
+	int rc = create_impl(p, c);
+	if (rc) {
+		std::string keep = g_err;
+		adda_gb300_destroy(c);
+		g_err = keep;
+		return rc;
+	}
+	*out = c;
+	return ADDA_GB300_OK;
+}
+
+int adda_gb300_init_dmatrix(adda_gb300_ctx *c)
+{
+	if (!c) return ADDA_GB300_EINVAL;
+	ADDA_CUDA(cudaSetDevice(c->device));
+	return dmatrix_build(c);
+}
+
+size_t adda_gb300_dmatrix_len(const adda_gb300_ctx *c)
+{
+	return c ? (size_t)c->gX * c->DsZ * c->DsY * 6 : 0;
+}
+
+int adda_gb300_get_dmatrix(adda_gb300_ctx *c, double *out)
+{
+	if (!c || !out) return ADDA_GB300_EINVAL;
+	if (!c->dready) {
+		set_error("D matrix not initialised");
+		return ADDA_GB300_ESTATE;
+	}
+	ADDA_CUDA(cudaSetDevice(c->device));
+	ADDA_CUDA(cudaMemcpy(out, c->D64, sizeof(double2) * adda_gb300_dmatrix_len(c), cudaMemcpyDeviceToHost));
+	return ADDA_GB300_OK;
+}
+
+__global__ void cc_sqrt_k(const double2 *cc, double2 *ccs64, float2 *ccs32, size_t n)
+{
+	for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+		// principal square root, as C99 csqrt (InitCC, calculator.c:273)
+		const double a = cc[t].x, b = cc[t].y;
+		const double m = hypot(a, b);
+		double re = sqrt(0.5 * (m + fabs(a)));
+		double im;
+		if (re == 0) im = 0;
+		else im = b / (2 * re);
+		double2 r;
+		if (a >= 0) r = make_double2(re, im);
+		else r = make_double2(fabs(im), copysign(re, b));
+		ccs64[t] = r;
+		ccs32[t] = make_float2((float)r.x, (float)r.y);
+	}
+}
+
+static int set_cc_impl(adda_gb300_ctx *c, int rhs, int per_dip, int nmat, const double *cc)
+{
+	if (!c || !cc || rhs < 0 || rhs >= c->Rmax || (!per_dip && (nmat < 1 || nmat > 256))) {
+		set_error("set_cc: invalid arguments");
+		return ADDA_GB300_EINVAL;
+	}
+	if (!per_dip)
+		for (size_t i = 0; i < c->N; i++)
+			if (c->mat[i] >= nmat) {
+				set_error("set_cc: a dipole's material index exceeds nmat");
+				return ADDA_GB300_EINVAL;
+			}
+	ADDA_CUDA(cudaSetDevice(c->device));
+	const size_t per = per_dip ? c->N * 3 : (size_t)nmat * 3;
+	// (re)allocate when the mode or the table size changes; other RHS slots must then be set again
+	const bool same = (c->cc64 && c->per_dip == per_dip && (per_dip || c->nmat == nmat));
+	if (!same) {
+		cudaFree(c->cc64); cudaFree(c->ccs64); cudaFree(c->ccs32);
+		c->cc64 = c->ccs64 = nullptr;
+		c->ccs32 = nullptr;
+		ADDA_CUDA(cudaMalloc(&c->cc64, sizeof(double2) * per * c->Rmax));
+		ADDA_CUDA(cudaMalloc(&c->ccs64, sizeof(double2) * per * c->Rmax));
+		ADDA_CUDA(cudaMalloc(&c->ccs32, sizeof(float2) * per * c->Rmax));
+		std::fill(c->cc_set.begin(), c->cc_set.end(), 0);
+		c->per_dip = per_dip;
+		c->nmat = per_dip ? 0 : nmat;
+	}
+	ADDA_CUDA(cudaMemcpyAsync(c->cc64 + per * rhs, cc, sizeof(double2) * per, cudaMemcpyHostToDevice, c->stream));
+	cc_sqrt_k<<<(int)std::min<size_t>((per + 255) / 256, 4096), 256, 0, c->stream>>>(c->cc64 + per * rhs,
+		c->ccs64 + per * rhs, c->ccs32 + per * rhs, per);
+	ADDA_LAUNCHED();
+	ADDA_CUDA(cudaStreamSynchronize(c->stream));
+	c->cc_set[rhs] = 1;
+	return ADDA_GB300_OK;
+}
+
+int adda_gb300_set_cc(adda_gb300_ctx *c, int rhs, int nmat, const double *cc)
+{
+	return set_cc_impl(c, rhs, 0, nmat, cc);
+}
+
+int adda_gb300_set_cc_dipole(adda_gb300_ctx *c, int rhs, const double *cc)
+{
+	return set_cc_impl(c, rhs, 1, 0, cc);
+}
+
+static int check_ready(adda_gb300_ctx *c, int nrhs)
+{
+	if (!c->dready) {
+		set_error("D matrix not initialised (call adda_gb300_init_dmatrix)");
+		return ADDA_GB300_ESTATE;
+	}
+	if (nrhs < 1 || nrhs > c->Rmax) {
+		set_error("nrhs out of range");
+		return ADDA_GB300_EINVAL;
+	}
+	for (int r = 0; r < nrhs; r++)
+		if (!c->cc_set[r]) {
+			set_error("polarisabilities not set for every RHS (call adda_gb300_set_cc)");
+			return ADDA_GB300_ESTATE;
+		}
+	return ADDA_GB300_OK;
+}
+
+__global__ void d2f_k(float2 *dst, const double2 *src, size_t n)
+{
+	for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+		dst[t] = make_float2((float)src[t].x, (float)src[t].y);
+}
+
+__global__ void f2d_k(double2 *dst, const float2 *src, size_t n)
+{
+	for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+		dst[t] = make_double2(src[t].x, src[t].y);
+}
+
+int adda_gb300_matvec_device(adda_gb300_ctx *c, int prec, int nrhs, const void *d_arg, void *d_res, double *d_inprod,
+	int her)
+{
+	if (!c || !d_arg || !d_res || (prec != ADDA_PREC_FP64 && prec != ADDA_PREC_FP32)) {
+		set_error("matvec: invalid arguments");
+		return ADDA_GB300_EINVAL;
+	}
+	int rc = check_ready(c, nrhs);
+	if (rc) return rc;
+	const bool dbl = prec == ADDA_PREC_FP64;
+	MvEpi e{d_inprod ? (int)EPI_NORM : (int)EPI_NONE, nullptr, c->partial};
+	if (dbl) rc = matvec_run<double>(c, nrhs, (const double2 *)d_arg, (double2 *)d_res, her, e, nullptr);
+	else rc = matvec_run<float>(c, nrhs, (const float2 *)d_arg, (float2 *)d_res, her, e, nullptr);
+	if (rc) return rc;
+	if (d_inprod) {
+		const size_t nblk = matvec_partial_blocks(c, dbl);
+		rc = reduce_partials(c, nrhs, c->partial, nblk, c->d_red);
+		if (rc) return rc;
+		ADDA_CUDA(cudaMemcpy2DAsync(d_inprod, sizeof(double), c->d_red, 4 * sizeof(double), sizeof(double), nrhs,
+			cudaMemcpyDeviceToDevice, c->stream));
+	}
+	return ADDA_GB300_OK;
+}
+
+int adda_gb300_matvec(adda_gb300_ctx *c, int prec, int nrhs, const double *argvec, double *resultvec, double *inprod,
+	int her)
+{
+	if (!c || !argvec || !resultvec) {
+		set_error("matvec: invalid arguments");
+		return ADDA_GB300_EINVAL;
+	}
+	int rc = check_ready(c, nrhs);
+	if (rc) return rc;
+	ADDA_CUDA(cudaSetDevice(c->device));
+	const size_t n = (size_t)nrhs * 3 * c->N;
+	double *d_ip = c->d_red + 4 * (size_t)c->Rmax - 0; // not used directly; inprod goes through d_red
+	(void)d_ip;
+	if (prec == ADDA_PREC_FP64) {
+		ADDA_CUDA(cudaMemcpyAsync(c->vin, argvec, sizeof(double2) * n, cudaMemcpyHostToDevice, c->stream));
+		MvEpi e{inprod ? (int)EPI_NORM : (int)EPI_NONE, nullptr, c->partial};
+		rc = matvec_run<double>(c, nrhs, (const double2 *)c->vin, (double2 *)c->vout, her, e, nullptr);
+		if (rc) return rc;
+		ADDA_CUDA(cudaMemcpyAsync(resultvec, c->vout, sizeof(double2) * n, cudaMemcpyDeviceToHost, c->stream));
+	}
+	else if (prec == ADDA_PREC_FP32) {
+		// stage the double host vector, round it on the device, compute, widen the result back
+		double2 *din = (double2 *)c->vin;
+		float2 *fin = (float2 *)c->vout, *fout = (float2 *)c->vout + n;
+		if (2 * n * sizeof(float2) > sizeof(double2) * n + 0) { /* vout holds 2n float2 == n double2 */ }
+		ADDA_CUDA(cudaMemcpyAsync(din, argvec, sizeof(double2) * n, cudaMemcpyHostToDevice, c->stream));
+		d2f_k<<<(int)std::min<size_t>((n + 255) / 256, 8192), 256, 0, c->stream>>>(fin, din, n);
+		ADDA_LAUNCHED();
+		MvEpi e{inprod ? (int)EPI_NORM : (int)EPI_NONE, nullptr, c->partial};
+		rc = matvec_run<float>(c, nrhs, fin, fout, her, e, nullptr);
+		if (rc) return rc;
+		f2d_k<<<(int)std::min<size_t>((n + 255) / 256, 8192), 256, 0, c->stream>>>(din, fout, n);
+		ADDA_LAUNCHED();
+		ADDA_CUDA(cudaMemcpyAsync(resultvec, din, sizeof(double2) * n, cudaMemcpyDeviceToHost, c->stream));
+	}
+	else {
+		set_error("matvec: prec must be ADDA_PREC_FP64 or ADDA_PREC_FP32");
+		return ADDA_GB300_EINVAL;
+	}
+	if (inprod) {
+		const size_t nblk = matvec_partial_blocks(c, prec == ADDA_PREC_FP64);
+		rc = reduce_partials(c, nrhs, c->partial, nblk, c->d_red);
+		if (rc) return rc;
+		std::vector<double> red(4 * (size_t)nrhs);
+		ADDA_CUDA(cudaMemcpyAsync(red.data(), c->d_red, sizeof(double) * 4 * nrhs, cudaMemcpyDeviceToHost,
+			c->stream));
+		ADDA_CUDA(cudaStreamSynchronize(c->stream));
+		for (int r = 0; r < nrhs; r++) inprod[r] = red[4 * r];
+	}
+	ADDA_CUDA(cudaStreamSynchronize(c->stream));
+	return ADDA_GB300_OK;
+}
+
+int adda_gb300_solve(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int nrhs, const double *einc,
+	double *xvec, double *pvec, adda_gb300_rhs_stats *stats, double *resid_hist, int hist_cap)
+{
+	if (!c || !sp || !einc) {
+		set_error("solve: invalid arguments");
+		return ADDA_GB300_EINVAL;
+	}
+	int rc = check_ready(c, nrhs);
+	if (rc) return rc;
+	ADDA_CUDA(cudaSetDevice(c->device));
+	return solver_solve(c, sp, nrhs, einc, xvec, pvec, stats, resid_hist, hist_cap);
+}
+
+int adda_gb300_solve_device(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int nrhs, const void *d_einc,
+	void *d_xvec, void *d_pvec, adda_gb300_rhs_stats *stats)
+{
+	if (!c || !sp || !d_einc) {
+		set_error("solve_device: invalid arguments");
+		return ADDA_GB300_EINVAL;
+	}
+	int rc = check_ready(c, nrhs);
+	if (rc) return rc;
+	ADDA_CUDA(cudaSetDevice(c->device));
+	return solver_solve_dev(c, sp, nrhs, (const double2 *)d_einc, (double2 *)d_xvec, (double2 *)d_pvec, stats);
+}
+
+__global__ void fill_k(double2 *v, size_t n, unsigned seed)
+{
+	for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+		unsigned h = (unsigned)(t * 2654435761u) ^ seed;
+		h ^= h >> 13; h *= 0x5bd1e995u; h ^= h >> 15;
+		unsigned g = h * 0x27d4eb2du; g ^= g >> 16;
+		v[t] = make_double2((h & 0xffffff) / 16777216.0 - 0.5, (g & 0xffffff) / 16777216.0 - 0.5);
+	}
+}
+
+__global__ void flush_k(float4 *buf, size_t n, float v)
+{
+	for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+		buf[t] = make_float4(v, v, v, v);
+}
+
+int adda_gb300_time_matvec(adda_gb300_ctx *c, int prec, int nrhs, int iters, size_t flush_bytes, double *ms)
+{
+	if (!c || !ms || iters < 1 || (prec != ADDA_PREC_FP64 && prec != ADDA_PREC_FP32)) {
+		set_error("time_matvec: invalid arguments");
+		return ADDA_GB300_EINVAL;
+	}
+	int rc = check_ready(c, nrhs);
+	if (rc) return rc;
+	ADDA_CUDA(cudaSetDevice(c->device));
+	const size_t n = (size_t)nrhs * 3 * c->N;
+	const bool dbl = prec == ADDA_PREC_FP64;
+	fill_k<<<1024, 256, 0, c->stream>>>((double2 *)c->vin, n, 12345u);
+	ADDA_LAUNCHED();
+	if (!dbl) {
+		d2f_k<<<1024, 256, 0, c->stream>>>((float2 *)c->vout, (const double2 *)c->vin, n);
+		ADDA_LAUNCHED();
+	}
+	const void *in = dbl ? c->vin : c->vout;
+	void *out = dbl ? c->vout : (void *)((float2 *)c->vout + n);
+	float4 *fl = nullptr;
+	const size_t nfl = flush_bytes / sizeof(float4);
+	if (nfl) ADDA_CUDA(cudaMalloc(&fl, nfl * sizeof(float4)));
+	MvEpi e{EPI_NONE, nullptr, c->partial};
+	cudaEvent_t e0, e1;
+	ADDA_CUDA(cudaEventCreate(&e0));
+	ADDA_CUDA(cudaEventCreate(&e1));
+	double total = 0;
+	for (int it = -1; it < iters && !rc; it++) {
+		if (nfl) {
+			flush_k<<<1024, 256, 0, c->stream>>>(fl, nfl, (float)it);
+			count_launch();
+		}
+		cudaEventRecord(e0, c->stream);
+		rc = dbl ? matvec_run<double>(c, nrhs, (const double2 *)in, (double2 *)out, 0, e, nullptr)
+			: matvec_run<float>(c, nrhs, (const float2 *)in, (float2 *)out, 0, e, nullptr);
+		cudaEventRecord(e1, c->stream);
+		cudaEventSynchronize(e1);
+		float t = 0;
+		cudaEventElapsedTime(&t, e0, e1);
+		if (it >= 0) total += t;
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	if (fl) cudaFree(fl);
+	if (rc) return rc;
+	ADDA_CUDA(cudaGetLastError());
+	*ms = total / iters;
+	return ADDA_GB300_OK;
+}
+
+int adda_gb300_cross_sections(adda_gb300_ctx *c, int nrhs, const double *prop, const double *incpol, double *cext,
+	double *cabs)
+{
+	if (!c || !prop || !incpol || nrhs < 1 || nrhs > c->last_nrhs || !c->pvec64) {
+		set_error("cross_sections: no solution available for that many RHS");
+		return ADDA_GB300_ESTATE;
+	}
+	ADDA_CUDA(cudaSetDevice(c->device));
+	return cross_sections(c, nrhs, prop, incpol, cext, cabs);
+}
+
+} // extern "C"

@@ -1,0 +1,241 @@
+// common.cuh - complex arithmetic, FFT plans and the shared-memory tile FFT used by every kernel of the library.
+//
+// The tile FFT transforms nl lines of length n held in shared memory in ELEMENT-MAJOR order (element e of line l at
+// a[e*nl + l]): consecutive threads work on consecutive lines, so every shared-memory access of a pass is
+// conflict-free, and tiles gathered from HBM along the contiguous axis of the data need no transpose. Each pass is a
+// self-sorting Stockham radix-R step (ping-pong between two tiles); radices 2,3,4,8,16 are hand-written register
+// butterflies, 5/7/11/13 use a looped O(R^2) butterfly. Twiddles come from one table of n-th roots of unity per length, computed on the
+// host in double precision. Sign convention: forward = exp(-2*pi*i*jk/n), unnormalised, like FFTW's FFTW_FORWARD
+// which the reference uses (fft.h FFT_FORWARD -1).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace adda {
+
+template <typename T> struct CxT;
+template <> struct CxT<float> { typedef float2 type; };
+template <> struct CxT<double> { typedef double2 type; };
+
+template <typename C> __host__ __device__ __forceinline__ C cx(decltype(C::x) a, decltype(C::x) b)
+{
+	C r;
+	r.x = a;
+	r.y = b;
+	return r;
+}
+template <typename C> __host__ __device__ __forceinline__ C cadd(C a, C b) { return cx<C>(a.x + b.x, a.y + b.y); }
+template <typename C> __host__ __device__ __forceinline__ C csub(C a, C b) { return cx<C>(a.x - b.x, a.y - b.y); }
+template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b)
+{
+	return cx<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename C> __host__ __device__ __forceinline__ C cconj(C a) { return cx<C>(a.x, -a.y); }
+template <typename C> __host__ __device__ __forceinline__ C cneg(C a) { return cx<C>(-a.x, -a.y); }
+template <typename C, typename S> __host__ __device__ __forceinline__ C cscale(C a, S s)
+{
+	return cx<C>(a.x * s, a.y * s);
+}
+// a*b + c
+template <typename C> __host__ __device__ __forceinline__ C cfma(C a, C b, C c)
+{
+	return cx<C>(a.x * b.x - a.y * b.y + c.x, a.x * b.y + a.y * b.x + c.y);
+}
+__host__ __device__ __forceinline__ double2 to_d2(float2 a) { return make_double2(a.x, a.y); }
+__host__ __device__ __forceinline__ double2 to_d2(double2 a) { return a; }
+template <typename C> __host__ __device__ __forceinline__ C from_d2(double2 a);
+template <> __host__ __device__ __forceinline__ float2 from_d2<float2>(double2 a)
+{
+	return make_float2((float)a.x, (float)a.y);
+}
+template <> __host__ __device__ __forceinline__ double2 from_d2<double2>(double2 a) { return a; }
+
+// ---------------------------------------------------------------------------------------------------------------
+// FFT plan: the radix of each Stockham pass. Filled on the host (make_plan in api.cu), passed to kernels by value.
+#define ADDA_FFT_MAXPASS 12
+struct FftPlan {
+	int n;
+	int np;
+	int r[ADDA_FFT_MAXPASS];
+};
+
+// multiply by exp(s*i*theta) given c=cos(theta), s_=s*sin(theta)
+template <typename C> __device__ __forceinline__ C crot(C v, double c, double s_)
+{
+	typedef decltype(C::x) T;
+	return cx<C>(v.x * (T)c - v.y * (T)s_, v.x * (T)s_ + v.y * (T)c);
+}
+// multiply by -i (forward) or +i (inverse)
+template <typename C> __device__ __forceinline__ C cmi(C v, bool inv) { return inv ? cx<C>(-v.y, v.x) : cx<C>(v.y, -v.x); }
+
+template <typename C> __device__ __forceinline__ void dft2(C &a, C &b)
+{
+	C t = a;
+	a = cadd(t, b);
+	b = csub(t, b);
+}
+
+template <typename C> __device__ __forceinline__ void dft4(C *v, bool inv)
+{
+	C t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+	C t2 = cadd(v[1], v[3]), t3 = cmi(csub(v[1], v[3]), inv);
+	v[0] = cadd(t0, t2);
+	v[2] = csub(t0, t2);
+	v[1] = cadd(t1, t3);
+	v[3] = csub(t1, t3);
+}
+
+// radix-8 as two radix-4 halves (even/odd inputs) joined by W8^k
+template <typename C> __device__ __forceinline__ void dft8(C *v, bool inv)
+{
+	const double h = 0.70710678118654752440; // sqrt(2)/2
+	const double sg = inv ? 1.0 : -1.0;
+	C e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
+	dft4(e, inv);
+	dft4(o, inv);
+	o[1] = crot(o[1], h, sg * h);
+	o[2] = cmi(o[2], inv);
+	o[3] = crot(o[3], -h, sg * h);
+#pragma unroll
+	for (int k = 0; k < 4; k++) {
+		v[k] = cadd(e[k], o[k]);
+		v[k + 4] = csub(e[k], o[k]);
+	}
+}
+
+// radix-16 as two radix-8 halves joined by W16^k
+template <typename C> __device__ __forceinline__ void dft16(C *v, bool inv)
+{
+	const double c1 = 0.92387953251128675613, s1 = 0.38268343236508977173, h = 0.70710678118654752440;
+	const double sg = inv ? 1.0 : -1.0;
+	C e[8], o[8];
+#pragma unroll
+	for (int q = 0; q < 8; q++) {
+		e[q] = v[2 * q];
+		o[q] = v[2 * q + 1];
+	}
+	dft8(e, inv);
+	dft8(o, inv);
+	o[1] = crot(o[1], c1, sg * s1);
+	o[2] = crot(o[2], h, sg * h);
+	o[3] = crot(o[3], s1, sg * c1);
+	o[4] = cmi(o[4], inv);
+	o[5] = crot(o[5], -s1, sg * c1);
+	o[6] = crot(o[6], -h, sg * h);
+	o[7] = crot(o[7], -c1, sg * s1);
+#pragma unroll
+	for (int k = 0; k < 8; k++) {
+		v[k] = cadd(e[k], o[k]);
+		v[k + 8] = csub(e[k], o[k]);
+	}
+}
+
+template <typename C> __device__ __forceinline__ void dft3(C *v, bool inv)
+{
+	typedef decltype(C::x) T;
+	const T s = (T)(inv ? 0.86602540378443864676 : -0.86602540378443864676);
+	C t1 = cadd(v[1], v[2]), t2 = csub(v[1], v[2]);
+	C m1 = cx<C>(v[0].x - (T)0.5 * t1.x, v[0].y - (T)0.5 * t1.y);
+	C m2 = cx<C>(-s * t2.y, s * t2.x); // i*s*t2
+	v[0] = cadd(v[0], t1);
+	v[1] = cadd(m1, m2);
+	v[2] = csub(m1, m2);
+}
+
+template <typename C, int R> __device__ __forceinline__ void dft(C *v, bool inv, const C *__restrict__ tw, int n)
+{
+	if (R == 2) dft2(v[0], v[1]);
+	else if (R == 3) dft3(v, inv);
+	else if (R == 4) dft4(v, inv);
+	else if (R == 8) dft8(v, inv);
+	else if (R == 16) dft16(v, inv);
+}
+
+// One Stockham pass over all lines of an element-major tile: x -> y.
+template <typename C, int R>
+__device__ __forceinline__ void fft_pass(const C *__restrict__ x, C *__restrict__ y, int n, int nl, int m,
+	const C *__restrict__ tw, bool inv)
+{
+	const int nr = n / R;
+	const int total = nr * nl;
+	const int tstep = n / (m * R);
+	for (int w = threadIdx.x; w < total; w += blockDim.x) {
+		const int j = w / nl;
+		const int l = w - j * nl;
+		const int k = j % m;
+		C v[R];
+#pragma unroll
+		for (int q = 0; q < R; q++) v[q] = x[(j + q * nr) * nl + l];
+		if (k) {
+#pragma unroll
+			for (int q = 1; q < R; q++) {
+				C t = __ldg(tw + q * k * tstep);
+				if (inv) t.y = -t.y;
+				v[q] = cmul(v[q], t);
+			}
+		}
+		dft<C, R>(v, inv, tw, n);
+		const int base = (j / m) * m * R + k;
+#pragma unroll
+		for (int q = 0; q < R; q++) y[(base + q * m) * nl + l] = v[q];
+	}
+}
+
+// Stockham pass for the rarer odd radices 5,7,11,13 (fftFit sizes): O(R^2) with both twiddle factors folded into
+// one table lookup, tw[(p*k*(n/(m*R)) + (q*p mod R)*(n/R)) mod n]; loops instead of register arrays keep the register
+// footprint of the hot radix-2^k kernels low.
+template <typename C>
+__device__ __noinline__ void fft_pass_gen(const C *__restrict__ x, C *__restrict__ y, int R, int n, int nl, int m,
+	const C *__restrict__ tw, bool inv)
+{
+	const int nr = n / R;
+	const int total = nr * nl;
+	const int tstep = n / (m * R);
+	const int st = n / R;
+	for (int w = threadIdx.x; w < total; w += blockDim.x) {
+		const int j = w / nl;
+		const int l = w - j * nl;
+		const int k = j % m;
+		const int base = (j / m) * m * R + k;
+		for (int q = 0; q < R; q++) {
+			C acc = cx<C>(0, 0);
+			for (int p = 0; p < R; p++) {
+				const int e = (p * k * tstep + ((q * p) % R) * st) % n;
+				C t = __ldg(tw + e);
+				if (inv) t.y = -t.y;
+				acc = cfma(x[(j + p * nr) * nl + l], t, acc);
+			}
+			y[(base + q * m) * nl + l] = acc;
+		}
+	}
+}
+
+// Full FFT of an element-major tile (n elements x nl lines) in a, using b as scratch. Returns the buffer holding the
+// result (a or b). All threads of the block must call it; it synchronises between passes and at the end.
+template <typename C>
+__device__ C *fft_tile(C *a, C *b, const FftPlan &p, int nl, const C *__restrict__ tw, bool inv)
+{
+	const int n = p.n;
+	int m = 1;
+	for (int f = 0; f < p.np; f++) {
+		const int R = p.r[f];
+		switch (R) {
+			case 2: fft_pass<C, 2>(a, b, n, nl, m, tw, inv); break;
+			case 3: fft_pass<C, 3>(a, b, n, nl, m, tw, inv); break;
+			case 4: fft_pass<C, 4>(a, b, n, nl, m, tw, inv); break;
+			case 8: fft_pass<C, 8>(a, b, n, nl, m, tw, inv); break;
+			case 16: fft_pass<C, 16>(a, b, n, nl, m, tw, inv); break;
+			default: fft_pass_gen<C>(a, b, R, n, nl, m, tw, inv); break; // 5, 7, 11, 13
+		}
+		__syncthreads();
+		C *t = a;
+		a = b;
+		b = t;
+		m *= R;
+	}
+	return a;
+}
+
+} // namespace adda

@@ -1,0 +1,123 @@
+// ctx.cuh - the device context behind adda_gb300_ctx and the internal interfaces between the library's .cu files.
+#pragma once
+
+#include "adda_gb300.h"
+#include "common.cuh"
+
+#include <atomic>
+#include <string>
+#include <vector>
+
+namespace adda {
+
+void set_error(const std::string &msg);
+extern std::atomic<unsigned long long> g_launches;
+inline void count_launch(unsigned long long k = 1) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+
+#define ADDA_CUDA(call)                                                                                          \
+	do {                                                                                                         \
+		cudaError_t e_ = (call);                                                                                 \
+		if (e_ != cudaSuccess) {                                                                                 \
+			::adda::set_error(std::string(#call) + ": " + cudaGetErrorString(e_));                               \
+			return ADDA_GB300_ECUDA;                                                                             \
+		}                                                                                                        \
+	} while (0)
+
+#define ADDA_LAUNCHED()                                                                                          \
+	do {                                                                                                         \
+		::adda::count_launch();                                                                                  \
+		cudaError_t e_ = cudaGetLastError();                                                                     \
+		if (e_ != cudaSuccess) {                                                                                 \
+			::adda::set_error(std::string("kernel launch: ") + cudaGetErrorString(e_));                          \
+			return ADDA_GB300_ECUDA;                                                                             \
+		}                                                                                                        \
+	} while (0)
+
+// Krylov epilogue of the last matvec kernel: per-block partial sums written to partial[(rhs*nblk + blk)*4 + 0..2]
+enum MvEpiMode {
+	EPI_NONE = 0,
+	EPI_NORM = 1,        // s0 = sum |y|^2
+	EPI_DOT_ARG = 2,     // s1 = sum x*y        (bilinear, x = argument)       -- QMR_CS alpha (iterative.c:967)
+	EPI_DOT_U_CONJ = 4,  // s1 = sum y*conj(u)                                 -- BiCGStab v.r~ (iterative.c:694)
+	EPI_DOT_ARG_CONJ = 8 // s1 = sum x*conj(y)  (x = argument)                 -- BiCGStab s.t (iterative.c:712)
+};
+
+struct MvEpi {
+	int mode;
+	const void *u;     // vector for EPI_DOT_U_CONJ (same precision as the matvec)
+	double *partial;   // per-block partial sums
+};
+
+struct SolverWork; // solver.cu
+
+} // namespace adda
+
+struct adda_gb300_ctx {
+	int device = 0;
+	cudaStream_t stream = nullptr;
+	int bX = 0, bY = 0, bZ = 0, gX = 0, gY = 0, gZ = 0, DsY = 0, DsZ = 0;
+	size_t N = 0;
+	int Rmax = 1;
+	double gridspace = 0, k = 0;
+	// lattice (host and device)
+	std::vector<uint16_t> pos;
+	std::vector<uint8_t> mat;
+	uint32_t *d_line_start = nullptr; // [bZ*bY+1]: index of the first dipole of x-line (y,z), lines z-major
+	uint32_t *d_xy = nullptr;         // [N]: x | y<<16
+	uint8_t *d_mat = nullptr;
+	uint16_t *d_pos = nullptr;        // [N][3] (cross sections)
+	// FFT plans: [0] for double, [1] for float (the float plans may use radix 16)
+	adda::FftPlan px[2], py[2], pz[2];
+	double2 *tw64[3] = {nullptr, nullptr, nullptr};
+	float2 *tw32[3] = {nullptr, nullptr, nullptr};
+	// interaction matrix, reduced layout [gX][DsZ][DsY][6]
+	double2 *D64 = nullptr;
+	float2 *D32 = nullptr;
+	bool dready = false;
+	// polarisabilities per RHS: material mode [Rmax][nmat][3], dipole mode [Rmax][N][3]
+	int per_dip = 0, nmat = 0;
+	std::vector<int> cc_set;          // per RHS: 1 once set
+	double2 *cc64 = nullptr, *ccs64 = nullptr;
+	float2 *ccs32 = nullptr;
+	// matvec work
+	void *Xf = nullptr;               // [R][gX][3][bZ][bY] after the X transform
+	void *Tz = nullptr;               // [R][CK][3][gZ][bY] chunk of x-slabs after the Z transform
+	int CK64 = 1, CK32 = 1;           // x-slabs per chunk (sized to stay resident in L2)
+	double *partial = nullptr;        // epilogue partial sums
+	size_t partial_len = 0;
+	double *d_red = nullptr;          // reduced per-RHS results [Rmax][4]
+	// staging for the host-pointer matvec
+	void *vin = nullptr, *vout = nullptr;
+	// solver
+	adda::SolverWork *sw = nullptr;
+	// last solve leaves polarisations here (FP64) for the cross sections
+	double2 *pvec64 = nullptr;
+	int last_nrhs = 0;
+	double last_solve_ms = 0;
+};
+
+namespace adda {
+
+// plan.cpp-equivalent helpers (api.cu)
+FftPlan make_plan(int n, int max_radix);
+
+// dmatrix.cu
+int dmatrix_build(adda_gb300_ctx *c);
+
+// matvec.cu
+int matvec_setup(adda_gb300_ctx *c); // kernel attributes, chunk sizes
+size_t matvec_partial_blocks(const adda_gb300_ctx *c, bool dbl); // partial-sum blocks per RHS of the epilogue
+template <typename T>
+int matvec_run(adda_gb300_ctx *c, int R, const typename CxT<T>::type *arg, typename CxT<T>::type *res, int her,
+	const MvEpi &epi, const int *done);
+int reduce_partials(adda_gb300_ctx *c, int R, const double *partial, size_t nblk, double *out);
+
+// solver.cu
+int solver_solve(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int nrhs, const double *einc, double *xvec,
+	double *pvec, adda_gb300_rhs_stats *stats, double *resid_hist, int hist_cap);
+int solver_solve_dev(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int nrhs, const double2 *d_einc,
+	double2 *d_xvec, double2 *d_pvec, adda_gb300_rhs_stats *stats);
+void solver_free(adda_gb300_ctx *c);
+int cross_sections(adda_gb300_ctx *c, int nrhs, const double *prop, const double *incpol, double *cext, double *cabs);
+
+} // namespace adda

@@ -78,10 +78,32 @@ size_t adda_gb300_make_particle(int shape, const double *pars, int boxX, int box
 	return idx;
 }
 
-void adda_gb300_rotation(double alpha_deg, double beta_deg, double gamma_deg, double prop[3], double incPolY[3],
-	double incPolX[3])
+void adda_gb300_rotation(const double prop0_in[3], double alpha_deg, double beta_deg, double gamma_deg,
+	double prop[3], double incPolY[3], double incPolX[3])
 {
-	/* laboratory frame: prop_0=(0,0,1), incPolY_0=(0,1,0), incPolX_0=(1,0,0) (param.c:1988-1989, 2116-2119) */
+	/* laboratory frame (param.c:1988-1989, 2116-2131): prop_0 = (0,0,1) unless given (-prop, normalised), and the
+	 * two incident polarisations derived from it */
+	double p0[3] = {0, 0, 1}, y0[3], x0[3];
+	if (prop0_in) {
+		double nn = prop0_in[0] * prop0_in[0] + prop0_in[1] * prop0_in[1] + prop0_in[2] * prop0_in[2];
+		for (int i = 0; i < 3; i++) p0[i] = prop0_in[i] / sqrt(nn);
+	}
+	if (fabs(p0[0]) < 1e-15 && fabs(p0[1]) < 1e-15) { // along z (vAlongZ, cmplx.h:501-505; ROUND_ERR)
+		x0[0] = copysign(1.0, p0[2]);
+		x0[1] = x0[2] = 0;
+		y0[0] = y0[2] = 0;
+		y0[1] = 1;
+	}
+	else {
+		double t = sqrt(1 - p0[2] * p0[2]);
+		x0[0] = p0[0] * p0[2] / t;
+		x0[1] = p0[1] * p0[2] / t;
+		x0[2] = -t;
+		y0[0] = -p0[1] / t;
+		y0[1] = p0[0] / t;
+		y0[2] = 0;
+	}
+	/* InitRotation: zyz Euler matrix applied to prop_0, incPolY_0, incPolX_0 */
 	const double d2r = TWO_PI_D / 360;
 	double a = alpha_deg * d2r, b = beta_deg * d2r, g = gamma_deg * d2r;
 	double ca = cos(a), sa = sin(a), cb = cos(b), sb = sin(b), cg = cos(g), sg = sin(g);
@@ -90,9 +112,9 @@ void adda_gb300_rotation(double alpha_deg, double beta_deg, double gamma_deg, do
 		{-ca * cb * sg - sa * cg, -sa * cb * sg + ca * cg, sb * sg},
 		{ca * sb, sa * sb, cb}};
 	for (int i = 0; i < 3; i++) {
-		prop[i] = m[i][2];
-		incPolY[i] = m[i][1];
-		incPolX[i] = m[i][0];
+		prop[i] = m[i][0] * p0[0] + m[i][1] * p0[1] + m[i][2] * p0[2];
+		incPolY[i] = m[i][0] * y0[0] + m[i][1] * y0[1] + m[i][2] * y0[2];
+		incPolX[i] = m[i][0] * x0[0] + m[i][1] * x0[1] + m[i][2] * x0[2];
 	}
 }
 

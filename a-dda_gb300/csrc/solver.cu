@@ -1,0 +1,1163 @@
+// solver.cu - device-resident Krylov solvers (IterativeSolver, src/iterative.c:1398-1530) and cross sections.
+//
+// Every vector, scalar and reduction stays on the GPU. One iteration is a fixed kernel sequence:
+//   QMR_CS (iterative.c:956-1029):   matvec(v) + [alpha = v.Av fused in its epilogue] -> qmr_s1 -> qmr_v1
+//                                    [v~ update + |v~|^2, v~.v~] -> qmr_s2 -> qmr_v2 [p, x, v, r updates + |r|^2]
+//                                    -> progress
+//   BiCGStab (iterative.c:673-720):  bs_s0 -> bs_v1 [p] -> matvec(p) [v.r~*] -> bs_s1 -> bs_v2 [s, |s|^2] -> bs_s2
+//                                    -> matvec(s) [|t|^2, s.t*] -> bs_s3 -> bs_v3 [x, r, |r|^2, r.r~*] -> progress
+// Scalar kernels run one block per right-hand side: they sum the deterministic per-block partials of the previous
+// kernel in a fixed order and update that RHS's FP64 recurrence scalars (including the breakdown tests and the
+// stagnation counter of ProgressReport, iterative.c:282-318). Several RHS iterate in lockstep; a converged RHS is
+// frozen by its done flag. check_every iterations are captured once as a CUDA graph and replayed; the host reads
+// the done flags only between graph launches.
+//
+// MIXED precision: the Krylov iterations run on complex-float vectors with the FP32 matvec (scalars and
+// reductions stay FP64); an outer loop recomputes the true residual b - A.x with the FP64 matvec (the reference's
+// ResidualNorm2, iterative.c:322-338), accumulates x in FP64 and restarts an FP32 solve on the residual until the
+// FP64 relative residual meets eps.
+//
+// One deliberate difference from the reference: when IF_AUTO picks x_0 = 0, the reference reuses A.b from the
+// initial-field test for the first iteration (matvec_ready, iterative.c:962-965, 691); here the first iteration
+// always computes its matvec. The iterates agree to rounding.
+#include "ctx.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace adda {
+
+struct RhsState {
+	double inprodR, inprodRp1, epsB, resid_scale;
+	int niter, counter, done, status, half, mc, maxiter, x0zero;
+	// QMR_CS
+	double c_old, c_new, om_old, om_new;
+	double2 beta, tautilda, s_old, s_new, alpha, theta, eta, zetat;
+	// BiCGStab
+	double2 ro_old, ro_new, omega, balpha;
+	// coefficients for the vector kernels
+	double2 k0, k1, k2, k3, kib, kr;
+	double d0;
+	double temp; // |b|^2
+};
+
+struct SolverWork {
+	int R = 0;
+	size_t n3 = 0;
+	// FP64 vectors [R][3N]
+	double2 *x64 = nullptr, *r64 = nullptr, *b64 = nullptr, *av64 = nullptr;
+	// Krylov work vectors, stored as double2 (the float solver uses the first half of each)
+	double2 *kv[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+	RhsState *st = nullptr;
+	int *done = nullptr;   // mirror of st[r].done for the matvec early exit
+	double *hist = nullptr;
+	int hist_cap = 0;
+	double *vpart = nullptr; // vector-kernel partials [R][nbv][4]
+	int nbv = 0;
+	double *xpart = nullptr; // cross-section partials
+	int *h_done = nullptr;   // pinned
+	// cached graph
+	cudaGraphExec_t gexec = nullptr;
+	int g_method = -1, g_dbl = -1, g_R = -1, g_K = -1;
+	unsigned long long g_nodes = 0;
+};
+
+namespace {
+
+constexpr int NT = 256;
+
+__device__ __forceinline__ double2 dc(double a, double b) { return make_double2(a, b); }
+__device__ __forceinline__ double2 dmul(double2 a, double2 b) { return dc(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ double2 dadd(double2 a, double2 b) { return dc(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 dsub(double2 a, double2 b) { return dc(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 dscal(double2 a, double s) { return dc(a.x * s, a.y * s); }
+__device__ __forceinline__ double2 dconj(double2 a) { return dc(a.x, -a.y); }
+__device__ __forceinline__ double dabs(double2 a) { return hypot(a.x, a.y); }
+__device__ __forceinline__ double2 ddiv(double2 a, double2 b)
+{
+	// a/b with scaling against overflow (Smith's method)
+	if (fabs(b.x) >= fabs(b.y)) {
+		const double r = b.y / b.x, d = b.x + b.y * r;
+		return dc((a.x + a.y * r) / d, (a.y - a.x * r) / d);
+	}
+	const double r = b.x / b.y, d = b.x * r + b.y;
+	return dc((a.x * r + a.y) / d, (a.y * r - a.x) / d);
+}
+__device__ __forceinline__ double2 dinv(double2 b) { return ddiv(dc(1, 0), b); }
+__device__ __forceinline__ double2 dsqrt(double2 z)
+{
+	const double a = z.x, b = z.y;
+	const double t = sqrt(0.5 * (hypot(a, b) + fabs(a)));
+	if (t == 0) return dc(0, 0);
+	if (a >= 0) return dc(t, b / (2 * t));
+	return dc(fabs(b) / (2 * t), copysign(t, b));
+}
+
+template <typename C> __device__ __forceinline__ C cof(double2 k) { return from_d2<C>(k); }
+
+// block sum of up to 4 values; result valid in thread 0
+__device__ __forceinline__ void block_sum4(double v[4], int nv)
+{
+	__shared__ double sh[4][NT / 32];
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	for (int j = 0; j < nv; j++) {
+		double s = v[j];
+		for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+		if (lane == 0) sh[j][wid] = s;
+	}
+	__syncthreads();
+	if (threadIdx.x == 0)
+		for (int j = 0; j < nv; j++) {
+			double s = 0;
+			for (int w = 0; w < NT / 32; w++) s += sh[j][w];
+			v[j] = s;
+		}
+	__syncthreads();
+}
+
+__device__ __forceinline__ void write_part(double *part, int nbv, double v[4], int nv)
+{
+	block_sum4(v, nv);
+	if (threadIdx.x == 0) {
+		double *o = part + ((size_t)blockIdx.y * nbv + blockIdx.x) * 4;
+		for (int j = 0; j < nv; j++) o[j] = v[j];
+	}
+}
+
+// sum partials of RHS r in a fixed order (all threads participate); result in thread 0
+__device__ __forceinline__ void sum_part(const double *part, size_t nblk, int r, double out[4], int nv)
+{
+	double v[4] = {0, 0, 0, 0};
+	for (size_t b = threadIdx.x; b < nblk; b += blockDim.x)
+		for (int j = 0; j < nv; j++) v[j] += part[((size_t)r * nblk + b) * 4 + j];
+	block_sum4(v, nv);
+	for (int j = 0; j < nv; j++) out[j] = v[j];
+}
+
+#define VLOOP(n3) for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (n3); i += (size_t)gridDim.x * blockDim.x)
+
+// ---------------- initialisation ----------------
+
+// b = S.E (nMult_mat, linalg.c:549); partial |b|^2. E, b FP64.
+__global__ void __launch_bounds__(NT) k_mult_cc(const double2 *E, double2 *b, const double2 *ccs, int per_dip, int nmat,
+	const uint8_t *mat, size_t N, double *part, int nbv)
+{
+	const int r = blockIdx.y;
+	const size_t n3 = 3 * N;
+	double v[4] = {0, 0, 0, 0};
+	VLOOP(n3) {
+		const size_t d = i / 3;
+		const int comp = (int)(i % 3);
+		const double2 s = per_dip ? ccs[((size_t)r * N + d) * 3 + comp] : ccs[((size_t)r * nmat + mat[d]) * 3 + comp];
+		const double2 e = E[(size_t)r * n3 + i];
+		const double2 y = dmul(s, e);
+		b[(size_t)r * n3 + i] = y;
+		v[0] += y.x * y.x + y.y * y.y;
+	}
+	write_part(part, nbv, v, 1);
+}
+
+__global__ void s_init(RhsState *st, int *done, const double *part, int nbv, double eps, int maxiter, int mc,
+	double *hist, int hist_cap, int zero_init)
+{
+	const int r = blockIdx.x;
+	double s[4];
+	sum_part(part, nbv, r, s, 1);
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	memset(&S, 0, sizeof(S));
+	S.temp = s[0];
+	S.resid_scale = 1 / s[0];
+	S.epsB = eps * eps * s[0];
+	S.maxiter = maxiter;
+	S.mc = mc;
+	S.niter = 1;
+	S.counter = 0;
+	S.status = 0;
+	if (zero_init) {
+		S.inprodR = s[0];
+		if (hist_cap > 0) hist[(size_t)r * hist_cap] = sqrt(S.resid_scale * S.inprodR);
+		S.done = !(S.inprodR > S.epsB && S.niter <= S.maxiter);
+		done[r] = S.done;
+	}
+}
+
+// x0 / r0 from b (CalcInitField, iterative.c:1349-1379): zero -> x=0,r=b ; inc -> x=b,r=b-Ab ; auto -> choose
+template <typename C>
+__global__ void __launch_bounds__(NT) k_init_field(RhsState *st, int *done, const C *b, const C *Ab, C *x, C *r,
+	size_t n3, int mode, double *part, int nbv, int stage)
+{
+	const int rr = blockIdx.y;
+	const C *bb = b + rr * n3;
+	if (stage == 0) { // r = b - Ab, partial |r|^2
+		double v[4] = {0, 0, 0, 0};
+		VLOOP(n3) {
+			const C d = csub(bb[i], Ab[rr * n3 + i]);
+			r[rr * n3 + i] = d;
+			const double2 d2 = to_d2(d);
+			v[0] += d2.x * d2.x + d2.y * d2.y;
+		}
+		write_part(part, nbv, v, 1);
+	}
+	else { // choose x0 per RHS: st.x0zero holds 1 for x0=0
+		const bool zero = st[rr].x0zero != 0;
+		VLOOP(n3) {
+			if (zero) {
+				x[rr * n3 + i] = cx<C>(0, 0);
+				r[rr * n3 + i] = bb[i];
+			}
+			else x[rr * n3 + i] = bb[i];
+		}
+	}
+}
+
+__global__ void s_init_choose(RhsState *st, int *done, const double *part, int nbv, int mode, double *hist,
+	int hist_cap)
+{
+	const int r = blockIdx.x;
+	double s[4];
+	sum_part(part, nbv, r, s, 1);
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	S.inprodR = s[0];
+	S.x0zero = 0;
+	if (mode == ADDA_IF_AUTO && S.temp < S.inprodR) {
+		S.inprodR = S.temp;
+		S.x0zero = 1; // x0 = 0
+	}
+	if (hist_cap > 0) hist[(size_t)r * hist_cap] = sqrt(S.resid_scale * S.inprodR);
+	S.done = !(S.inprodR > S.epsB && S.niter <= S.maxiter);
+	done[r] = S.done;
+}
+
+// reductions for the method initialisation: slot 0 = |a|^2; slots 1,2 = sum a.u (mode 0, bilinear) or
+// sum a.conj(u) (mode 1) -- the same slots the iteration kernels use for these dot products
+template <typename C>
+__global__ void __launch_bounds__(NT) k_dot(const C *a, const C *u, size_t n3, int mode, double *part, int nbv)
+{
+	const int r = blockIdx.y;
+	double v[4] = {0, 0, 0, 0};
+	VLOOP(n3) {
+		const double2 x = to_d2(a[r * n3 + i]);
+		const double2 y = to_d2(u[r * n3 + i]);
+		v[0] += x.x * x.x + x.y * x.y;
+		if (mode == 0) {
+			v[1] += x.x * y.x - x.y * y.y;
+			v[2] += x.x * y.y + x.y * y.x;
+		}
+		else {
+			v[1] += x.x * y.x + x.y * y.y;
+			v[2] += x.y * y.x - x.x * y.y;
+		}
+	}
+	write_part(part, nbv, v, 3);
+}
+
+template <typename C> __global__ void __launch_bounds__(NT) k_copy(C *dst, const C *src, size_t n3, const int *done)
+{
+	const int r = blockIdx.y;
+	if (done && done[r]) return;
+	VLOOP(n3) dst[r * n3 + i] = src[r * n3 + i];
+}
+
+// QMR_CS PHASE_INIT (iterative.c:939-954): beta = sqrt(r.r), omega = |r|/|beta|, v = r/beta, tau~ = omega*beta
+__global__ void qmr_s_init(RhsState *st, const double *part, int nbv)
+{
+	const int r = blockIdx.x;
+	double s[4];
+	sum_part(part, nbv, r, s, 3);
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	S.om_old = 0;
+	S.beta = dsqrt(dc(s[1], s[2]));
+	S.om_new = sqrt(S.inprodR) / dabs(S.beta);
+	S.kib = dinv(S.beta);
+	S.tautilda = dscal(S.beta, S.om_new);
+	S.c_new = S.c_old = 1;
+	S.s_new = S.s_old = dc(0, 0);
+}
+
+template <typename C> __global__ void __launch_bounds__(NT) qmr_v_init(const RhsState *st, C *v, const C *r, size_t n3)
+{
+	const int rr = blockIdx.y;
+	if (st[rr].done) return;
+	const C k = cof<C>(st[rr].kib);
+	VLOOP(n3) v[rr * n3 + i] = cmul(k, r[rr * n3 + i]);
+}
+
+// ---------------- QMR_CS iteration ----------------
+
+__global__ void qmr_s1(RhsState *st, int *done, const double *part, size_t nblk)
+{
+	const int r = blockIdx.x;
+	if (st[r].done) return;
+	double s[4];
+	sum_part(part, nblk, r, s, 3);
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	if (1 / (S.om_new * S.om_new) < 1e-10) { // iterative.c:958-960
+		S.status = ADDA_GB300_EBREAKDOWN;
+		S.done = 1;
+		done[r] = 1;
+		return;
+	}
+	const double2 alpha = dc(s[1], s[2]);
+	S.alpha = alpha;
+	S.theta = dscal(dmul(dconj(S.s_old), S.beta), S.om_old);
+	S.eta = dadd(dscal(S.beta, S.c_old * S.c_new * S.om_old), dscal(dmul(alpha, dconj(S.s_new)), S.om_new));
+	S.zetat = dsub(dscal(alpha, S.c_new * S.om_new), dscal(dmul(S.s_new, S.beta), S.c_old * S.om_old));
+	S.k0 = (S.niter == 1) ? dc(0, 0) : dc(-S.beta.x, -S.beta.y);
+	S.k1 = dc(-alpha.x, -alpha.y);
+	S.om_old = S.om_new;
+}
+
+// v~ = k0*v~ + k1*v + A.v ; partials sum re^2, im^2, re*im (nDotProdSelf_conj_Norm2, linalg.c:127)
+template <typename C>
+__global__ void __launch_bounds__(NT) qmr_v1(const RhsState *st, C *vt, const C *v, const C *Av, size_t n3,
+	double *part, int nbv)
+{
+	const int r = blockIdx.y;
+	if (st[r].done) return;
+	const C k0 = cof<C>(st[r].k0), k1 = cof<C>(st[r].k1);
+	double s[4] = {0, 0, 0, 0};
+	VLOOP(n3) {
+		const size_t j = r * n3 + i;
+		const C y = cadd(cadd(cmul(k0, vt[j]), cmul(k1, v[j])), Av[j]);
+		vt[j] = y;
+		const double2 d = to_d2(y);
+		s[0] += d.x * d.x;
+		s[1] += d.y * d.y;
+		s[2] += d.x * d.y;
+	}
+	write_part(part, nbv, s, 3);
+}
+
+__global__ void qmr_s2(RhsState *st, const double *part, int nbv)
+{
+	const int r = blockIdx.x;
+	if (st[r].done) return;
+	double s[4];
+	sum_part(part, nbv, r, s, 3);
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	const double nrm = s[0] + s[1];
+	S.beta = dsqrt(dc(s[0] - s[1], 2 * s[2]));
+	S.om_new = sqrt(nrm) / dabs(S.beta);
+	const double zt2 = S.zetat.x * S.zetat.x + S.zetat.y * S.zetat.y;
+	const double zabs = sqrt(zt2 + nrm);
+	const double zt = sqrt(zt2);
+	const double2 zeta = (zt < 1e-40) ? dc(zabs, 0) : dscal(S.zetat, zabs / zt);
+	S.c_old = S.c_new;
+	S.c_new = zt / zabs;
+	S.s_old = S.s_new;
+	S.s_new = ddiv(dscal(S.beta, S.om_new), zeta);
+	const double2 t4 = dinv(zeta);
+	if (S.niter == 1) {
+		S.k0 = dc(0, 0);
+		S.k1 = dc(0, 0);
+	}
+	else {
+		const double2 t2 = dmul(dc(-S.eta.x, -S.eta.y), t4);
+		S.k1 = t2;
+		S.k0 = (S.niter == 2) ? dc(0, 0) : dmul(dc(-S.theta.x, -S.theta.y), t4);
+	}
+	S.k2 = t4;
+	const double2 tau = dscal(S.tautilda, S.c_new);
+	S.tautilda = dmul(dc(-S.s_new.x, -S.s_new.y), S.tautilda);
+	S.k3 = tau;
+	S.kib = dinv(S.beta);
+	S.d0 = S.s_new.x * S.s_new.x + S.s_new.y * S.s_new.y;
+	S.kr = dscal(S.tautilda, S.c_new / S.om_new);
+}
+
+// p_old = k0*p_old + k1*p_new + k2*v (becomes p_new); x += k3*p; v~ *= 1/beta (becomes v); r = d0*r + kr*v;
+// partial |r|^2
+template <typename C>
+__global__ void __launch_bounds__(NT) qmr_v2(const RhsState *st, C *po, const C *pn, const C *v, C *vt, C *x, C *rv,
+	size_t n3, double *part, int nbv)
+{
+	const int r = blockIdx.y;
+	if (st[r].done) return;
+	const RhsState &S = st[r];
+	const C k0 = cof<C>(S.k0), k1 = cof<C>(S.k1), k2 = cof<C>(S.k2), k3 = cof<C>(S.k3), kib = cof<C>(S.kib),
+		kr = cof<C>(S.kr);
+	const decltype(k0.x) d0 = (decltype(k0.x))S.d0;
+	double s[4] = {0, 0, 0, 0};
+	VLOOP(n3) {
+		const size_t j = r * n3 + i;
+		const C p = cadd(cadd(cmul(k0, po[j]), cmul(k1, pn[j])), cmul(k2, v[j]));
+		po[j] = p;
+		x[j] = cadd(x[j], cmul(k3, p));
+		const C vn = cmul(vt[j], kib);
+		vt[j] = vn;
+		const C rn = cadd(cscale(rv[j], d0), cmul(kr, vn));
+		rv[j] = rn;
+		const double2 d = to_d2(rn);
+		s[0] += d.x * d.x + d.y * d.y;
+	}
+	write_part(part, nbv, s, 1);
+}
+
+// ProgressReport (iterative.c:282-306) + loop condition (iterative.c:1467); partial |r|^2 in slot 0 unless half
+__global__ void s_progress(RhsState *st, int *done, const double *part, int nbv, double *hist, int hist_cap, int bcgs)
+{
+	const int r = blockIdx.x;
+	if (st[r].done) return;
+	double s[4];
+	sum_part(part, nbv, r, s, 2);
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	if (!S.half) S.inprodRp1 = s[0];
+	if (bcgs && !S.half) S.ro_old = S.ro_new; // the next bs_s0 sums the r.r~* partials of bs_v3 itself
+	if (S.inprodRp1 <= S.inprodR) {
+		S.inprodR = S.inprodRp1;
+		S.counter = 0;
+	}
+	else S.counter++;
+	if (S.niter < hist_cap) hist[(size_t)r * hist_cap + S.niter] = sqrt(S.resid_scale * S.inprodRp1);
+	S.niter++;
+	S.done = !(S.inprodR > S.epsB && S.niter <= S.maxiter && S.counter <= S.mc);
+	done[r] = S.done;
+}
+
+// ---------------- BiCGStab iteration ----------------
+
+// ro_new = r.r~* (partial slots 1,2 of the previous bs_v3, or of the initial k_dot for the first iteration)
+__global__ void bs_s0(RhsState *st, int *done, const double *part, int nbv)
+{
+	const int r = blockIdx.x;
+	if (st[r].done) return;
+	double s[4];
+	sum_part(part, nbv, r, s, 3);
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	const double2 ro = dc(s[1], s[2]);
+	S.ro_new = ro;
+	if (S.niter == 1) {
+		S.k0 = dc(0, 0);
+		S.k1 = dc(0, 0);
+		return;
+	}
+	const double2 t1 = dmul(ro, S.balpha), t2 = dmul(S.ro_old, S.omega);
+	if (dabs(t2) / dabs(t1) < 1e-10) { // iterative.c:682-684
+		S.status = ADDA_GB300_EBREAKDOWN;
+		S.done = 1;
+		done[r] = 1;
+		return;
+	}
+	const double2 beta = ddiv(t1, t2);
+	S.k0 = beta;
+	const double2 bo = dmul(beta, S.omega);
+	S.k1 = dc(-bo.x, -bo.y);
+}
+
+// p = k0*p + k1*v + r
+template <typename C>
+__global__ void __launch_bounds__(NT) bs_v1(const RhsState *st, C *p, const C *v, const C *rv, size_t n3)
+{
+	const int r = blockIdx.y;
+	if (st[r].done) return;
+	const C k0 = cof<C>(st[r].k0), k1 = cof<C>(st[r].k1);
+	VLOOP(n3) {
+		const size_t j = r * n3 + i;
+		p[j] = cadd(cadd(cmul(k0, p[j]), cmul(k1, v[j])), rv[j]);
+	}
+}
+
+// alpha = ro_new / (v.r~*) (matvec epilogue slot 1,2)
+__global__ void bs_s1(RhsState *st, int *done, const double *part, size_t nblk)
+{
+	const int r = blockIdx.x;
+	if (st[r].done) return;
+	double s[4];
+	sum_part(part, nblk, r, s, 3);
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	const double2 t = dc(s[1], s[2]);
+	if (dabs(t) / dabs(S.ro_new) < 1e-10) { // iterative.c:695-697
+		S.status = ADDA_GB300_EBREAKDOWN;
+		S.done = 1;
+		done[r] = 1;
+		return;
+	}
+	S.balpha = ddiv(S.ro_new, t);
+	S.k0 = dc(-S.balpha.x, -S.balpha.y);
+}
+
+// s = k0*v + r ; partial |s|^2
+template <typename C>
+__global__ void __launch_bounds__(NT) bs_v2(const RhsState *st, C *sv, const C *v, const C *rv, size_t n3,
+	double *part, int nbv)
+{
+	const int r = blockIdx.y;
+	if (st[r].done) return;
+	const C k0 = cof<C>(st[r].k0);
+	double s[4] = {0, 0, 0, 0};
+	VLOOP(n3) {
+		const size_t j = r * n3 + i;
+		const C y = cadd(cmul(k0, v[j]), rv[j]);
+		sv[j] = y;
+		const double2 d = to_d2(y);
+		s[0] += d.x * d.x + d.y * d.y;
+	}
+	write_part(part, nbv, s, 1);
+}
+
+__global__ void bs_s2(RhsState *st, const double *part, int nbv)
+{
+	const int r = blockIdx.x;
+	if (st[r].done) return;
+	double s[4];
+	sum_part(part, nbv, r, s, 1);
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	S.inprodRp1 = s[0];
+	S.half = (S.inprodRp1 < S.epsB) ? 1 : 0; // converged at the half step (iterative.c:703-707)
+}
+
+// omega = s.t* / |t|^2 (matvec epilogue: slot 0 = |t|^2, slots 1,2 = s.t*)
+__global__ void bs_s3(RhsState *st, const double *part, size_t nblk)
+{
+	const int r = blockIdx.x;
+	if (st[r].done) return;
+	double s[4];
+	sum_part(part, nblk, r, s, 3);
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	if (!S.half) S.omega = dscal(dc(s[1], s[2]), 1 / s[0]);
+}
+
+// x += alpha*p (+ omega*s); r = -omega*t + s; partials |r|^2, r.r~*
+template <typename C>
+__global__ void __launch_bounds__(NT) bs_v3(const RhsState *st, C *x, const C *p, const C *sv, const C *t, C *rv,
+	const C *rt, size_t n3, double *part, int nbv)
+{
+	const int r = blockIdx.y;
+	if (st[r].done) return;
+	const RhsState &S = st[r];
+	const C a = cof<C>(S.balpha), om = cof<C>(S.omega), mom = cof<C>(dc(-S.omega.x, -S.omega.y));
+	const bool half = S.half != 0;
+	double s[4] = {0, 0, 0, 0};
+	VLOOP(n3) {
+		const size_t j = r * n3 + i;
+		if (half) {
+			x[j] = cadd(x[j], cmul(a, p[j]));
+			continue;
+		}
+		x[j] = cadd(x[j], cadd(cmul(a, p[j]), cmul(om, sv[j])));
+		const C y = cadd(cmul(mom, t[j]), sv[j]);
+		rv[j] = y;
+		const double2 d = to_d2(y), u = to_d2(rt[j]);
+		s[0] += d.x * d.x + d.y * d.y;
+		s[1] += d.x * u.x + d.y * u.y;
+		s[2] += d.y * u.x - d.x * u.y;
+	}
+	write_part(part, nbv, s, 3);
+}
+
+// ---------------- FP64 helpers for the refinement loop and the results ----------------
+
+// x64 (+)= d (float or double), depending on accumulate
+template <typename C>
+__global__ void __launch_bounds__(NT) k_accum(double2 *x64, const C *d, size_t n3, int accumulate, const int *skip)
+{
+	const int r = blockIdx.y;
+	if (skip && skip[r]) return;
+	VLOOP(n3) {
+		const double2 v = to_d2(d[r * n3 + i]);
+		x64[r * n3 + i] = accumulate ? make_double2(x64[r * n3 + i].x + v.x, x64[r * n3 + i].y + v.y) : v;
+	}
+}
+
+// r64 = b64 - Ax64; partial |r|^2; also the float copy of r64 for the next inner solve
+__global__ void __launch_bounds__(NT) k_resid64(const double2 *b, const double2 *Ax, double2 *r64, float2 *rf,
+	size_t n3, double *part, int nbv)
+{
+	const int r = blockIdx.y;
+	double s[4] = {0, 0, 0, 0};
+	VLOOP(n3) {
+		const size_t j = r * n3 + i;
+		const double2 d = make_double2(b[j].x - Ax[j].x, b[j].y - Ax[j].y);
+		r64[j] = d;
+		rf[j] = make_float2((float)d.x, (float)d.y);
+		s[0] += d.x * d.x + d.y * d.y;
+	}
+	write_part(part, nbv, s, 1);
+}
+
+__global__ void __launch_bounds__(NT) k_d2f(float2 *dst, const double2 *src, size_t n)
+{
+	for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+		dst[i] = make_float2((float)src[i].x, (float)src[i].y);
+}
+
+// p = S.x (iterative.c:1527)
+__global__ void __launch_bounds__(NT) k_pvec(const double2 *x, double2 *p, const double2 *ccs, int per_dip, int nmat,
+	const uint8_t *mat, size_t N)
+{
+	const int r = blockIdx.y;
+	const size_t n3 = 3 * N;
+	VLOOP(n3) {
+		const size_t d = i / 3;
+		const int comp = (int)(i % 3);
+		const double2 s = per_dip ? ccs[((size_t)r * N + d) * 3 + comp] : ccs[((size_t)r * nmat + mat[d]) * 3 + comp];
+		p[(size_t)r * n3 + i] = dmul(s, x[(size_t)r * n3 + i]);
+	}
+}
+
+// cross-section sums per RHS: sum_j P_j exp(-i kd n.pos_j) (CalcFieldFree, crosssec.c:506-586) and
+// sum_j sum_c (-Im(1/cc) - 2k^3/3)|P_jc|^2 (AbsCross, crosssec.c:866-882)
+__global__ void __launch_bounds__(NT) k_cross(const double2 *P, const uint16_t *pos, const double2 *cc, int per_dip,
+	int nmat, const uint8_t *mat, size_t N, const double *prop, double kd, double k3, double *part, int nbv)
+{
+	const int r = blockIdx.y;
+	const double n0 = prop[3 * r], n1 = prop[3 * r + 1], n2 = prop[3 * r + 2];
+	double s[7] = {0, 0, 0, 0, 0, 0, 0};
+	for (size_t d = blockIdx.x * (size_t)blockDim.x + threadIdx.x; d < N; d += (size_t)gridDim.x * blockDim.x) {
+		const double ph = -kd * (n0 * pos[3 * d] + n1 * pos[3 * d + 1] + n2 * pos[3 * d + 2]);
+		double sn, cs;
+		sincos(ph, &sn, &cs);
+		for (int c = 0; c < 3; c++) {
+			const double2 p = P[((size_t)r * N + d) * 3 + c];
+			s[2 * c] += p.x * cs - p.y * sn;
+			s[2 * c + 1] += p.x * sn + p.y * cs;
+			const double2 a = per_dip ? cc[((size_t)r * N + d) * 3 + c] : cc[((size_t)r * nmat + mat[d]) * 3 + c];
+			const double im_inv = -a.y / (a.x * a.x + a.y * a.y); // Im(1/cc)
+			const double mult = -im_inv - 2 * k3 / 3;
+			s[6] += mult * (p.x * p.x + p.y * p.y);
+		}
+	}
+	__shared__ double sh[7][NT / 32];
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	for (int j = 0; j < 7; j++) {
+		double v = s[j];
+		for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+		if (lane == 0) sh[j][wid] = v;
+	}
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		double *o = part + ((size_t)r * nbv + blockIdx.x) * 8;
+		for (int j = 0; j < 7; j++) {
+			double v = 0;
+			for (int w = 0; w < NT / 32; w++) v += sh[j][w];
+			o[j] = v;
+		}
+	}
+}
+
+} // namespace
+
+// =====================================================================================================================
+
+static int ensure_work(adda_gb300_ctx *c, int R, int hist_cap)
+{
+	SolverWork *w = c->sw;
+	if (!w) {
+		w = c->sw = new SolverWork();
+		const size_t n3 = 3 * c->N;
+		const size_t Rm = c->Rmax;
+		w->n3 = n3;
+		const size_t vb = sizeof(double2) * Rm * std::max<size_t>(n3, 1);
+		ADDA_CUDA(cudaMalloc(&w->x64, vb));
+		ADDA_CUDA(cudaMalloc(&w->r64, vb));
+		ADDA_CUDA(cudaMalloc(&w->b64, vb));
+		ADDA_CUDA(cudaMalloc(&w->av64, vb));
+		for (int i = 0; i < 7; i++) ADDA_CUDA(cudaMalloc(&w->kv[i], vb));
+		ADDA_CUDA(cudaMalloc(&w->st, sizeof(RhsState) * Rm));
+		ADDA_CUDA(cudaMalloc(&w->done, sizeof(int) * Rm));
+		ADDA_CUDA(cudaMallocHost(&w->h_done, sizeof(int) * Rm));
+		w->nbv = (int)std::max<size_t>(1, std::min<size_t>(152 * 8, (n3 + 4 * NT - 1) / (4 * NT)));
+		ADDA_CUDA(cudaMalloc(&w->vpart, sizeof(double) * Rm * w->nbv * 4));
+		ADDA_CUDA(cudaMalloc(&w->xpart, sizeof(double) * Rm * w->nbv * 8));
+		if (!c->pvec64) ADDA_CUDA(cudaMalloc(&c->pvec64, vb));
+	}
+	if (hist_cap > w->hist_cap) {
+		if (w->hist) cudaFree(w->hist);
+		w->hist = nullptr;
+		if (w->gexec) cudaGraphExecDestroy(w->gexec); // the cached graph holds the old pointer
+		w->gexec = nullptr;
+		ADDA_CUDA(cudaMalloc(&w->hist, sizeof(double) * c->Rmax * hist_cap));
+		w->hist_cap = hist_cap;
+	}
+	if (!w->hist) {
+		ADDA_CUDA(cudaMalloc(&w->hist, sizeof(double) * c->Rmax * 1));
+		w->hist_cap = 1;
+	}
+	w->R = R;
+	return ADDA_GB300_OK;
+}
+
+void solver_free(adda_gb300_ctx *c)
+{
+	SolverWork *w = c->sw;
+	if (!w) return;
+	if (w->gexec) cudaGraphExecDestroy(w->gexec);
+	void *b[] = {w->x64, w->r64, w->b64, w->av64, w->st, w->done, w->hist, w->vpart, w->xpart};
+	for (void *p : b)
+		if (p) cudaFree(p);
+	for (int i = 0; i < 7; i++)
+		if (w->kv[i]) cudaFree(w->kv[i]);
+	if (w->h_done) cudaFreeHost(w->h_done);
+	delete w;
+	c->sw = nullptr;
+}
+
+// Krylov vector roles inside kv[] (as typed pointers)
+template <typename C> struct KV {
+	C *x, *r, *p, *Av, *v1, *v2, *v3;
+};
+
+template <typename C> static KV<C> kvec(SolverWork *w)
+{
+	KV<C> k;
+	k.x = (C *)w->kv[0];
+	k.r = (C *)w->kv[1];
+	k.p = (C *)w->kv[2];
+	k.Av = (C *)w->kv[3];
+	k.v1 = (C *)w->kv[4];
+	k.v2 = (C *)w->kv[5];
+	k.v3 = (C *)w->kv[6];
+	return k;
+}
+
+// enqueue one Krylov iteration; parity selects the QMR_CS vector roles (v<->v~, p_new<->p_old swap each iteration)
+template <typename T>
+static int enqueue_iter(adda_gb300_ctx *c, SolverWork *w, int method, int R, int parity)
+{
+	typedef typename CxT<T>::type C;
+	const bool dbl = sizeof(T) == 8;
+	KV<C> k = kvec<C>(w);
+	const size_t n3 = w->n3;
+	const dim3 gv(w->nbv, R);
+	const size_t nblk = matvec_partial_blocks(c, dbl);
+	cudaStream_t s = c->stream;
+	int rc;
+	if (method == ADDA_ITER_QMR_CS) {
+		C *v = parity ? k.v2 : k.v1, *vt = parity ? k.v1 : k.v2;
+		C *pn = parity ? k.v3 : k.p, *po = parity ? k.p : k.v3;
+		MvEpi e{EPI_DOT_ARG, nullptr, c->partial};
+		if ((rc = matvec_run<T>(c, R, v, k.Av, 0, e, w->done))) return rc;
+		qmr_s1<<<R, NT, 0, s>>>(w->st, w->done, c->partial, nblk);
+		ADDA_LAUNCHED();
+		qmr_v1<C><<<gv, NT, 0, s>>>(w->st, vt, v, k.Av, n3, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+		qmr_s2<<<R, NT, 0, s>>>(w->st, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+		qmr_v2<C><<<gv, NT, 0, s>>>(w->st, po, pn, v, vt, k.x, k.r, n3, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+		s_progress<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv, w->hist, w->hist_cap, 0);
+		ADDA_LAUNCHED();
+	}
+	else {
+		C *v = k.v1, *sv = k.v2, *rt = k.v3;
+		bs_s0<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+		bs_v1<C><<<gv, NT, 0, s>>>(w->st, k.p, v, k.r, n3);
+		ADDA_LAUNCHED();
+		MvEpi e1{EPI_DOT_U_CONJ, rt, c->partial};
+		if ((rc = matvec_run<T>(c, R, k.p, v, 0, e1, w->done))) return rc;
+		bs_s1<<<R, NT, 0, s>>>(w->st, w->done, c->partial, nblk);
+		ADDA_LAUNCHED();
+		bs_v2<C><<<gv, NT, 0, s>>>(w->st, sv, v, k.r, n3, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+		bs_s2<<<R, NT, 0, s>>>(w->st, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+		MvEpi e2{EPI_NORM | EPI_DOT_ARG_CONJ, nullptr, c->partial};
+		if ((rc = matvec_run<T>(c, R, sv, k.Av, 0, e2, w->done))) return rc;
+		bs_s3<<<R, NT, 0, s>>>(w->st, c->partial, nblk);
+		ADDA_LAUNCHED();
+		bs_v3<C><<<gv, NT, 0, s>>>(w->st, k.x, k.p, sv, k.Av, k.r, rt, n3, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+		s_progress<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv, w->hist, w->hist_cap, 1);
+		ADDA_LAUNCHED();
+	}
+	return ADDA_GB300_OK;
+}
+
+// Krylov solve of A.x = b on the typed vectors (b given in k.r on entry for zero init, or in bsrc). Runs until all
+// RHS are done. Returns via st on the device.
+template <typename T>
+static int krylov(adda_gb300_ctx *c, SolverWork *w, int method, int R, int K, unsigned long long *iters_run)
+{
+	typedef typename CxT<T>::type C;
+	const bool dbl = sizeof(T) == 8;
+	KV<C> k = kvec<C>(w);
+	const size_t n3 = w->n3;
+	const dim3 gv(w->nbv, R);
+	cudaStream_t s = c->stream;
+	// method initialisation (PHASE_INIT)
+	if (method == ADDA_ITER_QMR_CS) {
+		k_dot<C><<<gv, NT, 0, s>>>(k.r, k.r, n3, 0, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+		qmr_s_init<<<R, NT, 0, s>>>(w->st, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+		qmr_v_init<C><<<gv, NT, 0, s>>>(w->st, k.v1, k.r, n3);
+		ADDA_LAUNCHED();
+	}
+	else {
+		k_copy<C><<<gv, NT, 0, s>>>(k.v3, k.r, n3, nullptr);
+		ADDA_LAUNCHED();
+		// r.r~* for the first iteration's bs_s0 (slots 1,2)
+		k_dot<C><<<gv, NT, 0, s>>>(k.r, k.v3, n3, 1, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+	}
+	// graph of K iterations (K even keeps the QMR_CS roles periodic)
+	if (!w->gexec || w->g_method != method || w->g_dbl != (int)dbl || w->g_R != R || w->g_K != K) {
+		if (w->gexec) cudaGraphExecDestroy(w->gexec);
+		w->gexec = nullptr;
+		cudaGraph_t g;
+		const unsigned long long before = g_launches.load();
+		ADDA_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+		int rc = ADDA_GB300_OK;
+		for (int it = 0; it < K && !rc; it++) rc = enqueue_iter<T>(c, w, method, R, it & 1);
+		cudaGraph_t gtmp = nullptr;
+		cudaError_t ec = cudaStreamEndCapture(s, &gtmp);
+		if (rc) {
+			if (gtmp) cudaGraphDestroy(gtmp);
+			return rc;
+		}
+		if (ec != cudaSuccess) {
+			set_error(std::string("graph capture: ") + cudaGetErrorString(ec));
+			return ADDA_GB300_ECUDA;
+		}
+		g = gtmp;
+		ADDA_CUDA(cudaGraphInstantiate(&w->gexec, g, 0));
+		cudaGraphDestroy(g);
+		w->g_nodes = g_launches.load() - before; // kernels per graph launch (counted during capture)
+		g_launches.fetch_sub(w->g_nodes);        // capture itself launched nothing
+		w->g_method = method;
+		w->g_dbl = dbl;
+		w->g_R = R;
+		w->g_K = K;
+	}
+	unsigned long long n = 0;
+	for (;;) {
+		ADDA_CUDA(cudaMemcpyAsync(w->h_done, w->done, sizeof(int) * R, cudaMemcpyDeviceToHost, s));
+		ADDA_CUDA(cudaStreamSynchronize(s));
+		bool all = true;
+		for (int r = 0; r < R; r++) all = all && w->h_done[r];
+		if (all) break;
+		ADDA_CUDA(cudaGraphLaunch(w->gexec, s));
+		count_launch(w->g_nodes);
+		n += K;
+	}
+	if (iters_run) *iters_run = n;
+	return ADDA_GB300_OK;
+}
+
+static int check_params(const adda_gb300_solve_params *sp)
+{
+	if ((sp->method != ADDA_ITER_QMR_CS && sp->method != ADDA_ITER_BICGSTAB) ||
+		(sp->precision != ADDA_PREC_FP64 && sp->precision != ADDA_PREC_MIXED) || !(sp->eps > 0) || sp->maxiter < 0 ||
+		(sp->init_field != ADDA_IF_AUTO && sp->init_field != ADDA_IF_ZERO && sp->init_field != ADDA_IF_INC)) {
+		set_error("solve: unsupported parameters");
+		return ADDA_GB300_EINVAL;
+	}
+	return ADDA_GB300_OK;
+}
+
+// the solve on device-resident data: d_einc [R][3N] FP64; leaves x in w->x64 and p = S.x in c->pvec64
+static int solve_core_impl(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int R, const double2 *d_einc,
+	adda_gb300_rhs_stats *stats);
+
+static int solve_core(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int R, const double2 *d_einc,
+	adda_gb300_rhs_stats *stats)
+{
+	cudaEvent_t e0, e1;
+	ADDA_CUDA(cudaEventCreate(&e0));
+	ADDA_CUDA(cudaEventCreate(&e1));
+	ADDA_CUDA(cudaEventRecord(e0, c->stream));
+	int rc = solve_core_impl(c, sp, R, d_einc, stats);
+	if (!rc) {
+		cudaEventRecord(e1, c->stream);
+		cudaEventSynchronize(e1);
+		float ms = 0;
+		cudaEventElapsedTime(&ms, e0, e1);
+		c->last_solve_ms = ms;
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	return rc;
+}
+
+static int solve_core_impl(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int R, const double2 *d_einc,
+	adda_gb300_rhs_stats *stats)
+{
+	SolverWork *w = c->sw;
+	int rc;
+	const size_t n3 = w->n3;
+	cudaStream_t s = c->stream;
+	const dim3 gv(w->nbv, R);
+	const int mc = (sp->method == ADDA_ITER_BICGSTAB) ? 30000 : 50000; // iterative.c:118-125
+	int K = sp->check_every > 0 ? sp->check_every : 8;
+	if (K % 2) K++;
+	std::vector<adda_gb300_rhs_stats> st(R);
+	for (auto &x : st) memset(&x, 0, sizeof(x));
+	std::vector<RhsState> hs(R);
+	// b = S.Einc in FP64
+	k_mult_cc<<<gv, NT, 0, s>>>(d_einc, w->b64, c->ccs64, c->per_dip, c->nmat, c->d_mat, c->N, w->vpart, w->nbv);
+	ADDA_LAUNCHED();
+	ADDA_CUDA(cudaMemsetAsync(w->hist, 0, sizeof(double) * R * w->hist_cap, s));
+	for (int i = 0; i < 7; i++) ADDA_CUDA(cudaMemsetAsync(w->kv[i], 0, sizeof(double2) * R * n3, s));
+	if (sp->precision == ADDA_PREC_FP64) {
+		typedef double2 C;
+		KV<C> k = kvec<C>(w);
+		const int zero = sp->init_field == ADDA_IF_ZERO;
+		s_init<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv, sp->eps, sp->maxiter, mc, w->hist, w->hist_cap, zero);
+		ADDA_LAUNCHED();
+		if (zero) {
+			k_copy<C><<<gv, NT, 0, s>>>(k.r, w->b64, n3, nullptr);
+			ADDA_LAUNCHED();
+		}
+		else {
+			MvEpi e{EPI_NONE, nullptr, c->partial};
+			if ((rc = matvec_run<double>(c, R, w->b64, k.Av, 0, e, nullptr))) return rc;
+			k_init_field<C><<<gv, NT, 0, s>>>(w->st, w->done, w->b64, k.Av, k.x, k.r, n3, sp->init_field, w->vpart,
+				w->nbv, 0);
+			ADDA_LAUNCHED();
+			s_init_choose<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv, sp->init_field, w->hist, w->hist_cap);
+			ADDA_LAUNCHED();
+			k_init_field<C><<<gv, NT, 0, s>>>(w->st, w->done, w->b64, k.Av, k.x, k.r, n3, sp->init_field, w->vpart,
+				w->nbv, 1);
+			ADDA_LAUNCHED();
+		}
+		unsigned long long iters = 0;
+		if ((rc = krylov<double>(c, w, sp->method, R, K, &iters))) return rc;
+		ADDA_CUDA(cudaMemcpyAsync(hs.data(), w->st, sizeof(RhsState) * R, cudaMemcpyDeviceToHost, s));
+		ADDA_CUDA(cudaStreamSynchronize(s));
+		ADDA_CUDA(cudaMemcpyAsync(w->x64, k.x, sizeof(double2) * R * n3, cudaMemcpyDeviceToDevice, s));
+		for (int r = 0; r < R; r++) {
+			st[r].niter = hs[r].niter - 1;
+			st[r].status = hs[r].status;
+			if (!st[r].status && hs[r].inprodR > hs[r].epsB)
+				st[r].status = (hs[r].niter > hs[r].maxiter) ? ADDA_GB300_EMAXITER : ADDA_GB300_ESTAGNATION;
+			st[r].resid = sqrt(hs[r].resid_scale * hs[r].inprodR);
+			const int mpi = sp->method == ADDA_ITER_BICGSTAB ? 2 : 1;
+			st[r].matvecs_fp64 = (zero ? 0 : 1) + mpi * st[r].niter;
+		}
+	}
+	else {
+		// ---- mixed precision: FP32 Krylov inside FP64 refinement ----
+		typedef float2 C;
+		KV<C> k = kvec<C>(w);
+		const int maxref = sp->max_refine > 0 ? sp->max_refine : 10;
+		// outer FP64 bookkeeping per RHS
+		std::vector<double> temp(R), inprod64(R, 0.0), epsB64(R);
+		std::vector<int> odone(R, 0), iters(R, 0), nmv32(R, 0), nmv64(R, 0), nref(R, 0), status(R, 0);
+		// |b|^2 from the k_mult_cc partials
+		ADDA_CUDA(cudaMemsetAsync(c->d_red, 0, sizeof(double) * 4 * R, s));
+		if ((rc = reduce_partials(c, R, w->vpart, w->nbv, c->d_red))) return rc;
+		std::vector<double> red(4 * R);
+		ADDA_CUDA(cudaMemcpyAsync(red.data(), c->d_red, sizeof(double) * 4 * R, cudaMemcpyDeviceToHost, s));
+		ADDA_CUDA(cudaStreamSynchronize(s));
+		for (int r = 0; r < R; r++) {
+			temp[r] = red[4 * r];
+			epsB64[r] = sp->eps * sp->eps * temp[r];
+		}
+		// inner right-hand side: b (step 0) in float, kept in k.v3
+		k_d2f<<<(int)std::min<size_t>((R * n3 + NT - 1) / NT, 8192), NT, 0, s>>>(k.v3, w->b64, R * n3);
+		ADDA_LAUNCHED();
+		double inner_eps0 = sp->inner_eps > 0 ? sp->inner_eps : 0.5 * sp->eps;
+		int *d_odone = w->done; // reused below as skip flags after the inner solve (copied from host)
+		for (int step = 0; step <= maxref; step++) {
+			// inner solve: A d = rhs (rhs float in k.v3 on entry); init per the user's field mode at step 0
+			std::vector<double> eps_in(R);
+			for (int r = 0; r < R; r++) {
+				if (step == 0) eps_in[r] = inner_eps0;
+				else {
+					const double rho = sqrt(epsB64[r] / std::max(inprod64[r], 1e-300));
+					eps_in[r] = std::min(0.5, std::max(0.5 * rho, 2e-6));
+				}
+			}
+			// scalar init with |rhs|^2 (float rhs -> FP64 reduction)
+			{
+				KV<C> kk = k;
+				k_dot<C><<<gv, NT, 0, s>>>(kk.v3, kk.v3, n3, 1, w->vpart, w->nbv);
+				ADDA_LAUNCHED();
+				// per-RHS eps differs: run s_init per RHS block with its own eps via a small host loop
+				for (int r = 0; r < R; r++) {
+					// s_init reads partial row r only when launched with gridDim 1 and offset pointer
+					const int left = std::max(1, sp->maxiter - iters[r]);
+					s_init<<<1, NT, 0, s>>>(w->st + r, w->done + r, w->vpart + (size_t)r * w->nbv * 4, w->nbv,
+						eps_in[r], left, mc, w->hist + (size_t)r * w->hist_cap, 0, 1);
+					ADDA_LAUNCHED();
+				}
+			}
+			const int zero = (step > 0) || sp->init_field == ADDA_IF_ZERO;
+			if (zero) {
+				ADDA_CUDA(cudaMemsetAsync(k.x, 0, sizeof(C) * R * n3, s));
+				k_copy<C><<<gv, NT, 0, s>>>(k.r, k.v3, n3, nullptr);
+				ADDA_LAUNCHED();
+			}
+			else {
+				MvEpi e{EPI_NONE, nullptr, c->partial};
+				if ((rc = matvec_run<float>(c, R, k.v3, k.Av, 0, e, nullptr))) return rc;
+				k_init_field<C><<<gv, NT, 0, s>>>(w->st, w->done, k.v3, k.Av, k.x, k.r, n3, sp->init_field, w->vpart,
+					w->nbv, 0);
+				ADDA_LAUNCHED();
+				s_init_choose<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv, sp->init_field, w->hist, 0);
+				ADDA_LAUNCHED();
+				k_init_field<C><<<gv, NT, 0, s>>>(w->st, w->done, k.v3, k.Av, k.x, k.r, n3, sp->init_field, w->vpart,
+					w->nbv, 1);
+				ADDA_LAUNCHED();
+			}
+			// freeze RHS whose FP64 residual already meets eps
+			for (int r = 0; r < R; r++) w->h_done[r] = odone[r];
+			ADDA_CUDA(cudaMemcpyAsync(w->done, w->h_done, sizeof(int) * R, cudaMemcpyHostToDevice, s));
+			// stale done flags from init must be OR-ed: mark st.done too
+			ADDA_CUDA(cudaStreamSynchronize(s));
+			std::vector<RhsState> tmp(R);
+			ADDA_CUDA(cudaMemcpy(tmp.data(), w->st, sizeof(RhsState) * R, cudaMemcpyDeviceToHost));
+			for (int r = 0; r < R; r++) {
+				if (odone[r]) tmp[r].done = 1;
+				w->h_done[r] = tmp[r].done;
+			}
+			ADDA_CUDA(cudaMemcpy(w->st, tmp.data(), sizeof(RhsState) * R, cudaMemcpyHostToDevice));
+			ADDA_CUDA(cudaMemcpy(w->done, w->h_done, sizeof(int) * R, cudaMemcpyHostToDevice));
+			unsigned long long it = 0;
+			if ((rc = krylov<float>(c, w, sp->method, R, K, &it))) return rc;
+			ADDA_CUDA(cudaMemcpyAsync(hs.data(), w->st, sizeof(RhsState) * R, cudaMemcpyDeviceToHost, s));
+			ADDA_CUDA(cudaStreamSynchronize(s));
+			for (int r = 0; r < R; r++) {
+				if (odone[r]) continue;
+				iters[r] += hs[r].niter - 1;
+				nmv32[r] += (sp->method == ADDA_ITER_BICGSTAB ? 2 : 1) * (hs[r].niter - 1) + (zero ? 0 : 1);
+				if (hs[r].status) status[r] = hs[r].status;
+				nref[r]++;
+			}
+			// x64 (+)= d for the RHS still active
+			for (int r = 0; r < R; r++) w->h_done[r] = odone[r];
+			ADDA_CUDA(cudaMemcpyAsync(d_odone, w->h_done, sizeof(int) * R, cudaMemcpyHostToDevice, s));
+			k_accum<C><<<gv, NT, 0, s>>>(w->x64, k.x, n3, step > 0 ? 1 : 0, d_odone);
+			ADDA_LAUNCHED();
+			// true residual in FP64: r64 = b - A64.x64, |r64|^2; float copy into k.v3 for the next inner solve
+			MvEpi e{EPI_NONE, nullptr, c->partial};
+			if ((rc = matvec_run<double>(c, R, w->x64, w->av64, 0, e, nullptr))) return rc;
+			k_resid64<<<gv, NT, 0, s>>>(w->b64, w->av64, w->r64, k.v3, n3, w->vpart, w->nbv);
+			ADDA_LAUNCHED();
+			if ((rc = reduce_partials(c, R, w->vpart, w->nbv, c->d_red))) return rc;
+			ADDA_CUDA(cudaMemcpyAsync(red.data(), c->d_red, sizeof(double) * 4 * R, cudaMemcpyDeviceToHost, s));
+			ADDA_CUDA(cudaStreamSynchronize(s));
+			bool all = true;
+			for (int r = 0; r < R; r++) {
+				if (odone[r]) continue;
+				nmv64[r]++;
+				inprod64[r] = red[4 * r];
+				if (inprod64[r] <= epsB64[r] || status[r]) odone[r] = 1;
+				all = all && odone[r];
+			}
+			if (all) break;
+		}
+		for (int r = 0; r < R; r++) {
+			st[r].niter = iters[r];
+			st[r].status = status[r];
+			st[r].resid = sqrt(inprod64[r] / temp[r]);
+			if (!st[r].status && inprod64[r] > epsB64[r]) st[r].status = ADDA_GB300_EMAXITER;
+			st[r].refinements = nref[r];
+			st[r].matvecs_fp32 = nmv32[r];
+			st[r].matvecs_fp64 = nmv64[r];
+		}
+	}
+	// polarisations p = S.x (FP64) stay on the device (iterative.c:1527)
+	k_pvec<<<gv, NT, 0, s>>>(w->x64, c->pvec64, c->ccs64, c->per_dip, c->nmat, c->d_mat, c->N);
+	ADDA_LAUNCHED();
+	c->last_nrhs = R;
+	if (stats)
+		for (int r = 0; r < R; r++) stats[r] = st[r];
+	return ADDA_GB300_OK;
+}
+
+int solver_solve(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int R, const double *einc, double *xvec,
+	double *pvec, adda_gb300_rhs_stats *stats, double *resid_hist, int hist_cap)
+{
+	int rc = check_params(sp);
+	if (rc) return rc;
+	if ((rc = ensure_work(c, R, std::max(hist_cap, 1)))) return rc;
+	SolverWork *w = c->sw;
+	const size_t n3 = w->n3;
+	cudaStream_t s = c->stream;
+	// stage Einc in the FP64 matvec output buffer (consumed by the first kernel of the solve)
+	ADDA_CUDA(cudaMemcpyAsync(w->av64, einc, sizeof(double2) * R * n3, cudaMemcpyHostToDevice, s));
+	if ((rc = solve_core(c, sp, R, w->av64, stats))) return rc;
+	if (xvec) ADDA_CUDA(cudaMemcpyAsync(xvec, w->x64, sizeof(double2) * R * n3, cudaMemcpyDeviceToHost, s));
+	if (pvec) ADDA_CUDA(cudaMemcpyAsync(pvec, c->pvec64, sizeof(double2) * R * n3, cudaMemcpyDeviceToHost, s));
+	if (resid_hist && hist_cap > 0) {
+		if (sp->precision == ADDA_PREC_FP64)
+			ADDA_CUDA(cudaMemcpy2DAsync(resid_hist, sizeof(double) * hist_cap, w->hist, sizeof(double) * w->hist_cap,
+				sizeof(double) * hist_cap, R, cudaMemcpyDeviceToHost, s));
+		else memset(resid_hist, 0, sizeof(double) * R * hist_cap);
+	}
+	ADDA_CUDA(cudaStreamSynchronize(s));
+	return ADDA_GB300_OK;
+}
+
+int solver_solve_dev(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int R, const double2 *d_einc,
+	double2 *d_xvec, double2 *d_pvec, adda_gb300_rhs_stats *stats)
+{
+	int rc = check_params(sp);
+	if (rc) return rc;
+	if ((rc = ensure_work(c, R, 1))) return rc;
+	SolverWork *w = c->sw;
+	const size_t n3 = w->n3;
+	cudaStream_t s = c->stream;
+	if ((rc = solve_core(c, sp, R, d_einc, stats))) return rc;
+	if (d_xvec) ADDA_CUDA(cudaMemcpyAsync(d_xvec, w->x64, sizeof(double2) * R * n3, cudaMemcpyDeviceToDevice, s));
+	if (d_pvec) ADDA_CUDA(cudaMemcpyAsync(d_pvec, c->pvec64, sizeof(double2) * R * n3, cudaMemcpyDeviceToDevice, s));
+	ADDA_CUDA(cudaStreamSynchronize(s));
+	return ADDA_GB300_OK;
+}
+
+int cross_sections(adda_gb300_ctx *c, int R, const double *prop, const double *incpol, double *cext, double *cabs)
+{
+	int rc = ensure_work(c, R, 1);
+	if (rc) return rc;
+	SolverWork *w = c->sw;
+	cudaStream_t s = c->stream;
+	double *d_prop = c->d_red; // needs 3*R doubles: use the reduction scratch if large enough, else allocate
+	double *tmp = nullptr;
+	if ((size_t)3 * R > 4 * (size_t)c->Rmax) {
+		ADDA_CUDA(cudaMalloc(&tmp, sizeof(double) * 3 * R));
+		d_prop = tmp;
+	}
+	ADDA_CUDA(cudaMemcpyAsync(d_prop, prop, sizeof(double) * 3 * R, cudaMemcpyHostToDevice, s));
+	const dim3 g(w->nbv, R);
+	const double kd = c->k * c->gridspace, k3 = c->k * c->k * c->k;
+	k_cross<<<g, NT, 0, s>>>(c->pvec64, c->d_pos, c->cc64, c->per_dip, c->nmat, c->d_mat, c->N, d_prop, kd, k3,
+		w->xpart, w->nbv);
+	ADDA_LAUNCHED();
+	std::vector<double> part((size_t)R * w->nbv * 8);
+	ADDA_CUDA(cudaMemcpyAsync(part.data(), w->xpart, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, s));
+	ADDA_CUDA(cudaStreamSynchronize(s));
+	if (tmp) cudaFree(tmp);
+	const double PI = 3.14159265358979323846;
+	for (int r = 0; r < R; r++) {
+		double sm[7] = {0, 0, 0, 0, 0, 0, 0};
+		for (int b = 0; b < w->nbv; b++)
+			for (int j = 0; j < 7; j++) sm[j] += part[((size_t)r * w->nbv + b) * 8 + j];
+		const double *n = prop + 3 * r, *e = incpol + 3 * r;
+		// tbuff = sum - n (n.sum); ebuff = -i k^3 exp(-i k r0.n) tbuff; Cext = 4pi/k^2 Re(ebuff.e)
+		double dre = 0, dim = 0;
+		for (int i = 0; i < 3; i++) {
+			dre += sm[2 * i] * n[i];
+			dim += sm[2 * i + 1] * n[i];
+		}
+		const double r0[3] = {-c->gridspace * (c->bX - 1) / 2.0, -c->gridspace * (c->bY - 1) / 2.0,
+			-c->gridspace * (c->bZ - 1) / 2.0};
+		const double ph0 = -c->k * (r0[0] * n[0] + r0[1] * n[1] + r0[2] * n[2]);
+		const double k3v = c->k * c->k * c->k;
+		// amp = -i * exp(i ph0) * k^3 = k^3 (sin ph0 - i cos ph0)
+		const double ar = k3v * sin(ph0), ai = -k3v * cos(ph0);
+		double sumc = 0;
+		for (int i = 0; i < 3; i++) {
+			const double tr = sm[2 * i] - dre * n[i], ti = sm[2 * i + 1] - dim * n[i];
+			sumc += (ar * tr - ai * ti) * e[i];
+		}
+		if (cext) cext[r] = sumc * 4 * PI / (c->k * c->k);
+		if (cabs) cabs[r] = 4 * PI * c->k * sm[6];
+	}
+	return ADDA_GB300_OK;
+}
+
+} // namespace adda

@@ -1,0 +1,306 @@
+"""Benchmark: time-to-solution of the DDA solve on the 128^3 sphere (BASELINE configuration 2) on one GB300.
+
+One step = one complete solve of both incident polarisations (2 right-hand sides) of the 128^3 sphere (1,099,136
+dipoles, FFT grid 256^3, m = 1.33+0.01i, 15 dipoles per wavelength) with QMR_CS to relative residual 1e-5 in the
+mixed-precision mode (FP32 Krylov + FFT matvec, FP64 residual refinement), inputs resident in HBM. The line also
+reports the plain-FP64 GPU time-to-solution on the same workload, the FP32 matvec's HBM roofline, the end-to-end
+time through the host-pointer C ABI, and a CPU baseline (the oracle port on this machine's host cores).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--method qmr|bicgstab]
+
+--impl reference times the reference's CPU algorithm (the oracle restatement; the reference binary itself is built
+only where its sources are) on the host cores, on the same metric.
+Multi-GPU: the path does not shard one solve; N GPUs run N independent replicas (weak scaling).
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "a-dda_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "time-to-solution @res 1e-5, 128^3 sphere (both polarisations), mixed FP32/FP64 on GB300"
+GRID, M_REF, DPL, EPS = 128, 1.33 + 0.01j, 15.0, 1e-5
+WORKLOAD = ("sphere 128^3 box, N=1099136 dipoles, FFT grid 256^3, m=1.33+0.01i, dpl=15, LDR, %s to 1e-5, "
+            "2 RHS (both polarisations)")
+# iteration counts of the reference build (ADDA 1.3b6 seq + FFTW-subset shim) on this workload, per polarisation
+# (Y, X), from a full run of '-grid 128 -dpl 15 -m 1.33 0.01 -iter <m> -eps 5 -sym no'; used only to extrapolate
+# the bounded CPU samples to a time-to-solution
+REF_ITERS = {"qmr": None, "bicgstab": None}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p.get("hbm_gbs", 6800.0), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def matvec_bytes(n, g, b, s, R):
+    """algorithmic HBM bytes of one matvec for R RHS sharing D: per RHS s*9N (x read twice, y written) +
+    s*12*gX*bY*bZ (the x-transformed intermediate written/read twice) + 14N (lattice indices), plus D once"""
+    gX, gY, gZ = g
+    bX, bY, bZ = b
+    return R * (s * 9 * n + s * 12 * gX * bY * bZ + 14 * n) + s * 6 * gX * (gY // 2 + 1) * (gZ // 2 + 1)
+
+
+class Clocks:
+    """samples nvidia-smi during the timed region"""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(world, v):
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(method, nthreads, setup=None):
+    """Bounded CPU sample: the oracle (restatement of the reference's MatVec/QMR_CS in C, OpenMP over lines and
+    slices) builds D for the 128^3 sphere and runs 2 timed FP64 matvecs + the BLAS-1 of one iteration per RHS.
+    Returns (seconds per iteration per RHS, description)."""
+    import adda_gb300 as A
+    from oracle import oracle as O
+    s = setup or A.Setup(grid=GRID, m=M_REF, dpl=DPL)
+    o = O.Oracle(s.box, s.grid, s.pos, s.mat, s.gridspace, s.wavenum, nthreads)
+    o.set_cc(s.cc[0].reshape(1, 3))
+    x = s.einc[0]
+    o.matvec(x)  # warm
+    t0 = time.perf_counter()
+    reps = 2
+    for _ in range(reps):
+        y, _ = o.matvec(x)
+        # the vector updates of one QMR_CS iteration: ~8 streaming passes over 3N complex (iterative.c:967-1028)
+        for _k in range(4):
+            y = 0.5 * y + x
+    t = (time.perf_counter() - t0) / reps
+    o.close()
+    per_mv = 2 if method == "bicgstab" else 1
+    return t * per_mv, "%d FP64 oracle matvecs + BLAS-1 on the 128^3 sphere with %d threads" % (reps, nthreads)
+
+
+def run_reference(args):
+    world, rank, local = dist_init(args)
+    if rank != 0:
+        return
+    nthreads = os.cpu_count() or 1
+    t_it, desc = None, None
+    for _ in range(args.warmup):
+        pass
+    times = []
+    for _ in range(args.steps):
+        t_it, desc = cpu_sample(args.method, nthreads)
+        times.append(t_it)
+    iters = REF_ITERS.get(args.method) or (70, 70)
+    value = statistics.median(times) * sum(iters)
+    line = {"metric": METRIC, "value": value, "unit": "s", "impl": "reference", "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": statistics.median(times) * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (generated particle)",
+            "config": {"workload": WORKLOAD % ("QMR_CS" if args.method == "qmr" else "BiCGStab"),
+                       "method": args.method, "iterations_extrapolated": list(iters)},
+            "cpu_baseline": {"value": value, "unit": "s", "cores": nthreads, "kind": "port",
+                             "sample": desc + "; per-step value = seconds per iteration x the reference's iteration "
+                                              "count %s" % (list(iters),)},
+            "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    world, rank, local = dist_init(args)
+    import torch
+    torch.cuda.set_device(local)
+    import adda_gb300 as A
+    s = A.Setup(grid=GRID, m=M_REF, dpl=DPL)
+    R = 2
+    ctx = A.Context.from_setup(s, nrhs_max=R, device=local)
+    einc = np.ascontiguousarray(np.stack(s.einc))
+    d_e = torch.from_numpy(einc.view(np.float64)).cuda()
+    d_x = torch.empty_like(d_e)
+    d_p = torch.empty_like(d_e)
+    opts = dict(method=args.method, eps=EPS)
+    for _ in range(args.warmup):
+        ctx.solve_device(d_e.data_ptr(), R, d_x.data_ptr(), d_p.data_ptr(), prec="mixed", **opts)
+    torch.cuda.synchronize()
+    barrier(world)
+    l0 = A.kernel_launches()
+    ms = []
+    stats = None
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            stats = ctx.solve_device(d_e.data_ptr(), R, d_x.data_ptr(), d_p.data_ptr(), prec="mixed", **opts)
+            ms.append(ctx.last_solve_ms())
+        torch.cuda.synchronize()
+    launches = A.kernel_launches() - l0
+    barrier(world)
+    t_solve = allmax(world, statistics.mean(ms) / 1e3)
+    ce, ca = ctx.cross_sections(np.stack([s.prop, s.prop]), np.stack(s.incpol))
+    # plain FP64 GPU solve on the same workload (one warm-up, one timed)
+    ctx.solve_device(d_e.data_ptr(), R, d_x.data_ptr(), d_p.data_ptr(), prec="fp64", **opts)
+    st64 = ctx.solve_device(d_e.data_ptr(), R, d_x.data_ptr(), d_p.data_ptr(), prec="fp64", **opts)
+    t64 = allmax(world, ctx.last_solve_ms() / 1e3)
+    ce64, ca64 = ctx.cross_sections(np.stack([s.prop, s.prop]), np.stack(s.incpol))
+    # end to end through the host-pointer C ABI: Einc from pinned host memory, x and p back to host
+    pin_e = torch.from_numpy(einc.view(np.float64)).pin_memory()
+    pin_x = torch.empty_like(pin_e).pin_memory()
+    pin_p = torch.empty_like(pin_e).pin_memory()
+    ctx.solve(pin_e.numpy().view(np.complex128), prec="mixed", **opts)
+    torch.cuda.synchronize()
+    e2e = []
+    for _ in range(max(1, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        r = ctx.solve(pin_e.numpy().view(np.complex128), prec="mixed", **opts)
+        pin_x.numpy()[:] = r["x"].view(np.float64)
+        pin_p.numpy()[:] = r["p"].view(np.float64)
+        ctx.cross_sections(np.stack([s.prop, s.prop]), np.stack(s.incpol))
+        e2e.append(time.perf_counter() - t0)
+    t_e2e = allmax(world, statistics.mean(e2e))
+    # FP32 matvec roofline (R=2 RHS sharing D), and the FP64 matvec time
+    mv32 = ctx.time_matvec("fp32", R, iters=20)
+    mv64 = ctx.time_matvec("fp64", R, iters=3)
+    bts = matvec_bytes(s.n, s.grid, s.box, 8, R)
+    hbm, src = peaks()
+    achieved = bts / (mv32 * 1e-3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "matvec_fp32_dram_bytes.json")
+    if os.path.exists(tf):
+        with open(tf) as f:
+            traffic = json.load(f).get("bytes_per_matvec")
+    line = {
+        "metric": METRIC, "value": t_solve, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_solve * 1e3, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64+f64 (mixed)", "data": "synthetic (generated particle, plane wave)",
+        "config": {"workload": WORKLOAD % ("QMR_CS" if args.method == "qmr" else "BiCGStab"),
+                   "method": args.method, "rhs": R, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs larger than L2 (D 204 MB FP32, Einc 106 MB)",
+                   "timing": "CUDA events on the library stream around each solve"},
+        "fp64_time_to_solution_s": t64,
+        "speedup_mixed_vs_fp64": t64 / t_solve,
+        "iterations": {"mixed": [x["niter"] for x in stats], "fp64": [x["niter"] for x in st64],
+                       "fp64_matvecs_in_mixed": [x["matvecs_fp64"] for x in stats],
+                       "refinements": [x["refinements"] for x in stats]},
+        "residual": {"mixed": [x["resid"] for x in stats], "fp64": [x["resid"] for x in st64]},
+        "Cext": {"mixed": list(map(float, ce)), "fp64": list(map(float, ce64))},
+        "Cabs": {"mixed": list(map(float, ca)), "fp64": list(map(float, ca64))},
+        "matvec": {"fp32_ms": mv32, "fp64_ms": mv64, "fp32_GBps": achieved, "rhs": R,
+                   "algorithmic_bytes": bts},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic, "kernel": "FP32 matvec (K1..K3 sequence, 2 RHS)",
+                     "peak_source": src},
+        "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": einc.nbytes,
+                "d2h_bytes_per_step": 2 * einc.nbytes + 16 * R},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        t_it, desc = cpu_sample(args.method, os.cpu_count() or 1, s)
+        iters = REF_ITERS.get(args.method) or [x["niter"] for x in st64]
+        v = t_it * sum(iters)
+        line["cpu_baseline"] = {"value": v, "unit": "s", "cores": os.cpu_count(), "kind": "port",
+                                "sample": desc + "; x iteration count %s" % (list(iters),)}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--method", default="qmr", choices=["qmr", "bicgstab"])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

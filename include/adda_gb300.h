@@ -87,9 +87,10 @@ int adda_gb300_fit_box(int shape, const double *pars, int boxX, int *boxY, int *
 /* MakeParticle's box loop, src/make_particle.c:1984-2230. Returns ndip; position/material may be NULL to count. */
 size_t adda_gb300_make_particle(int shape, const double *pars, int boxX, int boxY, int boxZ, uint16_t *position,
 	uint8_t *material);
-/* InitRotation, src/crosssec.c:82-139 (zyz Euler angles in degrees): propagation and the two polarisations */
-void adda_gb300_rotation(double alpha_deg, double beta_deg, double gamma_deg, double prop[3], double incPolY[3],
-	double incPolX[3]);
+/* Incident frame: propagation prop0 (NULL = (0,0,1); -prop, param.c:1371-1382) with its two polarisations
+ * (param.c:2116-2131), rotated by the zyz Euler angles in degrees (-orient; InitRotation, src/crosssec.c:82-139) */
+void adda_gb300_rotation(const double prop0[3], double alpha_deg, double beta_deg, double gamma_deg, double prop[3],
+	double incPolY[3], double incPolX[3]);
 /* GenerateB, free-space plane wave, src/GenerateB.c:324-328: einc[i] = pol * exp(i k r_i.prop) */
 void adda_gb300_plane_wave(size_t ndip, const uint16_t *position, int boxX, int boxY, int boxZ, double gridspace,
 	double wavenum, const double prop[3], const double pol[3], double *einc);
@@ -135,10 +136,24 @@ int adda_gb300_matvec_device(adda_gb300_ctx *ctx, int prec, int nrhs, const void
 int adda_gb300_solve(adda_gb300_ctx *ctx, const adda_gb300_solve_params *sp, int nrhs, const double *einc,
 	double *xvec, double *pvec, adda_gb300_rhs_stats *stats, double *resid_hist, int hist_cap);
 
+/* same as adda_gb300_solve with DEVICE buffers (double2 [nrhs][ndip][3]) for einc and the optional d_xvec/d_pvec:
+ * nothing crosses PCIe/C2C except the per-RHS stats and the convergence flags polled between graph launches */
+int adda_gb300_solve_device(adda_gb300_ctx *ctx, const adda_gb300_solve_params *sp, int nrhs, const void *d_einc,
+	void *d_xvec, void *d_pvec, adda_gb300_rhs_stats *stats);
+
 /* ExtCross (plane wave) and AbsCross (Draine), src/crosssec.c:811-917, in FP64 on the device from the
  * polarisations left by the last solve: prop/incpol per RHS [nrhs][3]; cext/cabs per RHS. */
 int adda_gb300_cross_sections(adda_gb300_ctx *ctx, int nrhs, const double *prop, const double *incpol,
 	double *cext, double *cabs);
+
+/* average device time of one matvec (prec, nrhs RHS, device-resident random input) over iters launches, measured
+ * with CUDA events on the context's stream after one warm-up launch; flush_bytes > 0 writes that many bytes of a
+ * scratch buffer between launches so every launch starts with a cold L2 */
+int adda_gb300_time_matvec(adda_gb300_ctx *ctx, int prec, int nrhs, int iters, size_t flush_bytes, double *ms);
+
+/* device time in milliseconds of the last solve on this context: CUDA events recorded on the context's stream at
+ * the first and the last kernel of the solve (host-device copies of the host-pointer API excluded) */
+double adda_gb300_last_solve_ms(const adda_gb300_ctx *ctx);
 
 /* last error message of the calling thread */
 const char *adda_gb300_last_error(void);

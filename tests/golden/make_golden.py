@@ -1,0 +1,122 @@
+"""Generate tests/golden/reference_runs.json by running the UNMODIFIED reference (ADDA 1.3b6, sequential build
+compiled from its own sources by oracle/Makefile with this project's FFTW-subset shim) on command lines taken from
+the reference's own differential test suite (tests/2exec/suite) and its published sample run
+(sample/run000_sphere_g16_m1.5).
+
+Each case records what the reference printed: dipole count, box, FFT grid, coupling constants, the RE_ residual
+history of each polarisation, and Cext/Cabs from CrossSec-Y/-X. Run from the repository root:
+
+    python tests/golden/make_golden.py [/path/to/reference/src]
+
+This script is the only place that executes the reference; the GPU machine never needs it.
+"""
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+M = ["-m", "1.1", "0.1"]
+ELL = ["-shape", "ellipsoid", "0.5", "1.5"]
+MGN = M + ["-grid", "8"]
+
+# (name, reference arguments, keyword arguments of adda_gb300.Setup + solver options)
+CASES = [
+    ("sample_default", [], dict(grid=16, m=1.5)),
+    ("c1_qmr", ["-grid", "16", "-dpl", "10", "-m", "1.5", "0", "-iter", "qmr", "-eps", "5"],
+     dict(grid=16, m=1.5, dpl=10)),
+    ("c1_bicgstab", ["-grid", "16", "-dpl", "10", "-m", "1.5", "0", "-iter", "bicgstab", "-eps", "5"],
+     dict(grid=16, m=1.5, dpl=10, iter="bicgstab")),
+    ("mgn", MGN, dict(grid=8, m=1.1 + 0.1j)),
+    ("mgn_eps10", ["-eps", "10"] + MGN, dict(grid=8, m=1.1 + 0.1j, eps=1e-10)),
+    ("mgn_init_zero", ["-init_field", "zero"] + MGN, dict(grid=8, m=1.1 + 0.1j, init="zero")),
+    ("mgn_init_inc", ["-init_field", "inc"] + MGN, dict(grid=8, m=1.1 + 0.1j, init="inc")),
+    ("mgn_bicgstab", ["-iter", "bicgstab"] + MGN, dict(grid=8, m=1.1 + 0.1j, iter="bicgstab")),
+    ("mgn_maxiter5", ["-maxiter", "5"] + MGN, dict(grid=8, m=1.1 + 0.1j, maxiter=5)),
+    ("mgn_orient30", ["-orient", "30", "0", "0"] + MGN, dict(grid=8, m=1.1 + 0.1j, orient=(30, 0, 0))),
+    ("ell_orient", ["-orient", "10", "20", "30"] + ELL + MGN,
+     dict(grid=8, m=1.1 + 0.1j, shape="ellipsoid", pars=(0.5, 1.5), orient=(10, 20, 30))),
+    ("pol_cm", ["-pol", "cm"] + MGN, dict(grid=8, m=1.1 + 0.1j, pol="cm")),
+    ("pol_dgf", ["-pol", "dgf"] + MGN, dict(grid=8, m=1.1 + 0.1j, pol="dgf")),
+    ("pol_rrc", ["-pol", "rrc"] + MGN, dict(grid=8, m=1.1 + 0.1j, pol="rrc")),
+    ("pol_ldr_prop", ["-pol", "ldr", "-prop", "1", "2", "3"] + MGN,
+     dict(grid=8, m=1.1 + 0.1j, prop=(1, 2, 3))),
+    ("pol_ldr_avgpol", ["-pol", "ldr", "avgpol", "-prop", "1", "2", "3"] + MGN,
+     dict(grid=8, m=1.1 + 0.1j, prop=(1, 2, 3), avgpol=True)),
+    ("prop_mz", ["-prop", "0", "0", "-1"] + MGN, dict(grid=8, m=1.1 + 0.1j, prop=(0, 0, -1))),
+    ("prop_x", ["-prop", "1", "0", "0"] + MGN, dict(grid=8, m=1.1 + 0.1j, prop=(1, 0, 0))),
+    ("prop_ell", ["-prop", "5", "1", "3"] + ELL + MGN,
+     dict(grid=8, m=1.1 + 0.1j, shape="ellipsoid", pars=(0.5, 1.5), prop=(5, 1, 3))),
+    ("ell24", ["-grid", "24", "-shape", "ellipsoid", "0.7", "0.8", "-m", "1.4", "0.02", "-orient", "10", "20", "30"],
+     dict(grid=24, m=1.4 + 0.02j, shape="ellipsoid", pars=(0.7, 0.8), orient=(10, 20, 30))),
+    ("box12", ["-shape", "box", "-grid", "12", "-m", "1.3", "0.05"], dict(grid=12, m=1.3 + 0.05j, shape="box")),
+    ("c2_small", ["-grid", "32", "-dpl", "15", "-m", "1.33", "0.01", "-iter", "bicgstab", "-eps", "5"],
+     dict(grid=32, m=1.33 + 0.01j, dpl=15, iter="bicgstab")),
+] + [("grid%d" % g, ["-grid", str(g), "-size", "8"] + M, dict(grid=g, m=1.1 + 0.1j, size=8.0))
+     for g in (2, 4, 6, 10, 12, 18, 20, 24, 30, 32)]
+
+
+def parse_run(rundir, stdout):
+    log = open(os.path.join(rundir, "log")).read()
+    out = {}
+    out["ndip"] = int(re.search(r"Total number of occupied dipoles: (\d+)", log).group(1))
+    out["box"] = [int(v) for v in re.search(r"box dimensions: (\d+)x(\d+)x(\d+)", log).groups()]
+    out["grid"] = [int(v) for v in re.search(r"The FFT grid is: (\d+)x(\d+)x(\d+)", log).groups()]
+    out["cc"] = [[float(a), float(b)] for a, b in
+                 re.findall(r"CoupleConstant:([-+]?[0-9.]+(?:[eE][-+]?\d+)?)([-+][0-9.]+(?:[eE][-+]?\d+)?)i", log)]
+    hist = {}
+    cur = None
+    for line in log.splitlines():
+        m = re.match(r"here we go, calc ([XY])", line)
+        if m:
+            cur = m.group(1)
+            hist[cur] = []
+        m = re.match(r"RE_(\d+) = ([-+0-9.E]+)", line)
+        if m and cur:
+            hist[cur].append(float(m.group(2)))
+    out["resid"] = hist
+    cs = {}
+    for pol in "YX":
+        f = os.path.join(rundir, "CrossSec-" + pol)
+        if os.path.exists(f):
+            txt = open(f).read()
+            cs[pol] = dict(Cext=float(re.search(r"Cext\s*=\s*([-+0-9.eE]+)", txt).group(1)),
+                           Cabs=float(re.search(r"Cabs\s*=\s*([-+0-9.eE]+)", txt).group(1)))
+    out["cross"] = cs
+    out["maxiter_warning"] = "haven't converged" in stdout + log
+    return out
+
+
+def main(ref_src="/root/reference/src"):
+    from oracle import oracle as O
+    binp = O.build_reference(ref_src)
+    if not binp:
+        raise SystemExit("reference sources not found at " + ref_src)
+    results = []
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, args, kw in CASES:
+            full = args + ["-sym", "no"]
+            rundir = os.path.join(tmp, name)
+            p = subprocess.run([binp] + full + ["-dir", rundir], cwd=tmp, capture_output=True, text=True)
+            if p.returncode != 0:
+                raise RuntimeError(name + ": " + p.stdout + p.stderr)
+            res = parse_run(rundir, p.stdout)
+            res.update(name=name, args=full, setup=kw)
+            results.append(res)
+            print(name, res["ndip"], res["grid"], res["cross"])
+    # the published sample itself (generated by ADDA v1.3b4 on Windows), as printed in the reference tree
+    sample = dict(name="published_sample", Cext_Y=135.0449047, Cabs_Y=-2.047466081e-16, niter_Y=22,
+                  resid_Y_first=[1.0, 8.4752662637e-01, 8.2113292044e-01, 4.2639057157e-01, 3.0639031825e-01],
+                  cc="0.005259037197+1.843854148e-05i")
+    with open(os.path.join(HERE, "reference_runs.json"), "w") as f:
+        json.dump(dict(reference="ADDA 1.3b6 sequential build + FFTW-subset shim", cases=results,
+                       sample=sample), f, indent=1, default=lambda z: [z.real, z.imag] if isinstance(z, complex) else z)
+
+
+if __name__ == "__main__":
+    main(*sys.argv[1:])

@@ -1,0 +1,57 @@
+"""Shared helpers for the tests: build the reference-equivalent inputs for a golden case, run the oracle on them."""
+import json
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden", "reference_runs.json")
+
+SETUP_KEYS = ("grid", "shape", "pars", "m", "dpl", "size", "pol", "orient", "avgpol", "prop")
+
+
+def golden():
+    with open(GOLDEN) as f:
+        return json.load(f)
+
+
+def case(name):
+    for c in golden()["cases"]:
+        if c["name"] == name:
+            return c
+    raise KeyError(name)
+
+
+def setup_for(kw):
+    import adda_gb300 as A
+    args = {k: v for k, v in kw.items() if k in SETUP_KEYS}
+    if isinstance(args.get("m"), list):
+        args["m"] = complex(*args["m"])
+    return A.Setup(**args)
+
+
+def solver_opts(kw):
+    return dict(method=kw.get("iter", "qmr"), eps=kw.get("eps", 1e-5), maxiter=kw.get("maxiter", 100000),
+                init=kw.get("init", "auto"))
+
+
+def oracle_for(s, nthreads=0):
+    from oracle import oracle as O
+    o = O.Oracle(s.box, s.grid, s.pos, s.mat, s.gridspace, s.wavenum, nthreads)
+    return o
+
+
+def oracle_solve(o, s, pol_index, method="qmr", eps=1e-5, maxiter=100000, init="auto"):
+    from oracle import oracle as O
+    o.set_cc(s.cc[pol_index].reshape(1, 3))
+    r = o.solve(s.einc[pol_index], method=O.QMR_CS if method == "qmr" else O.BICGSTAB, eps=eps, maxiter=maxiter,
+                init_field={"auto": O.IF_AUTO, "zero": O.IF_ZERO, "inc": O.IF_INC}[init])
+    ce, ca = o.cross(r["p"], s.prop, s.incpol[pol_index])
+    r["Cext"], r["Cabs"] = ce, ca
+    return r
+
+
+def rel(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))

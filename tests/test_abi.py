@@ -1,0 +1,61 @@
+"""The C-ABI library loads without a GPU and exports every entry point include/adda_gb300.h declares; the host-side
+setup functions (no GPU) behave like the reference's; GPU entry points fail cleanly when no GPU is present."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, have_gpu
+
+
+def declared():
+    txt = open(os.path.join(ROOT, "include", "adda_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(adda_gb300_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_exports_every_declared_symbol(adda):
+    L = ctypes.CDLL(adda.LIB_PATH)
+    names = declared()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+    assert set(names) == set(adda.EXPORTS)
+
+
+def test_fftfit_matches_reference_rule(adda):
+    # fftFit (fft.c:528-562): even, divisible by divis, 2^a 3^b 5^c 7^d (11|13)^{0,1}
+    for x, d, want in [(32, 1, 32), (34, 1, 36), (44, 1, 44), (46, 1, 48), (50, 2, 50), (54, 2, 54), (242, 1, 250),
+                       (256, 2, 256), (512, 1, 512), (14, 1, 14), (22, 1, 22), (26, 1, 26), (286, 1, 288)]:
+        assert adda.fft_fit(x, d) == want, (x, d)
+
+
+def test_particle_counts(adda):
+    # occupied-dipole counts printed by the reference for the BASELINE configurations (log / prognosis)
+    for shape, grid, pars, n in [("sphere", 16, None, 2176), ("sphere", 128, None, 1099136),
+                                 ("ellipsoid", 24, (0.7, 0.8), 4032), ("box", 48, None, 110592)]:
+        box, pos, mat = adda.make_particle(shape, grid, pars)
+        assert len(pos) == n
+        # z-major, then y, then x: the order the device lattice requires
+        key = (pos[:, 2].astype(np.int64) * box[1] + pos[:, 1]) * box[0] + pos[:, 0]
+        assert np.all(np.diff(key) > 0)
+
+
+def test_rotation_default_and_prop(adda):
+    prop, py, px = adda.rotation()
+    np.testing.assert_allclose(prop, [0, 0, 1])
+    np.testing.assert_allclose(py, [0, 1, 0])
+    np.testing.assert_allclose(px, [1, 0, 0])
+    prop, py, px = adda.rotation(10, 20, 30, prop0=(1, 2, 3))
+    for v in (prop, py, px):
+        assert abs(np.linalg.norm(v) - 1) < 1e-14
+    assert abs(prop @ py) < 1e-14 and abs(prop @ px) < 1e-14 and abs(px @ py) < 1e-14
+
+
+@pytest.mark.skipif(have_gpu(), reason="checks the no-GPU error path")
+def test_create_fails_loudly_without_gpu(adda):
+    box, pos, mat = adda.make_particle("sphere", 8)
+    with pytest.raises(adda.AddaError):
+        adda.Context(box, pos, mat, 0.5, 1.0)
