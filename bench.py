@@ -287,6 +287,25 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_profile(args):
+    """small, fixed workloads for ncu: 'solve' = one warm-up + one mixed solve of the bench workload;
+    'matvec' = three FP32 matvecs (2 RHS) of the bench workload"""
+    import torch
+    import adda_gb300 as A
+    s = A.Setup(grid=args.grid, m=M_REF, dpl=DPL)
+    ctx = A.Context.from_setup(s, nrhs_max=2)
+    torch.cuda.synchronize()
+    if args.mode == "profile-solve":
+        einc = np.ascontiguousarray(np.stack(s.einc))
+        d_e = torch.from_numpy(einc.view(np.float64)).cuda()
+        for _ in range(2):
+            st = ctx.solve_device(d_e.data_ptr(), 2, None, None, method=args.method, prec="mixed", eps=EPS)
+        print(json.dumps({"mode": args.mode, "ms": ctx.last_solve_ms(), "stats": st}))
+    else:
+        ms = ctx.time_matvec("fp32", 2, iters=3)
+        print(json.dumps({"mode": args.mode, "fp32_matvec_ms": ms}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -295,8 +314,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--method", default="qmr", choices=["qmr", "bicgstab"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--mode", default="bench", choices=["bench", "profile-solve", "profile-matvec"])
+    ap.add_argument("--grid", type=int, default=GRID, help="sphere box size for the profile modes")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.mode != "bench":
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -37,7 +37,7 @@ CASES = [
     ("mgn_init_zero", ["-init_field", "zero"] + MGN, dict(grid=8, m=1.1 + 0.1j, init="zero")),
     ("mgn_init_inc", ["-init_field", "inc"] + MGN, dict(grid=8, m=1.1 + 0.1j, init="inc")),
     ("mgn_bicgstab", ["-iter", "bicgstab"] + MGN, dict(grid=8, m=1.1 + 0.1j, iter="bicgstab")),
-    ("mgn_maxiter5", ["-maxiter", "5"] + MGN, dict(grid=8, m=1.1 + 0.1j, maxiter=5)),
+    ("mgn_maxiter3", ["-maxiter", "3"] + MGN, dict(grid=8, m=1.1 + 0.1j, maxiter=3)),
     ("mgn_orient30", ["-orient", "30", "0", "0"] + MGN, dict(grid=8, m=1.1 + 0.1j, orient=(30, 0, 0))),
     ("ell_orient", ["-orient", "10", "20", "30"] + ELL + MGN,
      dict(grid=8, m=1.1 + 0.1j, shape="ellipsoid", pars=(0.5, 1.5), orient=(10, 20, 30))),
