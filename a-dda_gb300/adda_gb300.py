@@ -48,7 +48,7 @@ class RhsStats(ctypes.Structure):
 EXPORTS = ["adda_gb300_fft_fit", "adda_gb300_fit_box", "adda_gb300_make_particle", "adda_gb300_rotation",
            "adda_gb300_plane_wave", "adda_gb300_polarizability", "adda_gb300_create", "adda_gb300_destroy",
            "adda_gb300_get_grid", "adda_gb300_init_dmatrix", "adda_gb300_dmatrix_len", "adda_gb300_get_dmatrix",
-           "adda_gb300_set_cc", "adda_gb300_set_cc_dipole", "adda_gb300_matvec", "adda_gb300_matvec_device",
+           "adda_gb300_set_cc", "adda_gb300_set_cc_sqrt", "adda_gb300_set_cc_dipole", "adda_gb300_matvec", "adda_gb300_matvec_device",
            "adda_gb300_solve", "adda_gb300_solve_device", "adda_gb300_cross_sections", "adda_gb300_time_matvec",
            "adda_gb300_last_solve_ms", "adda_gb300_last_error", "adda_gb300_kernel_launches"]
 
@@ -84,6 +84,7 @@ def lib():
             "adda_gb300_dmatrix_len": ([P], SZ),
             "adda_gb300_get_dmatrix": ([P, P], I),
             "adda_gb300_set_cc": ([P, I, I, P], I),
+            "adda_gb300_set_cc_sqrt": ([P, I, I, P], I),
             "adda_gb300_set_cc_dipole": ([P, I, P], I),
             "adda_gb300_matvec": ([P, I, I, P, P, P, I], I),
             "adda_gb300_matvec_device": ([P, I, I, P, P, P, I], I),

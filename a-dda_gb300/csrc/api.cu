@@ -265,7 +265,16 @@ __global__ void cc_sqrt_k(const double2 *cc, double2 *ccs64, float2 *ccs32, size
 	}
 }
 
-static int set_cc_impl(adda_gb300_ctx *c, int rhs, int per_dip, int nmat, const double *cc)
+__global__ void cc_from_sqrt_k(double2 *cc, const double2 *ccs64, float2 *ccs32, size_t n)
+{
+	for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+		const double2 r = ccs64[t];
+		cc[t] = make_double2(r.x * r.x - r.y * r.y, 2 * r.x * r.y);
+		ccs32[t] = make_float2((float)r.x, (float)r.y);
+	}
+}
+
+static int set_cc_impl(adda_gb300_ctx *c, int rhs, int per_dip, int nmat, const double *cc, bool given_sqrt = false)
 {
 	if (!c || !cc || rhs < 0 || rhs >= c->Rmax || (!per_dip && (nmat < 1 || nmat > 256))) {
 		set_error("set_cc: invalid arguments");
@@ -292,9 +301,15 @@ static int set_cc_impl(adda_gb300_ctx *c, int rhs, int per_dip, int nmat, const 
 		c->per_dip = per_dip;
 		c->nmat = per_dip ? 0 : nmat;
 	}
-	ADDA_CUDA(cudaMemcpyAsync(c->cc64 + per * rhs, cc, sizeof(double2) * per, cudaMemcpyHostToDevice, c->stream));
-	cc_sqrt_k<<<(int)std::min<size_t>((per + 255) / 256, 4096), 256, 0, c->stream>>>(c->cc64 + per * rhs,
-		c->ccs64 + per * rhs, c->ccs32 + per * rhs, per);
+	const int g = (int)std::min<size_t>((per + 255) / 256, 4096);
+	if (given_sqrt) {
+		ADDA_CUDA(cudaMemcpyAsync(c->ccs64 + per * rhs, cc, sizeof(double2) * per, cudaMemcpyHostToDevice, c->stream));
+		cc_from_sqrt_k<<<g, 256, 0, c->stream>>>(c->cc64 + per * rhs, c->ccs64 + per * rhs, c->ccs32 + per * rhs, per);
+	}
+	else {
+		ADDA_CUDA(cudaMemcpyAsync(c->cc64 + per * rhs, cc, sizeof(double2) * per, cudaMemcpyHostToDevice, c->stream));
+		cc_sqrt_k<<<g, 256, 0, c->stream>>>(c->cc64 + per * rhs, c->ccs64 + per * rhs, c->ccs32 + per * rhs, per);
+	}
 	ADDA_LAUNCHED();
 	ADDA_CUDA(cudaStreamSynchronize(c->stream));
 	c->cc_set[rhs] = 1;
@@ -304,6 +319,11 @@ static int set_cc_impl(adda_gb300_ctx *c, int rhs, int per_dip, int nmat, const 
 int adda_gb300_set_cc(adda_gb300_ctx *c, int rhs, int nmat, const double *cc)
 {
 	return set_cc_impl(c, rhs, 0, nmat, cc);
+}
+
+int adda_gb300_set_cc_sqrt(adda_gb300_ctx *c, int rhs, int nmat, const double *cc_sqrt)
+{
+	return set_cc_impl(c, rhs, 0, nmat, cc_sqrt, true);
 }
 
 int adda_gb300_set_cc_dipole(adda_gb300_ctx *c, int rhs, const double *cc)

@@ -1,0 +1,221 @@
+/* adda_dropin.c - the reference's fft.c / matvec.c / iterative.c entry points, implemented on libadda_gb300.
+ *
+ * Link this object and libadda_gb300.so instead of the reference's fft.c, matvec.c and iterative.c (all other
+ * reference sources unchanged): the host parses the command line, builds the particle and the incident beam, and
+ * calls InitDmatrix / IterativeSolver / Free_FFT_Dmat exactly as before (calculator.c:685,563; CalculateE.c:860);
+ * the D matrix, every matvec and the whole Krylov solve then run on the GPU, and xvec/pvec come back to the host for
+ * the reference's own cross sections and scattering output.
+ *
+ * The reference's globals, types and host services used here are declared below with the file that defines them; they
+ * must match the reference's sequential build (FFTW3 branch, no MPI).
+ *
+ * Environment (the reference's command line is left unchanged):
+ *   ADDA_GB300_PREC=fp64|mixed   arithmetic of IterativeSolver (default fp64, the reference's)
+ *   ADDA_GB300_DEVICE=<n>        CUDA device (default 0)
+ * Supported: -int poi, reduced FFT, no -surf, -iter qmr|bicgstab, -init_field auto|zero|inc. Anything else stops
+ * with the reference's LogError.
+ */
+#include "adda_gb300.h"
+#include "adda_dropin.h"
+
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define MAX_NMAT 15 /* const.h:106 */
+enum enwho { ALL, ONE };                                           /* const.h:406-409 */
+enum ec { EC_OK, EC_ERROR, EC_WARN, EC_INFO };                     /* const.h:418-423 */
+enum inter { G_FCD, G_FCD_ST, G_IGT, G_IGT_SO, G_NLOC, G_NLOC_AV, G_POINT_DIP, G_SO }; /* const.h:212-224 */
+enum init_field { IF_AUTO, IF_ZERO, IF_INC, IF_READ, IF_WKB };     /* const.h:321-327 */
+
+/* globals of the reference host: vars.c, param.c, timing.c, calculator.c */
+extern int boxX, boxY, boxZ, nprocs, Nmat, maxiter;
+extern size_t gridX, gridY, gridZ, gridYZ, local_Nsmall, local_nvoid_Ndip, local_nRows;
+extern double gridspace, WaveNum, memory;
+extern bool prognosis, reduced_FFT, surface, orient_avg, ipr_required;
+extern enum inter IntRelation;
+extern FILE *logfile;
+extern unsigned short *position;
+extern unsigned char *material;
+extern doublecomplex cc_sqrt[MAX_NMAT][3];
+extern doublecomplex *xvec, *pvec, *Einc;
+extern const double iter_eps;
+extern const enum init_field InitField;
+extern const bool recalc_resid;
+extern clock_t Timing_Dm_Init, Timing_FFT_Init, Timing_OneIter, Timing_InitIter, Timing_MVP;
+extern size_t TotalIter, TotalMatVec;
+/* host services: io.c */
+void LogError(enum enwho who, const char *srcfile, int srcline, const char *fmt, ...);
+void LogWarning(enum ec code, enum enwho who, const char *srcfile, int srcline, const char *fmt, ...);
+void PrintBoth(FILE *file, const char *fmt, ...);
+
+/* the reference's fft.c also defines these globals; other reference files may name them */
+doublecomplex *Xmatrix, *Dmatrix, *slices, *slices_tr;
+double *BT_buffer, *BT_rbuffer;
+
+#define ERR(...) LogError(ONE, __FILE__, __LINE__, __VA_ARGS__)
+
+static adda_gb300_ctx *g_ctx;
+static doublecomplex g_ccs[MAX_NMAT][3];
+static int g_ccs_valid;
+
+static int env_prec(void)
+{
+	const char *p = getenv("ADDA_GB300_PREC");
+	return (p && !strcmp(p, "mixed")) ? ADDA_PREC_MIXED : ADDA_PREC_FP64;
+}
+
+int fftFit(int x, int divis)
+{
+	return adda_gb300_fft_fit(x, divis);
+}
+
+void CheckNprocs(void)
+{
+	if (nprocs != 1) ERR("The GPU build runs one process per GPU; %d processes were started", nprocs);
+}
+
+void InitDmatrix(void)
+{
+	clock_t start = clock();
+	if (surface) ERR("The GPU build does not support -surf");
+	if (IntRelation != G_POINT_DIP) ERR("The GPU build supports only the point-dipole interaction (-int poi)");
+	if (!reduced_FFT) ERR("The GPU build requires the reduced FFT (do not use -no_reduced_fft)");
+	local_Nsmall = (gridX / 2) * (gridYZ / 2); /* fft.c:975 with nprocs=1 */
+	if (logfile) fprintf(logfile, "The FFT grid is: %zux%zux%zu\n", gridX, gridY, gridZ);
+	/* device memory of the matvec (D in FP64+FP32, expanded grid, chunk buffer) for the log */
+	double dlen = 6.0 * gridX * (gridY / 2 + 1) * (gridZ / 2 + 1);
+	double mem = 24 * dlen + 16.0 * 3 * gridX * boxY * boxZ;
+	PrintBoth(logfile, "Memory usage for MatVec matrices (GPU): %.1f MB\n", mem / (1024.0 * 1024.0));
+	if (prognosis) return;
+	adda_gb300_problem p;
+	memset(&p, 0, sizeof(p));
+	p.boxX = boxX; p.boxY = boxY; p.boxZ = boxZ;
+	p.gridX = (int)gridX; p.gridY = (int)gridY; p.gridZ = (int)gridZ;
+	p.ndip = local_nvoid_Ndip;
+	p.position = position;
+	p.material = material;
+	p.gridspace = gridspace;
+	p.wavenum = WaveNum;
+	p.nrhs_max = 1;
+	p.device = getenv("ADDA_GB300_DEVICE") ? atoi(getenv("ADDA_GB300_DEVICE")) : 0;
+	if (adda_gb300_create(&p, &g_ctx)) ERR("GPU initialisation failed: %s", adda_gb300_last_error());
+	if (adda_gb300_init_dmatrix(g_ctx)) ERR("GPU D-matrix initialisation failed: %s", adda_gb300_last_error());
+	g_ccs_valid = 0;
+	Timing_Dm_Init = clock() - start;
+	Timing_FFT_Init = 0;
+}
+
+void Free_FFT_Dmat(void)
+{
+	if (g_ctx) adda_gb300_destroy(g_ctx);
+	g_ctx = NULL;
+}
+
+/* InitCC (calculator.c:266) may change cc_sqrt between the two polarisations: upload when it changed */
+static void sync_cc(void)
+{
+	if (g_ccs_valid && !memcmp(g_ccs, cc_sqrt, sizeof(g_ccs))) return;
+	if (adda_gb300_set_cc_sqrt(g_ctx, 0, Nmat, (const double *)cc_sqrt))
+		ERR("GPU: %s", adda_gb300_last_error());
+	memcpy(g_ccs, cc_sqrt, sizeof(g_ccs));
+	g_ccs_valid = 1;
+}
+
+void MatVec(doublecomplex *argvec, doublecomplex *resultvec, double *inprod, bool her, clock_t *timing,
+	clock_t *comm_timing)
+{
+	(void)comm_timing;
+	clock_t t0 = clock();
+	if (inprod && !ipr_required) ERR("Incompatibility error in MatVec"); /* matvec.c:184 */
+	if (!g_ctx) ERR("MatVec called before InitDmatrix");
+	sync_cc();
+	if (adda_gb300_matvec(g_ctx, ADDA_PREC_FP64, 1, (const double *)argvec, (double *)resultvec, inprod, her))
+		ERR("GPU MatVec failed: %s", adda_gb300_last_error());
+	*timing += clock() - t0;
+	TotalMatVec++;
+}
+
+/* ProgressReport output format, iterative.c:69-70, 295-305 */
+static void report(int niter, double err, double prev_err, int counter)
+{
+	double progr = 1 - err / prev_err;
+	const char *tag = (counter == 0) ? "+ " : (progr > 0 ? "-+" : "- ");
+	if (!orient_avg && logfile) fprintf(logfile, "RE_%03d = %.10E  %s  progress =% .6f\n", niter, err, tag, progr);
+	printf("RE_%03d = %.10E  %s\n", niter, err, tag);
+}
+
+int IterativeSolver(enum iter method, enum incpol which)
+{
+	(void)which;
+	adda_gb300_solve_params sp;
+	memset(&sp, 0, sizeof(sp));
+	if (method == IT_QMR_CS) sp.method = ADDA_ITER_QMR_CS;
+	else if (method == IT_BICGSTAB) sp.method = ADDA_ITER_BICGSTAB;
+	else ERR("The GPU build supports -iter qmr and -iter bicgstab only");
+	if (InitField == IF_AUTO) sp.init_field = ADDA_IF_AUTO;
+	else if (InitField == IF_ZERO) sp.init_field = ADDA_IF_ZERO;
+	else if (InitField == IF_INC) sp.init_field = ADDA_IF_INC;
+	else ERR("The GPU build supports -init_field auto|zero|inc only");
+	if (!g_ctx) ERR("IterativeSolver called before InitDmatrix");
+	sp.precision = env_prec();
+	sp.eps = iter_eps;
+	sp.maxiter = maxiter;
+	clock_t t0 = clock();
+	sync_cc();
+	const int cap = (maxiter < 100000 ? maxiter : 100000) + 2;
+	double *hist = calloc((size_t)cap, sizeof(double));
+	adda_gb300_rhs_stats st;
+	int rc = adda_gb300_solve(g_ctx, &sp, 1, (const double *)Einc, (double *)xvec, (double *)pvec, &st, hist, cap);
+	if (rc < 0) ERR("GPU IterativeSolver failed: %s", adda_gb300_last_error());
+	/* print the initial field choice and the residual history like IterativeSolver/ProgressReport */
+	if (sp.precision == ADDA_PREC_FP64) {
+		const char *descr = (sp.init_field == ADDA_IF_ZERO || (sp.init_field == ADDA_IF_AUTO && hist[0] == 1.0))
+			? "x_0 = 0\n" : "x_0 = E_inc\n";
+		if (!orient_avg && logfile) fprintf(logfile, "%sRE_%03d = %.10E\n", descr, 0, hist[0]);
+		printf("%sRE_%03d = %.10E\n", descr, 0, hist[0]);
+		double best = hist[0], prev = hist[0];
+		int counter = 0;
+		for (int i = 1; i <= st.niter && i < cap; i++) {
+			if (hist[i] <= best) { best = hist[i]; counter = 0; }
+			else counter++;
+			report(i, hist[i], prev, counter);
+			prev = hist[i];
+		}
+	}
+	else {
+		PrintBoth(logfile, "Mixed precision: %d FP32 iterations, %d FP64 refinement steps, final FP64 residual "
+			"RE = %.10E\n", st.niter, st.refinements, st.resid);
+	}
+	free(hist);
+	if (st.status == ADDA_GB300_EBREAKDOWN) ERR("Krylov solver breakdown on the GPU (iteration %d)", st.niter);
+	if (st.status == ADDA_GB300_ESTAGNATION)
+		ERR("Residual norm haven't decreased for maximum allowed number of iterations");
+	if (st.status == ADDA_GB300_EMAXITER)
+		LogWarning(EC_WARN, ONE, __FILE__, __LINE__, "Iterations haven't converged in %d iterations. Further "
+			"calculated scattering quantities may be less accurate.", maxiter);
+	if (recalc_resid) { /* iterative.c:1512-1520: |A.x - b|^2 / |b|^2 with the FP64 matvec */
+		doublecomplex *ax = malloc(sizeof(doublecomplex) * local_nRows);
+		clock_t tm = 0;
+		MatVec(xvec, ax, NULL, false, &tm, NULL);
+		double num = 0, den = 0;
+		for (size_t i = 0; i < local_nvoid_Ndip; i++)
+			for (int c = 0; c < 3; c++) {
+				doublecomplex b = cc_sqrt[material[i]][c] * Einc[3 * i + c];
+				doublecomplex d = ax[3 * i + c] - b;
+				num += creal(d) * creal(d) + cimag(d) * cimag(d);
+				den += creal(b) * creal(b) + cimag(b) * cimag(b);
+			}
+		free(ax);
+		if (!orient_avg && logfile) fprintf(logfile, "Final (recalculated) residual norm: %.10E\n", sqrt(num / den));
+		printf("Final (recalculated) residual norm: %.10E\n", sqrt(num / den));
+	}
+	TotalIter += (size_t)st.niter;
+	TotalMatVec += (size_t)(st.matvecs_fp64 + st.matvecs_fp32);
+	Timing_InitIter = 0;
+	Timing_MVP = clock() - t0;
+	Timing_OneIter = st.niter ? (clock() - t0) / st.niter : 0;
+	return st.niter;
+}

@@ -117,6 +117,9 @@ int adda_gb300_get_dmatrix(adda_gb300_ctx *ctx, double *out);
 
 /* InitCC, src/calculator.c:266-289, for right-hand side rhs: cc per material [nmat][3] complex */
 int adda_gb300_set_cc(adda_gb300_ctx *ctx, int rhs, int nmat, const double *cc);
+/* same with the square roots given directly (the reference's cc_sqrt[MAX_NMAT][3] after InitCC); cc = cc_sqrt^2 is
+ * kept for the absorption cross section */
+int adda_gb300_set_cc_sqrt(adda_gb300_ctx *ctx, int rhs, int nmat, const double *cc_sqrt);
 /* per-dipole polarisabilities [ndip][3] complex for right-hand side rhs (inhomogeneous media) */
 int adda_gb300_set_cc_dipole(adda_gb300_ctx *ctx, int rhs, const double *cc);
 

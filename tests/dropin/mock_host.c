@@ -1,0 +1,122 @@
+/* mock_host.c - a minimal stand-in for the reference's C host, for testing the drop-in layer (adda_dropin.c) where
+ * the reference sources are not available. It defines the reference globals the drop-in reads (with the reference's
+ * names and types, vars.c / param.c / timing.c / calculator.c), the three io.c services it calls, and a main() that
+ * drives the drop-in exactly like Calculator/CalculateE do: ParSetup's fftFit, InitDmatrix, IterativeSolver,
+ * MatVec, Free_FFT_Dmat. Inputs come from libadda_gb300's host-side setup.
+ *
+ * usage: mock_host <grid> <m_re> <m_im> <dpl> <qmr|bicgstab> <eps_exponent> <out.bin>
+ * writes: ndip (int64), then pvec and a MatVec of Einc (complex doubles, 3*ndip each)
+ */
+#include "adda_gb300.h"
+#include "adda_dropin.h"
+
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+enum enwho { ALL, ONE };
+enum ec { EC_OK, EC_ERROR, EC_WARN, EC_INFO };
+enum inter { G_FCD, G_FCD_ST, G_IGT, G_IGT_SO, G_NLOC, G_NLOC_AV, G_POINT_DIP, G_SO };
+enum init_field { IF_AUTO, IF_ZERO, IF_INC, IF_READ, IF_WKB };
+
+int boxX, boxY, boxZ, nprocs = 1, Nmat = 1, maxiter = 100000;
+size_t gridX, gridY, gridZ, gridYZ, local_Nsmall, local_nvoid_Ndip, local_nRows;
+double gridspace, WaveNum, memory;
+bool prognosis = false, reduced_FFT = true, surface = false, orient_avg = false, ipr_required = false;
+enum inter IntRelation = G_POINT_DIP;
+FILE *logfile;
+unsigned short *position;
+unsigned char *material;
+doublecomplex cc_sqrt[15][3];
+doublecomplex *xvec, *pvec, *Einc;
+double iter_eps = 1e-5;
+enum init_field InitField = IF_AUTO;
+bool recalc_resid = true;
+clock_t Timing_Dm_Init, Timing_FFT_Init, Timing_OneIter, Timing_InitIter, Timing_MVP;
+size_t TotalIter, TotalMatVec;
+
+void LogError(enum enwho who, const char *srcfile, int srcline, const char *fmt, ...)
+{
+	(void)who;
+	va_list a;
+	va_start(a, fmt);
+	fprintf(stderr, "ERROR: (%s:%d) ", srcfile, srcline);
+	vfprintf(stderr, fmt, a);
+	fprintf(stderr, "\n");
+	va_end(a);
+	exit(1);
+}
+
+void LogWarning(enum ec code, enum enwho who, const char *srcfile, int srcline, const char *fmt, ...)
+{
+	(void)code; (void)who; (void)srcfile; (void)srcline;
+	va_list a;
+	va_start(a, fmt);
+	fprintf(stderr, "WARNING: ");
+	vfprintf(stderr, fmt, a);
+	fprintf(stderr, "\n");
+	va_end(a);
+}
+
+void PrintBoth(FILE *file, const char *fmt, ...)
+{
+	va_list a;
+	va_start(a, fmt);
+	if (file) vfprintf(file, fmt, a);
+	va_end(a);
+	va_start(a, fmt);
+	vprintf(fmt, a);
+	va_end(a);
+}
+
+int main(int argc, char **argv)
+{
+	if (argc < 8) return 2;
+	const int grid = atoi(argv[1]);
+	const double mre = atof(argv[2]), mim = atof(argv[3]), dpl = atof(argv[4]);
+	const enum iter method = strcmp(argv[5], "bicgstab") ? IT_QMR_CS : IT_BICGSTAB;
+	iter_eps = pow(10, -atof(argv[6]));
+	logfile = stdout;
+	CheckNprocs();
+	if (adda_gb300_fit_box(ADDA_SHAPE_SPHERE, NULL, grid, &boxY, &boxZ)) return 3;
+	boxX = grid;
+	local_nvoid_Ndip = adda_gb300_make_particle(ADDA_SHAPE_SPHERE, NULL, boxX, boxY, boxZ, NULL, NULL);
+	local_nRows = 3 * local_nvoid_Ndip;
+	position = malloc(sizeof(unsigned short) * local_nRows);
+	material = malloc(local_nvoid_Ndip);
+	adda_gb300_make_particle(ADDA_SHAPE_SPHERE, NULL, boxX, boxY, boxZ, position, material);
+	gridX = fftFit(2 * boxX, 1); /* ParSetup, comm.c:489-491 */
+	gridY = fftFit(2 * boxY, 1);
+	gridZ = fftFit(2 * boxZ, 2);
+	gridYZ = gridY * gridZ;
+	WaveNum = 1.0;
+	gridspace = 2 * M_PI / dpl;
+	double prop[3], py[3], px[3], cc[6];
+	adda_gb300_rotation(NULL, 0, 0, 0, prop, py, px);
+	adda_gb300_polarizability(ADDA_POL_LDR, mre, mim, 2 * M_PI / dpl, gridspace, prop, py, 0, cc);
+	for (int c = 0; c < 3; c++) cc_sqrt[0][c] = csqrt(cc[2 * c] + I * cc[2 * c + 1]);
+	Einc = malloc(sizeof(doublecomplex) * local_nRows);
+	xvec = malloc(sizeof(doublecomplex) * local_nRows);
+	pvec = malloc(sizeof(doublecomplex) * local_nRows);
+	adda_gb300_plane_wave(local_nvoid_Ndip, position, boxX, boxY, boxZ, gridspace, WaveNum, prop, py, (double *)Einc);
+	InitDmatrix();
+	int niter = IterativeSolver(method, INCPOL_Y);
+	doublecomplex *y = malloc(sizeof(doublecomplex) * local_nRows);
+	clock_t t = 0;
+	ipr_required = true;
+	double ip = 0;
+	MatVec(Einc, y, &ip, false, &t, NULL);
+	FILE *f = fopen(argv[7], "wb");
+	long long n = (long long)local_nvoid_Ndip;
+	fwrite(&n, sizeof(n), 1, f);
+	fwrite(&niter, sizeof(niter), 1, f);
+	fwrite(&ip, sizeof(ip), 1, f);
+	fwrite(pvec, sizeof(doublecomplex), local_nRows, f);
+	fwrite(y, sizeof(doublecomplex), local_nRows, f);
+	fclose(f);
+	Free_FFT_Dmat();
+	printf("mock host: %lld dipoles, %d iterations, %zu matvecs\n", n, niter, TotalMatVec);
+	return 0;
+}
