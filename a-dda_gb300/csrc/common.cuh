@@ -1,8 +1,10 @@
 // common.cuh - complex arithmetic, FFT plans and the shared-memory tile FFT used by every kernel of the library.
 //
 // The tile FFT transforms nl lines of length n held in shared memory in ELEMENT-MAJOR order (element e of line l at
-// a[e*nl + l]): consecutive threads work on consecutive lines, so every shared-memory access of a pass is
-// conflict-free, and tiles gathered from HBM along the contiguous axis of the data need no transpose. Each pass is a
+// a[e*ls + l], ls = odd stride >= nl): consecutive threads work on consecutive lines, so every pass is conflict-free,
+// and the odd stride also keeps the element-strided accesses of the load/store phases conflict-free (an 8-byte
+// element at an odd stride visits every bank pair once per 16 threads). Tiles gathered from HBM along the contiguous
+// axis of the data need no transpose. Each pass is a
 // self-sorting Stockham radix-R step (ping-pong between two tiles); radices 2,3,4,8,16 are hand-written register
 // butterflies, 5/7/11/13 use a looped O(R^2) butterfly. Twiddles come from one table of n-th roots of unity per length, computed on the
 // host in double precision. Sign convention: forward = exp(-2*pi*i*jk/n), unnormalised, like FFTW's FFTW_FORWARD
@@ -155,7 +157,7 @@ template <typename C, int R> __device__ __forceinline__ void dft(C *v, bool inv,
 
 // One Stockham pass over all lines of an element-major tile: x -> y.
 template <typename C, int R>
-__device__ __forceinline__ void fft_pass(const C *__restrict__ x, C *__restrict__ y, int n, int nl, int m,
+__device__ __forceinline__ void fft_pass(const C *__restrict__ x, C *__restrict__ y, int n, int nl, int ls, int m,
 	const C *__restrict__ tw, bool inv)
 {
 	const int nr = n / R;
@@ -167,7 +169,7 @@ __device__ __forceinline__ void fft_pass(const C *__restrict__ x, C *__restrict_
 		const int k = j % m;
 		C v[R];
 #pragma unroll
-		for (int q = 0; q < R; q++) v[q] = x[(j + q * nr) * nl + l];
+		for (int q = 0; q < R; q++) v[q] = x[(j + q * nr) * ls + l];
 		if (k) {
 #pragma unroll
 			for (int q = 1; q < R; q++) {
@@ -179,7 +181,7 @@ __device__ __forceinline__ void fft_pass(const C *__restrict__ x, C *__restrict_
 		dft<C, R>(v, inv, tw, n);
 		const int base = (j / m) * m * R + k;
 #pragma unroll
-		for (int q = 0; q < R; q++) y[(base + q * m) * nl + l] = v[q];
+		for (int q = 0; q < R; q++) y[(base + q * m) * ls + l] = v[q];
 	}
 }
 
@@ -187,8 +189,8 @@ __device__ __forceinline__ void fft_pass(const C *__restrict__ x, C *__restrict_
 // one table lookup, tw[(p*k*(n/(m*R)) + (q*p mod R)*(n/R)) mod n]; loops instead of register arrays keep the register
 // footprint of the hot radix-2^k kernels low.
 template <typename C>
-__device__ __noinline__ void fft_pass_gen(const C *__restrict__ x, C *__restrict__ y, int R, int n, int nl, int m,
-	const C *__restrict__ tw, bool inv)
+__device__ __noinline__ void fft_pass_gen(const C *__restrict__ x, C *__restrict__ y, int R, int n, int nl, int ls,
+	int m, const C *__restrict__ tw, bool inv)
 {
 	const int nr = n / R;
 	const int total = nr * nl;
@@ -205,29 +207,32 @@ __device__ __noinline__ void fft_pass_gen(const C *__restrict__ x, C *__restrict
 				const int e = (p * k * tstep + ((q * p) % R) * st) % n;
 				C t = __ldg(tw + e);
 				if (inv) t.y = -t.y;
-				acc = cfma(x[(j + p * nr) * nl + l], t, acc);
+				acc = cfma(x[(j + p * nr) * ls + l], t, acc);
 			}
-			y[(base + q * m) * nl + l] = acc;
+			y[(base + q * m) * ls + l] = acc;
 		}
 	}
 }
 
-// Full FFT of an element-major tile (n elements x nl lines) in a, using b as scratch. Returns the buffer holding the
-// result (a or b). All threads of the block must call it; it synchronises between passes and at the end.
+// odd line stride for an element-major tile of nl lines
+__host__ __device__ constexpr int tile_ls(int nl) { return nl | 1; }
+
+// Full FFT of an element-major tile (n elements x nl lines, stride ls) in a, using b as scratch. Returns the buffer
+// holding the result (a or b). All threads of the block must call it; it synchronises between passes and at the end.
 template <typename C>
-__device__ C *fft_tile(C *a, C *b, const FftPlan &p, int nl, const C *__restrict__ tw, bool inv)
+__device__ C *fft_tile(C *a, C *b, const FftPlan &p, int nl, int ls, const C *__restrict__ tw, bool inv)
 {
 	const int n = p.n;
 	int m = 1;
 	for (int f = 0; f < p.np; f++) {
 		const int R = p.r[f];
 		switch (R) {
-			case 2: fft_pass<C, 2>(a, b, n, nl, m, tw, inv); break;
-			case 3: fft_pass<C, 3>(a, b, n, nl, m, tw, inv); break;
-			case 4: fft_pass<C, 4>(a, b, n, nl, m, tw, inv); break;
-			case 8: fft_pass<C, 8>(a, b, n, nl, m, tw, inv); break;
-			case 16: fft_pass<C, 16>(a, b, n, nl, m, tw, inv); break;
-			default: fft_pass_gen<C>(a, b, R, n, nl, m, tw, inv); break; // 5, 7, 11, 13
+			case 2: fft_pass<C, 2>(a, b, n, nl, ls, m, tw, inv); break;
+			case 3: fft_pass<C, 3>(a, b, n, nl, ls, m, tw, inv); break;
+			case 4: fft_pass<C, 4>(a, b, n, nl, ls, m, tw, inv); break;
+			case 8: fft_pass<C, 8>(a, b, n, nl, ls, m, tw, inv); break;
+			case 16: fft_pass<C, 16>(a, b, n, nl, ls, m, tw, inv); break;
+			default: fft_pass_gen<C>(a, b, R, n, nl, ls, m, tw, inv); break; // 5, 7, 11, 13
 		}
 		__syncthreads();
 		C *t = a;

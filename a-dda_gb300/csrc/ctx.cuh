@@ -107,9 +107,9 @@ int dmatrix_build(adda_gb300_ctx *c);
 // matvec.cu
 int matvec_setup(adda_gb300_ctx *c); // kernel attributes, chunk sizes
 size_t matvec_partial_blocks(const adda_gb300_ctx *c, bool dbl); // partial-sum blocks per RHS of the epilogue
-template <typename T>
-int matvec_run(adda_gb300_ctx *c, int R, const typename CxT<T>::type *arg, typename CxT<T>::type *res, int her,
-	const MvEpi &epi, const int *done);
+// T = FFT/D arithmetic (float or double), V = dipole-vector type (float2 or double2)
+template <typename T, typename V>
+int matvec_run(adda_gb300_ctx *c, int R, const V *arg, V *res, int her, const MvEpi &epi, const int *done);
 int reduce_partials(adda_gb300_ctx *c, int R, const double *partial, size_t nblk, double *out);
 
 // solver.cu

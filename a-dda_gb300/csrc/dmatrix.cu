@@ -70,8 +70,9 @@ __global__ void __launch_bounds__(256) fft_lines(C *data, FftPlan p, const C *__
 	size_t ls, int nl_inner, size_t od, int TL)
 {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
+	const int LS = tile_ls(TL);
 	C *a = reinterpret_cast<C *>(smem_raw);
-	C *b = a + (size_t)p.n * TL;
+	C *b = a + (size_t)p.n * LS;
 	const int n = p.n;
 	const int l0 = blockIdx.x * TL;
 	const int tl = min(TL, nl_inner - l0);
@@ -81,15 +82,15 @@ __global__ void __launch_bounds__(256) fft_lines(C *data, FftPlan p, const C *__
 		int e, l;
 		if (contig) { l = t / n; e = t % n; }
 		else { e = t / TL; l = t % TL; }
-		a[e * TL + l] = (l < tl) ? base[(size_t)l * ls + (size_t)e * es] : cx<C>(0, 0);
+		a[e * LS + l] = (l < tl) ? base[(size_t)l * ls + (size_t)e * es] : cx<C>(0, 0);
 	}
 	__syncthreads();
-	C *o = fft_tile<C>(a, b, p, TL, tw, inv != 0);
+	C *o = fft_tile<C>(a, b, p, TL, LS, tw, inv != 0);
 	for (int t = threadIdx.x; t < n * TL; t += blockDim.x) {
 		int e, l;
 		if (contig) { l = t / n; e = t % n; }
 		else { e = t / TL; l = t % TL; }
-		if (l < tl) base[(size_t)l * ls + (size_t)e * es] = o[e * TL + l];
+		if (l < tl) base[(size_t)l * ls + (size_t)e * es] = o[e * LS + l];
 	}
 }
 
@@ -149,8 +150,8 @@ int fft_lines_run(adda_gb300_ctx *c, double2 *data, const FftPlan &p, const doub
 	size_t ls, int nl_inner, size_t od, int nouter)
 {
 	int TL = 16;
-	while (TL > 1 && 2 * sizeof(double2) * (size_t)p.n * TL > 200 * 1024) TL /= 2;
-	const size_t smem = 2 * sizeof(double2) * (size_t)p.n * TL;
+	while (TL > 1 && 2 * sizeof(double2) * (size_t)p.n * tile_ls(TL) > 200 * 1024) TL /= 2;
+	const size_t smem = 2 * sizeof(double2) * (size_t)p.n * tile_ls(TL);
 	ADDA_CUDA(cudaFuncSetAttribute(fft_lines<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 	dim3 g((nl_inner + TL - 1) / TL, nouter);
 	fft_lines<double2><<<g, 256, smem, c->stream>>>(data, p, tw, inv ? 1 : 0, es, ls, nl_inner, od, TL);

