@@ -306,7 +306,8 @@ def run_profile(args):
         einc = np.ascontiguousarray(np.stack(s.einc))
         d_e = torch.from_numpy(einc.view(np.float64)).cuda()
         for _ in range(2):
-            st = ctx.solve_device(d_e.data_ptr(), 2, None, None, method=args.method, prec="mixed", eps=EPS)
+            st = ctx.solve_device(d_e.data_ptr(), 2, None, None, method=args.method, prec="mixed", eps=EPS,
+                                  maxiter=args.maxiter)
         print(json.dumps({"mode": args.mode, "ms": ctx.last_solve_ms(), "stats": st}))
     else:
         ms = ctx.time_matvec("fp32", 2, iters=3)
@@ -323,6 +324,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--mode", default="bench", choices=["bench", "profile-solve", "profile-matvec"])
     ap.add_argument("--grid", type=int, default=GRID, help="sphere box size for the profile modes")
+    ap.add_argument("--maxiter", type=int, default=100000, help="iteration cap of the profile-solve mode")
     args = ap.parse_args()
     if args.mode != "bench":
         run_profile(args)
