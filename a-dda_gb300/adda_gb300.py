@@ -46,10 +46,12 @@ class RhsStats(ctypes.Structure):
 
 
 EXPORTS = ["adda_gb300_fft_fit", "adda_gb300_fit_box", "adda_gb300_make_particle", "adda_gb300_rotation",
-           "adda_gb300_plane_wave", "adda_gb300_polarizability", "adda_gb300_create", "adda_gb300_destroy",
+           "adda_gb300_plane_wave", "adda_gb300_polarizability", "adda_gb300_polarizability_dchi",
+           "adda_gb300_create", "adda_gb300_destroy",
            "adda_gb300_get_grid", "adda_gb300_init_dmatrix", "adda_gb300_dmatrix_len", "adda_gb300_get_dmatrix",
            "adda_gb300_set_cc", "adda_gb300_set_cc_sqrt", "adda_gb300_set_cc_dipole", "adda_gb300_matvec", "adda_gb300_matvec_device",
-           "adda_gb300_solve", "adda_gb300_solve_device", "adda_gb300_cross_sections", "adda_gb300_time_matvec",
+           "adda_gb300_solve", "adda_gb300_solve_device", "adda_gb300_vjp_chi", "adda_gb300_cross_sections",
+           "adda_gb300_time_matvec",
            "adda_gb300_last_solve_ms", "adda_gb300_last_error", "adda_gb300_kernel_launches"]
 
 _lib = None
@@ -77,6 +79,8 @@ def lib():
             "adda_gb300_rotation": ([P, D, D, D, P, P, P], None),
             "adda_gb300_plane_wave": ([SZ, P, I, I, I, D, D, P, P, P], None),
             "adda_gb300_polarizability": ([I, D, D, D, D, P, P, I, P], I),
+            "adda_gb300_polarizability_dchi": ([I, D, D, D, D, P, P, I, P], I),
+            "adda_gb300_vjp_chi": ([P, P, I, P, P, P, P, P], I),
             "adda_gb300_create": ([P, P], I),
             "adda_gb300_destroy": ([P], I),
             "adda_gb300_get_grid": ([P, P], I),
@@ -165,6 +169,16 @@ def polarizability(m, kd, gridspace, prop, incpol, relation="ldr", avgpol=False)
 
 VOLUME_RATIO = {"sphere": lambda p: math.pi / 6, "ellipsoid": lambda p: math.pi / 6 * p[0] * p[1],
                 "box": lambda p: p[0] * p[1]}
+
+
+def polarizability_dchi(m, kd, gridspace, prop, incpol, relation="ldr", avgpol=False):
+    """d(1/alpha)/dchi, chi = (m^2-1)/(4 pi)"""
+    out = np.zeros(1, np.complex128)
+    _check(lib().adda_gb300_polarizability_dchi(POLS[relation], complex(m).real, complex(m).imag, kd, gridspace,
+                                                _p(np.ascontiguousarray(prop, float)),
+                                                _p(np.ascontiguousarray(incpol, float)), int(avgpol), _p(out)),
+           "polarizability_dchi")
+    return out[0]
 
 
 class Setup:
@@ -298,6 +312,17 @@ class Context:
         _check(self.L.adda_gb300_time_matvec(self.h, PREC[prec], nrhs, iters, flush_bytes, ctypes.byref(ms)),
                "time_matvec")
         return ms.value
+
+    def vjp_chi(self, rhs, prop, incpol, dinv_alpha, method="qmr", prec="fp64", eps=1e-10, maxiter=100000):
+        """gradients of Cext and Cabs of RHS `rhs` of the last solve w.r.t. each dipole's chi: two [N,2] arrays
+        (d/dRe chi, d/dIm chi)"""
+        f = np.ascontiguousarray(dinv_alpha, dtype=np.complex128).reshape(self.n)
+        ge = np.zeros((self.n, 2))
+        ga = np.zeros((self.n, 2))
+        sp = SolveParams(ITERS[method], PREC[prec], eps, maxiter, INIT["zero"], 0, 0.0, 0)
+        _check(self.L.adda_gb300_vjp_chi(self.h, ctypes.byref(sp), rhs, _p(np.ascontiguousarray(prop, float)),
+                                         _p(np.ascontiguousarray(incpol, float)), _p(f), _p(ge), _p(ga)), "vjp_chi")
+        return ge, ga
 
     def cross_sections(self, prop, incpol):
         """prop/incpol: [nrhs,3]; returns (Cext[nrhs], Cabs[nrhs]) from the last solve's polarisations."""

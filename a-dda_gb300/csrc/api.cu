@@ -530,6 +530,17 @@ int adda_gb300_time_matvec(adda_gb300_ctx *c, int prec, int nrhs, int iters, siz
 	return ADDA_GB300_OK;
 }
 
+int adda_gb300_vjp_chi(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int rhs, const double prop[3],
+	const double incpol[3], const double *dinv_alpha, double *grad_cext, double *grad_cabs)
+{
+	if (!c || !sp || !prop || !incpol || !dinv_alpha || !grad_cext || !grad_cabs) {
+		set_error("vjp_chi: invalid arguments");
+		return ADDA_GB300_EINVAL;
+	}
+	ADDA_CUDA(cudaSetDevice(c->device));
+	return vjp_chi(c, sp, rhs, prop, incpol, dinv_alpha, grad_cext, grad_cabs);
+}
+
 int adda_gb300_cross_sections(adda_gb300_ctx *c, int nrhs, const double *prop, const double *incpol, double *cext,
 	double *cabs)
 {

@@ -183,6 +183,37 @@ int adda_gb300_polarizability(int relation, double m_re, double m_im, double kd,
 	return ADDA_GB300_OK;
 }
 
+int adda_gb300_polarizability_dchi(int relation, double m_re, double m_im, double kd, double gridspace,
+	const double prop[3], const double incPol[3], int avgpol, double out[2])
+{
+	/* 1/alpha = 1/alpha_CM - M/d^3 with 1/alpha_CM = 4pi/(3d^3) + 1/(d^3 chi), chi = (m^2-1)/(4pi), and for LDR
+	 * M = (b1 + (b2 + b3 S) m^2) kd^2 + 2i kd^3/3 (calculator.c:100-132, 214-222); CM, RRC and DGF have M independent
+	 * of m, so d(1/alpha)/dchi = -1/(d^3 chi^2) - 4pi (b2 + b3 S) kd^2/d^3 [LDR only] */
+	const double dipvol = gridspace * gridspace * gridspace;
+	const double complex m = m_re + I * m_im;
+	const double complex chi = (m * m - 1) / FOUR_PI_D;
+	double complex r = -1 / (dipvol * chi * chi);
+	switch (relation) {
+		case ADDA_POL_CM:
+		case ADDA_POL_RRC:
+		case ADDA_POL_DGF: break;
+		case ADDA_POL_LDR: {
+			const double b2 = -0.1648469, b3 = 1.7700004;
+			double S;
+			if (avgpol) S = 0.5 * (1 - (prop[0] * prop[0] * prop[0] * prop[0] + prop[1] * prop[1] * prop[1] * prop[1]
+				+ prop[2] * prop[2] * prop[2] * prop[2]));
+			else S = prop[0] * prop[0] * incPol[0] * incPol[0] + prop[1] * prop[1] * incPol[1] * incPol[1]
+				+ prop[2] * prop[2] * incPol[2] * incPol[2];
+			r -= FOUR_PI_D * (b2 + b3 * S) * kd * kd / dipvol;
+			break;
+		}
+		default: return ADDA_GB300_EINVAL;
+	}
+	out[0] = creal(r);
+	out[1] = cimag(r);
+	return ADDA_GB300_OK;
+}
+
 int adda_gb300_fft_fit(int x, int divis)
 {
 	if (x < 1 || divis < 1) return ADDA_GB300_EINVAL;

@@ -648,6 +648,59 @@ __global__ void __launch_bounds__(NT) k_cross(const double2 *P, const uint16_t *
 	}
 }
 
+// adjoint right-hand sides for the VJP (written as "incident fields" E so that the solver's b = S.E gives the scaled
+// system): E0_j = c_j incpol with c_j = (4pi/k^2)(-i k^3) exp(-i k r0.n) exp(-i kd n.pos_j)  (d Cext/d P_j), and
+// E1_j = conj(mu_j P_j) with mu_jc = -Im(1/alpha_jc) - 2k^3/3  (half the gradient of Cabs/(4 pi k) w.r.t. conj P)
+__global__ void __launch_bounds__(NT) k_adj_rhs(double2 *E, const double2 *P, const uint16_t *pos, const double2 *cc,
+	int per_dip, int nmat, const uint8_t *mat, size_t N, double n0, double n1, double n2, double e0, double e1,
+	double e2, double kd, double k, double ph0)
+{
+	const double PI = 3.14159265358979323846;
+	const double k3 = k * k * k;
+	for (size_t d = blockIdx.x * (size_t)blockDim.x + threadIdx.x; d < N; d += (size_t)gridDim.x * blockDim.x) {
+		const double ph = ph0 - kd * (n0 * pos[3 * d] + n1 * pos[3 * d + 1] + n2 * pos[3 * d + 2]);
+		double sn, cs;
+		sincos(ph, &sn, &cs);
+		// c = (4pi/k^2) * (-i k^3) * exp(i ph) = 4 pi k (sin ph - i cos ph)
+		const double cr = 4 * PI * k * sn, ci = -4 * PI * k * cs;
+		const double ev[3] = {e0, e1, e2};
+		for (int c = 0; c < 3; c++) {
+			E[d * 3 + c] = make_double2(cr * ev[c], ci * ev[c]);
+			const double2 a = per_dip ? cc[d * 3 + c] : cc[(size_t)mat[d] * 3 + c];
+			const double mu = a.y / (a.x * a.x + a.y * a.y) - 2 * k3 / 3;
+			const double2 p = P[d * 3 + c];
+			E[(N + d) * 3 + c] = make_double2(mu * p.x, -mu * p.y);
+		}
+	}
+}
+
+// per-dipole gradients from the forward P and the adjoint solutions lambda (extinction) and nu (absorption)
+__global__ void __launch_bounds__(NT) k_vjp_grad(const double2 *P, const double2 *lam, const double2 *nu,
+	const double2 *f, size_t N, double k, double *gext, double *gabs)
+{
+	const double PI = 3.14159265358979323846;
+	for (size_t d = blockIdx.x * (size_t)blockDim.x + threadIdx.x; d < N; d += (size_t)gridDim.x * blockDim.x) {
+		double lr = 0, li = 0, nr = 0, ni = 0, p2 = 0;
+		for (int c = 0; c < 3; c++) {
+			const double2 p = P[d * 3 + c], l = lam[d * 3 + c], v = nu[d * 3 + c];
+			lr += l.x * p.x - l.y * p.y;
+			li += l.x * p.y + l.y * p.x;
+			nr += v.x * p.x - v.y * p.y;
+			ni += v.x * p.y + v.y * p.x;
+			p2 += p.x * p.x + p.y * p.y;
+		}
+		const double2 fd = f[d];
+		// dF/dchi = -f sum(lambda P); dCext/dRe = Re, dCext/dIm = -Im
+		const double gr = -(fd.x * lr - fd.y * li), gi = -(fd.x * li + fd.y * lr);
+		gext[2 * d] = gr;
+		gext[2 * d + 1] = -gi;
+		// dCabs/dRe chi = 4pi k (-Im f |P|^2 - 2 Re(f s)); dCabs/dIm chi = 4pi k (-Re f |P|^2 + 2 Im(f s)), s = sum nu P
+		const double fsr = fd.x * nr - fd.y * ni, fsi = fd.x * ni + fd.y * nr;
+		gabs[2 * d] = 4 * PI * k * (-fd.y * p2 - 2 * fsr);
+		gabs[2 * d + 1] = 4 * PI * k * (-fd.x * p2 + 2 * fsi);
+	}
+}
+
 } // namespace
 
 // =====================================================================================================================
@@ -1127,6 +1180,85 @@ int solver_solve_dev(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int R
 	if (d_pvec) ADDA_CUDA(cudaMemcpyAsync(d_pvec, c->pvec64, sizeof(double2) * R * n3, cudaMemcpyDeviceToDevice, s));
 	ADDA_CUDA(cudaStreamSynchronize(s));
 	return ADDA_GB300_OK;
+}
+
+int vjp_chi(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int rhs, const double prop[3], const double incpol[3],
+	const double *dinv_alpha, double *grad_cext, double *grad_cabs)
+{
+	int rc = check_params(sp);
+	if (rc) return rc;
+	if (c->Rmax < 2 || !c->pvec64 || rhs < 0 || rhs >= c->last_nrhs) {
+		set_error("vjp_chi: needs nrhs_max >= 2 and a previous solve covering the requested RHS");
+		return ADDA_GB300_ESTATE;
+	}
+	if ((rc = ensure_work(c, 2, 1))) return rc;
+	SolverWork *w = c->sw;
+	const size_t n3 = w->n3, N = c->N;
+	cudaStream_t s = c->stream;
+	const int last = c->last_nrhs;
+	const size_t per = c->per_dip ? 3 * N : (size_t)c->nmat * 3;
+	// keep the forward polarisations and the cc of slots 0,1; slots 0,1 get the forward RHS's cc
+	double2 *save_p = nullptr, *save_cc = nullptr, *dF = nullptr;
+	double *dg = nullptr;
+	float2 *save_cc32 = nullptr;
+	ADDA_CUDA(cudaMalloc(&save_p, sizeof(double2) * n3 * last));
+	ADDA_CUDA(cudaMalloc(&save_cc, sizeof(double2) * per * 4));
+	ADDA_CUDA(cudaMalloc(&save_cc32, sizeof(float2) * per * 2));
+	ADDA_CUDA(cudaMalloc(&dF, sizeof(double2) * N));
+	ADDA_CUDA(cudaMalloc(&dg, sizeof(double) * 4 * N));
+	ADDA_CUDA(cudaMemcpyAsync(save_p, c->pvec64, sizeof(double2) * n3 * last, cudaMemcpyDeviceToDevice, s));
+	ADDA_CUDA(cudaMemcpyAsync(save_cc, c->cc64, sizeof(double2) * per * 2, cudaMemcpyDeviceToDevice, s));
+	ADDA_CUDA(cudaMemcpyAsync(save_cc + 2 * per, c->ccs64, sizeof(double2) * per * 2, cudaMemcpyDeviceToDevice, s));
+	ADDA_CUDA(cudaMemcpyAsync(save_cc32, c->ccs32, sizeof(float2) * per * 2, cudaMemcpyDeviceToDevice, s));
+	const std::vector<int> cc_set_saved = c->cc_set;
+	for (int slot = 0; slot < 2; slot++)
+		if (slot != rhs) {
+			ADDA_CUDA(cudaMemcpyAsync(c->cc64 + per * slot, c->cc64 + per * rhs, sizeof(double2) * per,
+				cudaMemcpyDeviceToDevice, s));
+			ADDA_CUDA(cudaMemcpyAsync(c->ccs64 + per * slot, c->ccs64 + per * rhs, sizeof(double2) * per,
+				cudaMemcpyDeviceToDevice, s));
+			ADDA_CUDA(cudaMemcpyAsync(c->ccs32 + per * slot, c->ccs32 + per * rhs, sizeof(float2) * per,
+				cudaMemcpyDeviceToDevice, s));
+		}
+	c->cc_set[0] = c->cc_set[1] = 1;
+	// adjoint right-hand sides into the staging buffer of the solve
+	const double kd = c->k * c->gridspace;
+	const double r0[3] = {-c->gridspace * (c->bX - 1) / 2.0, -c->gridspace * (c->bY - 1) / 2.0,
+		-c->gridspace * (c->bZ - 1) / 2.0};
+	const double ph0 = -c->k * (r0[0] * prop[0] + r0[1] * prop[1] + r0[2] * prop[2]);
+	const double2 *ccr = c->cc64 + per * rhs;
+	const int gN = (int)std::max<size_t>(1, std::min<size_t>((N + NT - 1) / NT, 152 * 16));
+	k_adj_rhs<<<gN, NT, 0, s>>>(w->av64, save_p + n3 * rhs, c->d_pos, ccr, c->per_dip, c->nmat, c->d_mat, N, prop[0],
+		prop[1], prop[2], incpol[0], incpol[1], incpol[2], kd, c->k, ph0);
+	ADDA_LAUNCHED();
+	adda_gb300_rhs_stats st[2];
+	rc = solve_core(c, sp, 2, w->av64, st);
+	if (!rc) {
+		ADDA_CUDA(cudaMemcpyAsync(dF, dinv_alpha, sizeof(double2) * N, cudaMemcpyHostToDevice, s));
+		k_vjp_grad<<<gN, NT, 0, s>>>(save_p + n3 * rhs, c->pvec64, c->pvec64 + n3, dF, N, c->k, dg, dg + 2 * N);
+		ADDA_LAUNCHED();
+		ADDA_CUDA(cudaMemcpyAsync(grad_cext, dg, sizeof(double) * 2 * N, cudaMemcpyDeviceToHost, s));
+		ADDA_CUDA(cudaMemcpyAsync(grad_cabs, dg + 2 * N, sizeof(double) * 2 * N, cudaMemcpyDeviceToHost, s));
+		for (int r = 0; r < 2; r++)
+			if (st[r].status) {
+				set_error("vjp_chi: the adjoint solve did not converge");
+				rc = st[r].status;
+			}
+	}
+	// restore the forward state
+	ADDA_CUDA(cudaMemcpyAsync(c->pvec64, save_p, sizeof(double2) * n3 * last, cudaMemcpyDeviceToDevice, s));
+	ADDA_CUDA(cudaMemcpyAsync(c->cc64, save_cc, sizeof(double2) * per * 2, cudaMemcpyDeviceToDevice, s));
+	ADDA_CUDA(cudaMemcpyAsync(c->ccs64, save_cc + 2 * per, sizeof(double2) * per * 2, cudaMemcpyDeviceToDevice, s));
+	ADDA_CUDA(cudaMemcpyAsync(c->ccs32, save_cc32, sizeof(float2) * per * 2, cudaMemcpyDeviceToDevice, s));
+	ADDA_CUDA(cudaStreamSynchronize(s));
+	c->cc_set = cc_set_saved;
+	c->last_nrhs = last;
+	cudaFree(save_p);
+	cudaFree(save_cc);
+	cudaFree(save_cc32);
+	cudaFree(dF);
+	cudaFree(dg);
+	return rc;
 }
 
 int cross_sections(adda_gb300_ctx *c, int R, const double *prop, const double *incpol, double *cext, double *cabs)

@@ -100,6 +100,10 @@ void adda_gb300_plane_wave(size_t ndip, const uint16_t *position, int boxX, int 
 int adda_gb300_polarizability(int relation, double m_re, double m_im, double kd, double gridspace,
 	const double prop[3], const double incPol[3], int avgpol, double cc[6]);
 
+/* d(1/alpha)/dchi for the same relations (chi = (m^2-1)/(4pi), the susceptibility), the input of adda_gb300_vjp_chi */
+int adda_gb300_polarizability_dchi(int relation, double m_re, double m_im, double kd, double gridspace,
+	const double prop[3], const double incPol[3], int avgpol, double out[2]);
+
 /* ---- device context ------------------------------------------------------------------------------------------ */
 
 /* ParSetup + allocation half of InitDmatrix (comm.c:481-535, fft.c:1164-1209): validates the lattice, uploads it
@@ -159,6 +163,15 @@ int adda_gb300_time_matvec(adda_gb300_ctx *ctx, int prec, int nrhs, int iters, s
 /* device time in milliseconds of the last solve on this context: CUDA events recorded on the context's stream at
  * the first and the last kernel of the solve (host-device copies of the host-pointer API excluded) */
 double adda_gb300_last_solve_ms(const adda_gb300_ctx *ctx);
+
+/* Adjoint (VJP) of Cext and Cabs of right-hand side `rhs` of the last solve with respect to every dipole's
+ * susceptibility chi_j (isotropic), by one more solve with the same complex-symmetric matrix (A^T = A), for the two
+ * adjoint right-hand sides at once: extinction (Cext is linear in P, crosssec.c:811-822) and absorption (Cabs is
+ * quadratic in P and depends on alpha, crosssec.c:866-882). dinv_alpha [ndip] complex = d(1/alpha_j)/dchi_j (see
+ * adda_gb300_polarizability_dchi). Outputs [ndip][2]: (dC/dRe chi_j, dC/dIm chi_j). sp selects the arithmetic of the
+ * adjoint solve. Requires nrhs_max >= 2; the forward polarisations stay available for adda_gb300_cross_sections. */
+int adda_gb300_vjp_chi(adda_gb300_ctx *ctx, const adda_gb300_solve_params *sp, int rhs, const double prop[3],
+	const double incpol[3], const double *dinv_alpha, double *grad_cext, double *grad_cabs);
 
 /* last error message of the calling thread */
 const char *adda_gb300_last_error(void);
