@@ -243,4 +243,59 @@ __device__ C *fft_tile(C *a, C *b, const FftPlan &p, int nl, int ls, const C *__
 	return a;
 }
 
+// ---------------------------------------------------------------------------------------------------------------
+// Compile-time plans for power-of-two lengths. Every trip count, stride and divisor of a pass is a constant, so the
+// element/line decomposition costs shifts instead of integer divisions and the passes unroll; the direction is a
+// template parameter too. Radix MAXR first (16 for float, 8 for double), then the remaining power of two.
+
+template <typename C, int R, int N, int NL, int LS, int M, int NT, bool INV>
+__device__ __forceinline__ void fft_pass_s(const C *__restrict__ x, C *__restrict__ y, const C *__restrict__ tw)
+{
+	constexpr int NR = N / R, TOTAL = NR * NL, TSTEP = N / (M * R);
+#pragma unroll 2
+	for (int w = threadIdx.x; w < TOTAL; w += NT) {
+		const int j = w / NL;
+		const int l = w - j * NL;
+		const int k = j & (M - 1);
+		C v[R];
+#pragma unroll
+		for (int q = 0; q < R; q++) v[q] = x[(j + q * NR) * LS + l];
+		if (M > 1) {
+#pragma unroll
+			for (int q = 1; q < R; q++) {
+				C t = __ldg(tw + q * k * TSTEP);
+				if (INV) t.y = -t.y;
+				v[q] = cmul(v[q], t);
+			}
+		}
+		dft<C, R>(v, INV, tw, N);
+		const int base = (j - k) * R + k;
+#pragma unroll
+		for (int q = 0; q < R; q++) y[(base + q * M) * LS + l] = v[q];
+	}
+}
+
+template <typename C, int N, int NL, int LS, int M, int MAXR, int NT, bool INV>
+__device__ __forceinline__ C *fft_static(C *a, C *b, const C *__restrict__ tw)
+{
+	if constexpr (M >= N) {
+		return a;
+	}
+	else {
+		constexpr int REM = N / M;
+		constexpr int R = REM >= MAXR ? MAXR : REM;
+		fft_pass_s<C, R, N, NL, LS, M, NT, INV>(a, b, tw);
+		__syncthreads();
+		return fft_static<C, N, NL, LS, M * R, MAXR, NT, INV>(b, a, tw);
+	}
+}
+
+// tile FFT with a compile-time plan when NS > 0 (power of two), the runtime plan otherwise
+template <typename C, int NS, int NL, int LS, bool INV>
+__device__ __forceinline__ C *tile_fft(C *a, C *b, const FftPlan &p, const C *__restrict__ tw)
+{
+	if constexpr (NS > 0) return fft_static<C, NS, NL, LS, 1, (sizeof(C) == 8 ? 16 : 8), 256, INV>(a, b, tw);
+	else return fft_tile<C>(a, b, p, NL, LS, tw, INV);
+}
+
 } // namespace adda

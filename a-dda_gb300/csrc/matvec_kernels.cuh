@@ -1,0 +1,417 @@
+// matvec_kernels.cuh - the kernels of the FFT-accelerated DDA matvec y = x + S.D.S.x (MatVec, src/matvec.c:128).
+//
+// Data flow for R right-hand sides sharing one interaction matrix D (all in HBM unless noted):
+//   K1 mv_scatter_fftx : per (rhs, z, block of W y-lines): gather S.x of the dipoles of those x-lines straight from
+//                        the dipole vector (no zeroed expanded grid, the reference's Xmatrix fill + Arith1), pad to
+//                        gridX in shared memory, forward FFT along x  ->  Xf[r][kx][comp][z][y]
+//   then per chunk of CK x-slabs (chunk buffer Tz sized to stay in L2):
+//   K2a mv_fftz        : forward FFT along z of each y-line block (zero padding z>=boxZ in shared memory)
+//   K2b mv_fft_y_dmul  : per (kx, kz block, RHS group): forward FFT along y, 6-component symmetric D~ x X~ product
+//                        (D read once per grid point and reused by every RHS of the block), inverse FFT along y
+//   K2c mv_fftz (inv)  : inverse FFT along z, keep z<boxZ  ->  Xf
+//   K3 mv_fftx_gather  : inverse FFT along x, y = x + S.X for the dipoles of the lines, optional Krylov reductions
+//                        (|y|^2, x.y, y.u*, x.y*) as deterministic per-block partial sums.
+// The reference's explicit transposes (TransposeYZ), slice zeroing and copies (Arith2/Arith4) do not exist here:
+// every tile is loaded along the contiguous axis of its buffer and transformed in element-major shared memory.
+// Every kernel is instantiated with a compile-time FFT length NS for the power-of-two grids (all index arithmetic
+// folds to shifts, passes unroll) and with NS = 0 (runtime plan) for the other fftFit sizes. Blocks are 256 threads.
+#pragma once
+
+#include "ctx.cuh"
+
+#include <algorithm>
+
+namespace adda {
+namespace mv {
+
+// T = arithmetic of the FFTs, D and the expanded grid (float or double); V = complex type of the dipole vectors the
+// caller passes (float2 or double2). With T=float, V=double2 (the MIXED solver) the inputs are rounded on the fly and
+// y = x + S.X is accumulated in double, so the identity part of A is exact.
+template <typename T, typename V> struct MvP {
+	typedef typename CxT<T>::type C;
+	int bX, bY, bZ, gX, gY, gZ, DsY, DsZ;
+	int R;
+	size_t N;
+	const uint32_t *line_start;
+	const uint32_t *xy;
+	const uint8_t *mat;
+	const C *ccs;   // per-RHS cc_sqrt: [R][nmat][3] or [R][N][3]
+	int nmat, per_dip;
+	const V *arg;
+	V *res;
+	C *Xf;
+	C *Tz;
+	int CK, kx0;
+	const C *D;
+	FftPlan px, py, pz;
+	const C *twx, *twy, *twz;
+	int her;
+	int KB, RG;      // K2b: kz per block, RHS per block (KB*RG <= Tiles<T>::PAIRS)
+	const int *done; // per-RHS done flags (may be null): every kernel returns at once when all are set
+};
+
+template <typename To, typename From> __device__ __forceinline__ To cvt(From a) { return from_d2<To>(to_d2(a)); }
+
+template <typename P> __device__ __forceinline__ bool all_done(const P &p)
+{
+	if (!p.done) return false;
+	for (int r = 0; r < p.R; r++)
+		if (!p.done[r]) return false;
+	return true;
+}
+
+template <typename C> __device__ __forceinline__ C ccs_of(const C *ccs, int per_dip, int nmat, size_t N, int r,
+	size_t i, uint8_t m, int comp)
+{
+	return per_dip ? ccs[((size_t)r * N + i) * 3 + comp] : ccs[((size_t)r * nmat + m) * 3 + comp];
+}
+
+// tile widths: W1 y-lines per K1/K3 block, W2 y-lines per K2a/K2c block, PAIRS (RHS, kz) pairs per K2b block
+template <typename T> struct Tiles;
+template <> struct Tiles<float> { static constexpr int W1 = 8, W2 = 16, PAIRS = 8; };
+template <> struct Tiles<double> { static constexpr int W1 = 4, W2 = 8, PAIRS = 4; };
+
+// K1: scatter S.x of W consecutive x-lines (one z) into shared memory and FFT along x. Tile: gX x (3*W) lines.
+template <typename T, typename V, int W, int NS> __global__ void __launch_bounds__(256) mv_scatter_fftx(MvP<T, V> p)
+{
+	typedef typename CxT<T>::type C;
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	if (all_done(p)) return;
+	constexpr int NL = 3 * W, LS = tile_ls(3 * W);
+	const int n = NS ? NS : p.gX;
+	C *a = reinterpret_cast<C *>(smem_raw);
+	C *b = a + (size_t)n * LS;
+	const int r = blockIdx.z, z = blockIdx.y, y0 = blockIdx.x * W;
+	const int wy = min(W, p.bY - y0);
+	for (int t = threadIdx.x; t < n * LS; t += 256) a[t] = cx<C>(0, 0);
+	__syncthreads();
+	const size_t line = (size_t)z * p.bY + y0;
+	const uint32_t i0 = p.line_start[line], i1 = p.line_start[line + wy];
+	const V *arg = p.arg + (size_t)r * p.N * 3;
+	const uint32_t cnt = (i1 - i0) * 3;
+#pragma unroll 4
+	for (uint32_t t = threadIdx.x; t < cnt; t += 256) {
+		const size_t i = i0 + t / 3;
+		const int comp = t % 3;
+		const uint32_t q = p.xy[i];
+		const int x = q & 0xffff, y = q >> 16;
+		C v = cvt<C>(arg[i * 3 + comp]);
+		if (p.her) v = cconj(v);
+		v = cmul(ccs_of(p.ccs, p.per_dip, p.nmat, p.N, r, i, p.mat[i], comp), v);
+		a[x * LS + comp * W + (y - y0)] = v;
+	}
+	__syncthreads();
+	C *o = tile_fft<C, NS, NL, LS, false>(a, b, p.px, p.twx);
+	const size_t plane = (size_t)p.bZ * p.bY;
+	C *xf = p.Xf + (size_t)r * p.gX * 3 * plane + (size_t)z * p.bY + y0;
+	for (int t = threadIdx.x; t < n * NL; t += 256) {
+		const int yy = t % W, rest = t / W;
+		const int comp = rest % 3, kx = rest / 3;
+		if (yy < wy) xf[((size_t)kx * 3 + comp) * plane + yy] = o[kx * LS + comp * W + yy];
+	}
+}
+
+// K2a/K2c: FFT along z of W consecutive y-lines of one (rhs, kx, comp). Forward reads Xf (z<bZ, zero padded) and
+// writes Tz (all kz); inverse reads Tz and writes z<bZ back to Xf.
+template <typename T, typename V, int W, bool INV, int NS> __global__ void __launch_bounds__(256) mv_fftz(MvP<T, V> p)
+{
+	typedef typename CxT<T>::type C;
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	if (all_done(p)) return;
+	constexpr int LS = tile_ls(W);
+	const int n = NS ? NS : p.gZ;
+	C *a = reinterpret_cast<C *>(smem_raw);
+	C *b = a + (size_t)n * LS;
+	const int r = blockIdx.z;
+	const int kxl = blockIdx.y / 3, comp = blockIdx.y % 3;
+	const int kx = p.kx0 + kxl;
+	const int y0 = blockIdx.x * W;
+	const int wy = min(W, p.bY - y0);
+	const size_t plane = (size_t)p.bZ * p.bY;
+	C *xf = p.Xf + (((size_t)r * p.gX + kx) * 3 + comp) * plane + y0;
+	C *tz = p.Tz + (((size_t)r * p.CK + kxl) * 3 + comp) * (size_t)n * p.bY + y0;
+#pragma unroll 4
+	for (int t = threadIdx.x; t < n * W; t += 256) {
+		const int yy = t % W, z = t / W;
+		C v = cx<C>(0, 0);
+		if (!INV) {
+			if (z < p.bZ && yy < wy) v = xf[(size_t)z * p.bY + yy];
+		}
+		else if (yy < wy) v = tz[(size_t)z * p.bY + yy];
+		a[z * LS + yy] = v;
+	}
+	__syncthreads();
+	C *o = tile_fft<C, NS, W, LS, INV>(a, b, p.pz, p.twz);
+	const int zmax = INV ? p.bZ : n;
+	for (int t = threadIdx.x; t < zmax * W; t += 256) {
+		const int yy = t % W, z = t / W;
+		if (yy >= wy) continue;
+		if (!INV) tz[(size_t)z * p.bY + yy] = o[z * LS + yy];
+		else xf[(size_t)z * p.bY + yy] = o[z * LS + yy];
+	}
+}
+
+// K2b: per (kx, KB kz, RG RHS) with KB*RG <= PAIRS: y-FFT of the 3 components, D product (matvec.c:271-305 incl. the
+// reduced-FFT signs), inverse y-FFT. Line l = pair*3 + comp, pair = kk*RG + rr. Warp w loads/stores lines w, w+8, w+16
+// with its 32 lanes along y (coalesced rows of Tz, odd tile stride: conflict-free).
+template <typename T, typename V, int NS> __global__ void __launch_bounds__(256) mv_fft_y_dmul(MvP<T, V> p)
+{
+	typedef typename CxT<T>::type C;
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	if (all_done(p)) return;
+	constexpr int NL = 3 * Tiles<T>::PAIRS, LS = tile_ls(NL);
+	const int n = NS ? NS : p.gY;
+	C *a = reinterpret_cast<C *>(smem_raw);
+	C *b = a + (size_t)n * LS;
+	const int KB = p.KB, RG = p.RG;
+	const int rg0 = blockIdx.z * RG;
+	const int kxl = blockIdx.y, kx = p.kx0 + kxl;
+	const int kz0 = blockIdx.x * KB;
+	const size_t lz = (size_t)p.gZ * p.bY; // one (rhs, kx, comp) block of Tz
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	for (int l = warp; l < NL; l += 8) {
+		const int pair = l / 3, comp = l - 3 * pair;
+		const int kk = pair / RG, rr = pair - kk * RG;
+		const int kz = kz0 + kk;
+		const bool ok = kk < KB && rg0 + rr < p.R && kz < p.gZ;
+		const C *src = p.Tz + (((size_t)(rg0 + rr) * p.CK + kxl) * 3 + comp) * lz + (size_t)kz * p.bY;
+#pragma unroll 4
+		for (int y = lane; y < n; y += 32) a[y * LS + l] = (ok && y < p.bY) ? src[y] : cx<C>(0, 0);
+	}
+	__syncthreads();
+	C *o = tile_fft<C, NS, NL, LS, false>(a, b, p.py, p.twy);
+	C *s = (o == a) ? b : a;
+	for (int t = threadIdx.x; t < KB * n; t += 256) {
+		const int ky = t % n, kk = t / n;
+		const int kz = kz0 + kk;
+		if (kz >= p.gZ) continue;
+		const bool ry = ky >= p.DsY, rz = kz >= p.DsZ;
+		const int yy = ry ? p.gY - ky : ky, zz = rz ? p.gZ - kz : kz;
+		const C *f = p.D + (((size_t)kx * p.DsZ + zz) * p.DsY + yy) * 6;
+		C m0 = f[0], m1 = f[1], m2 = f[2], m3 = f[3], m4 = f[4], m5 = f[5];
+		if (ry) {
+			m1 = cneg(m1);
+			if (rz) m2 = cneg(m2);
+			else m4 = cneg(m4);
+		}
+		else if (rz) {
+			m2 = cneg(m2);
+			m4 = cneg(m4);
+		}
+		const int rgn = min(RG, p.R - rg0);
+		for (int rr = 0; rr < rgn; rr++) {
+			const int l0 = (kk * RG + rr) * 3;
+			C *row = o + ky * LS + l0;
+			const C v0 = row[0], v1 = row[1], v2 = row[2];
+			row[0] = cfma(m0, v0, cfma(m1, v1, cmul(m2, v2)));
+			row[1] = cfma(m1, v0, cfma(m3, v1, cmul(m4, v2)));
+			row[2] = cfma(m2, v0, cfma(m4, v1, cmul(m5, v2)));
+		}
+	}
+	__syncthreads();
+	C *o2 = tile_fft<C, NS, NL, LS, true>(o, s, p.py, p.twy);
+	for (int l = warp; l < NL; l += 8) {
+		const int pair = l / 3, comp = l - 3 * pair;
+		const int kk = pair / RG, rr = pair - kk * RG;
+		const int kz = kz0 + kk;
+		if (!(kk < KB && rg0 + rr < p.R && kz < p.gZ)) continue;
+		C *dst = p.Tz + (((size_t)(rg0 + rr) * p.CK + kxl) * 3 + comp) * lz + (size_t)kz * p.bY;
+		for (int y = lane; y < p.bY; y += 32) dst[y] = o2[y * LS + l];
+	}
+}
+
+__device__ __forceinline__ double block_sum(double v, double *sh)
+{
+	for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	__syncthreads();
+	if (lane == 0) sh[wid] = v;
+	__syncthreads();
+	double s = 0;
+	if (threadIdx.x == 0)
+		for (int w = 0; w < 8; w++) s += sh[w];
+	return s; // valid in thread 0
+}
+
+// K3: inverse FFT along x of W y-lines (one z), then y = x + S.X for their dipoles, with the epilogue reductions.
+template <typename T, typename V, int W, int NS>
+__global__ void __launch_bounds__(256) mv_fftx_gather(MvP<T, V> p, MvEpi e)
+{
+	typedef typename CxT<T>::type C;
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	__shared__ double red[32];
+	if (all_done(p)) return;
+	constexpr int NL = 3 * W, LS = tile_ls(3 * W);
+	const int n = NS ? NS : p.gX;
+	C *a = reinterpret_cast<C *>(smem_raw);
+	C *b = a + (size_t)n * LS;
+	const int r = blockIdx.z, z = blockIdx.y, y0 = blockIdx.x * W;
+	const int wy = min(W, p.bY - y0);
+	const size_t plane = (size_t)p.bZ * p.bY;
+	const C *xf = p.Xf + (size_t)r * p.gX * 3 * plane + (size_t)z * p.bY + y0;
+#pragma unroll 4
+	for (int t = threadIdx.x; t < n * NL; t += 256) {
+		const int yy = t % W, rest = t / W;
+		const int comp = rest % 3, kx = rest / 3;
+		a[kx * LS + comp * W + yy] = (yy < wy) ? xf[((size_t)kx * 3 + comp) * plane + yy] : cx<C>(0, 0);
+	}
+	__syncthreads();
+	C *o = tile_fft<C, NS, NL, LS, true>(a, b, p.px, p.twx);
+	const size_t line = (size_t)z * p.bY + y0;
+	const uint32_t i0 = p.line_start[line], i1 = p.line_start[line + wy];
+	const V *arg = p.arg + (size_t)r * p.N * 3;
+	V *res = p.res + (size_t)r * p.N * 3;
+	const V *u = e.u ? reinterpret_cast<const V *>(e.u) + (size_t)r * p.N * 3 : nullptr;
+	double s0 = 0, s1r = 0, s1i = 0;
+	const uint32_t cnt = (i1 - i0) * 3;
+#pragma unroll 2
+	for (uint32_t t = threadIdx.x; t < cnt; t += 256) {
+		const size_t i = i0 + t / 3;
+		const int comp = t % 3;
+		const uint32_t q = p.xy[i];
+		const int x = q & 0xffff, y = q >> 16;
+		V xv = arg[i * 3 + comp];
+		if (p.her) xv = cconj(xv);
+		const C sx = cmul(ccs_of(p.ccs, p.per_dip, p.nmat, p.N, r, i, p.mat[i], comp), o[x * LS + comp * W + (y - y0)]);
+		V yv = cadd(xv, cvt<V>(sx));
+		if (p.her) yv = cconj(yv);
+		res[i * 3 + comp] = yv;
+		if (e.mode) {
+			const double2 y2 = to_d2(yv);
+			if (e.mode & EPI_NORM) s0 += y2.x * y2.x + y2.y * y2.y;
+			if (e.mode & EPI_DOT_ARG) {
+				const double2 x2 = to_d2(arg[i * 3 + comp]);
+				s1r += x2.x * y2.x - x2.y * y2.y;
+				s1i += x2.x * y2.y + x2.y * y2.x;
+			}
+			if (e.mode & EPI_DOT_ARG_CONJ) {
+				const double2 x2 = to_d2(arg[i * 3 + comp]);
+				s1r += x2.x * y2.x + x2.y * y2.y;
+				s1i += x2.y * y2.x - x2.x * y2.y;
+			}
+			if (e.mode & EPI_DOT_U_CONJ) {
+				const double2 u2 = to_d2(u[i * 3 + comp]);
+				s1r += y2.x * u2.x + y2.y * u2.y;
+				s1i += y2.y * u2.x - y2.x * u2.y;
+			}
+		}
+	}
+	if (e.mode) {
+		const size_t nblk = (size_t)gridDim.x * gridDim.y;
+		const size_t blk = (size_t)blockIdx.y * gridDim.x + blockIdx.x;
+		double *out = e.partial + ((size_t)r * nblk + blk) * 4;
+		double v0 = block_sum(s0, red);
+		double v1 = block_sum(s1r, red);
+		double v2 = block_sum(s1i, red);
+		if (threadIdx.x == 0) {
+			out[0] = v0;
+			out[1] = v1;
+			out[2] = v2;
+		}
+	}
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// host side
+
+template <typename T> size_t smem_k1(int gX) { return 2 * sizeof(typename CxT<T>::type) * (size_t)gX * tile_ls(3 * Tiles<T>::W1); }
+template <typename T> size_t smem_k2(int gZ) { return 2 * sizeof(typename CxT<T>::type) * (size_t)gZ * tile_ls(Tiles<T>::W2); }
+template <typename T> size_t smem_k2b(int gY)
+{
+	return 2 * sizeof(typename CxT<T>::type) * (size_t)gY * tile_ls(3 * Tiles<T>::PAIRS);
+}
+
+// compile-time length for the power-of-two grids the kernels are instantiated for, 0 otherwise
+inline int static_len(int n)
+{
+	return (n == 64 || n == 128 || n == 256 || n == 512) ? n : 0;
+}
+
+#define ADDA_NS_SWITCH(n, CALL)                                                                                     \
+	switch (static_len(n)) {                                                                                        \
+		case 64: { constexpr int NS = 64; CALL; } break;                                                            \
+		case 128: { constexpr int NS = 128; CALL; } break;                                                          \
+		case 256: { constexpr int NS = 256; CALL; } break;                                                          \
+		case 512: { constexpr int NS = 512; CALL; } break;                                                          \
+		default: { constexpr int NS = 0; CALL; } break;                                                             \
+	}
+
+template <typename T, typename V> int set_attrs_tv()
+{
+	constexpr int W1 = Tiles<T>::W1, W2 = Tiles<T>::W2;
+	const int mx = 227 * 1024;
+#define ADDA_SET(kern) ADDA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))
+#define ADDA_SET_ALL(NS)                                                                                            \
+	ADDA_SET((mv_scatter_fftx<T, V, W1, NS>));                                                                      \
+	ADDA_SET((mv_fftx_gather<T, V, W1, NS>));                                                                       \
+	ADDA_SET((mv_fftz<T, V, W2, false, NS>));                                                                       \
+	ADDA_SET((mv_fftz<T, V, W2, true, NS>));                                                                        \
+	ADDA_SET((mv_fft_y_dmul<T, V, NS>))
+	ADDA_SET_ALL(0);
+	ADDA_SET_ALL(64);
+	ADDA_SET_ALL(128);
+	ADDA_SET_ALL(256);
+	ADDA_SET_ALL(512);
+#undef ADDA_SET_ALL
+#undef ADDA_SET
+	return ADDA_GB300_OK;
+}
+
+template <typename T, typename V>
+int launch_matvec(adda_gb300_ctx *c, int R, const V *arg, V *res, int her, const MvEpi &epi, const int *done)
+{
+	typedef typename CxT<T>::type C;
+	constexpr bool dbl = sizeof(T) == 8;
+	constexpr int W1 = Tiles<T>::W1, W2 = Tiles<T>::W2;
+	MvP<T, V> p;
+	p.bX = c->bX; p.bY = c->bY; p.bZ = c->bZ;
+	p.gX = c->gX; p.gY = c->gY; p.gZ = c->gZ;
+	p.DsY = c->DsY; p.DsZ = c->DsZ;
+	p.R = R;
+	p.N = c->N;
+	p.line_start = c->d_line_start;
+	p.xy = c->d_xy;
+	p.mat = c->d_mat;
+	p.ccs = dbl ? (const C *)c->ccs64 : (const C *)c->ccs32;
+	p.nmat = c->nmat;
+	p.per_dip = c->per_dip;
+	p.arg = arg;
+	p.res = res;
+	p.Xf = (C *)c->Xf;
+	p.Tz = (C *)c->Tz;
+	p.CK = dbl ? c->CK64 : c->CK32;
+	p.D = dbl ? (const C *)c->D64 : (const C *)c->D32;
+	const int pi = dbl ? 0 : 1;
+	p.px = c->px[pi]; p.py = c->py[pi]; p.pz = c->pz[pi];
+	p.twx = dbl ? (const C *)c->tw64[0] : (const C *)c->tw32[0];
+	p.twy = dbl ? (const C *)c->tw64[1] : (const C *)c->tw32[1];
+	p.twz = dbl ? (const C *)c->tw64[2] : (const C *)c->tw32[2];
+	p.her = her;
+	p.done = done;
+	p.kx0 = 0;
+	p.RG = std::min(R, Tiles<T>::PAIRS);
+	p.KB = std::max(1, Tiles<T>::PAIRS / p.RG);
+	cudaStream_t st = c->stream;
+	const dim3 blk(256);
+	const dim3 g1((c->bY + W1 - 1) / W1, c->bZ, R);
+	ADDA_NS_SWITCH(c->gX, (mv_scatter_fftx<T, V, W1, NS><<<g1, blk, smem_k1<T>(c->gX), st>>>(p)));
+	ADDA_LAUNCHED();
+	for (int kx0 = 0; kx0 < c->gX; kx0 += p.CK) {
+		p.kx0 = kx0;
+		const int ck = std::min(p.CK, c->gX - kx0);
+		const dim3 g2((c->bY + W2 - 1) / W2, 3 * ck, R);
+		ADDA_NS_SWITCH(c->gZ, (mv_fftz<T, V, W2, false, NS><<<g2, blk, smem_k2<T>(c->gZ), st>>>(p)));
+		ADDA_LAUNCHED();
+		const dim3 g2b((c->gZ + p.KB - 1) / p.KB, ck, (R + p.RG - 1) / p.RG);
+		ADDA_NS_SWITCH(c->gY, (mv_fft_y_dmul<T, V, NS><<<g2b, blk, smem_k2b<T>(c->gY), st>>>(p)));
+		ADDA_LAUNCHED();
+		ADDA_NS_SWITCH(c->gZ, (mv_fftz<T, V, W2, true, NS><<<g2, blk, smem_k2<T>(c->gZ), st>>>(p)));
+		ADDA_LAUNCHED();
+	}
+	ADDA_NS_SWITCH(c->gX, (mv_fftx_gather<T, V, W1, NS><<<g1, blk, smem_k1<T>(c->gX), st>>>(p, epi)));
+	ADDA_LAUNCHED();
+	return ADDA_GB300_OK;
+}
+
+} // namespace mv
+} // namespace adda
