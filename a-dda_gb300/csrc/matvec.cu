@@ -33,7 +33,7 @@ size_t matvec_partial_blocks(const adda_gb300_ctx *c, bool dbl)
 
 int matvec_setup(adda_gb300_ctx *c)
 {
-	const size_t cap = 227 * 1024;
+	const size_t cap = 216 * 1024;
 	if (mv::smem_k1<double>(c->gX) > cap || mv::smem_k2<double>(c->gZ) > cap || mv::smem_k2b<double>(c->gY) > cap ||
 		mv::smem_k1<float>(c->gX) > cap || mv::smem_k2<float>(c->gZ) > cap || mv::smem_k2b<float>(c->gY) > cap) {
 		set_error("FFT grid too large for the shared-memory tiles (maximum 512 per axis)");
