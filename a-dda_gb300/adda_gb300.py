@@ -51,7 +51,7 @@ EXPORTS = ["adda_gb300_fft_fit", "adda_gb300_fit_box", "adda_gb300_make_particle
            "adda_gb300_get_grid", "adda_gb300_init_dmatrix", "adda_gb300_dmatrix_len", "adda_gb300_get_dmatrix",
            "adda_gb300_set_cc", "adda_gb300_set_cc_sqrt", "adda_gb300_set_cc_dipole", "adda_gb300_matvec", "adda_gb300_matvec_device",
            "adda_gb300_solve", "adda_gb300_solve_device", "adda_gb300_vjp_chi", "adda_gb300_cross_sections",
-           "adda_gb300_time_matvec",
+           "adda_gb300_cross_sections_noalloc", "adda_gb300_time_matvec",
            "adda_gb300_last_solve_ms", "adda_gb300_last_error", "adda_gb300_kernel_launches"]
 
 _lib = None
@@ -96,6 +96,7 @@ def lib():
             "adda_gb300_solve_device": ([P, P, I, P, P, P, P], I),
             "adda_gb300_time_matvec": ([P, I, I, I, SZ, P], I),
             "adda_gb300_cross_sections": ([P, I, P, P, P, P], I),
+            "adda_gb300_cross_sections_noalloc": ([I, SZ, P, P, P, P, I, I, I, I, I, D, D, P, P, P, P, P], I),
             "adda_gb300_last_error": ([], ctypes.c_char_p),
             "adda_gb300_last_solve_ms": ([P], D),
             "adda_gb300_kernel_launches": ([], ctypes.c_uint64),

@@ -173,6 +173,22 @@ double adda_gb300_last_solve_ms(const adda_gb300_ctx *ctx);
 int adda_gb300_vjp_chi(adda_gb300_ctx *ctx, const adda_gb300_solve_params *sp, int rhs, const double prop[3],
 	const double incpol[3], const double *dinv_alpha, double *grad_cext, double *grad_cabs);
 
+/* Allocation-free variant of adda_gb300_cross_sections; it has no counterpart in the reference (whose host never
+ * runs where allocation is forbidden). For callers that cannot call cudaMalloc at this point: code running inside a
+ * framework that owns all device memory through its own pool, or a sequence being recorded into a CUDA graph.
+ * Everything is passed as device pointers: polarisations d_pvec [nrhs][ndip][3] double2, d_position [ndip][3],
+ * d_material [ndip] (or NULL for one material), polarisabilities d_cc [nrhs][nmat][3] (per_dipole=0) or
+ * [nrhs][ndip][3] (per_dipole=1) double2, d_prop/d_incpol [nrhs][3]; results to d_cext/d_cabs [nrhs]. The call is
+ * asynchronous on `stream` (a cudaStream_t, or NULL) and allocates nothing: its partial sums live in a 1 MiB static
+ * device array (256 partials x 8 doubles x ADDA_GB300_NOALLOC_MAX_RHS) that every GPU loading the library holds until
+ * exit. The first call on a device looks up that array's address (do it before any stream capture). All calls share
+ * the array: calls that overlap on the GPU race. nrhs > ADDA_GB300_NOALLOC_MAX_RHS is rejected (ADDA_GB300_EINVAL). */
+#define ADDA_GB300_NOALLOC_MAX_RHS 64
+int adda_gb300_cross_sections_noalloc(int nrhs, size_t ndip, const void *d_pvec, const uint16_t *d_position,
+	const uint8_t *d_material, const void *d_cc, int nmat, int per_dipole, int boxX, int boxY, int boxZ,
+	double gridspace, double wavenum, const double *d_prop, const double *d_incpol, double *d_cext, double *d_cabs,
+	void *stream);
+
 /* last error message of the calling thread */
 const char *adda_gb300_last_error(void);
 /* number of kernels this library has launched in the calling process (for launch accounting) */
