@@ -50,7 +50,8 @@ EXPORTS = ["adda_gb300_fft_fit", "adda_gb300_fit_box", "adda_gb300_make_particle
            "adda_gb300_create", "adda_gb300_destroy",
            "adda_gb300_get_grid", "adda_gb300_init_dmatrix", "adda_gb300_dmatrix_len", "adda_gb300_get_dmatrix",
            "adda_gb300_set_cc", "adda_gb300_set_cc_sqrt", "adda_gb300_set_cc_dipole", "adda_gb300_matvec", "adda_gb300_matvec_device",
-           "adda_gb300_solve", "adda_gb300_solve_device", "adda_gb300_vjp_chi", "adda_gb300_cross_sections",
+           "adda_gb300_solve", "adda_gb300_solve_device", "adda_gb300_solve_many", "adda_gb300_vjp_chi",
+           "adda_gb300_cross_sections",
            "adda_gb300_cross_sections_noalloc", "adda_gb300_time_matvec",
            "adda_gb300_last_solve_ms", "adda_gb300_last_error", "adda_gb300_kernel_launches"]
 
@@ -94,6 +95,7 @@ def lib():
             "adda_gb300_matvec_device": ([P, I, I, P, P, P, I], I),
             "adda_gb300_solve": ([P, P, I, P, P, P, P, P, I], I),
             "adda_gb300_solve_device": ([P, P, I, P, P, P, P], I),
+            "adda_gb300_solve_many": ([I, P, P, P, P, P, P, P], I),
             "adda_gb300_time_matvec": ([P, I, I, I, SZ, P], I),
             "adda_gb300_cross_sections": ([P, I, P, P, P, P], I),
             "adda_gb300_cross_sections_noalloc": ([I, SZ, P, P, P, P, I, I, I, I, I, D, D, P, P, P, P, P], I),
@@ -211,6 +213,29 @@ class Setup:
 
 # ---------------------------------------------------------------------------------------------------------------------
 # device context
+
+def solve_many(ctxs, eincs, method="qmr", prec="mixed", eps=1e-5, maxiter=100000, init="auto", check_every=0):
+    """solve several contexts (particles) concurrently; eincs[i]: [nrhs_i, 3N_i] complex. Returns per context
+    (x, p, stats)."""
+    L = lib()
+    n = len(ctxs)
+    es = [np.ascontiguousarray(e, dtype=np.complex128).reshape(-1, 3 * c.n) for c, e in zip(ctxs, eincs)]
+    xs = [np.empty_like(e) for e in es]
+    ps = [np.empty_like(e) for e in es]
+    sts = [(RhsStats * e.shape[0])() for e in es]
+    P = ctypes.c_void_p
+    arr = lambda vals: (P * n)(*vals)
+    nr = (ctypes.c_int * n)(*[e.shape[0] for e in es])
+    sp = SolveParams(ITERS[method], PREC[prec], eps, maxiter, INIT[init], check_every, 0.0, 0)
+    _check(L.adda_gb300_solve_many(n, arr([c.h.value for c in ctxs]), ctypes.byref(sp), nr,
+                                   arr([e.ctypes.data for e in es]), arr([x.ctypes.data for x in xs]),
+                                   arr([p.ctypes.data for p in ps]), arr([ctypes.addressof(s) for s in sts])),
+           "solve_many")
+    out = []
+    for x, p, st in zip(xs, ps, sts):
+        out.append((x, p, [dict(niter=s.niter, status=STATUS.get(s.status, s.status), resid=s.resid) for s in st]))
+    return out
+
 
 class Context:
     """One particle lattice on one GPU: the interaction matrix, FP64/FP32 matvecs, solver and cross sections."""

@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <thread>
 
 namespace adda {
 
@@ -449,6 +450,32 @@ int adda_gb300_solve(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int n
 	if (rc) return rc;
 	ADDA_CUDA(cudaSetDevice(c->device));
 	return solver_solve(c, sp, nrhs, einc, xvec, pvec, stats, resid_hist, hist_cap);
+}
+
+int adda_gb300_solve_many(int nctx, adda_gb300_ctx *const *ctxs, const adda_gb300_solve_params *sp, const int *nrhs,
+	const double *const *einc, double *const *xvec, double *const *pvec, adda_gb300_rhs_stats *const *stats)
+{
+	if (nctx < 0 || (nctx && (!ctxs || !sp || !nrhs || !einc))) {
+		set_error("solve_many: invalid arguments");
+		return ADDA_GB300_EINVAL;
+	}
+	std::vector<int> rcs(nctx, ADDA_GB300_OK);
+	std::vector<std::string> errs(nctx);
+	std::vector<std::thread> th;
+	th.reserve(nctx);
+	for (int i = 0; i < nctx; i++)
+		th.emplace_back([&, i]() {
+			rcs[i] = adda_gb300_solve(ctxs[i], sp, nrhs[i], einc[i], xvec ? xvec[i] : nullptr,
+				pvec ? pvec[i] : nullptr, stats ? stats[i] : nullptr, nullptr, 0);
+			if (rcs[i]) errs[i] = g_err;
+		});
+	for (auto &t : th) t.join();
+	for (int i = 0; i < nctx; i++)
+		if (rcs[i]) {
+			set_error("solve_many: context " + std::to_string(i) + ": " + errs[i]);
+			return rcs[i];
+		}
+	return ADDA_GB300_OK;
 }
 
 int adda_gb300_solve_device(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int nrhs, const void *d_einc,

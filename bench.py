@@ -281,6 +281,8 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
+    if args.with_scale:
+        line["scale_config5"] = run_scale(args)
     if rank == 0 and world == 1 and not args.no_cpu:
         t_it, desc = cpu_sample(args.method, os.cpu_count() or 1, s)
         iters = REF_ITERS.get(args.method) or [x["niter"] for x in st64]
@@ -292,6 +294,33 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def run_scale(args):
+    """BASELINE configuration 5: sphere on a 256^3 box (N = 8,783,848), FFT grid 512^3, m = 1.2, dpl 10, mixed QMR_CS
+    to 1e-5, both polarisations as 2 RHS, device-resident (one warm-up solve, one timed)"""
+    import torch
+    import adda_gb300 as A
+    s = A.Setup(grid=256, m=1.2, dpl=10)
+    t0 = time.perf_counter()
+    ctx = A.Context.from_setup(s, nrhs_max=2)
+    torch.cuda.synchronize()
+    t_init = time.perf_counter() - t0
+    einc = np.ascontiguousarray(np.stack(s.einc))
+    d_e = torch.from_numpy(einc.view(np.float64)).cuda()
+    st = ctx.solve_device(d_e.data_ptr(), 2, None, None, method=args.method, prec="mixed", eps=EPS)
+    t_solve = ctx.last_solve_ms() / 1e3
+    ce, ca = ctx.cross_sections(np.stack([s.prop, s.prop]), np.stack(s.incpol))
+    mv32 = ctx.time_matvec("fp32", 2, iters=5)
+    bts = matvec_bytes(s.n, s.grid, s.box, 8, 2)
+    out = {"workload": "sphere 256^3 box, N=%d, FFT grid %s, m=1.2, dpl=10, mixed %s to 1e-5, 2 RHS"
+           % (s.n, "x".join(map(str, s.grid)), args.method),
+           "time_to_solution_s": t_solve, "init_s (D matrix + setup)": t_init,
+           "iterations": [x["niter"] for x in st], "residual": [x["resid"] for x in st],
+           "Cext": list(map(float, ce)), "Cabs": list(map(float, ca)),
+           "fp32_matvec_ms": mv32, "fp32_matvec_GBps": bts / (mv32 * 1e-3) / 1e9}
+    ctx.close()
+    return out
 
 
 def run_profile(args):
@@ -322,6 +351,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--method", default="qmr", choices=["qmr", "bicgstab"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--with-scale", action="store_true", help="also time BASELINE configuration 5 (512^3 grid)")
     ap.add_argument("--mode", default="bench", choices=["bench", "profile-solve", "profile-matvec"])
     ap.add_argument("--grid", type=int, default=GRID, help="sphere box size for the profile modes")
     ap.add_argument("--maxiter", type=int, default=100000, help="iteration cap of the profile-solve mode")

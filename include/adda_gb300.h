@@ -150,6 +150,14 @@ int adda_gb300_solve(adda_gb300_ctx *ctx, const adda_gb300_solve_params *sp, int
 int adda_gb300_solve_device(adda_gb300_ctx *ctx, const adda_gb300_solve_params *sp, int nrhs, const void *d_einc,
 	void *d_xvec, void *d_pvec, adda_gb300_rhs_stats *stats);
 
+/* Several particles at once (uneven grids): solves context i for nrhs[i] right-hand sides einc[i] (host), writing
+ * xvec[i]/pvec[i] (host, may be NULL) and stats[i] (nrhs[i] entries, may be NULL). The contexts run concurrently, each
+ * on its own stream from its own host thread, so small lattices share the GPU instead of queueing. Returns the first
+ * non-zero status (and keeps going for the others). The reference solves particles one after another
+ * (orientation/particle loops of calculator.c:348-358 around IterativeSolver). */
+int adda_gb300_solve_many(int nctx, adda_gb300_ctx *const *ctxs, const adda_gb300_solve_params *sp, const int *nrhs,
+	const double *const *einc, double *const *xvec, double *const *pvec, adda_gb300_rhs_stats *const *stats);
+
 /* ExtCross (plane wave) and AbsCross (Draine), src/crosssec.c:811-917, in FP64 on the device from the
  * polarisations left by the last solve: prop/incpol per RHS [nrhs][3]; cext/cabs per RHS. */
 int adda_gb300_cross_sections(adda_gb300_ctx *ctx, int nrhs, const double *prop, const double *incpol,
