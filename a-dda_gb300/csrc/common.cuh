@@ -134,6 +134,35 @@ template <typename C> __device__ __forceinline__ void dft16(C *v, bool inv)
 	}
 }
 
+// radix-32 as two radix-16 halves joined by W32^k (k = 0..15)
+template <typename C> __device__ __forceinline__ void dft32(C *v, bool inv)
+{
+	const double sg = inv ? 1.0 : -1.0;
+	C e[16], o[16];
+#pragma unroll
+	for (int q = 0; q < 16; q++) {
+		e[q] = v[2 * q];
+		o[q] = v[2 * q + 1];
+	}
+	dft16(e, inv);
+	dft16(o, inv);
+	// cos/sin(k*pi/16), k = 1..7
+	const double c[8] = {1.0, 0.98078528040323044913, 0.92387953251128675613, 0.83146961230254523708,
+		0.70710678118654752440, 0.55557023301960222474, 0.38268343236508977173, 0.19509032201612826785};
+#pragma unroll
+	for (int k = 1; k < 16; k++) {
+		// angle k*pi/16: cos = c[k] for k<8, -c[16-k] for k>8; sin = c[8-k] for k<=8, c[k-8] for k>8
+		const double cs = (k < 8) ? c[k] : (k == 8 ? 0.0 : -c[16 - k]);
+		const double sn = (k <= 8) ? (k == 8 ? 1.0 : c[8 - k]) : c[k - 8];
+		o[k] = crot(o[k], cs, sg * sn);
+	}
+#pragma unroll
+	for (int k = 0; k < 16; k++) {
+		v[k] = cadd(e[k], o[k]);
+		v[k + 16] = csub(e[k], o[k]);
+	}
+}
+
 template <typename C> __device__ __forceinline__ void dft3(C *v, bool inv)
 {
 	typedef decltype(C::x) T;
@@ -153,6 +182,7 @@ template <typename C, int R> __device__ __forceinline__ void dft(C *v, bool inv,
 	else if (R == 4) dft4(v, inv);
 	else if (R == 8) dft8(v, inv);
 	else if (R == 16) dft16(v, inv);
+	else if (R == 32) dft32(v, inv);
 }
 
 // One Stockham pass over all lines of an element-major tile: x -> y.
@@ -296,6 +326,61 @@ __device__ __forceinline__ C *tile_fft(C *a, C *b, const FftPlan &p, const C *__
 {
 	if constexpr (NS > 0) return fft_static<C, NS, NL, LS, 1, (sizeof(C) == 8 ? 16 : 8), 256, INV>(a, b, tw);
 	else return fft_tile<C>(a, b, p, NL, LS, tw, INV);
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Register-resident two-step FFT of power-of-two length N = T*E for lines held by T consecutive lanes each
+// (T <= E, T | 16): lane j1 of a line owns the E elements j1 + T*j2 in v[j2]. Step 1: DFT_E over j2 in registers,
+// twiddle W_N^(j1*k2), transpose through the line's own shared buffer buf[k2*(T+1) + j1] (odd stride: conflict-free);
+// step 2: each lane takes the E/T columns k2 = j1 + i*T and does DFT_T over j1 in registers. On return v[i*T + k1]
+// holds X[j1 + i*T + E*k1], i.e. element j1 + T*(i + (E/T)*k1): the same "lane j1 owns j1 + T*j" form as the input,
+// with j = i + (E/T)*k1 (reg_natural reorders it). Only the line's lanes synchronise (gmask = their warp lanes).
+template <int N> struct RegShape {
+	static constexpr int LOG = (N >= 512) ? 9 : (N >= 256) ? 8 : (N >= 128) ? 7 : (N >= 64) ? 6 : 5;
+	static constexpr int T = 1 << (LOG / 2), E = N / T; // T <= E
+	static constexpr int BUF = E * (T + 1);             // complex elements of a line's transpose buffer
+};
+
+template <typename C, int N, bool INV>
+__device__ __forceinline__ void reg_fft(C *v, C *buf, int j1, unsigned gmask, const C *__restrict__ tw)
+{
+	constexpr int T = RegShape<N>::T, E = RegShape<N>::E;
+	dft<C, E>(v, INV, tw, N);
+#pragma unroll
+	for (int k2 = 1; k2 < E; k2++) {
+		C t = __ldg(tw + j1 * k2);
+		if (INV) t.y = -t.y;
+		v[k2] = cmul(v[k2], t);
+	}
+	__syncwarp(gmask);
+#pragma unroll
+	for (int k2 = 0; k2 < E; k2++) buf[k2 * (T + 1) + j1] = v[k2];
+	__syncwarp(gmask);
+#pragma unroll
+	for (int i = 0; i < E / T; i++) {
+		C u[T];
+		const int k2 = j1 + i * T;
+#pragma unroll
+		for (int q = 0; q < T; q++) u[q] = buf[k2 * (T + 1) + q];
+		dft<C, T>(u, INV, tw, N);
+#pragma unroll
+		for (int q = 0; q < T; q++) v[i * T + q] = u[q];
+	}
+}
+
+// reorder the output of reg_fft into the input form (v[j] = element j1 + T*j)
+template <typename C, int N> __device__ __forceinline__ void reg_natural(C *v)
+{
+	constexpr int T = RegShape<N>::T, E = RegShape<N>::E;
+	if constexpr (E != T) {
+		C w[E];
+#pragma unroll
+		for (int i = 0; i < E / T; i++)
+#pragma unroll
+			for (int k1 = 0; k1 < T; k1++) w[i + (E / T) * k1] = v[i * T + k1];
+#pragma unroll
+		for (int j = 0; j < E; j++) v[j] = w[j];
+	}
 }
 
 } // namespace adda

@@ -7,7 +7,9 @@
 //   then per chunk of CK x-slabs (chunk buffer Tz sized to stay in L2):
 //   K2a mv_fftz        : forward FFT along z of each y-line block (zero padding z>=boxZ in shared memory)
 //   K2b mv_fft_y_dmul  : per (kx, kz block, RHS group): forward FFT along y, 6-component symmetric D~ x X~ product
-//                        (D read once per grid point and reused by every RHS of the block), inverse FFT along y
+//                        (D read once per grid point and reused by every RHS of the block), inverse FFT along y;
+//       mv_fft_y_reg   : the same in register form (FP32, power-of-two gY <= 256): one lane group per column, lines
+//                        straight from Tz into registers, in-register two-step FFT, no block barrier
 //   K2c mv_fftz (inv)  : inverse FFT along z, keep z<boxZ  ->  Xf
 //   K3 mv_fftx_gather  : inverse FFT along x, y = x + S.X for the dipoles of the lines, optional Krylov reductions
 //                        (|y|^2, x.y, y.u*, x.y*) as deterministic per-block partial sums.
@@ -220,6 +222,80 @@ template <typename T, typename V, int NS> __global__ void __launch_bounds__(256)
 	}
 }
 
+// K2b, register form for FP32 and power-of-two gY <= 256: one group of T lanes per (kx, kz, rhs) column; each
+// component line goes from Tz straight into registers (lane j1 holds y = j1 + T*j: half-warp rows of 128 B) and is
+// transformed by reg_fft (one transpose through a slot of the group's shared memory, no block barrier). The spectra
+// of components 0 and 1 are parked in their slots (lane-interleaved: conflict-free) while component 2 stays in
+// registers; the 6-component D product at every ky the lane holds (matvec.c:271-305 incl. the reduced-FFT signs)
+// writes back to the same places, then each component is transformed back and stored for y < bY. Groups of one block
+// cover consecutive (kz, rhs) units with the RHS fastest, so the D rows a block reads are shared through L1.
+template <typename V, int NS, int NT> __global__ void __launch_bounds__(NT, 4) mv_fft_y_reg(MvP<float, V> p)
+{
+	typedef float2 C;
+	constexpr int T = RegShape<NS>::T, E = RegShape<NS>::E, BUF = RegShape<NS>::BUF, G = NT / T;
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	if (all_done(p)) return;
+	const int g = threadIdx.x / T, j1 = threadIdx.x % T;
+	const int unit = blockIdx.x * G + g;
+	const int r = unit % p.R, kz = unit / p.R;
+	if (kz >= p.gZ) return; // whole groups leave together
+	const unsigned gmask = ((1u << T) - 1u) << ((threadIdx.x & 31) & ~(T - 1));
+	const int kxl = blockIdx.y, kx = p.kx0 + kxl;
+	C *slot = reinterpret_cast<C *>(smem_raw) + (size_t)g * 3 * BUF; // slots c*BUF, c = 0..2
+	const size_t lz = (size_t)p.gZ * p.bY;
+	C *col = p.Tz + (((size_t)r * p.CK + kxl) * 3) * lz + (size_t)kz * p.bY;
+	C v[E];
+#pragma unroll 1
+	for (int c = 0; c < 3; c++) {
+#pragma unroll
+		for (int j = 0; j < E; j++) {
+			const int y = j1 + T * j;
+			v[j] = (y < p.bY) ? col[c * lz + y] : make_float2(0.f, 0.f);
+		}
+		reg_fft<C, NS, false>(v, slot + c * BUF, j1, gmask, p.twy);
+		reg_natural<C, NS>(v);
+		if (c < 2) {
+			__syncwarp(gmask);
+#pragma unroll
+			for (int j = 0; j < E; j++) slot[c * BUF + j * T + j1] = v[j];
+		}
+	}
+	const bool rz = kz >= p.DsZ;
+	const int zz = rz ? p.gZ - kz : kz;
+	const float4 *drow = reinterpret_cast<const float4 *>(p.D + ((size_t)kx * p.DsZ + zz) * p.DsY * 6);
+#pragma unroll
+	for (int j = 0; j < E; j++) {
+		const int ky = j1 + T * j;
+		const bool ry = ky >= p.DsY;
+		const int yy = ry ? p.gY - ky : ky;
+		const float4 *f = drow + (size_t)yy * 3;
+		const float4 d0 = __ldg(f), d1 = __ldg(f + 1), d2 = __ldg(f + 2);
+		C m0 = make_float2(d0.x, d0.y), m1 = make_float2(d0.z, d0.w), m2 = make_float2(d1.x, d1.y);
+		C m3 = make_float2(d1.z, d1.w), m4 = make_float2(d2.x, d2.y), m5 = make_float2(d2.z, d2.w);
+		if (ry) m1 = cneg(m1);
+		if (ry != rz) m4 = cneg(m4);
+		if (rz) m2 = cneg(m2);
+		const C v0 = slot[j * T + j1], v1 = slot[BUF + j * T + j1], v2 = v[j];
+		slot[j * T + j1] = cfma(m0, v0, cfma(m1, v1, cmul(m2, v2)));
+		slot[BUF + j * T + j1] = cfma(m1, v0, cfma(m3, v1, cmul(m4, v2)));
+		v[j] = cfma(m2, v0, cfma(m4, v1, cmul(m5, v2)));
+	}
+#pragma unroll 1
+	for (int c = 2; c >= 0; c--) {
+		if (c < 2) {
+#pragma unroll
+			for (int j = 0; j < E; j++) v[j] = slot[c * BUF + j * T + j1];
+		}
+		reg_fft<C, NS, true>(v, slot + c * BUF, j1, gmask, p.twy);
+		reg_natural<C, NS>(v);
+#pragma unroll
+		for (int j = 0; j < E; j++) {
+			const int y = j1 + T * j;
+			if (y < p.bY) col[c * lz + y] = v[j];
+		}
+	}
+}
+
 __device__ __forceinline__ double block_sum(double v, double *sh)
 {
 	for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -327,7 +403,13 @@ inline int static_len(int n)
 	return (n == 64 || n == 128 || n == 256 || n == 512) ? n : 0;
 }
 
-#define ADDA_NS_SWITCH(n, CALL)                                                                                     \
+// K2b in register form (mv_fft_y_reg): FP32 arithmetic, power-of-two gY up to 256 (E <= 16 registers per component)
+template <typename T> inline bool use_k2b_reg(int gY)
+{
+	return sizeof(T) == 4 && (gY == 64 || gY == 128 || gY == 256);
+}
+
+#define ADDA_NS_SWITCH(n, CALL)                                                                                   \
 	switch (static_len(n)) {                                                                                        \
 		case 64: { constexpr int NS = 64; CALL; } break;                                                            \
 		case 128: { constexpr int NS = 128; CALL; } break;                                                          \
@@ -348,6 +430,11 @@ template <typename T, typename V> int set_attrs_tv()
 	ADDA_SET((mv_fftz<T, V, W2, false, NS>));                                                                       \
 	ADDA_SET((mv_fftz<T, V, W2, true, NS>));                                                                        \
 	ADDA_SET((mv_fft_y_dmul<T, V, NS>))
+	if constexpr (sizeof(T) == 4) {
+		ADDA_SET((mv_fft_y_reg<V, 64, 128>));
+		ADDA_SET((mv_fft_y_reg<V, 128, 128>));
+		ADDA_SET((mv_fft_y_reg<V, 256, 128>));
+	}
 	ADDA_SET_ALL(0);
 	ADDA_SET_ALL(64);
 	ADDA_SET_ALL(128);
@@ -403,8 +490,27 @@ int launch_matvec(adda_gb300_ctx *c, int R, const V *arg, V *res, int her, const
 		const dim3 g2((c->bY + W2 - 1) / W2, 3 * ck, R);
 		ADDA_NS_SWITCH(c->gZ, (mv_fftz<T, V, W2, false, NS><<<g2, blk, smem_k2<T>(c->gZ), st>>>(p)));
 		ADDA_LAUNCHED();
-		const dim3 g2b((c->gZ + p.KB - 1) / p.KB, ck, (R + p.RG - 1) / p.RG);
-		ADDA_NS_SWITCH(c->gY, (mv_fft_y_dmul<T, V, NS><<<g2b, blk, smem_k2b<T>(c->gY), st>>>(p)));
+		if (use_k2b_reg<T>(c->gY)) {
+			if constexpr (sizeof(T) == 4) {
+				constexpr int NT = 128;
+				switch (c->gY) {
+#define ADDA_K2B_REG(NS)                                                                                            \
+	case NS: {                                                                                                      \
+		constexpr int G = NT / RegShape<NS>::T;                                                                     \
+		const dim3 g((c->gZ * R + G - 1) / G, ck);                                                                  \
+		mv_fft_y_reg<V, NS, NT><<<g, NT, G * 3 * RegShape<NS>::BUF * sizeof(float2), st>>>(p);                      \
+	} break;
+					ADDA_K2B_REG(64)
+					ADDA_K2B_REG(128)
+					ADDA_K2B_REG(256)
+#undef ADDA_K2B_REG
+				}
+			}
+		}
+		else {
+			const dim3 g2b((c->gZ + p.KB - 1) / p.KB, ck, (R + p.RG - 1) / p.RG);
+			ADDA_NS_SWITCH(c->gY, (mv_fft_y_dmul<T, V, NS><<<g2b, blk, smem_k2b<T>(c->gY), st>>>(p)));
+		}
 		ADDA_LAUNCHED();
 		ADDA_NS_SWITCH(c->gZ, (mv_fftz<T, V, W2, true, NS><<<g2, blk, smem_k2<T>(c->gZ), st>>>(p)));
 		ADDA_LAUNCHED();
