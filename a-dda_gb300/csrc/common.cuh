@@ -55,6 +55,144 @@ template <> __host__ __device__ __forceinline__ float2 from_d2<float2>(double2 a
 template <> __host__ __device__ __forceinline__ double2 from_d2<double2>(double2 a) { return a; }
 
 // ---------------------------------------------------------------------------------------------------------------
+// Double-float numbers: the unevaluated sum h + l of two floats with |l| <= ulp(h)/2 (about 48 significant bits),
+// computed on the FP32 pipes with error-free transformations: TwoSum (Knuth), FastTwoSum (Dekker) and the exact
+// product error through FMA; addition and multiplication follow the double-double algorithms of Dekker (1971) as
+// used in Bailey's QD library, with floats in place of doubles (addition in its "sloppy" form: error bounded by a
+// few 2^-48 of the operands). GB300 executes FP64 at about 1/64 of its FP32 rate, so Krylov vectors held in this
+// form update at memory speed. The __f*_rn intrinsics are never contracted into FMAs, which the transformations
+// rely on.
+struct DF {
+	float h, l;
+};
+
+__host__ __device__ __forceinline__ DF df_two_sum(float a, float b)
+{
+#ifdef __CUDA_ARCH__
+	const float s = __fadd_rn(a, b), v = __fsub_rn(s, a);
+	return DF{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v))};
+#else
+	const float s = a + b, v = s - a;
+	return DF{s, (a - (s - v)) + (b - v)};
+#endif
+}
+__host__ __device__ __forceinline__ DF df_fast_two_sum(float a, float b) // |a| >= |b|
+{
+#ifdef __CUDA_ARCH__
+	const float s = __fadd_rn(a, b);
+	return DF{s, __fsub_rn(b, __fsub_rn(s, a))};
+#else
+	const float s = a + b;
+	return DF{s, b - (s - a)};
+#endif
+}
+__host__ __device__ __forceinline__ DF operator+(DF a, DF b)
+{
+	const DF s = df_two_sum(a.h, b.h);
+#ifdef __CUDA_ARCH__
+	return df_fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+#else
+	return df_fast_two_sum(s.h, s.l + (a.l + b.l));
+#endif
+}
+__host__ __device__ __forceinline__ DF operator-(DF a) { return DF{-a.h, -a.l}; }
+__host__ __device__ __forceinline__ DF operator-(DF a, DF b) { return a + (-b); }
+__host__ __device__ __forceinline__ DF operator*(DF a, DF b)
+{
+#ifdef __CUDA_ARCH__
+	const float p = __fmul_rn(a.h, b.h);
+	float e = __fmaf_rn(a.h, b.h, -p);
+	e = __fmaf_rn(a.h, b.l, e);
+	e = __fmaf_rn(a.l, b.h, e);
+	return df_fast_two_sum(p, e);
+#else
+	const double p = (double)a.h * b.h + (double)a.h * b.l + (double)a.l * b.h;
+	const float h = (float)p;
+	return DF{h, (float)(p - h)};
+#endif
+}
+__host__ __device__ __forceinline__ DF df_of(double v)
+{
+	const float h = (float)v;
+	return DF{h, (float)(v - (double)h)};
+}
+__host__ __device__ __forceinline__ double df_val(DF a) { return (double)a.h + (double)a.l; }
+
+// complex double-float: the Krylov vector element of the MIXED solver (16 bytes, like double2)
+struct __align__(16) dd2 {
+	DF x, y;
+};
+__host__ __device__ __forceinline__ double2 to_d2(dd2 a) { return make_double2(df_val(a.x), df_val(a.y)); }
+template <> __host__ __device__ __forceinline__ dd2 from_d2<dd2>(double2 a)
+{
+	dd2 r;
+	r.x = df_of(a.x);
+	r.y = df_of(a.y);
+	return r;
+}
+
+// real coefficient in the arithmetic of the vector type C
+template <typename C> __host__ __device__ __forceinline__ decltype(C::x) rof(double v) { return (decltype(C::x))v; }
+template <> __host__ __device__ __forceinline__ DF rof<dd2>(double v) { return df_of(v); }
+
+// Per-thread accumulators of the fused reductions: double for float2/double2 vectors (exact products of floats,
+// FP64 sums), double-float for dd2 vectors (no FP64 instruction per element). acc_val gives the double the block
+// reductions continue with.
+template <typename C> struct AccOf {
+	typedef double T;
+};
+template <> struct AccOf<dd2> {
+	typedef DF T;
+};
+__host__ __device__ __forceinline__ double acc_val(double a) { return a; }
+__host__ __device__ __forceinline__ double acc_val(DF a) { return df_val(a); }
+// s += |y|^2
+template <typename C> __device__ __forceinline__ void acc_abs2(double &s, C y)
+{
+	const double2 d = to_d2(y);
+	s += d.x * d.x + d.y * d.y;
+}
+__device__ __forceinline__ void acc_abs2(DF &s, dd2 y) { s = s + (y.x * y.x + y.y * y.y); }
+// (sr, si) += a*b
+template <typename C> __device__ __forceinline__ void acc_cmul(double &sr, double &si, C a, C b)
+{
+	const double2 x = to_d2(a), y = to_d2(b);
+	sr += x.x * y.x - x.y * y.y;
+	si += x.x * y.y + x.y * y.x;
+}
+__device__ __forceinline__ void acc_cmul(DF &sr, DF &si, dd2 a, dd2 b)
+{
+	sr = sr + (a.x * b.x - a.y * b.y);
+	si = si + (a.x * b.y + a.y * b.x);
+}
+// (sr, si) += a*conj(b)
+template <typename C> __device__ __forceinline__ void acc_cmulc(double &sr, double &si, C a, C b)
+{
+	const double2 x = to_d2(a), y = to_d2(b);
+	sr += x.x * y.x + x.y * y.y;
+	si += x.y * y.x - x.x * y.y;
+}
+__device__ __forceinline__ void acc_cmulc(DF &sr, DF &si, dd2 a, dd2 b)
+{
+	sr = sr + (a.x * b.x + a.y * b.y);
+	si = si + (a.y * b.x - a.x * b.y);
+}
+// s[0] += Re(y)^2, s[1] += Im(y)^2, s[2] += Re(y)*Im(y)
+template <typename C> __device__ __forceinline__ void acc_sq3(double *s, C y)
+{
+	const double2 d = to_d2(y);
+	s[0] += d.x * d.x;
+	s[1] += d.y * d.y;
+	s[2] += d.x * d.y;
+}
+__device__ __forceinline__ void acc_sq3(DF *s, dd2 y)
+{
+	s[0] = s[0] + y.x * y.x;
+	s[1] = s[1] + y.y * y.y;
+	s[2] = s[2] + y.x * y.y;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
 // FFT plan: the radix of each Stockham pass. Filled on the host (make_plan in api.cu), passed to kernels by value.
 #define ADDA_FFT_MAXPASS 12
 struct FftPlan {

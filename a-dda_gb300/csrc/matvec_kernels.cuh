@@ -27,8 +27,9 @@ namespace adda {
 namespace mv {
 
 // T = arithmetic of the FFTs, D and the expanded grid (float or double); V = complex type of the dipole vectors the
-// caller passes (float2 or double2). With T=float, V=double2 (the MIXED solver) the inputs are rounded on the fly and
-// y = x + S.X is accumulated in double, so the identity part of A is exact.
+// caller passes (float2, double2 or double-float dd2). With T=float and V=double2 or dd2 (the MIXED solvers) the
+// inputs are rounded on the fly and y = x + S.X is accumulated in the vector's precision, so the identity part of A
+// keeps that precision.
 template <typename T, typename V> struct MvP {
 	typedef typename CxT<T>::type C;
 	int bX, bY, bZ, gX, gY, gZ, DsY, DsZ;
@@ -53,6 +54,18 @@ template <typename T, typename V> struct MvP {
 };
 
 template <typename To, typename From> __device__ __forceinline__ To cvt(From a) { return from_d2<To>(to_d2(a)); }
+// double-float vectors: round to float on load (K1) and widen the float S.X exactly (K3), all on the FP32 pipes
+template <> __device__ __forceinline__ float2 cvt<float2, dd2>(dd2 a)
+{
+	return make_float2(__fadd_rn(a.x.h, a.x.l), __fadd_rn(a.y.h, a.y.l));
+}
+template <> __device__ __forceinline__ dd2 cvt<dd2, float2>(float2 a)
+{
+	dd2 r;
+	r.x = DF{a.x, 0.f};
+	r.y = DF{a.y, 0.f};
+	return r;
+}
 
 template <typename P> __device__ __forceinline__ bool all_done(const P &p)
 {
@@ -338,7 +351,7 @@ __global__ void __launch_bounds__(256) mv_fftx_gather(MvP<T, V> p, MvEpi e)
 	const V *arg = p.arg + (size_t)r * p.N * 3;
 	V *res = p.res + (size_t)r * p.N * 3;
 	const V *u = e.u ? reinterpret_cast<const V *>(e.u) + (size_t)r * p.N * 3 : nullptr;
-	double s0 = 0, s1r = 0, s1i = 0;
+	typename AccOf<V>::T s0{}, s1r{}, s1i{};
 	const uint32_t cnt = (i1 - i0) * 3;
 #pragma unroll 2
 	for (uint32_t t = threadIdx.x; t < cnt; t += 256) {
@@ -353,32 +366,19 @@ __global__ void __launch_bounds__(256) mv_fftx_gather(MvP<T, V> p, MvEpi e)
 		if (p.her) yv = cconj(yv);
 		res[i * 3 + comp] = yv;
 		if (e.mode) {
-			const double2 y2 = to_d2(yv);
-			if (e.mode & EPI_NORM) s0 += y2.x * y2.x + y2.y * y2.y;
-			if (e.mode & EPI_DOT_ARG) {
-				const double2 x2 = to_d2(arg[i * 3 + comp]);
-				s1r += x2.x * y2.x - x2.y * y2.y;
-				s1i += x2.x * y2.y + x2.y * y2.x;
-			}
-			if (e.mode & EPI_DOT_ARG_CONJ) {
-				const double2 x2 = to_d2(arg[i * 3 + comp]);
-				s1r += x2.x * y2.x + x2.y * y2.y;
-				s1i += x2.y * y2.x - x2.x * y2.y;
-			}
-			if (e.mode & EPI_DOT_U_CONJ) {
-				const double2 u2 = to_d2(u[i * 3 + comp]);
-				s1r += y2.x * u2.x + y2.y * u2.y;
-				s1i += y2.y * u2.x - y2.x * u2.y;
-			}
+			if (e.mode & EPI_NORM) acc_abs2(s0, yv);
+			if (e.mode & EPI_DOT_ARG) acc_cmul(s1r, s1i, arg[i * 3 + comp], yv);      // x.y
+			if (e.mode & EPI_DOT_ARG_CONJ) acc_cmulc(s1r, s1i, arg[i * 3 + comp], yv); // x.y*
+			if (e.mode & EPI_DOT_U_CONJ) acc_cmulc(s1r, s1i, yv, u[i * 3 + comp]);     // y.u*
 		}
 	}
 	if (e.mode) {
 		const size_t nblk = (size_t)gridDim.x * gridDim.y;
 		const size_t blk = (size_t)blockIdx.y * gridDim.x + blockIdx.x;
 		double *out = e.partial + ((size_t)r * nblk + blk) * 4;
-		double v0 = block_sum(s0, red);
-		double v1 = block_sum(s1r, red);
-		double v2 = block_sum(s1i, red);
+		double v0 = block_sum(acc_val(s0), red);
+		double v1 = block_sum(acc_val(s1r), red);
+		double v2 = block_sum(acc_val(s1i), red);
 		if (threadIdx.x == 0) {
 			out[0] = v0;
 			out[1] = v1;

@@ -12,10 +12,11 @@
 // frozen by its done flag. check_every iterations are captured once as a CUDA graph and replayed; the host reads
 // the done flags only between graph launches.
 //
-// MIXED precision: the Krylov iterations run on complex-float vectors with the FP32 matvec (scalars and
-// reductions stay FP64); an outer loop recomputes the true residual b - A.x with the FP64 matvec (the reference's
-// ResidualNorm2, iterative.c:322-338), accumulates x in FP64 and restarts an FP32 solve on the residual until the
-// FP64 relative residual meets eps.
+// MIXED precision: the Krylov iterations run with the FP32 matvec on double-float vectors (dd2: pairs of floats,
+// about 48 significant bits, all arithmetic on the FP32 pipes; MIXED_F64VEC: double2 vectors, MIXED_F32VEC: float2);
+// scalars stay FP64 and reductions end in FP64. An outer loop recomputes the true residual b - A.x with the FP64
+// matvec (the reference's ResidualNorm2, iterative.c:322-338), accumulates x in FP64 and restarts the inner solve
+// on the residual until the FP64 relative residual meets eps.
 //
 // One deliberate difference from the reference: when IF_AUTO picks x_0 = 0, the reference reuses A.b from the
 // initial-field test for the first iteration (matvec_ready, iterative.c:962-965, 691); here the first iteration
@@ -25,6 +26,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 namespace adda {
@@ -126,6 +128,14 @@ __device__ __forceinline__ void write_part(double *part, int nbv, double v[4], i
 	}
 }
 
+// the same from double-float accumulators
+__device__ __forceinline__ void write_part(double *part, int nbv, DF a[4], int nv)
+{
+	double v[4];
+	for (int j = 0; j < 4; j++) v[j] = acc_val(a[j]);
+	write_part(part, nbv, v, nv);
+}
+
 // sum partials of RHS r in a fixed order (all threads participate); result in thread 0
 __device__ __forceinline__ void sum_part(const double *part, size_t nblk, int r, double out[4], int nv)
 {
@@ -192,12 +202,11 @@ __global__ void __launch_bounds__(NT) k_init_field(RhsState *st, int *done, cons
 	const int rr = blockIdx.y;
 	const C *bb = b + rr * n3;
 	if (stage == 0) { // r = b - Ab, partial |r|^2
-		double v[4] = {0, 0, 0, 0};
+		typename AccOf<C>::T v[4] = {};
 		VLOOP(n3) {
 			const C d = csub(bb[i], Ab[rr * n3 + i]);
 			r[rr * n3 + i] = d;
-			const double2 d2 = to_d2(d);
-			v[0] += d2.x * d2.x + d2.y * d2.y;
+			acc_abs2(v[0], d);
 		}
 		write_part(part, nbv, v, 1);
 	}
@@ -205,7 +214,7 @@ __global__ void __launch_bounds__(NT) k_init_field(RhsState *st, int *done, cons
 		const bool zero = st[rr].x0zero != 0;
 		VLOOP(n3) {
 			if (zero) {
-				x[rr * n3 + i] = cx<C>(0, 0);
+				x[rr * n3 + i] = C{};
 				r[rr * n3 + i] = bb[i];
 			}
 			else x[rr * n3 + i] = bb[i];
@@ -238,19 +247,12 @@ template <typename C>
 __global__ void __launch_bounds__(NT) k_dot(const C *a, const C *u, size_t n3, int mode, double *part, int nbv)
 {
 	const int r = blockIdx.y;
-	double v[4] = {0, 0, 0, 0};
+	typename AccOf<C>::T v[4] = {};
 	VLOOP(n3) {
-		const double2 x = to_d2(a[r * n3 + i]);
-		const double2 y = to_d2(u[r * n3 + i]);
-		v[0] += x.x * x.x + x.y * x.y;
-		if (mode == 0) {
-			v[1] += x.x * y.x - x.y * y.y;
-			v[2] += x.x * y.y + x.y * y.x;
-		}
-		else {
-			v[1] += x.x * y.x + x.y * y.y;
-			v[2] += x.y * y.x - x.x * y.y;
-		}
+		const C x = a[r * n3 + i], y = u[r * n3 + i];
+		acc_abs2(v[0], x);
+		if (mode == 0) acc_cmul(v[1], v[2], x, y);
+		else acc_cmulc(v[1], v[2], x, y);
 	}
 	write_part(part, nbv, v, 3);
 }
@@ -321,15 +323,12 @@ __global__ void __launch_bounds__(NT) qmr_v1(const RhsState *st, C *vt, const C 
 	const int r = blockIdx.y;
 	if (st[r].done) return;
 	const C k0 = cof<C>(st[r].k0), k1 = cof<C>(st[r].k1);
-	double s[4] = {0, 0, 0, 0};
+	typename AccOf<C>::T s[4] = {};
 	VLOOP(n3) {
 		const size_t j = r * n3 + i;
 		const C y = cadd(cadd(cmul(k0, vt[j]), cmul(k1, v[j])), Av[j]);
 		vt[j] = y;
-		const double2 d = to_d2(y);
-		s[0] += d.x * d.x;
-		s[1] += d.y * d.y;
-		s[2] += d.x * d.y;
+		acc_sq3(s, y);
 	}
 	write_part(part, nbv, s, 3);
 }
@@ -383,8 +382,8 @@ __global__ void __launch_bounds__(NT) qmr_v2(const RhsState *st, C *po, const C 
 	const RhsState &S = st[r];
 	const C k0 = cof<C>(S.k0), k1 = cof<C>(S.k1), k2 = cof<C>(S.k2), k3 = cof<C>(S.k3), kib = cof<C>(S.kib),
 		kr = cof<C>(S.kr);
-	const decltype(k0.x) d0 = (decltype(k0.x))S.d0;
-	double s[4] = {0, 0, 0, 0};
+	const auto d0 = rof<C>(S.d0);
+	typename AccOf<C>::T s[4] = {};
 	VLOOP(n3) {
 		const size_t j = r * n3 + i;
 		const C p = cadd(cadd(cmul(k0, po[j]), cmul(k1, pn[j])), cmul(k2, v[j]));
@@ -394,8 +393,7 @@ __global__ void __launch_bounds__(NT) qmr_v2(const RhsState *st, C *po, const C 
 		vt[j] = vn;
 		const C rn = cadd(cscale(rv[j], d0), cmul(kr, vn));
 		rv[j] = rn;
-		const double2 d = to_d2(rn);
-		s[0] += d.x * d.x + d.y * d.y;
+		acc_abs2(s[0], rn);
 	}
 	write_part(part, nbv, s, 1);
 }
@@ -494,13 +492,12 @@ __global__ void __launch_bounds__(NT) bs_v2(const RhsState *st, C *sv, const C *
 	const int r = blockIdx.y;
 	if (st[r].done) return;
 	const C k0 = cof<C>(st[r].k0);
-	double s[4] = {0, 0, 0, 0};
+	typename AccOf<C>::T s[4] = {};
 	VLOOP(n3) {
 		const size_t j = r * n3 + i;
 		const C y = cadd(cmul(k0, v[j]), rv[j]);
 		sv[j] = y;
-		const double2 d = to_d2(y);
-		s[0] += d.x * d.x + d.y * d.y;
+		acc_abs2(s[0], y);
 	}
 	write_part(part, nbv, s, 1);
 }
@@ -539,7 +536,7 @@ __global__ void __launch_bounds__(NT) bs_v3(const RhsState *st, C *x, const C *p
 	const RhsState &S = st[r];
 	const C a = cof<C>(S.balpha), om = cof<C>(S.omega), mom = cof<C>(dc(-S.omega.x, -S.omega.y));
 	const bool half = S.half != 0;
-	double s[4] = {0, 0, 0, 0};
+	typename AccOf<C>::T s[4] = {};
 	VLOOP(n3) {
 		const size_t j = r * n3 + i;
 		if (half) {
@@ -549,10 +546,8 @@ __global__ void __launch_bounds__(NT) bs_v3(const RhsState *st, C *x, const C *p
 		x[j] = cadd(x[j], cadd(cmul(a, p[j]), cmul(om, sv[j])));
 		const C y = cadd(cmul(mom, t[j]), sv[j]);
 		rv[j] = y;
-		const double2 d = to_d2(y), u = to_d2(rt[j]);
-		s[0] += d.x * d.x + d.y * d.y;
-		s[1] += d.x * u.x + d.y * u.y;
-		s[2] += d.y * u.x - d.x * u.y;
+		acc_abs2(s[0], y);
+		acc_cmulc(s[1], s[2], y, rt[j]);
 	}
 	write_part(part, nbv, s, 3);
 }
@@ -835,7 +830,8 @@ static int enqueue_iter(adda_gb300_ctx *c, SolverWork *w, int method, int R, int
 template <typename T, typename C>
 static int krylov(adda_gb300_ctx *c, SolverWork *w, int method, int R, int K, unsigned long long *iters_run)
 {
-	const int mode = (sizeof(T) == 8 ? 0 : 1) + (sizeof(C) == 8 ? 2 : 0); // graph key: arithmetic and vector type
+	// graph key: arithmetic and vector type
+	const int mode = (sizeof(T) == 8 ? 0 : 1) + (sizeof(C) == 8 ? 2 : 0) + (std::is_same<C, dd2>::value ? 4 : 0);
 	KV<C> k = kvec<C>(w);
 	const size_t n3 = w->n3;
 	const dim3 gv(w->nbv, R);
@@ -1039,7 +1035,7 @@ static int check_params(const adda_gb300_solve_params *sp)
 {
 	if ((sp->method != ADDA_ITER_QMR_CS && sp->method != ADDA_ITER_BICGSTAB) ||
 		(sp->precision != ADDA_PREC_FP64 && sp->precision != ADDA_PREC_MIXED &&
-			sp->precision != ADDA_PREC_MIXED_F32VEC) || !(sp->eps > 0) || sp->maxiter < 0 ||
+			sp->precision != ADDA_PREC_MIXED_F32VEC && sp->precision != ADDA_PREC_MIXED_F64VEC) || !(sp->eps > 0) || sp->maxiter < 0 ||
 		(sp->init_field != ADDA_IF_AUTO && sp->init_field != ADDA_IF_ZERO && sp->init_field != ADDA_IF_INC)) {
 		set_error("solve: unsupported parameters");
 		return ADDA_GB300_EINVAL;
@@ -1128,6 +1124,9 @@ static int solve_core_impl(adda_gb300_ctx *c, const adda_gb300_solve_params *sp,
 		}
 	}
 	else if (sp->precision == ADDA_PREC_MIXED) {
+		if ((rc = solve_mixed<dd2>(c, sp, R, st.data(), mc, K))) return rc;
+	}
+	else if (sp->precision == ADDA_PREC_MIXED_F64VEC) {
 		if ((rc = solve_mixed<double2>(c, sp, R, st.data(), mc, K))) return rc;
 	}
 	else {

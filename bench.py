@@ -30,8 +30,9 @@ for _p in (ROOT, os.path.join(ROOT, "a-dda_gb300")):
 import numpy as np  # noqa: E402
 
 METRIC = "time-to-solution @res 1e-5, 128^3 sphere (both polarisations), mixed FP32/FP64 on GB300"
-# MIXED here = FP32 matvec (FFTs, D, expanded grid) with FP64 Krylov vectors and FP64 residual refinement; the
-# variant with FP32 Krylov vectors as well is reported beside it ("mixed_f32vec")
+# MIXED here = FP32 matvec (FFTs, D, expanded grid) with double-float Krylov vectors (float pairs, ~48 bits, FP32
+# pipes), FP64 recurrence scalars and FP64 residual refinement; the variants with FP64 ("mixed_f64vec") and FP32
+# ("mixed_f32vec") Krylov vectors are reported beside it
 GRID, M_REF, DPL, EPS = 128, 1.33 + 0.01j, 15.0, 1e-5
 WORKLOAD = ("sphere 128^3 box, N=1099136 dipoles, FFT grid 256^3, m=1.33+0.01i, dpl=15, LDR, %s to 1e-5, "
             "2 RHS (both polarisations)")
@@ -221,9 +222,11 @@ def run_ours(args):
     barrier(world)
     t_solve = allmax(world, statistics.mean(ms) / 1e3)
     ce, ca = ctx.cross_sections(np.stack([s.prop, s.prop]), np.stack(s.incpol))
-    # the all-FP32 Krylov variant (FP32 vectors too), once, for comparison
+    # the variants with FP32 and with FP64 Krylov vectors, once each, for comparison
     st32 = ctx.solve_device(d_e.data_ptr(), R, d_x.data_ptr(), d_p.data_ptr(), prec="mixed_f32vec", **opts)
     t_f32vec = ctx.last_solve_ms() / 1e3
+    st64v = ctx.solve_device(d_e.data_ptr(), R, d_x.data_ptr(), d_p.data_ptr(), prec="mixed_f64vec", **opts)
+    t_f64vec = ctx.last_solve_ms() / 1e3
     # plain FP64 GPU solve on the same workload (one warm-up, one timed)
     ctx.solve_device(d_e.data_ptr(), R, d_x.data_ptr(), d_p.data_ptr(), prec="fp64", **opts)
     st64 = ctx.solve_device(d_e.data_ptr(), R, d_x.data_ptr(), d_p.data_ptr(), prec="fp64", **opts)
@@ -258,7 +261,7 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": t_solve, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_solve * 1e3, "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "c64 matvec + c128 Krylov (mixed)", "data": "synthetic (generated particle, plane wave)",
+        "vs_baseline": None, "dtype": "c64 matvec + double-float Krylov vectors + f64 scalars/refinement (mixed)", "data": "synthetic (generated particle, plane wave)",
         "config": {"workload": WORKLOAD % ("QMR_CS" if args.method == "qmr" else "BiCGStab"),
                    "method": args.method, "rhs": R, "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (D 204 MB FP32, Einc 106 MB)",
@@ -266,6 +269,8 @@ def run_ours(args):
         "fp64_time_to_solution_s": t64,
         "mixed_f32vec_time_to_solution_s": t_f32vec,
         "mixed_f32vec_iterations": [x["niter"] for x in st32],
+        "mixed_f64vec_time_to_solution_s": t_f64vec,
+        "mixed_f64vec_iterations": [x["niter"] for x in st64v],
         "speedup_mixed_vs_fp64": t64 / t_solve,
         "iterations": {"mixed": [x["niter"] for x in stats], "fp64": [x["niter"] for x in st64],
                        "fp64_matvecs_in_mixed": [x["matvecs_fp64"] for x in stats],

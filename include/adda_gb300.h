@@ -37,11 +37,19 @@ enum adda_gb300_shape { ADDA_SHAPE_SPHERE = 0, ADDA_SHAPE_ELLIPSOID = 1, ADDA_SH
 enum adda_gb300_pol { ADDA_POL_LDR = 0, ADDA_POL_CM = 1, ADDA_POL_RRC = 2, ADDA_POL_DGF = 3 };
 enum adda_gb300_iter { ADDA_ITER_QMR_CS = 0, ADDA_ITER_BICGSTAB = 1 };
 /* arithmetic of a matvec / solve. FP64: everything in double. FP32: complex-float FFTs, D-matrix and vectors.
- * MIXED (solve only): Krylov solves whose matvec runs in FP32 (FFTs, D, expanded grid) while the Krylov vectors,
- * recurrences and reductions stay FP64, inside an iterative-refinement loop whose residual is recomputed with the
- * FP64 matvec (the reference's ResidualNorm2, iterative.c:322-338) until it meets eps.
- * MIXED_F32VEC (solve only): the same with the Krylov vectors in FP32 as well. */
-enum adda_gb300_prec { ADDA_PREC_FP64 = 0, ADDA_PREC_FP32 = 1, ADDA_PREC_MIXED = 2, ADDA_PREC_MIXED_F32VEC = 3 };
+ * MIXED (solve only): Krylov solves whose matvec runs in FP32 (FFTs, D, expanded grid) while the Krylov vectors are
+ * double-float (pairs of floats, about 48 significant bits, updated with error-free FP32 arithmetic), the
+ * recurrence scalars FP64 and the reductions end in FP64, inside an iterative-refinement loop whose residual is
+ * recomputed with the FP64 matvec (the reference's ResidualNorm2, iterative.c:322-338) until it meets eps.
+ * MIXED_F64VEC (solve only): the same with FP64 Krylov vectors (slower on GPUs with a reduced FP64 rate).
+ * MIXED_F32VEC (solve only): the same with the Krylov vectors in FP32. */
+enum adda_gb300_prec {
+	ADDA_PREC_FP64 = 0,
+	ADDA_PREC_FP32 = 1,
+	ADDA_PREC_MIXED = 2,
+	ADDA_PREC_MIXED_F32VEC = 3,
+	ADDA_PREC_MIXED_F64VEC = 4
+};
 enum adda_gb300_init_field { ADDA_IF_AUTO = 0, ADDA_IF_ZERO = 1, ADDA_IF_INC = 2 };
 
 typedef struct adda_gb300_ctx adda_gb300_ctx;
@@ -62,7 +70,7 @@ typedef struct {
 
 typedef struct {
 	int method;                  /* enum adda_gb300_iter (-iter) */
-	int precision;               /* ADDA_PREC_FP64, ADDA_PREC_MIXED or ADDA_PREC_MIXED_F32VEC */
+	int precision;               /* ADDA_PREC_FP64, ADDA_PREC_MIXED, ADDA_PREC_MIXED_F64VEC or ADDA_PREC_MIXED_F32VEC */
 	double eps;                  /* relative residual target (-eps e => 10^-e) */
 	int maxiter;                 /* -maxiter */
 	int init_field;              /* enum adda_gb300_init_field (-init_field) */

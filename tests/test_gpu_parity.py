@@ -167,7 +167,7 @@ def test_solve_fp64_vs_oracle_tight(method):
         assert abs(ca[r] / ro["Cabs"] - 1) < 1e-9
 
 
-@pytest.mark.parametrize("prec", ["mixed", "mixed_f32vec"])
+@pytest.mark.parametrize("prec", ["mixed", "mixed_f64vec", "mixed_f32vec"])
 @pytest.mark.parametrize("method", ["qmr", "bicgstab"])
 @pytest.mark.parametrize("name", ["c1_qmr", "ell24", "c2_small"])
 def test_solve_mixed(name, method, prec):
