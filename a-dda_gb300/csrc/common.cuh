@@ -506,6 +506,66 @@ __device__ __forceinline__ void reg_fft(C *v, C *buf, int j1, unsigned gmask, co
 	}
 }
 
+// In-place FFT of column l of an element-major tile (element e at a[e*LS + l], e < N) by the T lanes of one group
+// (lane j1, group lanes gmask): the two steps of reg_fft with the transpose done inside the column itself. Step 1's
+// Y[j1][k2] goes to element k2*T + ((j1 + k2) mod T): for a fixed k2 the T lanes write T consecutive elements, and
+// the step-2 reads (lane j1 takes column k2 = j1 + i*T, rows q) hit T consecutive elements modulo T too, so with an
+// odd LS both phases are bank-conflict-free. The result is written back in natural order. The caller synchronises
+// the block before (tile filled) and after (tile read by other lanes).
+template <typename C, int N, int LS, bool INV>
+__device__ __forceinline__ void col_fft(C *a, int l, int j1, unsigned gmask, const C *__restrict__ tw)
+{
+	constexpr int T = RegShape<N>::T, E = RegShape<N>::E;
+	C v[E];
+#pragma unroll
+	for (int j = 0; j < E; j++) v[j] = a[(j1 + T * j) * LS + l];
+	dft<C, E>(v, INV, tw, N);
+#pragma unroll
+	for (int k2 = 1; k2 < E; k2++) {
+		C t = __ldg(tw + j1 * k2);
+		if (INV) t.y = -t.y;
+		v[k2] = cmul(v[k2], t);
+	}
+	__syncwarp(gmask);
+#pragma unroll
+	for (int k2 = 0; k2 < E; k2++) a[(k2 * T + ((j1 + k2) & (T - 1))) * LS + l] = v[k2];
+	__syncwarp(gmask);
+#pragma unroll
+	for (int i = 0; i < E / T; i++) {
+		const int k2 = j1 + i * T;
+		C u[T];
+#pragma unroll
+		for (int q = 0; q < T; q++) u[q] = a[(k2 * T + ((q + k2) & (T - 1))) * LS + l];
+		dft<C, T>(u, INV, tw, N);
+#pragma unroll
+		for (int k1 = 0; k1 < T; k1++) v[i * T + k1] = u[k1];
+	}
+	__syncwarp(gmask);
+#pragma unroll
+	for (int i = 0; i < E / T; i++)
+#pragma unroll
+		for (int k1 = 0; k1 < T; k1++) a[(j1 + i * T + E * k1) * LS + l] = v[i * T + k1];
+}
+
+// FFT of all NL columns of an element-major tile by NT threads in groups of T lanes (line l = group, group + G, ...)
+template <typename C, int N, int NL, int LS, int NT, bool INV>
+__device__ __forceinline__ void tile_cols_fft(C *a, const C *__restrict__ tw)
+{
+	constexpr int T = RegShape<N>::T, G = NT / T;
+	const int g = threadIdx.x / T, j1 = threadIdx.x % T;
+	const unsigned gmask = ((1u << T) - 1u) << ((threadIdx.x & 31) & ~(T - 1));
+	for (int l = g; l < NL; l += G) col_fft<C, N, LS, INV>(a, l, j1, gmask, tw);
+	__syncthreads();
+}
+
+// whether a kernel of compile-time length NS and arithmetic T transforms its single tile with tile_cols_fft
+// (FP32, power-of-two 64..512) rather than with ping-pong Stockham passes, and its thread count for NL lines
+template <typename T, int NS> __host__ __device__ constexpr bool reg_cols() { return sizeof(T) == 4 && NS >= 64 && NS <= 512; }
+template <typename T, int NS, int NL> __host__ __device__ constexpr int col_threads()
+{
+	return reg_cols<T, NS>() ? NL * RegShape<NS>::T : 256;
+}
+
 // reorder the output of reg_fft into the input form (v[j] = element j1 + T*j)
 template <typename C, int N> __device__ __forceinline__ void reg_natural(C *v)
 {

@@ -16,7 +16,10 @@
 // The reference's explicit transposes (TransposeYZ), slice zeroing and copies (Arith2/Arith4) do not exist here:
 // every tile is loaded along the contiguous axis of its buffer and transformed in element-major shared memory.
 // Every kernel is instantiated with a compile-time FFT length NS for the power-of-two grids (all index arithmetic
-// folds to shifts, passes unroll) and with NS = 0 (runtime plan) for the other fftFit sizes. Blocks are 256 threads.
+// folds to shifts, passes unroll) and with NS = 0 (runtime plan) for the other fftFit sizes. With FP32 arithmetic and
+// a power-of-two length the tile is transformed column by column in registers (tile_cols_fft: one tile instead of
+// two, one group of 8-16 lanes per line, warp-local synchronisation); blocks then have lines x group-size threads,
+// otherwise 256 threads and ping-pong Stockham passes.
 #pragma once
 
 #include "ctx.cuh"
@@ -87,25 +90,27 @@ template <> struct Tiles<float> { static constexpr int W1 = 8, W2 = 16, PAIRS = 
 template <> struct Tiles<double> { static constexpr int W1 = 4, W2 = 8, PAIRS = 4; };
 
 // K1: scatter S.x of W consecutive x-lines (one z) into shared memory and FFT along x. Tile: gX x (3*W) lines.
-template <typename T, typename V, int W, int NS> __global__ void __launch_bounds__(256) mv_scatter_fftx(MvP<T, V> p)
+template <typename T, typename V, int W, int NS>
+__global__ void __launch_bounds__(col_threads<T, NS, 3 * W>()) mv_scatter_fftx(MvP<T, V> p)
 {
 	typedef typename CxT<T>::type C;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	if (all_done(p)) return;
-	constexpr int NL = 3 * W, LS = tile_ls(3 * W);
+	constexpr int NL = 3 * W, LS = tile_ls(3 * W), NT = col_threads<T, NS, 3 * W>();
+	constexpr bool RC = reg_cols<T, NS>();
 	const int n = NS ? NS : p.gX;
 	C *a = reinterpret_cast<C *>(smem_raw);
-	C *b = a + (size_t)n * LS;
+	C *b = a + (size_t)n * LS; // second tile of the Stockham form only
 	const int r = blockIdx.z, z = blockIdx.y, y0 = blockIdx.x * W;
 	const int wy = min(W, p.bY - y0);
-	for (int t = threadIdx.x; t < n * LS; t += 256) a[t] = cx<C>(0, 0);
+	for (int t = threadIdx.x; t < n * LS; t += NT) a[t] = cx<C>(0, 0);
 	__syncthreads();
 	const size_t line = (size_t)z * p.bY + y0;
 	const uint32_t i0 = p.line_start[line], i1 = p.line_start[line + wy];
 	const V *arg = p.arg + (size_t)r * p.N * 3;
 	const uint32_t cnt = (i1 - i0) * 3;
 #pragma unroll 4
-	for (uint32_t t = threadIdx.x; t < cnt; t += 256) {
+	for (uint32_t t = threadIdx.x; t < cnt; t += NT) {
 		const size_t i = i0 + t / 3;
 		const int comp = t % 3;
 		const uint32_t q = p.xy[i];
@@ -116,10 +121,12 @@ template <typename T, typename V, int W, int NS> __global__ void __launch_bounds
 		a[x * LS + comp * W + (y - y0)] = v;
 	}
 	__syncthreads();
-	C *o = tile_fft<C, NS, NL, LS, false>(a, b, p.px, p.twx);
+	C *o = a;
+	if constexpr (RC) tile_cols_fft<C, NS, NL, LS, NT, false>(a, p.twx);
+	else o = tile_fft<C, NS, NL, LS, false>(a, b, p.px, p.twx);
 	const size_t plane = (size_t)p.bZ * p.bY;
 	C *xf = p.Xf + (size_t)r * p.gX * 3 * plane + (size_t)z * p.bY + y0;
-	for (int t = threadIdx.x; t < n * NL; t += 256) {
+	for (int t = threadIdx.x; t < n * NL; t += NT) {
 		const int yy = t % W, rest = t / W;
 		const int comp = rest % 3, kx = rest / 3;
 		if (yy < wy) xf[((size_t)kx * 3 + comp) * plane + yy] = o[kx * LS + comp * W + yy];
@@ -128,12 +135,14 @@ template <typename T, typename V, int W, int NS> __global__ void __launch_bounds
 
 // K2a/K2c: FFT along z of W consecutive y-lines of one (rhs, kx, comp). Forward reads Xf (z<bZ, zero padded) and
 // writes Tz (all kz); inverse reads Tz and writes z<bZ back to Xf.
-template <typename T, typename V, int W, bool INV, int NS> __global__ void __launch_bounds__(256) mv_fftz(MvP<T, V> p)
+template <typename T, typename V, int W, bool INV, int NS>
+__global__ void __launch_bounds__(col_threads<T, NS, W>()) mv_fftz(MvP<T, V> p)
 {
 	typedef typename CxT<T>::type C;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	if (all_done(p)) return;
-	constexpr int LS = tile_ls(W);
+	constexpr int LS = tile_ls(W), NT = col_threads<T, NS, W>();
+	constexpr bool RC = reg_cols<T, NS>();
 	const int n = NS ? NS : p.gZ;
 	C *a = reinterpret_cast<C *>(smem_raw);
 	C *b = a + (size_t)n * LS;
@@ -146,7 +155,7 @@ template <typename T, typename V, int W, bool INV, int NS> __global__ void __lau
 	C *xf = p.Xf + (((size_t)r * p.gX + kx) * 3 + comp) * plane + y0;
 	C *tz = p.Tz + (((size_t)r * p.CK + kxl) * 3 + comp) * (size_t)n * p.bY + y0;
 #pragma unroll 4
-	for (int t = threadIdx.x; t < n * W; t += 256) {
+	for (int t = threadIdx.x; t < n * W; t += NT) {
 		const int yy = t % W, z = t / W;
 		C v = cx<C>(0, 0);
 		if (!INV) {
@@ -156,9 +165,11 @@ template <typename T, typename V, int W, bool INV, int NS> __global__ void __lau
 		a[z * LS + yy] = v;
 	}
 	__syncthreads();
-	C *o = tile_fft<C, NS, W, LS, INV>(a, b, p.pz, p.twz);
+	C *o = a;
+	if constexpr (RC) tile_cols_fft<C, NS, W, LS, NT, INV>(a, p.twz);
+	else o = tile_fft<C, NS, W, LS, INV>(a, b, p.pz, p.twz);
 	const int zmax = INV ? p.bZ : n;
-	for (int t = threadIdx.x; t < zmax * W; t += 256) {
+	for (int t = threadIdx.x; t < zmax * W; t += NT) {
 		const int yy = t % W, z = t / W;
 		if (yy >= wy) continue;
 		if (!INV) tz[(size_t)z * p.bY + yy] = o[z * LS + yy];
@@ -318,19 +329,20 @@ __device__ __forceinline__ double block_sum(double v, double *sh)
 	__syncthreads();
 	double s = 0;
 	if (threadIdx.x == 0)
-		for (int w = 0; w < 8; w++) s += sh[w];
+		for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += sh[w];
 	return s; // valid in thread 0
 }
 
 // K3: inverse FFT along x of W y-lines (one z), then y = x + S.X for their dipoles, with the epilogue reductions.
 template <typename T, typename V, int W, int NS>
-__global__ void __launch_bounds__(256) mv_fftx_gather(MvP<T, V> p, MvEpi e)
+__global__ void __launch_bounds__(col_threads<T, NS, 3 * W>()) mv_fftx_gather(MvP<T, V> p, MvEpi e)
 {
 	typedef typename CxT<T>::type C;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	__shared__ double red[32];
 	if (all_done(p)) return;
-	constexpr int NL = 3 * W, LS = tile_ls(3 * W);
+	constexpr int NL = 3 * W, LS = tile_ls(3 * W), NT = col_threads<T, NS, 3 * W>();
+	constexpr bool RC = reg_cols<T, NS>();
 	const int n = NS ? NS : p.gX;
 	C *a = reinterpret_cast<C *>(smem_raw);
 	C *b = a + (size_t)n * LS;
@@ -339,13 +351,15 @@ __global__ void __launch_bounds__(256) mv_fftx_gather(MvP<T, V> p, MvEpi e)
 	const size_t plane = (size_t)p.bZ * p.bY;
 	const C *xf = p.Xf + (size_t)r * p.gX * 3 * plane + (size_t)z * p.bY + y0;
 #pragma unroll 4
-	for (int t = threadIdx.x; t < n * NL; t += 256) {
+	for (int t = threadIdx.x; t < n * NL; t += NT) {
 		const int yy = t % W, rest = t / W;
 		const int comp = rest % 3, kx = rest / 3;
 		a[kx * LS + comp * W + yy] = (yy < wy) ? xf[((size_t)kx * 3 + comp) * plane + yy] : cx<C>(0, 0);
 	}
 	__syncthreads();
-	C *o = tile_fft<C, NS, NL, LS, true>(a, b, p.px, p.twx);
+	C *o = a;
+	if constexpr (RC) tile_cols_fft<C, NS, NL, LS, NT, true>(a, p.twx);
+	else o = tile_fft<C, NS, NL, LS, true>(a, b, p.px, p.twx);
 	const size_t line = (size_t)z * p.bY + y0;
 	const uint32_t i0 = p.line_start[line], i1 = p.line_start[line + wy];
 	const V *arg = p.arg + (size_t)r * p.N * 3;
@@ -354,7 +368,7 @@ __global__ void __launch_bounds__(256) mv_fftx_gather(MvP<T, V> p, MvEpi e)
 	typename AccOf<V>::T s0{}, s1r{}, s1i{};
 	const uint32_t cnt = (i1 - i0) * 3;
 #pragma unroll 2
-	for (uint32_t t = threadIdx.x; t < cnt; t += 256) {
+	for (uint32_t t = threadIdx.x; t < cnt; t += NT) {
 		const size_t i = i0 + t / 3;
 		const int comp = t % 3;
 		const uint32_t q = p.xy[i];
@@ -390,8 +404,11 @@ __global__ void __launch_bounds__(256) mv_fftx_gather(MvP<T, V> p, MvEpi e)
 // ---------------------------------------------------------------------------------------------------------------
 // host side
 
+// shared memory of K1/K3 and K2a/K2c: two tiles for the Stockham form, one for the column form (NS known)
 template <typename T> size_t smem_k1(int gX) { return 2 * sizeof(typename CxT<T>::type) * (size_t)gX * tile_ls(3 * Tiles<T>::W1); }
 template <typename T> size_t smem_k2(int gZ) { return 2 * sizeof(typename CxT<T>::type) * (size_t)gZ * tile_ls(Tiles<T>::W2); }
+template <typename T, int NS> size_t smem_k1s(int gX) { return (reg_cols<T, NS>() ? 1 : 2) * smem_k1<T>(gX) / 2; }
+template <typename T, int NS> size_t smem_k2s(int gZ) { return (reg_cols<T, NS>() ? 1 : 2) * smem_k2<T>(gZ) / 2; }
 template <typename T> size_t smem_k2b(int gY)
 {
 	return 2 * sizeof(typename CxT<T>::type) * (size_t)gY * tile_ls(3 * Tiles<T>::PAIRS);
@@ -482,13 +499,14 @@ int launch_matvec(adda_gb300_ctx *c, int R, const V *arg, V *res, int her, const
 	cudaStream_t st = c->stream;
 	const dim3 blk(256);
 	const dim3 g1((c->bY + W1 - 1) / W1, c->bZ, R);
-	ADDA_NS_SWITCH(c->gX, (mv_scatter_fftx<T, V, W1, NS><<<g1, blk, smem_k1<T>(c->gX), st>>>(p)));
+	ADDA_NS_SWITCH(c->gX, (mv_scatter_fftx<T, V, W1, NS>
+		<<<g1, col_threads<T, NS, 3 * W1>(), smem_k1s<T, NS>(c->gX), st>>>(p)));
 	ADDA_LAUNCHED();
 	for (int kx0 = 0; kx0 < c->gX; kx0 += p.CK) {
 		p.kx0 = kx0;
 		const int ck = std::min(p.CK, c->gX - kx0);
 		const dim3 g2((c->bY + W2 - 1) / W2, 3 * ck, R);
-		ADDA_NS_SWITCH(c->gZ, (mv_fftz<T, V, W2, false, NS><<<g2, blk, smem_k2<T>(c->gZ), st>>>(p)));
+		ADDA_NS_SWITCH(c->gZ, (mv_fftz<T, V, W2, false, NS><<<g2, col_threads<T, NS, W2>(), smem_k2s<T, NS>(c->gZ), st>>>(p)));
 		ADDA_LAUNCHED();
 		if (use_k2b_reg<T>(c->gY)) {
 			if constexpr (sizeof(T) == 4) {
@@ -512,10 +530,11 @@ int launch_matvec(adda_gb300_ctx *c, int R, const V *arg, V *res, int her, const
 			ADDA_NS_SWITCH(c->gY, (mv_fft_y_dmul<T, V, NS><<<g2b, blk, smem_k2b<T>(c->gY), st>>>(p)));
 		}
 		ADDA_LAUNCHED();
-		ADDA_NS_SWITCH(c->gZ, (mv_fftz<T, V, W2, true, NS><<<g2, blk, smem_k2<T>(c->gZ), st>>>(p)));
+		ADDA_NS_SWITCH(c->gZ, (mv_fftz<T, V, W2, true, NS><<<g2, col_threads<T, NS, W2>(), smem_k2s<T, NS>(c->gZ), st>>>(p)));
 		ADDA_LAUNCHED();
 	}
-	ADDA_NS_SWITCH(c->gX, (mv_fftx_gather<T, V, W1, NS><<<g1, blk, smem_k1<T>(c->gX), st>>>(p, epi)));
+	ADDA_NS_SWITCH(c->gX, (mv_fftx_gather<T, V, W1, NS>
+		<<<g1, col_threads<T, NS, 3 * W1>(), smem_k1s<T, NS>(c->gX), st>>>(p, epi)));
 	ADDA_LAUNCHED();
 	return ADDA_GB300_OK;
 }
