@@ -467,6 +467,22 @@ __device__ __forceinline__ C *tile_fft(C *a, C *b, const FftPlan &p, const C *__
 }
 
 // ---------------------------------------------------------------------------------------------------------------
+// Asynchronous global -> shared copies of one complex element (cp.async, 8 or 16 bytes): the copy does not pass
+// through registers, so a thread can have all of its tile loads in flight at once. With valid == false nothing is
+// read and the destination is zero-filled (src-size 0); src must still be a mapped address.
+template <typename C> __device__ __forceinline__ void cp_async_elem(C *dst, const C *src, bool valid)
+{
+	const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+	const int n = valid ? (int)sizeof(C) : 0;
+	if (sizeof(C) == 16)
+		asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(n) : "memory");
+	else
+		asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// ---------------------------------------------------------------------------------------------------------------
 // Register-resident two-step FFT of power-of-two length N = T*E for lines held by T consecutive lanes each
 // (T <= E, T | 16): lane j1 of a line owns the E elements j1 + T*j2 in v[j2]. Step 1: DFT_E over j2 in registers,
 // twiddle W_N^(j1*k2), transpose through the line's own shared buffer buf[k2*(T+1) + j1] (odd stride: conflict-free);
@@ -564,6 +580,11 @@ template <typename T, int NS> __host__ __device__ constexpr bool reg_cols() { re
 template <typename T, int NS, int NL> __host__ __device__ constexpr int col_threads()
 {
 	return reg_cols<T, NS>() ? NL * RegShape<NS>::T : 256;
+}
+// resident blocks per SM the column kernels are compiled for (at most 56 registers a thread up to length 256)
+template <typename T, int NS, int NL> __host__ __device__ constexpr int col_minblocks()
+{
+	return (reg_cols<T, NS>() && NS <= 256) ? 65536 / (col_threads<T, NS, NL>() * 56) : 1;
 }
 
 // reorder the output of reg_fft into the input form (v[j] = element j1 + T*j)

@@ -91,7 +91,8 @@ template <> struct Tiles<double> { static constexpr int W1 = 4, W2 = 8, PAIRS = 
 
 // K1: scatter S.x of W consecutive x-lines (one z) into shared memory and FFT along x. Tile: gX x (3*W) lines.
 template <typename T, typename V, int W, int NS>
-__global__ void __launch_bounds__(col_threads<T, NS, 3 * W>()) mv_scatter_fftx(MvP<T, V> p)
+__global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T, NS, 3 * W>()))
+	mv_scatter_fftx(MvP<T, V> p)
 {
 	typedef typename CxT<T>::type C;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -136,7 +137,7 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>()) mv_scatter_fftx(M
 // K2a/K2c: FFT along z of W consecutive y-lines of one (rhs, kx, comp). Forward reads Xf (z<bZ, zero padded) and
 // writes Tz (all kz); inverse reads Tz and writes z<bZ back to Xf.
 template <typename T, typename V, int W, bool INV, int NS>
-__global__ void __launch_bounds__(col_threads<T, NS, W>()) mv_fftz(MvP<T, V> p)
+__global__ void __launch_bounds__(col_threads<T, NS, W>(), (col_minblocks<T, NS, W>())) mv_fftz(MvP<T, V> p)
 {
 	typedef typename CxT<T>::type C;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -157,13 +158,14 @@ __global__ void __launch_bounds__(col_threads<T, NS, W>()) mv_fftz(MvP<T, V> p)
 #pragma unroll 4
 	for (int t = threadIdx.x; t < n * W; t += NT) {
 		const int yy = t % W, z = t / W;
-		C v = cx<C>(0, 0);
 		if (!INV) {
-			if (z < p.bZ && yy < wy) v = xf[(size_t)z * p.bY + yy];
+			const bool ok = z < p.bZ && yy < wy;
+			cp_async_elem(a + z * LS + yy, ok ? xf + (size_t)z * p.bY + yy : xf, ok);
 		}
-		else if (yy < wy) v = tz[(size_t)z * p.bY + yy];
-		a[z * LS + yy] = v;
+		else cp_async_elem(a + z * LS + yy, yy < wy ? tz + (size_t)z * p.bY + yy : tz, yy < wy);
 	}
+	cp_async_commit();
+	cp_async_wait<0>();
 	__syncthreads();
 	C *o = a;
 	if constexpr (RC) tile_cols_fft<C, NS, W, LS, NT, INV>(a, p.twz);
@@ -268,13 +270,27 @@ template <typename V, int NS, int NT> __global__ void __launch_bounds__(NT, 4) m
 	C *slot = reinterpret_cast<C *>(smem_raw) + (size_t)g * 3 * BUF; // slots c*BUF, c = 0..2
 	const size_t lz = (size_t)p.gZ * p.bY;
 	C *col = p.Tz + (((size_t)r * p.CK + kxl) * 3) * lz + (size_t)kz * p.bY;
-	C v[E];
-#pragma unroll 1
+	// the three component lines go to their slots asynchronously (lane j1 writes and later reads only its own
+	// elements, at j*T + j1), one commit group each, so components 1 and 2 arrive during component 0's transform
+#pragma unroll
 	for (int c = 0; c < 3; c++) {
 #pragma unroll
 		for (int j = 0; j < E; j++) {
 			const int y = j1 + T * j;
-			v[j] = (y < p.bY) ? col[c * lz + y] : make_float2(0.f, 0.f);
+			if (y < p.bY) cp_async_elem(slot + c * BUF + j * T + j1, col + c * lz + y, true);
+		}
+		cp_async_commit();
+	}
+	C v[E];
+#pragma unroll
+	for (int c = 0; c < 3; c++) {
+		if (c == 0) cp_async_wait<2>();
+		else if (c == 1) cp_async_wait<1>();
+		else cp_async_wait<0>();
+#pragma unroll
+		for (int j = 0; j < E; j++) {
+			const int y = j1 + T * j;
+			v[j] = (y < p.bY) ? slot[c * BUF + j * T + j1] : make_float2(0.f, 0.f);
 		}
 		reg_fft<C, NS, false>(v, slot + c * BUF, j1, gmask, p.twy);
 		reg_natural<C, NS>(v);
@@ -335,7 +351,8 @@ __device__ __forceinline__ double block_sum(double v, double *sh)
 
 // K3: inverse FFT along x of W y-lines (one z), then y = x + S.X for their dipoles, with the epilogue reductions.
 template <typename T, typename V, int W, int NS>
-__global__ void __launch_bounds__(col_threads<T, NS, 3 * W>()) mv_fftx_gather(MvP<T, V> p, MvEpi e)
+__global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T, NS, 3 * W>()))
+	mv_fftx_gather(MvP<T, V> p, MvEpi e)
 {
 	typedef typename CxT<T>::type C;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -354,8 +371,11 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>()) mv_fftx_gather(Mv
 	for (int t = threadIdx.x; t < n * NL; t += NT) {
 		const int yy = t % W, rest = t / W;
 		const int comp = rest % 3, kx = rest / 3;
-		a[kx * LS + comp * W + yy] = (yy < wy) ? xf[((size_t)kx * 3 + comp) * plane + yy] : cx<C>(0, 0);
+		const bool ok = yy < wy;
+		cp_async_elem(a + kx * LS + comp * W + yy, ok ? xf + ((size_t)kx * 3 + comp) * plane + yy : xf, ok);
 	}
+	cp_async_commit();
+	cp_async_wait<0>();
 	__syncthreads();
 	C *o = a;
 	if constexpr (RC) tile_cols_fft<C, NS, NL, LS, NT, true>(a, p.twx);
