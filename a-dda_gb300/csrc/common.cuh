@@ -6,7 +6,7 @@
 // element at an odd stride visits every bank pair once per 16 threads). Tiles gathered from HBM along the contiguous
 // axis of the data need no transpose. Each pass is a
 // self-sorting Stockham radix-R step (ping-pong between two tiles); radices 2,3,4,8,16 are hand-written register
-// butterflies, 5/7/11/13 use a looped O(R^2) butterfly. Twiddles come from one table of n-th roots of unity per length, computed on the
+// butterflies, 5/7/11/13 a symmetric-pair register butterfly (dft_odd). Twiddles come from one table of n-th roots of unity per length, computed on the
 // host in double precision. Sign convention: forward = exp(-2*pi*i*jk/n), unnormalised, like FFTW's FFTW_FORWARD
 // which the reference uses (fft.h FFT_FORWARD -1).
 #pragma once
@@ -313,14 +313,98 @@ template <typename C> __device__ __forceinline__ void dft3(C *v, bool inv)
 	v[2] = csub(m1, m2);
 }
 
+// cos/sin(2*pi*k/R), k = 0..(R-1)/2, for the odd prime radices of fftFit's sizes (local constant tables: with the
+// index known after unrolling they fold into immediates)
+template <int R> __device__ __forceinline__ double odd_cos(int k)
+{
+	if constexpr (R == 5) {
+		const double t[3] = {1.0, 0.30901699437494745126, -0.80901699437494734024};
+		return t[k];
+	}
+	else if constexpr (R == 7) {
+		const double t[4] = {1.0, 0.62348980185873359439, -0.22252093395631433737, -0.90096886790241903498};
+		return t[k];
+	}
+	else if constexpr (R == 11) {
+		const double t[6] = {1.0, 0.84125353283118120551, 0.41541501300188643508, -0.14231483827328500480,
+			-0.65486073394528498959, -0.95949297361449736865};
+		return t[k];
+	}
+	else {
+		const double t[7] = {1.0, 0.88545602565320991051, 0.56806474673115592289, 0.12053668025532300601,
+			-0.35460488704253545489, -0.74851074817110119231, -0.97094181742605201180};
+		return t[k];
+	}
+}
+template <int R> __device__ __forceinline__ double odd_sin(int k)
+{
+	if constexpr (R == 5) {
+		const double t[3] = {0.0, 0.95105651629515353118, 0.58778525229247324813};
+		return t[k];
+	}
+	else if constexpr (R == 7) {
+		const double t[4] = {0.0, 0.78183148246802980363, 0.97492791218182361934, 0.43388373911755823142};
+		return t[k];
+	}
+	else if constexpr (R == 11) {
+		const double t[6] = {0.0, 0.54064081745559755543, 0.90963199535451833011, 0.98982144188093279524,
+			0.75574957435425826890, 0.28173255684142967104};
+		return t[k];
+	}
+	else {
+		const double t[7] = {0.0, 0.46472317204376850652, 0.82298386589365635224, 0.99270887409805397272,
+			0.93501624268541483342, 0.66312265824079519305, 0.23931566428755768339};
+		return t[k];
+	}
+}
+
+// DFT of odd prime length R in registers, symmetric-pair form: with a_p = x_p + x_(R-p), b_p = x_p - x_(R-p),
+// X_k = x_0 + sum_p a_p cos(2 pi p k / R) -/+ i sum_p b_p sin(2 pi p k / R) and X_(R-k) with the other sign
+// ((R-1)^2 real multiply-adds instead of the R^2 complex ones of the direct sum).
+template <typename C, int R> __device__ __forceinline__ void dft_odd(C *v, bool inv)
+{
+	typedef decltype(C::x) T;
+	constexpr int H = (R - 1) / 2;
+	C a[H], b[H];
+#pragma unroll
+	for (int p = 1; p <= H; p++) {
+		a[p - 1] = cadd(v[p], v[R - p]);
+		b[p - 1] = csub(v[p], v[R - p]);
+	}
+	const C x0 = v[0];
+	C sum = x0;
+#pragma unroll
+	for (int p = 0; p < H; p++) sum = cadd(sum, a[p]);
+	v[0] = sum;
+#pragma unroll
+	for (int k = 1; k <= H; k++) {
+		C t = x0, u = cx<C>(0, 0);
+#pragma unroll
+		for (int p = 1; p <= H; p++) {
+			const int i = (p * k) % R;
+			const T cs = (T)(i <= H ? odd_cos<R>(i) : odd_cos<R>(R - i));
+			const T sn = (T)(i <= H ? odd_sin<R>(i) : -odd_sin<R>(R - i));
+			t.x += cs * a[p - 1].x;
+			t.y += cs * a[p - 1].y;
+			u.x += sn * b[p - 1].x;
+			u.y += sn * b[p - 1].y;
+		}
+		// forward: X_k = t - i u, X_(R-k) = t + i u; inverse the other way round
+		const C m = cx<C>(t.x + u.y, t.y - u.x), q = cx<C>(t.x - u.y, t.y + u.x);
+		v[k] = inv ? q : m;
+		v[R - k] = inv ? m : q;
+	}
+}
+
 template <typename C, int R> __device__ __forceinline__ void dft(C *v, bool inv, const C *__restrict__ tw, int n)
 {
-	if (R == 2) dft2(v[0], v[1]);
-	else if (R == 3) dft3(v, inv);
-	else if (R == 4) dft4(v, inv);
-	else if (R == 8) dft8(v, inv);
-	else if (R == 16) dft16(v, inv);
-	else if (R == 32) dft32(v, inv);
+	if constexpr (R == 2) dft2(v[0], v[1]);
+	else if constexpr (R == 3) dft3(v, inv);
+	else if constexpr (R == 4) dft4(v, inv);
+	else if constexpr (R == 8) dft8(v, inv);
+	else if constexpr (R == 16) dft16(v, inv);
+	else if constexpr (R == 32) dft32(v, inv);
+	else if constexpr (R == 5 || R == 7 || R == 11 || R == 13) dft_odd<C, R>(v, inv);
 }
 
 // One Stockham pass over all lines of an element-major tile: x -> y.
@@ -400,7 +484,11 @@ __device__ C *fft_tile(C *a, C *b, const FftPlan &p, int nl, int ls, const C *__
 			case 4: fft_pass<C, 4>(a, b, n, nl, ls, m, tw, inv); break;
 			case 8: fft_pass<C, 8>(a, b, n, nl, ls, m, tw, inv); break;
 			case 16: fft_pass<C, 16>(a, b, n, nl, ls, m, tw, inv); break;
-			default: fft_pass_gen<C>(a, b, R, n, nl, ls, m, tw, inv); break; // 5, 7, 11, 13
+			case 5: fft_pass<C, 5>(a, b, n, nl, ls, m, tw, inv); break;
+			case 7: fft_pass<C, 7>(a, b, n, nl, ls, m, tw, inv); break;
+			case 11: fft_pass<C, 11>(a, b, n, nl, ls, m, tw, inv); break;
+			case 13: fft_pass<C, 13>(a, b, n, nl, ls, m, tw, inv); break;
+			default: fft_pass_gen<C>(a, b, R, n, nl, ls, m, tw, inv); break;
 		}
 		__syncthreads();
 		C *t = a;

@@ -929,6 +929,15 @@ static int solve_mixed(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int
 		double inner_eps0 = sp->inner_eps > 0 ? sp->inner_eps : 0.5 * sp->eps;
 		int *d_odone = w->done; // reused below as skip flags after the inner solve (copied from host)
 		for (int step = 0; step <= maxref; step++) {
+			// an RHS whose inner solves used up maxiter stops refining (reported as maxiter below)
+			if (step > 0) {
+				bool all = true;
+				for (int r = 0; r < R; r++) {
+					if (!odone[r] && iters[r] >= sp->maxiter) odone[r] = 1;
+					all = all && odone[r];
+				}
+				if (all) break;
+			}
 			// inner solve: A d = rhs (rhs float in k.v3 on entry); init per the user's field mode at step 0
 			std::vector<double> eps_in(R);
 			for (int r = 0; r < R; r++) {

@@ -56,6 +56,13 @@ SETUPS = {
     "cube_7x11x13_radix7_11_13": lambda: cube_setup((7, 11, 13), (14, 22, 26)),
     "cube_5x3x9_radix5_3": lambda: cube_setup((5, 3, 9), (10, 6, 18)),
     "grid2_tiny": lambda: setup_for(case("grid2")["setup"]),
+    # power-of-two axes of 64..512 take the compile-time kernels (register/column FFTs in FP32): one axis of 512
+    # at a time on thin boxes, and 64/128/256 together, each checked against the oracle
+    "thin_x512": lambda: cube_setup((256, 3, 2), (512, 6, 4)),
+    "thin_y512": lambda: cube_setup((2, 256, 3), (4, 512, 6)),
+    "thin_z512": lambda: cube_setup((3, 2, 256), (6, 4, 512)),
+    "box_64x128x256": lambda: cube_setup((32, 64, 128), (64, 128, 256)),
+    "box_256x64x128": lambda: cube_setup((128, 32, 64), (256, 64, 128)),
 }
 
 
