@@ -39,8 +39,10 @@ WORKLOAD = ("sphere 128^3 box, N=1099136 dipoles, FFT grid 256^3, m=1.33+0.01i, 
 # iteration counts of the reference build (ADDA 1.3b6 seq + FFTW-subset shim) on this workload, per polarisation
 # (Y, X), from a full run of '-grid 128 -dpl 15 -m 1.33 0.01 -iter <m> -eps 5 -sym no'; used only to extrapolate
 # the bounded CPU samples to a time-to-solution
-REF_ITERS = {"qmr": None, "bicgstab": None}  # the reference's own iteration counts, when known
-# iteration counts of the FP64 GPU solve of this workload (Y, X polarisation), used until REF_ITERS is known
+# (tests/golden/reference_c2.json: 623 + 648 QMR_CS iterations in 6956 s, 311 + 314 BiCGStab iterations in 6726 s
+# of one x86 core)
+REF_ITERS = {"qmr": (623, 648), "bicgstab": (311, 314)}
+# iteration counts of the FP64 GPU solve of this workload (Y, X polarisation)
 FP64_ITERS = {"qmr": (647, 641), "bicgstab": (309, 308)}
 
 
