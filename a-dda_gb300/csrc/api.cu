@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -10,6 +11,9 @@
 namespace adda {
 
 static thread_local std::string g_err;
+
+// largest L2 chunk budget the FP32 matvec tuner tries (MB)
+constexpr int CHUNK_TUNE_MAX_MB = 128;
 std::atomic<unsigned long long> g_launches{0};
 
 void set_error(const std::string &msg) { g_err = msg; }
@@ -168,10 +172,22 @@ static int create_impl(const adda_gb300_problem *p, adda_gb300_ctx *c)
 	const size_t R = c->Rmax;
 	ADDA_CUDA(cudaMalloc(&c->Xf, sizeof(double2) * R * c->gX * 3 * (size_t)c->bZ * c->bY));
 	const size_t slab = R * 3 * (size_t)c->gZ * c->bY; // complex elements of one x-slab for all RHS
+	// FP64: 48 MB chunks. FP32: the chunk is tuned after the D matrix (tune_chunks) among budgets up to
+	// CHUNK_TUNE_MAX_MB; ADDA_GB300_CHUNK_MB fixes the FP32 budget instead.
 	const size_t budget = 48u << 20;
 	c->CK64 = (int)std::max<size_t>(1, std::min<size_t>(c->gX, budget / (slab * sizeof(double2))));
-	c->CK32 = (int)std::max<size_t>(1, std::min<size_t>(c->gX, budget / (slab * sizeof(float2))));
-	const size_t tz = std::max(c->CK64 * sizeof(double2), c->CK32 * sizeof(float2)) * slab;
+	size_t b32 = budget;
+	if (const char *e = getenv("ADDA_GB300_CHUNK_MB")) {
+		const long mb = atol(e);
+		if (mb > 0 && mb <= 4096) {
+			b32 = (size_t)mb << 20;
+			c->chunk_fixed = true;
+		}
+	}
+	c->CK32 = (int)std::max<size_t>(1, std::min<size_t>(c->gX, b32 / (slab * sizeof(float2))));
+	c->CK32max = c->chunk_fixed ? c->CK32
+		: (int)std::max<size_t>(1, std::min<size_t>(c->gX, ((size_t)CHUNK_TUNE_MAX_MB << 20) / (slab * sizeof(float2))));
+	const size_t tz = std::max(c->CK64 * sizeof(double2), c->CK32max * sizeof(float2)) * slab;
 	ADDA_CUDA(cudaMalloc(&c->Tz, tz));
 	c->partial_len = R * matvec_partial_blocks(c, true) * 4;
 	ADDA_CUDA(cudaMalloc(&c->partial, sizeof(double) * c->partial_len));
@@ -222,6 +238,61 @@ int adda_gb300_create(const adda_gb300_problem *p, adda_gb300_ctx **out)
 	}
 	*out = c;
 	return ADDA_GB300_OK;
+}
+
+__global__ void fill_k(double2 *v, size_t n, unsigned seed);
+__global__ void d2f_k(float2 *dst, const double2 *src, size_t n);
+
+// The FP32 matvec's chunk (x-slabs whose z-transformed data pass through L2 between K2a, K2b and K2c) trades L2
+// residency against launch count and tail waves; its best size depends on the grid and the RHS count. Measured once
+// per context on its own data sizes: budgets of 24..CHUNK_TUNE_MAX_MB, one warm-up and two timed matvecs each with
+// Rmax RHS of random data (CUDA events on the context stream); the fastest is kept. Runs from check_ready, i.e.
+// only once the D matrix and the polarisability buffers a matvec reads exist, and before any graph capture.
+static int tune_chunks(adda_gb300_ctx *c)
+{
+	if (c->chunk_fixed || c->chunk_tuned || c->N == 0 || !c->dready || !c->ccs32) return ADDA_GB300_OK;
+	ADDA_CUDA(cudaSetDevice(c->device));
+	cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+	ADDA_CUDA(cudaStreamIsCapturing(c->stream, &cap));
+	if (cap != cudaStreamCaptureStatusNone) return ADDA_GB300_OK; // a caller is recording: keep the default
+	c->chunk_tuned = true;
+	const size_t slab = (size_t)c->Rmax * 3 * c->gZ * c->bY;
+	const size_t n = (size_t)c->Rmax * 3 * c->N;
+	fill_k<<<1024, 256, 0, c->stream>>>((double2 *)c->vin, n, 777u);
+	ADDA_LAUNCHED();
+	d2f_k<<<1024, 256, 0, c->stream>>>((float2 *)c->vout, (const double2 *)c->vin, n);
+	ADDA_LAUNCHED();
+	const float2 *in = (const float2 *)c->vout;
+	float2 *out = (float2 *)c->vout + n;
+	MvEpi e{EPI_NONE, nullptr, c->partial};
+	cudaEvent_t e0, e1;
+	ADDA_CUDA(cudaEventCreate(&e0));
+	ADDA_CUDA(cudaEventCreate(&e1));
+	const int mbs[] = {24, 48, 64, 96, CHUNK_TUNE_MAX_MB};
+	int best_ck = c->CK32, last = -1, rc = ADDA_GB300_OK;
+	float best = 1e30f;
+	for (int mb : mbs) {
+		const int ck = (int)std::max<size_t>(1, std::min<size_t>(c->CK32max, ((size_t)mb << 20) / (slab * sizeof(float2))));
+		if (ck == last) continue;
+		last = ck;
+		c->CK32 = ck;
+		if ((rc = matvec_run<float>(c, c->Rmax, in, out, 0, e, nullptr))) break;
+		cudaEventRecord(e0, c->stream);
+		for (int i = 0; i < 2 && !rc; i++) rc = matvec_run<float>(c, c->Rmax, in, out, 0, e, nullptr);
+		cudaEventRecord(e1, c->stream);
+		if (cudaEventSynchronize(e1) != cudaSuccess) rc = ADDA_GB300_ECUDA;
+		if (rc) break;
+		float t = 0;
+		cudaEventElapsedTime(&t, e0, e1);
+		if (t < best) {
+			best = t;
+			best_ck = ck;
+		}
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	c->CK32 = best_ck;
+	return rc;
 }
 
 int adda_gb300_init_dmatrix(adda_gb300_ctx *c)
@@ -347,7 +418,7 @@ static int check_ready(adda_gb300_ctx *c, int nrhs)
 			set_error("polarisabilities not set for every RHS (call adda_gb300_set_cc)");
 			return ADDA_GB300_ESTATE;
 		}
-	return ADDA_GB300_OK;
+	return tune_chunks(c);
 }
 
 __global__ void d2f_k(float2 *dst, const double2 *src, size_t n)

@@ -83,6 +83,9 @@ struct adda_gb300_ctx {
 	void *Xf = nullptr;               // [R][gX][3][bZ][bY] after the X transform
 	void *Tz = nullptr;               // [R][CK][3][gZ][bY] chunk of x-slabs after the Z transform
 	int CK64 = 1, CK32 = 1;           // x-slabs per chunk (sized to stay resident in L2)
+	int CK32max = 1;                  // largest FP32 chunk the Tz buffer holds
+	bool chunk_fixed = false;         // chunk size set by the environment: no tuning
+	bool chunk_tuned = false;         // FP32 chunk size measured (tune_chunks)
 	double *partial = nullptr;        // epilogue partial sums
 	size_t partial_len = 0;
 	double *d_red = nullptr;          // reduced per-RHS results [Rmax][4]
