@@ -109,17 +109,18 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T,
 	const size_t line = (size_t)z * p.bY + y0;
 	const uint32_t i0 = p.line_start[line], i1 = p.line_start[line + wy];
 	const V *arg = p.arg + (size_t)r * p.N * 3;
-	const uint32_t cnt = (i1 - i0) * 3;
-#pragma unroll 4
-	for (uint32_t t = threadIdx.x; t < cnt; t += NT) {
-		const size_t i = i0 + t / 3;
-		const int comp = t % 3;
+#pragma unroll 2
+	for (uint32_t i = i0 + threadIdx.x; i < i1; i += NT) {
 		const uint32_t q = p.xy[i];
 		const int x = q & 0xffff, y = q >> 16;
-		C v = cvt<C>(arg[i * 3 + comp]);
-		if (p.her) v = cconj(v);
-		v = cmul(ccs_of(p.ccs, p.per_dip, p.nmat, p.N, r, i, p.mat[i], comp), v);
-		a[x * LS + comp * W + (y - y0)] = v;
+		const uint8_t m = p.mat[i];
+#pragma unroll
+		for (int comp = 0; comp < 3; comp++) {
+			C v = cvt<C>(arg[(size_t)i * 3 + comp]);
+			if (p.her) v = cconj(v);
+			v = cmul(ccs_of(p.ccs, p.per_dip, p.nmat, p.N, r, i, m, comp), v);
+			a[x * LS + comp * W + (y - y0)] = v;
+		}
 	}
 	__syncthreads();
 	C *o = a;
@@ -127,10 +128,22 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T,
 	else o = tile_fft<C, NS, NL, LS, false>(a, b, p.px, p.twx);
 	const size_t plane = (size_t)p.bZ * p.bY;
 	C *xf = p.Xf + (size_t)r * p.gX * 3 * plane + (size_t)z * p.bY + y0;
-	for (int t = threadIdx.x; t < n * NL; t += NT) {
-		const int yy = t % W, rest = t / W;
-		const int comp = rest % 3, kx = rest / 3;
-		if (yy < wy) xf[((size_t)kx * 3 + comp) * plane + yy] = o[kx * LS + comp * W + yy];
+	if constexpr (RC) {
+		// NT is a multiple of NL: each thread keeps one line (comp, yy) and walks kx
+		constexpr int KS = NT / NL;
+		const int l = threadIdx.x % NL, comp = l / W, yy = l % W;
+		if (yy < wy) {
+			C *dst = xf + (size_t)comp * plane + yy + (size_t)(threadIdx.x / NL) * 3 * plane;
+#pragma unroll 4
+			for (int kx = threadIdx.x / NL; kx < NS; kx += KS, dst += (size_t)KS * 3 * plane) *dst = o[kx * LS + l];
+		}
+	}
+	else {
+		for (int t = threadIdx.x; t < n * NL; t += NT) {
+			const int yy = t % W, rest = t / W;
+			const int comp = rest % 3, kx = rest / 3;
+			if (yy < wy) xf[((size_t)kx * 3 + comp) * plane + yy] = o[kx * LS + comp * W + yy];
+		}
 	}
 }
 
@@ -155,14 +168,19 @@ __global__ void __launch_bounds__(col_threads<T, NS, W>(), (col_minblocks<T, NS,
 	const size_t plane = (size_t)p.bZ * p.bY;
 	C *xf = p.Xf + (((size_t)r * p.gX + kx) * 3 + comp) * plane + y0;
 	C *tz = p.Tz + (((size_t)r * p.CK + kxl) * 3 + comp) * (size_t)n * p.bY + y0;
+	// NT is a multiple of W: each thread keeps one y-line and walks z with a constant stride
+	constexpr int ZS = NT / W;
+	const int yy = threadIdx.x % W, z0 = threadIdx.x / W;
+	const bool yok = yy < wy;
+	{
+		const C *src = (INV ? tz : xf) + (size_t)z0 * p.bY + yy;
+		const C *base = INV ? tz : xf;
+		const size_t step = (size_t)ZS * p.bY;
 #pragma unroll 4
-	for (int t = threadIdx.x; t < n * W; t += NT) {
-		const int yy = t % W, z = t / W;
-		if (!INV) {
-			const bool ok = z < p.bZ && yy < wy;
-			cp_async_elem(a + z * LS + yy, ok ? xf + (size_t)z * p.bY + yy : xf, ok);
+		for (int z = z0; z < n; z += ZS, src += step) {
+			const bool ok = yok && (INV || z < p.bZ);
+			cp_async_elem(a + z * LS + yy, ok ? src : base, ok);
 		}
-		else cp_async_elem(a + z * LS + yy, yy < wy ? tz + (size_t)z * p.bY + yy : tz, yy < wy);
 	}
 	cp_async_commit();
 	cp_async_wait<0>();
@@ -171,11 +189,11 @@ __global__ void __launch_bounds__(col_threads<T, NS, W>(), (col_minblocks<T, NS,
 	if constexpr (RC) tile_cols_fft<C, NS, W, LS, NT, INV>(a, p.twz);
 	else o = tile_fft<C, NS, W, LS, INV>(a, b, p.pz, p.twz);
 	const int zmax = INV ? p.bZ : n;
-	for (int t = threadIdx.x; t < zmax * W; t += NT) {
-		const int yy = t % W, z = t / W;
-		if (yy >= wy) continue;
-		if (!INV) tz[(size_t)z * p.bY + yy] = o[z * LS + yy];
-		else xf[(size_t)z * p.bY + yy] = o[z * LS + yy];
+	if (yok) {
+		C *dst = (INV ? xf : tz) + (size_t)z0 * p.bY + yy;
+		const size_t step = (size_t)ZS * p.bY;
+#pragma unroll 4
+		for (int z = z0; z < zmax; z += ZS, dst += step) *dst = o[z * LS + yy];
 	}
 }
 
@@ -367,12 +385,23 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T,
 	const int wy = min(W, p.bY - y0);
 	const size_t plane = (size_t)p.bZ * p.bY;
 	const C *xf = p.Xf + (size_t)r * p.gX * 3 * plane + (size_t)z * p.bY + y0;
-#pragma unroll 4
-	for (int t = threadIdx.x; t < n * NL; t += NT) {
-		const int yy = t % W, rest = t / W;
-		const int comp = rest % 3, kx = rest / 3;
+	if constexpr (RC) {
+		constexpr int KS = NT / NL;
+		const int l = threadIdx.x % NL, comp = l / W, yy = l % W;
 		const bool ok = yy < wy;
-		cp_async_elem(a + kx * LS + comp * W + yy, ok ? xf + ((size_t)kx * 3 + comp) * plane + yy : xf, ok);
+		const C *src = xf + (size_t)comp * plane + yy + (size_t)(threadIdx.x / NL) * 3 * plane;
+#pragma unroll 4
+		for (int kx = threadIdx.x / NL; kx < NS; kx += KS, src += (size_t)KS * 3 * plane)
+			cp_async_elem(a + kx * LS + l, ok ? src : xf, ok);
+	}
+	else {
+#pragma unroll 4
+		for (int t = threadIdx.x; t < n * NL; t += NT) {
+			const int yy = t % W, rest = t / W;
+			const int comp = rest % 3, kx = rest / 3;
+			const bool ok = yy < wy;
+			cp_async_elem(a + kx * LS + comp * W + yy, ok ? xf + ((size_t)kx * 3 + comp) * plane + yy : xf, ok);
+		}
 	}
 	cp_async_commit();
 	cp_async_wait<0>();
@@ -386,24 +415,25 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T,
 	V *res = p.res + (size_t)r * p.N * 3;
 	const V *u = e.u ? reinterpret_cast<const V *>(e.u) + (size_t)r * p.N * 3 : nullptr;
 	typename AccOf<V>::T s0{}, s1r{}, s1i{};
-	const uint32_t cnt = (i1 - i0) * 3;
-#pragma unroll 2
-	for (uint32_t t = threadIdx.x; t < cnt; t += NT) {
-		const size_t i = i0 + t / 3;
-		const int comp = t % 3;
+	for (uint32_t i = i0 + threadIdx.x; i < i1; i += NT) {
 		const uint32_t q = p.xy[i];
 		const int x = q & 0xffff, y = q >> 16;
-		V xv = arg[i * 3 + comp];
-		if (p.her) xv = cconj(xv);
-		const C sx = cmul(ccs_of(p.ccs, p.per_dip, p.nmat, p.N, r, i, p.mat[i], comp), o[x * LS + comp * W + (y - y0)]);
-		V yv = cadd(xv, cvt<V>(sx));
-		if (p.her) yv = cconj(yv);
-		res[i * 3 + comp] = yv;
-		if (e.mode) {
-			if (e.mode & EPI_NORM) acc_abs2(s0, yv);
-			if (e.mode & EPI_DOT_ARG) acc_cmul(s1r, s1i, arg[i * 3 + comp], yv);      // x.y
-			if (e.mode & EPI_DOT_ARG_CONJ) acc_cmulc(s1r, s1i, arg[i * 3 + comp], yv); // x.y*
-			if (e.mode & EPI_DOT_U_CONJ) acc_cmulc(s1r, s1i, yv, u[i * 3 + comp]);     // y.u*
+		const uint8_t m = p.mat[i];
+#pragma unroll
+		for (int comp = 0; comp < 3; comp++) {
+			const size_t j = (size_t)i * 3 + comp;
+			const V x0 = arg[j];
+			const V xv = p.her ? cconj(x0) : x0;
+			const C sx = cmul(ccs_of(p.ccs, p.per_dip, p.nmat, p.N, r, i, m, comp), o[x * LS + comp * W + (y - y0)]);
+			V yv = cadd(xv, cvt<V>(sx));
+			if (p.her) yv = cconj(yv);
+			res[j] = yv;
+			if (e.mode) {
+				if (e.mode & EPI_NORM) acc_abs2(s0, yv);
+				if (e.mode & EPI_DOT_ARG) acc_cmul(s1r, s1i, x0, yv);      // x.y
+				if (e.mode & EPI_DOT_ARG_CONJ) acc_cmulc(s1r, s1i, x0, yv); // x.y*
+				if (e.mode & EPI_DOT_U_CONJ) acc_cmulc(s1r, s1i, yv, u[j]);  // y.u*
+			}
 		}
 	}
 	if (e.mode) {
