@@ -476,6 +476,142 @@ static int bcgs_iter(solver *s, bcgs_state *b)
 	return OR_OK;
 }
 
+/* BiCG_CS (COCG), src/iterative.c:490-637 */
+static int bicg_iter(solver *s, cplx *ro_old)
+{
+	const size_t n = s->n;
+	cplx ro_new = ndot_conj(s->r, s->r, n);
+	const double abs_ro = cabs(ro_new);
+	if (abs_ro / s->inprodR < 1e-10) return OR_EBREAKDOWN;
+	if (s->niter == 1) memcpy(s->p, s->r, sizeof(cplx) * n);
+	else {
+		cplx beta = ro_new / *ro_old;
+		for (size_t i = 0; i < n; i++) s->p[i] = beta * s->p[i] + s->r[i];
+	}
+	if (!(s->niter == 1 && s->matvec_ready)) mv(s, s->p, s->Av, NULL);
+	cplx mu = ndot_conj(s->p, s->Av, n);
+	if (cabs(mu) / abs_ro < 1e-10) return OR_EBREAKDOWN;
+	cplx alpha = ro_new / mu;
+	for (size_t i = 0; i < n; i++) s->x[i] += alpha * s->p[i];
+	cplx ma = -alpha;
+	double sum = 0;
+	for (size_t i = 0; i < n; i++) {
+		s->r[i] += ma * s->Av[i];
+		sum += creal(s->r[i]) * creal(s->r[i]) + cimag(s->r[i]) * cimag(s->r[i]);
+	}
+	s->inprodRp1 = sum;
+	*ro_old = ro_new;
+	return OR_OK;
+}
+
+/* CGNR, src/iterative.c:729-769: CG on A^H A x = A^H b, real recurrence scalars */
+static int cgnr_iter(solver *s, double *ro_old)
+{
+	const size_t n = s->n;
+	double ro_new, den;
+	if (s->niter == 1) or_matvec(s->c, (const double *)s->r, (double *)s->p, &ro_new, 1);
+	else {
+		or_matvec(s->c, (const double *)s->r, (double *)s->Av, &ro_new, 1);
+		const double beta = ro_new / *ro_old;
+		for (size_t i = 0; i < n; i++) s->p[i] = beta * s->p[i] + s->Av[i];
+	}
+	mv(s, s->p, s->Av, &den);
+	const double alpha = ro_new / den;
+	for (size_t i = 0; i < n; i++) s->x[i] += alpha * s->p[i];
+	double sum = 0;
+	for (size_t i = 0; i < n; i++) {
+		s->r[i] += -alpha * s->Av[i];
+		sum += creal(s->r[i]) * creal(s->r[i]) + cimag(s->r[i]) * cimag(s->r[i]);
+	}
+	s->inprodRp1 = sum;
+	*ro_old = ro_new;
+	return OR_OK;
+}
+
+/* CSYM (Bunse-Gerstner & Stover), src/iterative.c:773-892; q_k lives in r (q_new) and v1 (q_old), p_k in p / v2 */
+typedef struct {
+	double beta, c_old, c_new;
+	cplx tau, s_old, s_new;
+	cplx *q_new, *q_old, *p_new, *p_old;
+} csym_state;
+
+static void csym_init(solver *s, csym_state *q)
+{
+	q->q_new = s->r; q->q_old = s->v1; q->p_new = s->p; q->p_old = s->v2;
+	q->tau = sqrt(s->inprodR);
+	const double t = 1 / creal(q->tau);
+	for (size_t i = 0; i < s->n; i++) q->q_new[i] = t * conj(q->q_new[i]);
+	q->c_new = 1;
+	q->c_old = 0;
+	q->s_new = q->s_old = 0;
+	q->beta = 0;
+}
+
+static int csym_iter(solver *s, csym_state *q)
+{
+	const size_t n = s->n;
+	mv(s, q->q_new, s->Av, NULL);
+	cplx alpha = ndot_conj(q->q_new, s->Av, n);
+	cplx eta = q->c_old * q->c_new * q->beta + alpha * conj(q->s_new);
+	cplx gamma = q->c_new * alpha - q->c_old * q->s_new * q->beta;
+	cplx theta = q->beta * conj(q->s_old);
+	cplx ma = -alpha;
+	double dtmp = 0;
+	if (s->niter == 1)
+		for (size_t i = 0; i < n; i++) {
+			q->q_old[i] = ma * conj(q->q_new[i]) + s->Av[i];
+			dtmp += creal(q->q_old[i]) * creal(q->q_old[i]) + cimag(q->q_old[i]) * cimag(q->q_old[i]);
+		}
+	else
+		for (size_t i = 0; i < n; i++) {
+			q->q_old[i] = -q->beta * conj(q->q_old[i]) + ma * conj(q->q_new[i]) + s->Av[i];
+			dtmp += creal(q->q_old[i]) * creal(q->q_old[i]) + cimag(q->q_old[i]) * cimag(q->q_old[i]);
+		}
+	q->beta = sqrt(dtmp);
+	q->c_old = q->c_new;
+	q->s_old = q->s_new;
+	cplx invksi;
+	double ag = cabs(gamma);
+	if (ag == 0) {
+		if (q->beta == 0) return OR_EBREAKDOWN; // singular interaction matrix (iterative.c:845)
+		q->c_new = 0;
+		q->s_new = 1;
+		invksi = 1 / q->beta;
+	}
+	else {
+		if (ag < q->beta) {
+			ag = ag / q->beta;
+			q->c_new = ag / sqrt(1 + ag * ag);
+		}
+		else {
+			ag = q->beta / ag;
+			q->c_new = 1 / sqrt(1 + ag * ag);
+		}
+		invksi = q->c_new / gamma;
+		q->s_new = q->beta * invksi;
+	}
+	if (s->niter == 1)
+		for (size_t i = 0; i < n; i++) q->p_new[i] = invksi * q->q_new[i];
+	else {
+		cplx t1 = -eta * invksi;
+		if (s->niter == 2)
+			for (size_t i = 0; i < n; i++) q->p_old[i] = t1 * q->p_new[i] + invksi * q->q_new[i];
+		else {
+			cplx t2 = -theta * invksi;
+			for (size_t i = 0; i < n; i++) q->p_old[i] = t2 * q->p_old[i] + t1 * q->p_new[i] + invksi * q->q_new[i];
+		}
+		cplx *tp = q->p_old; q->p_old = q->p_new; q->p_new = tp;
+	}
+	cplx t1 = q->c_new * q->tau;
+	for (size_t i = 0; i < n; i++) s->x[i] += t1 * q->p_new[i];
+	const double ib = 1 / q->beta;
+	for (size_t i = 0; i < n; i++) q->q_old[i] = ib * conj(q->q_old[i]);
+	cplx *tq = q->q_old; q->q_old = q->q_new; q->q_new = tq;
+	q->tau *= -q->s_new;
+	s->inprodRp1 = creal(q->tau) * creal(q->tau) + cimag(q->tau) * cimag(q->tau);
+	return OR_OK;
+}
+
 /* IterativeSolver, src/iterative.c:1398-1530 with CalcInitField (:1342-1394) and ProgressReport (:282-318).
  * einc: incident field [N][3]; xvec receives x, pvec the polarisations S.x; resid_hist[0..] the relative residuals
  * RE_000, RE_001, ... (at most hist_cap values). Returns a status code; *niter_out = iterations performed. */
@@ -527,19 +663,29 @@ int or_solve(or_ctx *c, int method, const double *einc, double eps, int maxiter,
 	if (nh < hist_cap) resid_hist[nh++] = sqrt(resid_scale * S.inprodR);
 	S.niter = 1;
 	S.counter = 0;
-	const int mc = 50000; // QMR_CS and BiCGStab stagnation limits are 50000 and 30000 (iterative.c:118-125)
-	const int mcm = (method == OR_BICGSTAB) ? 30000 : mc;
+	// stagnation limits per method (iterative.c:118-125)
+	const int mcm = (method == OR_BICGSTAB) ? 30000 : (method == OR_CGNR || method == OR_CSYM) ? 10 : 50000;
 	qmr_state q;
 	bcgs_state bs;
+	csym_state cs;
+	cplx ro_c = 0;
+	double ro_d = 0;
 	if (method == OR_QMR_CS) qmr_init(&S, &q);
-	else {
+	else if (method == OR_BICGSTAB) {
 		bs.v = S.v1; bs.sv = S.v2; bs.rt = S.v3;
 		memcpy(bs.rt, S.r, sizeof(cplx) * n);
 	}
+	else if (method == OR_CSYM) csym_init(&S, &cs);
 	int status = OR_OK;
 	while (S.inprodR > S.epsB && S.niter <= maxiter && S.counter <= mcm) {
 		S.complete = 1;
-		status = (method == OR_QMR_CS) ? qmr_iter(&S, &q) : bcgs_iter(&S, &bs);
+		switch (method) {
+			case OR_QMR_CS: status = qmr_iter(&S, &q); break;
+			case OR_BICGSTAB: status = bcgs_iter(&S, &bs); break;
+			case OR_BICG_CS: status = bicg_iter(&S, &ro_c); break;
+			case OR_CGNR: status = cgnr_iter(&S, &ro_d); break;
+			default: status = csym_iter(&S, &cs); break;
+		}
 		if (status != OR_OK) break;
 		if (S.inprodRp1 <= S.inprodR) {
 			S.inprodR = S.inprodRp1;

@@ -57,6 +57,20 @@ CASES = [
     ("box12", ["-shape", "box", "-grid", "12", "-m", "1.3", "0.05"], dict(grid=12, m=1.3 + 0.05j, shape="box")),
     ("c2_small", ["-grid", "32", "-dpl", "15", "-m", "1.33", "0.01", "-iter", "bicgstab", "-eps", "5"],
      dict(grid=32, m=1.33 + 0.01j, dpl=15, iter="bicgstab")),
+    # the other solvers of the reference (-iter bicg|cgnr|csym)
+    ("mgn_bicg", ["-iter", "bicg"] + MGN, dict(grid=8, m=1.1 + 0.1j, iter="bicg")),
+    ("mgn_cgnr", ["-iter", "cgnr"] + MGN, dict(grid=8, m=1.1 + 0.1j, iter="cgnr")),
+    ("mgn_csym", ["-iter", "csym"] + MGN, dict(grid=8, m=1.1 + 0.1j, iter="csym")),
+    ("c1_bicg", ["-grid", "16", "-dpl", "10", "-m", "1.5", "0", "-iter", "bicg", "-eps", "5"],
+     dict(grid=16, m=1.5, dpl=10, iter="bicg")),
+    ("c1_cgnr", ["-grid", "16", "-dpl", "10", "-m", "1.5", "0", "-iter", "cgnr", "-eps", "5"],
+     dict(grid=16, m=1.5, dpl=10, iter="cgnr")),
+    ("c1_csym", ["-grid", "16", "-dpl", "10", "-m", "1.5", "0", "-iter", "csym", "-eps", "5"],
+     dict(grid=16, m=1.5, dpl=10, iter="csym")),
+    ("ell_bicg_eps8", ["-iter", "bicg", "-eps", "8"] + ELL + MGN,
+     dict(grid=8, m=1.1 + 0.1j, shape="ellipsoid", pars=(0.5, 1.5), iter="bicg", eps=1e-8)),
+    ("ell_csym_eps8", ["-iter", "csym", "-eps", "8"] + ELL + MGN,
+     dict(grid=8, m=1.1 + 0.1j, shape="ellipsoid", pars=(0.5, 1.5), iter="csym", eps=1e-8)),
 ] + [("grid%d" % g, ["-grid", str(g), "-size", "8"] + M, dict(grid=g, m=1.1 + 0.1j, size=8.0))
      for g in (2, 4, 6, 10, 12, 18, 20, 24, 30, 32)]
 

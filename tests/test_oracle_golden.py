@@ -37,16 +37,20 @@ def test_solve_matches_reference(c):
         ref_hist = np.array(c["resid"][pol])
         assert r["niter"] == len(ref_hist) - 1, (pol, r["niter"], len(ref_hist) - 1)
         # RE_ values are printed with 11 significant digits; rounding differences between two FFT call orders grow
-        # by about 10x per iteration in BiCGStab (QMR_CS is far tamer), so the history is compared until the
-        # residual has dropped by 1e3 and the cross sections with a method-dependent bar
-        early = ref_hist > 1e-3
+        # by about 10x per iteration in BiCGStab and CGNR (QMR_CS, BiCG_CS and CSYM are far tamer: measured, they
+        # follow the reference to 1e-8 over the whole history), so for those two the history is compared while the
+        # residual is above 1e-3 (BiCGStab) or 1e-1 (CGNR, whose first 1e-8 difference appears at 0.05) and the
+        # cross sections with a method-dependent bar
+        it = c["setup"].get("iter", "qmr")
+        early = ref_hist > {"bicgstab": 1e-3, "cgnr": 1e-1}.get(it, 0)
         np.testing.assert_allclose(r["resid"][early], ref_hist[early], rtol=1e-8)
-        np.testing.assert_allclose(r["resid"], ref_hist, rtol=2e-2)
-        bcgs = c["setup"].get("iter") == "bicgstab"
+        np.testing.assert_allclose(r["resid"], ref_hist, rtol=2e-2 if it != "cgnr" else 0.25)
         for q in ("Cext", "Cabs"):
             want = c["cross"][pol][q]
-            if bcgs:
+            if it == "bicgstab":
                 assert abs(r[q] - want) <= max(2e-7 * abs(want), 1e-12), (q, r[q], want)
+            elif it == "cgnr":
+                assert abs(r[q] - want) <= max(1e-8 * abs(want), 1e-12), (q, r[q], want)
             else:
                 assert close10(r[q], want, 1e-12), (q, r[q], want)
     o.close()
