@@ -154,7 +154,10 @@ int IterativeSolver(enum iter method, enum incpol which)
 	memset(&sp, 0, sizeof(sp));
 	if (method == IT_QMR_CS) sp.method = ADDA_ITER_QMR_CS;
 	else if (method == IT_BICGSTAB) sp.method = ADDA_ITER_BICGSTAB;
-	else ERR("The GPU build supports -iter qmr and -iter bicgstab only");
+	else if (method == IT_BICG_CS) sp.method = ADDA_ITER_BICG_CS;
+	else if (method == IT_CGNR) sp.method = ADDA_ITER_CGNR;
+	else if (method == IT_CSYM) sp.method = ADDA_ITER_CSYM;
+	else ERR("The GPU build supports -iter qmr|bicgstab|bicg|cgnr|csym only");
 	if (InitField == IF_AUTO) sp.init_field = ADDA_IF_AUTO;
 	else if (InitField == IF_ZERO) sp.init_field = ADDA_IF_ZERO;
 	else if (InitField == IF_INC) sp.init_field = ADDA_IF_INC;

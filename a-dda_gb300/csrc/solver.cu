@@ -37,8 +37,10 @@ struct RhsState {
 	// QMR_CS
 	double c_old, c_new, om_old, om_new;
 	double2 beta, tautilda, s_old, s_new, alpha, theta, eta, zetat;
-	// BiCGStab
+	// BiCGStab, BiCG_CS (ro, balpha), CGNR (real parts of ro, balpha)
 	double2 ro_old, ro_new, omega, balpha;
+	// CSYM: beta_(k+1) = |w| (real); tau, c, s, theta, eta share the QMR_CS fields, gamma is kept in zetat
+	double cs_beta;
 	// coefficients for the vector kernels
 	double2 k0, k1, k2, k3, kib, kr;
 	double d0;
@@ -399,7 +401,9 @@ __global__ void __launch_bounds__(NT) qmr_v2(const RhsState *st, C *po, const C 
 }
 
 // ProgressReport (iterative.c:282-306) + loop condition (iterative.c:1467); partial |r|^2 in slot 0 unless half
-__global__ void s_progress(RhsState *st, int *done, const double *part, int nbv, double *hist, int hist_cap, int bcgs)
+// mode 0: |r|^2 from partial slot 0; 1: BiCGStab (also the next ro, half-step exit); 2: inprodRp1 already set by the
+// method's scalar kernel (CSYM's |tau|^2)
+__global__ void s_progress(RhsState *st, int *done, const double *part, int nbv, double *hist, int hist_cap, int mode)
 {
 	const int r = blockIdx.x;
 	if (st[r].done) return;
@@ -407,7 +411,8 @@ __global__ void s_progress(RhsState *st, int *done, const double *part, int nbv,
 	sum_part(part, nbv, r, s, 2);
 	if (threadIdx.x) return;
 	RhsState &S = st[r];
-	if (!S.half) S.inprodRp1 = s[0];
+	const bool bcgs = mode == 1;
+	if (!S.half && mode != 2) S.inprodRp1 = s[0];
 	if (bcgs && !S.half) S.ro_old = S.ro_new; // the next bs_s0 sums the r.r~* partials of bs_v3 itself
 	if (S.inprodRp1 <= S.inprodR) {
 		S.inprodR = S.inprodRp1;
@@ -550,6 +555,280 @@ __global__ void __launch_bounds__(NT) bs_v3(const RhsState *st, C *x, const C *p
 		acc_cmulc(s[1], s[2], y, rt[j]);
 	}
 	write_part(part, nbv, s, 3);
+}
+
+// ---------------- BiCG_CS (COCG), iterative.c:490-637 ----------------
+
+// ro_new = r.r (slots 1,2 of the previous r update or of the initial k_dot); breakdown |rT.r|/(r.r) (:559-560);
+// beta = ro_new/ro_old for p = beta*p + r (:566-569)
+__global__ void bg_s0(RhsState *st, int *done, const double *part, int nbv)
+{
+	const int r = blockIdx.x;
+	if (st[r].done) return;
+	double s[4];
+	sum_part(part, nbv, r, s, 3);
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	S.ro_new = dc(s[1], s[2]);
+	if (dabs(S.ro_new) / S.inprodR < 1e-10) {
+		S.status = ADDA_GB300_EBREAKDOWN;
+		S.done = 1;
+		done[r] = 1;
+		return;
+	}
+	S.k0 = (S.niter == 1) ? dc(0, 0) : ddiv(S.ro_new, S.ro_old);
+}
+
+// p = r (first iteration) or p = k0*p + r
+template <typename C> __global__ void __launch_bounds__(NT) bg_v1(const RhsState *st, C *p, const C *rv, size_t n3)
+{
+	const int r = blockIdx.y;
+	if (st[r].done) return;
+	const bool first = st[r].niter == 1;
+	const C k0 = cof<C>(st[r].k0);
+	VLOOP(n3) {
+		const size_t j = r * n3 + i;
+		p[j] = first ? rv[j] : cadd(cmul(k0, p[j]), rv[j]);
+	}
+}
+
+// mu = p.Ap (matvec epilogue slots 1,2); breakdown |pT.A.p|/(rT.r) (:594-595); alpha = ro_new/mu
+__global__ void bg_s1(RhsState *st, int *done, const double *part, size_t nblk)
+{
+	const int r = blockIdx.x;
+	if (st[r].done) return;
+	double s[4];
+	sum_part(part, nblk, r, s, 3);
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	const double2 mu = dc(s[1], s[2]);
+	if (dabs(mu) / dabs(S.ro_new) < 1e-10) {
+		S.status = ADDA_GB300_EBREAKDOWN;
+		S.done = 1;
+		done[r] = 1;
+		return;
+	}
+	S.balpha = ddiv(S.ro_new, mu);
+	S.ro_old = S.ro_new;
+}
+
+// x += alpha*p; r -= alpha*Ap; partials |r|^2 and r.r
+template <typename C>
+__global__ void __launch_bounds__(NT) bg_v2(const RhsState *st, C *x, const C *p, C *rv, const C *Av, size_t n3,
+	double *part, int nbv)
+{
+	const int r = blockIdx.y;
+	if (st[r].done) return;
+	const C a = cof<C>(st[r].balpha), ma = cof<C>(dc(-st[r].balpha.x, -st[r].balpha.y));
+	typename AccOf<C>::T s[4] = {};
+	VLOOP(n3) {
+		const size_t j = r * n3 + i;
+		x[j] = cadd(x[j], cmul(a, p[j]));
+		const C y = cadd(rv[j], cmul(ma, Av[j]));
+		rv[j] = y;
+		acc_abs2(s[0], y);
+		acc_cmul(s[1], s[2], y, y);
+	}
+	write_part(part, nbv, s, 3);
+}
+
+// ---------------- CGNR, iterative.c:729-769 ----------------
+
+// ro_new = |A^H r|^2 (epilogue slot 0 of the her matvec); beta = ro_new/ro_old
+__global__ void cg_s0(RhsState *st, const double *part, size_t nblk)
+{
+	const int r = blockIdx.x;
+	if (st[r].done) return;
+	double s[4];
+	sum_part(part, nblk, r, s, 1);
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	S.ro_new = dc(s[0], 0);
+	S.k0 = dc(S.niter == 1 ? 0 : s[0] / S.ro_old.x, 0);
+}
+
+// p = A^H r (first iteration) or p = beta*p + A^H r
+template <typename C> __global__ void __launch_bounds__(NT) cg_v1(const RhsState *st, C *p, const C *ahr, size_t n3)
+{
+	const int r = blockIdx.y;
+	if (st[r].done) return;
+	const bool first = st[r].niter == 1;
+	const auto beta = rof<C>(st[r].k0.x);
+	VLOOP(n3) {
+		const size_t j = r * n3 + i;
+		p[j] = first ? ahr[j] : cadd(cscale(p[j], beta), ahr[j]);
+	}
+}
+
+// alpha = ro_new / |A.p|^2 (epilogue slot 0)
+__global__ void cg_s1(RhsState *st, const double *part, size_t nblk)
+{
+	const int r = blockIdx.x;
+	if (st[r].done) return;
+	double s[4];
+	sum_part(part, nblk, r, s, 1);
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	S.balpha = dc(S.ro_new.x / s[0], 0);
+	S.ro_old = S.ro_new;
+}
+
+// x += alpha*p; r -= alpha*Ap (real alpha); partial |r|^2
+template <typename C>
+__global__ void __launch_bounds__(NT) cg_v2(const RhsState *st, C *x, const C *p, C *rv, const C *Av, size_t n3,
+	double *part, int nbv)
+{
+	const int r = blockIdx.y;
+	if (st[r].done) return;
+	const auto a = rof<C>(st[r].balpha.x), ma = rof<C>(-st[r].balpha.x);
+	typename AccOf<C>::T s[4] = {};
+	VLOOP(n3) {
+		const size_t j = r * n3 + i;
+		x[j] = cadd(x[j], cscale(p[j], a));
+		const C y = cadd(rv[j], cscale(Av[j], ma));
+		rv[j] = y;
+		acc_abs2(s[0], y);
+	}
+	write_part(part, nbv, s, 1);
+}
+
+// ---------------- CSYM, iterative.c:773-892 ----------------
+
+// PHASE_INIT: tau = |r_0|, c_0 = 1, c_-1 = 0, s_0 = s_-1 = 0; q_1 = r_0(*)/tau (cs_init_v)
+__global__ void cs_init_s(RhsState *st)
+{
+	const int r = blockIdx.x;
+	if (threadIdx.x || st[r].done) return;
+	RhsState &S = st[r];
+	const double tau = sqrt(S.inprodR);
+	S.tautilda = dc(tau, 0);
+	S.kib = dc(1 / tau, 0);
+	S.c_new = 1;
+	S.c_old = 0;
+	S.s_new = S.s_old = dc(0, 0);
+	S.cs_beta = 0;
+}
+
+// a = conj(a) * kib.x (nMultSelf_conj)
+template <typename C> __global__ void __launch_bounds__(NT) cs_conj_scale(const RhsState *st, C *a, size_t n3)
+{
+	const int r = blockIdx.y;
+	if (st[r].done) return;
+	const auto k = rof<C>(st[r].kib.x);
+	VLOOP(n3) {
+		const size_t j = r * n3 + i;
+		a[j] = cscale(cconj(a[j]), k);
+	}
+}
+
+// alpha = q.Aq (epilogue slots 1,2); eta, gamma, theta (:819-824); w coefficients k0 = -alpha, k1 = -beta
+__global__ void cs_s1(RhsState *st, const double *part, size_t nblk)
+{
+	const int r = blockIdx.x;
+	if (st[r].done) return;
+	double s[4];
+	sum_part(part, nblk, r, s, 3);
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	const double2 alpha = dc(s[1], s[2]);
+	const double beta = S.cs_beta;
+	S.eta = dadd(dc(S.c_old * S.c_new * beta, 0), dmul(alpha, dconj(S.s_new)));
+	S.zetat = dsub(dscal(alpha, S.c_new), dscal(S.s_new, S.c_old * beta)); // gamma
+	S.theta = dscal(dconj(S.s_old), beta);
+	S.k0 = dc(-alpha.x, -alpha.y);
+	S.k1 = dc(-beta, 0);
+}
+
+// w = -beta*q_old(*) - alpha*q_new(*) + Aq (q_0 = 0 in the first iteration), stored in q_old; partial |w|^2
+template <typename C>
+__global__ void __launch_bounds__(NT) cs_v1(const RhsState *st, C *qo, const C *qn, const C *Av, size_t n3, double *part,
+	int nbv)
+{
+	const int r = blockIdx.y;
+	if (st[r].done) return;
+	const bool first = st[r].niter == 1;
+	const C k0 = cof<C>(st[r].k0);
+	const auto k1 = rof<C>(st[r].k1.x);
+	typename AccOf<C>::T s[4] = {};
+	VLOOP(n3) {
+		const size_t j = r * n3 + i;
+		C w = cadd(cmul(k0, cconj(qn[j])), Av[j]);
+		if (!first) w = cadd(cscale(cconj(qo[j]), k1), w);
+		qo[j] = w;
+		acc_abs2(s[0], w);
+	}
+	write_part(part, nbv, s, 1);
+}
+
+// beta_(k+1) = |w|; Givens rotation c_k, s_k, 1/ksi_k (:832-862); p and x coefficients; tau_(k+1) = -s_k*tau_k and
+// |r_k| = |tau_(k+1)|
+__global__ void cs_s2(RhsState *st, int *done, const double *part, int nbv)
+{
+	const int r = blockIdx.x;
+	if (st[r].done) return;
+	double s[4];
+	sum_part(part, nbv, r, s, 1);
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	const double beta = sqrt(s[0]);
+	S.cs_beta = beta;
+	S.c_old = S.c_new;
+	S.s_old = S.s_new;
+	const double2 gamma = S.zetat;
+	double g = dabs(gamma);
+	double2 invksi;
+	if (g == 0) {
+		if (beta == 0) { // singular interaction matrix (iterative.c:845)
+			S.status = ADDA_GB300_EBREAKDOWN;
+			S.done = 1;
+			done[r] = 1;
+			return;
+		}
+		S.c_new = 0;
+		S.s_new = dc(1, 0);
+		invksi = dc(1 / beta, 0);
+	}
+	else {
+		if (g < beta) {
+			g = g / beta;
+			S.c_new = g / sqrt(1 + g * g);
+		}
+		else {
+			g = beta / g;
+			S.c_new = 1 / sqrt(1 + g * g);
+		}
+		invksi = ddiv(dc(S.c_new, 0), gamma);
+		S.s_new = dscal(invksi, beta);
+	}
+	// p_out = k2*p_old + k1*p_new + k3*q_new (terms absent in the first two iterations); x += kr*p_out
+	S.k3 = invksi;
+	S.k1 = (S.niter >= 2) ? dmul(dc(-S.eta.x, -S.eta.y), invksi) : dc(0, 0);
+	S.k2 = (S.niter >= 3) ? dmul(dc(-S.theta.x, -S.theta.y), invksi) : dc(0, 0);
+	S.kr = dscal(S.tautilda, S.c_new);
+	S.kib = dc(1 / beta, 0);
+	S.tautilda = dmul(dc(-S.s_new.x, -S.s_new.y), S.tautilda);
+	S.inprodRp1 = S.tautilda.x * S.tautilda.x + S.tautilda.y * S.tautilda.y;
+}
+
+// p_out (into the p_old buffer) = k2*p_old + k1*p_new + k3*q_new; x += kr*p_out; q_old = w(*)/beta
+template <typename C>
+__global__ void __launch_bounds__(NT) cs_v2(const RhsState *st, C *po, const C *pn, const C *qn, C *qo, C *x, size_t n3)
+{
+	const int r = blockIdx.y;
+	if (st[r].done) return;
+	const RhsState &S = st[r];
+	const int it = S.niter;
+	const C k1 = cof<C>(S.k1), k2 = cof<C>(S.k2), k3 = cof<C>(S.k3), kr = cof<C>(S.kr);
+	const auto kib = rof<C>(S.kib.x);
+	VLOOP(n3) {
+		const size_t j = r * n3 + i;
+		C pv = cmul(k3, qn[j]);
+		if (it >= 2) pv = cadd(cmul(k1, pn[j]), pv);
+		if (it >= 3) pv = cadd(cmul(k2, po[j]), pv);
+		po[j] = pv;
+		x[j] = cadd(x[j], cmul(kr, pv));
+		qo[j] = cscale(cconj(qo[j]), kib);
+	}
 }
 
 // ---------------- FP64 helpers for the refinement loop and the results ----------------
@@ -771,6 +1050,11 @@ template <typename C> static KV<C> kvec(SolverWork *w)
 	return k;
 }
 
+static int matvecs_per_iter(int method)
+{
+	return (method == ADDA_ITER_BICGSTAB || method == ADDA_ITER_CGNR) ? 2 : 1;
+}
+
 // enqueue one Krylov iteration; parity selects the QMR_CS vector roles (v<->v~, p_new<->p_old swap each iteration).
 // T = matvec arithmetic, C = complex type of the Krylov vectors.
 template <typename T, typename C>
@@ -797,6 +1081,53 @@ static int enqueue_iter(adda_gb300_ctx *c, SolverWork *w, int method, int R, int
 		qmr_v2<C><<<gv, NT, 0, s>>>(w->st, po, pn, v, vt, k.x, k.r, n3, w->vpart, w->nbv);
 		ADDA_LAUNCHED();
 		s_progress<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv, w->hist, w->hist_cap, 0);
+		ADDA_LAUNCHED();
+	}
+	else if (method == ADDA_ITER_BICG_CS) {
+		bg_s0<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+		bg_v1<C><<<gv, NT, 0, s>>>(w->st, k.p, k.r, n3);
+		ADDA_LAUNCHED();
+		MvEpi e{EPI_DOT_ARG, nullptr, c->partial};
+		if ((rc = matvec_run<T>(c, R, k.p, k.Av, 0, e, w->done))) return rc;
+		bg_s1<<<R, NT, 0, s>>>(w->st, w->done, c->partial, nblk);
+		ADDA_LAUNCHED();
+		bg_v2<C><<<gv, NT, 0, s>>>(w->st, k.x, k.p, k.r, k.Av, n3, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+		s_progress<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv, w->hist, w->hist_cap, 0);
+		ADDA_LAUNCHED();
+	}
+	else if (method == ADDA_ITER_CGNR) {
+		MvEpi e1{EPI_NORM, nullptr, c->partial};
+		if ((rc = matvec_run<T>(c, R, k.r, k.Av, 1, e1, w->done))) return rc; // A^H r
+		cg_s0<<<R, NT, 0, s>>>(w->st, c->partial, nblk);
+		ADDA_LAUNCHED();
+		cg_v1<C><<<gv, NT, 0, s>>>(w->st, k.p, k.Av, n3);
+		ADDA_LAUNCHED();
+		MvEpi e2{EPI_NORM, nullptr, c->partial};
+		if ((rc = matvec_run<T>(c, R, k.p, k.Av, 0, e2, w->done))) return rc;
+		cg_s1<<<R, NT, 0, s>>>(w->st, c->partial, nblk);
+		ADDA_LAUNCHED();
+		cg_v2<C><<<gv, NT, 0, s>>>(w->st, k.x, k.p, k.r, k.Av, n3, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+		s_progress<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv, w->hist, w->hist_cap, 0);
+		ADDA_LAUNCHED();
+	}
+	else if (method == ADDA_ITER_CSYM) {
+		// q_k and p_k swap buffers every iteration (q in r/v1, p in p/v2)
+		C *qn = parity ? k.v1 : k.r, *qo = parity ? k.r : k.v1;
+		C *pn = parity ? k.v2 : k.p, *po = parity ? k.p : k.v2;
+		MvEpi e{EPI_DOT_ARG, nullptr, c->partial};
+		if ((rc = matvec_run<T>(c, R, qn, k.Av, 0, e, w->done))) return rc;
+		cs_s1<<<R, NT, 0, s>>>(w->st, c->partial, nblk);
+		ADDA_LAUNCHED();
+		cs_v1<C><<<gv, NT, 0, s>>>(w->st, qo, qn, k.Av, n3, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+		cs_s2<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+		cs_v2<C><<<gv, NT, 0, s>>>(w->st, po, pn, qn, qo, k.x, n3);
+		ADDA_LAUNCHED();
+		s_progress<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv, w->hist, w->hist_cap, 2);
 		ADDA_LAUNCHED();
 	}
 	else {
@@ -845,11 +1176,23 @@ static int krylov(adda_gb300_ctx *c, SolverWork *w, int method, int R, int K, un
 		qmr_v_init<C><<<gv, NT, 0, s>>>(w->st, k.v1, k.r, n3);
 		ADDA_LAUNCHED();
 	}
-	else {
+	else if (method == ADDA_ITER_BICGSTAB) {
 		k_copy<C><<<gv, NT, 0, s>>>(k.v3, k.r, n3, nullptr);
 		ADDA_LAUNCHED();
 		// r.r~* for the first iteration's bs_s0 (slots 1,2)
 		k_dot<C><<<gv, NT, 0, s>>>(k.r, k.v3, n3, 1, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+	}
+	else if (method == ADDA_ITER_BICG_CS) {
+		// r.r for the first iteration's bg_s0 (slots 1,2)
+		k_dot<C><<<gv, NT, 0, s>>>(k.r, k.r, n3, 0, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+	}
+	else if (method == ADDA_ITER_CSYM) {
+		// tau_1 = |r_0|, q_1 = r_0(*)/tau_1 in place (r is q_1)
+		cs_init_s<<<R, 32, 0, s>>>(w->st);
+		ADDA_LAUNCHED();
+		cs_conj_scale<C><<<gv, NT, 0, s>>>(w->st, k.r, n3);
 		ADDA_LAUNCHED();
 	}
 	// graph of K iterations (K even keeps the QMR_CS roles periodic)
@@ -999,7 +1342,7 @@ static int solve_mixed(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int
 			for (int r = 0; r < R; r++) {
 				if (odone[r]) continue;
 				iters[r] += hs[r].niter - 1;
-				nmv32[r] += (sp->method == ADDA_ITER_BICGSTAB ? 2 : 1) * (hs[r].niter - 1) + (zero ? 0 : 1);
+				nmv32[r] += matvecs_per_iter(sp->method) * (hs[r].niter - 1) + (zero ? 0 : 1);
 				if (hs[r].status) status[r] = hs[r].status;
 				nref[r]++;
 			}
@@ -1042,7 +1385,7 @@ static int solve_mixed(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int
 
 static int check_params(const adda_gb300_solve_params *sp)
 {
-	if ((sp->method != ADDA_ITER_QMR_CS && sp->method != ADDA_ITER_BICGSTAB) ||
+	if (sp->method < ADDA_ITER_QMR_CS || sp->method > ADDA_ITER_CSYM ||
 		(sp->precision != ADDA_PREC_FP64 && sp->precision != ADDA_PREC_MIXED &&
 			sp->precision != ADDA_PREC_MIXED_F32VEC && sp->precision != ADDA_PREC_MIXED_F64VEC) || !(sp->eps > 0) || sp->maxiter < 0 ||
 		(sp->init_field != ADDA_IF_AUTO && sp->init_field != ADDA_IF_ZERO && sp->init_field != ADDA_IF_INC)) {
@@ -1084,7 +1427,9 @@ static int solve_core_impl(adda_gb300_ctx *c, const adda_gb300_solve_params *sp,
 	const size_t n3 = w->n3;
 	cudaStream_t s = c->stream;
 	const dim3 gv(w->nbv, R);
-	const int mc = (sp->method == ADDA_ITER_BICGSTAB) ? 30000 : 50000; // iterative.c:118-125
+	// stagnation limits per method (iterative.c:118-125)
+	const int mc = (sp->method == ADDA_ITER_BICGSTAB) ? 30000
+		: (sp->method == ADDA_ITER_CGNR || sp->method == ADDA_ITER_CSYM) ? 10 : 50000;
 	int K = sp->check_every > 0 ? sp->check_every : 8;
 	if (K % 2) K++;
 	std::vector<adda_gb300_rhs_stats> st(R);
@@ -1128,7 +1473,7 @@ static int solve_core_impl(adda_gb300_ctx *c, const adda_gb300_solve_params *sp,
 			if (!st[r].status && hs[r].inprodR > hs[r].epsB)
 				st[r].status = (hs[r].niter > hs[r].maxiter) ? ADDA_GB300_EMAXITER : ADDA_GB300_ESTAGNATION;
 			st[r].resid = sqrt(hs[r].resid_scale * hs[r].inprodR);
-			const int mpi = sp->method == ADDA_ITER_BICGSTAB ? 2 : 1;
+			const int mpi = matvecs_per_iter(sp->method);
 			st[r].matvecs_fp64 = (zero ? 0 : 1) + mpi * st[r].niter;
 		}
 	}

@@ -125,7 +125,8 @@ def test_matvec_per_dipole_cc():
 
 SOLVE_CASES = ["c1_qmr", "c1_bicgstab", "mgn", "mgn_eps10", "mgn_init_zero", "mgn_init_inc", "mgn_bicgstab",
                "mgn_maxiter3", "ell_orient", "pol_ldr_prop", "prop_ell", "ell24", "box12", "grid6", "grid18",
-               "sample_default", "c2_small"]
+               "sample_default", "c2_small", "mgn_bicg", "mgn_cgnr", "mgn_csym", "c1_bicg", "c1_cgnr", "c1_csym",
+               "ell_bicg_eps8", "ell_csym_eps8"]
 
 
 @pytest.mark.parametrize("name", SOLVE_CASES)
@@ -150,7 +151,10 @@ def test_solve_fp64_vs_reference(name):
             assert st["status"] == "ok"
             assert st["resid"] <= opts["eps"]
         h = res["hist"][r][: st["niter"] + 1]
-        early = ref_hist[: len(h)] > 1e-2
+        # CGNR and CSYM amplify rounding differences between two FFT call orders from a residual of ~5e-2 on
+        # (measured: CGNR oracle vs reference, CSYM GPU vs reference on c1 at iteration 28; both still end within
+        # 6 iterations and 2e-6 in the cross sections, and match the oracle at eps=1e-10)
+        early = ref_hist[: len(h)] > (1e-1 if opts["method"] in ("cgnr", "csym") else 1e-2)
         np.testing.assert_allclose(h[: len(ref_hist)][early], ref_hist[: len(h)][early], rtol=1e-7)
         tol = 1e-9 if tight else 2e-6
         for q, v in (("Cext", ce[r]), ("Cabs", ca[r])):
@@ -158,7 +162,7 @@ def test_solve_fp64_vs_reference(name):
             assert abs(v - want) <= max(tol * abs(want), 1e-12), (pol, q, v, want)
 
 
-@pytest.mark.parametrize("method", ["qmr", "bicgstab"])
+@pytest.mark.parametrize("method", ["qmr", "bicgstab", "bicg", "cgnr", "csym"])
 def test_solve_fp64_vs_oracle_tight(method):
     """at eps=1e-10 the GPU FP64 solve and the oracle agree on Cext/Cabs to 1e-9 and per dipole to 1e-8"""
     import adda_gb300 as A
@@ -197,6 +201,25 @@ def test_solve_mixed(name, method, prec):
         assert abs(ce[r] / rc["Cext"] - 1) < 2e-6, (ce[r], rc["Cext"])
         assert abs(ca[r] - rc["Cabs"]) < 2e-6 * max(abs(rc["Cabs"]), abs(rc["Cext"]))
         assert abs(ce[r] / ro["Cext"] - 1) < 3e-6, (ce[r], ro["Cext"])
+
+
+@pytest.mark.parametrize("method", ["bicg", "cgnr", "csym"])
+@pytest.mark.parametrize("name", ["c1_qmr", "ell24"])
+def test_solve_mixed_other_methods(name, method):
+    """BiCG_CS, CGNR and CSYM in mixed precision (double-float vectors): FP64 residual meets eps, cross sections within
+    2e-6 of the converged FP64 oracle"""
+    import adda_gb300 as A
+    s = setup_for(case(name)["setup"])
+    o = oracle_for(s)
+    ctx = A.Context.from_setup(s, nrhs_max=2)
+    res = ctx.solve(np.stack(s.einc), method=method, prec="mixed", eps=1e-5)
+    ce, ca = ctx.cross_sections(np.stack([s.prop, s.prop]), np.stack(s.incpol))
+    for r in range(2):
+        st = res["stats"][r]
+        assert st["status"] == "ok" and st["resid"] <= 1e-5, st
+        rc = oracle_solve(o, s, r, method="qmr", eps=1e-10)
+        assert abs(ce[r] / rc["Cext"] - 1) < 2e-6, (ce[r], rc["Cext"])
+        assert abs(ca[r] - rc["Cabs"]) < 2e-6 * max(abs(rc["Cabs"]), abs(rc["Cext"]))
 
 
 def test_cross_sections_from_pvec():
