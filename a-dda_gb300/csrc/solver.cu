@@ -41,6 +41,9 @@ struct RhsState {
 	double2 ro_old, ro_new, omega, balpha;
 	// CSYM: beta_(k+1) = |w| (real); tau, c, s, theta, eta share the QMR_CS fields, gamma is kept in zetat
 	double cs_beta;
+	// QMR_CS_2: ro_k, theta_(k-1), c_(k-1); eps_(k-1), eta_(k-1), beta_k; delta_k = v_k.v_k
+	double q2_ro, q2_theta, q2_c;
+	double2 q2_eps, q2_eta, q2_beta, q2_delta;
 	// coefficients for the vector kernels
 	double2 k0, k1, k2, k3, kib, kr;
 	double d0;
@@ -831,6 +834,146 @@ __global__ void __launch_bounds__(NT) cs_v2(const RhsState *st, C *po, const C *
 	}
 }
 
+// ---------------- QMR_CS_2, iterative.c:1038-1132 ----------------
+
+// PHASE_INIT: ro_1 = |r_0|, v~_1 = r_0 (copied by the caller), c_0 = eps_0 = 1, theta_0 = 0, eta_0 = -1; delta_1 from
+// the r.r partials (slots 1,2 of k_dot) as (r.r)/ro_1^2, i.e. v_1.v_1 with v_1 = v~_1/ro_1
+__global__ void q2_init_s(RhsState *st, const double *part, int nbv)
+{
+	const int r = blockIdx.x;
+	double s[4];
+	sum_part(part, nbv, r, s, 3);
+	if (threadIdx.x || st[r].done) return;
+	RhsState &S = st[r];
+	S.q2_ro = sqrt(S.inprodR);
+	S.q2_c = 1;
+	S.q2_eps = dc(1, 0);
+	S.q2_theta = 0;
+	S.q2_eta = dc(-1, 0);
+	S.q2_delta = dscal(dc(s[1], s[2]), 1 / S.inprodR);
+}
+
+// delta_k test (:1086-1089); p coefficient -ro_k*delta_k/eps_(k-1) (:1091-1094); v scale 1/ro_k
+__global__ void q2_s0(RhsState *st, int *done)
+{
+	const int r = blockIdx.x;
+	if (threadIdx.x || st[r].done) return;
+	RhsState &S = st[r];
+	if (dabs(S.q2_delta) < 1e-10) {
+		S.status = ADDA_GB300_EBREAKDOWN;
+		S.done = 1;
+		done[r] = 1;
+		return;
+	}
+	S.kib = dc(1 / S.q2_ro, 0);
+	S.k0 = (S.niter == 1) ? dc(0, 0) : dscal(ddiv(S.q2_delta, S.q2_eps), -S.q2_ro);
+}
+
+// v = v~/ro_k; p = v (first iteration) or p = k0*p + v
+template <typename C> __global__ void __launch_bounds__(NT) q2_v1(const RhsState *st, C *v, C *p, size_t n3)
+{
+	const int r = blockIdx.y;
+	if (st[r].done) return;
+	const bool first = st[r].niter == 1;
+	const auto ir = rof<C>(st[r].kib.x);
+	const C k0 = cof<C>(st[r].k0);
+	VLOOP(n3) {
+		const size_t j = r * n3 + i;
+		const C vv = cscale(v[j], ir);
+		v[j] = vv;
+		p[j] = first ? vv : cadd(cmul(k0, p[j]), vv);
+	}
+}
+
+// eps_k = p.Ap (epilogue slots 1,2); beta_k = eps_k/delta_k; test |eps_k| (:1104-1107)
+__global__ void q2_s1(RhsState *st, int *done, const double *part, size_t nblk)
+{
+	const int r = blockIdx.x;
+	if (st[r].done) return;
+	double s[4];
+	sum_part(part, nblk, r, s, 3);
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	S.q2_eps = dc(s[1], s[2]);
+	S.q2_beta = ddiv(S.q2_eps, S.q2_delta);
+	if (dabs(S.q2_eps) < 1e-10) {
+		S.status = ADDA_GB300_EBREAKDOWN;
+		S.done = 1;
+		done[r] = 1;
+		return;
+	}
+	S.k1 = dc(-S.q2_beta.x, -S.q2_beta.y);
+}
+
+// v~_(k+1) = A.p_k - beta_k*v_k (in place); partials |v~|^2 and v~.v~
+template <typename C>
+__global__ void __launch_bounds__(NT) q2_v2(const RhsState *st, C *v, const C *Av, size_t n3, double *part, int nbv)
+{
+	const int r = blockIdx.y;
+	if (st[r].done) return;
+	const C k1 = cof<C>(st[r].k1);
+	typename AccOf<C>::T s[4] = {};
+	VLOOP(n3) {
+		const size_t j = r * n3 + i;
+		const C y = cadd(cmul(k1, v[j]), Av[j]);
+		v[j] = y;
+		acc_abs2(s[0], y);
+		acc_cmul(s[1], s[2], y, y);
+	}
+	write_part(part, nbv, s, 3);
+}
+
+// ro_(k+1) = |v~_(k+1)|; theta_k, c_k, |s_k|^2, eta_k (:1111-1120); coefficients of d, x, r; delta_(k+1)
+__global__ void q2_s2(RhsState *st, const double *part, int nbv)
+{
+	const int r = blockIdx.x;
+	if (st[r].done) return;
+	double s[4];
+	sum_part(part, nbv, r, s, 3);
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	const double ro_new = sqrt(s[0]);
+	const double theta_new = ro_new / (S.q2_c * dabs(S.q2_beta));
+	const double th2 = theta_new * theta_new;
+	const double c_new = 1 / sqrt(1 + th2);
+	const double sabs2 = th2 / (1 + th2);
+	const double cr = c_new / S.q2_c;
+	S.q2_eta = ddiv(dscal(S.q2_eta, -S.q2_ro * cr * cr), S.q2_beta);
+	const double tc = S.q2_theta * c_new;
+	S.d0 = (S.niter == 1) ? 0 : tc * tc; // d = d0*d + eta*p
+	S.k2 = S.q2_eta;
+	S.kr = dc(-S.q2_eta.x, -S.q2_eta.y); // r = sabs2*r - eta*v~
+	S.k3 = dc(sabs2, 0);
+	S.q2_delta = dscal(dc(s[1], s[2]), 1 / s[0]); // v_(k+1).v_(k+1) with v_(k+1) = v~_(k+1)/ro_(k+1)
+	S.q2_ro = ro_new;
+	S.q2_theta = theta_new;
+	S.q2_c = c_new;
+}
+
+// d = eta*p (first iteration) or d0*d + eta*p; x += d; r = sabs2*r - eta*v~; partial |r|^2
+template <typename C>
+__global__ void __launch_bounds__(NT) q2_v3(const RhsState *st, C *d, const C *p, C *x, C *rv, const C *v, size_t n3,
+	double *part, int nbv)
+{
+	const int r = blockIdx.y;
+	if (st[r].done) return;
+	const RhsState &S = st[r];
+	const bool first = S.niter == 1;
+	const C eta = cof<C>(S.k2), me = cof<C>(S.kr);
+	const auto d0 = rof<C>(S.d0), sa = rof<C>(S.k3.x);
+	typename AccOf<C>::T s[4] = {};
+	VLOOP(n3) {
+		const size_t j = r * n3 + i;
+		const C dv = first ? cmul(eta, p[j]) : cadd(cscale(d[j], d0), cmul(eta, p[j]));
+		d[j] = dv;
+		x[j] = cadd(x[j], dv);
+		const C y = cadd(cscale(rv[j], sa), cmul(me, v[j]));
+		rv[j] = y;
+		acc_abs2(s[0], y);
+	}
+	write_part(part, nbv, s, 1);
+}
+
 // ---------------- FP64 helpers for the refinement loop and the results ----------------
 
 // x64 (+)= d (float or double), depending on accumulate
@@ -1113,6 +1256,25 @@ static int enqueue_iter(adda_gb300_ctx *c, SolverWork *w, int method, int R, int
 		s_progress<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv, w->hist, w->hist_cap, 0);
 		ADDA_LAUNCHED();
 	}
+	else if (method == ADDA_ITER_QMR_CS_2) {
+		// v in v1, d in v2
+		q2_s0<<<R, 32, 0, s>>>(w->st, w->done);
+		ADDA_LAUNCHED();
+		q2_v1<C><<<gv, NT, 0, s>>>(w->st, k.v1, k.p, n3);
+		ADDA_LAUNCHED();
+		MvEpi e{EPI_DOT_ARG, nullptr, c->partial};
+		if ((rc = matvec_run<T>(c, R, k.p, k.Av, 0, e, w->done))) return rc;
+		q2_s1<<<R, NT, 0, s>>>(w->st, w->done, c->partial, nblk);
+		ADDA_LAUNCHED();
+		q2_v2<C><<<gv, NT, 0, s>>>(w->st, k.v1, k.Av, n3, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+		q2_s2<<<R, NT, 0, s>>>(w->st, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+		q2_v3<C><<<gv, NT, 0, s>>>(w->st, k.v2, k.p, k.x, k.r, k.v1, n3, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+		s_progress<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv, w->hist, w->hist_cap, 0);
+		ADDA_LAUNCHED();
+	}
 	else if (method == ADDA_ITER_CSYM) {
 		// q_k and p_k swap buffers every iteration (q in r/v1, p in p/v2)
 		C *qn = parity ? k.v1 : k.r, *qo = parity ? k.r : k.v1;
@@ -1186,6 +1348,14 @@ static int krylov(adda_gb300_ctx *c, SolverWork *w, int method, int R, int K, un
 	else if (method == ADDA_ITER_BICG_CS) {
 		// r.r for the first iteration's bg_s0 (slots 1,2)
 		k_dot<C><<<gv, NT, 0, s>>>(k.r, k.r, n3, 0, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+	}
+	else if (method == ADDA_ITER_QMR_CS_2) {
+		k_copy<C><<<gv, NT, 0, s>>>(k.v1, k.r, n3, nullptr);
+		ADDA_LAUNCHED();
+		k_dot<C><<<gv, NT, 0, s>>>(k.r, k.r, n3, 0, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+		q2_init_s<<<R, NT, 0, s>>>(w->st, w->vpart, w->nbv);
 		ADDA_LAUNCHED();
 	}
 	else if (method == ADDA_ITER_CSYM) {
@@ -1385,7 +1555,7 @@ static int solve_mixed(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int
 
 static int check_params(const adda_gb300_solve_params *sp)
 {
-	if (sp->method < ADDA_ITER_QMR_CS || sp->method > ADDA_ITER_CSYM ||
+	if (sp->method < ADDA_ITER_QMR_CS || sp->method > ADDA_ITER_QMR_CS_2 ||
 		(sp->precision != ADDA_PREC_FP64 && sp->precision != ADDA_PREC_MIXED &&
 			sp->precision != ADDA_PREC_MIXED_F32VEC && sp->precision != ADDA_PREC_MIXED_F64VEC) || !(sp->eps > 0) || sp->maxiter < 0 ||
 		(sp->init_field != ADDA_IF_AUTO && sp->init_field != ADDA_IF_ZERO && sp->init_field != ADDA_IF_INC)) {

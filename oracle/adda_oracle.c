@@ -612,6 +612,74 @@ static int csym_iter(solver *s, csym_state *q)
 	return OR_OK;
 }
 
+/* QMR_CS_2 (Freund & Nachtigal coupled two-term recurrences), src/iterative.c:1038-1132; v in v1, d in v2 */
+typedef struct {
+	double c_old, theta_old, ro_old;
+	cplx eps, eta;
+} qmr2_state;
+
+static void qmr2_init(solver *s, qmr2_state *q)
+{
+	q->ro_old = sqrt(s->inprodR);
+	memcpy(s->v1, s->r, sizeof(cplx) * s->n);
+	q->c_old = 1;
+	q->eps = 1;
+	q->theta_old = 0;
+	q->eta = -1;
+}
+
+static int qmr2_iter(solver *s, qmr2_state *q)
+{
+	const size_t n = s->n;
+	cplx *v = s->v1, *d = s->v2;
+	const double iro = 1 / q->ro_old;
+	for (size_t i = 0; i < n; i++) v[i] *= iro;
+	cplx delta = ndot_conj(v, v, n);
+	if (cabs(delta) < 1e-10) return OR_EBREAKDOWN;
+	if (s->niter == 1) memcpy(s->p, v, sizeof(cplx) * n);
+	else {
+		cplx t = -q->ro_old * delta / q->eps;
+		for (size_t i = 0; i < n; i++) s->p[i] = t * s->p[i] + v[i];
+	}
+	if (s->niter == 1 && s->matvec_ready)
+		for (size_t i = 0; i < n; i++) s->Av[i] *= iro;
+	else mv(s, s->p, s->Av, NULL);
+	q->eps = ndot_conj(s->p, s->Av, n);
+	cplx beta = q->eps / delta;
+	if (cabs(q->eps) < 1e-10) return OR_EBREAKDOWN;
+	cplx mb = -beta;
+	double dt = 0;
+	for (size_t i = 0; i < n; i++) {
+		v[i] = mb * v[i] + s->Av[i];
+		dt += creal(v[i]) * creal(v[i]) + cimag(v[i]) * cimag(v[i]);
+	}
+	const double ro_new = sqrt(dt);
+	const double theta_new = ro_new / (q->c_old * cabs(beta));
+	const double th2 = theta_new * theta_new;
+	const double c_new = 1 / sqrt(1 + th2);
+	const double sabs2 = th2 / (1 + th2);
+	const double cr = c_new / q->c_old;
+	q->eta = -q->ro_old * cr * cr * q->eta / beta;
+	if (s->niter == 1)
+		for (size_t i = 0; i < n; i++) d[i] = q->eta * s->p[i];
+	else {
+		const double tc = q->theta_old * c_new, tc2 = tc * tc;
+		for (size_t i = 0; i < n; i++) d[i] = tc2 * d[i] + q->eta * s->p[i];
+	}
+	for (size_t i = 0; i < n; i++) s->x[i] += d[i];
+	cplx me = -q->eta;
+	double sum = 0;
+	for (size_t i = 0; i < n; i++) {
+		s->r[i] = sabs2 * s->r[i] + me * v[i];
+		sum += creal(s->r[i]) * creal(s->r[i]) + cimag(s->r[i]) * cimag(s->r[i]);
+	}
+	s->inprodRp1 = sum;
+	q->ro_old = ro_new;
+	q->theta_old = theta_new;
+	q->c_old = c_new;
+	return OR_OK;
+}
+
 /* IterativeSolver, src/iterative.c:1398-1530 with CalcInitField (:1342-1394) and ProgressReport (:282-318).
  * einc: incident field [N][3]; xvec receives x, pvec the polarisations S.x; resid_hist[0..] the relative residuals
  * RE_000, RE_001, ... (at most hist_cap values). Returns a status code; *niter_out = iterations performed. */
@@ -668,6 +736,7 @@ int or_solve(or_ctx *c, int method, const double *einc, double eps, int maxiter,
 	qmr_state q;
 	bcgs_state bs;
 	csym_state cs;
+	qmr2_state q2;
 	cplx ro_c = 0;
 	double ro_d = 0;
 	if (method == OR_QMR_CS) qmr_init(&S, &q);
@@ -676,6 +745,7 @@ int or_solve(or_ctx *c, int method, const double *einc, double eps, int maxiter,
 		memcpy(bs.rt, S.r, sizeof(cplx) * n);
 	}
 	else if (method == OR_CSYM) csym_init(&S, &cs);
+	else if (method == OR_QMR_CS_2) qmr2_init(&S, &q2);
 	int status = OR_OK;
 	while (S.inprodR > S.epsB && S.niter <= maxiter && S.counter <= mcm) {
 		S.complete = 1;
@@ -684,6 +754,7 @@ int or_solve(or_ctx *c, int method, const double *einc, double eps, int maxiter,
 			case OR_BICGSTAB: status = bcgs_iter(&S, &bs); break;
 			case OR_BICG_CS: status = bicg_iter(&S, &ro_c); break;
 			case OR_CGNR: status = cgnr_iter(&S, &ro_d); break;
+			case OR_QMR_CS_2: status = qmr2_iter(&S, &q2); break;
 			default: status = csym_iter(&S, &cs); break;
 		}
 		if (status != OR_OK) break;

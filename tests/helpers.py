@@ -44,7 +44,8 @@ def oracle_for(s, nthreads=0):
 def oracle_solve(o, s, pol_index, method="qmr", eps=1e-5, maxiter=100000, init="auto"):
     from oracle import oracle as O
     o.set_cc(s.cc[pol_index].reshape(1, 3))
-    methods = {"qmr": O.QMR_CS, "bicgstab": O.BICGSTAB, "bicg": O.BICG_CS, "cgnr": O.CGNR, "csym": O.CSYM}
+    methods = {"qmr": O.QMR_CS, "bicgstab": O.BICGSTAB, "bicg": O.BICG_CS, "cgnr": O.CGNR, "csym": O.CSYM,
+               "qmr2": O.QMR_CS_2}
     r = o.solve(s.einc[pol_index], method=methods[method], eps=eps, maxiter=maxiter,
                 init_field={"auto": O.IF_AUTO, "zero": O.IF_ZERO, "inc": O.IF_INC}[init])
     ce, ca = o.cross(r["p"], s.prop, s.incpol[pol_index])
