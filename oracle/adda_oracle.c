@@ -328,7 +328,7 @@ static cplx ndot_conj(const cplx *a, const cplx *b, size_t n) // sum a*b, linalg
 typedef struct {
 	or_ctx *c;
 	size_t n;                 // 3*N
-	cplx *x, *r, *p, *Av, *v1, *v2, *v3;
+	cplx *x, *r, *p, *Av, *v1, *v2, *v3, *v4;
 	double inprodR, inprodRp1, epsB;
 	int niter, counter, matvec_ready, complete;
 } solver;
@@ -680,6 +680,85 @@ static int qmr2_iter(solver *s, qmr2_state *q)
 	return OR_OK;
 }
 
+/* BCGS2 = BiCGstab(l) with l = 2 (Fokkema's enhanced implementation without reliable updates),
+ * src/iterative.c:340-487: r_0..2 in r, v1, v3; u_0..2 in v2, Av, v4; r~0 in p */
+typedef struct {
+	cplx rho0, alpha;
+} bcgs2_state;
+
+static int bcgs2_iter(solver *s, bcgs2_state *b)
+{
+	const size_t n = s->n;
+	cplx *r[3] = {s->r, s->v1, s->v3}, *u[3] = {s->v2, s->Av, s->v4};
+	const cplx *rt = s->p;
+	cplx rho1, beta, sigma;
+	for (int j = 0; j < 2; j++) {
+		rho1 = ndot(r[j], rt, n);
+		if (s->niter == 1 && j == 0) memcpy(u[0], r[0], sizeof(cplx) * n);
+		else {
+			if (cabs(b->rho0) / (cabs(rho1) * cabs(b->alpha)) < 1e-10) return OR_EBREAKDOWN;
+			beta = b->alpha * rho1 / b->rho0;
+			cplx mb = -beta;
+			for (int i = 0; i <= j; i++)
+				for (size_t k = 0; k < n; k++) u[i][k] = mb * u[i][k] + r[i][k];
+		}
+		b->rho0 = rho1;
+		if (!(s->niter == 1 && j == 0 && s->matvec_ready)) mv(s, u[j], u[j + 1], NULL);
+		sigma = ndot(u[j + 1], rt, n);
+		if (cabs(sigma) / cabs(rho1) < 1e-10) return OR_EBREAKDOWN;
+		b->alpha = rho1 / sigma;
+		for (size_t k = 0; k < n; k++) s->x[k] += b->alpha * u[0][k];
+		cplx ma = -b->alpha;
+		for (int i = 0; i <= j; i++)
+			for (size_t k = 0; k < n; k++) r[i][k] += ma * u[i + 1][k];
+		mv(s, r[j], r[j + 1], NULL);
+	}
+	// convex polynomial part: Z = R'R (Z[i][j] = r_j . conj(r_i))
+	cplx Z[3][3], y0[3], yl[3], zy0[3], zyl[3];
+	for (int i = 0; i <= 2; i++)
+		for (int j = 0; j <= i; j++) {
+			Z[i][j] = ndot(r[j], r[i], n);
+			if (i != j) Z[j][i] = conj(Z[i][j]);
+		}
+	y0[0] = -1; y0[1] = Z[1][0] / Z[1][1]; y0[2] = 0;
+	yl[0] = 0; yl[1] = Z[1][2] / Z[1][1]; yl[2] = -1;
+	for (int i = 0; i <= 2; i++) {
+		zy0[i] = zyl[i] = 0;
+		for (int j = 0; j <= 2; j++) {
+			zy0[i] += Z[i][j] * y0[j];
+			zyl[i] += Z[i][j] * yl[j];
+		}
+	}
+	double d = 0;
+	for (int i = 0; i <= 2; i++) d += creal(zy0[i] * conj(y0[i]));
+	const double kappa0 = sqrt(d);
+	d = 0;
+	for (int i = 0; i <= 2; i++) d += creal(zyl[i] * conj(yl[i]));
+	const double kappal = sqrt(d);
+	cplx varrho = 0;
+	for (int i = 0; i <= 2; i++) varrho += zy0[i] * conj(yl[i]);
+	varrho /= kappa0 * kappal;
+	d = cabs(varrho);
+	cplx hatgamma = varrho * (d > 0.7 ? d : 0.7) / d;
+	cplx t = -hatgamma * kappa0 / kappal;
+	for (int i = 0; i <= 2; i++) y0[i] += t * yl[i];
+	const cplx omega = y0[2];
+	for (int i = 1; i <= 2; i++) {
+		cplx m = -y0[i];
+		for (size_t k = 0; k < n; k++) u[0][k] += m * u[i][k];
+		for (size_t k = 0; k < n; k++) s->x[k] += y0[i] * r[i - 1][k];
+		for (size_t k = 0; k < n; k++) r[0][k] += m * r[i][k];
+	}
+	for (int i = 0; i <= 2; i++) {
+		zy0[i] = 0;
+		for (int j = 0; j <= 2; j++) zy0[i] += Z[i][j] * y0[j];
+	}
+	s->inprodRp1 = 0;
+	for (int i = 0; i <= 2; i++) s->inprodRp1 += creal(zy0[i] * conj(y0[i]));
+	b->rho0 *= -omega;
+	return OR_OK;
+}
+
 /* IterativeSolver, src/iterative.c:1398-1530 with CalcInitField (:1342-1394) and ProgressReport (:282-318).
  * einc: incident field [N][3]; xvec receives x, pvec the polarisations S.x; resid_hist[0..] the relative residuals
  * RE_000, RE_001, ... (at most hist_cap values). Returns a status code; *niter_out = iterations performed. */
@@ -700,6 +779,7 @@ int or_solve(or_ctx *c, int method, const double *einc, double eps, int maxiter,
 	S.v1 = malloc(sizeof(cplx) * n);
 	S.v2 = malloc(sizeof(cplx) * n);
 	S.v3 = malloc(sizeof(cplx) * n);
+	S.v4 = malloc(sizeof(cplx) * n);
 	// b = S.Einc (nMult_mat)
 	for (size_t i = 0; i < c->n; i++)
 		for (int a = 0; a < 3; a++) b[3 * i + a] = ccs_of(c, i, a) * E[3 * i + a];
@@ -732,11 +812,13 @@ int or_solve(or_ctx *c, int method, const double *einc, double eps, int maxiter,
 	S.niter = 1;
 	S.counter = 0;
 	// stagnation limits per method (iterative.c:118-125)
-	const int mcm = (method == OR_BICGSTAB) ? 30000 : (method == OR_CGNR || method == OR_CSYM) ? 10 : 50000;
+	const int mcm = (method == OR_BICGSTAB) ? 30000 : (method == OR_CGNR || method == OR_CSYM) ? 10
+		: (method == OR_BCGS2) ? 15000 : 50000;
 	qmr_state q;
 	bcgs_state bs;
 	csym_state cs;
 	qmr2_state q2;
+	bcgs2_state b2 = {-1, 0};
 	cplx ro_c = 0;
 	double ro_d = 0;
 	if (method == OR_QMR_CS) qmr_init(&S, &q);
@@ -746,6 +828,7 @@ int or_solve(or_ctx *c, int method, const double *einc, double eps, int maxiter,
 	}
 	else if (method == OR_CSYM) csym_init(&S, &cs);
 	else if (method == OR_QMR_CS_2) qmr2_init(&S, &q2);
+	else if (method == OR_BCGS2) memcpy(S.p, S.r, sizeof(cplx) * n); // r~0 = r_0, rho0 = -1
 	int status = OR_OK;
 	while (S.inprodR > S.epsB && S.niter <= maxiter && S.counter <= mcm) {
 		S.complete = 1;
@@ -755,6 +838,7 @@ int or_solve(or_ctx *c, int method, const double *einc, double eps, int maxiter,
 			case OR_BICG_CS: status = bicg_iter(&S, &ro_c); break;
 			case OR_CGNR: status = cgnr_iter(&S, &ro_d); break;
 			case OR_QMR_CS_2: status = qmr2_iter(&S, &q2); break;
+			case OR_BCGS2: status = bcgs2_iter(&S, &b2); break;
 			default: status = csym_iter(&S, &cs); break;
 		}
 		if (status != OR_OK) break;
@@ -770,7 +854,7 @@ int or_solve(or_ctx *c, int method, const double *einc, double eps, int maxiter,
 	for (size_t i = 0; i < c->n; i++)
 		for (int a = 0; a < 3; a++) b[3 * i + a] = ccs_of(c, i, a) * S.x[3 * i + a];
 	if (niter_out) *niter_out = S.niter - 1;
-	free(S.r); free(S.p); free(S.Av); free(S.v1); free(S.v2); free(S.v3);
+	free(S.r); free(S.p); free(S.Av); free(S.v1); free(S.v2); free(S.v3); free(S.v4);
 	return status;
 }
 

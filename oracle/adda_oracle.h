@@ -8,7 +8,7 @@
  *   or_matvec        <- MatVec                   src/matvec.c:128-425
  *   or_solve         <- IterativeSolver          src/iterative.c:1398-1530, QMR_CS :898-1032, BiCGStab :640-724,
  *                                               BiCG_CS :490-637, CGNR :729-769, CSYM :773-892,
- *                                               QMR_CS_2 :1038-1132
+ *                                               QMR_CS_2 :1038-1132, BCGS2 :340-487
  *   or_cross         <- ExtCross / AbsCross      src/crosssec.c:811-917 (plane wave, free space, Draine)
  * Complex vectors are interleaved (re,im) doubles, dipole-major [dipole][3], like the reference's doublecomplex.
  */
@@ -21,7 +21,7 @@
 typedef struct or_ctx or_ctx;
 
 /* iterative methods and initial-field modes, same meaning as -iter and -init_field */
-enum { OR_QMR_CS = 0, OR_BICGSTAB = 1, OR_BICG_CS = 2, OR_CGNR = 3, OR_CSYM = 4, OR_QMR_CS_2 = 5 };
+enum { OR_QMR_CS = 0, OR_BICGSTAB = 1, OR_BICG_CS = 2, OR_CGNR = 3, OR_CSYM = 4, OR_QMR_CS_2 = 5, OR_BCGS2 = 6 };
 enum { OR_IF_AUTO = 0, OR_IF_ZERO = 1, OR_IF_INC = 2 };
 /* solver status codes */
 enum { OR_OK = 0, OR_EBREAKDOWN = 1, OR_ESTAGNATION = 2, OR_EMAXITER = 3 };

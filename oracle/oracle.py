@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_BIN = os.path.join(HERE, "_ref", "adda")
 
-QMR_CS, BICGSTAB, BICG_CS, CGNR, CSYM, QMR_CS_2 = 0, 1, 2, 3, 4, 5
+QMR_CS, BICGSTAB, BICG_CS, CGNR, CSYM, QMR_CS_2, BCGS2 = 0, 1, 2, 3, 4, 5, 6
 IF_AUTO, IF_ZERO, IF_INC = 0, 1, 2
 STATUS = {0: "ok", 1: "breakdown", 2: "stagnation", 3: "maxiter"}
 

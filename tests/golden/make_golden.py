@@ -76,6 +76,11 @@ CASES = [
      dict(grid=16, m=1.5, dpl=10, iter="qmr2")),
     ("ell_qmr2_eps8", ["-iter", "qmr2", "-eps", "8"] + ELL + MGN,
      dict(grid=8, m=1.1 + 0.1j, shape="ellipsoid", pars=(0.5, 1.5), iter="qmr2", eps=1e-8)),
+    ("mgn_bcgs2", ["-iter", "bcgs2"] + MGN, dict(grid=8, m=1.1 + 0.1j, iter="bcgs2")),
+    ("c1_bcgs2", ["-grid", "16", "-dpl", "10", "-m", "1.5", "0", "-iter", "bcgs2", "-eps", "5"],
+     dict(grid=16, m=1.5, dpl=10, iter="bcgs2")),
+    ("ell_bcgs2_eps8", ["-iter", "bcgs2", "-eps", "8"] + ELL + MGN,
+     dict(grid=8, m=1.1 + 0.1j, shape="ellipsoid", pars=(0.5, 1.5), iter="bcgs2", eps=1e-8)),
 ] + [("grid%d" % g, ["-grid", str(g), "-size", "8"] + M, dict(grid=g, m=1.1 + 0.1j, size=8.0))
      for g in (2, 4, 6, 10, 12, 18, 20, 24, 30, 32)]
 

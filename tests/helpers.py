@@ -45,7 +45,7 @@ def oracle_solve(o, s, pol_index, method="qmr", eps=1e-5, maxiter=100000, init="
     from oracle import oracle as O
     o.set_cc(s.cc[pol_index].reshape(1, 3))
     methods = {"qmr": O.QMR_CS, "bicgstab": O.BICGSTAB, "bicg": O.BICG_CS, "cgnr": O.CGNR, "csym": O.CSYM,
-               "qmr2": O.QMR_CS_2}
+               "qmr2": O.QMR_CS_2, "bcgs2": O.BCGS2}
     r = o.solve(s.einc[pol_index], method=methods[method], eps=eps, maxiter=maxiter,
                 init_field={"auto": O.IF_AUTO, "zero": O.IF_ZERO, "inc": O.IF_INC}[init])
     ce, ca = o.cross(r["p"], s.prop, s.incpol[pol_index])
