@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libadda_gb300.so")
 
 SHAPES = {"sphere": 0, "ellipsoid": 1, "box": 2}
 POLS = {"ldr": 0, "cm": 1, "rrc": 2, "dgf": 3}
-ITERS = {"qmr": 0, "bicgstab": 1, "bicg": 2, "cgnr": 3, "csym": 4, "qmr2": 5}
+ITERS = {"qmr": 0, "bicgstab": 1, "bicg": 2, "cgnr": 3, "csym": 4, "qmr2": 5, "bcgs2": 6}
 PREC = {"fp64": 0, "fp32": 1, "mixed": 2, "mixed_f32vec": 3, "mixed_f64vec": 4}
 INIT = {"auto": 0, "zero": 1, "inc": 2}
 STATUS = {0: "ok", 1: "breakdown", 2: "stagnation", 3: "maxiter"}

@@ -158,7 +158,8 @@ int IterativeSolver(enum iter method, enum incpol which)
 	else if (method == IT_CGNR) sp.method = ADDA_ITER_CGNR;
 	else if (method == IT_CSYM) sp.method = ADDA_ITER_CSYM;
 	else if (method == IT_QMR_CS_2) sp.method = ADDA_ITER_QMR_CS_2;
-	else ERR("The GPU build supports -iter qmr|qmr2|bicgstab|bicg|cgnr|csym only");
+	else if (method == IT_BCGS2) sp.method = ADDA_ITER_BCGS2;
+	else ERR("Unknown -iter method for the GPU build");
 	if (InitField == IF_AUTO) sp.init_field = ADDA_IF_AUTO;
 	else if (InitField == IF_ZERO) sp.init_field = ADDA_IF_ZERO;
 	else if (InitField == IF_INC) sp.init_field = ADDA_IF_INC;

@@ -44,6 +44,8 @@ struct RhsState {
 	// QMR_CS_2: ro_k, theta_(k-1), c_(k-1); eps_(k-1), eta_(k-1), beta_k; delta_k = v_k.v_k
 	double q2_ro, q2_theta, q2_c;
 	double2 q2_eps, q2_eta, q2_beta, q2_delta;
+	// BCGS2: rho_0, rho_1, alpha; the convex-combination coefficients y0[1], y0[2]
+	double2 b2_rho0, b2_rho1, b2_alpha, b2_y1, b2_y2;
 	// coefficients for the vector kernels
 	double2 k0, k1, k2, k3, kib, kr;
 	double d0;
@@ -56,7 +58,7 @@ struct SolverWork {
 	// FP64 vectors [R][3N]
 	double2 *x64 = nullptr, *r64 = nullptr, *b64 = nullptr, *av64 = nullptr;
 	// Krylov work vectors, stored as double2 (the float solver uses the first half of each)
-	double2 *kv[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+	double2 *kv[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 	RhsState *st = nullptr;
 	int *done = nullptr;   // mirror of st[r].done for the matvec early exit
 	double *hist = nullptr;
@@ -974,6 +976,217 @@ __global__ void __launch_bounds__(NT) q2_v3(const RhsState *st, C *d, const C *p
 	write_part(part, nbv, s, 1);
 }
 
+// ---------------- BCGS2 = BiCGstab(2), iterative.c:340-487 ----------------
+// r_0..2 in r, v1, v3; u_0..2 in v2, Av, v4; r~_0 in p. Four matvecs per iteration.
+
+__global__ void b2_init_s(RhsState *st)
+{
+	const int r = blockIdx.x;
+	if (threadIdx.x || st[r].done) return;
+	st[r].b2_rho0 = dc(-1, 0);
+	st[r].b2_alpha = dc(0, 0);
+}
+
+// rho1 = r_j.r~0 (slots 1,2 of part); 1/|beta| test (:402-405); beta = alpha*rho1/rho0; rho0 = rho1
+__global__ void b2_s_beta(RhsState *st, int *done, const double *part, size_t nblk, int j)
+{
+	const int r = blockIdx.x;
+	if (st[r].done) return;
+	double s[4];
+	sum_part(part, nblk, r, s, 3);
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	const double2 rho1 = dc(s[1], s[2]);
+	if (S.niter == 1 && j == 0) S.k0 = dc(0, 0);
+	else {
+		if (dabs(S.b2_rho0) / (dabs(rho1) * dabs(S.b2_alpha)) < 1e-10) {
+			S.status = ADDA_GB300_EBREAKDOWN;
+			S.done = 1;
+			done[r] = 1;
+			return;
+		}
+		const double2 beta = ddiv(dmul(S.b2_alpha, rho1), S.b2_rho0);
+		S.k0 = dc(-beta.x, -beta.y);
+	}
+	S.b2_rho0 = rho1;
+	S.b2_rho1 = rho1;
+}
+
+// u_i = r_i - beta*u_i for i <= j (u_0 = r_0 in the very first step)
+template <typename C>
+__global__ void __launch_bounds__(NT) b2_vu(const RhsState *st, C *u0, const C *r0, C *u1, const C *r1, size_t n3, int j)
+{
+	const int r = blockIdx.y;
+	if (st[r].done) return;
+	const bool copy = st[r].niter == 1 && j == 0;
+	const C k0 = cof<C>(st[r].k0);
+	VLOOP(n3) {
+		const size_t q = r * n3 + i;
+		u0[q] = copy ? r0[q] : cadd(cmul(k0, u0[q]), r0[q]);
+		if (j == 1) u1[q] = cadd(cmul(k0, u1[q]), r1[q]);
+	}
+}
+
+// sigma = u_(j+1).r~0 (matvec epilogue slots 1,2); test (:411-414); alpha = rho1/sigma
+__global__ void b2_s_alpha(RhsState *st, int *done, const double *part, size_t nblk)
+{
+	const int r = blockIdx.x;
+	if (st[r].done) return;
+	double s[4];
+	sum_part(part, nblk, r, s, 3);
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	const double2 sigma = dc(s[1], s[2]);
+	if (dabs(sigma) / dabs(S.b2_rho1) < 1e-10) {
+		S.status = ADDA_GB300_EBREAKDOWN;
+		S.done = 1;
+		done[r] = 1;
+		return;
+	}
+	S.b2_alpha = ddiv(S.b2_rho1, sigma);
+}
+
+// x += alpha*u_0; r_i -= alpha*u_(i+1) for i <= j; for j = 1 also the partial |r_0|^2 (Z_00, slot 0)
+template <typename C>
+__global__ void __launch_bounds__(NT) b2_vx(const RhsState *st, C *x, const C *u0, C *r0, const C *u1, C *r1,
+	const C *u2, size_t n3, int j, double *part, int nbv)
+{
+	const int r = blockIdx.y;
+	if (st[r].done) return;
+	const C a = cof<C>(st[r].b2_alpha), ma = cof<C>(dc(-st[r].b2_alpha.x, -st[r].b2_alpha.y));
+	typename AccOf<C>::T s[4] = {};
+	VLOOP(n3) {
+		const size_t q = r * n3 + i;
+		x[q] = cadd(x[q], cmul(a, u0[q]));
+		const C y = cadd(r0[q], cmul(ma, u1[q]));
+		r0[q] = y;
+		if (j == 1) {
+			r1[q] = cadd(r1[q], cmul(ma, u2[q]));
+			acc_abs2(s[0], y);
+		}
+	}
+	if (j == 1) write_part(part, nbv, s, 1);
+}
+
+// Gram entries Z_11, Z_22, Z_10 = r_0.r_1*, Z_20 = r_0.r_2*, Z_21 = r_1.r_2* (8 slots of xpart)
+template <typename C>
+__global__ void __launch_bounds__(NT) b2_gram(const RhsState *st, const C *r0, const C *r1, const C *r2, size_t n3,
+	double *xpart, int nbv)
+{
+	const int r = blockIdx.y;
+	if (st[r].done) return;
+	typename AccOf<C>::T s[8] = {};
+	VLOOP(n3) {
+		const size_t q = r * n3 + i;
+		const C a = r0[q], b = r1[q], c = r2[q];
+		acc_abs2(s[0], b);
+		acc_abs2(s[1], c);
+		acc_cmulc(s[2], s[3], a, b);
+		acc_cmulc(s[4], s[5], a, c);
+		acc_cmulc(s[6], s[7], b, c);
+	}
+	double v[8];
+	for (int k = 0; k < 8; k++) v[k] = acc_val(s[k]);
+	block_sum4(v, 4);
+	block_sum4(v + 4, 4);
+	if (threadIdx.x == 0) {
+		double *o = xpart + ((size_t)blockIdx.y * nbv + blockIdx.x) * 8;
+		for (int k = 0; k < 8; k++) o[k] = v[k];
+	}
+}
+
+// convex polynomial part (:427-480): minimal-residual combination of r_0..2 from the Gram matrix; y0[1], y0[2],
+// omega = y0[2], |r|^2 = y0.Z.y0, rho0 *= -omega
+__global__ void b2_s_final(RhsState *st, const double *vpart, const double *xpart, int nbv)
+{
+	const int r = blockIdx.x;
+	if (st[r].done) return;
+	__shared__ double sh[8][NT / 32];
+	double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+	for (int b = threadIdx.x; b < nbv; b += blockDim.x) {
+		v[0] += vpart[((size_t)r * nbv + b) * 4];
+		for (int k = 0; k < 8; k++) v[1 + k] += xpart[((size_t)r * nbv + b) * 8 + k];
+	}
+	double tot[9];
+	for (int k = 0; k < 9; k++) {
+		double x = v[k];
+		for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+		__syncthreads();
+		if ((threadIdx.x & 31) == 0) sh[0][threadIdx.x >> 5] = x;
+		__syncthreads();
+		tot[k] = 0;
+		for (int w = 0; w < NT / 32; w++) tot[k] += sh[0][w];
+	}
+	if (threadIdx.x) return;
+	RhsState &S = st[r];
+	double2 Z[3][3];
+	Z[0][0] = dc(tot[0], 0);
+	Z[1][1] = dc(tot[1], 0);
+	Z[2][2] = dc(tot[2], 0);
+	Z[1][0] = dc(tot[3], tot[4]);
+	Z[2][0] = dc(tot[5], tot[6]);
+	Z[2][1] = dc(tot[7], tot[8]);
+	Z[0][1] = dconj(Z[1][0]);
+	Z[0][2] = dconj(Z[2][0]);
+	Z[1][2] = dconj(Z[2][1]);
+	double2 y0[3] = {dc(-1, 0), ddiv(Z[1][0], Z[1][1]), dc(0, 0)};
+	const double2 yl[3] = {dc(0, 0), ddiv(Z[1][2], Z[1][1]), dc(-1, 0)};
+	double2 zy0[3], zyl[3];
+	for (int i = 0; i < 3; i++) {
+		zy0[i] = zyl[i] = dc(0, 0);
+		for (int j = 0; j < 3; j++) {
+			zy0[i] = dadd(zy0[i], dmul(Z[i][j], y0[j]));
+			zyl[i] = dadd(zyl[i], dmul(Z[i][j], yl[j]));
+		}
+	}
+	double d = 0;
+	for (int i = 0; i < 3; i++) d += dmul(zy0[i], dconj(y0[i])).x;
+	const double kappa0 = sqrt(d);
+	d = 0;
+	for (int i = 0; i < 3; i++) d += dmul(zyl[i], dconj(yl[i])).x;
+	const double kappal = sqrt(d);
+	double2 varrho = dc(0, 0);
+	for (int i = 0; i < 3; i++) varrho = dadd(varrho, dmul(zy0[i], dconj(yl[i])));
+	varrho = dscal(varrho, 1 / (kappa0 * kappal));
+	d = dabs(varrho);
+	const double2 hatgamma = dscal(varrho, (d > 0.7 ? d : 0.7) / d);
+	const double2 t = dscal(hatgamma, -kappa0 / kappal);
+	for (int i = 0; i < 3; i++) y0[i] = dadd(y0[i], dmul(t, yl[i]));
+	const double2 omega = y0[2];
+	S.b2_y1 = y0[1];
+	S.b2_y2 = y0[2];
+	for (int i = 0; i < 3; i++) {
+		zy0[i] = dc(0, 0);
+		for (int j = 0; j < 3; j++) zy0[i] = dadd(zy0[i], dmul(Z[i][j], y0[j]));
+	}
+	d = 0;
+	for (int i = 0; i < 3; i++) d += dmul(zy0[i], dconj(y0[i])).x;
+	S.inprodRp1 = d;
+	S.b2_rho0 = dmul(S.b2_rho0, dc(-omega.x, -omega.y));
+}
+
+// u_0 -= y1*u_1 + y2*u_2; x += y1*r_0 + y2*r_1; r_0 -= y1*r_1 + y2*r_2; partial r_0.r~0 for the next iteration
+template <typename C>
+__global__ void __launch_bounds__(NT) b2_vfinal(const RhsState *st, C *u0, const C *u1, const C *u2, C *x, C *r0,
+	const C *r1, const C *r2, const C *rt, size_t n3, double *part, int nbv)
+{
+	const int r = blockIdx.y;
+	if (st[r].done) return;
+	const C y1 = cof<C>(st[r].b2_y1), y2 = cof<C>(st[r].b2_y2);
+	const C my1 = cof<C>(dc(-st[r].b2_y1.x, -st[r].b2_y1.y)), my2 = cof<C>(dc(-st[r].b2_y2.x, -st[r].b2_y2.y));
+	typename AccOf<C>::T s[4] = {};
+	VLOOP(n3) {
+		const size_t q = r * n3 + i;
+		u0[q] = cadd(cadd(u0[q], cmul(my1, u1[q])), cmul(my2, u2[q]));
+		const C a = r0[q], b = r1[q];
+		x[q] = cadd(cadd(x[q], cmul(y1, a)), cmul(y2, b));
+		const C y = cadd(cadd(a, cmul(my1, b)), cmul(my2, r2[q]));
+		r0[q] = y;
+		acc_cmulc(s[1], s[2], y, rt[q]);
+	}
+	write_part(part, nbv, s, 3);
+}
+
 // ---------------- FP64 helpers for the refinement loop and the results ----------------
 
 // x64 (+)= d (float or double), depending on accumulate
@@ -1135,7 +1348,7 @@ static int ensure_work(adda_gb300_ctx *c, int R, int hist_cap)
 		ADDA_CUDA(cudaMalloc(&w->r64, vb));
 		ADDA_CUDA(cudaMalloc(&w->b64, vb));
 		ADDA_CUDA(cudaMalloc(&w->av64, vb));
-		for (int i = 0; i < 7; i++) ADDA_CUDA(cudaMalloc(&w->kv[i], vb));
+		for (int i = 0; i < 8; i++) ADDA_CUDA(cudaMalloc(&w->kv[i], vb));
 		ADDA_CUDA(cudaMalloc(&w->st, sizeof(RhsState) * Rm));
 		ADDA_CUDA(cudaMalloc(&w->done, sizeof(int) * Rm));
 		ADDA_CUDA(cudaMallocHost(&w->h_done, sizeof(int) * Rm));
@@ -1168,7 +1381,7 @@ void solver_free(adda_gb300_ctx *c)
 	void *b[] = {w->x64, w->r64, w->b64, w->av64, w->st, w->done, w->hist, w->vpart, w->xpart};
 	for (void *p : b)
 		if (p) cudaFree(p);
-	for (int i = 0; i < 7; i++)
+	for (int i = 0; i < 8; i++)
 		if (w->kv[i]) cudaFree(w->kv[i]);
 	if (w->h_done) cudaFreeHost(w->h_done);
 	delete w;
@@ -1177,7 +1390,7 @@ void solver_free(adda_gb300_ctx *c)
 
 // Krylov vector roles inside kv[] (as typed pointers)
 template <typename C> struct KV {
-	C *x, *r, *p, *Av, *v1, *v2, *v3;
+	C *x, *r, *p, *Av, *v1, *v2, *v3, *v4;
 };
 
 template <typename C> static KV<C> kvec(SolverWork *w)
@@ -1190,12 +1403,13 @@ template <typename C> static KV<C> kvec(SolverWork *w)
 	k.v1 = (C *)w->kv[4];
 	k.v2 = (C *)w->kv[5];
 	k.v3 = (C *)w->kv[6];
+	k.v4 = (C *)w->kv[7];
 	return k;
 }
 
 static int matvecs_per_iter(int method)
 {
-	return (method == ADDA_ITER_BICGSTAB || method == ADDA_ITER_CGNR) ? 2 : 1;
+	return (method == ADDA_ITER_BICGSTAB || method == ADDA_ITER_CGNR) ? 2 : (method == ADDA_ITER_BCGS2) ? 4 : 1;
 }
 
 // enqueue one Krylov iteration; parity selects the QMR_CS vector roles (v<->v~, p_new<->p_old swap each iteration).
@@ -1254,6 +1468,33 @@ static int enqueue_iter(adda_gb300_ctx *c, SolverWork *w, int method, int R, int
 		cg_v2<C><<<gv, NT, 0, s>>>(w->st, k.x, k.p, k.r, k.Av, n3, w->vpart, w->nbv);
 		ADDA_LAUNCHED();
 		s_progress<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv, w->hist, w->hist_cap, 0);
+		ADDA_LAUNCHED();
+	}
+	else if (method == ADDA_ITER_BCGS2) {
+		C *r0 = k.r, *r1 = k.v1, *r2 = k.v3, *u0 = k.v2, *u1 = k.Av, *u2 = k.v4, *rt = k.p;
+		for (int j = 0; j < 2 && !rc; j++) {
+			// rho1 of j = 0 comes from the previous b2_vfinal (or the init k_dot), of j = 1 from the r_1 matvec
+			if (j == 0) b2_s_beta<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv, 0);
+			else b2_s_beta<<<R, NT, 0, s>>>(w->st, w->done, c->partial, nblk, 1);
+			ADDA_LAUNCHED();
+			b2_vu<C><<<gv, NT, 0, s>>>(w->st, u0, r0, u1, r1, n3, j);
+			ADDA_LAUNCHED();
+			MvEpi eu{EPI_DOT_U_CONJ, rt, c->partial};
+			if ((rc = matvec_run<T>(c, R, j ? u1 : u0, j ? u2 : u1, 0, eu, w->done))) return rc;
+			b2_s_alpha<<<R, NT, 0, s>>>(w->st, w->done, c->partial, nblk);
+			ADDA_LAUNCHED();
+			b2_vx<C><<<gv, NT, 0, s>>>(w->st, k.x, u0, r0, u1, r1, u2, n3, j, w->vpart, w->nbv);
+			ADDA_LAUNCHED();
+			MvEpi er{j ? (int)EPI_NONE : (int)EPI_DOT_U_CONJ, rt, c->partial};
+			if ((rc = matvec_run<T>(c, R, j ? r1 : r0, j ? r2 : r1, 0, er, w->done))) return rc;
+		}
+		b2_gram<C><<<gv, NT, 0, s>>>(w->st, r0, r1, r2, n3, w->xpart, w->nbv);
+		ADDA_LAUNCHED();
+		b2_s_final<<<R, NT, 0, s>>>(w->st, w->vpart, w->xpart, w->nbv);
+		ADDA_LAUNCHED();
+		b2_vfinal<C><<<gv, NT, 0, s>>>(w->st, u0, u1, u2, k.x, r0, r1, r2, rt, n3, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+		s_progress<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv, w->hist, w->hist_cap, 2);
 		ADDA_LAUNCHED();
 	}
 	else if (method == ADDA_ITER_QMR_CS_2) {
@@ -1348,6 +1589,15 @@ static int krylov(adda_gb300_ctx *c, SolverWork *w, int method, int R, int K, un
 	else if (method == ADDA_ITER_BICG_CS) {
 		// r.r for the first iteration's bg_s0 (slots 1,2)
 		k_dot<C><<<gv, NT, 0, s>>>(k.r, k.r, n3, 0, w->vpart, w->nbv);
+		ADDA_LAUNCHED();
+	}
+	else if (method == ADDA_ITER_BCGS2) {
+		// r~0 = r_0 (in p), rho0 = -1; r_0.r~0 for the first b2_s_beta (slots 1,2)
+		k_copy<C><<<gv, NT, 0, s>>>(k.p, k.r, n3, nullptr);
+		ADDA_LAUNCHED();
+		b2_init_s<<<R, 32, 0, s>>>(w->st);
+		ADDA_LAUNCHED();
+		k_dot<C><<<gv, NT, 0, s>>>(k.r, k.p, n3, 1, w->vpart, w->nbv);
 		ADDA_LAUNCHED();
 	}
 	else if (method == ADDA_ITER_QMR_CS_2) {
@@ -1555,7 +1805,7 @@ static int solve_mixed(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int
 
 static int check_params(const adda_gb300_solve_params *sp)
 {
-	if (sp->method < ADDA_ITER_QMR_CS || sp->method > ADDA_ITER_QMR_CS_2 ||
+	if (sp->method < ADDA_ITER_QMR_CS || sp->method > ADDA_ITER_BCGS2 ||
 		(sp->precision != ADDA_PREC_FP64 && sp->precision != ADDA_PREC_MIXED &&
 			sp->precision != ADDA_PREC_MIXED_F32VEC && sp->precision != ADDA_PREC_MIXED_F64VEC) || !(sp->eps > 0) || sp->maxiter < 0 ||
 		(sp->init_field != ADDA_IF_AUTO && sp->init_field != ADDA_IF_ZERO && sp->init_field != ADDA_IF_INC)) {
@@ -1599,7 +1849,8 @@ static int solve_core_impl(adda_gb300_ctx *c, const adda_gb300_solve_params *sp,
 	const dim3 gv(w->nbv, R);
 	// stagnation limits per method (iterative.c:118-125)
 	const int mc = (sp->method == ADDA_ITER_BICGSTAB) ? 30000
-		: (sp->method == ADDA_ITER_CGNR || sp->method == ADDA_ITER_CSYM) ? 10 : 50000;
+		: (sp->method == ADDA_ITER_CGNR || sp->method == ADDA_ITER_CSYM) ? 10
+		: (sp->method == ADDA_ITER_BCGS2) ? 15000 : 50000;
 	int K = sp->check_every > 0 ? sp->check_every : 8;
 	if (K % 2) K++;
 	std::vector<adda_gb300_rhs_stats> st(R);
@@ -1609,7 +1860,7 @@ static int solve_core_impl(adda_gb300_ctx *c, const adda_gb300_solve_params *sp,
 	k_mult_cc<<<gv, NT, 0, s>>>(d_einc, w->b64, c->ccs64, c->per_dip, c->nmat, c->d_mat, c->N, w->vpart, w->nbv);
 	ADDA_LAUNCHED();
 	ADDA_CUDA(cudaMemsetAsync(w->hist, 0, sizeof(double) * R * w->hist_cap, s));
-	for (int i = 0; i < 7; i++) ADDA_CUDA(cudaMemsetAsync(w->kv[i], 0, sizeof(double2) * R * n3, s));
+	for (int i = 0; i < 8; i++) ADDA_CUDA(cudaMemsetAsync(w->kv[i], 0, sizeof(double2) * R * n3, s));
 	if (sp->precision == ADDA_PREC_FP64) {
 		typedef double2 C;
 		KV<C> k = kvec<C>(w);

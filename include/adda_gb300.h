@@ -35,14 +35,16 @@ extern "C" {
 
 enum adda_gb300_shape { ADDA_SHAPE_SPHERE = 0, ADDA_SHAPE_ELLIPSOID = 1, ADDA_SHAPE_BOX = 2 };
 enum adda_gb300_pol { ADDA_POL_LDR = 0, ADDA_POL_CM = 1, ADDA_POL_RRC = 2, ADDA_POL_DGF = 3 };
-/* Krylov methods of the reference's -iter: qmr, bicgstab, bicg (BiCG_CS / COCG), cgnr, csym, qmr2 (QMR_CS_2) */
+/* Krylov methods of the reference's -iter: qmr, bicgstab, bicg (BiCG_CS / COCG), cgnr, csym, qmr2 (QMR_CS_2),
+ * bcgs2 (BiCGstab(2)) */
 enum adda_gb300_iter {
 	ADDA_ITER_QMR_CS = 0,
 	ADDA_ITER_BICGSTAB = 1,
 	ADDA_ITER_BICG_CS = 2,
 	ADDA_ITER_CGNR = 3,
 	ADDA_ITER_CSYM = 4,
-	ADDA_ITER_QMR_CS_2 = 5
+	ADDA_ITER_QMR_CS_2 = 5,
+	ADDA_ITER_BCGS2 = 6
 };
 /* arithmetic of a matvec / solve. FP64: everything in double. FP32: complex-float FFTs, D-matrix and vectors.
  * MIXED (solve only): Krylov solves whose matvec runs in FP32 (FFTs, D, expanded grid) while the Krylov vectors are

@@ -126,7 +126,8 @@ def test_matvec_per_dipole_cc():
 SOLVE_CASES = ["c1_qmr", "c1_bicgstab", "mgn", "mgn_eps10", "mgn_init_zero", "mgn_init_inc", "mgn_bicgstab",
                "mgn_maxiter3", "ell_orient", "pol_ldr_prop", "prop_ell", "ell24", "box12", "grid6", "grid18",
                "sample_default", "c2_small", "mgn_bicg", "mgn_cgnr", "mgn_csym", "c1_bicg", "c1_cgnr", "c1_csym",
-               "ell_bicg_eps8", "ell_csym_eps8", "mgn_qmr2", "c1_qmr2", "ell_qmr2_eps8"]
+               "ell_bicg_eps8", "ell_csym_eps8", "mgn_qmr2", "c1_qmr2", "ell_qmr2_eps8",
+               "mgn_bcgs2", "c1_bcgs2", "ell_bcgs2_eps8"]
 
 
 @pytest.mark.parametrize("name", SOLVE_CASES)
@@ -162,7 +163,7 @@ def test_solve_fp64_vs_reference(name):
             assert abs(v - want) <= max(tol * abs(want), 1e-12), (pol, q, v, want)
 
 
-@pytest.mark.parametrize("method", ["qmr", "bicgstab", "bicg", "cgnr", "csym", "qmr2"])
+@pytest.mark.parametrize("method", ["qmr", "bicgstab", "bicg", "cgnr", "csym", "qmr2", "bcgs2"])
 def test_solve_fp64_vs_oracle_tight(method):
     """at eps=1e-10 the GPU FP64 solve and the oracle agree on Cext/Cabs to 1e-9 and per dipole to 1e-8"""
     import adda_gb300 as A
@@ -203,7 +204,7 @@ def test_solve_mixed(name, method, prec):
         assert abs(ce[r] / ro["Cext"] - 1) < 3e-6, (ce[r], ro["Cext"])
 
 
-@pytest.mark.parametrize("method", ["bicg", "cgnr", "csym", "qmr2"])
+@pytest.mark.parametrize("method", ["bicg", "cgnr", "csym", "qmr2", "bcgs2"])
 @pytest.mark.parametrize("name", ["c1_qmr", "ell24"])
 def test_solve_mixed_other_methods(name, method):
     """BiCG_CS, CGNR and CSYM in mixed precision (double-float vectors): FP64 residual meets eps, cross sections within
