@@ -51,7 +51,7 @@ EXPORTS = ["adda_gb300_fft_fit", "adda_gb300_fit_box", "adda_gb300_make_particle
            "adda_gb300_get_grid", "adda_gb300_init_dmatrix", "adda_gb300_dmatrix_len", "adda_gb300_get_dmatrix",
            "adda_gb300_set_cc", "adda_gb300_set_cc_sqrt", "adda_gb300_set_cc_dipole", "adda_gb300_matvec", "adda_gb300_matvec_device",
            "adda_gb300_solve", "adda_gb300_solve_device", "adda_gb300_solve_many", "adda_gb300_vjp_chi",
-           "adda_gb300_cross_sections",
+           "adda_gb300_cross_sections", "adda_gb300_scattered_fields",
            "adda_gb300_cross_sections_noalloc", "adda_gb300_time_matvec",
            "adda_gb300_last_solve_ms", "adda_gb300_last_error", "adda_gb300_kernel_launches"]
 
@@ -98,6 +98,7 @@ def lib():
             "adda_gb300_solve_many": ([I, P, P, P, P, P, P, P], I),
             "adda_gb300_time_matvec": ([P, I, I, I, SZ, P], I),
             "adda_gb300_cross_sections": ([P, I, P, P, P, P], I),
+            "adda_gb300_scattered_fields": ([P, I, I, P, P], I),
             "adda_gb300_cross_sections_noalloc": ([I, SZ, P, P, P, P, I, I, I, I, I, D, D, P, P, P, P, P], I),
             "adda_gb300_last_error": ([], ctypes.c_char_p),
             "adda_gb300_last_solve_ms": ([P], D),
@@ -358,3 +359,48 @@ class Context:
         ce, ca = np.zeros(R), np.zeros(R)
         _check(self.L.adda_gb300_cross_sections(self.h, R, _p(prop), _p(inc), _p(ce), _p(ca)), "cross_sections")
         return ce, ca
+
+    def scattered_fields(self, dirs, nrhs=1):
+        """scattering amplitudes E(n) of the last solve's first nrhs RHS for unit directions dirs [ndir,3]:
+        complex [nrhs, ndir, 3] (CalcFieldFree, crosssec.c:506-596)"""
+        d = np.ascontiguousarray(dirs, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros((nrhs, d.shape[0], 3), np.complex128)
+        _check(self.L.adda_gb300_scattered_fields(self.h, nrhs, d.shape[0], _p(d), _p(out)), "scattered_fields")
+        return out
+
+    def mueller_yz(self, prop, incpol_y, incpol_x, thetas_deg):
+        """Mueller matrices [ntheta, 4, 4] in the plane of prop and incpol_y, for a last solve whose RHS 0 and 1 are
+        the Y and X polarisations: CalcEplaneYZ (CalculateE.c:423-500: observer n = cos(t) prop + sin(t) incpol_y,
+        E_per = E.incpol_x, E_par = E.(-sin(t) prop + cos(t) incpol_y)) and ComputeMuellerMatrix (CalculateE.c:83-118,
+        Bohren & Huffman 3.16) with s1 = Eper(X), s2 = Epar(Y), s3 = Epar(X), s4 = Eper(Y) (CalculateE.c:244)"""
+        prop, py, px = (np.asarray(v, dtype=np.float64) for v in (prop, incpol_y, incpol_x))
+        t = np.radians(np.asarray(thetas_deg, dtype=np.float64))
+        co, si = np.cos(t)[:, None], np.sin(t)[:, None]
+        e = self.scattered_fields(co * prop + si * py, nrhs=2)
+        epar = -si * prop + co * py
+        per = e @ px                                    # [2, ntheta]
+        par = np.einsum("rtc,tc->rt", e, epar)
+        return mueller_matrix(per[1], par[0], par[1], per[0])
+
+
+def mueller_matrix(s1, s2, s3, s4):
+    """4x4 Mueller matrices from the amplitude-matrix elements (ComputeMuellerMatrix, CalculateE.c:83-118)"""
+    a1, a2, a3, a4 = (np.abs(v) ** 2 for v in (s1, s2, s3, s4))
+    m = np.empty(np.shape(s1) + (4, 4))
+    m[..., 0, 0] = 0.5 * (a1 + a2 + a3 + a4)
+    m[..., 0, 1] = 0.5 * (a2 - a1 + a4 - a3)
+    m[..., 0, 2] = (s2 * np.conj(s3) + s1 * np.conj(s4)).real
+    m[..., 0, 3] = (s2 * np.conj(s3) - s1 * np.conj(s4)).imag
+    m[..., 1, 0] = 0.5 * (a2 - a1 + a3 - a4)
+    m[..., 1, 1] = 0.5 * (a2 + a1 - a3 - a4)
+    m[..., 1, 2] = (s2 * np.conj(s3) - s1 * np.conj(s4)).real
+    m[..., 1, 3] = (s2 * np.conj(s3) + s1 * np.conj(s4)).imag
+    m[..., 2, 0] = (s2 * np.conj(s4) + s1 * np.conj(s3)).real
+    m[..., 2, 1] = (s2 * np.conj(s4) - s1 * np.conj(s3)).real
+    m[..., 2, 2] = (s1 * np.conj(s2) + s3 * np.conj(s4)).real
+    m[..., 2, 3] = (s2 * np.conj(s1) + s4 * np.conj(s3)).imag
+    m[..., 3, 0] = (s4 * np.conj(s2) + s1 * np.conj(s3)).imag
+    m[..., 3, 1] = (s4 * np.conj(s2) - s1 * np.conj(s3)).imag
+    m[..., 3, 2] = (s1 * np.conj(s2) - s3 * np.conj(s4)).imag
+    m[..., 3, 3] = (s1 * np.conj(s2) - s3 * np.conj(s4)).real
+    return m

@@ -650,4 +650,14 @@ int adda_gb300_cross_sections(adda_gb300_ctx *c, int nrhs, const double *prop, c
 	return cross_sections(c, nrhs, prop, incpol, cext, cabs);
 }
 
+int adda_gb300_scattered_fields(adda_gb300_ctx *c, int nrhs, int ndir, const double *dirs, double *ebuff)
+{
+	if (!c || !dirs || !ebuff || ndir < 1 || nrhs < 1 || nrhs > c->last_nrhs || !c->pvec64) {
+		set_error("scattered_fields: invalid arguments or no solution available for that many RHS");
+		return ADDA_GB300_ESTATE;
+	}
+	ADDA_CUDA(cudaSetDevice(c->device));
+	return scattered_fields(c, nrhs, ndir, dirs, ebuff);
+}
+
 } // extern "C"

@@ -122,6 +122,7 @@ int solver_solve_dev(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int n
 	double2 *d_xvec, double2 *d_pvec, adda_gb300_rhs_stats *stats);
 void solver_free(adda_gb300_ctx *c);
 int cross_sections(adda_gb300_ctx *c, int nrhs, const double *prop, const double *incpol, double *cext, double *cabs);
+int scattered_fields(adda_gb300_ctx *c, int nrhs, int ndir, const double *dirs, double *ebuff);
 int vjp_chi(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int rhs, const double prop[3], const double incpol[3],
 	const double *dinv_alpha, double *grad_cext, double *grad_cabs);
 

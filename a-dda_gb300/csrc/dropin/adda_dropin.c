@@ -58,6 +58,8 @@ double *BT_buffer, *BT_rbuffer;
 #define ERR(...) LogError(ONE, __FILE__, __LINE__, __VA_ARGS__)
 
 static adda_gb300_ctx *g_ctx;
+/* the device polarisations belong to the host's pvec of the last IterativeSolver */
+static int g_pvec_valid = 0;
 static doublecomplex g_ccs[MAX_NMAT][3];
 static int g_ccs_valid;
 
@@ -104,6 +106,7 @@ void InitDmatrix(void)
 	if (adda_gb300_create(&p, &g_ctx)) ERR("GPU initialisation failed: %s", adda_gb300_last_error());
 	if (adda_gb300_init_dmatrix(g_ctx)) ERR("GPU D-matrix initialisation failed: %s", adda_gb300_last_error());
 	g_ccs_valid = 0;
+	g_pvec_valid = 0;
 	Timing_Dm_Init = clock() - start;
 	Timing_FFT_Init = 0;
 }
@@ -112,6 +115,7 @@ void Free_FFT_Dmat(void)
 {
 	if (g_ctx) adda_gb300_destroy(g_ctx);
 	g_ctx = NULL;
+	g_pvec_valid = 0;
 }
 
 /* InitCC (calculator.c:266) may change cc_sqrt between the two polarisations: upload when it changed */
@@ -222,5 +226,19 @@ int IterativeSolver(enum iter method, enum incpol which)
 	Timing_InitIter = 0;
 	Timing_MVP = clock() - t0;
 	Timing_OneIter = st.niter ? (clock() - t0) / st.niter : 0;
+	g_pvec_valid = 1;
 	return st.niter;
+}
+
+extern const enum scat ScatRelation;
+void __real_CalcField(doublecomplex ebuff[3], const double n[3]);
+
+void __wrap_CalcField(doublecomplex ebuff[3], const double n[3])
+{
+	if (g_ctx && g_pvec_valid && !surface && (ScatRelation == SQ_DRAINE || ScatRelation == SQ_FINDIP)) {
+		if (adda_gb300_scattered_fields(g_ctx, 1, 1, n, (double *)ebuff))
+			ERR("GPU CalcField failed: %s", adda_gb300_last_error());
+		return;
+	}
+	__real_CalcField(ebuff, n);
 }

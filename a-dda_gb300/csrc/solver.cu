@@ -1278,6 +1278,54 @@ __global__ void __launch_bounds__(NT) k_cross(const double2 *P, const uint16_t *
 	}
 }
 
+// scattering amplitudes (CalcFieldFree, crosssec.c:506-596), first stage: per block partial sums of
+// P_j exp(-i kd n.pos_j) for direction blockIdx.y and RHS blockIdx.z (6 doubles: Re/Im of the 3 components)
+__global__ void __launch_bounds__(NT) k_field(const double2 *P, const uint16_t *pos, size_t N, const double *dirs,
+	double kd, double *part)
+{
+	const int d = blockIdx.y, r = blockIdx.z, nb = gridDim.x;
+	const double n0 = dirs[3 * d], n1 = dirs[3 * d + 1], n2 = dirs[3 * d + 2];
+	double s[6] = {0, 0, 0, 0, 0, 0};
+	for (size_t j = blockIdx.x * (size_t)NT + threadIdx.x; j < N; j += (size_t)nb * NT) {
+		const double ph = -kd * (n0 * pos[3 * j] + n1 * pos[3 * j + 1] + n2 * pos[3 * j + 2]);
+		double sn, cs;
+		sincos(ph, &sn, &cs);
+		for (int c = 0; c < 3; c++) {
+			const double2 p = P[((size_t)r * N + j) * 3 + c];
+			s[2 * c] += p.x * cs - p.y * sn;
+			s[2 * c + 1] += p.x * sn + p.y * cs;
+		}
+	}
+	block_sum4(s, 4);
+	block_sum4(s + 4, 2);
+	if (threadIdx.x == 0) {
+		double *o = part + (((size_t)r * gridDim.y + d) * nb + blockIdx.x) * 6;
+		for (int k = 0; k < 6; k++) o[k] = s[k];
+	}
+}
+
+// second stage, one thread per (direction, RHS): fixed-order sum of the block partials, (I - nn), and the factor
+// (-i k^3) exp(-i k r0.n) with r0 the centre offset of the box's first dipole (make_particle.c:2305-2308)
+__global__ void k_field_fin(const double *part, int nb, int ndir, int R, const double *dirs, double k, double gs,
+	int bX, int bY, int bZ, double2 *out)
+{
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= ndir * R) return;
+	const int r = t / ndir, d = t % ndir;
+	const double n[3] = {dirs[3 * d], dirs[3 * d + 1], dirs[3 * d + 2]};
+	double2 sum[3] = {dc(0, 0), dc(0, 0), dc(0, 0)};
+	const double *p = part + ((size_t)r * ndir + d) * nb * 6;
+	for (int b = 0; b < nb; b++)
+		for (int c = 0; c < 3; c++) sum[c] = dadd(sum[c], dc(p[b * 6 + 2 * c], p[b * 6 + 2 * c + 1]));
+	const double2 dpr = dadd(dadd(dscal(sum[0], n[0]), dscal(sum[1], n[1])), dscal(sum[2], n[2]));
+	const double r0[3] = {-gs * (bX - 1) / 2.0, -gs * (bY - 1) / 2.0, -gs * (bZ - 1) / 2.0};
+	double sn, cs;
+	sincos(-k * (r0[0] * n[0] + r0[1] * n[1] + r0[2] * n[2]), &sn, &cs);
+	const double k3 = k * k * k;
+	const double2 amp = dc(sn * k3, -cs * k3); // -i k^3 (cs + i sn)
+	for (int c = 0; c < 3; c++) out[((size_t)r * ndir + d) * 3 + c] = dmul(amp, dsub(sum[c], dscal(dpr, n[c])));
+}
+
 // adjoint right-hand sides for the VJP (written as "incident fields" E so that the solver's b = S.E gives the scaled
 // system): E0_j = c_j incpol with c_j = (4pi/k^2)(-i k^3) exp(-i k r0.n) exp(-i kd n.pos_j)  (d Cext/d P_j), and
 // E1_j = conj(mu_j P_j) with mu_jc = -Im(1/alpha_jc) - 2k^3/3  (half the gradient of Cabs/(4 pi k) w.r.t. conj P)
@@ -2032,6 +2080,43 @@ int vjp_chi(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int rhs, const
 	cudaFree(save_cc32);
 	cudaFree(dF);
 	cudaFree(dg);
+	return rc;
+}
+
+int scattered_fields(adda_gb300_ctx *c, int R, int ndir, const double *dirs, double *ebuff)
+{
+	const size_t N = c->N;
+	cudaStream_t s = c->stream;
+	// blocks per (direction, RHS): at least 8 dipoles a thread, at most 128 blocks
+	const int nb = (int)std::max<size_t>(1, std::min<size_t>(128, (N + 8 * NT - 1) / (8 * NT)));
+	double *d_dirs = nullptr, *d_part = nullptr;
+	double2 *d_out = nullptr;
+	ADDA_CUDA(cudaMalloc(&d_dirs, sizeof(double) * 3 * ndir));
+	ADDA_CUDA(cudaMalloc(&d_part, sizeof(double) * 6 * (size_t)nb * ndir * R));
+	ADDA_CUDA(cudaMalloc(&d_out, sizeof(double2) * 3 * (size_t)ndir * R));
+	int rc = ADDA_GB300_OK;
+	if (cudaMemcpyAsync(d_dirs, dirs, sizeof(double) * 3 * ndir, cudaMemcpyHostToDevice, s) != cudaSuccess)
+		rc = ADDA_GB300_ECUDA;
+	if (!rc && N) {
+		k_field<<<dim3(nb, ndir, R), NT, 0, s>>>(c->pvec64, c->d_pos, N, d_dirs, c->k * c->gridspace, d_part);
+		if (cudaGetLastError() != cudaSuccess) rc = ADDA_GB300_ECUDA;
+		else count_launch();
+	}
+	if (!rc) {
+		if (!N) cudaMemsetAsync(d_part, 0, sizeof(double) * 6 * (size_t)nb * ndir * R, s);
+		k_field_fin<<<(ndir * R + 127) / 128, 128, 0, s>>>(d_part, nb, ndir, R, d_dirs, c->k, c->gridspace, c->bX,
+			c->bY, c->bZ, d_out);
+		if (cudaGetLastError() != cudaSuccess) rc = ADDA_GB300_ECUDA;
+		else count_launch();
+	}
+	if (!rc && (cudaMemcpyAsync(ebuff, d_out, sizeof(double2) * 3 * (size_t)ndir * R, cudaMemcpyDeviceToHost, s) !=
+					cudaSuccess ||
+				   cudaStreamSynchronize(s) != cudaSuccess))
+		rc = ADDA_GB300_ECUDA;
+	if (rc) set_error(std::string("scattered_fields: ") + cudaGetErrorString(cudaGetLastError()));
+	cudaFree(d_dirs);
+	cudaFree(d_part);
+	cudaFree(d_out);
 	return rc;
 }
 

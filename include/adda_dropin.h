@@ -18,6 +18,7 @@
 typedef double complex doublecomplex;
 enum iter { IT_BCGS2, IT_BICG_CS, IT_BICGSTAB, IT_CGNR, IT_CSYM, IT_QMR_CS, IT_QMR_CS_2 };
 enum incpol { INCPOL_Y, INCPOL_X };
+enum scat { SQ_DRAINE, SQ_FINDIP, SQ_IGT_SO, SQ_SO }; /* src/const.h:203-209 */
 #endif
 
 /* fftFit, src/fft.c:528 (fft.h:41): padded FFT size; called by ParSetup (comm.c:489-491) */
@@ -33,5 +34,10 @@ void MatVec(doublecomplex *argvec, doublecomplex *resultvec, double *inprod, boo
 	clock_t *comm_timing);
 /* IterativeSolver, src/iterative.c:1398: solves for Einc (host), leaves xvec and pvec (host), prints RE_ lines */
 int IterativeSolver(enum iter method, enum incpol which);
+/* CalcField, src/crosssec.c:801, reached through the linker's --wrap=CalcField (so the reference's crosssec.c stays
+ * unchanged): the scattering amplitude in direction n from the polarisations of the last IterativeSolver, on the GPU
+ * (CalcFieldFree, crosssec.c:506-596) for free space with the Draine/FINDIP relations; surface mode and the
+ * second-order relations go to the reference's own routine (__real_CalcField). */
+void __wrap_CalcField(doublecomplex ebuff[3], const double n[3]);
 
 #endif

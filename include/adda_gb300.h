@@ -181,6 +181,13 @@ int adda_gb300_solve_many(int nctx, adda_gb300_ctx *const *ctxs, const adda_gb30
 int adda_gb300_cross_sections(adda_gb300_ctx *ctx, int nrhs, const double *prop, const double *incpol,
 	double *cext, double *cabs);
 
+/* Scattering amplitudes, CalcField / CalcFieldFree (src/crosssec.c:506-596, 801-808; free space, Draine
+ * scattering relation), in FP64 on the device from the polarisations left by the last solve:
+ * E_r(n) = (-i k^3) exp(-i k r0.n) (I - nn).sum_j P_rj exp(-i kd n.pos_j) for each RHS r < nrhs and each unit
+ * direction n of dirs [ndir][3]; ebuff [nrhs][ndir][3] complex (interleaved re, im). The reference's callers
+ * (CalcEplaneYZ and friends, CalculateE.c:423-500) turn these into Mueller matrices; so does the Python layer. */
+int adda_gb300_scattered_fields(adda_gb300_ctx *ctx, int nrhs, int ndir, const double *dirs, double *ebuff);
+
 /* average device time of one matvec (prec, nrhs RHS, device-resident random input) over iters launches, measured
  * with CUDA events on the context's stream after one warm-up launch; flush_bytes > 0 writes that many bytes of a
  * scratch buffer between launches so every launch starts with a cold L2 */

@@ -861,26 +861,37 @@ int or_solve(or_ctx *c, int method, const double *einc, double eps, int maxiter,
 /* ExtCross (plane wave, free space) via CalcFieldFree, src/crosssec.c:506-596, 811-822; AbsCross (Draine),
  * src/crosssec.c:852-917. Positions are taken relative to the first dipole of the box, whose centre is at
  * box_origin = -gridspace*((boxX-1)/2, (boxY-1)/2, (boxZ-1)/2) (make_particle.c:2305-2308). */
-void or_cross(or_ctx *c, const double *pvec, const double prop[3], const double incpol[3], double *cext,
-	double *cabs)
+/* CalcFieldFree, src/crosssec.c:506-596: scattering amplitude ebuff = (-i k^3) exp(-ik r0.n) (I - nn).sum_j P_j
+ * exp(-i kd n.pos_j) for the direction n (unit vector), with r0 the box origin (make_particle.c:2305-2308) */
+void or_field(const or_ctx *c, const double *pvec, const double n[3], double *ebuff)
 {
 	const cplx *P = (const cplx *)pvec;
 	const double kd = c->k * c->gridspace;
 	cplx sum[3] = {0, 0, 0};
 	for (size_t j = 0; j < c->n; j++) {
-		double ph = -kd * (prop[0] * c->pos[3 * j] + prop[1] * c->pos[3 * j + 1] + prop[2] * c->pos[3 * j + 2]);
+		double ph = -kd * (n[0] * c->pos[3 * j] + n[1] * c->pos[3 * j + 1] + n[2] * c->pos[3 * j + 2]);
 		cplx a = cos(ph) + I * sin(ph);
 		for (int i = 0; i < 3; i++) sum[i] += P[3 * j + i] * a;
 	}
-	cplx dpr = sum[0] * prop[0] + sum[1] * prop[1] + sum[2] * prop[2];
-	cplx tb[3];
-	for (int i = 0; i < 3; i++) tb[i] = sum[i] - dpr * prop[i];
+	cplx dpr = sum[0] * n[0] + sum[1] * n[1] + sum[2] * n[2];
 	double r0[3] = {-c->gridspace * (c->bX - 1) / 2.0, -c->gridspace * (c->bY - 1) / 2.0,
 		-c->gridspace * (c->bZ - 1) / 2.0};
-	double ph0 = -c->k * (r0[0] * prop[0] + r0[1] * prop[1] + r0[2] * prop[2]);
+	double ph0 = -c->k * (r0[0] * n[0] + r0[1] * n[1] + r0[2] * n[2]);
 	cplx amp = -I * (cos(ph0) + I * sin(ph0)) * (c->k * c->k * c->k);
+	cplx *e = (cplx *)ebuff;
+	for (int i = 0; i < 3; i++) e[i] = amp * (sum[i] - dpr * n[i]);
+}
+
+/* ExtCross (plane wave, free space) via CalcField in the propagation direction, src/crosssec.c:811-822; AbsCross
+ * (Draine), src/crosssec.c:852-917 */
+void or_cross(or_ctx *c, const double *pvec, const double prop[3], const double incpol[3], double *cext,
+	double *cabs)
+{
+	const cplx *P = (const cplx *)pvec;
+	cplx e[3];
+	or_field(c, pvec, prop, (double *)e);
 	double s = 0;
-	for (int i = 0; i < 3; i++) s += creal(amp * tb[i] * incpol[i]);
+	for (int i = 0; i < 3; i++) s += creal(e[i] * incpol[i]);
 	*cext = s * 4 * M_PI / (c->k * c->k);
 	const double t1 = 2 * c->k * c->k * c->k / 3;
 	double sa = 0;

@@ -10,6 +10,7 @@
  *                                               BiCG_CS :490-637, CGNR :729-769, CSYM :773-892,
  *                                               QMR_CS_2 :1038-1132, BCGS2 :340-487
  *   or_cross         <- ExtCross / AbsCross      src/crosssec.c:811-917 (plane wave, free space, Draine)
+ *   or_field         <- CalcFieldFree            src/crosssec.c:506-596 (scattering amplitude in one direction)
  * Complex vectors are interleaved (re,im) doubles, dipole-major [dipole][3], like the reference's doublecomplex.
  */
 #ifndef ADDA_ORACLE_H
@@ -41,5 +42,6 @@ int or_solve(or_ctx *c, int method, const double *einc, double eps, int maxiter,
 	double *xvec, double *pvec, double *resid_hist, int hist_cap, int *niter_out);
 void or_cross(or_ctx *c, const double *pvec, const double prop[3], const double incpol[3], double *cext,
 	double *cabs);
+void or_field(const or_ctx *c, const double *pvec, const double n[3], double *ebuff);
 
 #endif

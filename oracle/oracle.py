@@ -56,6 +56,7 @@ def lib():
         L.or_solve.argtypes = [c_p, c_i, c_p, c_d, c_i, c_i, c_p, c_p, c_p, c_i, c_p]
         L.or_solve.restype = c_i
         L.or_cross.argtypes = [c_p, c_p, c_p, c_p, c_p, c_p]
+        L.or_field.argtypes = [c_p, c_p, c_p, c_p]
         _lib = L
     return _lib
 
@@ -131,6 +132,14 @@ class Oracle:
         ce, ca = ctypes.c_double(0), ctypes.c_double(0)
         self.L.or_cross(self.h, _ptr(pvec), _ptr(prop), _ptr(incpol), ctypes.byref(ce), ctypes.byref(ca))
         return ce.value, ca.value
+
+    def field(self, pvec, n):
+        """scattering amplitude (CalcFieldFree) for the unit direction n: complex [3]"""
+        pvec = np.ascontiguousarray(pvec, dtype=np.complex128)
+        n = np.ascontiguousarray(n, dtype=np.float64)
+        e = np.zeros(3, np.complex128)
+        self.L.or_field(self.h, _ptr(pvec), _ptr(n), _ptr(e))
+        return e
 
 
 def fftfit(x, divis=1):

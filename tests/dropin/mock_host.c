@@ -33,6 +33,10 @@ doublecomplex cc_sqrt[15][3];
 doublecomplex *xvec, *pvec, *Einc;
 double iter_eps = 1e-5;
 enum init_field InitField = IF_AUTO;
+enum scat ScatRelation = SQ_DRAINE;
+/* the reference's CalcField lives in another object (mock_crosssec.c, like crosssec.c), so that this file's calls
+ * go through the linker's --wrap=CalcField */
+void CalcField(doublecomplex ebuff[3], const double n[3]);
 bool recalc_resid = true;
 clock_t Timing_Dm_Init, Timing_FFT_Init, Timing_OneIter, Timing_InitIter, Timing_MVP;
 size_t TotalIter, TotalMatVec;
@@ -115,6 +119,13 @@ int main(int argc, char **argv)
 	fwrite(&ip, sizeof(ip), 1, f);
 	fwrite(pvec, sizeof(doublecomplex), local_nRows, f);
 	fwrite(y, sizeof(doublecomplex), local_nRows, f);
+	/* scattered fields through the reference's CalcField call (wrapped at link time): forward and two more */
+	const double dirs[3][3] = {{prop[0], prop[1], prop[2]}, {0.6, 0.0, 0.8}, {0.0, -1.0, 0.0}};
+	for (int d = 0; d < 3; d++) {
+		doublecomplex e[3];
+		CalcField(e, dirs[d]);
+		fwrite(e, sizeof(doublecomplex), 3, f);
+	}
 	fclose(f);
 	Free_FFT_Dmat();
 	printf("mock host: %lld dipoles, %d iterations, %zu matvecs\n", n, niter, TotalMatVec);

@@ -76,6 +76,11 @@ CASES = [
      dict(grid=16, m=1.5, dpl=10, iter="qmr2")),
     ("ell_qmr2_eps8", ["-iter", "qmr2", "-eps", "8"] + ELL + MGN,
      dict(grid=8, m=1.1 + 0.1j, shape="ellipsoid", pars=(0.5, 1.5), iter="qmr2", eps=1e-8)),
+    # scattered fields: the Mueller matrix in the yz plane every 10 degrees (-ntheta 18)
+    ("mueller_c1", ["-grid", "16", "-dpl", "10", "-m", "1.5", "0", "-eps", "10", "-ntheta", "18"],
+     dict(grid=16, m=1.5, dpl=10, eps=1e-10)),
+    ("mueller_ell", ["-orient", "10", "20", "30", "-eps", "10", "-ntheta", "18"] + ELL + MGN,
+     dict(grid=8, m=1.1 + 0.1j, shape="ellipsoid", pars=(0.5, 1.5), orient=(10, 20, 30), eps=1e-10)),
     ("mgn_bcgs2", ["-iter", "bcgs2"] + MGN, dict(grid=8, m=1.1 + 0.1j, iter="bcgs2")),
     ("c1_bcgs2", ["-grid", "16", "-dpl", "10", "-m", "1.5", "0", "-iter", "bcgs2", "-eps", "5"],
      dict(grid=16, m=1.5, dpl=10, iter="bcgs2")),
@@ -113,6 +118,10 @@ def parse_run(rundir, stdout):
                            Cabs=float(re.search(r"Cabs\s*=\s*([-+0-9.eE]+)", txt).group(1)))
     out["cross"] = cs
     out["maxiter_warning"] = "haven't converged" in stdout + log
+    mf = os.path.join(rundir, "mueller")
+    if os.path.exists(mf) and "-ntheta" in open(os.path.join(rundir, "log")).read():
+        rows = [l.split() for l in open(mf).read().splitlines()[1:] if l.strip()]
+        out["mueller"] = [[float(v) for v in r] for r in rows]  # theta, s11 s12 ... s44
     return out
 
 

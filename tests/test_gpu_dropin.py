@@ -20,8 +20,9 @@ def build_mock():
     inc = os.path.join(ROOT, "include")
     subprocess.run(["gcc", "-std=gnu11", "-O2", "-fcommon", "-I", inc, "-o", exe,
                     os.path.join(ROOT, "tests", "dropin", "mock_host.c"),
+                    os.path.join(ROOT, "tests", "dropin", "mock_crosssec.c"),
                     os.path.join(ROOT, "a-dda_gb300", "csrc", "dropin", "adda_dropin.c"),
-                    "-L" + BUILD, "-ladda_gb300", "-Wl,-rpath," + BUILD, "-lm"], check=True)
+                    "-L" + BUILD, "-ladda_gb300", "-Wl,-rpath," + BUILD, "-Wl,--wrap=CalcField", "-lm"], check=True)
     return exe
 
 
@@ -39,7 +40,7 @@ def test_dropin_solve_and_matvec(tmp_path, method):
     niter = int(np.frombuffer(raw[8:12], np.int32)[0])
     ip = float(np.frombuffer(raw[12:20], np.float64)[0])
     vec = np.frombuffer(raw[20:], np.complex128)
-    pv, y = vec[:3 * n], vec[3 * n:]
+    pv, y, fields = vec[:3 * n], vec[3 * n:6 * n], vec[6 * n:].reshape(3, 3)
     s = setup_for(dict(grid=16, m=1.5, dpl=10))
     assert n == s.n
     o = oracle_for(s)
@@ -51,3 +52,7 @@ def test_dropin_solve_and_matvec(tmp_path, method):
     yr, ipr = o.matvec(s.einc[0])
     assert np.linalg.norm(y - yr) / np.linalg.norm(yr) < 1e-13
     assert abs(ip / ipr - 1) < 1e-12
+    # CalcField through the link-time wrapper, on the GPU, against the oracle's field of the same polarisations
+    for d, n_ in enumerate([s.prop, (0.6, 0.0, 0.8), (0.0, -1.0, 0.0)]):
+        eo = o.field(pv, np.asarray(n_, dtype=float))
+        assert np.linalg.norm(fields[d] - eo) <= 1e-12 * np.linalg.norm(eo), (d, fields[d], eo)
