@@ -245,7 +245,8 @@ __global__ void d2f_k(float2 *dst, const double2 *src, size_t n);
 
 // The FP32 matvec's chunk (x-slabs whose z-transformed data pass through L2 between K2a, K2b and K2c) trades L2
 // residency against launch count and tail waves; its best size depends on the grid and the RHS count. Measured once
-// per context on its own data sizes: budgets of 24..CHUNK_TUNE_MAX_MB, one warm-up and two timed matvecs each with
+// per context on its own data sizes: balanced splits of the x-slabs into chunks of 24..CHUNK_TUNE_MAX_MB, one
+// warm-up and two timed matvecs each with
 // Rmax RHS of random data (CUDA events on the context stream); the fastest is kept. Runs from check_ready, i.e.
 // only once the D matrix and the polarisability buffers a matvec reads exist, and before any graph capture.
 static int tune_chunks(adda_gb300_ctx *c)
@@ -268,12 +269,16 @@ static int tune_chunks(adda_gb300_ctx *c)
 	cudaEvent_t e0, e1;
 	ADDA_CUDA(cudaEventCreate(&e0));
 	ADDA_CUDA(cudaEventCreate(&e1));
-	const int mbs[] = {24, 48, 64, 96, CHUNK_TUNE_MAX_MB};
+	// candidates: the gX x-slabs split into nc balanced chunks (no small tail chunk), from the largest chunk that
+	// fits the Tz buffer down to about 24 MB
 	int best_ck = c->CK32, last = -1, rc = ADDA_GB300_OK;
 	float best = 1e30f;
-	for (int mb : mbs) {
-		const int ck = (int)std::max<size_t>(1, std::min<size_t>(c->CK32max, ((size_t)mb << 20) / (slab * sizeof(float2))));
-		if (ck == last) continue;
+	const size_t min_ck = std::max<size_t>(1, ((size_t)24 << 20) / (slab * sizeof(float2)));
+	for (int nc = 1; nc <= c->gX; nc++) {
+		const int ck = (c->gX + nc - 1) / nc;
+		if (ck > c->CK32max) continue;
+		if (last > 0 && 5 * ck > 4 * last) continue; // next candidate at least 20 % smaller
+		if ((size_t)ck < min_ck && last > 0) break;
 		last = ck;
 		c->CK32 = ck;
 		if ((rc = matvec_run<float>(c, c->Rmax, in, out, 0, e, nullptr))) break;
