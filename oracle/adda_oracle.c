@@ -24,6 +24,7 @@ struct or_ctx {
 	uint16_t *pos;       // [n][3] grid coordinates
 	uint8_t *mat;        // [n] material index
 	double gridspace, k;
+	int inter;           // 0 point dipoles, 1 FCD, 2 static FCD
 	size_t DsY, DsZ;     // reduced D sizes (fft.c:955-963)
 	cplx *D;             // [gX][DsZ][DsY][6]
 	int per_dip, nmat;
@@ -104,6 +105,78 @@ static void green_poi(const or_ctx *c, int i, int j, int k, cplx g[6])
 	}
 }
 
+/* Ci(x) = gamma + ln x + sum_k (-1)^k x^(2k)/(2k (2k)!), Si(x) = sum_k (-1)^k x^(2k+1)/((2k+1)(2k+1)!) for x <= 3;
+ * for larger x from the exponential integral E1(ix) = -Ci(x) + i(Si(x) - pi/2) (Abramowitz & Stegun 5.2.23), whose
+ * continued fraction E1(z) = exp(-z)/(z+1- 1/(z+3- 4/(z+5- ...))) is evaluated by the modified Lentz method */
+void or_cisi(double x, double *ci, double *si)
+{
+	const double euler = 0.57721566490153286061;
+	if (x <= 3) {
+		double sc = 0, ss = 0, term = 1; // term = x^n / n!
+		for (int n = 1; n < 80; n++) {
+			term *= x / n;
+			if (n % 2) ss += ((n / 2) % 2 ? -1 : 1) * term / n;
+			else sc += ((n / 2) % 2 ? -1 : 1) * term / n;
+			if (term < 1e-18 * (fabs(ss) + fabs(sc) + 1)) break;
+		}
+		*ci = euler + log(x) + sc;
+		*si = ss;
+		return;
+	}
+	const cplx z = I * x;
+	cplx b = z + 1, cc = 1e300, d = 1 / b, h = d;
+	for (int i = 1; i < 10000; i++) {
+		const double a = -(double)i * i;
+		b += 2;
+		d = 1 / (a * d + b);
+		cc = b + a / cc;
+		const cplx del = cc * d;
+		h *= del;
+		if (cabs(del - 1) < 1e-16) break;
+	}
+	h *= cos(x) - I * sin(x); // E1(ix)
+	*ci = -creal(h);
+	*si = M_PI / 2 + cimag(h);
+}
+
+void or_set_interaction(or_ctx *c, int relation)
+{
+	c->inter = relation;
+}
+
+/* FCD corrections of the point-dipole term, InterTerm_fcd / InterTerm_fcd_st, src/interaction.c:335-411
+ * (Gay-Balmaz & Martin 2002, Piller 1998): with k_F = pi/d, kfr = pi*|q| */
+static void green_fcd(const or_ctx *c, int i, int j, int k, cplx g[6])
+{
+	green_poi(c, i, j, k, g);
+	const double rn = sqrt((double)i * i + (double)j * j + (double)k * k);
+	const double rr = rn * c->gridspace, invr3 = 1 / (rr * rr * rr), kr = c->k * rr, kr2 = kr * kr;
+	const double kfr = M_PI * rn;
+	const double ce = cos(kfr), se = sin(kfr);
+	if (c->inter == 2) {
+		double ci, si;
+		or_cisi(kfr, &ci, &si);
+		const double brd = 2 / (3 * M_PI) * (3 * si + kfr * ce - 4 * se);
+		for (int a = 0; a < 6; a++) g[a] *= brd;
+		return;
+	}
+	const cplx ev = invr3 * (cos(kr) + I * sin(kr));
+	double ci1, si1, ci2, si2;
+	or_cisi(kfr + kr, &ci1, &si1);
+	or_cisi(kfr - kr, &ci2, &si2);
+	const double ci = ci1 - ci2, si = M_PI - si1 - si2;
+	const double g0 = (cimag(ev) * ci + creal(ev) * si) / M_PI;
+	const double g2 = (kr * (creal(ev) * ci - cimag(ev) * si) + 2.0 / 3 * invr3 * (kfr * ce - 4 * se)) / M_PI - g0;
+	const double t = g0 * kr2;
+	const double q[3] = {i / rn, j / rn, k / rn};
+	const double qm[6] = {q[0] * q[0], q[0] * q[1], q[0] * q[2], q[1] * q[1], q[1] * q[2], q[2] * q[2]};
+	for (int a = 0; a < 6; a++) {
+		double brd = qm[a] * (t + 3 * g2);
+		if (a == 0 || a == 3 || a == 5) brd -= t + g2;
+		g[a] += brd;
+	}
+}
+
 size_t or_dmatrix_len(const or_ctx *c)
 {
 	return (size_t)c->gX * c->DsZ * c->DsY * 6;
@@ -127,7 +200,8 @@ void or_init_dmatrix(or_ctx *c)
 			for (int i = 1 - bX; i < bX; i++) {
 				if (!i && !j && !k) continue;
 				cplx g[6];
-				green_poi(c, i, j, k, g);
+				if (c->inter) green_fcd(c, i, j, k, g);
+				else green_poi(c, i, j, k, g);
 				size_t idx = ((size_t)k * bY + j) * gX + (i < 0 ? i + gX : i);
 				for (int a = 0; a < 6; a++) G[a * lines * gX + idx] = g[a];
 			}

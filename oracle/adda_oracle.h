@@ -31,6 +31,11 @@ int or_fftfit(int x, int divis);
 or_ctx *or_create(int boxX, int boxY, int boxZ, int gridX, int gridY, int gridZ, size_t nvoid,
 	const uint16_t *position, const uint8_t *material, double gridspace, double wavenum, int nthreads);
 void or_free(or_ctx *c);
+/* interaction term of D: 0 point dipoles (InterTerm_poi), 1 FCD (InterTerm_fcd), 2 static FCD (InterTerm_fcd_st),
+ * src/interaction.c:315-411; set before or_init_dmatrix */
+void or_set_interaction(or_ctx *c, int relation);
+/* cosine and sine integrals Ci(x), Si(x) for x > 0 (the reference's cisi, sinint.c) */
+void or_cisi(double x, double *ci, double *si);
 void or_init_dmatrix(or_ctx *c);
 size_t or_dmatrix_len(const or_ctx *c);        // complex elements, layout [x][z<DsizeZ][y<DsizeY][6]
 void or_get_dmatrix(const or_ctx *c, double *out);

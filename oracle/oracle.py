@@ -55,6 +55,8 @@ def lib():
         L.or_matvec.argtypes = [c_p, c_p, c_p, c_p, c_i]
         L.or_solve.argtypes = [c_p, c_i, c_p, c_d, c_i, c_i, c_p, c_p, c_p, c_i, c_p]
         L.or_solve.restype = c_i
+        L.or_set_interaction.argtypes = [c_p, ctypes.c_int]
+        L.or_cisi.argtypes = [ctypes.c_double, c_p, c_p]
         L.or_cross.argtypes = [c_p, c_p, c_p, c_p, c_p, c_p]
         L.or_field.argtypes = [c_p, c_p, c_p, c_p]
         _lib = L
@@ -68,7 +70,7 @@ def _ptr(a):
 class Oracle:
     """One particle lattice on the CPU: D matrix, matvec, QMR_CS/BiCGStab and Cext/Cabs in double precision."""
 
-    def __init__(self, box, grid, position, material, gridspace, wavenum, nthreads=0):
+    def __init__(self, box, grid, position, material, gridspace, wavenum, nthreads=0, interaction="poi"):
         self.L = lib()
         self.position = np.ascontiguousarray(position, dtype=np.uint16).reshape(-1, 3)
         self.material = np.ascontiguousarray(material if material is not None
@@ -77,6 +79,7 @@ class Oracle:
         self.box, self.grid = tuple(box), tuple(grid)
         self.h = self.L.or_create(*box, *grid, self.n, _ptr(self.position), _ptr(self.material),
                                   gridspace, wavenum, nthreads)
+        self.L.or_set_interaction(self.h, {"poi": 0, "fcd": 1, "fcd_st": 2}[interaction])
         self.L.or_init_dmatrix(self.h)
 
     def close(self):

@@ -80,7 +80,12 @@ int main(int argc, char **argv)
 	if (argc < 8) return 2;
 	const int grid = atoi(argv[1]);
 	const double mre = atof(argv[2]), mim = atof(argv[3]), dpl = atof(argv[4]);
-	const enum iter method = strcmp(argv[5], "bicgstab") ? IT_QMR_CS : IT_BICGSTAB;
+	/* -iter names of param.c:1232-1238 */
+	const char *names[] = {"bcgs2", "bicg", "bicgstab", "cgnr", "csym", "qmr", "qmr2"};
+	const enum iter ids[] = {IT_BCGS2, IT_BICG_CS, IT_BICGSTAB, IT_CGNR, IT_CSYM, IT_QMR_CS, IT_QMR_CS_2};
+	enum iter method = IT_QMR_CS;
+	for (int i = 0; i < 7; i++)
+		if (!strcmp(argv[5], names[i])) method = ids[i];
 	iter_eps = pow(10, -atof(argv[6]));
 	logfile = stdout;
 	CheckNprocs();

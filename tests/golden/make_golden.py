@@ -81,6 +81,19 @@ CASES = [
      dict(grid=16, m=1.5, dpl=10, eps=1e-10)),
     ("mueller_ell", ["-orient", "10", "20", "30", "-eps", "10", "-ntheta", "18"] + ELL + MGN,
      dict(grid=8, m=1.1 + 0.1j, shape="ellipsoid", pars=(0.5, 1.5), orient=(10, 20, 30), eps=1e-10)),
+    # the other polarizability prescriptions (-pol) and interaction terms (-int)
+    ("pol_cldr", ["-pol", "cldr", "-prop", "1", "2", "3"] + MGN, dict(grid=8, m=1.1 + 0.1j, pol="cldr", prop=(1, 2, 3))),
+    ("pol_fcd", ["-pol", "fcd"] + MGN, dict(grid=8, m=1.1 + 0.1j, pol="fcd")),
+    ("pol_igt_so", ["-pol", "igt_so"] + MGN, dict(grid=8, m=1.1 + 0.1j, pol="igt_so")),
+    ("pol_lak", ["-pol", "lak"] + MGN, dict(grid=8, m=1.1 + 0.1j, pol="lak")),
+    ("pol_so", ["-pol", "so"] + MGN, dict(grid=8, m=1.1 + 0.1j, pol="so")),
+    ("int_fcd", ["-int", "fcd", "-pol", "fcd"] + MGN, dict(grid=8, m=1.1 + 0.1j, pol="fcd", interaction="fcd")),
+    ("int_fcd_st", ["-int", "fcd_st", "-pol", "fcd"] + MGN,
+     dict(grid=8, m=1.1 + 0.1j, pol="fcd", interaction="fcd_st")),
+    ("c1_fcd", ["-grid", "16", "-dpl", "10", "-m", "1.5", "0", "-int", "fcd", "-pol", "fcd", "-eps", "5"],
+     dict(grid=16, m=1.5, dpl=10, pol="fcd", interaction="fcd")),
+    ("ell_fcd_eps8", ["-int", "fcd", "-pol", "fcd", "-eps", "8"] + ELL + MGN,
+     dict(grid=8, m=1.1 + 0.1j, shape="ellipsoid", pars=(0.5, 1.5), pol="fcd", interaction="fcd", eps=1e-8)),
     ("mgn_bcgs2", ["-iter", "bcgs2"] + MGN, dict(grid=8, m=1.1 + 0.1j, iter="bcgs2")),
     ("c1_bcgs2", ["-grid", "16", "-dpl", "10", "-m", "1.5", "0", "-iter", "bcgs2", "-eps", "5"],
      dict(grid=16, m=1.5, dpl=10, iter="bcgs2")),
@@ -96,8 +109,11 @@ def parse_run(rundir, stdout):
     out["ndip"] = int(re.search(r"Total number of occupied dipoles: (\d+)", log).group(1))
     out["box"] = [int(v) for v in re.search(r"box dimensions: (\d+)x(\d+)x(\d+)", log).groups()]
     out["grid"] = [int(v) for v in re.search(r"The FFT grid is: (\d+)x(\d+)x(\d+)", log).groups()]
-    out["cc"] = [[float(a), float(b)] for a, b in
-                 re.findall(r"CoupleConstant:([-+]?[0-9.]+(?:[eE][-+]?\d+)?)([-+][0-9.]+(?:[eE][-+]?\d+)?)i", log)]
+    num = r"([-+]?[0-9.]+(?:[eE][-+]?\d+)?)([-+][0-9.]+(?:[eE][-+]?\d+)?)i"
+    out["cc"] = [[float(a), float(b)] for a, b in re.findall(r"CoupleConstant:" + num, log)]
+    # anisotropic prescriptions print the three diagonal components: CoupleConstant:(a+bi,c+di,e+fi)
+    out["cc3"] = [[[float(a), float(b)] for a, b in re.findall(num, grp)]
+                  for grp in re.findall(r"CoupleConstant:\(([^)]*)\)", log)]
     hist = {}
     cur = None
     for line in log.splitlines():

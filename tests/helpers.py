@@ -7,7 +7,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden", "reference_runs.json")
 
-SETUP_KEYS = ("grid", "shape", "pars", "m", "dpl", "size", "pol", "orient", "avgpol", "prop")
+SETUP_KEYS = ("grid", "shape", "pars", "m", "dpl", "size", "pol", "orient", "avgpol", "prop", "interaction")
 
 
 def golden():
@@ -37,7 +37,8 @@ def solver_opts(kw):
 
 def oracle_for(s, nthreads=0):
     from oracle import oracle as O
-    o = O.Oracle(s.box, s.grid, s.pos, s.mat, s.gridspace, s.wavenum, nthreads)
+    o = O.Oracle(s.box, s.grid, s.pos, s.mat, s.gridspace, s.wavenum, nthreads,
+                 interaction=getattr(s, "interaction", "poi"))
     return o
 
 

