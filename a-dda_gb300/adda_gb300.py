@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libadda_gb300.so")
 
 SHAPES = {"sphere": 0, "ellipsoid": 1, "box": 2}
-POLS = {"ldr": 0, "cm": 1, "rrc": 2, "dgf": 3}
+POLS = {"ldr": 0, "cm": 1, "rrc": 2, "dgf": 3, "cldr": 4, "fcd": 5, "igt_so": 6, "lak": 7, "so": 8}
 ITERS = {"qmr": 0, "bicgstab": 1, "bicg": 2, "cgnr": 3, "csym": 4, "qmr2": 5, "bcgs2": 6}
 PREC = {"fp64": 0, "fp32": 1, "mixed": 2, "mixed_f32vec": 3, "mixed_f64vec": 4}
 INIT = {"auto": 0, "zero": 1, "inc": 2}
@@ -31,7 +31,10 @@ class Problem(ctypes.Structure):
                 ("gridX", ctypes.c_int), ("gridY", ctypes.c_int), ("gridZ", ctypes.c_int),
                 ("ndip", ctypes.c_size_t), ("position", ctypes.c_void_p), ("material", ctypes.c_void_p),
                 ("gridspace", ctypes.c_double), ("wavenum", ctypes.c_double), ("nrhs_max", ctypes.c_int),
-                ("device", ctypes.c_int)]
+                ("device", ctypes.c_int), ("interaction", ctypes.c_int)]
+
+
+INTERACTIONS = {"poi": 0, "fcd": 1, "fcd_st": 2}
 
 
 class SolveParams(ctypes.Structure):
@@ -193,7 +196,8 @@ class Setup:
     Order of the RHS: Y polarisation first, then X (calculator.c:309-330)."""
 
     def __init__(self, grid=16, shape="sphere", pars=None, m=1.5, dpl=None, size=None, pol="ldr", orient=(0, 0, 0),
-                 avgpol=False, prop=None, lam=2 * math.pi):
+                 avgpol=False, prop=None, lam=2 * math.pi, interaction="poi"):
+        self.interaction = interaction
         self.box, self.pos, self.mat = make_particle(shape, grid, pars)
         self.n = len(self.pos)
         self.grid = (fft_fit(2 * self.box[0]), fft_fit(2 * self.box[1]), fft_fit(2 * self.box[2], 2))
@@ -241,14 +245,15 @@ def solve_many(ctxs, eincs, method="qmr", prec="mixed", eps=1e-5, maxiter=100000
 class Context:
     """One particle lattice on one GPU: the interaction matrix, FP64/FP32 matvecs, solver and cross sections."""
 
-    def __init__(self, box, pos, mat, gridspace, wavenum, grid=(0, 0, 0), nrhs_max=2, device=0):
+    def __init__(self, box, pos, mat, gridspace, wavenum, grid=(0, 0, 0), nrhs_max=2, device=0, interaction="poi"):
         self.L = lib()
         self.pos = np.ascontiguousarray(pos, dtype=np.uint16).reshape(-1, 3)
         self.mat = None if mat is None else np.ascontiguousarray(mat, dtype=np.uint8)
         self.n = len(self.pos)
         self.nrhs_max = nrhs_max
         pr = Problem(box[0], box[1], box[2], grid[0], grid[1], grid[2], self.n, _p(self.pos).value,
-                     None if self.mat is None else _p(self.mat).value, gridspace, wavenum, nrhs_max, device)
+                     None if self.mat is None else _p(self.mat).value, gridspace, wavenum, nrhs_max, device,
+                     INTERACTIONS[interaction])
         self.h = ctypes.c_void_p()
         _check(self.L.adda_gb300_create(ctypes.byref(pr), ctypes.byref(self.h)), "create")
         g = (ctypes.c_int * 3)()
@@ -257,7 +262,7 @@ class Context:
 
     @classmethod
     def from_setup(cls, s, nrhs_max=2, device=0):
-        c = cls(s.box, s.pos, s.mat, s.gridspace, s.wavenum, s.grid, nrhs_max, device)
+        c = cls(s.box, s.pos, s.mat, s.gridspace, s.wavenum, s.grid, nrhs_max, device, s.interaction)
         c.init_dmatrix()
         for r in range(min(nrhs_max, len(s.cc))):
             c.set_cc(r, s.cc[r].reshape(1, 3))

@@ -58,6 +58,7 @@ struct adda_gb300_ctx {
 	int bX = 0, bY = 0, bZ = 0, gX = 0, gY = 0, gZ = 0, DsY = 0, DsZ = 0;
 	size_t N = 0;
 	int Rmax = 1;
+	int interaction = 0; // enum adda_gb300_inter
 	double gridspace = 0, k = 0;
 	// lattice (host and device)
 	std::vector<uint16_t> pos;

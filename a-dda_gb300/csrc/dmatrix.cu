@@ -1,6 +1,7 @@
 // dmatrix.cu - the interaction matrix D = -FFT(G)/Ngrid on the GPU in FP64 (InitDmatrix, src/fft.c:918-1416).
 //
-//   1. green_fill      : point-dipole Green's tensor (interaction.c:290-331) for every lattice offset
+//   1. green_fill      : point-dipole Green's tensor (interaction.c:290-331), optionally with the FCD corrections
+//                        (interaction.c:335-411), for every lattice offset
 //                        (i in (-bX,bX), j in [0,bY), k in [0,bZ)), stored per component as [k][j][i mod gX]
 //   2. fft_lines (x)   : forward FFT along x of every (component, k, j) line
 //   3. per component   : slice_fill mirrors the (j,k) quarter into the full (y,z) plane of every kx with the
@@ -15,7 +16,60 @@ namespace adda {
 
 namespace {
 
-__global__ void green_fill(double2 *G, int bX, int bY, int bZ, int gX, double gridspace, double k)
+// cosine and sine integrals for x > 0: power series up to x = 2, above it the continued fraction of the exponential
+// integral E1(ix) = -Ci(x) + i(Si(x) - pi/2) (Abramowitz & Stegun 5.2.23) by the modified Lentz method
+__device__ void cisi_d(double x, double &ci, double &si)
+{
+	if (x <= 2) {
+		double sc = 0, ss = 0, term = 1; // x^n / n!
+		for (int n = 1; n < 60; n++) {
+			term *= x / n;
+			const double sg = ((n >> 1) & 1) ? -1.0 : 1.0;
+			if (n & 1) ss += sg * term / n;
+			else sc += sg * term / n;
+			if (term < 1e-18) break;
+		}
+		ci = 0.57721566490153286061 + log(x) + sc;
+		si = ss;
+		return;
+	}
+	// complex arithmetic on (re, im) pairs; z = i x
+	double br = 1, bi = x;                       // b = z + 1
+	double dr, di;                               // d = 1/b
+	{
+		const double m = br * br + bi * bi;
+		dr = br / m;
+		di = -bi / m;
+	}
+	double cr = 1e300, ci2 = 0, hr = dr, hi = di; // c, h
+	for (int i = 1; i < 10000; i++) {
+		const double a = -(double)i * i;
+		br += 2;
+		// d = 1/(a d + b)
+		const double tr = a * dr + br, ti = a * di + bi, m = tr * tr + ti * ti;
+		dr = tr / m;
+		di = -ti / m;
+		// c = b + a/c
+		const double cm = cr * cr + ci2 * ci2;
+		const double qr = br + a * cr / cm, qi = bi - a * ci2 / cm;
+		cr = qr;
+		ci2 = qi;
+		// del = c d; h *= del
+		const double er = cr * dr - ci2 * di, ei = cr * di + ci2 * dr;
+		const double nr = hr * er - hi * ei, ni = hr * ei + hi * er;
+		hr = nr;
+		hi = ni;
+		if (fabs(er - 1) + fabs(ei) < 1e-16) break;
+	}
+	double sn, cs;
+	sincos(x, &sn, &cs);
+	// E1(ix) = h exp(-ix)
+	const double e1r = hr * cs + hi * sn, e1i = hi * cs - hr * sn;
+	ci = -e1r;
+	si = 1.57079632679489661923 + e1i;
+}
+
+__global__ void green_fill(double2 *G, int bX, int bY, int bZ, int gX, double gridspace, double k, int inter)
 {
 	const size_t lines = (size_t)bZ * bY;
 	const size_t total = lines * gX;
@@ -55,6 +109,34 @@ __global__ void green_fill(double2 *G, int bX, int bY, int bZ, int gX, double gr
 					im = t2 * qm[a];
 				}
 				g[a] = make_double2(re * evr - im * evi, re * evi + im * evr);
+			}
+			if (inter) {
+				// FCD corrections of the real part (InterTerm_fcd / _fcd_st, interaction.c:335-411): k_F = pi/d
+				const double kfr = 3.14159265358979323846 * rn;
+				double sf, cf;
+				sincos(kfr, &sf, &cf);
+				if (inter == 2) {
+					double cI, sI;
+					cisi_d(kfr, cI, sI);
+					const double brd = 2 / (3 * 3.14159265358979323846) * (3 * sI + kfr * cf - 4 * sf);
+					for (int a = 0; a < 6; a++) g[a] = make_double2(g[a].x * brd, g[a].y * brd);
+				}
+				else {
+					double ci1, si1, ci2, si2;
+					cisi_d(kfr + kr, ci1, si1);
+					cisi_d(kfr - kr, ci2, si2);
+					const double cI = ci1 - ci2, sI = 3.14159265358979323846 - si1 - si2;
+					const double ipi = 0.31830988618379067154;
+					const double g0 = ipi * (evi * cI + evr * sI);
+					const double g2 = ipi * (kr * (evr * cI - evi * sI) + 2.0 / 3 * invr3 * (kfr * cf - 4 * sf)) - g0;
+					const double tt = g0 * kr2;
+#pragma unroll
+					for (int a = 0; a < 6; a++) {
+						double brd = qm[a] * (tt + 3 * g2);
+						if (a == 0 || a == 3 || a == 5) brd -= tt + g2;
+						g[a].x += brd;
+					}
+				}
 			}
 		}
 		else
@@ -178,7 +260,7 @@ int dmatrix_build(adda_gb300_ctx *c)
 	}
 	const double invN = 1.0 / (gX * ((double)gY * gZ));
 	do {
-		green_fill<<<grid_for(gsz), 256, 0, c->stream>>>(G, bX, bY, bZ, gX, c->gridspace, c->k);
+		green_fill<<<grid_for(gsz), 256, 0, c->stream>>>(G, bX, bY, bZ, gX, c->gridspace, c->k, c->interaction);
 		count_launch();
 		if (cudaGetLastError() != cudaSuccess) { rc = ADDA_GB300_ECUDA; break; }
 		// x transform of all 6*bZ*bY lines (contiguous, length gX)

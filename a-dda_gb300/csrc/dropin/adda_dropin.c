@@ -83,7 +83,11 @@ void InitDmatrix(void)
 {
 	clock_t start = clock();
 	if (surface) ERR("The GPU build does not support -surf");
-	if (IntRelation != G_POINT_DIP) ERR("The GPU build supports only the point-dipole interaction (-int poi)");
+	int inter;
+	if (IntRelation == G_POINT_DIP) inter = ADDA_INT_POI;
+	else if (IntRelation == G_FCD) inter = ADDA_INT_FCD;
+	else if (IntRelation == G_FCD_ST) inter = ADDA_INT_FCD_ST;
+	else ERR("The GPU build supports the interaction terms -int poi|fcd|fcd_st only");
 	if (!reduced_FFT) ERR("The GPU build requires the reduced FFT (do not use -no_reduced_fft)");
 	local_Nsmall = (gridX / 2) * (gridYZ / 2); /* fft.c:975 with nprocs=1 */
 	if (logfile) fprintf(logfile, "The FFT grid is: %zux%zux%zu\n", gridX, gridY, gridZ);
@@ -103,6 +107,7 @@ void InitDmatrix(void)
 	p.wavenum = WaveNum;
 	p.nrhs_max = 1;
 	p.device = getenv("ADDA_GB300_DEVICE") ? atoi(getenv("ADDA_GB300_DEVICE")) : 0;
+	p.interaction = inter;
 	if (adda_gb300_create(&p, &g_ctx)) ERR("GPU initialisation failed: %s", adda_gb300_last_error());
 	if (adda_gb300_init_dmatrix(g_ctx)) ERR("GPU D-matrix initialisation failed: %s", adda_gb300_last_error());
 	g_ccs_valid = 0;

@@ -153,32 +153,63 @@ static double complex pol_rr(double complex M, double complex m, double kd, doub
 	return pol_m(M + I * 2 * kd * kd * kd / 3, m, dipvol);
 }
 
+/* coefficients of the lattice-dispersion-type prescriptions, M = (b1 + (b2 + b3 S) m^2) kd^2 (const.h:234-241):
+ * LDR (Draine & Goodman) and the second-order (SO) formulation of Gutkowicz-Krusin & Draine */
+#define LDR_B1 1.8915316
+#define LDR_B2 (-0.1648469)
+#define LDR_B3 1.7700004
+#define SO_B1 1.5867182426530356710958782335228
+#define SO_B2 0.13488017286410948123541594310740
+#define SO_B3 0.11895825700597042937085940122438
+#define DGF_B1 1.6119919540164696407169668466385 /* (4pi/3)^(1/3) */
+#define LAK_C 0.62035049089940001666800681204778  /* (4pi/3)^(-1/3) */
+
+/* sum_i prop_i^2 e_i^2 (LDR's S, calculator.c:214-222), or its orientation average */
+static double ldr_s(const double prop[3], const double incPol[3], int avgpol)
+{
+	if (avgpol)
+		return 0.5 * (1 - (prop[0] * prop[0] * prop[0] * prop[0] + prop[1] * prop[1] * prop[1] * prop[1] +
+						  prop[2] * prop[2] * prop[2] * prop[2]));
+	return prop[0] * prop[0] * incPol[0] * incPol[0] + prop[1] * prop[1] * incPol[1] * incPol[1] +
+		prop[2] * prop[2] * incPol[2] * incPol[2];
+}
+
 int adda_gb300_polarizability(int relation, double m_re, double m_im, double kd, double gridspace,
 	const double prop[3], const double incPol[3], int avgpol, double cc[6])
 {
 	const double dipvol = gridspace * gridspace * gridspace;
 	const double complex m = m_re + I * m_im;
-	double complex r;
+	const double kd2 = kd * kd;
+	double complex r[3];
 	switch (relation) {
-		case ADDA_POL_CM: r = pol_cm(m, dipvol); break;
-		case ADDA_POL_RRC: r = pol_rr(0, m, kd, dipvol); break;
-		case ADDA_POL_DGF: r = pol_rr(1.6119919540164696407169668466385 * kd * kd, m, kd, dipvol); break;
-		case ADDA_POL_LDR: {
-			/* LDR coefficients b1,b2,b3 (const.h:234-236); S = sum_i prop_i^2 e_i^2, or its average */
-			const double b1 = 1.8915316, b2 = -0.1648469, b3 = 1.7700004;
-			double S;
-			if (avgpol) S = 0.5 * (1 - (prop[0] * prop[0] * prop[0] * prop[0] + prop[1] * prop[1] * prop[1] * prop[1]
-				+ prop[2] * prop[2] * prop[2] * prop[2]));
-			else S = prop[0] * prop[0] * incPol[0] * incPol[0] + prop[1] * prop[1] * incPol[1] * incPol[1]
-				+ prop[2] * prop[2] * incPol[2] * incPol[2];
-			r = pol_rr((b1 + (b2 + b3 * S) * m * m) * kd * kd, m, kd, dipvol);
+		case ADDA_POL_CM: r[0] = pol_cm(m, dipvol); break;
+		case ADDA_POL_RRC: r[0] = pol_rr(0, m, kd, dipvol); break;
+		case ADDA_POL_DGF: r[0] = pol_rr(DGF_B1 * kd2, m, kd, dipvol); break;
+		case ADDA_POL_LDR:
+			r[0] = pol_rr((LDR_B1 + (LDR_B2 + LDR_B3 * ldr_s(prop, incPol, avgpol)) * m * m) * kd2, m, kd, dipvol);
+			break;
+		case ADDA_POL_FCD: /* M0 = (4/3)kd^2 + (2/(3pi)) log((pi-kd)/(pi+kd)) kd^3 (calculator.c:206-208) */
+			r[0] = pol_rr(2.0 / 3 * kd2 * (2 + kd / M_PI * log((M_PI - kd) / (M_PI + kd))), m, kd, dipvol);
+			break;
+		case ADDA_POL_IGT_SO: r[0] = pol_rr(SO_B1 * kd2, m, kd, dipvol); break;
+		case ADDA_POL_LAK: { /* M = (8pi/3)[(1-ika)exp(ika)-1], a = (4pi/3)^(-1/3) d (calculator.c:210-213) */
+			const double ka = LAK_C * kd;
+			r[0] = pol_m(2 * FOUR_PI_D / 3 * ((1 - I * ka) * cexp(I * ka) - 1), m, dipvol);
 			break;
 		}
+		case ADDA_POL_CLDR: /* per component, S_i = prop_i^2 (calculator.c:196) */
+			for (int a = 0; a < 3; a++)
+				r[a] = pol_rr((LDR_B1 + (LDR_B2 + LDR_B3 * prop[a] * prop[a]) * m * m) * kd2, m, kd, dipvol);
+			break;
+		case ADDA_POL_SO: /* orientation-averaged S = 1/3 (calculator.c:197) */
+			r[0] = pol_rr((SO_B1 + (SO_B2 + SO_B3 / 3) * m * m) * kd2, m, kd, dipvol);
+			break;
 		default: return ADDA_GB300_EINVAL;
 	}
+	if (relation != ADDA_POL_CLDR) r[1] = r[2] = r[0];
 	for (int a = 0; a < 3; a++) {
-		cc[2 * a] = creal(r);
-		cc[2 * a + 1] = cimag(r);
+		cc[2 * a] = creal(r[a]);
+		cc[2 * a + 1] = cimag(r[a]);
 	}
 	return ADDA_GB300_OK;
 }
@@ -196,18 +227,13 @@ int adda_gb300_polarizability_dchi(int relation, double m_re, double m_im, doubl
 	switch (relation) {
 		case ADDA_POL_CM:
 		case ADDA_POL_RRC:
-		case ADDA_POL_DGF: break;
-		case ADDA_POL_LDR: {
-			const double b2 = -0.1648469, b3 = 1.7700004;
-			double S;
-			if (avgpol) S = 0.5 * (1 - (prop[0] * prop[0] * prop[0] * prop[0] + prop[1] * prop[1] * prop[1] * prop[1]
-				+ prop[2] * prop[2] * prop[2] * prop[2]));
-			else S = prop[0] * prop[0] * incPol[0] * incPol[0] + prop[1] * prop[1] * incPol[1] * incPol[1]
-				+ prop[2] * prop[2] * incPol[2] * incPol[2];
-			r -= FOUR_PI_D * (b2 + b3 * S) * kd * kd / dipvol;
-			break;
-		}
-		default: return ADDA_GB300_EINVAL;
+		case ADDA_POL_DGF:
+		case ADDA_POL_FCD:
+		case ADDA_POL_IGT_SO:
+		case ADDA_POL_LAK: break;
+		case ADDA_POL_LDR: r -= FOUR_PI_D * (LDR_B2 + LDR_B3 * ldr_s(prop, incPol, avgpol)) * kd * kd / dipvol; break;
+		case ADDA_POL_SO: r -= FOUR_PI_D * (SO_B2 + SO_B3 / 3) * kd * kd / dipvol; break;
+		default: return ADDA_GB300_EINVAL; /* CLDR is anisotropic: no scalar derivative */
 	}
 	out[0] = creal(r);
 	out[1] = cimag(r);

@@ -34,7 +34,19 @@ extern "C" {
 #define ADDA_GB300_EMAXITER 3       /* maxiter reached without convergence (iterative.c:1507, a warning there) */
 
 enum adda_gb300_shape { ADDA_SHAPE_SPHERE = 0, ADDA_SHAPE_ELLIPSOID = 1, ADDA_SHAPE_BOX = 2 };
-enum adda_gb300_pol { ADDA_POL_LDR = 0, ADDA_POL_CM = 1, ADDA_POL_RRC = 2, ADDA_POL_DGF = 3 };
+/* polarizability prescriptions of the reference's -pol (calculator.c:170-262; nloc and nloc_av need the Gaussian
+ * width of -pol nloc and are not provided) */
+enum adda_gb300_pol {
+	ADDA_POL_LDR = 0,
+	ADDA_POL_CM = 1,
+	ADDA_POL_RRC = 2,
+	ADDA_POL_DGF = 3,
+	ADDA_POL_CLDR = 4,
+	ADDA_POL_FCD = 5,
+	ADDA_POL_IGT_SO = 6,
+	ADDA_POL_LAK = 7,
+	ADDA_POL_SO = 8
+};
 /* Krylov methods of the reference's -iter: qmr, bicgstab, bicg (BiCG_CS / COCG), cgnr, csym, qmr2 (QMR_CS_2),
  * bcgs2 (BiCGstab(2)) */
 enum adda_gb300_iter {
@@ -60,6 +72,9 @@ enum adda_gb300_prec {
 	ADDA_PREC_MIXED_F32VEC = 3,
 	ADDA_PREC_MIXED_F64VEC = 4
 };
+/* interaction terms of the reference's -int (interaction.c:290-411): point dipoles, filtered coupled dipoles (FCD,
+ * Gay-Balmaz & Martin / Piller) and its static limit; igt, igt_so, nloc and so are not provided */
+enum adda_gb300_inter { ADDA_INT_POI = 0, ADDA_INT_FCD = 1, ADDA_INT_FCD_ST = 2 };
 enum adda_gb300_init_field { ADDA_IF_AUTO = 0, ADDA_IF_ZERO = 1, ADDA_IF_INC = 2 };
 
 typedef struct adda_gb300_ctx adda_gb300_ctx;
@@ -76,6 +91,7 @@ typedef struct {
 	double wavenum;              /* k = 2*pi/lambda */
 	int nrhs_max;                /* right-hand sides solved together (>=1) */
 	int device;                  /* CUDA device ordinal */
+	int interaction;             /* enum adda_gb300_inter (-int); 0 = point dipoles */
 } adda_gb300_problem;
 
 typedef struct {

@@ -63,12 +63,17 @@ SETUPS = {
     "thin_z512": lambda: cube_setup((3, 2, 256), (6, 4, 512)),
     "box_64x128x256": lambda: cube_setup((32, 64, 128), (64, 128, 256)),
     "box_256x64x128": lambda: cube_setup((128, 32, 64), (256, 64, 128)),
+    # FCD interaction terms (with their Ci/Si) in D
+    "int_fcd": lambda: setup_for(case("int_fcd")["setup"]),
+    "int_fcd_st": lambda: setup_for(case("int_fcd_st")["setup"]),
+    "ell_fcd": lambda: setup_for(case("ell_fcd_eps8")["setup"]),
 }
 
 
 def context(s, R=2):
     import adda_gb300 as A
-    c = A.Context(s.box, s.pos, s.mat, s.gridspace, s.wavenum, s.grid, nrhs_max=R)
+    c = A.Context(s.box, s.pos, s.mat, s.gridspace, s.wavenum, s.grid, nrhs_max=R,
+                  interaction=getattr(s, "interaction", "poi"))
     c.init_dmatrix()
     for r in range(R):
         c.set_cc(r, s.cc[r % 2].reshape(1, 3))
@@ -127,7 +132,8 @@ SOLVE_CASES = ["c1_qmr", "c1_bicgstab", "mgn", "mgn_eps10", "mgn_init_zero", "mg
                "mgn_maxiter3", "ell_orient", "pol_ldr_prop", "prop_ell", "ell24", "box12", "grid6", "grid18",
                "sample_default", "c2_small", "mgn_bicg", "mgn_cgnr", "mgn_csym", "c1_bicg", "c1_cgnr", "c1_csym",
                "ell_bicg_eps8", "ell_csym_eps8", "mgn_qmr2", "c1_qmr2", "ell_qmr2_eps8",
-               "mgn_bcgs2", "c1_bcgs2", "ell_bcgs2_eps8"]
+               "mgn_bcgs2", "c1_bcgs2", "ell_bcgs2_eps8", "pol_cldr", "pol_fcd", "pol_igt_so", "pol_lak", "pol_so",
+               "int_fcd", "int_fcd_st", "c1_fcd", "ell_fcd_eps8"]
 
 
 @pytest.mark.parametrize("name", SOLVE_CASES)
