@@ -18,7 +18,7 @@ SHAPES = {"sphere": 0, "ellipsoid": 1, "box": 2}
 POLS = {"ldr": 0, "cm": 1, "rrc": 2, "dgf": 3, "cldr": 4, "fcd": 5, "igt_so": 6, "lak": 7, "so": 8}
 ITERS = {"qmr": 0, "bicgstab": 1, "bicg": 2, "cgnr": 3, "csym": 4, "qmr2": 5, "bcgs2": 6}
 PREC = {"fp64": 0, "fp32": 1, "mixed": 2, "mixed_f32vec": 3, "mixed_f64vec": 4}
-INIT = {"auto": 0, "zero": 1, "inc": 2}
+INIT = {"auto": 0, "zero": 1, "inc": 2, "x0": 3}
 STATUS = {0: "ok", 1: "breakdown", 2: "stagnation", 3: "maxiter"}
 
 
@@ -49,7 +49,8 @@ class RhsStats(ctypes.Structure):
 
 
 EXPORTS = ["adda_gb300_fft_fit", "adda_gb300_fit_box", "adda_gb300_make_particle", "adda_gb300_rotation",
-           "adda_gb300_plane_wave", "adda_gb300_polarizability", "adda_gb300_polarizability_dchi",
+           "adda_gb300_plane_wave", "adda_gb300_wkb_field", "adda_gb300_polarizability",
+           "adda_gb300_polarizability_dchi",
            "adda_gb300_create", "adda_gb300_destroy",
            "adda_gb300_get_grid", "adda_gb300_init_dmatrix", "adda_gb300_dmatrix_len", "adda_gb300_get_dmatrix",
            "adda_gb300_set_cc", "adda_gb300_set_cc_sqrt", "adda_gb300_set_cc_dipole", "adda_gb300_matvec", "adda_gb300_matvec_device",
@@ -82,6 +83,7 @@ def lib():
             "adda_gb300_make_particle": ([I, P, I, I, I, P, P], SZ),
             "adda_gb300_rotation": ([P, D, D, D, P, P, P], None),
             "adda_gb300_plane_wave": ([SZ, P, I, I, I, D, D, P, P, P], None),
+            "adda_gb300_wkb_field": ([I, I, I, SZ, P, P, I, P, D, P, P], I),
             "adda_gb300_polarizability": ([I, D, D, D, D, P, P, I, P], I),
             "adda_gb300_polarizability_dchi": ([I, D, D, D, D, P, P, I, P], I),
             "adda_gb300_vjp_chi": ([P, P, I, P, P, P, P, P], I),
@@ -176,6 +178,30 @@ def polarizability(m, kd, gridspace, prop, incpol, relation="ldr", avgpol=False)
 
 VOLUME_RATIO = {"sphere": lambda p: math.pi / 6, "ellipsoid": lambda p: math.pi / 6 * p[0] * p[1],
                 "box": lambda p: p[0] * p[1]}
+
+
+def wkb_field(box, pos, mat, ref_index, kd, einc):
+    """internal field in the WKB approximation for incidence along +z (CalcFieldWKB, iterative.c:1227-1322):
+    ref_index per material; einc [3N] complex -> field [3N] complex"""
+    pos = np.ascontiguousarray(pos, dtype=np.uint16).reshape(-1, 3)
+    m = None if mat is None else np.ascontiguousarray(mat, dtype=np.uint8)
+    ri = np.ascontiguousarray(np.atleast_1d(np.asarray(ref_index, dtype=np.complex128)))
+    e = np.ascontiguousarray(einc, dtype=np.complex128)
+    out = np.zeros_like(e)
+    _check(lib().adda_gb300_wkb_field(int(box[0]), int(box[1]), int(box[2]), len(pos), _p(pos), _p(m), len(ri),
+                                      _p(ri), kd, _p(e), _p(out)), "wkb_field")
+    return out
+
+
+def field_to_x0(field, cc, ref_index, gridspace, mat=None):
+    """starting vector x_0 = E/(cc_sqrt*chi_inv) of a field E [3N] (InitFieldfromE, iterative.c:1325-1338):
+    chi_inv = 4pi/(d^3 (m^2-1)) per material, cc [nmat,3] the polarizabilities"""
+    ri = np.atleast_1d(np.asarray(ref_index, dtype=np.complex128))
+    cc = np.asarray(cc, dtype=np.complex128).reshape(len(ri), 3)
+    chi_inv = 4 * np.pi / (gridspace ** 3 * (ri * ri - 1))
+    mult = 1 / (np.sqrt(cc) * chi_inv[:, None])                       # [nmat,3]
+    idx = np.zeros(len(field) // 3, np.int64) if mat is None else np.asarray(mat, dtype=np.int64)
+    return (np.asarray(field).reshape(-1, 3) * mult[idx]).reshape(-1)
 
 
 def polarizability_dchi(m, kd, gridspace, prop, incpol, relation="ldr", avgpol=False):
@@ -307,11 +333,15 @@ class Context:
         return (y[0], ip[0]) if one else (y, ip)
 
     def solve(self, einc, method="qmr", prec="fp64", eps=1e-5, maxiter=100000, init="auto", check_every=0,
-              inner_eps=0.0, max_refine=0, hist_cap=0):
-        """einc: [nrhs, 3N] complex. Returns dict with x, p [nrhs,3N], stats per RHS and residual histories."""
+              inner_eps=0.0, max_refine=0, hist_cap=0, x0=None):
+        """einc: [nrhs, 3N] complex. Returns dict with x, p [nrhs,3N], stats per RHS and residual histories.
+        init="x0" starts from x0 [nrhs, 3N] (see field_to_x0 for a field read from file or from wkb_field)."""
         e = np.ascontiguousarray(einc, dtype=np.complex128).reshape(-1, 3 * self.n)
         R = e.shape[0]
-        x = np.empty_like(e)
+        if init == "x0":
+            x = np.ascontiguousarray(np.array(x0, dtype=np.complex128).reshape(R, 3 * self.n))
+        else:
+            x = np.empty_like(e)
         p = np.empty_like(e)
         st = (RhsStats * R)()
         hist = np.zeros((R, hist_cap)) if hist_cap else None

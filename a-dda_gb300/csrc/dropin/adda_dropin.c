@@ -41,6 +41,10 @@ extern unsigned short *position;
 extern unsigned char *material;
 extern doublecomplex cc_sqrt[MAX_NMAT][3];
 extern doublecomplex *xvec, *pvec, *Einc;
+extern doublecomplex ref_index[MAX_NMAT], chi_inv[MAX_NMAT][3];
+extern double prop[3];
+extern const char *infi_fnameY, *infi_fnameX;
+void ReadField(const char *fname, doublecomplex *field); /* comm.c:562 */
 extern const double iter_eps;
 extern const enum init_field InitField;
 extern const bool recalc_resid;
@@ -83,7 +87,7 @@ void InitDmatrix(void)
 {
 	clock_t start = clock();
 	if (surface) ERR("The GPU build does not support -surf");
-	int inter;
+	int inter = ADDA_INT_POI;
 	if (IntRelation == G_POINT_DIP) inter = ADDA_INT_POI;
 	else if (IntRelation == G_FCD) inter = ADDA_INT_FCD;
 	else if (IntRelation == G_FCD_ST) inter = ADDA_INT_FCD_ST;
@@ -158,7 +162,6 @@ static void report(int niter, double err, double prev_err, int counter)
 
 int IterativeSolver(enum iter method, enum incpol which)
 {
-	(void)which;
 	adda_gb300_solve_params sp;
 	memset(&sp, 0, sizeof(sp));
 	if (method == IT_QMR_CS) sp.method = ADDA_ITER_QMR_CS;
@@ -172,7 +175,29 @@ int IterativeSolver(enum iter method, enum incpol which)
 	if (InitField == IF_AUTO) sp.init_field = ADDA_IF_AUTO;
 	else if (InitField == IF_ZERO) sp.init_field = ADDA_IF_ZERO;
 	else if (InitField == IF_INC) sp.init_field = ADDA_IF_INC;
-	else ERR("The GPU build supports -init_field auto|zero|inc only");
+	else if (InitField == IF_READ || InitField == IF_WKB) {
+		/* CalcInitField (iterative.c:1380-1392): a field E in xvec -- read from file (ReadField, comm.c:562) or
+		 * the WKB approximation -- turned into x_0 = E/(cc_sqrt*chi_inv) (InitFieldfromE, iterative.c:1325-1332) */
+		if (InitField == IF_READ) ReadField(which == INCPOL_Y ? infi_fnameY : infi_fnameX, xvec);
+		else {
+			if (prop[2] != 1)
+				ERR("WKB initial field currently works only with default incident direction of the incoming wave "
+					"(along z-axis)");
+			double ri[2 * MAX_NMAT];
+			for (int i = 0; i < Nmat; i++) {
+				ri[2 * i] = creal(ref_index[i]);
+				ri[2 * i + 1] = cimag(ref_index[i]);
+			}
+			if (adda_gb300_wkb_field(boxX, boxY, boxZ, local_nvoid_Ndip, position, material, Nmat, ri,
+					WaveNum * gridspace, (const double *)Einc, (double *)xvec))
+				ERR("WKB initial field failed: %s", adda_gb300_last_error());
+		}
+		for (size_t i = 0; i < local_nvoid_Ndip; i++)
+			for (int a = 0; a < 3; a++)
+				xvec[3 * i + a] /= cc_sqrt[material[i]][a] * chi_inv[material[i]][a];
+		sp.init_field = ADDA_IF_X0;
+	}
+	else ERR("Unknown -init_field for the GPU build");
 	if (!g_ctx) ERR("IterativeSolver called before InitDmatrix");
 	sp.precision = env_prec();
 	sp.eps = iter_eps;
@@ -188,6 +213,12 @@ int IterativeSolver(enum iter method, enum incpol which)
 	if (sp.precision == ADDA_PREC_FP64) {
 		const char *descr = (sp.init_field == ADDA_IF_ZERO || (sp.init_field == ADDA_IF_AUTO && hist[0] == 1.0))
 			? "x_0 = 0\n" : "x_0 = E_inc\n";
+		char fdescr[512];
+		if (InitField == IF_WKB) descr = "x_0 = result of WKB\n"; /* iterative.c:1383,1390 */
+		else if (InitField == IF_READ) {
+			snprintf(fdescr, sizeof(fdescr), "x_0 = from file %s\n", which == INCPOL_Y ? infi_fnameY : infi_fnameX);
+			descr = fdescr;
+		}
 		if (!orient_avg && logfile) fprintf(logfile, "%sRE_%03d = %.10E\n", descr, 0, hist[0]);
 		printf("%sRE_%03d = %.10E\n", descr, 0, hist[0]);
 		double best = hist[0], prev = hist[0];

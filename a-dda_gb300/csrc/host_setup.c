@@ -13,6 +13,7 @@
 
 #include <complex.h>
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #define TWO_PI_D 6.283185307179586476925286766559
@@ -237,6 +238,50 @@ int adda_gb300_polarizability_dchi(int relation, double m_re, double m_im, doubl
 	}
 	out[0] = creal(r);
 	out[1] = cimag(r);
+	return ADDA_GB300_OK;
+}
+
+int adda_gb300_wkb_field(int boxX, int boxY, int boxZ, size_t ndip, const uint16_t *position, const uint8_t *material,
+	int nmat, const double *ref_index, double kd, const double *einc, double *field)
+{
+	if (boxX < 1 || boxY < 1 || boxZ < 1 || nmat < 1 || nmat > 255 || !position || !ref_index || !einc || !field)
+		return ADDA_GB300_EINVAL;
+	const size_t plane = (size_t)boxX * boxY, cells = plane * boxZ;
+	unsigned char *mg = malloc(cells);
+	double complex *arg = malloc(sizeof(double complex) * cells);
+	double complex *top = malloc(sizeof(double complex) * plane);
+	double complex vals[256];
+	if (!mg || !arg || !top) {
+		free(mg); free(arg); free(top);
+		return ADDA_GB300_ENOMEM;
+	}
+	for (int i = 0; i < nmat; i++) vals[i] = I * (ref_index[2 * i] - 1 + I * ref_index[2 * i + 1]) * kd / 2;
+	vals[nmat] = 0;
+	memset(mg, nmat, cells);
+	for (size_t d = 0; d < ndip; d++) {
+		const size_t cell = ((size_t)position[3 * d + 2] * boxY + position[3 * d + 1]) * boxX + position[3 * d];
+		mg[cell] = material ? material[d] : 0;
+	}
+	for (size_t i = 0; i < plane; i++) top[i] = 0;
+	/* arg(z) = arg(z-1) + v(z-1) + v(z): half a cell of phase on each side of every cell boundary */
+	for (int z = 0; z < boxZ; z++)
+		for (size_t i = 0; i < plane; i++) {
+			const size_t cell = (size_t)z * plane + i;
+			arg[cell] = top[i] + vals[mg[cell]];
+			top[i] = arg[cell] + vals[mg[cell]];
+		}
+	for (size_t d = 0; d < ndip; d++) {
+		const size_t cell = ((size_t)position[3 * d + 2] * boxY + position[3 * d + 1]) * boxX + position[3 * d];
+		const double complex f = cexp(arg[cell]);
+		for (int a = 0; a < 3; a++) {
+			const double complex e = (einc[6 * d + 2 * a] + I * einc[6 * d + 2 * a + 1]) * f;
+			field[6 * d + 2 * a] = creal(e);
+			field[6 * d + 2 * a + 1] = cimag(e);
+		}
+	}
+	free(mg);
+	free(arg);
+	free(top);
 	return ADDA_GB300_OK;
 }
 

@@ -1739,7 +1739,29 @@ static int solve_mixed(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int
 		ADDA_LAUNCHED();
 		double inner_eps0 = sp->inner_eps > 0 ? sp->inner_eps : 0.5 * sp->eps;
 		int *d_odone = w->done; // reused below as skip flags after the inner solve (copied from host)
+		// caller-supplied x_0 (staged in x64): start like a refinement step from r = b - A.x_0 in FP64
+		const bool x0mode = sp->init_field == ADDA_IF_X0;
+		if (x0mode) {
+			MvEpi e{EPI_NONE, nullptr, c->partial};
+			if ((rc = matvec_run<double>(c, R, w->x64, w->av64, 0, e, nullptr))) return rc;
+			k_resid64<C><<<gv, NT, 0, s>>>(w->b64, w->av64, w->r64, k.v3, n3, w->vpart, w->nbv);
+			ADDA_LAUNCHED();
+			if ((rc = reduce_partials(c, R, w->vpart, w->nbv, c->d_red))) return rc;
+			ADDA_CUDA(cudaMemcpyAsync(red.data(), c->d_red, sizeof(double) * 4 * R, cudaMemcpyDeviceToHost, s));
+			ADDA_CUDA(cudaStreamSynchronize(s));
+			for (int r = 0; r < R; r++) {
+				inprod64[r] = red[4 * r];
+				nmv64[r]++;
+				if (inprod64[r] <= epsB64[r]) odone[r] = 1;
+			}
+		}
 		for (int step = 0; step <= maxref; step++) {
+			const bool refine = step > 0 || x0mode; // the inner solve corrects an FP64 residual
+			if (step == 0 && x0mode) {
+				bool all = true;
+				for (int r = 0; r < R; r++) all = all && odone[r];
+				if (all) break;
+			}
 			// an RHS whose inner solves used up maxiter stops refining (reported as maxiter below)
 			if (step > 0) {
 				bool all = true;
@@ -1752,7 +1774,7 @@ static int solve_mixed(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int
 			// inner solve: A d = rhs (rhs float in k.v3 on entry); init per the user's field mode at step 0
 			std::vector<double> eps_in(R);
 			for (int r = 0; r < R; r++) {
-				if (step == 0) eps_in[r] = inner_eps0;
+				if (!refine) eps_in[r] = inner_eps0;
 				else {
 					const double rho = sqrt(epsB64[r] / std::max(inprod64[r], 1e-300));
 					eps_in[r] = std::min(0.5, std::max(0.5 * rho, 2e-6));
@@ -1772,7 +1794,7 @@ static int solve_mixed(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int
 					ADDA_LAUNCHED();
 				}
 			}
-			const int zero = (step > 0) || sp->init_field == ADDA_IF_ZERO;
+			const int zero = refine || sp->init_field == ADDA_IF_ZERO;
 			if (zero) {
 				ADDA_CUDA(cudaMemsetAsync(k.x, 0, sizeof(C) * R * n3, s));
 				k_copy<C><<<gv, NT, 0, s>>>(k.r, k.v3, n3, nullptr);
@@ -1817,7 +1839,7 @@ static int solve_mixed(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int
 			// x64 (+)= d for the RHS still active
 			for (int r = 0; r < R; r++) w->h_done[r] = odone[r];
 			ADDA_CUDA(cudaMemcpyAsync(d_odone, w->h_done, sizeof(int) * R, cudaMemcpyHostToDevice, s));
-			k_accum<C><<<gv, NT, 0, s>>>(w->x64, k.x, n3, step > 0 ? 1 : 0, d_odone);
+			k_accum<C><<<gv, NT, 0, s>>>(w->x64, k.x, n3, refine ? 1 : 0, d_odone);
 			ADDA_LAUNCHED();
 			// true residual in FP64: r64 = b - A64.x64, |r64|^2; float copy into k.v3 for the next inner solve
 			MvEpi e{EPI_NONE, nullptr, c->partial};
@@ -1856,7 +1878,8 @@ static int check_params(const adda_gb300_solve_params *sp)
 	if (sp->method < ADDA_ITER_QMR_CS || sp->method > ADDA_ITER_BCGS2 ||
 		(sp->precision != ADDA_PREC_FP64 && sp->precision != ADDA_PREC_MIXED &&
 			sp->precision != ADDA_PREC_MIXED_F32VEC && sp->precision != ADDA_PREC_MIXED_F64VEC) || !(sp->eps > 0) || sp->maxiter < 0 ||
-		(sp->init_field != ADDA_IF_AUTO && sp->init_field != ADDA_IF_ZERO && sp->init_field != ADDA_IF_INC)) {
+		(sp->init_field != ADDA_IF_AUTO && sp->init_field != ADDA_IF_ZERO && sp->init_field != ADDA_IF_INC &&
+			sp->init_field != ADDA_IF_X0)) {
 		set_error("solve: unsupported parameters");
 		return ADDA_GB300_EINVAL;
 	}
@@ -1919,6 +1942,18 @@ static int solve_core_impl(adda_gb300_ctx *c, const adda_gb300_solve_params *sp,
 			k_copy<C><<<gv, NT, 0, s>>>(k.r, w->b64, n3, nullptr);
 			ADDA_LAUNCHED();
 		}
+		else if (sp->init_field == ADDA_IF_X0) {
+			// x_0 from the caller (staged in x64): r_0 = b - A.x_0 (InitFieldfromE, iterative.c:1335-1337)
+			k_copy<C><<<gv, NT, 0, s>>>(k.x, w->x64, n3, nullptr);
+			ADDA_LAUNCHED();
+			MvEpi e{EPI_NONE, nullptr, c->partial};
+			if ((rc = matvec_run<double>(c, R, k.x, k.Av, 0, e, nullptr))) return rc;
+			k_init_field<C><<<gv, NT, 0, s>>>(w->st, w->done, w->b64, k.Av, k.x, k.r, n3, sp->init_field, w->vpart,
+				w->nbv, 0);
+			ADDA_LAUNCHED();
+			s_init_choose<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv, sp->init_field, w->hist, w->hist_cap);
+			ADDA_LAUNCHED();
+		}
 		else {
 			MvEpi e{EPI_NONE, nullptr, c->partial};
 			if ((rc = matvec_run<double>(c, R, w->b64, k.Av, 0, e, nullptr))) return rc;
@@ -1975,6 +2010,13 @@ int solver_solve(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int R, co
 	cudaStream_t s = c->stream;
 	// stage Einc in the FP64 matvec output buffer (consumed by the first kernel of the solve)
 	ADDA_CUDA(cudaMemcpyAsync(w->av64, einc, sizeof(double2) * R * n3, cudaMemcpyHostToDevice, s));
+	if (sp->init_field == ADDA_IF_X0) {
+		if (!xvec) {
+			set_error("solve: init_field X0 needs x_0 in xvec");
+			return ADDA_GB300_EINVAL;
+		}
+		ADDA_CUDA(cudaMemcpyAsync(w->x64, xvec, sizeof(double2) * R * n3, cudaMemcpyHostToDevice, s));
+	}
 	if ((rc = solve_core(c, sp, R, w->av64, stats))) return rc;
 	if (xvec) ADDA_CUDA(cudaMemcpyAsync(xvec, w->x64, sizeof(double2) * R * n3, cudaMemcpyDeviceToHost, s));
 	if (pvec) ADDA_CUDA(cudaMemcpyAsync(pvec, c->pvec64, sizeof(double2) * R * n3, cudaMemcpyDeviceToHost, s));
@@ -1997,6 +2039,13 @@ int solver_solve_dev(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int R
 	SolverWork *w = c->sw;
 	const size_t n3 = w->n3;
 	cudaStream_t s = c->stream;
+	if (sp->init_field == ADDA_IF_X0) {
+		if (!d_xvec) {
+			set_error("solve_device: init_field X0 needs x_0 in d_xvec");
+			return ADDA_GB300_EINVAL;
+		}
+		ADDA_CUDA(cudaMemcpyAsync(w->x64, d_xvec, sizeof(double2) * R * n3, cudaMemcpyDeviceToDevice, s));
+	}
 	if ((rc = solve_core(c, sp, R, d_einc, stats))) return rc;
 	if (d_xvec) ADDA_CUDA(cudaMemcpyAsync(d_xvec, w->x64, sizeof(double2) * R * n3, cudaMemcpyDeviceToDevice, s));
 	if (d_pvec) ADDA_CUDA(cudaMemcpyAsync(d_pvec, c->pvec64, sizeof(double2) * R * n3, cudaMemcpyDeviceToDevice, s));
@@ -2054,7 +2103,9 @@ int vjp_chi(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int rhs, const
 		prop[1], prop[2], incpol[0], incpol[1], incpol[2], kd, c->k, ph0);
 	ADDA_LAUNCHED();
 	adda_gb300_rhs_stats st[2];
-	rc = solve_core(c, sp, 2, w->av64, st);
+	adda_gb300_solve_params asp = *sp;
+	if (asp.init_field == ADDA_IF_X0) asp.init_field = ADDA_IF_AUTO; // no caller x_0 for the adjoint systems
+	rc = solve_core(c, &asp, 2, w->av64, st);
 	if (!rc) {
 		ADDA_CUDA(cudaMemcpyAsync(dF, dinv_alpha, sizeof(double2) * N, cudaMemcpyHostToDevice, s));
 		k_vjp_grad<<<gN, NT, 0, s>>>(save_p + n3 * rhs, c->pvec64, c->pvec64 + n3, dF, N, c->k, dg, dg + 2 * N);

@@ -75,7 +75,11 @@ enum adda_gb300_prec {
 /* interaction terms of the reference's -int (interaction.c:290-411): point dipoles, filtered coupled dipoles (FCD,
  * Gay-Balmaz & Martin / Piller) and its static limit; igt, igt_so, nloc and so are not provided */
 enum adda_gb300_inter { ADDA_INT_POI = 0, ADDA_INT_FCD = 1, ADDA_INT_FCD_ST = 2 };
-enum adda_gb300_init_field { ADDA_IF_AUTO = 0, ADDA_IF_ZERO = 1, ADDA_IF_INC = 2 };
+/* -init_field: auto, zero, inc (CalcInitField, iterative.c:1342-1394), and X0: the starting vector x_0 is supplied by
+ * the caller in xvec (host API) or d_xvec (device API) -- the reference's "read" and "wkb" modes, which turn an
+ * electric field E into x_0 = E/(cc_sqrt*chi_inv) (InitFieldfromE, iterative.c:1325-1338; see
+ * adda_gb300_wkb_field) */
+enum adda_gb300_init_field { ADDA_IF_AUTO = 0, ADDA_IF_ZERO = 1, ADDA_IF_INC = 2, ADDA_IF_X0 = 3 };
 
 typedef struct adda_gb300_ctx adda_gb300_ctx;
 
@@ -130,7 +134,14 @@ void adda_gb300_rotation(const double prop0[3], double alpha_deg, double beta_de
 /* GenerateB, free-space plane wave, src/GenerateB.c:324-328: einc[i] = pol * exp(i k r_i.prop) */
 void adda_gb300_plane_wave(size_t ndip, const uint16_t *position, int boxX, int boxY, int boxZ, double gridspace,
 	double wavenum, const double prop[3], const double pol[3], double *einc);
-/* CoupleConstant, src/calculator.c:170-262 (CM, RRC, DGF, LDR [avgpol]); cc = 3 identical complex values */
+
+/* CalcFieldWKB (iterative.c:1227-1322): the internal field in the WKB approximation for incidence along +z:
+ * E_j = Einc_j exp(phi_j), phi accumulated along each z column of the box with i(m-1)kd/2 per half cell (void cells
+ * add nothing). material [ndip] (NULL = all 0), ref_index [nmat][2] (re, im); einc and field [ndip][3] complex. */
+int adda_gb300_wkb_field(int boxX, int boxY, int boxZ, size_t ndip, const uint16_t *position, const uint8_t *material,
+	int nmat, const double *ref_index, double kd, const double *einc, double *field);
+/* CoupleConstant, src/calculator.c:170-262 (enum adda_gb300_pol; LDR with avgpol); cc = the 3 diagonal components
+ * (identical except for CLDR) */
 int adda_gb300_polarizability(int relation, double m_re, double m_im, double kd, double gridspace,
 	const double prop[3], const double incPol[3], int avgpol, double cc[6]);
 

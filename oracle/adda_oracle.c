@@ -865,6 +865,15 @@ int or_solve(or_ctx *c, int method, const double *einc, double eps, int maxiter,
 		memcpy(S.r, b, sizeof(cplx) * n);
 		S.inprodR = temp;
 	}
+	else if (init_field == OR_IF_X0) { // x_0 from the caller: InitFieldfromE, iterative.c:1335-1337
+		mv(&S, S.x, S.Av, NULL);
+		double ip = 0;
+		for (size_t i = 0; i < n; i++) {
+			S.r[i] = b[i] - S.Av[i];
+			ip += creal(S.r[i]) * creal(S.r[i]) + cimag(S.r[i]) * cimag(S.r[i]);
+		}
+		S.inprodR = ip;
+	}
 	else {
 		mv(&S, b, S.Av, NULL);
 		double ip = 0;

@@ -23,7 +23,7 @@ typedef struct or_ctx or_ctx;
 
 /* iterative methods and initial-field modes, same meaning as -iter and -init_field */
 enum { OR_QMR_CS = 0, OR_BICGSTAB = 1, OR_BICG_CS = 2, OR_CGNR = 3, OR_CSYM = 4, OR_QMR_CS_2 = 5, OR_BCGS2 = 6 };
-enum { OR_IF_AUTO = 0, OR_IF_ZERO = 1, OR_IF_INC = 2 };
+enum { OR_IF_AUTO = 0, OR_IF_ZERO = 1, OR_IF_INC = 2, OR_IF_X0 = 3 }; /* X0: x_0 given in xvec */
 /* solver status codes */
 enum { OR_OK = 0, OR_EBREAKDOWN = 1, OR_ESTAGNATION = 2, OR_EMAXITER = 3 };
 

@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_BIN = os.path.join(HERE, "_ref", "adda")
 
 QMR_CS, BICGSTAB, BICG_CS, CGNR, CSYM, QMR_CS_2, BCGS2 = 0, 1, 2, 3, 4, 5, 6
-IF_AUTO, IF_ZERO, IF_INC = 0, 1, 2
+IF_AUTO, IF_ZERO, IF_INC, IF_X0 = 0, 1, 2, 3
 STATUS = {0: "ok", 1: "breakdown", 2: "stagnation", 3: "maxiter"}
 
 _lib = None
@@ -118,9 +118,9 @@ class Oracle:
         self.L.or_matvec(self.h, _ptr(x), _ptr(y), ctypes.byref(ip), int(her))
         return y, ip.value
 
-    def solve(self, einc, method=QMR_CS, eps=1e-5, maxiter=100000, init_field=IF_AUTO, hist_cap=100000):
+    def solve(self, einc, method=QMR_CS, eps=1e-5, maxiter=100000, init_field=IF_AUTO, hist_cap=100000, x0=None):
         einc = np.ascontiguousarray(einc, dtype=np.complex128)
-        x = np.empty_like(einc)
+        x = np.empty_like(einc) if x0 is None else np.array(x0, dtype=np.complex128)
         p = np.empty_like(einc)
         hist = np.zeros(hist_cap)
         nit = ctypes.c_int(0)

@@ -4,8 +4,9 @@
  * drives the drop-in exactly like Calculator/CalculateE do: ParSetup's fftFit, InitDmatrix, IterativeSolver,
  * MatVec, Free_FFT_Dmat. Inputs come from libadda_gb300's host-side setup.
  *
- * usage: mock_host <grid> <m_re> <m_im> <dpl> <qmr|bicgstab> <eps_exponent> <out.bin>
+ * usage: mock_host <grid> <m_re> <m_im> <dpl> <qmr|bicgstab> <eps_exponent> <out.bin> [wkb | read <field.bin>]
  * writes: ndip (int64), then pvec and a MatVec of Einc (complex doubles, 3*ndip each)
+ * read: the field file holds 3*ndip complex doubles (the mock's ReadField; the reference's reads io.c's text format)
  */
 #include "adda_gb300.h"
 #include "adda_dropin.h"
@@ -33,6 +34,19 @@ doublecomplex cc_sqrt[15][3];
 doublecomplex *xvec, *pvec, *Einc;
 double iter_eps = 1e-5;
 enum init_field InitField = IF_AUTO;
+doublecomplex ref_index[15], chi_inv[15][3];
+double prop[3];
+const char *infi_fnameY, *infi_fnameX;
+
+void ReadField(const char *fname, doublecomplex *field)
+{
+	FILE *f = fopen(fname, "rb");
+	if (!f || fread(field, sizeof(doublecomplex), local_nRows, f) != local_nRows) {
+		fprintf(stderr, "ERROR: cannot read %s\n", fname);
+		exit(1);
+	}
+	fclose(f);
+}
 enum scat ScatRelation = SQ_DRAINE;
 /* the reference's CalcField lives in another object (mock_crosssec.c, like crosssec.c), so that this file's calls
  * go through the linker's --wrap=CalcField */
@@ -102,10 +116,17 @@ int main(int argc, char **argv)
 	gridYZ = gridY * gridZ;
 	WaveNum = 1.0;
 	gridspace = 2 * M_PI / dpl;
-	double prop[3], py[3], px[3], cc[6];
+	double py[3], px[3], cc[6];
 	adda_gb300_rotation(NULL, 0, 0, 0, prop, py, px);
 	adda_gb300_polarizability(ADDA_POL_LDR, mre, mim, 2 * M_PI / dpl, gridspace, prop, py, 0, cc);
 	for (int c = 0; c < 3; c++) cc_sqrt[0][c] = csqrt(cc[2 * c] + I * cc[2 * c + 1]);
+	ref_index[0] = mre + I * mim; /* calculator.c:278: chi_inv = 4pi/(d^3 (m^2-1)) */
+	for (int c = 0; c < 3; c++) chi_inv[0][c] = 4 * M_PI / (pow(gridspace, 3) * (ref_index[0] * ref_index[0] - 1));
+	if (argc > 8 && !strcmp(argv[8], "wkb")) InitField = IF_WKB;
+	if (argc > 9 && !strcmp(argv[8], "read")) {
+		InitField = IF_READ;
+		infi_fnameY = infi_fnameX = argv[9];
+	}
 	Einc = malloc(sizeof(doublecomplex) * local_nRows);
 	xvec = malloc(sizeof(doublecomplex) * local_nRows);
 	pvec = malloc(sizeof(doublecomplex) * local_nRows);

@@ -94,6 +94,12 @@ CASES = [
      dict(grid=16, m=1.5, dpl=10, pol="fcd", interaction="fcd")),
     ("ell_fcd_eps8", ["-int", "fcd", "-pol", "fcd", "-eps", "8"] + ELL + MGN,
      dict(grid=8, m=1.1 + 0.1j, shape="ellipsoid", pars=(0.5, 1.5), pol="fcd", interaction="fcd", eps=1e-8)),
+    # WKB initial field (-init_field wkb, incidence along z)
+    ("mgn_wkb", ["-init_field", "wkb"] + MGN, dict(grid=8, m=1.1 + 0.1j, init="wkb")),
+    ("c1_wkb", ["-grid", "16", "-dpl", "10", "-m", "1.5", "0", "-init_field", "wkb", "-eps", "5"],
+     dict(grid=16, m=1.5, dpl=10, init="wkb")),
+    ("ell_wkb_eps8", ["-init_field", "wkb", "-eps", "8"] + ELL + MGN,
+     dict(grid=8, m=1.1 + 0.1j, shape="ellipsoid", pars=(0.5, 1.5), init="wkb", eps=1e-8)),
     ("mgn_bcgs2", ["-iter", "bcgs2"] + MGN, dict(grid=8, m=1.1 + 0.1j, iter="bcgs2")),
     ("c1_bcgs2", ["-grid", "16", "-dpl", "10", "-m", "1.5", "0", "-iter", "bcgs2", "-eps", "5"],
      dict(grid=16, m=1.5, dpl=10, iter="bcgs2")),

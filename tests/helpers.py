@@ -42,13 +42,23 @@ def oracle_for(s, nthreads=0):
     return o
 
 
-def oracle_solve(o, s, pol_index, method="qmr", eps=1e-5, maxiter=100000, init="auto"):
+def wkb_x0(s, pol_index):
+    """the reference's -init_field wkb starting vector for polarisation pol_index: the WKB field of the product's host
+    code turned into x_0 (InitFieldfromE)"""
+    import adda_gb300 as A
+    e = A.wkb_field(s.box, s.pos, s.mat, [s.m], s.kd, s.einc[pol_index])
+    return A.field_to_x0(e, s.cc[pol_index].reshape(1, 3), [s.m], s.gridspace, s.mat)
+
+
+def oracle_solve(o, s, pol_index, method="qmr", eps=1e-5, maxiter=100000, init="auto", x0=None):
+    if init == "wkb":
+        init, x0 = "x0", wkb_x0(s, pol_index)
     from oracle import oracle as O
     o.set_cc(s.cc[pol_index].reshape(1, 3))
     methods = {"qmr": O.QMR_CS, "bicgstab": O.BICGSTAB, "bicg": O.BICG_CS, "cgnr": O.CGNR, "csym": O.CSYM,
                "qmr2": O.QMR_CS_2, "bcgs2": O.BCGS2}
     r = o.solve(s.einc[pol_index], method=methods[method], eps=eps, maxiter=maxiter,
-                init_field={"auto": O.IF_AUTO, "zero": O.IF_ZERO, "inc": O.IF_INC}[init])
+                init_field={"auto": O.IF_AUTO, "zero": O.IF_ZERO, "inc": O.IF_INC, "x0": O.IF_X0}[init], x0=x0)
     ce, ca = o.cross(r["p"], s.prop, s.incpol[pol_index])
     r["Cext"], r["Cabs"] = ce, ca
     return r

@@ -58,3 +58,50 @@ def test_dropin_solve_and_matvec(tmp_path, method):
     for d, n_ in enumerate([s.prop, (0.6, 0.0, 0.8), (0.0, -1.0, 0.0)]):
         eo = o.field(pv, np.asarray(n_, dtype=float))
         assert np.linalg.norm(fields[d] - eo) <= 1e-12 * np.linalg.norm(eo), (d, fields[d], eo)
+
+
+def _run_mock(tmp_path, extra, eps="10"):
+    exe = build_mock()
+    out = tmp_path / "res.bin"
+    p = subprocess.run([exe, "16", "1.5", "0", "10", "qmr", eps, str(out), *extra], capture_output=True, text=True)
+    assert p.returncode == 0, p.stdout + p.stderr
+    raw = open(out, "rb").read()
+    n = int(np.frombuffer(raw[:8], np.int64)[0])
+    niter = int(np.frombuffer(raw[8:12], np.int32)[0])
+    return p.stdout, n, niter, np.frombuffer(raw[20:], np.complex128)[:3 * n]
+
+
+def test_dropin_init_field_wkb(tmp_path):
+    """-init_field wkb: the drop-in computes the WKB field on the host, turns it into x_0 (InitFieldfromE) and the
+    GPU solve from there ends at the oracle's solution from the same start"""
+    import adda_gb300 as A
+    from helpers import wkb_x0
+    A.lib()
+    out, n, niter, pv = _run_mock(tmp_path, ["wkb"])
+    assert "x_0 = result of WKB" in out
+    s = setup_for(dict(grid=16, m=1.5, dpl=10))
+    o = oracle_for(s)
+    r = oracle_solve(o, s, 0, eps=1e-10, init="x0", x0=wkb_x0(s, 0))
+    # the starting residual is the oracle's to the printed digits
+    re0 = float(out.split("RE_000 = ")[1].split()[0])
+    assert abs(re0 / r["resid"][0] - 1) < 1e-9, (re0, r["resid"][0])
+    assert abs(niter - r["niter"]) <= max(3, 0.1 * r["niter"])
+    ce, _ = o.cross(pv, s.prop, s.incpol[0])
+    assert abs(ce / r["Cext"] - 1) < 1e-9
+
+
+def test_dropin_init_field_read(tmp_path):
+    """-init_field read: a field file holding the converged internal field E = chi_inv p makes the solve stop at
+    iteration 0 with the same polarisation"""
+    import adda_gb300 as A
+    A.lib()
+    s = setup_for(dict(grid=16, m=1.5, dpl=10))
+    o = oracle_for(s)
+    r = oracle_solve(o, s, 0, eps=1e-12)
+    chi_inv = 4 * np.pi / (s.gridspace ** 3 * (1.5 ** 2 - 1))
+    f = tmp_path / "field.bin"
+    (chi_inv * r["p"]).astype(np.complex128).tofile(f)
+    out, n, niter, pv = _run_mock(tmp_path, ["read", str(f)])
+    assert "x_0 = from file " + str(f) in out
+    assert niter == 0, out
+    assert np.linalg.norm(pv - r["p"]) <= 1e-10 * np.linalg.norm(r["p"])
