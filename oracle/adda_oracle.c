@@ -405,6 +405,7 @@ typedef struct {
 	cplx *x, *r, *p, *Av, *v1, *v2, *v3, *v4;
 	double inprodR, inprodRp1, epsB;
 	int niter, counter, matvec_ready, complete;
+	int full; // no exit at BiCGStab's half step: checkpoints of type always (iterative.c:703)
 } solver;
 
 static void mv(solver *s, const cplx *in, cplx *out, double *ipr)
@@ -529,7 +530,7 @@ static int bcgs_iter(solver *s, bcgs_state *b)
 		sum += creal(b->sv[i]) * creal(b->sv[i]) + cimag(b->sv[i]) * cimag(b->sv[i]);
 	}
 	s->inprodRp1 = sum;
-	if (s->inprodRp1 < s->epsB) {
+	if (s->inprodRp1 < s->epsB && !s->full) {
 		for (size_t i = 0; i < n; i++) s->x[i] += b->alpha * s->p[i];
 		s->complete = 0;
 	}
@@ -833,11 +834,129 @@ static int bcgs2_iter(solver *s, bcgs2_state *b)
 	return OR_OK;
 }
 
+/* ---------------- checkpoints, src/iterative.c:165-278 ----------------
+ * File layout (native byte order, fields back to back): int ind_m (index of the method in the reference's params
+ * table, iterative.c:118-125), size_t local_nRows, int niter, int counter, double inprodR, double prev_err,
+ * double resid_scale, the method's scalars, then xvec, rvec, pvec and the method's vectors (local_nRows complex
+ * doubles each). The reference stores buffers, not roles: QMR_CS and CSYM swap their vector pointers every
+ * iteration, so which buffer holds which vector follows from the parity of niter (the pointer swaps on load,
+ * iterative.c:809-812,935-938). */
+typedef struct {
+	unsigned char *buf;
+	size_t cap, len;
+} chp_w;
+typedef struct {
+	const unsigned char *buf;
+	size_t len, pos;
+	int bad;
+} chp_r;
+
+static void chp_put(chp_w *w, const void *p, size_t n)
+{
+	if (w->buf && w->len + n <= w->cap) memcpy(w->buf + w->len, p, n);
+	w->len += n;
+}
+
+static void chp_get(chp_r *r, void *p, size_t n)
+{
+	if (r->pos + n > r->len) {
+		r->bad = 1;
+		memset(p, 0, n);
+	}
+	else memcpy(p, r->buf + r->pos, n);
+	r->pos += n;
+}
+
+// index in the reference's params table (alphabetical: BCGS2, BiCG_CS, BiCGStab, CGNR, CSYM, QMR_CS, QMR_CS_2)
+static const int chp_ind[7] = {5, 2, 1, 3, 4, 6, 0};
+
+typedef struct {
+	cplx *rvec, *pvec, *vec[3];
+	int nvec;
+} chp_roles;
+
+/* buffers in the reference's order for the state before iteration niter */
+static chp_roles chp_layout(solver *S, int method, qmr_state *q, bcgs_state *bs, csym_state *cs)
+{
+	chp_roles L;
+	memset(&L, 0, sizeof(L));
+	L.rvec = S->r;
+	L.pvec = S->p;
+	const int odd = S->niter & 1;
+	switch (method) {
+		case OR_QMR_CS: // v=vec1, vtilda=vec2 for odd niter, swapped for even; p_new=vec3, p_old=pvec for odd
+			L.pvec = odd ? q->po : q->pn;
+			L.vec[0] = odd ? q->v : q->vt;
+			L.vec[1] = odd ? q->vt : q->v;
+			L.vec[2] = odd ? q->pn : q->po;
+			L.nvec = 3;
+			break;
+		case OR_BICGSTAB:
+			L.vec[0] = bs->v;
+			L.vec[1] = bs->sv;
+			L.vec[2] = bs->rt;
+			L.nvec = 3;
+			break;
+		case OR_CSYM: // q_new=rvec, q_old=vec1 for odd niter, swapped for even; p_new=vec2, p_old=pvec for odd
+			L.rvec = odd ? cs->q_new : cs->q_old;
+			L.vec[0] = odd ? cs->q_old : cs->q_new;
+			L.pvec = odd ? cs->p_old : cs->p_new;
+			L.vec[1] = odd ? cs->p_new : cs->p_old;
+			L.nvec = 2;
+			break;
+		case OR_QMR_CS_2:
+			L.vec[0] = S->v1; // v
+			L.vec[1] = S->v2; // d
+			L.nvec = 2;
+			break;
+		case OR_BCGS2:
+			L.vec[0] = S->v2; // u[0]; pvec holds r~0
+			L.nvec = 1;
+			break;
+		default: break; // BiCG_CS, CGNR: p in pvec only
+	}
+	return L;
+}
+
+/* the method's scalars in the order of its PHASE_VARS (iterative.c:383-386,520-521,661-664,741-742,796-803,
+ * 919-928,1060-1066); dir = 0 writes, 1 reads */
+static void chp_scalars(void *io, int dir, int method, qmr_state *q, bcgs_state *bs, csym_state *cs,
+	qmr2_state *q2, bcgs2_state *b2, cplx *ro_c, double *ro_d)
+{
+#define CHP_IO(v) (dir ? chp_get((chp_r *)io, &(v), sizeof(v)) : chp_put((chp_w *)io, &(v), sizeof(v)))
+	switch (method) {
+		case OR_QMR_CS:
+			CHP_IO(q->om_old); CHP_IO(q->om_new); CHP_IO(q->c_old); CHP_IO(q->c_new);
+			CHP_IO(q->beta); CHP_IO(q->tautilda); CHP_IO(q->s_old); CHP_IO(q->s_new);
+			break;
+		case OR_BICGSTAB: CHP_IO(bs->ro_old); CHP_IO(bs->omega); CHP_IO(bs->alpha); break;
+		case OR_BICG_CS: CHP_IO(*ro_c); break;
+		case OR_CGNR: CHP_IO(*ro_d); break;
+		case OR_CSYM:
+			CHP_IO(cs->beta); CHP_IO(cs->c_old); CHP_IO(cs->c_new); CHP_IO(cs->tau); CHP_IO(cs->s_old);
+			CHP_IO(cs->s_new);
+			break;
+		case OR_QMR_CS_2:
+			CHP_IO(q2->c_old); CHP_IO(q2->theta_old); CHP_IO(q2->ro_old); CHP_IO(q2->eps); CHP_IO(q2->eta);
+			break;
+		default: CHP_IO(b2->rho0); CHP_IO(b2->alpha); break;
+	}
+#undef CHP_IO
+}
+
 /* IterativeSolver, src/iterative.c:1398-1530 with CalcInitField (:1342-1394) and ProgressReport (:282-318).
  * einc: incident field [N][3]; xvec receives x, pvec the polarisations S.x; resid_hist[0..] the relative residuals
  * RE_000, RE_001, ... (at most hist_cap values). Returns a status code; *niter_out = iterations performed. */
 int or_solve(or_ctx *c, int method, const double *einc, double eps, int maxiter, int init_field,
 	double *xvec, double *pvec, double *resid_hist, int hist_cap, int *niter_out)
+{
+	return or_solve_chp(c, method, einc, eps, maxiter, init_field, xvec, pvec, resid_hist, hist_cap, niter_out, NULL,
+		0, NULL, NULL);
+}
+
+int or_solve_chp(or_ctx *c, int method, const double *einc, double eps, int maxiter, int init_field,
+	double *xvec, double *pvec, double *resid_hist, int hist_cap, int *niter_out, const void *chp_in,
+	size_t chp_in_len, void *chp_out, size_t *chp_out_len)
 {
 	solver S;
 	memset(&S, 0, sizeof(S));
@@ -854,13 +973,17 @@ int or_solve(or_ctx *c, int method, const double *einc, double eps, int maxiter,
 	S.v2 = malloc(sizeof(cplx) * n);
 	S.v3 = malloc(sizeof(cplx) * n);
 	S.v4 = malloc(sizeof(cplx) * n);
+	S.full = chp_out != NULL;
 	// b = S.Einc (nMult_mat)
 	for (size_t i = 0; i < c->n; i++)
 		for (int a = 0; a < 3; a++) b[3 * i + a] = ccs_of(c, i, a) * E[3 * i + a];
 	double temp = nnorm2(b, n);
 	double resid_scale = 1 / temp;
 	S.epsB = eps * eps * temp;
-	if (init_field == OR_IF_ZERO) {
+	if (chp_in) {
+		/* LoadIterChpoint replaces CalcInitField and the method's PHASE_INIT */
+	}
+	else if (init_field == OR_IF_ZERO) {
 		memset(S.x, 0, sizeof(cplx) * n);
 		memcpy(S.r, b, sizeof(cplx) * n);
 		S.inprodR = temp;
@@ -891,7 +1014,7 @@ int or_solve(or_ctx *c, int method, const double *einc, double eps, int maxiter,
 		else memcpy(S.x, b, sizeof(cplx) * n);
 	}
 	int nh = 0;
-	if (nh < hist_cap) resid_hist[nh++] = sqrt(resid_scale * S.inprodR);
+	double prev_err = sqrt(resid_scale * S.inprodR);
 	S.niter = 1;
 	S.counter = 0;
 	// stagnation limits per method (iterative.c:118-125)
@@ -904,14 +1027,42 @@ int or_solve(or_ctx *c, int method, const double *einc, double eps, int maxiter,
 	bcgs2_state b2 = {-1, 0};
 	cplx ro_c = 0;
 	double ro_d = 0;
-	if (method == OR_QMR_CS) qmr_init(&S, &q);
-	else if (method == OR_BICGSTAB) {
-		bs.v = S.v1; bs.sv = S.v2; bs.rt = S.v3;
-		memcpy(bs.rt, S.r, sizeof(cplx) * n);
+	bs.v = S.v1; bs.sv = S.v2; bs.rt = S.v3;
+	q.v = S.v1; q.vt = S.v2; q.pn = S.p; q.po = S.v3;
+	cs.q_new = S.r; cs.q_old = S.v1; cs.p_new = S.p; cs.p_old = S.v2;
+	if (chp_in) {
+		chp_r R = {chp_in, chp_in_len, 0, 0};
+		int ind;
+		size_t rows;
+		chp_get(&R, &ind, sizeof(ind));
+		chp_get(&R, &rows, sizeof(rows));
+		if (R.bad || ind != chp_ind[method] || rows != n) {
+			free(S.r); free(S.p); free(S.Av); free(S.v1); free(S.v2); free(S.v3); free(S.v4);
+			return -1; // "is for different iterative method" / "different vector size" (iterative.c:238-241)
+		}
+		chp_get(&R, &S.niter, sizeof(int));
+		chp_get(&R, &S.counter, sizeof(int));
+		chp_get(&R, &S.inprodR, sizeof(double));
+		chp_get(&R, &prev_err, sizeof(double));
+		chp_get(&R, &resid_scale, sizeof(double));
+		chp_scalars(&R, 1, method, &q, &bs, &cs, &q2, &b2, &ro_c, &ro_d);
+		S.epsB = eps * eps / resid_scale;
+		chp_roles L = chp_layout(&S, method, &q, &bs, &cs);
+		chp_get(&R, S.x, sizeof(cplx) * n);
+		chp_get(&R, L.rvec, sizeof(cplx) * n);
+		chp_get(&R, L.pvec, sizeof(cplx) * n);
+		for (int v = 0; v < L.nvec; v++) chp_get(&R, L.vec[v], sizeof(cplx) * n);
+		if (R.bad || R.pos != R.len) { // "Failed reading" / "is too long" (iterative.c:258-266)
+			free(S.r); free(S.p); free(S.Av); free(S.v1); free(S.v2); free(S.v3); free(S.v4);
+			return -1;
+		}
 	}
+	else if (method == OR_QMR_CS) qmr_init(&S, &q);
+	else if (method == OR_BICGSTAB) memcpy(bs.rt, S.r, sizeof(cplx) * n);
 	else if (method == OR_CSYM) csym_init(&S, &cs);
 	else if (method == OR_QMR_CS_2) qmr2_init(&S, &q2);
 	else if (method == OR_BCGS2) memcpy(S.p, S.r, sizeof(cplx) * n); // r~0 = r_0, rho0 = -1
+	if (nh < hist_cap) resid_hist[nh++] = prev_err;
 	int status = OR_OK;
 	while (S.inprodR > S.epsB && S.niter <= maxiter && S.counter <= mcm) {
 		S.complete = 1;
@@ -930,8 +1081,28 @@ int or_solve(or_ctx *c, int method, const double *einc, double eps, int maxiter,
 			S.counter = 0;
 		}
 		else S.counter++;
-		if (nh < hist_cap) resid_hist[nh++] = sqrt(resid_scale * S.inprodRp1);
+		prev_err = sqrt(resid_scale * S.inprodRp1);
+		if (nh < hist_cap) resid_hist[nh++] = prev_err;
 		S.niter++;
+	}
+	if (chp_out_len && status == OR_OK) { // SaveIterChpoint after the loop (-chp_type always, iterative.c:1498)
+		chp_w W = {chp_out, *chp_out_len, 0};
+		int ind = chp_ind[method];
+		size_t rows = n;
+		chp_put(&W, &ind, sizeof(ind));
+		chp_put(&W, &rows, sizeof(rows));
+		chp_put(&W, &S.niter, sizeof(int));
+		chp_put(&W, &S.counter, sizeof(int));
+		chp_put(&W, &S.inprodR, sizeof(double));
+		chp_put(&W, &prev_err, sizeof(double));
+		chp_put(&W, &resid_scale, sizeof(double));
+		chp_scalars(&W, 0, method, &q, &bs, &cs, &q2, &b2, &ro_c, &ro_d);
+		chp_roles L = chp_layout(&S, method, &q, &bs, &cs);
+		chp_put(&W, S.x, sizeof(cplx) * n);
+		chp_put(&W, L.rvec, sizeof(cplx) * n);
+		chp_put(&W, L.pvec, sizeof(cplx) * n);
+		for (int v = 0; v < L.nvec; v++) chp_put(&W, L.vec[v], sizeof(cplx) * n);
+		*chp_out_len = W.len;
 	}
 	if (status == OR_OK && S.inprodR > S.epsB) status = (S.niter > maxiter) ? OR_EMAXITER : OR_ESTAGNATION;
 	for (size_t i = 0; i < c->n; i++)

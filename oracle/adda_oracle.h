@@ -9,6 +9,7 @@
  *   or_solve         <- IterativeSolver          src/iterative.c:1398-1530, QMR_CS :898-1032, BiCGStab :640-724,
  *                                               BiCG_CS :490-637, CGNR :729-769, CSYM :773-892,
  *                                               QMR_CS_2 :1038-1132, BCGS2 :340-487
+ *   or_solve_chp     <- SaveIterChpoint / LoadIterChpoint  src/iterative.c:165-278
  *   or_cross         <- ExtCross / AbsCross      src/crosssec.c:811-917 (plane wave, free space, Draine)
  *   or_field         <- CalcFieldFree            src/crosssec.c:506-596 (scattering amplitude in one direction)
  * Complex vectors are interleaved (re,im) doubles, dipole-major [dipole][3], like the reference's doublecomplex.
@@ -45,6 +46,14 @@ void or_set_cc_dip(or_ctx *c, const double *cc);
 void or_matvec(or_ctx *c, const double *argvec, double *resultvec, double *inprod, int her);
 int or_solve(or_ctx *c, int method, const double *einc, double eps, int maxiter, int init_field,
 	double *xvec, double *pvec, double *resid_hist, int hist_cap, int *niter_out);
+/* or_solve with the reference's iteration checkpoints (SaveIterChpoint / LoadIterChpoint, src/iterative.c:165-278):
+ * chp_in (chp_in_len bytes, the reference's chp.<ringid> format) replaces the initialisation by the saved state
+ * (the residual history then starts at the saved iteration number, resid_hist[0] = its RE value); chp_out receives
+ * the state at the end of the solve like -chp_type always (iterative.c:1498), *chp_out_len = bytes needed (written
+ * only when they fit the capacity passed in *chp_out_len). Returns -1 for a checkpoint of another method or size. */
+int or_solve_chp(or_ctx *c, int method, const double *einc, double eps, int maxiter, int init_field,
+	double *xvec, double *pvec, double *resid_hist, int hist_cap, int *niter_out, const void *chp_in,
+	size_t chp_in_len, void *chp_out, size_t *chp_out_len);
 void or_cross(or_ctx *c, const double *pvec, const double prop[3], const double incpol[3], double *cext,
 	double *cabs);
 void or_field(const or_ctx *c, const double *pvec, const double n[3], double *ebuff);

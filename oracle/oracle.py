@@ -55,6 +55,9 @@ def lib():
         L.or_matvec.argtypes = [c_p, c_p, c_p, c_p, c_i]
         L.or_solve.argtypes = [c_p, c_i, c_p, c_d, c_i, c_i, c_p, c_p, c_p, c_i, c_p]
         L.or_solve.restype = c_i
+        L.or_solve_chp.argtypes = [c_p, c_i, c_p, c_d, c_i, c_i, c_p, c_p, c_p, c_i, c_p, c_p, ctypes.c_size_t, c_p,
+                                   c_p]
+        L.or_solve_chp.restype = c_i
         L.or_set_interaction.argtypes = [c_p, ctypes.c_int]
         L.or_cisi.argtypes = [ctypes.c_double, c_p, c_p]
         L.or_cross.argtypes = [c_p, c_p, c_p, c_p, c_p, c_p]
@@ -118,15 +121,31 @@ class Oracle:
         self.L.or_matvec(self.h, _ptr(x), _ptr(y), ctypes.byref(ip), int(her))
         return y, ip.value
 
-    def solve(self, einc, method=QMR_CS, eps=1e-5, maxiter=100000, init_field=IF_AUTO, hist_cap=100000, x0=None):
+    def solve(self, einc, method=QMR_CS, eps=1e-5, maxiter=100000, init_field=IF_AUTO, hist_cap=100000, x0=None,
+              chp_in=None, chp_save=False):
+        """chp_in: the reference's checkpoint bytes to resume from (resid then starts at the saved iteration);
+        chp_save: also return the final state as checkpoint bytes ('chp', like -chp_type always)"""
         einc = np.ascontiguousarray(einc, dtype=np.complex128)
         x = np.empty_like(einc) if x0 is None else np.array(x0, dtype=np.complex128)
         p = np.empty_like(einc)
         hist = np.zeros(hist_cap)
         nit = ctypes.c_int(0)
-        st = self.L.or_solve(self.h, method, _ptr(einc), eps, maxiter, init_field, _ptr(x), _ptr(p), _ptr(hist),
-                             hist_cap, ctypes.byref(nit))
-        return dict(status=st, niter=nit.value, x=x, p=p, resid=hist[:min(nit.value + 1, hist_cap)])
+        cin = None if chp_in is None else ctypes.create_string_buffer(bytes(chp_in), len(chp_in))
+        cap = 64 + 8 * 16 + 8 * x.size * 16
+        cout = ctypes.create_string_buffer(cap) if chp_save else None
+        clen = ctypes.c_size_t(cap)
+        st = self.L.or_solve_chp(self.h, method, _ptr(einc), eps, maxiter, init_field, _ptr(x), _ptr(p), _ptr(hist),
+                                 hist_cap, ctypes.byref(nit), cin, 0 if chp_in is None else len(chp_in), cout,
+                                 ctypes.byref(clen) if chp_save else None)
+        if st < 0:
+            raise ValueError("checkpoint is for another iterative method or vector size")
+        first = 0
+        if chp_in is not None:
+            first = int(np.frombuffer(bytes(chp_in)[12:16], np.int32)[0]) - 1
+        res = dict(status=st, niter=nit.value, x=x, p=p, resid=hist[:min(nit.value + 1 - first, hist_cap)])
+        if chp_save:
+            res["chp"] = cout.raw[:clen.value]
+        return res
 
     def cross(self, pvec, prop, incpol):
         pvec = np.ascontiguousarray(pvec, dtype=np.complex128)

@@ -50,7 +50,8 @@ def wkb_x0(s, pol_index):
     return A.field_to_x0(e, s.cc[pol_index].reshape(1, 3), [s.m], s.gridspace, s.mat)
 
 
-def oracle_solve(o, s, pol_index, method="qmr", eps=1e-5, maxiter=100000, init="auto", x0=None):
+def oracle_solve(o, s, pol_index, method="qmr", eps=1e-5, maxiter=100000, init="auto", x0=None, chp_in=None,
+                 chp_save=False):
     if init == "wkb":
         init, x0 = "x0", wkb_x0(s, pol_index)
     from oracle import oracle as O
@@ -58,10 +59,31 @@ def oracle_solve(o, s, pol_index, method="qmr", eps=1e-5, maxiter=100000, init="
     methods = {"qmr": O.QMR_CS, "bicgstab": O.BICGSTAB, "bicg": O.BICG_CS, "cgnr": O.CGNR, "csym": O.CSYM,
                "qmr2": O.QMR_CS_2, "bcgs2": O.BCGS2}
     r = o.solve(s.einc[pol_index], method=methods[method], eps=eps, maxiter=maxiter,
-                init_field={"auto": O.IF_AUTO, "zero": O.IF_ZERO, "inc": O.IF_INC, "x0": O.IF_X0}[init], x0=x0)
+                init_field={"auto": O.IF_AUTO, "zero": O.IF_ZERO, "inc": O.IF_INC, "x0": O.IF_X0}[init], x0=x0,
+                chp_in=chp_in, chp_save=chp_save)
     ce, ca = o.cross(r["p"], s.prop, s.incpol[pol_index])
     r["Cext"], r["Cabs"] = ce, ca
     return r
+
+
+CHP_SCALARS = {"bcgs2": "cc", "bicg": "c", "bicgstab": "ccc", "cgnr": "d", "csym": "dddccc", "qmr": "ddddcccc",
+               "qmr2": "dddcc"}  # d: double, c: doublecomplex, in the order of each method's PHASE_VARS
+
+
+def parse_chpoint(raw, method):
+    """the reference's chp.<ringid> bytes (SaveIterChpoint, iterative.c:165-218): (ind_m, nRows, niter, counter,
+    inprodR, prev_err, resid_scale), [scalars], vectors [k][nRows] (xvec, rvec, pvec, then the method's own)"""
+    import struct
+    head = struct.unpack("<iQiiddd", raw[:44])
+    off, sc = 44, []
+    for t in CHP_SCALARS[method]:
+        if t == "d":
+            sc.append(struct.unpack("<d", raw[off:off + 8])[0])
+            off += 8
+        else:
+            sc.append(complex(*struct.unpack("<dd", raw[off:off + 16])))
+            off += 16
+    return head, sc, np.frombuffer(raw[off:], np.complex128).reshape(-1, head[1])
 
 
 def rel(a, b):
