@@ -18,8 +18,8 @@ SHAPES = {"sphere": 0, "ellipsoid": 1, "box": 2}
 POLS = {"ldr": 0, "cm": 1, "rrc": 2, "dgf": 3, "cldr": 4, "fcd": 5, "igt_so": 6, "lak": 7, "so": 8}
 ITERS = {"qmr": 0, "bicgstab": 1, "bicg": 2, "cgnr": 3, "csym": 4, "qmr2": 5, "bcgs2": 6}
 PREC = {"fp64": 0, "fp32": 1, "mixed": 2, "mixed_f32vec": 3, "mixed_f64vec": 4}
-INIT = {"auto": 0, "zero": 1, "inc": 2, "x0": 3}
-STATUS = {0: "ok", 1: "breakdown", 2: "stagnation", 3: "maxiter"}
+INIT = {"auto": 0, "zero": 1, "inc": 2, "x0": 3, "chpoint": 4}
+STATUS = {0: "ok", 1: "breakdown", 2: "stagnation", 3: "maxiter", 4: "chpoint"}
 
 
 class AddaError(RuntimeError):
@@ -40,7 +40,8 @@ INTERACTIONS = {"poi": 0, "fcd": 1, "fcd_st": 2}
 class SolveParams(ctypes.Structure):
     _fields_ = [("method", ctypes.c_int), ("precision", ctypes.c_int), ("eps", ctypes.c_double),
                 ("maxiter", ctypes.c_int), ("init_field", ctypes.c_int), ("check_every", ctypes.c_int),
-                ("inner_eps", ctypes.c_double), ("max_refine", ctypes.c_int)]
+                ("inner_eps", ctypes.c_double), ("max_refine", ctypes.c_int), ("chp_time", ctypes.c_double),
+                ("full_steps", ctypes.c_int)]
 
 
 class RhsStats(ctypes.Structure):
@@ -55,6 +56,7 @@ EXPORTS = ["adda_gb300_fft_fit", "adda_gb300_fit_box", "adda_gb300_make_particle
            "adda_gb300_get_grid", "adda_gb300_init_dmatrix", "adda_gb300_dmatrix_len", "adda_gb300_get_dmatrix",
            "adda_gb300_set_cc", "adda_gb300_set_cc_sqrt", "adda_gb300_set_cc_dipole", "adda_gb300_matvec", "adda_gb300_matvec_device",
            "adda_gb300_solve", "adda_gb300_solve_device", "adda_gb300_solve_many", "adda_gb300_vjp_chi",
+           "adda_gb300_chpoint_size", "adda_gb300_chpoint_save", "adda_gb300_chpoint_load",
            "adda_gb300_cross_sections", "adda_gb300_scattered_fields",
            "adda_gb300_cross_sections_noalloc", "adda_gb300_time_matvec",
            "adda_gb300_last_solve_ms", "adda_gb300_last_error", "adda_gb300_kernel_launches"]
@@ -101,6 +103,9 @@ def lib():
             "adda_gb300_solve": ([P, P, I, P, P, P, P, P, I], I),
             "adda_gb300_solve_device": ([P, P, I, P, P, P, P], I),
             "adda_gb300_solve_many": ([I, P, P, P, P, P, P, P], I),
+            "adda_gb300_chpoint_size": ([P, I], SZ),
+            "adda_gb300_chpoint_save": ([P, I, P, SZ], I),
+            "adda_gb300_chpoint_load": ([P, I, P, SZ], I),
             "adda_gb300_time_matvec": ([P, I, I, I, SZ, P], I),
             "adda_gb300_cross_sections": ([P, I, P, P, P, P], I),
             "adda_gb300_scattered_fields": ([P, I, I, P, P], I),
@@ -257,7 +262,7 @@ def solve_many(ctxs, eincs, method="qmr", prec="mixed", eps=1e-5, maxiter=100000
     P = ctypes.c_void_p
     arr = lambda vals: (P * n)(*vals)
     nr = (ctypes.c_int * n)(*[e.shape[0] for e in es])
-    sp = SolveParams(ITERS[method], PREC[prec], eps, maxiter, INIT[init], check_every, 0.0, 0)
+    sp = SolveParams(ITERS[method], PREC[prec], eps, maxiter, INIT[init], check_every, 0.0, 0, 0.0, 0)
     _check(L.adda_gb300_solve_many(n, arr([c.h.value for c in ctxs]), ctypes.byref(sp), nr,
                                    arr([e.ctypes.data for e in es]), arr([x.ctypes.data for x in xs]),
                                    arr([p.ctypes.data for p in ps]), arr([ctypes.addressof(s) for s in sts])),
@@ -333,9 +338,11 @@ class Context:
         return (y[0], ip[0]) if one else (y, ip)
 
     def solve(self, einc, method="qmr", prec="fp64", eps=1e-5, maxiter=100000, init="auto", check_every=0,
-              inner_eps=0.0, max_refine=0, hist_cap=0, x0=None):
-        """einc: [nrhs, 3N] complex. Returns dict with x, p [nrhs,3N], stats per RHS and residual histories.
-        init="x0" starts from x0 [nrhs, 3N] (see field_to_x0 for a field read from file or from wkb_field)."""
+              inner_eps=0.0, max_refine=0, hist_cap=0, x0=None, chp_time=0.0, full_steps=False):
+        """einc: [nrhs, 3N] complex. Returns dict with x, p [nrhs,3N], stats per RHS and residual histories
+        (hist[r][k] = RE_k). init="x0" starts from x0 [nrhs, 3N] (see field_to_x0 for a field read from file or from
+        wkb_field); init="chpoint" resumes every RHS from chpoint_load. chp_time > 0 stops after that many seconds
+        (status "chpoint", state kept for chpoint_save); full_steps: BiCGStab without its half-step exit."""
         e = np.ascontiguousarray(einc, dtype=np.complex128).reshape(-1, 3 * self.n)
         R = e.shape[0]
         if init == "x0":
@@ -345,7 +352,8 @@ class Context:
         p = np.empty_like(e)
         st = (RhsStats * R)()
         hist = np.zeros((R, hist_cap)) if hist_cap else None
-        sp = SolveParams(ITERS[method], PREC[prec], eps, maxiter, INIT[init], check_every, inner_eps, max_refine)
+        sp = SolveParams(ITERS[method], PREC[prec], eps, maxiter, INIT[init], check_every, inner_eps, max_refine,
+                         chp_time, int(full_steps))
         _check(self.L.adda_gb300_solve(self.h, ctypes.byref(sp), R, _p(e), _p(x), _p(p), st, _p(hist), hist_cap),
                "solve")
         stats = [dict(niter=s.niter, status=STATUS.get(s.status, s.status), resid=s.resid,
@@ -357,12 +365,32 @@ class Context:
                      init="auto", check_every=0, inner_eps=0.0, max_refine=0):
         """solve on device-resident buffers (raw CUDA pointers as ints, double2 [nrhs][3N])"""
         st = (RhsStats * nrhs)()
-        sp = SolveParams(ITERS[method], PREC[prec], eps, maxiter, INIT[init], check_every, inner_eps, max_refine)
+        sp = SolveParams(ITERS[method], PREC[prec], eps, maxiter, INIT[init], check_every, inner_eps, max_refine,
+                         0.0, 0)
         _check(self.L.adda_gb300_solve_device(self.h, ctypes.byref(sp), nrhs, ctypes.c_void_p(d_einc),
                                               ctypes.c_void_p(d_x) if d_x else None,
                                               ctypes.c_void_p(d_p) if d_p else None, st), "solve_device")
         return [dict(niter=s.niter, status=STATUS.get(s.status, s.status), resid=s.resid, refinements=s.refinements,
                      matvecs_fp64=s.matvecs_fp64, matvecs_fp32=s.matvecs_fp32) for s in st]
+
+    def chpoint_size(self, method="qmr"):
+        """bytes of an iteration checkpoint of that method (the reference's chp.<ringid> format)"""
+        return self.L.adda_gb300_chpoint_size(self.h, ITERS[method])
+
+    def chpoint_save(self, rhs=0):
+        """the FP64 solver state of right-hand side rhs after the last solve, as the reference's checkpoint bytes"""
+        # the method of the last solve is not known here: try the sizes (each method has its own)
+        n = max(self.chpoint_size(m) for m in ITERS)
+        buf = ctypes.create_string_buffer(n)
+        _check(self.L.adda_gb300_chpoint_save(self.h, rhs, buf, n), "chpoint_save")
+        head = np.frombuffer(buf.raw[:4], np.int32)[0]
+        meth = {5: "qmr", 2: "bicgstab", 1: "bicg", 3: "cgnr", 4: "csym", 6: "qmr2", 0: "bcgs2"}[int(head)]
+        return buf.raw[:self.chpoint_size(meth)]
+
+    def chpoint_load(self, rhs, data):
+        """keep checkpoint bytes (the reference's chp.<ringid> file) for the next solve with init="chpoint" """
+        data = bytes(data)
+        _check(self.L.adda_gb300_chpoint_load(self.h, rhs, data, len(data)), "chpoint_load")
 
     def last_solve_ms(self):
         """device milliseconds of the last solve (CUDA events on the context stream)"""
@@ -381,7 +409,7 @@ class Context:
         f = np.ascontiguousarray(dinv_alpha, dtype=np.complex128).reshape(self.n)
         ge = np.zeros((self.n, 2))
         ga = np.zeros((self.n, 2))
-        sp = SolveParams(ITERS[method], PREC[prec], eps, maxiter, INIT["zero"], 0, 0.0, 0)
+        sp = SolveParams(ITERS[method], PREC[prec], eps, maxiter, INIT["zero"], 0, 0.0, 0, 0.0, 0)
         _check(self.L.adda_gb300_vjp_chi(self.h, ctypes.byref(sp), rhs, _p(np.ascontiguousarray(prop, float)),
                                          _p(np.ascontiguousarray(incpol, float)), _p(f), _p(ge), _p(ga)), "vjp_chi")
         return ge, ga

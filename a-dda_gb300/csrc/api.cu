@@ -537,6 +537,31 @@ int adda_gb300_solve(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int n
 	return solver_solve(c, sp, nrhs, einc, xvec, pvec, stats, resid_hist, hist_cap);
 }
 
+size_t adda_gb300_chpoint_size(const adda_gb300_ctx *c, int method)
+{
+	return c ? solver_chpoint_size(c, method) : 0;
+}
+
+int adda_gb300_chpoint_save(adda_gb300_ctx *c, int rhs, void *buf, size_t size)
+{
+	if (!c) {
+		set_error("chpoint_save: invalid arguments");
+		return ADDA_GB300_EINVAL;
+	}
+	ADDA_CUDA(cudaSetDevice(c->device));
+	return solver_chpoint_save(c, rhs, buf, size);
+}
+
+int adda_gb300_chpoint_load(adda_gb300_ctx *c, int rhs, const void *buf, size_t size)
+{
+	if (!c) {
+		set_error("chpoint_load: invalid arguments");
+		return ADDA_GB300_EINVAL;
+	}
+	ADDA_CUDA(cudaSetDevice(c->device));
+	return solver_chpoint_load(c, rhs, buf, size);
+}
+
 int adda_gb300_solve_many(int nctx, adda_gb300_ctx *const *ctxs, const adda_gb300_solve_params *sp, const int *nrhs,
 	const double *const *einc, double *const *xvec, double *const *pvec, adda_gb300_rhs_stats *const *stats)
 {

@@ -123,6 +123,9 @@ int solver_solve_dev(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int n
 	double2 *d_xvec, double2 *d_pvec, adda_gb300_rhs_stats *stats);
 void solver_free(adda_gb300_ctx *c);
 int cross_sections(adda_gb300_ctx *c, int nrhs, const double *prop, const double *incpol, double *cext, double *cabs);
+size_t solver_chpoint_size(const adda_gb300_ctx *c, int method);
+int solver_chpoint_save(adda_gb300_ctx *c, int rhs, void *buf, size_t size);
+int solver_chpoint_load(adda_gb300_ctx *c, int rhs, const void *buf, size_t size);
 int scattered_fields(adda_gb300_ctx *c, int nrhs, int ndir, const double *dirs, double *ebuff);
 int vjp_chi(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int rhs, const double prop[3], const double incpol[3],
 	const double *dinv_alpha, double *grad_cext, double *grad_cabs);

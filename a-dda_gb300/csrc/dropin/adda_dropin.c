@@ -29,6 +29,9 @@ enum enwho { ALL, ONE };                                           /* const.h:40
 enum ec { EC_OK, EC_ERROR, EC_WARN, EC_INFO };                     /* const.h:418-423 */
 enum inter { G_FCD, G_FCD_ST, G_IGT, G_IGT_SO, G_NLOC, G_NLOC_AV, G_POINT_DIP, G_SO }; /* const.h:212-224 */
 enum init_field { IF_AUTO, IF_ZERO, IF_INC, IF_READ, IF_WKB };     /* const.h:321-327 */
+enum chpoint { CHP_NONE, CHP_NORMAL, CHP_REGULAR, CHP_ALWAYS };     /* const.h:313-319 */
+#define CHP_EXIT -2                                                  /* const.h:330 */
+#define UNDEF -1                                                     /* const.h:47 */
 
 /* globals of the reference host: vars.c, param.c, timing.c, calculator.c */
 extern int boxX, boxY, boxZ, nprocs, Nmat, maxiter;
@@ -48,12 +51,20 @@ void ReadField(const char *fname, doublecomplex *field); /* comm.c:562 */
 extern const double iter_eps;
 extern const enum init_field InitField;
 extern const bool recalc_resid;
+extern const enum chpoint chp_type;                                  /* param.c:142-144 */
+extern const time_t chp_time;
+extern const char *chp_dir;
+extern bool load_chpoint;                                            /* vars.c:54 */
+extern const char *directory;                                        /* vars.c:71 */
+extern int ringid;                                                   /* vars.c:100 */
+extern time_t last_chp_wt;                                           /* timing.c:60 */
 extern clock_t Timing_Dm_Init, Timing_FFT_Init, Timing_OneIter, Timing_InitIter, Timing_MVP;
 extern size_t TotalIter, TotalMatVec;
 /* host services: io.c */
 void LogError(enum enwho who, const char *srcfile, int srcline, const char *fmt, ...);
 void LogWarning(enum ec code, enum enwho who, const char *srcfile, int srcline, const char *fmt, ...);
 void PrintBoth(FILE *file, const char *fmt, ...);
+void MkDirErr(const char *dir, enum enwho who, const char *srcfile, int srcline);
 
 /* the reference's fft.c also defines these globals; other reference files may name them */
 doublecomplex *Xmatrix, *Dmatrix, *slices, *slices_tr;
@@ -62,6 +73,7 @@ double *BT_buffer, *BT_rbuffer;
 #define ERR(...) LogError(ONE, __FILE__, __LINE__, __VA_ARGS__)
 
 static adda_gb300_ctx *g_ctx;
+static int g_method; /* ADDA_ITER_* of the current IterativeSolver */
 /* the device polarisations belong to the host's pvec of the last IterativeSolver */
 static int g_pvec_valid = 0;
 static doublecomplex g_ccs[MAX_NMAT][3];
@@ -160,6 +172,52 @@ static void report(int niter, double err, double prev_err, int counter)
 	printf("RE_%03d = %.10E  %s\n", niter, err, tag);
 }
 
+/* SaveIterChpoint (iterative.c:165-218): <chp_dir>/chp.log and <chp_dir>/chp.<ringid> in the reference's format */
+static void save_chpoint(void)
+{
+	char fname[4096];
+	snprintf(fname, sizeof(fname), "%s/chp.log", chp_dir);
+	FILE *f = fopen(fname, "w");
+	if (!f) {
+		MkDirErr(chp_dir, ONE, __FILE__, __LINE__);
+		f = fopen(fname, "w");
+	}
+	if (!f) ERR("Failed to open file '%s'", fname);
+	fprintf(f, "Info about the run, which produced the checkpoint, can be found in ../%s", directory);
+	fclose(f);
+	size_t n = adda_gb300_chpoint_size(g_ctx, g_method);
+	unsigned char *buf = malloc(n);
+	if (!buf || adda_gb300_chpoint_save(g_ctx, 0, buf, n)) ERR("GPU checkpoint failed: %s", adda_gb300_last_error());
+	snprintf(fname, sizeof(fname), "%s/chp.%d", chp_dir, ringid);
+	if (!(f = fopen(fname, "wb"))) ERR("Failed to open file '%s'", fname);
+	if (fwrite(buf, 1, n, f) != n) ERR("Failed writing to file '%s'", fname);
+	fclose(f);
+	free(buf);
+	PrintBoth(logfile, "Checkpoint (iteration) saved\n");
+}
+
+/* LoadIterChpoint (iterative.c:222-278): the file is checked by the library and applied by the next solve */
+static void load_chpoint_file(void)
+{
+	char fname[4096];
+	snprintf(fname, sizeof(fname), "%s/chp.%d", chp_dir, ringid);
+	FILE *f = fopen(fname, "rb");
+	if (!f) ERR("Failed to open file '%s'", fname);
+	fseek(f, 0, SEEK_END);
+	const long n = ftell(f);
+	fseek(f, 0, SEEK_SET);
+	unsigned char *buf = malloc(n > 0 ? (size_t)n : 1);
+	if (n <= 0 || fread(buf, 1, (size_t)n, f) != (size_t)n) ERR("Failed reading from file '%s'", fname);
+	fclose(f);
+	int ind;
+	memcpy(&ind, buf, sizeof(int));
+	const int ind_of[7] = {5, 2, 1, 3, 4, 6, 0}; /* params table order, iterative.c:118-125 */
+	if (ind != ind_of[g_method]) ERR("File '%s' is for different iterative method", fname);
+	if (adda_gb300_chpoint_load(g_ctx, 0, buf, (size_t)n)) ERR("File '%s': %s", fname, adda_gb300_last_error());
+	free(buf);
+	PrintBoth(logfile, "Checkpoint (iteration) loaded\n");
+}
+
 int IterativeSolver(enum iter method, enum incpol which)
 {
 	adda_gb300_solve_params sp;
@@ -202,38 +260,83 @@ int IterativeSolver(enum iter method, enum incpol which)
 	sp.precision = env_prec();
 	sp.eps = iter_eps;
 	sp.maxiter = maxiter;
+	g_method = sp.method;
+	/* checkpoints (iterative.c:165-278,308-317,1498) work on the FP64 solver state */
+	if ((load_chpoint || chp_type != CHP_NONE) && sp.precision != ADDA_PREC_FP64)
+		ERR("Checkpoints need ADDA_GB300_PREC=fp64 in the GPU build");
+	if (load_chpoint) {
+		load_chpoint_file();
+		sp.init_field = ADDA_IF_CHPOINT;
+	}
+	if (chp_type == CHP_ALWAYS) sp.full_steps = 1; /* no half-step exit of BiCGStab (iterative.c:703) */
 	clock_t t0 = clock();
 	sync_cc();
 	const int cap = (maxiter < 100000 ? maxiter : 100000) + 2;
 	double *hist = calloc((size_t)cap, sizeof(double));
 	adda_gb300_rhs_stats st;
-	int rc = adda_gb300_solve(g_ctx, &sp, 1, (const double *)Einc, (double *)xvec, (double *)pvec, &st, hist, cap);
-	if (rc < 0) ERR("GPU IterativeSolver failed: %s", adda_gb300_last_error());
-	/* print the initial field choice and the residual history like IterativeSolver/ProgressReport */
-	if (sp.precision == ADDA_PREC_FP64) {
-		const char *descr = (sp.init_field == ADDA_IF_ZERO || (sp.init_field == ADDA_IF_AUTO && hist[0] == 1.0))
-			? "x_0 = 0\n" : "x_0 = E_inc\n";
-		char fdescr[512];
-		if (InitField == IF_WKB) descr = "x_0 = result of WKB\n"; /* iterative.c:1383,1390 */
-		else if (InitField == IF_READ) {
-			snprintf(fdescr, sizeof(fdescr), "x_0 = from file %s\n", which == INCPOL_Y ? infi_fnameY : infi_fnameX);
-			descr = fdescr;
+	int chp_exit = 0, first = 1, matvecs = 0;
+	for (;;) {
+		/* -chpoint <time>: the time left until the next checkpoint, counted from the last one (timing.c:102) */
+		if (chp_type != CHP_NONE && chp_time != UNDEF) {
+			const double left = (double)chp_time - difftime(time(NULL), last_chp_wt);
+			sp.chp_time = left > 0 ? left : 1e-9;
 		}
-		if (!orient_avg && logfile) fprintf(logfile, "%sRE_%03d = %.10E\n", descr, 0, hist[0]);
-		printf("%sRE_%03d = %.10E\n", descr, 0, hist[0]);
-		double best = hist[0], prev = hist[0];
-		int counter = 0;
-		for (int i = 1; i <= st.niter && i < cap; i++) {
-			if (hist[i] <= best) { best = hist[i]; counter = 0; }
-			else counter++;
-			report(i, hist[i], prev, counter);
-			prev = hist[i];
+		int rc = adda_gb300_solve(g_ctx, &sp, 1, (const double *)Einc, (double *)xvec, (double *)pvec, &st, hist,
+			cap);
+		if (rc < 0) ERR("GPU IterativeSolver failed: %s", adda_gb300_last_error());
+		matvecs += st.matvecs_fp64 + st.matvecs_fp32;
+		/* print the initial field choice and the residual history like IterativeSolver/ProgressReport */
+		if (sp.precision == ADDA_PREC_FP64) {
+			int i0 = 1;
+			if (sp.init_field == ADDA_IF_CHPOINT) {
+				/* resumed: the history continues after the saved iteration (hist[k] = RE_k) */
+				while (i0 < cap && hist[i0 - 1] == 0) i0++;
+				first = 0;
+			}
+			if (first) {
+				const char *descr = (sp.init_field == ADDA_IF_ZERO ||
+					(sp.init_field == ADDA_IF_AUTO && hist[0] == 1.0)) ? "x_0 = 0\n" : "x_0 = E_inc\n";
+				char fdescr[512];
+				if (InitField == IF_WKB) descr = "x_0 = result of WKB\n"; /* iterative.c:1383,1390 */
+				else if (InitField == IF_READ) {
+					snprintf(fdescr, sizeof(fdescr), "x_0 = from file %s\n",
+						which == INCPOL_Y ? infi_fnameY : infi_fnameX);
+					descr = fdescr;
+				}
+				if (!orient_avg && logfile) fprintf(logfile, "%sRE_%03d = %.10E\n", descr, 0, hist[0]);
+				printf("%sRE_%03d = %.10E\n", descr, 0, hist[0]);
+			}
+			double best = hist[i0 - 1], prev = hist[i0 - 1];
+			int counter = 0;
+			for (int i = i0; i <= st.niter && i < cap; i++) {
+				if (hist[i] <= best) { best = hist[i]; counter = 0; }
+				else counter++;
+				report(i, hist[i], prev, counter);
+				prev = hist[i];
+			}
 		}
+		else {
+			PrintBoth(logfile, "Mixed precision: %d FP32 iterations, %d FP64 refinement steps, final FP64 residual "
+				"RE = %.10E\n", st.niter, st.refinements, st.resid);
+		}
+		if (st.status != ADDA_GB300_CHPOINT) break;
+		/* the checkpoint time has passed (ProgressReport, iterative.c:308-317) */
+		save_chpoint();
+		time(&last_chp_wt);
+		if (chp_type != CHP_REGULAR) {
+			chp_exit = 1;
+			break;
+		}
+		/* regular checkpoints: carry on from the state just saved */
+		size_t n = adda_gb300_chpoint_size(g_ctx, g_method);
+		unsigned char *buf = malloc(n);
+		if (!buf || adda_gb300_chpoint_save(g_ctx, 0, buf, n) || adda_gb300_chpoint_load(g_ctx, 0, buf, n))
+			ERR("GPU checkpoint failed: %s", adda_gb300_last_error());
+		free(buf);
+		sp.init_field = ADDA_IF_CHPOINT;
+		first = 0;
 	}
-	else {
-		PrintBoth(logfile, "Mixed precision: %d FP32 iterations, %d FP64 refinement steps, final FP64 residual "
-			"RE = %.10E\n", st.niter, st.refinements, st.resid);
-	}
+	if (chp_type == CHP_ALWAYS && !chp_exit) save_chpoint(); /* iterative.c:1498 */
 	free(hist);
 	if (st.status == ADDA_GB300_EBREAKDOWN) ERR("Krylov solver breakdown on the GPU (iteration %d)", st.niter);
 	if (st.status == ADDA_GB300_ESTAGNATION)
@@ -258,11 +361,12 @@ int IterativeSolver(enum iter method, enum incpol which)
 		printf("Final (recalculated) residual norm: %.10E\n", sqrt(num / den));
 	}
 	TotalIter += (size_t)st.niter;
-	TotalMatVec += (size_t)(st.matvecs_fp64 + st.matvecs_fp32);
+	TotalMatVec += (size_t)matvecs;
 	Timing_InitIter = 0;
 	Timing_MVP = clock() - t0;
 	Timing_OneIter = st.niter ? (clock() - t0) / st.niter : 0;
 	g_pvec_valid = 1;
+	if (chp_exit) return CHP_EXIT; /* iterative.c:1528 */
 	return st.niter;
 }
 

@@ -24,6 +24,7 @@
 #include "ctx.cuh"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <type_traits>
@@ -34,6 +35,9 @@ namespace adda {
 struct RhsState {
 	double inprodR, inprodRp1, epsB, resid_scale;
 	int niter, counter, done, status, half, mc, maxiter, x0zero;
+	int it0;  // niter when the current Krylov run started (role parity of the swapped QMR_CS / CSYM buffers)
+	double prev_err; // last reported relative residual (ProgressReport's prev_err, kept in checkpoints)
+	int full; // BiCGStab: no half-step exit
 	// QMR_CS
 	double c_old, c_new, om_old, om_new;
 	double2 beta, tautilda, s_old, s_new, alpha, theta, eta, zetat;
@@ -67,6 +71,9 @@ struct SolverWork {
 	int nbv = 0;
 	double *xpart = nullptr; // cross-section partials
 	int *h_done = nullptr;   // pinned
+	// iteration checkpoints: the state of the last FP64 solve (valid until the next solve) and loaded states
+	int chp_valid = 0, chp_method = -1, chp_R = 0;
+	std::vector<std::vector<unsigned char>> chp_pend;
 	// cached graph
 	cudaGraphExec_t gexec = nullptr;
 	int g_method = -1, g_dbl = -1, g_R = -1, g_K = -1;
@@ -191,11 +198,13 @@ __global__ void s_init(RhsState *st, int *done, const double *part, int nbv, dou
 	S.maxiter = maxiter;
 	S.mc = mc;
 	S.niter = 1;
+	S.it0 = 1;
 	S.counter = 0;
 	S.status = 0;
 	if (zero_init) {
 		S.inprodR = s[0];
-		if (hist_cap > 0) hist[(size_t)r * hist_cap] = sqrt(S.resid_scale * S.inprodR);
+		S.prev_err = sqrt(S.resid_scale * S.inprodR);
+		if (hist_cap > 0) hist[(size_t)r * hist_cap] = S.prev_err;
 		S.done = !(S.inprodR > S.epsB && S.niter <= S.maxiter);
 		done[r] = S.done;
 	}
@@ -243,7 +252,8 @@ __global__ void s_init_choose(RhsState *st, int *done, const double *part, int n
 		S.inprodR = S.temp;
 		S.x0zero = 1; // x0 = 0
 	}
-	if (hist_cap > 0) hist[(size_t)r * hist_cap] = sqrt(S.resid_scale * S.inprodR);
+	S.prev_err = sqrt(S.resid_scale * S.inprodR);
+	if (hist_cap > 0) hist[(size_t)r * hist_cap] = S.prev_err;
 	S.done = !(S.inprodR > S.epsB && S.niter <= S.maxiter);
 	done[r] = S.done;
 }
@@ -424,7 +434,8 @@ __global__ void s_progress(RhsState *st, int *done, const double *part, int nbv,
 		S.counter = 0;
 	}
 	else S.counter++;
-	if (S.niter < hist_cap) hist[(size_t)r * hist_cap + S.niter] = sqrt(S.resid_scale * S.inprodRp1);
+	S.prev_err = sqrt(S.resid_scale * S.inprodRp1);
+	if (S.niter < hist_cap) hist[(size_t)r * hist_cap + S.niter] = S.prev_err;
 	S.niter++;
 	S.done = !(S.inprodR > S.epsB && S.niter <= S.maxiter && S.counter <= S.mc);
 	done[r] = S.done;
@@ -521,7 +532,7 @@ __global__ void bs_s2(RhsState *st, const double *part, int nbv)
 	if (threadIdx.x) return;
 	RhsState &S = st[r];
 	S.inprodRp1 = s[0];
-	S.half = (S.inprodRp1 < S.epsB) ? 1 : 0; // converged at the half step (iterative.c:703-707)
+	S.half = (S.inprodRp1 < S.epsB && !S.full) ? 1 : 0; // converged at the half step (iterative.c:703-707)
 }
 
 // omega = s.t* / |t|^2 (matvec epilogue: slot 0 = |t|^2, slots 1,2 = s.t*)
@@ -853,6 +864,17 @@ __global__ void q2_init_s(RhsState *st, const double *part, int nbv)
 	S.q2_theta = 0;
 	S.q2_eta = dc(-1, 0);
 	S.q2_delta = dscal(dc(s[1], s[2]), 1 / S.inprodR);
+}
+
+// resumed from a checkpoint: delta_k = v_k.v_k with v_k = v~_k/ro_k, from the v~.v~ partials (slots 1,2 of k_dot)
+__global__ void q2_resume_s(RhsState *st, const double *part, int nbv)
+{
+	const int r = blockIdx.x;
+	double s[4];
+	sum_part(part, nbv, r, s, 3);
+	if (threadIdx.x || st[r].done) return;
+	RhsState &S = st[r];
+	S.q2_delta = dscal(dc(s[1], s[2]), 1 / (S.q2_ro * S.q2_ro));
 }
 
 // delta_k test (:1086-1089); p coefficient -ro_k*delta_k/eps_(k-1) (:1091-1094); v scale 1/ro_k
@@ -1609,8 +1631,11 @@ static int enqueue_iter(adda_gb300_ctx *c, SolverWork *w, int method, int R, int
 
 // Krylov solve of A.x = b on the typed vectors (b given in k.r on entry for zero init, or in bsrc). Runs until all
 // RHS are done. Returns via st on the device.
+// resume: the method's PHASE_INIT is replaced by a loaded checkpoint (iteration state already in place);
+// chp_time > 0: stop once that many seconds have passed since t0 (checked between graph launches), *stopped = true
 template <typename T, typename C>
-static int krylov(adda_gb300_ctx *c, SolverWork *w, int method, int R, int K, unsigned long long *iters_run)
+static int krylov(adda_gb300_ctx *c, SolverWork *w, int method, int R, int K, unsigned long long *iters_run,
+	bool resume = false, double chp_time = 0, std::chrono::steady_clock::time_point t0 = {}, bool *stopped = nullptr)
 {
 	// graph key: arithmetic and vector type
 	const int mode = (sizeof(T) == 8 ? 0 : 1) + (sizeof(C) == 8 ? 2 : 0) + (std::is_same<C, dd2>::value ? 4 : 0);
@@ -1619,7 +1644,8 @@ static int krylov(adda_gb300_ctx *c, SolverWork *w, int method, int R, int K, un
 	const dim3 gv(w->nbv, R);
 	cudaStream_t s = c->stream;
 	// method initialisation (PHASE_INIT)
-	if (method == ADDA_ITER_QMR_CS) {
+	if (resume) {}
+	else if (method == ADDA_ITER_QMR_CS) {
 		k_dot<C><<<gv, NT, 0, s>>>(k.r, k.r, n3, 0, w->vpart, w->nbv);
 		ADDA_LAUNCHED();
 		qmr_s_init<<<R, NT, 0, s>>>(w->st, w->vpart, w->nbv);
@@ -1699,6 +1725,11 @@ static int krylov(adda_gb300_ctx *c, SolverWork *w, int method, int R, int K, un
 		bool all = true;
 		for (int r = 0; r < R; r++) all = all && w->h_done[r];
 		if (all) break;
+		if (chp_time > 0 && n > 0 &&
+			std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() >= chp_time) {
+			if (stopped) *stopped = true;
+			break;
+		}
 		ADDA_CUDA(cudaGraphLaunch(w->gexec, s));
 		count_launch(w->g_nodes);
 		n += K;
@@ -1878,12 +1909,100 @@ static int check_params(const adda_gb300_solve_params *sp)
 	if (sp->method < ADDA_ITER_QMR_CS || sp->method > ADDA_ITER_BCGS2 ||
 		(sp->precision != ADDA_PREC_FP64 && sp->precision != ADDA_PREC_MIXED &&
 			sp->precision != ADDA_PREC_MIXED_F32VEC && sp->precision != ADDA_PREC_MIXED_F64VEC) || !(sp->eps > 0) || sp->maxiter < 0 ||
-		(sp->init_field != ADDA_IF_AUTO && sp->init_field != ADDA_IF_ZERO && sp->init_field != ADDA_IF_INC &&
-			sp->init_field != ADDA_IF_X0)) {
+			(sp->init_field != ADDA_IF_AUTO && sp->init_field != ADDA_IF_ZERO && sp->init_field != ADDA_IF_INC &&
+			sp->init_field != ADDA_IF_X0 && sp->init_field != ADDA_IF_CHPOINT) || !(sp->chp_time >= 0)) {
 		set_error("solve: unsupported parameters");
 		return ADDA_GB300_EINVAL;
 	}
 	return ADDA_GB300_OK;
+}
+
+// ---------------- iteration checkpoints: the reference's chp.<ringid> format (iterative.c:165-278) ----------------
+
+// index of each ADDA_ITER_* method in the reference's params table (iterative.c:118-125, alphabetical) and the
+// number of its own vectors
+constexpr int kChpInd[7] = {5, 2, 1, 3, 4, 6, 0};
+constexpr int kChpVec[7] = {3, 3, 0, 0, 2, 2, 1};
+constexpr size_t kChpHead = sizeof(int) + sizeof(size_t) + 2 * sizeof(int) + 3 * sizeof(double);
+
+struct ChpScalar {
+	void *p;
+	size_t size;
+};
+
+// the method's scalars in the order of its PHASE_VARS (iterative.c:383-386,520-521,661-664,741-742,796-803,
+// 919-928,1060-1066); the reference's doublecomplex is a double2
+static int chp_scalars(RhsState &S, int method, ChpScalar out[8])
+{
+	int n = 0;
+	auto D = [&](double &v) { out[n++] = {&v, sizeof(double)}; };
+	auto Z = [&](double2 &v) { out[n++] = {&v, sizeof(double2)}; };
+	switch (method) {
+		case ADDA_ITER_QMR_CS:
+			D(S.om_old); D(S.om_new); D(S.c_old); D(S.c_new); Z(S.beta); Z(S.tautilda); Z(S.s_old); Z(S.s_new);
+			break;
+		case ADDA_ITER_BICGSTAB: Z(S.ro_old); Z(S.omega); Z(S.balpha); break;
+		case ADDA_ITER_BICG_CS: Z(S.ro_old); break;
+		case ADDA_ITER_CGNR: D(S.ro_old.x); break;
+		case ADDA_ITER_CSYM: D(S.cs_beta); D(S.c_old); D(S.c_new); Z(S.tautilda); Z(S.s_old); Z(S.s_new); break;
+		case ADDA_ITER_QMR_CS_2: D(S.q2_c); D(S.q2_theta); D(S.q2_ro); Z(S.q2_eps); Z(S.q2_eta); break;
+		default: Z(S.b2_rho0); Z(S.b2_alpha); break;
+	}
+	return n;
+}
+
+// kv[] buffer of each file vector (xvec, rvec, pvec, then the method's own) for the state before iteration niter.
+// The reference stores buffers, not roles: QMR_CS and CSYM swap their pointers every iteration and sort them out on
+// load by the parity of niter (odd; iterative.c:809-812,935-938). P is the parity of this solver's own buffer roles
+// (iterations run since it0); half: BiCGStab stopped at its half step, where the residual is s.
+static int chp_buffers(int method, int P, int odd, int half, int idx[6])
+{
+	enum { X = 0, RV = 1, PV = 2, V1 = 4, V2 = 5, V3 = 6 };
+	idx[0] = X;
+	idx[1] = RV;
+	idx[2] = PV;
+	switch (method) {
+		case ADDA_ITER_QMR_CS: { // v = vec1, v~ = vec2, p_new = vec3, p_old = pvec for odd niter
+			const int v = P ? V2 : V1, vt = P ? V1 : V2, pn = P ? V3 : PV, po = P ? PV : V3;
+			idx[2] = odd ? po : pn;
+			idx[3] = odd ? v : vt;
+			idx[4] = odd ? vt : v;
+			idx[5] = odd ? pn : po;
+			return 6;
+		}
+		case ADDA_ITER_BICGSTAB: // v, s, r~
+			if (half) idx[1] = V2;
+			idx[3] = V1;
+			idx[4] = V2;
+			idx[5] = V3;
+			return 6;
+		case ADDA_ITER_CSYM: { // q_new = rvec, q_old = vec1, p_new = vec2, p_old = pvec for odd niter
+			const int qn = P ? V1 : RV, qo = P ? RV : V1, pn = P ? V2 : PV, po = P ? PV : V2;
+			idx[1] = odd ? qn : qo;
+			idx[2] = odd ? po : pn;
+			idx[3] = odd ? qo : qn;
+			idx[4] = odd ? pn : po;
+			return 5;
+		}
+		case ADDA_ITER_QMR_CS_2: // v, d
+			idx[3] = V1;
+			idx[4] = V2;
+			return 5;
+		case ADDA_ITER_BCGS2: // u_0 (r~_0 is pvec)
+			idx[3] = V2;
+			return 4;
+		default: return 3; // BiCG_CS, CGNR: p is pvec
+	}
+}
+
+static size_t chp_size(int method, size_t n3)
+{
+	RhsState S;
+	ChpScalar sc[8];
+	const int ns = chp_scalars(S, method, sc);
+	size_t b = kChpHead;
+	for (int i = 0; i < ns; i++) b += sc[i].size;
+	return b + (3 + kChpVec[method]) * sizeof(double2) * n3;
 }
 
 // the solve on device-resident data: d_einc [R][3N] FP64; leaves x in w->x64 and p = S.x in c->pvec64
@@ -1918,6 +2037,27 @@ static int solve_core_impl(adda_gb300_ctx *c, const adda_gb300_solve_params *sp,
 	const size_t n3 = w->n3;
 	cudaStream_t s = c->stream;
 	const dim3 gv(w->nbv, R);
+	const auto t0 = std::chrono::steady_clock::now();
+	const bool resume = sp->init_field == ADDA_IF_CHPOINT;
+	w->chp_valid = 0;
+	if (resume) {
+		if (sp->precision != ADDA_PREC_FP64) {
+			set_error("solve: resuming from a checkpoint needs ADDA_PREC_FP64");
+			return ADDA_GB300_EINVAL;
+		}
+		for (int r = 0; r < R; r++) {
+			if ((int)w->chp_pend.size() <= r || w->chp_pend[r].empty()) {
+				set_error("solve: no checkpoint loaded for right-hand side " + std::to_string(r));
+				return ADDA_GB300_ESTATE;
+			}
+			int ind;
+			std::memcpy(&ind, w->chp_pend[r].data(), sizeof(int));
+			if (ind != kChpInd[sp->method] || w->chp_pend[r].size() != chp_size(sp->method, n3)) {
+				set_error("solve: the checkpoint is for different iterative method"); // iterative.c:239
+				return ADDA_GB300_EINVAL;
+			}
+		}
+	}
 	// stagnation limits per method (iterative.c:118-125)
 	const int mc = (sp->method == ADDA_ITER_BICGSTAB) ? 30000
 		: (sp->method == ADDA_ITER_CGNR || sp->method == ADDA_ITER_CSYM) ? 10
@@ -1936,9 +2076,65 @@ static int solve_core_impl(adda_gb300_ctx *c, const adda_gb300_solve_params *sp,
 		typedef double2 C;
 		KV<C> k = kvec<C>(w);
 		const int zero = sp->init_field == ADDA_IF_ZERO;
-		s_init<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv, sp->eps, sp->maxiter, mc, w->hist, w->hist_cap, zero);
-		ADDA_LAUNCHED();
-		if (zero) {
+		if (!resume) {
+			s_init<<<R, NT, 0, s>>>(w->st, w->done, w->vpart, w->nbv, sp->eps, sp->maxiter, mc, w->hist, w->hist_cap,
+				zero);
+			ADDA_LAUNCHED();
+		}
+		if (resume) { // LoadIterChpoint (iterative.c:222-278) in place of CalcInitField and PHASE_INIT
+			std::vector<int> dn(R);
+			std::vector<double> h0(R);
+			for (int r = 0; r < R; r++) {
+				const unsigned char *q = w->chp_pend[r].data() + sizeof(int) + sizeof(size_t);
+				RhsState &S = hs[r];
+				std::memset(&S, 0, sizeof(S));
+				std::memcpy(&S.niter, q, sizeof(int));
+				std::memcpy(&S.counter, q + 4, sizeof(int));
+				std::memcpy(&S.inprodR, q + 8, sizeof(double));
+				std::memcpy(&S.prev_err, q + 16, sizeof(double));
+				std::memcpy(&S.resid_scale, q + 24, sizeof(double));
+				q += 32;
+				ChpScalar sc[8];
+				const int ns = chp_scalars(S, sp->method, sc);
+				for (int i = 0; i < ns; i++) {
+					std::memcpy(sc[i].p, q, sc[i].size);
+					q += sc[i].size;
+				}
+				S.epsB = sp->eps * sp->eps / S.resid_scale; // iterative.c:270
+				S.temp = 1 / S.resid_scale;
+				S.inprodRp1 = S.prev_err * S.prev_err / S.resid_scale;
+				S.maxiter = sp->maxiter;
+				S.mc = mc;
+				S.it0 = S.niter;
+				S.full = sp->full_steps != 0;
+				S.done = !(S.inprodR > S.epsB && S.niter <= S.maxiter && S.counter <= S.mc);
+				dn[r] = S.done;
+				h0[r] = S.prev_err;
+				int idx[6];
+				const int nv = chp_buffers(sp->method, 0, S.niter & 1, 0, idx);
+				for (int v = 0; v < nv; v++, q += sizeof(double2) * n3)
+					ADDA_CUDA(cudaMemcpyAsync(w->kv[idx[v]] + (size_t)r * n3, q, sizeof(double2) * n3,
+						cudaMemcpyHostToDevice, s));
+				if (S.niter - 1 < w->hist_cap)
+					ADDA_CUDA(cudaMemcpyAsync(w->hist + (size_t)r * w->hist_cap + S.niter - 1, &h0[r], sizeof(double),
+						cudaMemcpyHostToDevice, s));
+			}
+			ADDA_CUDA(cudaMemcpyAsync(w->st, hs.data(), sizeof(RhsState) * R, cudaMemcpyHostToDevice, s));
+			ADDA_CUDA(cudaMemcpyAsync(w->done, dn.data(), sizeof(int) * R, cudaMemcpyHostToDevice, s));
+			ADDA_CUDA(cudaStreamSynchronize(s));
+			for (int r = 0; r < R; r++) w->chp_pend[r].clear(); // a checkpoint is loaded once
+			// dot products the first resumed iteration takes from the previous one's fused update
+			if (sp->method == ADDA_ITER_BICGSTAB) k_dot<C><<<gv, NT, 0, s>>>(k.r, k.v3, n3, 1, w->vpart, w->nbv);
+			else if (sp->method == ADDA_ITER_BICG_CS) k_dot<C><<<gv, NT, 0, s>>>(k.r, k.r, n3, 0, w->vpart, w->nbv);
+			else if (sp->method == ADDA_ITER_BCGS2) k_dot<C><<<gv, NT, 0, s>>>(k.r, k.p, n3, 1, w->vpart, w->nbv);
+			else if (sp->method == ADDA_ITER_QMR_CS_2) {
+				k_dot<C><<<gv, NT, 0, s>>>(k.v1, k.v1, n3, 0, w->vpart, w->nbv);
+				ADDA_LAUNCHED();
+				q2_resume_s<<<R, NT, 0, s>>>(w->st, w->vpart, w->nbv);
+			}
+			ADDA_LAUNCHED();
+		}
+		else if (zero) {
 			k_copy<C><<<gv, NT, 0, s>>>(k.r, w->b64, n3, nullptr);
 			ADDA_LAUNCHED();
 		}
@@ -1967,19 +2163,33 @@ static int solve_core_impl(adda_gb300_ctx *c, const adda_gb300_solve_params *sp,
 			ADDA_LAUNCHED();
 		}
 		unsigned long long iters = 0;
-		if ((rc = krylov<double, double2>(c, w, sp->method, R, K, &iters))) return rc;
+		bool stopped = false;
+		if (!resume && sp->full_steps) { // BiCGStab without the half-step exit (-chp_type always)
+			std::vector<RhsState> h(R);
+			ADDA_CUDA(cudaMemcpyAsync(h.data(), w->st, sizeof(RhsState) * R, cudaMemcpyDeviceToHost, s));
+			ADDA_CUDA(cudaStreamSynchronize(s));
+			for (auto &x : h) x.full = 1;
+			ADDA_CUDA(cudaMemcpyAsync(w->st, h.data(), sizeof(RhsState) * R, cudaMemcpyHostToDevice, s));
+			ADDA_CUDA(cudaStreamSynchronize(s));
+		}
+		if ((rc = krylov<double, double2>(c, w, sp->method, R, K, &iters, resume, sp->chp_time, t0, &stopped)))
+			return rc;
 		ADDA_CUDA(cudaMemcpyAsync(hs.data(), w->st, sizeof(RhsState) * R, cudaMemcpyDeviceToHost, s));
 		ADDA_CUDA(cudaStreamSynchronize(s));
 		ADDA_CUDA(cudaMemcpyAsync(w->x64, k.x, sizeof(double2) * R * n3, cudaMemcpyDeviceToDevice, s));
 		for (int r = 0; r < R; r++) {
 			st[r].niter = hs[r].niter - 1;
 			st[r].status = hs[r].status;
-			if (!st[r].status && hs[r].inprodR > hs[r].epsB)
+			if (!st[r].status && stopped && !hs[r].done) st[r].status = ADDA_GB300_CHPOINT;
+			else if (!st[r].status && hs[r].inprodR > hs[r].epsB)
 				st[r].status = (hs[r].niter > hs[r].maxiter) ? ADDA_GB300_EMAXITER : ADDA_GB300_ESTAGNATION;
 			st[r].resid = sqrt(hs[r].resid_scale * hs[r].inprodR);
 			const int mpi = matvecs_per_iter(sp->method);
-			st[r].matvecs_fp64 = (zero ? 0 : 1) + mpi * st[r].niter;
+			st[r].matvecs_fp64 = (zero || resume ? 0 : 1) + mpi * (hs[r].niter - hs[r].it0);
 		}
+		w->chp_valid = 1;
+		w->chp_method = sp->method;
+		w->chp_R = R;
 	}
 	else if (sp->precision == ADDA_PREC_MIXED) {
 		if ((rc = solve_mixed<dd2>(c, sp, R, st.data(), mc, K))) return rc;
@@ -1996,6 +2206,95 @@ static int solve_core_impl(adda_gb300_ctx *c, const adda_gb300_solve_params *sp,
 	c->last_nrhs = R;
 	if (stats)
 		for (int r = 0; r < R; r++) stats[r] = st[r];
+	return ADDA_GB300_OK;
+}
+
+size_t solver_chpoint_size(const adda_gb300_ctx *c, int method)
+{
+	if (method < ADDA_ITER_QMR_CS || method > ADDA_ITER_BCGS2) return 0;
+	return chp_size(method, 3 * c->N);
+}
+
+// SaveIterChpoint (iterative.c:165-218) for one right-hand side of the last FP64 solve
+int solver_chpoint_save(adda_gb300_ctx *c, int rhs, void *buf, size_t size)
+{
+	SolverWork *w = c->sw;
+	if (!w || !w->chp_valid || rhs < 0 || rhs >= w->chp_R) {
+		set_error("chpoint_save: no FP64 solver state for that right-hand side");
+		return ADDA_GB300_ESTATE;
+	}
+	const int m = w->chp_method;
+	const size_t n3 = w->n3, need = chp_size(m, n3);
+	if (!buf || size < need) {
+		set_error("chpoint_save: buffer smaller than adda_gb300_chpoint_size");
+		return ADDA_GB300_EINVAL;
+	}
+	cudaStream_t s = c->stream;
+	RhsState S;
+	ADDA_CUDA(cudaMemcpyAsync(&S, w->st + rhs, sizeof(S), cudaMemcpyDeviceToHost, s));
+	ADDA_CUDA(cudaStreamSynchronize(s));
+	if (S.status == ADDA_GB300_EBREAKDOWN) {
+		set_error("chpoint_save: the solve of that right-hand side broke down");
+		return ADDA_GB300_ESTATE;
+	}
+	unsigned char *o = (unsigned char *)buf;
+	const int ind = kChpInd[m];
+	const size_t rows = n3;
+	auto put = [&](const void *p, size_t n) {
+		std::memcpy(o, p, n);
+		o += n;
+	};
+	put(&ind, sizeof(int));
+	put(&rows, sizeof(size_t));
+	put(&S.niter, sizeof(int));
+	put(&S.counter, sizeof(int));
+	put(&S.inprodR, sizeof(double));
+	put(&S.prev_err, sizeof(double));
+	put(&S.resid_scale, sizeof(double));
+	ChpScalar sc[8];
+	const int ns = chp_scalars(S, m, sc);
+	for (int i = 0; i < ns; i++) put(sc[i].p, sc[i].size);
+	int idx[6];
+	const int nv = chp_buffers(m, (S.niter - S.it0) & 1, S.niter & 1, m == ADDA_ITER_BICGSTAB && S.half, idx);
+	for (int v = 0; v < nv; v++, o += sizeof(double2) * n3)
+		ADDA_CUDA(cudaMemcpyAsync(o, w->kv[idx[v]] + (size_t)rhs * n3, sizeof(double2) * n3, cudaMemcpyDeviceToHost, s));
+	ADDA_CUDA(cudaStreamSynchronize(s));
+	return ADDA_GB300_OK;
+}
+
+// LoadIterChpoint's checks (iterative.c:238-266); the state is applied by the next solve with ADDA_IF_CHPOINT
+int solver_chpoint_load(adda_gb300_ctx *c, int rhs, const void *buf, size_t size)
+{
+	if (rhs < 0 || rhs >= c->Rmax || !buf || size < kChpHead) {
+		set_error("chpoint_load: invalid arguments");
+		return ADDA_GB300_EINVAL;
+	}
+	int rc = ensure_work(c, 1, 1);
+	if (rc) return rc;
+	SolverWork *w = c->sw;
+	int ind;
+	size_t rows;
+	std::memcpy(&ind, buf, sizeof(int));
+	std::memcpy(&rows, (const unsigned char *)buf + sizeof(int), sizeof(size_t));
+	int m = -1;
+	for (int i = 0; i < 7; i++)
+		if (kChpInd[i] == ind) m = i;
+	if (m < 0) {
+		set_error("chpoint_load: unknown iterative method index in the checkpoint");
+		return ADDA_GB300_EINVAL;
+	}
+	if (rows != w->n3) {
+		set_error("chpoint_load: the checkpoint is for different vector size");
+		return ADDA_GB300_EINVAL;
+	}
+	const size_t need = chp_size(m, w->n3);
+	if (size != need) {
+		set_error(size < need ? "chpoint_load: failed reading the checkpoint (too short)"
+		                      : "chpoint_load: the checkpoint is too long");
+		return ADDA_GB300_EINVAL;
+	}
+	if ((int)w->chp_pend.size() < c->Rmax) w->chp_pend.resize(c->Rmax);
+	w->chp_pend[rhs].assign((const unsigned char *)buf, (const unsigned char *)buf + size);
 	return ADDA_GB300_OK;
 }
 
@@ -2104,7 +2403,9 @@ int vjp_chi(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int rhs, const
 	ADDA_LAUNCHED();
 	adda_gb300_rhs_stats st[2];
 	adda_gb300_solve_params asp = *sp;
-	if (asp.init_field == ADDA_IF_X0) asp.init_field = ADDA_IF_AUTO; // no caller x_0 for the adjoint systems
+	// no caller x_0, no checkpoint and no time limit for the adjoint systems
+	if (asp.init_field == ADDA_IF_X0 || asp.init_field == ADDA_IF_CHPOINT) asp.init_field = ADDA_IF_AUTO;
+	asp.chp_time = 0;
 	rc = solve_core(c, &asp, 2, w->av64, st);
 	if (!rc) {
 		ADDA_CUDA(cudaMemcpyAsync(dF, dinv_alpha, sizeof(double2) * N, cudaMemcpyHostToDevice, s));

@@ -32,6 +32,9 @@ extern "C" {
 #define ADDA_GB300_EBREAKDOWN 1     /* Krylov breakdown (iterative.c:684,697,960) */
 #define ADDA_GB300_ESTAGNATION 2    /* residual stagnated > mc iterations (iterative.c:1509) */
 #define ADDA_GB300_EMAXITER 3       /* maxiter reached without convergence (iterative.c:1507, a warning there) */
+#define ADDA_GB300_CHPOINT 4        /* stopped at the checkpoint time (solve_params.chp_time, the reference's -chpoint;
+                                       ProgressReport, iterative.c:308-317): the state stays in the context for
+                                       adda_gb300_chpoint_save; the reference's CHP_EXIT */
 
 enum adda_gb300_shape { ADDA_SHAPE_SPHERE = 0, ADDA_SHAPE_ELLIPSOID = 1, ADDA_SHAPE_BOX = 2 };
 /* polarizability prescriptions of the reference's -pol (calculator.c:170-262; nloc and nloc_av need the Gaussian
@@ -79,7 +82,9 @@ enum adda_gb300_inter { ADDA_INT_POI = 0, ADDA_INT_FCD = 1, ADDA_INT_FCD_ST = 2 
  * the caller in xvec (host API) or d_xvec (device API) -- the reference's "read" and "wkb" modes, which turn an
  * electric field E into x_0 = E/(cc_sqrt*chi_inv) (InitFieldfromE, iterative.c:1325-1338; see
  * adda_gb300_wkb_field) */
-enum adda_gb300_init_field { ADDA_IF_AUTO = 0, ADDA_IF_ZERO = 1, ADDA_IF_INC = 2, ADDA_IF_X0 = 3 };
+enum adda_gb300_init_field { ADDA_IF_AUTO = 0, ADDA_IF_ZERO = 1, ADDA_IF_INC = 2, ADDA_IF_X0 = 3, ADDA_IF_CHPOINT = 4 };
+/* ADDA_IF_CHPOINT: every right-hand side resumes from the state given to adda_gb300_chpoint_load (the reference's
+ * -chp_load, LoadIterChpoint, iterative.c:222-278); FP64 only */
 
 typedef struct adda_gb300_ctx adda_gb300_ctx;
 
@@ -107,6 +112,11 @@ typedef struct {
 	int check_every;             /* iterations between host convergence checks (CUDA graph length); 0 = default */
 	double inner_eps;            /* MIXED: relative tolerance of each FP32 inner solve; 0 = default */
 	int max_refine;              /* MIXED: maximum outer refinement steps; 0 = default */
+	double chp_time;             /* FP64: > 0 stops the solve once this many seconds of wall time have passed (checked
+	                                every check_every iterations) with status ADDA_GB300_CHPOINT for the right-hand
+	                                sides still running (-chpoint <time>); 0 = none */
+	int full_steps;              /* BiCGStab: no exit at the half step (the reference with -chp_type always,
+	                                iterative.c:703), so that the final state is a complete iteration */
 } adda_gb300_solve_params;
 
 typedef struct {
@@ -189,6 +199,22 @@ int adda_gb300_matvec_device(adda_gb300_ctx *ctx, int prec, int nrhs, const void
  * resid_hist (may be NULL): [nrhs][hist_cap] relative residuals RE_000, RE_001, ... (iterative.c:69,301). */
 int adda_gb300_solve(adda_gb300_ctx *ctx, const adda_gb300_solve_params *sp, int nrhs, const double *einc,
 	double *xvec, double *pvec, adda_gb300_rhs_stats *stats, double *resid_hist, int hist_cap);
+
+/* Iteration checkpoints in the reference's chp.<ringid> byte format (SaveIterChpoint / LoadIterChpoint,
+ * src/iterative.c:165-278; native byte order, the reference's layout: int ind_m, size_t local_nRows, int niter, int
+ * counter, double inprodR, prev_err, resid_scale, the method's scalars, xvec, rvec, pvec, the method's vectors), so
+ * that a state saved by the reference resumes here and vice versa.
+ * adda_gb300_chpoint_size: bytes of a checkpoint of the given method for this lattice.
+ * adda_gb300_chpoint_save: the state of right-hand side rhs after the last FP64 solve (finished, or stopped with
+ * ADDA_GB300_CHPOINT) into buf (size >= adda_gb300_chpoint_size); ADDA_GB300_ESTATE when there is none (no FP64
+ * solve yet, a later MIXED solve or matvec-only use, or a breakdown).
+ * adda_gb300_chpoint_load: checks and keeps a checkpoint for right-hand side rhs until the next solve with
+ * init_field ADDA_IF_CHPOINT; ADDA_GB300_EINVAL for a file of another size or vector length (the reference's
+ * "different vector size" / "too long" / "Failed reading" errors, iterative.c:238-266). The method is checked by the
+ * solve ("different iterative method"). */
+size_t adda_gb300_chpoint_size(const adda_gb300_ctx *ctx, int method);
+int adda_gb300_chpoint_save(adda_gb300_ctx *ctx, int rhs, void *buf, size_t size);
+int adda_gb300_chpoint_load(adda_gb300_ctx *ctx, int rhs, const void *buf, size_t size);
 
 /* same as adda_gb300_solve with DEVICE buffers (double2 [nrhs][ndip][3]) for einc and the optional d_xvec/d_pvec:
  * nothing crosses PCIe/C2C except the per-RHS stats and the convergence flags polled between graph launches */

@@ -4,15 +4,18 @@
  * drives the drop-in exactly like Calculator/CalculateE do: ParSetup's fftFit, InitDmatrix, IterativeSolver,
  * MatVec, Free_FFT_Dmat. Inputs come from libadda_gb300's host-side setup.
  *
- * usage: mock_host <grid> <m_re> <m_im> <dpl> <qmr|bicgstab> <eps_exponent> <out.bin> [wkb | read <field.bin>]
+ * usage: mock_host <grid> <m_re> <m_im> <dpl> <method> <eps_exponent> <out.bin> [wkb | read <field.bin> |
+ *        chpoint <dir> <normal|regular|always> <seconds> [maxiter] | chp_load <dir>]
  * writes: ndip (int64), then pvec and a MatVec of Einc (complex doubles, 3*ndip each)
  * read: the field file holds 3*ndip complex doubles (the mock's ReadField; the reference's reads io.c's text format)
  */
 #include "adda_gb300.h"
 #include "adda_dropin.h"
 
+#include <errno.h>
 #include <math.h>
 #include <stdarg.h>
+#include <sys/stat.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -21,6 +24,7 @@ enum enwho { ALL, ONE };
 enum ec { EC_OK, EC_ERROR, EC_WARN, EC_INFO };
 enum inter { G_FCD, G_FCD_ST, G_IGT, G_IGT_SO, G_NLOC, G_NLOC_AV, G_POINT_DIP, G_SO };
 enum init_field { IF_AUTO, IF_ZERO, IF_INC, IF_READ, IF_WKB };
+enum chpoint { CHP_NONE, CHP_NORMAL, CHP_REGULAR, CHP_ALWAYS };
 
 int boxX, boxY, boxZ, nprocs = 1, Nmat = 1, maxiter = 100000;
 size_t gridX, gridY, gridZ, gridYZ, local_Nsmall, local_nvoid_Ndip, local_nRows;
@@ -37,6 +41,20 @@ enum init_field InitField = IF_AUTO;
 doublecomplex ref_index[15], chi_inv[15][3];
 double prop[3];
 const char *infi_fnameY, *infi_fnameX;
+enum chpoint chp_type = CHP_NONE;
+time_t chp_time = -1, last_chp_wt;
+const char *chp_dir = "chpoint", *directory = "run000";
+bool load_chpoint = false;
+int ringid = 0;
+
+void MkDirErr(const char *dir, enum enwho who, const char *srcfile, int srcline)
+{
+	(void)who; (void)srcfile; (void)srcline;
+	if (mkdir(dir, 0755) == -1 && errno != EEXIST) {
+		fprintf(stderr, "ERROR: Failed to make directory '%s'\n", dir);
+		exit(1);
+	}
+}
 
 void ReadField(const char *fname, doublecomplex *field)
 {
@@ -127,12 +145,24 @@ int main(int argc, char **argv)
 		InitField = IF_READ;
 		infi_fnameY = infi_fnameX = argv[9];
 	}
+	if (argc > 11 && !strcmp(argv[8], "chpoint")) { /* -chpoint <time> -chp_type <type> -chp_dir <dir> */
+		chp_dir = argv[9];
+		chp_type = !strcmp(argv[10], "normal") ? CHP_NORMAL : !strcmp(argv[10], "regular") ? CHP_REGULAR : CHP_ALWAYS;
+		chp_time = atoi(argv[11]) > 0 ? atoi(argv[11]) : -1;
+		if (argc > 12) maxiter = atoi(argv[12]);
+	}
+	if (argc > 9 && !strcmp(argv[8], "chp_load")) {
+		chp_dir = argv[9];
+		load_chpoint = true;
+	}
+	time(&last_chp_wt);
 	Einc = malloc(sizeof(doublecomplex) * local_nRows);
 	xvec = malloc(sizeof(doublecomplex) * local_nRows);
 	pvec = malloc(sizeof(doublecomplex) * local_nRows);
 	adda_gb300_plane_wave(local_nvoid_Ndip, position, boxX, boxY, boxZ, gridspace, WaveNum, prop, py, (double *)Einc);
 	InitDmatrix();
 	int niter = IterativeSolver(method, INCPOL_Y);
+	if (niter == -2) printf("mock host: exit after checkpoint\n"); /* CHP_EXIT: Calculator returns (calculator.c:312) */
 	doublecomplex *y = malloc(sizeof(doublecomplex) * local_nRows);
 	clock_t t = 0;
 	ipr_required = true;
