@@ -15,7 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libadda_gb300.so")
 
 SHAPES = {"sphere": 0, "ellipsoid": 1, "box": 2}
-POLS = {"ldr": 0, "cm": 1, "rrc": 2, "dgf": 3, "cldr": 4, "fcd": 5, "igt_so": 6, "lak": 7, "so": 8}
+POLS = {"ldr": 0, "cm": 1, "rrc": 2, "dgf": 3, "cldr": 4, "fcd": 5, "igt_so": 6, "lak": 7, "so": 8, "nloc": 9,
+        "nloc_av": 10}
 ITERS = {"qmr": 0, "bicgstab": 1, "bicg": 2, "cgnr": 3, "csym": 4, "qmr2": 5, "bcgs2": 6}
 PREC = {"fp64": 0, "fp32": 1, "mixed": 2, "mixed_f32vec": 3, "mixed_f64vec": 4}
 INIT = {"auto": 0, "zero": 1, "inc": 2, "x0": 3, "chpoint": 4}
@@ -31,10 +32,10 @@ class Problem(ctypes.Structure):
                 ("gridX", ctypes.c_int), ("gridY", ctypes.c_int), ("gridZ", ctypes.c_int),
                 ("ndip", ctypes.c_size_t), ("position", ctypes.c_void_p), ("material", ctypes.c_void_p),
                 ("gridspace", ctypes.c_double), ("wavenum", ctypes.c_double), ("nrhs_max", ctypes.c_int),
-                ("device", ctypes.c_int), ("interaction", ctypes.c_int)]
+                ("device", ctypes.c_int), ("interaction", ctypes.c_int), ("nloc_rp", ctypes.c_double)]
 
 
-INTERACTIONS = {"poi": 0, "fcd": 1, "fcd_st": 2}
+INTERACTIONS = {"poi": 0, "fcd": 1, "fcd_st": 2, "nloc": 3, "nloc_av": 4}
 
 
 class SolveParams(ctypes.Structure):
@@ -51,7 +52,7 @@ class RhsStats(ctypes.Structure):
 
 EXPORTS = ["adda_gb300_fft_fit", "adda_gb300_fit_box", "adda_gb300_make_particle", "adda_gb300_rotation",
            "adda_gb300_plane_wave", "adda_gb300_wkb_field", "adda_gb300_polarizability",
-           "adda_gb300_polarizability_dchi",
+           "adda_gb300_polarizability_dchi", "adda_gb300_polarizability_nloc",
            "adda_gb300_create", "adda_gb300_destroy",
            "adda_gb300_get_grid", "adda_gb300_init_dmatrix", "adda_gb300_dmatrix_len", "adda_gb300_get_dmatrix",
            "adda_gb300_set_cc", "adda_gb300_set_cc_sqrt", "adda_gb300_set_cc_dipole", "adda_gb300_matvec", "adda_gb300_matvec_device",
@@ -88,6 +89,7 @@ def lib():
             "adda_gb300_wkb_field": ([I, I, I, SZ, P, P, I, P, D, P, P], I),
             "adda_gb300_polarizability": ([I, D, D, D, D, P, P, I, P], I),
             "adda_gb300_polarizability_dchi": ([I, D, D, D, D, P, P, I, P], I),
+            "adda_gb300_polarizability_nloc": ([I, D, D, D, D, P], I),
             "adda_gb300_vjp_chi": ([P, P, I, P, P, P, P, P], I),
             "adda_gb300_create": ([P, P], I),
             "adda_gb300_destroy": ([P], I),
@@ -172,8 +174,13 @@ def plane_wave(box, pos, gridspace, wavenum, prop, pol):
     return e
 
 
-def polarizability(m, kd, gridspace, prop, incpol, relation="ldr", avgpol=False):
+def polarizability(m, kd, gridspace, prop, incpol, relation="ldr", avgpol=False, rp=0.0):
+    """CoupleConstant: the three diagonal components; rp is the Gaussian width of -pol nloc|nloc_av <Rp>"""
     cc = np.zeros(3, np.complex128)
+    if relation in ("nloc", "nloc_av"):
+        _check(lib().adda_gb300_polarizability_nloc(POLS[relation], complex(m).real, complex(m).imag, gridspace, rp,
+                                                    _p(cc)), "polarizability_nloc")
+        return cc
     _check(lib().adda_gb300_polarizability(POLS[relation], complex(m).real, complex(m).imag, kd, gridspace,
                                            _p(np.ascontiguousarray(prop, float)),
                                            _p(np.ascontiguousarray(incpol, float)), int(avgpol), _p(cc)),
@@ -227,8 +234,9 @@ class Setup:
     Order of the RHS: Y polarisation first, then X (calculator.c:309-330)."""
 
     def __init__(self, grid=16, shape="sphere", pars=None, m=1.5, dpl=None, size=None, pol="ldr", orient=(0, 0, 0),
-                 avgpol=False, prop=None, lam=2 * math.pi, interaction="poi"):
+                 avgpol=False, prop=None, lam=2 * math.pi, interaction="poi", nloc_rp=0.0, pol_rp=0.0):
         self.interaction = interaction
+        self.nloc_rp = float(nloc_rp)
         self.box, self.pos, self.mat = make_particle(shape, grid, pars)
         self.n = len(self.pos)
         self.grid = (fft_fit(2 * self.box[0]), fft_fit(2 * self.box[1]), fft_fit(2 * self.box[2], 2))
@@ -243,7 +251,8 @@ class Setup:
         self.kd = 2 * math.pi / self.dpl
         self.prop, py, px = rotation(*orient, prop0=prop)
         self.incpol = [py, px]
-        self.cc = [polarizability(self.m, self.kd, self.gridspace, self.prop, e, pol, avgpol) for e in self.incpol]
+        self.cc = [polarizability(self.m, self.kd, self.gridspace, self.prop, e, pol, avgpol, pol_rp)
+                   for e in self.incpol]
         self.einc = [plane_wave(self.box, self.pos, self.gridspace, self.wavenum, self.prop, e) for e in self.incpol]
 
 
@@ -276,7 +285,8 @@ def solve_many(ctxs, eincs, method="qmr", prec="mixed", eps=1e-5, maxiter=100000
 class Context:
     """One particle lattice on one GPU: the interaction matrix, FP64/FP32 matvecs, solver and cross sections."""
 
-    def __init__(self, box, pos, mat, gridspace, wavenum, grid=(0, 0, 0), nrhs_max=2, device=0, interaction="poi"):
+    def __init__(self, box, pos, mat, gridspace, wavenum, grid=(0, 0, 0), nrhs_max=2, device=0, interaction="poi",
+                 nloc_rp=0.0):
         self.L = lib()
         self.pos = np.ascontiguousarray(pos, dtype=np.uint16).reshape(-1, 3)
         self.mat = None if mat is None else np.ascontiguousarray(mat, dtype=np.uint8)
@@ -284,7 +294,7 @@ class Context:
         self.nrhs_max = nrhs_max
         pr = Problem(box[0], box[1], box[2], grid[0], grid[1], grid[2], self.n, _p(self.pos).value,
                      None if self.mat is None else _p(self.mat).value, gridspace, wavenum, nrhs_max, device,
-                     INTERACTIONS[interaction])
+                     INTERACTIONS[interaction], nloc_rp)
         self.h = ctypes.c_void_p()
         _check(self.L.adda_gb300_create(ctypes.byref(pr), ctypes.byref(self.h)), "create")
         g = (ctypes.c_int * 3)()
@@ -293,7 +303,8 @@ class Context:
 
     @classmethod
     def from_setup(cls, s, nrhs_max=2, device=0):
-        c = cls(s.box, s.pos, s.mat, s.gridspace, s.wavenum, s.grid, nrhs_max, device, s.interaction)
+        c = cls(s.box, s.pos, s.mat, s.gridspace, s.wavenum, s.grid, nrhs_max, device, s.interaction,
+                getattr(s, "nloc_rp", 0.0))
         c.init_dmatrix()
         for r in range(min(nrhs_max, len(s.cc))):
             c.set_cc(r, s.cc[r].reshape(1, 3))

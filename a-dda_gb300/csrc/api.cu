@@ -115,15 +115,17 @@ static int create_impl(const adda_gb300_problem *p, adda_gb300_ctx *c)
 	c->Rmax = p->nrhs_max > 0 ? p->nrhs_max : 1;
 	c->gridspace = p->gridspace;
 	c->k = p->wavenum;
-	if (p->interaction < ADDA_INT_POI || p->interaction > ADDA_INT_FCD_ST) {
-		set_error("create: unknown interaction term");
+	if (p->interaction < ADDA_INT_POI || p->interaction > ADDA_INT_NLOC_AV || !(p->nloc_rp >= 0)) {
+		set_error("create: unknown interaction term or negative Gaussian width");
 		return ADDA_GB300_EINVAL;
 	}
-	if (p->interaction != ADDA_INT_POI && !(p->wavenum * p->gridspace < 3.14159265358979323846)) {
+	if ((p->interaction == ADDA_INT_FCD || p->interaction == ADDA_INT_FCD_ST) &&
+		!(p->wavenum * p->gridspace < 3.14159265358979323846)) {
 		set_error("create: the FCD interaction needs kd < pi (at least 2 dipoles per wavelength)");
 		return ADDA_GB300_EINVAL;
 	}
 	c->interaction = p->interaction;
+	c->nloc_rp = p->nloc_rp;
 	const int g3[3] = {c->gX, c->gY, c->gZ};
 	FftPlan *pl[3] = {c->px, c->py, c->pz};
 	for (int d = 0; d < 3; d++) {

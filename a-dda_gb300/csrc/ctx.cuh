@@ -59,6 +59,7 @@ struct adda_gb300_ctx {
 	size_t N = 0;
 	int Rmax = 1;
 	int interaction = 0; // enum adda_gb300_inter
+	double nloc_rp = 0;  // Gaussian width of the non-local interaction
 	double gridspace = 0, k = 0;
 	// lattice (host and device)
 	std::vector<uint16_t> pos;

@@ -69,7 +69,32 @@ __device__ void cisi_d(double x, double &ci, double &si)
 	si = 1.57079632679489661923 + e1i;
 }
 
-__global__ void green_fill(double2 *G, int bX, int bY, int bZ, int gX, double gridspace, double k, int inter)
+// the scaled lower incomplete gamma function f = g(s, x)/x^s = exp(-x) sum_k Gamma(s) x^k / Gamma(s+k+1), by its
+// series (converges fast for x <= 1; the reference's gamma_scaled, interaction.c:603-621)
+__device__ double gamma_scaled(double s, double x, double expmx)
+{
+	double ap = s, del = 1 / s, sum = del;
+	for (int it = 0; it < 200; it++) {
+		ap += 1;
+		del *= x / ap;
+		sum += del;
+		if (fabs(del) <= fabs(sum) * 2.220446049250313e-16) break;
+	}
+	return sum * expmx;
+}
+
+// 2/(sqrt(2 pi) d Rp) times the integral of exp(-(x+t)^2/(2 Rp^2)) over t in [-d/2, d/2] (AverageGaussCube,
+// interaction.c:625-635), through erf or erfc so that no digits are lost
+__device__ double average_gauss_cube(double x, double d, double rp)
+{
+	x = fabs(x);
+	const double y = x / (1.4142135623730950488 * rp), z = d / (2 * 1.4142135623730950488 * rp);
+	const double dif = (x < 1) ? erf(y + z) - erf(y - z) : erfc(y - z) - erfc(y + z);
+	return dif / d;
+}
+
+__global__ void green_fill(double2 *G, int bX, int bY, int bZ, int gX, double gridspace, double k, int inter,
+	double rp)
 {
 	const size_t lines = (size_t)bZ * bY;
 	const size_t total = lines * gX;
@@ -110,7 +135,32 @@ __global__ void green_fill(double2 *G, int bX, int bY, int bZ, int gX, double gr
 				}
 				g[a] = make_double2(re * evr - im * evi, re * evi + im * evr);
 			}
-			if (inter) {
+			if (inter == ADDA_INT_NLOC || inter == ADDA_INT_NLOC_AV) {
+				// static non-local interaction of two Gaussian densities (InterTerm_nloc_both, interaction.c:637-703):
+				// G = t1 (3 qq - I) - t2 I with t1 = 4/(3 sqrt(pi) R^3) g(5/2, R^2/(2Rp^2)) and t2 = (4pi/3) h(R), h
+				// the Gaussian (or its cube average)
+				double t1, t2 = 0;
+				if (rp == 0) t1 = invr3; // no lattice offset lies inside the cube around 0
+				else {
+					const double invrp3 = 1 / (rp * rp * rp), sx = 0.70710678118654752440 * rr / rp, x = sx * sx;
+					const double expmx = exp(-x);
+					const double sqrt2_9pi = 0.26596152026762178529, sqrt_pi = 1.7724538509055160273;
+					if (x > 1) // g(5/2, x) by upward recursion from erf
+						t1 = 4 / (3 * sqrt_pi) * (0.75 * sqrt_pi * erf(sx) - sx * (1.5 + x) * expmx) * invr3;
+					else t1 = sqrt2_9pi * x * gamma_scaled(2.5, x, expmx) * invrp3;
+					if (inter == ADDA_INT_NLOC_AV)
+						t2 = 0.52359877559829887308 * average_gauss_cube(q0 * rr, gridspace, rp) *
+							average_gauss_cube(q1 * rr, gridspace, rp) * average_gauss_cube(q2 * rr, gridspace, rp);
+					else t2 = expmx * invrp3 * sqrt2_9pi;
+				}
+#pragma unroll
+				for (int a = 0; a < 6; a++) {
+					double re = 3 * t1 * qm[a];
+					if (a == 0 || a == 3 || a == 5) re -= t1 + t2;
+					g[a] = make_double2(re, 0);
+				}
+			}
+			else if (inter) {
 				// FCD corrections of the real part (InterTerm_fcd / _fcd_st, interaction.c:335-411): k_F = pi/d
 				const double kfr = 3.14159265358979323846 * rn;
 				double sf, cf;
@@ -260,7 +310,8 @@ int dmatrix_build(adda_gb300_ctx *c)
 	}
 	const double invN = 1.0 / (gX * ((double)gY * gZ));
 	do {
-		green_fill<<<grid_for(gsz), 256, 0, c->stream>>>(G, bX, bY, bZ, gX, c->gridspace, c->k, c->interaction);
+		green_fill<<<grid_for(gsz), 256, 0, c->stream>>>(G, bX, bY, bZ, gX, c->gridspace, c->k, c->interaction,
+			c->nloc_rp);
 		count_launch();
 		if (cudaGetLastError() != cudaSuccess) { rc = ADDA_GB300_ECUDA; break; }
 		// x transform of all 6*bZ*bY lines (contiguous, length gX)

@@ -39,6 +39,7 @@ extern size_t gridX, gridY, gridZ, gridYZ, local_Nsmall, local_nvoid_Ndip, local
 extern double gridspace, WaveNum, memory;
 extern bool prognosis, reduced_FFT, surface, orient_avg, ipr_required;
 extern enum inter IntRelation;
+extern const double nloc_Rp; /* param.c:132 */
 extern FILE *logfile;
 extern unsigned short *position;
 extern unsigned char *material;
@@ -103,7 +104,9 @@ void InitDmatrix(void)
 	if (IntRelation == G_POINT_DIP) inter = ADDA_INT_POI;
 	else if (IntRelation == G_FCD) inter = ADDA_INT_FCD;
 	else if (IntRelation == G_FCD_ST) inter = ADDA_INT_FCD_ST;
-	else ERR("The GPU build supports the interaction terms -int poi|fcd|fcd_st only");
+	else if (IntRelation == G_NLOC) inter = ADDA_INT_NLOC;
+	else if (IntRelation == G_NLOC_AV) inter = ADDA_INT_NLOC_AV;
+	else ERR("The GPU build supports the interaction terms -int poi|fcd|fcd_st|nloc|nloc_av only");
 	if (!reduced_FFT) ERR("The GPU build requires the reduced FFT (do not use -no_reduced_fft)");
 	local_Nsmall = (gridX / 2) * (gridYZ / 2); /* fft.c:975 with nprocs=1 */
 	if (logfile) fprintf(logfile, "The FFT grid is: %zux%zux%zu\n", gridX, gridY, gridZ);
@@ -124,6 +127,7 @@ void InitDmatrix(void)
 	p.nrhs_max = 1;
 	p.device = getenv("ADDA_GB300_DEVICE") ? atoi(getenv("ADDA_GB300_DEVICE")) : 0;
 	p.interaction = inter;
+	p.nloc_rp = nloc_Rp;
 	if (adda_gb300_create(&p, &g_ctx)) ERR("GPU initialisation failed: %s", adda_gb300_last_error());
 	if (adda_gb300_init_dmatrix(g_ctx)) ERR("GPU D-matrix initialisation failed: %s", adda_gb300_last_error());
 	g_ccs_valid = 0;

@@ -215,6 +215,53 @@ int adda_gb300_polarizability(int relation, double m_re, double m_im, double kd,
 	return ADDA_GB300_OK;
 }
 
+/* ellTheta(a) = a^3 (theta_3(0, exp(-pi a^2))^3 - 1) (calculator.c:137-166): the lattice sum of a normalised Gaussian
+ * over the cubic lattice minus its value at 0, scaled. theta_3(0, q) = 1 + 2 sum_k q^(k^2); for a >= 1 three terms
+ * reach double precision, for a < 1 the Jacobi identity theta_3(0, exp(-pi a^2)) = theta_3(0, exp(-pi/a^2))/a is
+ * used first */
+static double ell_theta(double a)
+{
+	const double a2 = a * a, a3 = a * a2;
+	if (a >= 1) {
+		const double q = exp(-M_PI * a2);
+		const double t = 2 * (q + pow(q, 4) + pow(q, 9)); /* theta_3 - 1 */
+		return a3 * t * (3 + t * (3 + t));                 /* a^3 ((1+t)^3 - 1) */
+	}
+	const double q = exp(-M_PI / a2);
+	const double th = 1 + 2 * (q + pow(q, 4) + pow(q, 9)); /* a theta_3(0, exp(-pi a^2)) */
+	return th * th * th - a3;
+}
+
+int adda_gb300_polarizability_nloc(int relation, double m_re, double m_im, double gridspace, double rp, double cc[6])
+{
+	if ((relation != ADDA_POL_NLOC && relation != ADDA_POL_NLOC_AV) || !(rp >= 0) || !(gridspace > 0))
+		return ADDA_GB300_EINVAL;
+	const double dipvol = gridspace * gridspace * gridspace;
+	const double complex m = m_re + I * m_im;
+	double complex r;
+	if (rp == 0) r = pol_cm(m, dipvol);
+	else if (relation == ADDA_POL_NLOC) r = pol_m(FOUR_PI_D / 3 * ell_theta(gridspace / (sqrt(2 * M_PI) * rp)), m, dipvol);
+	else {
+		/* 1 - erf(x)^3, through erfc for x >= 1 to keep the digits */
+		const double x = gridspace / (2 * M_SQRT2 * rp);
+		double g0;
+		if (x < 1) {
+			const double t = erf(x);
+			g0 = 1 - t * t * t;
+		}
+		else {
+			const double t = erfc(x);
+			g0 = t * (3 - 3 * t + t * t);
+		}
+		r = pol_m(FOUR_PI_D / 3 * g0, m, dipvol);
+	}
+	for (int a = 0; a < 3; a++) {
+		cc[2 * a] = creal(r);
+		cc[2 * a + 1] = cimag(r);
+	}
+	return ADDA_GB300_OK;
+}
+
 int adda_gb300_polarizability_dchi(int relation, double m_re, double m_im, double kd, double gridspace,
 	const double prop[3], const double incPol[3], int avgpol, double out[2])
 {

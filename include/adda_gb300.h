@@ -37,8 +37,8 @@ extern "C" {
                                        adda_gb300_chpoint_save; the reference's CHP_EXIT */
 
 enum adda_gb300_shape { ADDA_SHAPE_SPHERE = 0, ADDA_SHAPE_ELLIPSOID = 1, ADDA_SHAPE_BOX = 2 };
-/* polarizability prescriptions of the reference's -pol (calculator.c:170-262; nloc and nloc_av need the Gaussian
- * width of -pol nloc and are not provided) */
+/* polarizability prescriptions of the reference's -pol (calculator.c:170-262); nloc and nloc_av take the Gaussian
+ * width Rp of -pol nloc <Rp> and are computed by adda_gb300_polarizability_nloc */
 enum adda_gb300_pol {
 	ADDA_POL_LDR = 0,
 	ADDA_POL_CM = 1,
@@ -48,7 +48,9 @@ enum adda_gb300_pol {
 	ADDA_POL_FCD = 5,
 	ADDA_POL_IGT_SO = 6,
 	ADDA_POL_LAK = 7,
-	ADDA_POL_SO = 8
+	ADDA_POL_SO = 8,
+	ADDA_POL_NLOC = 9,
+	ADDA_POL_NLOC_AV = 10
 };
 /* Krylov methods of the reference's -iter: qmr, bicgstab, bicg (BiCG_CS / COCG), cgnr, csym, qmr2 (QMR_CS_2),
  * bcgs2 (BiCGstab(2)) */
@@ -75,9 +77,12 @@ enum adda_gb300_prec {
 	ADDA_PREC_MIXED_F32VEC = 3,
 	ADDA_PREC_MIXED_F64VEC = 4
 };
-/* interaction terms of the reference's -int (interaction.c:290-411): point dipoles, filtered coupled dipoles (FCD,
- * Gay-Balmaz & Martin / Piller) and its static limit; igt, igt_so, nloc and so are not provided */
-enum adda_gb300_inter { ADDA_INT_POI = 0, ADDA_INT_FCD = 1, ADDA_INT_FCD_ST = 2 };
+/* interaction terms of the reference's -int (interaction.c:290-411,589-707): point dipoles, filtered coupled dipoles
+ * (FCD, Gay-Balmaz & Martin / Piller) and its static limit, and the static non-local interaction of two Gaussian
+ * dipole densities of width Rp (problem.nloc_rp; nloc: point value of the non-locality function, nloc_av: its average
+ * over the dipole cube); igt, igt_so and so are not provided */
+enum adda_gb300_inter { ADDA_INT_POI = 0, ADDA_INT_FCD = 1, ADDA_INT_FCD_ST = 2, ADDA_INT_NLOC = 3,
+	ADDA_INT_NLOC_AV = 4 };
 /* -init_field: auto, zero, inc (CalcInitField, iterative.c:1342-1394), and X0: the starting vector x_0 is supplied by
  * the caller in xvec (host API) or d_xvec (device API) -- the reference's "read" and "wkb" modes, which turn an
  * electric field E into x_0 = E/(cc_sqrt*chi_inv) (InitFieldfromE, iterative.c:1325-1338; see
@@ -101,6 +106,7 @@ typedef struct {
 	int nrhs_max;                /* right-hand sides solved together (>=1) */
 	int device;                  /* CUDA device ordinal */
 	int interaction;             /* enum adda_gb300_inter (-int); 0 = point dipoles */
+	double nloc_rp;              /* Gaussian width Rp of -int nloc|nloc_av <Rp> (same length unit as gridspace) */
 } adda_gb300_problem;
 
 typedef struct {
@@ -154,6 +160,10 @@ int adda_gb300_wkb_field(int boxX, int boxY, int boxZ, size_t ndip, const uint16
  * (identical except for CLDR) */
 int adda_gb300_polarizability(int relation, double m_re, double m_im, double kd, double gridspace,
 	const double prop[3], const double incPol[3], int avgpol, double cc[6]);
+
+/* -pol nloc|nloc_av <Rp> (calculator.c:223-248, static): M = (4pi/3) ellTheta(d/(sqrt(2pi) Rp)) for nloc (lattice sum
+ * of the Gaussian's non-locality function) and (4pi/3)(1 - erf(d/(2 sqrt(2) Rp))^3) for nloc_av; Rp = 0 gives CM */
+int adda_gb300_polarizability_nloc(int relation, double m_re, double m_im, double gridspace, double rp, double cc[6]);
 
 /* d(1/alpha)/dchi for the same relations (chi = (m^2-1)/(4pi), the susceptibility), the input of adda_gb300_vjp_chi */
 int adda_gb300_polarizability_dchi(int relation, double m_re, double m_im, double kd, double gridspace,

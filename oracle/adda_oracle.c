@@ -24,7 +24,8 @@ struct or_ctx {
 	uint16_t *pos;       // [n][3] grid coordinates
 	uint8_t *mat;        // [n] material index
 	double gridspace, k;
-	int inter;           // 0 point dipoles, 1 FCD, 2 static FCD
+	int inter;           // 0 point dipoles, 1 FCD, 2 static FCD, 3 non-local, 4 non-local (cube-averaged)
+	double rp;           // Gaussian width of the non-local interaction
 	size_t DsY, DsZ;     // reduced D sizes (fft.c:955-963)
 	cplx *D;             // [gX][DsZ][DsY][6]
 	int per_dip, nmat;
@@ -144,6 +145,54 @@ void or_set_interaction(or_ctx *c, int relation)
 	c->inter = relation;
 }
 
+void or_set_nloc_rp(or_ctx *c, double rp)
+{
+	c->rp = rp;
+}
+
+/* Non-local interaction of two Gaussian dipole densities of width Rp, static (InterTerm_nloc_both,
+ * src/interaction.c:637-703): G = t1 (3 qq - I) - t2 I, t1 = 4/(3 sqrt(pi) R^3) g(5/2, x), x = R^2/(2 Rp^2), from
+ * erf by g(1/2,x) = sqrt(pi) erf(sqrt x), g(s+1,x) = s g(s,x) - exp(-x) x^s for x > 1 and from the series of
+ * g(5/2,x)/x^(5/2) below (gamma_scaled, :603-621); t2 = (4pi/3) h(R), the Gaussian exp(-x)/((2pi)^(3/2) Rp^3) or, for
+ * nloc_av, its average over the cube around the dipole (product of three erf differences, AverageGaussCube :625-635) */
+static double gauss_cube(const or_ctx *c, double x)
+{
+	x = fabs(x);
+	const double y = x / (M_SQRT2 * c->rp), z = c->gridspace / (2 * M_SQRT2 * c->rp);
+	return ((x < 1) ? erf(y + z) - erf(y - z) : erfc(y - z) - erfc(y + z)) / c->gridspace;
+}
+
+static void green_nloc(const or_ctx *c, int i, int j, int k, cplx g[6])
+{
+	const double rn = sqrt((double)i * i + (double)j * j + (double)k * k);
+	const double q[3] = {i / rn, j / rn, k / rn};
+	const double rr = rn * c->gridspace, invr3 = 1 / (rr * rr * rr);
+	double t1, t2 = 0;
+	if (c->rp == 0) t1 = invr3;
+	else {
+		const double x = rr * rr / (2 * c->rp * c->rp), sx = sqrt(x), e = exp(-x), irp3 = 1 / pow(c->rp, 3);
+		if (x > 1) {
+			const double g12 = sqrt(M_PI) * erf(sx);                    // g(1/2, x)
+			const double g32 = 0.5 * g12 - e * sx;                       // g(3/2, x)
+			const double g52 = 1.5 * g32 - e * x * sx;                   // g(5/2, x)
+			t1 = 4 / (3 * sqrt(M_PI)) * g52 * invr3;
+		}
+		else {
+			double term = 1 / 2.5, sum = term; // g(5/2,x)/x^(5/2) = exp(-x) sum_n x^n / ((5/2)(7/2)...(5/2+n))
+			for (int n = 1; n < 200 && term > sum * 1e-17; n++) {
+				term *= x / (2.5 + n);
+				sum += term;
+			}
+			t1 = 4 / (3 * sqrt(M_PI)) * e * sum * x * pow(2 * c->rp * c->rp, -1.5); // g52/R^3 = f x (2Rp^2)^(-3/2)
+		}
+		if (c->inter == 4)
+			t2 = M_PI / 6 * gauss_cube(c, q[0] * rr) * gauss_cube(c, q[1] * rr) * gauss_cube(c, q[2] * rr);
+		else t2 = e * irp3 * sqrt(2 / (9 * M_PI));
+	}
+	const double qm[6] = {q[0] * q[0], q[0] * q[1], q[0] * q[2], q[1] * q[1], q[1] * q[2], q[2] * q[2]};
+	for (int a = 0; a < 6; a++) g[a] = 3 * t1 * qm[a] - ((a == 0 || a == 3 || a == 5) ? t1 + t2 : 0);
+}
+
 /* FCD corrections of the point-dipole term, InterTerm_fcd / InterTerm_fcd_st, src/interaction.c:335-411
  * (Gay-Balmaz & Martin 2002, Piller 1998): with k_F = pi/d, kfr = pi*|q| */
 static void green_fcd(const or_ctx *c, int i, int j, int k, cplx g[6])
@@ -200,7 +249,8 @@ void or_init_dmatrix(or_ctx *c)
 			for (int i = 1 - bX; i < bX; i++) {
 				if (!i && !j && !k) continue;
 				cplx g[6];
-				if (c->inter) green_fcd(c, i, j, k, g);
+				if (c->inter >= 3) green_nloc(c, i, j, k, g);
+				else if (c->inter) green_fcd(c, i, j, k, g);
 				else green_poi(c, i, j, k, g);
 				size_t idx = ((size_t)k * bY + j) * gX + (i < 0 ? i + gX : i);
 				for (int a = 0; a < 6; a++) G[a * lines * gX + idx] = g[a];

@@ -35,6 +35,8 @@ void or_free(or_ctx *c);
 /* interaction term of D: 0 point dipoles (InterTerm_poi), 1 FCD (InterTerm_fcd), 2 static FCD (InterTerm_fcd_st),
  * src/interaction.c:315-411; set before or_init_dmatrix */
 void or_set_interaction(or_ctx *c, int relation);
+/* 3 = -int nloc, 4 = -int nloc_av (src/interaction.c:589-707): their Gaussian width Rp (gridspace units) */
+void or_set_nloc_rp(or_ctx *c, double rp);
 /* cosine and sine integrals Ci(x), Si(x) for x > 0 (the reference's cisi, sinint.c) */
 void or_cisi(double x, double *ci, double *si);
 void or_init_dmatrix(or_ctx *c);

@@ -31,6 +31,7 @@ size_t gridX, gridY, gridZ, gridYZ, local_Nsmall, local_nvoid_Ndip, local_nRows;
 double gridspace, WaveNum, memory;
 bool prognosis = false, reduced_FFT = true, surface = false, orient_avg = false, ipr_required = false;
 enum inter IntRelation = G_POINT_DIP;
+double nloc_Rp = 0;
 FILE *logfile;
 unsigned short *position;
 unsigned char *material;

@@ -101,6 +101,19 @@ CASES = [
     ("ell_wkb_eps8", ["-init_field", "wkb", "-eps", "8"] + ELL + MGN,
      dict(grid=8, m=1.1 + 0.1j, shape="ellipsoid", pars=(0.5, 1.5), init="wkb", eps=1e-8)),
     ("mgn_bcgs2", ["-iter", "bcgs2"] + MGN, dict(grid=8, m=1.1 + 0.1j, iter="bcgs2")),
+    # the static non-local interaction and polarizability (-int/-pol nloc|nloc_av <Rp>, Rp in um; d = 0.57 um here)
+    ("int_nloc", ["-int", "nloc", "0.3", "-pol", "nloc", "0.3"] + MGN,
+     dict(grid=8, m=1.1 + 0.1j, interaction="nloc", nloc_rp=0.3, pol="nloc", pol_rp=0.3)),
+    ("int_nloc_av", ["-int", "nloc_av", "0.5", "-pol", "nloc_av", "0.5"] + MGN,
+     dict(grid=8, m=1.1 + 0.1j, interaction="nloc_av", nloc_rp=0.5, pol="nloc_av", pol_rp=0.5)),
+    ("int_nloc_small", ["-int", "nloc", "0.1", "-pol", "nloc_av", "0.1"] + ELL + MGN,
+     dict(grid=8, m=1.1 + 0.1j, shape="ellipsoid", pars=(0.5, 1.5), interaction="nloc", nloc_rp=0.1, pol="nloc_av",
+          pol_rp=0.1)),
+    ("int_nloc0", ["-int", "nloc", "0", "-pol", "nloc", "0"] + MGN,
+     dict(grid=8, m=1.1 + 0.1j, interaction="nloc", nloc_rp=0.0, pol="nloc", pol_rp=0.0)),
+    ("c1_nloc_av", ["-grid", "16", "-dpl", "10", "-m", "1.5", "0", "-int", "nloc_av", "0.2", "-pol", "nloc", "0.2",
+                    "-eps", "8"],
+     dict(grid=16, m=1.5, dpl=10, interaction="nloc_av", nloc_rp=0.2, pol="nloc", pol_rp=0.2, eps=1e-8)),
     ("c1_bcgs2", ["-grid", "16", "-dpl", "10", "-m", "1.5", "0", "-iter", "bcgs2", "-eps", "5"],
      dict(grid=16, m=1.5, dpl=10, iter="bcgs2")),
     ("ell_bcgs2_eps8", ["-iter", "bcgs2", "-eps", "8"] + ELL + MGN,

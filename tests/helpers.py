@@ -7,7 +7,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden", "reference_runs.json")
 
-SETUP_KEYS = ("grid", "shape", "pars", "m", "dpl", "size", "pol", "orient", "avgpol", "prop", "interaction")
+SETUP_KEYS = ("grid", "shape", "pars", "m", "dpl", "size", "pol", "orient", "avgpol", "prop", "interaction", "nloc_rp",
+              "pol_rp")
 
 
 def golden():
@@ -38,7 +39,7 @@ def solver_opts(kw):
 def oracle_for(s, nthreads=0):
     from oracle import oracle as O
     o = O.Oracle(s.box, s.grid, s.pos, s.mat, s.gridspace, s.wavenum, nthreads,
-                 interaction=getattr(s, "interaction", "poi"))
+                 interaction=getattr(s, "interaction", "poi"), nloc_rp=getattr(s, "nloc_rp", 0.0))
     return o
 
 

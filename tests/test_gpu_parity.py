@@ -67,13 +67,17 @@ SETUPS = {
     "int_fcd": lambda: setup_for(case("int_fcd")["setup"]),
     "int_fcd_st": lambda: setup_for(case("int_fcd_st")["setup"]),
     "ell_fcd": lambda: setup_for(case("ell_fcd_eps8")["setup"]),
+    # static non-local interaction terms (erf / incomplete gamma) in D
+    "int_nloc": lambda: setup_for(case("int_nloc")["setup"]),
+    "int_nloc_av": lambda: setup_for(case("int_nloc_av")["setup"]),
+    "int_nloc_small": lambda: setup_for(case("int_nloc_small")["setup"]),
 }
 
 
 def context(s, R=2):
     import adda_gb300 as A
     c = A.Context(s.box, s.pos, s.mat, s.gridspace, s.wavenum, s.grid, nrhs_max=R,
-                  interaction=getattr(s, "interaction", "poi"))
+                  interaction=getattr(s, "interaction", "poi"), nloc_rp=getattr(s, "nloc_rp", 0.0))
     c.init_dmatrix()
     for r in range(R):
         c.set_cc(r, s.cc[r % 2].reshape(1, 3))
@@ -133,7 +137,8 @@ SOLVE_CASES = ["c1_qmr", "c1_bicgstab", "mgn", "mgn_eps10", "mgn_init_zero", "mg
                "sample_default", "c2_small", "mgn_bicg", "mgn_cgnr", "mgn_csym", "c1_bicg", "c1_cgnr", "c1_csym",
                "ell_bicg_eps8", "ell_csym_eps8", "mgn_qmr2", "c1_qmr2", "ell_qmr2_eps8",
                "mgn_bcgs2", "c1_bcgs2", "ell_bcgs2_eps8", "pol_cldr", "pol_fcd", "pol_igt_so", "pol_lak", "pol_so",
-               "int_fcd", "int_fcd_st", "c1_fcd", "ell_fcd_eps8", "mgn_wkb", "c1_wkb", "ell_wkb_eps8"]
+               "int_fcd", "int_fcd_st", "c1_fcd", "ell_fcd_eps8", "mgn_wkb", "c1_wkb", "ell_wkb_eps8",
+               "int_nloc", "int_nloc_av", "int_nloc_small", "int_nloc0", "c1_nloc_av"]
 
 
 @pytest.mark.parametrize("name", SOLVE_CASES)
