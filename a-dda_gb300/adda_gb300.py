@@ -45,6 +45,43 @@ class SolveParams(ctypes.Structure):
                 ("full_steps", ctypes.c_int)]
 
 
+class IntegrParms(ctypes.Structure):
+    """one angle's block of alldir_params.dat (degrees)"""
+    _fields_ = [("min", ctypes.c_double), ("max", ctypes.c_double), ("Jmin", ctypes.c_int), ("Jmax", ctypes.c_int),
+                ("eps", ctypes.c_double), ("equiv", ctypes.c_int), ("periodic", ctypes.c_int)]
+
+
+# the reference's alldir_params.dat defaults: theta, phi
+ALLDIR_DEFAULT = (dict(min=0.0, max=180.0, Jmin=2, Jmax=6, eps=0.0, equiv=False, periodic=False),
+                  dict(min=0.0, max=360.0, Jmin=2, Jmax=5, eps=0.0, equiv=True, periodic=True))
+
+
+def _parms(parms):
+    arr = (IntegrParms * 2)()
+    for i, p in enumerate(parms):
+        arr[i] = IntegrParms(p["min"], p["max"], p["Jmin"], p["Jmax"], p["eps"], int(p["equiv"]), int(p["periodic"]))
+    return arr
+
+
+def integr_points(p, in_cos):
+    """grid angles (degrees) of one alldir block: equal steps in cos for theta, in the angle for phi"""
+    arr = _parms([p, p])
+    n = lib().adda_gb300_integr_points(ctypes.byref(arr[0]), int(in_cos), None)
+    if n < 1:
+        raise AddaError("integr_points: inconsistent integration parameters")
+    out = np.zeros(n)
+    lib().adda_gb300_integr_points(ctypes.byref(arr[0]), int(in_cos), _p(out))
+    return out
+
+
+def romberg2d(parms, values):
+    """the reference's Romberg2D average of values [ntheta][nphi][dim] on the alldir grid"""
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    res = np.zeros(v.shape[2])
+    lib().adda_gb300_romberg2d(_parms(parms), v.shape[2], _p(v), _p(res))
+    return res
+
+
 class RhsStats(ctypes.Structure):
     _fields_ = [("niter", ctypes.c_int), ("status", ctypes.c_int), ("resid", ctypes.c_double),
                 ("refinements", ctypes.c_int), ("matvecs_fp64", ctypes.c_int), ("matvecs_fp32", ctypes.c_int)]
@@ -58,7 +95,8 @@ EXPORTS = ["adda_gb300_fft_fit", "adda_gb300_fit_box", "adda_gb300_make_particle
            "adda_gb300_set_cc", "adda_gb300_set_cc_sqrt", "adda_gb300_set_cc_dipole", "adda_gb300_matvec", "adda_gb300_matvec_device",
            "adda_gb300_solve", "adda_gb300_solve_device", "adda_gb300_solve_many", "adda_gb300_vjp_chi",
            "adda_gb300_chpoint_size", "adda_gb300_chpoint_save", "adda_gb300_chpoint_load",
-           "adda_gb300_cross_sections", "adda_gb300_scattered_fields",
+           "adda_gb300_cross_sections", "adda_gb300_scattered_fields", "adda_gb300_integr_points",
+           "adda_gb300_romberg2d", "adda_gb300_scattering_integrals",
            "adda_gb300_cross_sections_noalloc", "adda_gb300_time_matvec",
            "adda_gb300_last_solve_ms", "adda_gb300_last_error", "adda_gb300_kernel_launches"]
 
@@ -106,6 +144,9 @@ def lib():
             "adda_gb300_solve_device": ([P, P, I, P, P, P, P], I),
             "adda_gb300_solve_many": ([I, P, P, P, P, P, P, P], I),
             "adda_gb300_chpoint_size": ([P, I], SZ),
+            "adda_gb300_integr_points": ([P, I, P], I),
+            "adda_gb300_romberg2d": ([P, I, P, P], D),
+            "adda_gb300_scattering_integrals": ([P, I, P, P, P, P, P, P], I),
             "adda_gb300_chpoint_save": ([P, I, P, SZ], I),
             "adda_gb300_chpoint_load": ([P, I, P, SZ], I),
             "adda_gb300_time_matvec": ([P, I, I, I, SZ, P], I),
@@ -383,6 +424,16 @@ class Context:
                                               ctypes.c_void_p(d_p) if d_p else None, st), "solve_device")
         return [dict(niter=s.niter, status=STATUS.get(s.status, s.status), resid=s.resid, refinements=s.refinements,
                      matvecs_fp64=s.matvecs_fp64, matvecs_fp32=s.matvecs_fp32) for s in st]
+
+    def scattering_integrals(self, nrhs, prop, incpolx, incpoly, parms=ALLDIR_DEFAULT):
+        """Csca [nrhs] and Csca*g [nrhs,3] (beam frame) of the last solve's RHS 0..nrhs-1 sharing one incident frame,
+        from the GPU scattered field on the alldir grid and the reference's Romberg integration"""
+        csca = np.zeros(nrhs)
+        cg = np.zeros((nrhs, 3))
+        vec = [np.ascontiguousarray(v, dtype=np.float64) for v in (prop, incpolx, incpoly)]
+        _check(self.L.adda_gb300_scattering_integrals(self.h, nrhs, _parms(parms), *[_p(v) for v in vec], _p(csca),
+                                                      _p(cg)), "scattering_integrals")
+        return csca, cg
 
     def chpoint_size(self, method="qmr"):
         """bytes of an iteration checkpoint of that method (the reference's chp.<ringid> format)"""

@@ -18,7 +18,7 @@ LIB = os.path.join(OUT, "libadda_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 CU = ["api.cu", "matvec.cu", "matvec_f32.cu", "dmatrix.cu", "solver.cu", "noalloc.cu"]
-C = ["host_setup.c"]
+C = ["host_setup.c", "integrate.c"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -691,6 +691,64 @@ int adda_gb300_cross_sections(adda_gb300_ctx *c, int nrhs, const double *prop, c
 	return cross_sections(c, nrhs, prop, incpol, cext, cabs);
 }
 
+int adda_gb300_scattering_integrals(adda_gb300_ctx *c, int nrhs, const adda_gb300_integr_parms p[2],
+	const double prop[3], const double incpolx[3], const double incpoly[3], double *csca, double *csca_g)
+{
+	if (!c || !p || !prop || !incpolx || !incpoly || !csca || !csca_g || nrhs < 1 || nrhs > c->last_nrhs ||
+		!c->pvec64) {
+		set_error("scattering_integrals: invalid arguments or no solution available for that many RHS");
+		return ADDA_GB300_ESTATE;
+	}
+	const int nth = adda_gb300_integr_points(&p[0], 1, nullptr), nph = adda_gb300_integr_points(&p[1], 0, nullptr);
+	if (nth < 1 || nph < 1) {
+		set_error("scattering_integrals: inconsistent integration parameters");
+		return ADDA_GB300_EINVAL;
+	}
+	std::vector<double> th(nth), ph(nph), dirs((size_t)nth * nph * 3);
+	adda_gb300_integr_points(&p[0], 1, th.data());
+	adda_gb300_integr_points(&p[1], 0, ph.data());
+	const double d2r = 0.017453292519943295769236907684886;
+	for (int i = 0; i < nth; i++) {
+		const double t = d2r * th[i], ct = cos(t), st = sin(t);
+		for (int j = 0; j < nph; j++) {
+			const double f = d2r * ph[j], cf = cos(f), sf = sin(f);
+			double *d = &dirs[((size_t)i * nph + j) * 3];
+			for (int a = 0; a < 3; a++) d[a] = ct * prop[a] + st * (cf * incpolx[a] + sf * incpoly[a]);
+		}
+	}
+	const size_t nd = (size_t)nth * nph;
+	std::vector<double> e((size_t)nrhs * nd * 6);
+	ADDA_CUDA(cudaSetDevice(c->device));
+	int rc = scattered_fields(c, nrhs, (int)nd, dirs.data(), e.data());
+	if (rc) return rc;
+	std::vector<double> v(nd);
+	const double k2 = c->k * c->k, four_pi = 12.566370614359172953850573533118;
+	for (int r = 0; r < nrhs; r++) {
+		std::vector<double> e2(nd);
+		for (size_t q = 0; q < nd; q++) {
+			const double *x = &e[((size_t)r * nd + q) * 6];
+			e2[q] = x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + x[3] * x[3] + x[4] * x[4] + x[5] * x[5];
+		}
+		double res;
+		adda_gb300_romberg2d(p, 1, e2.data(), &res); // ScaCross
+		csca[r] = res * four_pi / k2;
+		for (int comp = 0; comp < 3; comp++) { // gx, gy, gz integrands (crosssec.c:1172-1245)
+			for (int i = 0; i < nth; i++) {
+				const double t = d2r * th[i];
+				for (int j = 0; j < nph; j++) {
+					const size_t q = (size_t)i * nph + j;
+					if (comp == 2) v[q] = e2[q] * cos(t);
+					else if (th[i] == 180) v[q] = 0;
+					else v[q] = e2[q] * sin(t) * (comp ? sin(d2r * ph[j]) : cos(d2r * ph[j]));
+				}
+			}
+			adda_gb300_romberg2d(p, 1, v.data(), &res);
+			csca_g[3 * r + comp] = res * four_pi / k2;
+		}
+	}
+	return ADDA_GB300_OK;
+}
+
 int adda_gb300_scattered_fields(adda_gb300_ctx *c, int nrhs, int ndir, const double *dirs, double *ebuff)
 {
 	if (!c || !dirs || !ebuff || ndir < 1 || nrhs < 1 || nrhs > c->last_nrhs || !c->pvec64) {

@@ -386,3 +386,56 @@ void __wrap_CalcField(doublecomplex ebuff[3], const double n[3])
 	}
 	__real_CalcField(ebuff, n);
 }
+
+/* CalcAlldir (crosssec.c:991-1050): the scattered field on the whole alldir grid, here in one batch on the GPU; the
+ * directions and the Epar/Eper unit vectors come from the reference's own SetScatPlane (crosssec.c:944-990), the
+ * host's Romberg integration (ScaCross, AsymParm_x/y/z) then reads E2_alldir as usual */
+typedef struct {
+	double min, max;
+	size_t N;
+	double *val;
+} angle_set; /* types.h:44-50 */
+extern angle_set theta_int, phi_int;           /* crosssec.c:62 */
+extern doublecomplex *E_ad;                    /* calculator.c:68-69 */
+extern double *E2_alldir;
+void SetScatPlane(const double ct, const double st, const double phi, double robs[3], double polPer[3]);
+void __real_CalcAlldir(void);
+
+void __wrap_CalcAlldir(void)
+{
+	if (!(g_ctx && g_pvec_valid && !surface && (ScatRelation == SQ_DRAINE || ScatRelation == SQ_FINDIP))) {
+		__real_CalcAlldir();
+		return;
+	}
+	const double deg = 0.017453292519943295769236907684886; /* Deg2Rad */
+	const size_t np = theta_int.N * phi_int.N;
+	double *dirs = malloc(sizeof(double) * 9 * np), *per = dirs + 3 * np, *par = dirs + 6 * np;
+	doublecomplex *e = malloc(sizeof(doublecomplex) * 3 * np);
+	if (!dirs || !e) ERR("CalcAlldir: out of host memory");
+	printf("Calculating scattered field for the whole solid angle:\n");
+	for (size_t i = 0, q = 0; i < theta_int.N; i++) {
+		const double th = deg * theta_int.val[i], ct = cos(th), st = sin(th);
+		for (size_t j = 0; j < phi_int.N; j++, q++) {
+			double *r = dirs + 3 * q, *u = per + 3 * q, *w = par + 3 * q;
+			SetScatPlane(ct, st, deg * phi_int.val[j], r, u);
+			w[0] = r[1] * u[2] - r[2] * u[1]; /* Epar = robserver x Eper */
+			w[1] = r[2] * u[0] - r[0] * u[2];
+			w[2] = r[0] * u[1] - r[1] * u[0];
+		}
+	}
+	if (adda_gb300_scattered_fields(g_ctx, 1, (int)np, dirs, (double *)e))
+		ERR("GPU CalcAlldir failed: %s", adda_gb300_last_error());
+	for (size_t q = 0; q < np; q++) {
+		doublecomplex a = 0, b = 0;
+		for (int k = 0; k < 3; k++) {
+			a += e[3 * q + k] * per[3 * q + k];
+			b += e[3 * q + k] * par[3 * q + k];
+		}
+		E_ad[2 * q] = a;
+		E_ad[2 * q + 1] = b;
+		E2_alldir[q] = creal(a) * creal(a) + cimag(a) * cimag(a) + creal(b) * creal(b) + cimag(b) * cimag(b);
+	}
+	printf("  done\n");
+	free(dirs);
+	free(e);
+}

@@ -2437,6 +2437,19 @@ int vjp_chi(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int rhs, const
 
 int scattered_fields(adda_gb300_ctx *c, int R, int ndir, const double *dirs, double *ebuff)
 {
+	constexpr int kMaxDir = 32768; // directions per launch (grid y extent)
+	if (ndir > kMaxDir) {
+		std::vector<double> part((size_t)R * kMaxDir * 6);
+		for (int d0 = 0; d0 < ndir; d0 += kMaxDir) {
+			const int nd = std::min(kMaxDir, ndir - d0);
+			int rc = scattered_fields(c, R, nd, dirs + 3 * (size_t)d0, part.data());
+			if (rc) return rc;
+			for (int r = 0; r < R; r++)
+				std::memcpy(ebuff + ((size_t)r * ndir + d0) * 6, part.data() + (size_t)r * nd * 6,
+					sizeof(double) * 6 * nd);
+		}
+		return ADDA_GB300_OK;
+	}
 	const size_t N = c->N;
 	cudaStream_t s = c->stream;
 	// blocks per (direction, RHS): at least 8 dipoles a thread, at most 128 blocks

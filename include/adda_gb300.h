@@ -244,6 +244,32 @@ int adda_gb300_solve_many(int nctx, adda_gb300_ctx *const *ctxs, const adda_gb30
 int adda_gb300_cross_sections(adda_gb300_ctx *ctx, int nrhs, const double *prop, const double *incpol,
 	double *cext, double *cabs);
 
+/* ---- integrals over scattering directions (host code; fields from the GPU) ------------------------------------- */
+
+/* one block of the reference's alldir_params.dat (theta: equal steps in cos, phi: equal steps in the angle; degrees):
+ * ScanIntegrParms, src/crosssec.c:233-307. The reference's defaults are theta {0, 180, 2, 6, 0, 0, 0} and phi
+ * {0, 360, 2, 5, 0, 1, 1}. */
+typedef struct {
+	double min, max;   /* degrees */
+	int Jmin, Jmax;    /* refinement stages: 2^Jmax + 1 grid points */
+	double eps;        /* relative error at which the integration may stop; 0 = use every point */
+	int equiv;         /* min and max are the same direction: the last point is not stored */
+	int periodic;      /* trapezoid rule instead of Romberg extrapolation */
+} adda_gb300_integr_parms;
+
+/* the grid angles in degrees (val may be NULL): equal steps in cos(angle) for in_cos (theta, from max down to min),
+ * in the angle otherwise. Returns the number of points, -1 for parameters the reference rejects. */
+int adda_gb300_integr_points(const adda_gb300_integr_parms *p, int in_cos, double *val);
+/* Romberg2D (src/Romberg.c:175-533): average over theta (outer, p[0]) and phi (inner, p[1]) of values
+ * [ntheta][nphi][dim] given on the grids above; returns the relative error estimate (-1 for bad arguments) */
+double adda_gb300_romberg2d(const adda_gb300_integr_parms p[2], int dim, const double *values, double *res);
+/* Csca and Csca*g of each RHS r < nrhs from the last solve (CalcAlldir + ScaCross + AsymParm_x/y/z, free space,
+ * src/crosssec.c:991-1260): the scattered field on the grid of p (directions cos(theta) prop + sin(theta)
+ * (cos(phi) incPolX + sin(phi) incPolY), SetScatPlane :944-990) on the GPU, |E|^2 and the Romberg integrals on the
+ * host. csca [nrhs]; csca_g [nrhs][3] in the beam frame (incPolX, incPolY, prop), g = csca_g / csca. */
+int adda_gb300_scattering_integrals(adda_gb300_ctx *ctx, int nrhs, const adda_gb300_integr_parms p[2],
+	const double prop[3], const double incpolx[3], const double incpoly[3], double *csca, double *csca_g);
+
 /* Scattering amplitudes, CalcField / CalcFieldFree (src/crosssec.c:506-596, 801-808; free space, Draine
  * scattering relation), in FP64 on the device from the polarisations left by the last solve:
  * E_r(n) = (-i k^3) exp(-i k r0.n) (I - nn).sum_j P_rj exp(-i kd n.pos_j) for each RHS r < nrhs and each unit

@@ -166,6 +166,111 @@ class Oracle:
         return e
 
 
+# ---- integrals over the scattering directions (src/crosssec.c:233-307, 991-1260; src/Romberg.c:175-533) ----
+# parms: dict(min, max, Jmin, Jmax, eps, equiv, periodic) per angle, degrees, as in alldir_params.dat
+ALLDIR_DEFAULT = (dict(min=0.0, max=180.0, Jmin=2, Jmax=6, eps=0.0, equiv=False, periodic=False),
+                  dict(min=0.0, max=360.0, Jmin=2, Jmax=5, eps=0.0, equiv=True, periodic=True))
+
+
+def alldir_angles(p, in_cos):
+    """grid angles in degrees: equal steps in cos for theta (from max down to min), in the angle for phi"""
+    if p["min"] == p["max"]:
+        return np.array([p["min"]])
+    G = 2 ** p["Jmax"] + 1
+    n = G - 1 if p["equiv"] else G
+    if in_cos:
+        lo, hi = np.cos(np.deg2rad(p["max"])), np.cos(np.deg2rad(p["min"]))
+        lo = 0.0 if abs(lo) < 1e-15 else lo
+        hi = 0.0 if abs(hi) < 1e-15 else hi
+        unit = (hi - lo) / (G - 1)
+        return np.array([np.rad2deg(np.arccos(lo + unit * i)) for i in range(n)])
+    unit = (p["max"] - p["min"]) / (G - 1)
+    return np.array([p["min"] + unit * i for i in range(n)])
+
+
+def _romberg(p, f, dim):
+    """one level of the bracketing Romberg scheme (Davis & Rabinowitz 6.3; trapezoid rule when periodic) over the
+    points 0..G-1 of a variable; f(i) -> (values[dim], abs error). Returns (average, abs error, rel error)."""
+    if p["min"] == p["max"]:
+        v, e = f(0)
+        return v, e, (0.0 if v[0] == 0 else e / abs(v[0]))
+    J, G = p["Jmax"], 2 ** p["Jmax"] + 1
+    c1 = [4.0 ** i for i in range(J + 1)]
+    c2 = [0.0] + [1 / (c1[i] - 1) for i in range(1, J + 1)]
+    c3 = [2 * c1[i] - 1 for i in range(J + 1)]
+    M = [np.zeros(dim) for _ in range(J + 1)]
+    T = np.zeros(dim)
+    abs_err = err = int_err = 0.0
+    m0 = 0
+    for m in range(J):
+        if m == 0:
+            T, int_err = f(0)
+            T = np.array(T, dtype=float)
+            if not p["equiv"]:
+                vl, el = f(G - 1)
+                int_err = 0.5 * (int_err + el)
+                T = 0.5 * (vl + T)
+        elif p["periodic"]:
+            T = 0.5 * (T + M[0])
+        else:
+            T = c3[m - 1] * c2[m] * (T - M[0]) + M[0]
+            m0 = m
+        step = (G - 1) >> m
+        acc, e = np.zeros(dim), 0.0
+        for j in range(step >> 1, G, step):
+            v, ej = f(j)
+            acc = acc + v
+            e += ej
+        sc = 2.0 ** (-m)
+        M[m0] = acc * sc
+        int_err = 0.5 * (int_err + e * sc)
+        if m0 != 0:
+            for k in range(m - 1, -1, -1):
+                M[k] = c2[m - k] * (c1[m - k] * M[k + 1] - M[k])
+        if m >= p["Jmin"] - 1:
+            abs_res = 0.5 * abs(M[0][0] + T[0])
+            abs_err = 0.5 * abs(M[0][0] - T[0]) + int_err
+            err = 0.0 if abs_res == 0 else abs_err / abs_res
+            if err < p["eps"]:
+                break
+    return 0.5 * (M[0] + T), abs_err, err
+
+
+def romberg2d(parms, values):
+    """Romberg2D: average of values [ntheta][nphi][dim] over theta (outer, cos spacing) and phi (inner)"""
+    values = np.asarray(values, dtype=float)
+    nphi = values.shape[1]
+
+    def inner(i):
+        def g(j):
+            return values[i, j if j < nphi else j - nphi], 0.0
+        r, e, _ = _romberg(parms[1], g, values.shape[2])
+        return r, e
+    return _romberg(parms[0], inner, values.shape[2])[0]
+
+
+def scattering_integrals(o, pvec, prop, incx, incy, wavenum, parms=ALLDIR_DEFAULT):
+    """Csca and Csca*g (beam frame) from the oracle's scattering amplitude on the alldir grid (CalcAlldir, ScaCross,
+    AsymParm_x/y/z)"""
+    th, ph = alldir_angles(parms[0], True), alldir_angles(parms[1], False)
+    prop, incx, incy = (np.asarray(v, dtype=float) for v in (prop, incx, incy))
+    e2 = np.zeros((len(th), len(ph)))
+    for i, t in enumerate(th):
+        ct, st = np.cos(np.deg2rad(t)), np.sin(np.deg2rad(t))
+        for j, f in enumerate(ph):
+            n = ct * prop + st * (np.cos(np.deg2rad(f)) * incx + np.sin(np.deg2rad(f)) * incy)
+            e = o.field(pvec, n)
+            e2[i, j] = np.sum(np.abs(e) ** 2)
+    scale = 4 * np.pi / wavenum ** 2
+    csca = romberg2d(parms, e2[:, :, None])[0] * scale
+    tr, pr = np.deg2rad(th)[:, None], np.deg2rad(ph)[None, :]
+    gx = np.where(th[:, None] == 180, 0.0, e2 * np.sin(tr) * np.cos(pr))
+    gy = np.where(th[:, None] == 180, 0.0, e2 * np.sin(tr) * np.sin(pr))
+    gz = e2 * np.cos(tr)
+    cg = np.array([romberg2d(parms, g[:, :, None])[0] * scale for g in (gx, gy, gz)])
+    return csca, cg
+
+
 def fftfit(x, divis=1):
     return lib().or_fftfit(x, divis)
 

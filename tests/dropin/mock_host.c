@@ -40,7 +40,16 @@ doublecomplex *xvec, *pvec, *Einc;
 double iter_eps = 1e-5;
 enum init_field InitField = IF_AUTO;
 doublecomplex ref_index[15], chi_inv[15][3];
-double prop[3];
+double prop[3], incPolX[3], incPolY[3];
+typedef struct {
+	double min, max;
+	size_t N;
+	double *val;
+} angle_set;
+angle_set theta_int, phi_int;
+doublecomplex *E_ad;
+double *E2_alldir;
+void CalcAlldir(void);
 const char *infi_fnameY, *infi_fnameX;
 enum chpoint chp_type = CHP_NONE;
 time_t chp_time = -1, last_chp_wt;
@@ -135,7 +144,7 @@ int main(int argc, char **argv)
 	gridYZ = gridY * gridZ;
 	WaveNum = 1.0;
 	gridspace = 2 * M_PI / dpl;
-	double py[3], px[3], cc[6];
+	double *py = incPolY, *px = incPolX, cc[6];
 	adda_gb300_rotation(NULL, 0, 0, 0, prop, py, px);
 	adda_gb300_polarizability(ADDA_POL_LDR, mre, mim, 2 * M_PI / dpl, gridspace, prop, py, 0, cc);
 	for (int c = 0; c < 3; c++) cc_sqrt[0][c] = csqrt(cc[2 * c] + I * cc[2 * c + 1]);
@@ -183,6 +192,14 @@ int main(int argc, char **argv)
 		CalcField(e, dirs[d]);
 		fwrite(e, sizeof(doublecomplex), 3, f);
 	}
+	/* the whole-solid-angle grid through the reference's CalcAlldir call (wrapped at link time): a small grid */
+	double thv[5] = {180, 120, 90, 60, 0}, phv[4] = {0, 90, 180, 270};
+	theta_int = (angle_set){0, 180, 5, thv};
+	phi_int = (angle_set){0, 270, 4, phv};
+	E_ad = malloc(sizeof(doublecomplex) * 2 * 20);
+	E2_alldir = malloc(sizeof(double) * 20);
+	CalcAlldir();
+	fwrite(E2_alldir, sizeof(double), 20, f);
 	fclose(f);
 	Free_FFT_Dmat();
 	printf("mock host: %lld dipoles, %d iterations, %zu matvecs\n", n, niter, TotalMatVec);

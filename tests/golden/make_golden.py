@@ -118,8 +118,34 @@ CASES = [
      dict(grid=16, m=1.5, dpl=10, iter="bcgs2")),
     ("ell_bcgs2_eps8", ["-iter", "bcgs2", "-eps", "8"] + ELL + MGN,
      dict(grid=8, m=1.1 + 0.1j, shape="ellipsoid", pars=(0.5, 1.5), iter="bcgs2", eps=1e-8)),
+    # Csca and the asymmetry vector from the alldir grid (-Csca -asym; -alldir_inp, written by alldir_file below)
+    # (converged solves, -eps 10, so that the integrals compare the quadrature and the fields, not where a solve
+    # stopped)
+    ("mgn_csca", ["-Csca", "-asym", "-eps", "10"] + MGN, dict(grid=8, m=1.1 + 0.1j, alldir="default", eps=1e-10)),
+    ("ell_orient_csca", ["-Csca", "-asym", "-eps", "10", "-orient", "10", "20", "30"] + ELL + MGN,
+     dict(grid=8, m=1.1 + 0.1j, shape="ellipsoid", pars=(0.5, 1.5), orient=(10, 20, 30), alldir="default",
+          eps=1e-10)),
+    ("c1_csca_adapt", ["-Csca", "-asym", "-eps", "10", "-grid", "16", "-dpl", "10", "-m", "1.5", "0"],
+     dict(grid=16, m=1.5, dpl=10, alldir="adapt", eps=1e-10)),
+    ("ell_csca_part", ["-Csca", "-asym", "-eps", "10", "-prop", "1", "2", "3"] + ELL + MGN,
+     dict(grid=8, m=1.1 + 0.1j, shape="ellipsoid", pars=(0.5, 1.5), prop=(1, 2, 3), alldir="part", eps=1e-10)),
 ] + [("grid%d" % g, ["-grid", str(g), "-size", "8"] + M, dict(grid=g, m=1.1 + 0.1j, size=8.0))
      for g in (2, 4, 6, 10, 12, 18, 20, 24, 30, 32)]
+
+
+# alldir_params.dat blocks (theta, phi): min, max, Jmin, Jmax, eps, equiv, periodic
+ALLDIR = {
+    "default": ((0, 180, 2, 6, 0, False, False), (0, 360, 2, 5, 0, True, True)),
+    "adapt": ((0, 180, 3, 7, 1e-3, False, False), (0, 360, 2, 5, 1e-4, True, True)),
+    "part": ((30, 150, 2, 4, 0, False, False), (0, 180, 1, 3, 0, False, False)),
+}
+
+
+def alldir_file(path, kind):
+    with open(path, "w") as f:
+        for name, (lo, hi, jmin, jmax, eps, eq, per) in zip(("theta", "phi"), ALLDIR[kind]):
+            f.write("%s:\nmin=%g\nmax=%g\nJmin=%d\nJmax=%d\neps=%g\nequiv=%s\nperiodic=%s\n\n" % (
+                name, lo, hi, jmin, jmax, eps, "true" if eq else "false", "true" if per else "false"))
 
 
 def parse_run(rundir, stdout):
@@ -151,6 +177,12 @@ def parse_run(rundir, stdout):
             txt = open(f).read()
             cs[pol] = dict(Cext=float(re.search(r"Cext\s*=\s*([-+0-9.eE]+)", txt).group(1)),
                            Cabs=float(re.search(r"Cabs\s*=\s*([-+0-9.eE]+)", txt).group(1)))
+            m = re.search(r"Csca\s*=\s*([-+0-9.eE]+)", txt)
+            if m:
+                cs[pol]["Csca"] = float(m.group(1))
+                vec = r"\(([-+0-9.eE]+),([-+0-9.eE]+),([-+0-9.eE]+)\)"
+                cs[pol]["Csca.g"] = [float(v) for v in re.search(r"Csca\.g\s*=\s*" + vec, txt).groups()]
+                cs[pol]["g"] = [float(v) for v in re.search(r"\ng\s*=\s*" + vec, txt).groups()]
     out["cross"] = cs
     out["maxiter_warning"] = "haven't converged" in stdout + log
     mf = os.path.join(rundir, "mueller")
@@ -169,6 +201,9 @@ def main(ref_src="/root/reference/src"):
     with tempfile.TemporaryDirectory() as tmp:
         for name, args, kw in CASES:
             full = args + ["-sym", "no"]
+            if "alldir" in kw:
+                alldir_file(os.path.join(tmp, name + "_alldir.dat"), kw["alldir"])
+                full += ["-alldir_inp", name + "_alldir.dat"]
             rundir = os.path.join(tmp, name)
             p = subprocess.run([binp] + full + ["-dir", rundir], cwd=tmp, capture_output=True, text=True)
             if p.returncode != 0:

@@ -77,8 +77,9 @@ def test_gpu_stop_and_resume_equals_uninterrupted(method):
         assert res["stats"][r]["status"] == full["stats"][r]["status"] == "ok"
         n = full["stats"][r]["niter"]
         # the dot products carried into the first resumed iteration are recomputed from the loaded vectors (same
-        # partition and order as the fused ones; QMR_CS_2's delta divides by ro^2 instead of |v~|^2)
-        np.testing.assert_allclose(res["hist"][r][3:n + 1], full["hist"][r][3:n + 1], rtol=1e-10)
+        # partition and order as the fused ones; QMR_CS_2's delta divides by ro^2 instead of |v~|^2, which moves late
+        # residuals of 1e-8 by ~1e-16 absolute)
+        np.testing.assert_allclose(res["hist"][r][3:n + 1], full["hist"][r][3:n + 1], rtol=1e-10, atol=1e-14)
         assert rel(res["x"][r], full["x"][r]) < 1e-10
 
 

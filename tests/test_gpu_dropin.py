@@ -22,7 +22,8 @@ def build_mock():
                     os.path.join(ROOT, "tests", "dropin", "mock_host.c"),
                     os.path.join(ROOT, "tests", "dropin", "mock_crosssec.c"),
                     os.path.join(ROOT, "a-dda_gb300", "csrc", "dropin", "adda_dropin.c"),
-                    "-L" + BUILD, "-ladda_gb300", "-Wl,-rpath," + BUILD, "-Wl,--wrap=CalcField", "-lm"], check=True)
+                    "-L" + BUILD, "-ladda_gb300", "-Wl,-rpath," + BUILD, "-Wl,--wrap=CalcField", "-Wl,--wrap=CalcAlldir",
+                    "-lm"], check=True)
     return exe
 
 
@@ -40,7 +41,8 @@ def test_dropin_solve_and_matvec(tmp_path, method):
     niter = int(np.frombuffer(raw[8:12], np.int32)[0])
     ip = float(np.frombuffer(raw[12:20], np.float64)[0])
     vec = np.frombuffer(raw[20:], np.complex128)
-    pv, y, fields = vec[:3 * n], vec[3 * n:6 * n], vec[6 * n:].reshape(3, 3)
+    pv, y, fields = vec[:3 * n], vec[3 * n:6 * n], vec[6 * n:6 * n + 9].reshape(3, 3)
+    e2 = np.frombuffer(raw[20 + 16 * (6 * n + 9):], np.float64)
     s = setup_for(dict(grid=16, m=1.5, dpl=10))
     assert n == s.n
     o = oracle_for(s)
@@ -58,6 +60,15 @@ def test_dropin_solve_and_matvec(tmp_path, method):
     for d, n_ in enumerate([s.prop, (0.6, 0.0, 0.8), (0.0, -1.0, 0.0)]):
         eo = o.field(pv, np.asarray(n_, dtype=float))
         assert np.linalg.norm(fields[d] - eo) <= 1e-12 * np.linalg.norm(eo), (d, fields[d], eo)
+    # CalcAlldir through its wrapper: |E|^2 on a 5 x 4 grid of beam-frame directions in one GPU batch
+    k = 0
+    for th in (180, 120, 90, 60, 0):
+        for ph in (0, 90, 180, 270):
+            t, f = np.deg2rad(th), np.deg2rad(ph)
+            dirn = np.cos(t) * s.prop + np.sin(t) * (np.cos(f) * s.incpol[1] + np.sin(f) * s.incpol[0])
+            eo = o.field(pv, dirn)
+            assert abs(e2[k] / np.sum(np.abs(eo) ** 2) - 1) < 1e-12, (th, ph, e2[k])
+            k += 1
 
 
 def _run_mock(tmp_path, extra, eps="10"):
