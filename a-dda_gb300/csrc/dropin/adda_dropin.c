@@ -439,3 +439,56 @@ void __wrap_CalcAlldir(void)
 	free(dirs);
 	free(e);
 }
+
+/* CalcScatGrid (crosssec.c:1055-1100): the field on the -scat_grid_inp grid (a theta x phi grid or theta/phi pairs)
+ * in one GPU batch, projected on Eper/Epar from the reference's SetScatPlane, into EgridY or EgridX */
+enum scatgrid { SG_GRID, SG_PAIRS };           /* const.h:291-294 */
+typedef struct {
+	enum scatgrid type;
+	size_t N;
+	angle_set theta, phi;
+} scat_grid_angles;                            /* types.h:52-58 */
+extern scat_grid_angles angles;                /* vars.c:95-97 */
+extern doublecomplex *EgridX, *EgridY;
+void __real_CalcScatGrid(enum incpol which);
+
+void __wrap_CalcScatGrid(enum incpol which)
+{
+	if (!(g_ctx && g_pvec_valid && !surface && (ScatRelation == SQ_DRAINE || ScatRelation == SQ_FINDIP))) {
+		__real_CalcScatGrid(which);
+		return;
+	}
+	const double deg = 0.017453292519943295769236907684886;
+	const size_t np = angles.N, nph = (angles.type == SG_GRID) ? angles.phi.N : 1;
+	double *dirs = malloc(sizeof(double) * 9 * np), *per = dirs + 3 * np, *par = dirs + 6 * np;
+	doublecomplex *e = malloc(sizeof(doublecomplex) * 3 * np);
+	if (!dirs || !e) ERR("CalcScatGrid: out of host memory");
+	printf("Calculating grid of scattered field:\n");
+	size_t q = 0;
+	for (size_t i = 0; i < angles.theta.N && q < np; i++) {
+		const double th = deg * angles.theta.val[i], ct = cos(th), st = sin(th);
+		for (size_t j = 0; j < nph && q < np; j++, q++) {
+			const double ph = deg * ((angles.type == SG_GRID) ? angles.phi.val[j] : angles.phi.val[i]);
+			double *r = dirs + 3 * q, *u = per + 3 * q, *w = par + 3 * q;
+			SetScatPlane(ct, st, ph, r, u);
+			w[0] = r[1] * u[2] - r[2] * u[1];
+			w[1] = r[2] * u[0] - r[0] * u[2];
+			w[2] = r[0] * u[1] - r[1] * u[0];
+		}
+	}
+	if (adda_gb300_scattered_fields(g_ctx, 1, (int)q, dirs, (double *)e))
+		ERR("GPU CalcScatGrid failed: %s", adda_gb300_last_error());
+	doublecomplex *grid = (which == INCPOL_Y) ? EgridY : EgridX;
+	for (size_t k = 0; k < q; k++) {
+		doublecomplex a = 0, b = 0;
+		for (int c = 0; c < 3; c++) {
+			a += e[3 * k + c] * per[3 * k + c];
+			b += e[3 * k + c] * par[3 * k + c];
+		}
+		grid[2 * k] = a;
+		grid[2 * k + 1] = b;
+	}
+	printf("  done\n");
+	free(dirs);
+	free(e);
+}

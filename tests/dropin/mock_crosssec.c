@@ -15,6 +15,13 @@ void CalcField(doublecomplex ebuff[3], const double n[3])
 	exit(3);
 }
 
+void CalcScatGrid(enum incpol which)
+{
+	(void)which;
+	fprintf(stderr, "mock host: the CPU CalcScatGrid was called\n");
+	exit(3);
+}
+
 void CalcAlldir(void)
 {
 	fprintf(stderr, "mock host: the CPU CalcAlldir was called\n");

@@ -50,6 +50,15 @@ angle_set theta_int, phi_int;
 doublecomplex *E_ad;
 double *E2_alldir;
 void CalcAlldir(void);
+enum scatgrid { SG_GRID, SG_PAIRS };
+typedef struct {
+	enum scatgrid type;
+	size_t N;
+	angle_set theta, phi;
+} scat_grid_angles;
+scat_grid_angles angles;
+doublecomplex *EgridX, *EgridY;
+void CalcScatGrid(enum incpol which);
 const char *infi_fnameY, *infi_fnameX;
 enum chpoint chp_type = CHP_NONE;
 time_t chp_time = -1, last_chp_wt;
@@ -200,6 +209,12 @@ int main(int argc, char **argv)
 	E2_alldir = malloc(sizeof(double) * 20);
 	CalcAlldir();
 	fwrite(E2_alldir, sizeof(double), 20, f);
+	/* three (theta, phi) pairs through the reference's CalcScatGrid call (wrapped at link time) */
+	double sgt[3] = {30, 90, 150}, sgp[3] = {10, 200, 300};
+	angles = (scat_grid_angles){SG_PAIRS, 3, {30, 150, 3, sgt}, {10, 300, 3, sgp}};
+	EgridY = malloc(sizeof(doublecomplex) * 6);
+	CalcScatGrid(INCPOL_Y);
+	fwrite(EgridY, sizeof(doublecomplex), 6, f);
 	fclose(f);
 	Free_FFT_Dmat();
 	printf("mock host: %lld dipoles, %d iterations, %zu matvecs\n", n, niter, TotalMatVec);

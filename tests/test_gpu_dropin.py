@@ -23,7 +23,7 @@ def build_mock():
                     os.path.join(ROOT, "tests", "dropin", "mock_crosssec.c"),
                     os.path.join(ROOT, "a-dda_gb300", "csrc", "dropin", "adda_dropin.c"),
                     "-L" + BUILD, "-ladda_gb300", "-Wl,-rpath," + BUILD, "-Wl,--wrap=CalcField", "-Wl,--wrap=CalcAlldir",
-                    "-lm"], check=True)
+                    "-Wl,--wrap=CalcScatGrid", "-lm"], check=True)
     return exe
 
 
@@ -42,7 +42,8 @@ def test_dropin_solve_and_matvec(tmp_path, method):
     ip = float(np.frombuffer(raw[12:20], np.float64)[0])
     vec = np.frombuffer(raw[20:], np.complex128)
     pv, y, fields = vec[:3 * n], vec[3 * n:6 * n], vec[6 * n:6 * n + 9].reshape(3, 3)
-    e2 = np.frombuffer(raw[20 + 16 * (6 * n + 9):], np.float64)
+    e2 = np.frombuffer(raw[20 + 16 * (6 * n + 9):20 + 16 * (6 * n + 9) + 160], np.float64)
+    egrid = np.frombuffer(raw[20 + 16 * (6 * n + 9) + 160:], np.complex128).reshape(3, 2)
     s = setup_for(dict(grid=16, m=1.5, dpl=10))
     assert n == s.n
     o = oracle_for(s)
@@ -69,6 +70,16 @@ def test_dropin_solve_and_matvec(tmp_path, method):
             eo = o.field(pv, dirn)
             assert abs(e2[k] / np.sum(np.abs(eo) ** 2) - 1) < 1e-12, (th, ph, e2[k])
             k += 1
+    # CalcScatGrid through its wrapper: E projected on Eper = robs x prop/|..| and Epar = robs x Eper (pairs)
+    for k, (th, ph) in enumerate(((30, 10), (90, 200), (150, 300))):
+        t, f = np.deg2rad(th), np.deg2rad(ph)
+        dirn = np.cos(t) * s.prop + np.sin(t) * (np.cos(f) * s.incpol[1] + np.sin(f) * s.incpol[0])
+        per = np.cross(dirn, s.prop)
+        per /= np.linalg.norm(per)
+        par = np.cross(dirn, per)
+        eo = o.field(pv, dirn)
+        want = np.array([eo @ per, eo @ par])
+        assert np.linalg.norm(egrid[k] - want) <= 1e-12 * np.linalg.norm(eo), (th, ph, egrid[k], want)
 
 
 def _run_mock(tmp_path, extra, eps="10"):
