@@ -390,18 +390,28 @@ class Context:
         return (y[0], ip[0]) if one else (y, ip)
 
     def solve(self, einc, method="qmr", prec="fp64", eps=1e-5, maxiter=100000, init="auto", check_every=0,
-              inner_eps=0.0, max_refine=0, hist_cap=0, x0=None, chp_time=0.0, full_steps=False):
+              inner_eps=0.0, max_refine=0, hist_cap=0, x0=None, chp_time=0.0, full_steps=False, out=None):
         """einc: [nrhs, 3N] complex. Returns dict with x, p [nrhs,3N], stats per RHS and residual histories
         (hist[r][k] = RE_k). init="x0" starts from x0 [nrhs, 3N] (see field_to_x0 for a field read from file or from
         wkb_field); init="chpoint" resumes every RHS from chpoint_load. chp_time > 0 stops after that many seconds
-        (status "chpoint", state kept for chpoint_save); full_steps: BiCGStab without its half-step exit."""
+        (status "chpoint", state kept for chpoint_save); full_steps: BiCGStab without its half-step exit.
+        out: optional (x, p) complex128 [nrhs, 3N] C-contiguous host arrays (e.g. views of pinned memory) that receive
+        the solution and the polarisations directly."""
         e = np.ascontiguousarray(einc, dtype=np.complex128).reshape(-1, 3 * self.n)
         R = e.shape[0]
-        if init == "x0":
+        if out is not None:
+            x, p = out
+            for a in (x, p):
+                if a.dtype != np.complex128 or a.shape != e.shape or not a.flags["C_CONTIGUOUS"]:
+                    raise ValueError("out arrays must be C-contiguous complex128 of shape %s" % (e.shape,))
+            if init == "x0":
+                x[:] = np.asarray(x0, dtype=np.complex128).reshape(R, 3 * self.n)
+        elif init == "x0":
             x = np.ascontiguousarray(np.array(x0, dtype=np.complex128).reshape(R, 3 * self.n))
         else:
             x = np.empty_like(e)
-        p = np.empty_like(e)
+        if out is None:
+            p = np.empty_like(e)
         st = (RhsStats * R)()
         hist = np.zeros((R, hist_cap)) if hist_cap else None
         sp = SolveParams(ITERS[method], PREC[prec], eps, maxiter, INIT[init], check_every, inner_eps, max_refine,
