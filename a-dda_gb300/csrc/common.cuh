@@ -30,6 +30,36 @@ template <typename C> __host__ __device__ __forceinline__ C cx(decltype(C::x) a,
 }
 template <typename C> __host__ __device__ __forceinline__ C cadd(C a, C b) { return cx<C>(a.x + b.x, a.y + b.y); }
 template <typename C> __host__ __device__ __forceinline__ C csub(C a, C b) { return cx<C>(a.x - b.x, a.y - b.y); }
+// Complex float2 sums on Blackwell's packed FP32 pipe: add/sub.rn.f32x2 process both halves in one issue slot, each
+// half rounded to nearest like the scalar instruction. The FFT butterflies are mostly such sums, so this halves
+// their issue slots. (Only the FP32 transforms use them; the double-float code keeps scalar error-free
+// transformations.)
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ unsigned long long f2_bits(float2 a)
+{
+	unsigned long long r;
+	asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+	return r;
+}
+__device__ __forceinline__ float2 f2_of(unsigned long long r)
+{
+	float2 a;
+	asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+	return a;
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b)
+{
+	unsigned long long r;
+	asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+	return f2_of(r);
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b)
+{
+	unsigned long long r;
+	asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+	return f2_of(r);
+}
+#endif
 template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b)
 {
 	return cx<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
