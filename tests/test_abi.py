@@ -59,3 +59,27 @@ def test_create_fails_loudly_without_gpu(adda):
     box, pos, mat = adda.make_particle("sphere", 8)
     with pytest.raises(adda.AddaError):
         adda.Context(box, pos, mat, 0.5, 1.0)
+
+
+def test_host_functions_reject_bad_arguments(adda):
+    """the host-side entry points return the reference's error cases as status codes instead of aborting"""
+    L = adda.lib()
+    prop = np.array([0.0, 0.0, 1.0])
+    pol = np.array([0.0, 1.0, 0.0])
+    cc = np.zeros(6)
+    p = prop.ctypes.data_as(ctypes.c_void_p)
+    q = pol.ctypes.data_as(ctypes.c_void_p)
+    c = cc.ctypes.data_as(ctypes.c_void_p)
+    assert L.adda_gb300_polarizability(99, 1.5, 0.0, 0.6, 0.1, p, q, 0, c) == -1       # unknown -pol
+    assert L.adda_gb300_polarizability_nloc(9, 1.5, 0.0, 0.1, -1.0, c) == -1          # negative Gaussian width
+    assert L.adda_gb300_polarizability_nloc(0, 1.5, 0.0, 0.1, 0.2, c) == -1           # not an nloc relation
+    by, bz = ctypes.c_int(), ctypes.c_int()
+    assert L.adda_gb300_fit_box(7, None, 16, ctypes.byref(by), ctypes.byref(bz)) != 0  # unknown shape
+    # alldir parameters the reference's ScanIntegrParms rejects
+    for bad in (dict(min=10.0, max=5.0), dict(Jmin=0), dict(Jmax=1, Jmin=2), dict(eps=-1.0), dict(max=190.0)):
+        prm = dict(adda.ALLDIR_DEFAULT[0])
+        prm.update(bad)
+        with pytest.raises(adda.AddaError):
+            adda.integr_points(prm, True)
+    assert len(adda.integr_points(adda.ALLDIR_DEFAULT[0], True)) == 65      # 2^6 + 1 values of cos(theta)
+    assert len(adda.integr_points(adda.ALLDIR_DEFAULT[1], False)) == 32     # 2^5 + 1 - 1 (min == max direction)
