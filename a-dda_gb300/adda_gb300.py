@@ -103,12 +103,13 @@ EXPORTS = ["adda_gb300_fft_fit", "adda_gb300_fit_box", "adda_gb300_make_particle
 _lib = None
 
 
-def build(force=False):
+def build(force=False, out=None, defines=()):
+    """compile the library (out/defines: a variant build in another directory with extra -D macros)"""
     import importlib.util
     spec = importlib.util.spec_from_file_location("adda_gb300_build", os.path.join(HERE, "build.py"))
     mod = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mod)
-    return mod.build(force=force)
+    return mod.build(force=force, out=out, defines=defines)
 
 
 def lib():
@@ -116,53 +117,58 @@ def lib():
     global _lib
     if _lib is None:
         build()
-        L = ctypes.CDLL(LIB_PATH)
-        P, I, D, SZ = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_size_t
-        sig = {
-            "adda_gb300_fft_fit": ([I, I], I),
-            "adda_gb300_fit_box": ([I, P, I, P, P], I),
-            "adda_gb300_make_particle": ([I, P, I, I, I, P, P], SZ),
-            "adda_gb300_rotation": ([P, D, D, D, P, P, P], None),
-            "adda_gb300_plane_wave": ([SZ, P, I, I, I, D, D, P, P, P], None),
-            "adda_gb300_wkb_field": ([I, I, I, SZ, P, P, I, P, D, P, P], I),
-            "adda_gb300_polarizability": ([I, D, D, D, D, P, P, I, P], I),
-            "adda_gb300_polarizability_dchi": ([I, D, D, D, D, P, P, I, P], I),
-            "adda_gb300_polarizability_nloc": ([I, D, D, D, D, P], I),
-            "adda_gb300_vjp_chi": ([P, P, I, P, P, P, P, P], I),
-            "adda_gb300_create": ([P, P], I),
-            "adda_gb300_destroy": ([P], I),
-            "adda_gb300_get_grid": ([P, P], I),
-            "adda_gb300_init_dmatrix": ([P], I),
-            "adda_gb300_dmatrix_len": ([P], SZ),
-            "adda_gb300_get_dmatrix": ([P, P], I),
-            "adda_gb300_set_cc": ([P, I, I, P], I),
-            "adda_gb300_set_cc_sqrt": ([P, I, I, P], I),
-            "adda_gb300_set_cc_dipole": ([P, I, P], I),
-            "adda_gb300_matvec": ([P, I, I, P, P, P, I], I),
-            "adda_gb300_matvec_device": ([P, I, I, P, P, P, I], I),
-            "adda_gb300_solve": ([P, P, I, P, P, P, P, P, I], I),
-            "adda_gb300_solve_device": ([P, P, I, P, P, P, P], I),
-            "adda_gb300_solve_many": ([I, P, P, P, P, P, P, P], I),
-            "adda_gb300_chpoint_size": ([P, I], SZ),
-            "adda_gb300_integr_points": ([P, I, P], I),
-            "adda_gb300_romberg2d": ([P, I, P, P], D),
-            "adda_gb300_scattering_integrals": ([P, I, P, P, P, P, P, P], I),
-            "adda_gb300_chpoint_save": ([P, I, P, SZ], I),
-            "adda_gb300_chpoint_load": ([P, I, P, SZ], I),
-            "adda_gb300_time_matvec": ([P, I, I, I, SZ, P], I),
-            "adda_gb300_cross_sections": ([P, I, P, P, P, P], I),
-            "adda_gb300_scattered_fields": ([P, I, I, P, P], I),
-            "adda_gb300_cross_sections_noalloc": ([I, SZ, P, P, P, P, I, I, I, I, I, D, D, P, P, P, P, P], I),
-            "adda_gb300_last_error": ([], ctypes.c_char_p),
-            "adda_gb300_last_solve_ms": ([P], D),
-            "adda_gb300_kernel_launches": ([], ctypes.c_uint64),
-        }
-        for name, (args, res) in sig.items():
-            f = getattr(L, name)
-            f.argtypes = args
-            f.restype = res
-        _lib = L
+        _lib = load_library(LIB_PATH)
     return _lib
+
+
+def load_library(path):
+    """a libadda_gb300.so with the C ABI's argument and result types bound"""
+    L = ctypes.CDLL(path)
+    P, I, D, SZ = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_size_t
+    sig = {
+        "adda_gb300_fft_fit": ([I, I], I),
+        "adda_gb300_fit_box": ([I, P, I, P, P], I),
+        "adda_gb300_make_particle": ([I, P, I, I, I, P, P], SZ),
+        "adda_gb300_rotation": ([P, D, D, D, P, P, P], None),
+        "adda_gb300_plane_wave": ([SZ, P, I, I, I, D, D, P, P, P], None),
+        "adda_gb300_wkb_field": ([I, I, I, SZ, P, P, I, P, D, P, P], I),
+        "adda_gb300_polarizability": ([I, D, D, D, D, P, P, I, P], I),
+        "adda_gb300_polarizability_dchi": ([I, D, D, D, D, P, P, I, P], I),
+        "adda_gb300_polarizability_nloc": ([I, D, D, D, D, P], I),
+        "adda_gb300_vjp_chi": ([P, P, I, P, P, P, P, P], I),
+        "adda_gb300_create": ([P, P], I),
+        "adda_gb300_destroy": ([P], I),
+        "adda_gb300_get_grid": ([P, P], I),
+        "adda_gb300_init_dmatrix": ([P], I),
+        "adda_gb300_dmatrix_len": ([P], SZ),
+        "adda_gb300_get_dmatrix": ([P, P], I),
+        "adda_gb300_set_cc": ([P, I, I, P], I),
+        "adda_gb300_set_cc_sqrt": ([P, I, I, P], I),
+        "adda_gb300_set_cc_dipole": ([P, I, P], I),
+        "adda_gb300_matvec": ([P, I, I, P, P, P, I], I),
+        "adda_gb300_matvec_device": ([P, I, I, P, P, P, I], I),
+        "adda_gb300_solve": ([P, P, I, P, P, P, P, P, I], I),
+        "adda_gb300_solve_device": ([P, P, I, P, P, P, P], I),
+        "adda_gb300_solve_many": ([I, P, P, P, P, P, P, P], I),
+        "adda_gb300_chpoint_size": ([P, I], SZ),
+        "adda_gb300_integr_points": ([P, I, P], I),
+        "adda_gb300_romberg2d": ([P, I, P, P], D),
+        "adda_gb300_scattering_integrals": ([P, I, P, P, P, P, P, P], I),
+        "adda_gb300_chpoint_save": ([P, I, P, SZ], I),
+        "adda_gb300_chpoint_load": ([P, I, P, SZ], I),
+        "adda_gb300_time_matvec": ([P, I, I, I, SZ, P], I),
+        "adda_gb300_cross_sections": ([P, I, P, P, P, P], I),
+        "adda_gb300_scattered_fields": ([P, I, I, P, P], I),
+        "adda_gb300_cross_sections_noalloc": ([I, SZ, P, P, P, P, I, I, I, I, I, D, D, P, P, P, P, P], I),
+        "adda_gb300_last_error": ([], ctypes.c_char_p),
+        "adda_gb300_last_solve_ms": ([P], D),
+        "adda_gb300_kernel_launches": ([], ctypes.c_uint64),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    return L
 
 
 def _p(a):
@@ -327,8 +333,8 @@ class Context:
     """One particle lattice on one GPU: the interaction matrix, FP64/FP32 matvecs, solver and cross sections."""
 
     def __init__(self, box, pos, mat, gridspace, wavenum, grid=(0, 0, 0), nrhs_max=2, device=0, interaction="poi",
-                 nloc_rp=0.0):
-        self.L = lib()
+                 nloc_rp=0.0, library=None):
+        self.L = library or lib()
         self.pos = np.ascontiguousarray(pos, dtype=np.uint16).reshape(-1, 3)
         self.mat = None if mat is None else np.ascontiguousarray(mat, dtype=np.uint8)
         self.n = len(self.pos)
@@ -343,9 +349,9 @@ class Context:
         self.grid = tuple(g)
 
     @classmethod
-    def from_setup(cls, s, nrhs_max=2, device=0):
+    def from_setup(cls, s, nrhs_max=2, device=0, library=None):
         c = cls(s.box, s.pos, s.mat, s.gridspace, s.wavenum, s.grid, nrhs_max, device, s.interaction,
-                getattr(s, "nloc_rp", 0.0))
+                getattr(s, "nloc_rp", 0.0), library)
         c.init_dmatrix()
         for r in range(min(nrhs_max, len(s.cc))):
             c.set_cc(r, s.cc[r].reshape(1, 3))

@@ -49,32 +49,36 @@ def _run(cmd):
     return r.stdout + r.stderr
 
 
-def build(force=False, verbose=False):
-    os.makedirs(OUT, exist_ok=True)
-    if not force and not _stale(LIB, _sources()):
-        return LIB
+def build(force=False, verbose=False, out=None, defines=()):
+    """compile the library into out (default a-dda_gb300/_build); defines: extra -D macros (a variant build, e.g. the
+    scalar-sum reference build ADDA_NO_F32X2 of the tests)"""
+    out_dir = out or OUT
+    lib_path = os.path.join(out_dir, "libadda_gb300.so")
+    os.makedirs(out_dir, exist_ok=True)
+    if not force and not _stale(lib_path, _sources()):
+        return lib_path
     nv = nvcc()
     jobs = []
     objs = []
     for f in CU:
-        o = os.path.join(OUT, f + ".o")
+        o = os.path.join(out_dir, f + ".o")
         objs.append(o)
         jobs.append([nv, "-c", os.path.join(CSRC, f), "-o", o, "-std=c++17", "-O3", "-lineinfo", *ARCH,
                      "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC, "--expt-relaxed-constexpr",
-                     "-Xptxas", "-v" if verbose else "-O3"])
+                     *["-D" + d for d in defines], "-Xptxas", "-v" if verbose else "-O3"])
     for f in C:
-        o = os.path.join(OUT, f + ".o")
+        o = os.path.join(out_dir, f + ".o")
         objs.append(o)
         jobs.append(["gcc", "-c", os.path.join(CSRC, f), "-o", o, "-O2", "-fPIC", "-std=gnu11", "-I", INCLUDE])
     logs = []
     with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         for out in ex.map(_run, jobs):
             logs.append(out)
-    _run([nv, "-shared", *ARCH, "-o", LIB + ".tmp", *objs, "-lm"])
-    os.replace(LIB + ".tmp", LIB)
+    _run([nv, "-shared", *ARCH, "-o", lib_path + ".tmp", *objs, "-lm"])
+    os.replace(lib_path + ".tmp", lib_path)
     if verbose:
         print("\n".join(logs))
-    return LIB
+    return lib_path
 
 
 if __name__ == "__main__":

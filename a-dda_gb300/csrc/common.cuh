@@ -33,8 +33,12 @@ template <typename C> __host__ __device__ __forceinline__ C csub(C a, C b) { ret
 // Complex float2 sums on Blackwell's packed FP32 pipe: add/sub.rn.f32x2 process both halves in one issue slot, each
 // half rounded to nearest like the scalar instruction. The FFT butterflies are mostly such sums, so this halves
 // their issue slots. (Only the FP32 transforms use them; the double-float code keeps scalar error-free
-// transformations.)
-#if defined(__CUDA_ARCH__)
+// transformations.) Built with -DADDA_NO_F32X2 the same sums are scalar round-to-nearest adds (__fadd_rn), which
+// must give the same bits: the tests compare the two builds.
+#if defined(__CUDA_ARCH__) && defined(ADDA_NO_F32X2)
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y)); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y)); }
+#elif defined(__CUDA_ARCH__)
 __device__ __forceinline__ unsigned long long f2_bits(float2 a)
 {
 	unsigned long long r;
