@@ -74,11 +74,12 @@ def integr_points(p, in_cos):
     return out
 
 
-def romberg2d(parms, values):
-    """the reference's Romberg2D average of values [ntheta][nphi][dim] on the alldir grid"""
+def romberg2d(parms, values, poles=False):
+    """the reference's Romberg2D average of values [ntheta][nphi][dim] on the alldir (or orientation) grid; poles:
+    full-range orientation averaging, where beta = 0 and 180 are single orientations"""
     v = np.ascontiguousarray(values, dtype=np.float64)
     res = np.zeros(v.shape[2])
-    lib().adda_gb300_romberg2d(_parms(parms), v.shape[2], _p(v), _p(res))
+    lib().adda_gb300_romberg2d_ex(_parms(parms), v.shape[2], _p(v), _p(res), int(poles))
     return res
 
 
@@ -96,7 +97,7 @@ EXPORTS = ["adda_gb300_fft_fit", "adda_gb300_fit_box", "adda_gb300_make_particle
            "adda_gb300_solve", "adda_gb300_solve_device", "adda_gb300_solve_many", "adda_gb300_vjp_chi",
            "adda_gb300_chpoint_size", "adda_gb300_chpoint_save", "adda_gb300_chpoint_load",
            "adda_gb300_cross_sections", "adda_gb300_scattered_fields", "adda_gb300_integr_points",
-           "adda_gb300_romberg2d", "adda_gb300_scattering_integrals",
+           "adda_gb300_romberg2d", "adda_gb300_romberg2d_ex", "adda_gb300_scattering_integrals",
            "adda_gb300_cross_sections_noalloc", "adda_gb300_time_matvec",
            "adda_gb300_last_solve_ms", "adda_gb300_last_error", "adda_gb300_kernel_launches"]
 
@@ -153,6 +154,7 @@ def load_library(path):
         "adda_gb300_chpoint_size": ([P, I], SZ),
         "adda_gb300_integr_points": ([P, I, P], I),
         "adda_gb300_romberg2d": ([P, I, P, P], D),
+        "adda_gb300_romberg2d_ex": ([P, I, P, P, I], D),
         "adda_gb300_scattering_integrals": ([P, I, P, P, P, P, P, P], I),
         "adda_gb300_chpoint_save": ([P, I, P, SZ], I),
         "adda_gb300_chpoint_load": ([P, I, P, SZ], I),
@@ -284,6 +286,7 @@ class Setup:
                  avgpol=False, prop=None, lam=2 * math.pi, interaction="poi", nloc_rp=0.0, pol_rp=0.0):
         self.interaction = interaction
         self.nloc_rp = float(nloc_rp)
+        self.pol, self.avgpol, self.pol_rp, self.prop0 = pol, avgpol, pol_rp, prop
         self.box, self.pos, self.mat = make_particle(shape, grid, pars)
         self.n = len(self.pos)
         self.grid = (fft_fit(2 * self.box[0]), fft_fit(2 * self.box[1]), fft_fit(2 * self.box[2], 2))
@@ -305,6 +308,44 @@ class Setup:
 
 # ---------------------------------------------------------------------------------------------------------------------
 # device context
+
+# the reference's avg_params.dat defaults for the Euler angles beta (equal steps in cos) and gamma
+AVG_DEFAULT = (dict(min=0.0, max=180.0, Jmin=2, Jmax=4, eps=1e-3, equiv=False, periodic=False),
+               dict(min=0.0, max=360.0, Jmin=2, Jmax=4, eps=1e-3, equiv=True, periodic=True))
+
+
+def orient_avg_cross_sections(ctx, s, parms=AVG_DEFAULT, full_alpha=True, method="qmr", prec="mixed", eps=1e-5,
+                              maxiter=100000):
+    """-orient avg for the cross sections (calculate_one_orientation and its Romberg integration over the Euler
+    angles, src/calculator.c:293-358,690-710; CalculateE.c:737-751): for every (beta, gamma) of the avg_params grid
+    (alpha = 0) the two incident polarisations are solved, the unpolarised Cext and Cabs are the means of the two, and
+    the two-level Romberg scheme averages them over the orientations (full_alpha: the first Euler angle covers
+    0..360, so beta = 0 and 180 are single orientations). The reference evaluates the orientations one after another
+    as the adaptive integration asks for them; here all of them are solved up front as right-hand sides of batched
+    solves (ctx.nrhs_max at a time), with each orientation's own polarisability (LDR averaged over the incident
+    polarisation, as the reference forces for -orient avg, param.c:2136-2139: it still depends on the direction).
+    s: the Setup the context was made from. Returns (Cext, Cabs) and the per-orientation values [nbeta][ngamma][2]."""
+    betas, gammas = integr_points(parms[0], True), integr_points(parms[1], False)
+    jobs = []  # (ib, ig, prop, incpol)
+    for ib, b in enumerate(betas):
+        for ig, g in enumerate(gammas):
+            prop, py, px = rotation(0.0, b, g, prop0=s.prop0)
+            jobs += [(ib, ig, prop, py), (ib, ig, prop, px)]
+    R = ctx.nrhs_max
+    vals = np.zeros((len(betas), len(gammas), 2))
+    for k0 in range(0, len(jobs), R):
+        batch = jobs[k0:k0 + R]
+        for r, (_, _, prop, inc) in enumerate(batch):
+            ctx.set_cc(r, polarizability(s.m, s.kd, s.gridspace, prop, inc, s.pol, True, s.pol_rp).reshape(1, 3))
+        einc = np.stack([plane_wave(s.box, s.pos, s.gridspace, s.wavenum, prop, inc) for _, _, prop, inc in batch])
+        ctx.solve(einc, method=method, prec=prec, eps=eps, maxiter=maxiter)
+        ce, ca = ctx.cross_sections(np.stack([b[2] for b in batch]), np.stack([b[3] for b in batch]))
+        for r, (ib, ig, _, _) in enumerate(batch):
+            vals[ib, ig, 0] += 0.5 * ce[r]
+            vals[ib, ig, 1] += 0.5 * ca[r]
+    res = romberg2d(parms, vals, poles=full_alpha)
+    return res[0], res[1], vals
+
 
 def solve_many(ctxs, eincs, method="qmr", prec="mixed", eps=1e-5, maxiter=100000, init="auto", check_every=0):
     """solve several contexts (particles) concurrently; eincs[i]: [nrhs_i, 3N_i] complex. Returns per context

@@ -127,7 +127,8 @@ typedef struct {
 	int Gt, Gp, nphi, dim;
 	const double *values;
 	const coefs *cf;
-	int theta; /* row of the inner integration */
+	int theta;              /* row of the inner integration */
+	int pole_lo, pole_hi;   /* the first / last outer point is a pole: its inner integral is its first value */
 } r2d;
 
 static double get_value(void *ctx, int j, double *out)
@@ -144,10 +145,17 @@ static double get_inner(void *ctx, int i, double *out)
 	r2d *s = ctx;
 	s->theta = i;
 	double rel;
+	if ((i == 0 && s->pole_lo) || (i == s->Gt - 1 && s->pole_hi)) return get_value(s, 0, out); /* onepoint */
 	return romberg_1d(&s->p[1], s->Gp, s->cf, s->dim, get_value, s, out, &rel);
 }
 
 double adda_gb300_romberg2d(const adda_gb300_integr_parms p[2], int dim, const double *values, double *res)
+{
+	return adda_gb300_romberg2d_ex(p, dim, values, res, 0);
+}
+
+double adda_gb300_romberg2d_ex(const adda_gb300_integr_parms p[2], int dim, const double *values, double *res,
+	int poles)
 {
 	const int nth = adda_gb300_integr_points(&p[0], 1, NULL), nph = adda_gb300_integr_points(&p[1], 0, NULL);
 	if (nth < 1 || nph < 1 || dim < 1 || !values || !res) return -1;
@@ -155,7 +163,10 @@ double adda_gb300_romberg2d(const adda_gb300_integr_parms p[2], int dim, const d
 	const int Jt = (p[0].min == p[0].max) ? 1 : p[0].Jmax, Jp = (p[1].min == p[1].max) ? 1 : p[1].Jmax;
 	set_coefs(&cf, (Jt > Jp ? Jt : Jp) + 1);
 	r2d s = {p, (p[0].min == p[0].max) ? 1 : (1 << p[0].Jmax) + 1, (p[1].min == p[1].max) ? 1 : (1 << p[1].Jmax) + 1,
-		nph, dim, values, &cf, 0};
+		nph, dim, values, &cf, 0, 0, 0};
+	/* the outer grid starts at cos(max) and ends at cos(min): a pole where that angle is 180 or 0 degrees */
+	s.pole_lo = poles && p[0].max == 180 && p[0].min != p[0].max;
+	s.pole_hi = poles && p[0].min == 0 && p[0].min != p[0].max;
 	adda_gb300_integr_parms outer = p[0], inner = p[1];
 	if (p[0].min == p[0].max) outer.Jmax = 1;
 	if (p[1].min == p[1].max) inner.Jmax = 1;

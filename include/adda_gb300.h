@@ -263,6 +263,11 @@ int adda_gb300_integr_points(const adda_gb300_integr_parms *p, int in_cos, doubl
 /* Romberg2D (src/Romberg.c:175-533): average over theta (outer, p[0]) and phi (inner, p[1]) of values
  * [ntheta][nphi][dim] given on the grids above; returns the relative error estimate (-1 for bad arguments) */
 double adda_gb300_romberg2d(const adda_gb300_integr_parms p[2], int dim, const double *values, double *res);
+/* the same with poles != 0 for orientation averaging over the full range of the first Euler angle (full_al_range,
+ * src/crosssec.c:369): at beta = 180 and beta = 0 every gamma is the same orientation, so the inner integral there is
+ * the value at gamma index 0 (OuterInitT's onepoint, src/Romberg.c:374-386) */
+double adda_gb300_romberg2d_ex(const adda_gb300_integr_parms p[2], int dim, const double *values, double *res,
+	int poles);
 /* Csca and Csca*g of each RHS r < nrhs from the last solve (CalcAlldir + ScaCross + AsymParm_x/y/z, free space,
  * src/crosssec.c:991-1260): the scattered field on the grid of p (directions cos(theta) prop + sin(theta)
  * (cos(phi) incPolX + sin(phi) incPolY), SetScatPlane :944-990) on the GPU, |E|^2 and the Romberg integrals on the

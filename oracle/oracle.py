@@ -236,13 +236,24 @@ def _romberg(p, f, dim):
     return 0.5 * (M[0] + T), abs_err, err
 
 
-def romberg2d(parms, values):
-    """Romberg2D: average of values [ntheta][nphi][dim] over theta (outer, cos spacing) and phi (inner)"""
+def romberg2d(parms, values, poles=False, used=None):
+    """Romberg2D: average of values [ntheta][nphi][dim] over theta (outer, cos spacing) and phi (inner); poles: the
+    outer end points at 180 and 0 degrees use their first inner value alone (orientation averaging over the full
+    alpha range, OuterInitT's onepoint, src/Romberg.c:347-360)"""
     values = np.asarray(values, dtype=float)
     nphi = values.shape[1]
+    nth = values.shape[0]
 
     def inner(i):
+        full = parms[0]["min"] != parms[0]["max"]
+        if poles and full and ((i == 0 and parms[0]["max"] == 180) or (i == nth - 1 and parms[0]["min"] == 0)):
+            if used is not None:
+                used.add((i, 0))
+            return values[i, 0], 0.0
+
         def g(j):
+            if used is not None:
+                used.add((i, j if j < nphi else j - nphi))
             return values[i, j if j < nphi else j - nphi], 0.0
         r, e, _ = _romberg(parms[1], g, values.shape[2])
         return r, e
