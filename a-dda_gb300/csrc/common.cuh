@@ -11,6 +11,7 @@
 // which the reference uses (fft.h FFT_FORWARD -1).
 #pragma once
 
+#include <cmath>
 #include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -30,15 +31,14 @@ template <typename C> __host__ __device__ __forceinline__ C cx(decltype(C::x) a,
 }
 template <typename C> __host__ __device__ __forceinline__ C cadd(C a, C b) { return cx<C>(a.x + b.x, a.y + b.y); }
 template <typename C> __host__ __device__ __forceinline__ C csub(C a, C b) { return cx<C>(a.x - b.x, a.y - b.y); }
-// Complex float2 sums on Blackwell's packed FP32 pipe: add/sub.rn.f32x2 process both halves in one issue slot, each
-// half rounded to nearest like the scalar instruction. The FFT butterflies are mostly such sums, so this halves
-// their issue slots. (Only the FP32 transforms use them; the double-float code keeps scalar error-free
-// transformations.) Built with -DADDA_NO_F32X2 the same sums are scalar round-to-nearest adds (__fadd_rn), which
-// must give the same bits: the tests compare the two builds.
-#if defined(__CUDA_ARCH__) && defined(ADDA_NO_F32X2)
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y)); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y)); }
-#elif defined(__CUDA_ARCH__)
+// Pairs of floats. Sums run on Blackwell's packed FP32 pipe: add/sub.rn.f32x2 process both halves in one issue slot,
+// each half rounded to nearest like the scalar instruction (never contracted: the error-free transformations of the
+// double-float code below rely on it). A complex float2 sum is one instruction, which halves the issue slots of the
+// FFT butterflies (mostly such sums) and of the double-float complex arithmetic. Built with -DADDA_NO_F32X2 the sums
+// are scalar __fadd_rn/__fsub_rn, which must give the same bits (the tests compare the two builds). Scalar on the
+// host.
+#if defined(__CUDA_ARCH__) && !defined(ADDA_NO_F32X2)
+#define ADDA_F32X2 1
 __device__ __forceinline__ unsigned long long f2_bits(float2 a)
 {
 	unsigned long long r;
@@ -51,19 +51,53 @@ __device__ __forceinline__ float2 f2_of(unsigned long long r)
 	asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
 	return a;
 }
-__device__ __forceinline__ float2 cadd(float2 a, float2 b)
+#endif
+__host__ __device__ __forceinline__ float2 p_add(float2 a, float2 b)
 {
+#ifdef ADDA_F32X2
 	unsigned long long r;
 	asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_bits(a)), "l"(f2_bits(b)));
 	return f2_of(r);
+#elif defined(__CUDA_ARCH__)
+	return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y));
+#else
+	return make_float2(a.x + b.x, a.y + b.y);
+#endif
 }
-__device__ __forceinline__ float2 csub(float2 a, float2 b)
+__host__ __device__ __forceinline__ float2 p_sub(float2 a, float2 b)
 {
+#ifdef ADDA_F32X2
 	unsigned long long r;
 	asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_bits(a)), "l"(f2_bits(b)));
 	return f2_of(r);
-}
+#elif defined(__CUDA_ARCH__)
+	return make_float2(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y));
+#else
+	return make_float2(a.x - b.x, a.y - b.y);
 #endif
+}
+// products stay scalar round-to-nearest operations: a packed mul.f32x2 did not give the scalar instruction's bits in
+// every compiled context (a bit-for-bit check against __fmul_rn found differences inside larger kernels), so only the
+// sums, which do, use the packed pipe
+__host__ __device__ __forceinline__ float2 p_mul(float2 a, float2 b)
+{
+#ifdef __CUDA_ARCH__
+	return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y));
+#else
+	return make_float2(a.x * b.x, a.y * b.y);
+#endif
+}
+// a*b + c per half, one rounding
+__host__ __device__ __forceinline__ float2 p_fma(float2 a, float2 b, float2 c)
+{
+#ifdef __CUDA_ARCH__
+	return make_float2(__fmaf_rn(a.x, b.x, c.x), __fmaf_rn(a.y, b.y, c.y));
+#else
+	return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y));
+#endif
+}
+__host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return p_add(a, b); }
+__host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return p_sub(a, b); }
 template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b)
 {
 	return cx<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -152,22 +186,106 @@ __host__ __device__ __forceinline__ DF df_of(double v)
 }
 __host__ __device__ __forceinline__ double df_val(DF a) { return (double)a.h + (double)a.l; }
 
-// complex double-float: the Krylov vector element of the MIXED solver (16 bytes, like double2)
+// complex double-float: the Krylov vector element of the MIXED solver (16 bytes, like double2). The high parts of
+// the real and imaginary part share one float2, the low parts the other, so that the double-float arithmetic of a
+// complex value runs on packed FP32 pairs (both parts in one instruction).
 struct __align__(16) dd2 {
-	DF x, y;
+	float2 h, l; // re = h.x + l.x, im = h.y + l.y
 };
-__host__ __device__ __forceinline__ double2 to_d2(dd2 a) { return make_double2(df_val(a.x), df_val(a.y)); }
-template <> __host__ __device__ __forceinline__ dd2 from_d2<dd2>(double2 a)
+__host__ __device__ __forceinline__ DF dd2_re(dd2 a) { return DF{a.h.x, a.l.x}; }
+__host__ __device__ __forceinline__ DF dd2_im(dd2 a) { return DF{a.h.y, a.l.y}; }
+__host__ __device__ __forceinline__ dd2 make_dd2(DF re, DF im)
 {
-	dd2 r;
-	r.x = df_of(a.x);
-	r.y = df_of(a.y);
-	return r;
+	return dd2{make_float2(re.h, im.h), make_float2(re.l, im.l)};
 }
+__host__ __device__ __forceinline__ double2 to_d2(dd2 a) { return make_double2(df_val(dd2_re(a)), df_val(dd2_im(a))); }
+template <> __host__ __device__ __forceinline__ dd2 from_d2<dd2>(double2 a) { return make_dd2(df_of(a.x), df_of(a.y)); }
+
+// Packed double-float arithmetic: the scalar algorithms above applied to the two halves at once.
+// TwoSum of each half: s + e = a + b exactly
+__host__ __device__ __forceinline__ void p_two_sum(float2 a, float2 b, float2 &s, float2 &e)
+{
+	s = p_add(a, b);
+	const float2 v = p_sub(s, a);
+	e = p_add(p_sub(a, p_sub(s, v)), p_sub(b, v));
+}
+// s + e = a - b exactly
+__host__ __device__ __forceinline__ void p_two_diff(float2 a, float2 b, float2 &s, float2 &e)
+{
+	s = p_sub(a, b);
+	const float2 v = p_sub(s, a);
+	e = p_sub(p_sub(a, p_sub(s, v)), p_add(b, v));
+}
+// renormalisation (FastTwoSum, |a| >= |b| per half)
+__host__ __device__ __forceinline__ dd2 p_renorm(float2 a, float2 b)
+{
+	const float2 s = p_add(a, b);
+	return dd2{s, p_sub(b, p_sub(s, a))};
+}
+__host__ __device__ __forceinline__ dd2 cadd(dd2 a, dd2 b)
+{
+	float2 s, e;
+	p_two_sum(a.h, b.h, s, e);
+	return p_renorm(s, p_add(e, p_add(a.l, b.l)));
+}
+__host__ __device__ __forceinline__ dd2 csub(dd2 a, dd2 b)
+{
+	float2 s, e;
+	p_two_diff(a.h, b.h, s, e);
+	return p_renorm(s, p_add(e, p_sub(a.l, b.l)));
+}
+// elementwise product of the halves: (a.re*b.re, a.im*b.im) as double-floats; exact product error through FMA
+__host__ __device__ __forceinline__ dd2 p_hmul(dd2 a, dd2 b)
+{
+	const float2 p = p_mul(a.h, b.h);
+	float2 e = p_fma(a.h, b.h, p_sub(make_float2(0.f, 0.f), p));
+	e = p_fma(a.h, b.l, e);
+	e = p_fma(a.l, b.h, e);
+	return p_renorm(p, e);
+}
+__host__ __device__ __forceinline__ dd2 dd2_swap(dd2 a)
+{
+	return dd2{make_float2(a.h.y, a.h.x), make_float2(a.l.y, a.l.x)};
+}
+__host__ __device__ __forceinline__ dd2 cconj(dd2 a)
+{
+	return dd2{make_float2(a.h.x, -a.h.y), make_float2(a.l.x, -a.l.y)};
+}
+__host__ __device__ __forceinline__ dd2 cneg(dd2 a) { return dd2{make_float2(-a.h.x, -a.h.y), make_float2(-a.l.x, -a.l.y)}; }
+// real double-float factor
+__host__ __device__ __forceinline__ dd2 cscale(dd2 a, DF s)
+{
+	return p_hmul(a, dd2{make_float2(s.h, s.h), make_float2(s.l, s.l)});
+}
+// a*b = (a.re b.re - a.im b.im, a.re b.im + a.im b.re) = a.re*(b.re, b.im) + a.im*(-b.im, b.re)
+__host__ __device__ __forceinline__ dd2 cmul(dd2 a, dd2 b)
+{
+	const dd2 ar{make_float2(a.h.x, a.h.x), make_float2(a.l.x, a.l.x)};
+	const dd2 ai{make_float2(-a.h.y, a.h.y), make_float2(-a.l.y, a.l.y)};
+	return cadd(p_hmul(ar, b), p_hmul(ai, dd2_swap(b)));
+}
+// a loop-invariant complex factor k prepared once: k*v = (k.re, k.re)*(v.re, v.im) + (-k.im, k.im)*(v.im, v.re)
+struct dd2k {
+	dd2 re, im;
+};
+__host__ __device__ __forceinline__ dd2k make_dd2k(dd2 k)
+{
+	return dd2k{dd2{make_float2(k.h.x, k.h.x), make_float2(k.l.x, k.l.x)},
+		dd2{make_float2(-k.h.y, k.h.y), make_float2(-k.l.y, k.l.y)}};
+}
+__host__ __device__ __forceinline__ dd2 cmul(dd2k k, dd2 v) { return cadd(p_hmul(k.re, v), p_hmul(k.im, dd2_swap(v))); }
+__host__ __device__ __forceinline__ dd2 cmul(dd2 v, dd2k k) { return cmul(k, v); }
 
 // real coefficient in the arithmetic of the vector type C
-template <typename C> __host__ __device__ __forceinline__ decltype(C::x) rof(double v) { return (decltype(C::x))v; }
-template <> __host__ __device__ __forceinline__ DF rof<dd2>(double v) { return df_of(v); }
+template <typename C> struct RealOf {
+	typedef decltype(C::x) T;
+	static __host__ __device__ __forceinline__ T make(double v) { return (T)v; }
+};
+template <> struct RealOf<dd2> {
+	typedef DF T;
+	static __host__ __device__ __forceinline__ DF make(double v) { return df_of(v); }
+};
+template <typename C> __host__ __device__ __forceinline__ typename RealOf<C>::T rof(double v) { return RealOf<C>::make(v); }
 
 // Per-thread accumulators of the fused reductions: double for float2/double2 vectors (exact products of floats,
 // FP64 sums), double-float for dd2 vectors (no FP64 instruction per element). acc_val gives the double the block
@@ -186,7 +304,11 @@ template <typename C> __device__ __forceinline__ void acc_abs2(double &s, C y)
 	const double2 d = to_d2(y);
 	s += d.x * d.x + d.y * d.y;
 }
-__device__ __forceinline__ void acc_abs2(DF &s, dd2 y) { s = s + (y.x * y.x + y.y * y.y); }
+__device__ __forceinline__ void acc_abs2(DF &s, dd2 y)
+{
+	const dd2 q = p_hmul(y, y); // (re^2, im^2)
+	s = s + (dd2_re(q) + dd2_im(q));
+}
 // (sr, si) += a*b
 template <typename C> __device__ __forceinline__ void acc_cmul(double &sr, double &si, C a, C b)
 {
@@ -196,8 +318,9 @@ template <typename C> __device__ __forceinline__ void acc_cmul(double &sr, doubl
 }
 __device__ __forceinline__ void acc_cmul(DF &sr, DF &si, dd2 a, dd2 b)
 {
-	sr = sr + (a.x * b.x - a.y * b.y);
-	si = si + (a.x * b.y + a.y * b.x);
+	const dd2 p = p_hmul(a, b), q = p_hmul(a, dd2_swap(b)); // (re*re, im*im), (re*im, im*re)
+	sr = sr + (dd2_re(p) - dd2_im(p));
+	si = si + (dd2_re(q) + dd2_im(q));
 }
 // (sr, si) += a*conj(b)
 template <typename C> __device__ __forceinline__ void acc_cmulc(double &sr, double &si, C a, C b)
@@ -208,8 +331,9 @@ template <typename C> __device__ __forceinline__ void acc_cmulc(double &sr, doub
 }
 __device__ __forceinline__ void acc_cmulc(DF &sr, DF &si, dd2 a, dd2 b)
 {
-	sr = sr + (a.x * b.x + a.y * b.y);
-	si = si + (a.y * b.x - a.x * b.y);
+	const dd2 p = p_hmul(a, b), q = p_hmul(a, dd2_swap(b)); // (re*re, im*im), (re*im, im*re)
+	sr = sr + (dd2_re(p) + dd2_im(p));
+	si = si + (dd2_im(q) - dd2_re(q));
 }
 // s[0] += Re(y)^2, s[1] += Im(y)^2, s[2] += Re(y)*Im(y)
 template <typename C> __device__ __forceinline__ void acc_sq3(double *s, C y)
@@ -221,9 +345,10 @@ template <typename C> __device__ __forceinline__ void acc_sq3(double *s, C y)
 }
 __device__ __forceinline__ void acc_sq3(DF *s, dd2 y)
 {
-	s[0] = s[0] + y.x * y.x;
-	s[1] = s[1] + y.y * y.y;
-	s[2] = s[2] + y.x * y.y;
+	const dd2 q = p_hmul(y, y), r = p_hmul(y, dd2_swap(y)); // (re^2, im^2), (re*im, im*re)
+	s[0] = s[0] + dd2_re(q);
+	s[1] = s[1] + dd2_im(q);
+	s[2] = s[2] + dd2_re(r);
 }
 
 // ---------------------------------------------------------------------------------------------------------------

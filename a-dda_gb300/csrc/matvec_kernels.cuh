@@ -58,17 +58,8 @@ template <typename T, typename V> struct MvP {
 
 template <typename To, typename From> __device__ __forceinline__ To cvt(From a) { return from_d2<To>(to_d2(a)); }
 // double-float vectors: round to float on load (K1) and widen the float S.X exactly (K3), all on the FP32 pipes
-template <> __device__ __forceinline__ float2 cvt<float2, dd2>(dd2 a)
-{
-	return make_float2(__fadd_rn(a.x.h, a.x.l), __fadd_rn(a.y.h, a.y.l));
-}
-template <> __device__ __forceinline__ dd2 cvt<dd2, float2>(float2 a)
-{
-	dd2 r;
-	r.x = DF{a.x, 0.f};
-	r.y = DF{a.y, 0.f};
-	return r;
-}
+template <> __device__ __forceinline__ float2 cvt<float2, dd2>(dd2 a) { return p_add(a.h, a.l); }
+template <> __device__ __forceinline__ dd2 cvt<dd2, float2>(float2 a) { return dd2{a, make_float2(0.f, 0.f)}; }
 
 template <typename P> __device__ __forceinline__ bool all_done(const P &p)
 {

@@ -111,7 +111,17 @@ __device__ __forceinline__ double2 dsqrt(double2 z)
 	return dc(fabs(b) / (2 * t), copysign(t, b));
 }
 
-template <typename C> __device__ __forceinline__ C cof(double2 k) { return from_d2<C>(k); }
+// a loop-invariant complex coefficient in the arithmetic of the vector type C (prepared for the packed double-float
+// products when C is dd2)
+template <typename C> struct CoefOf {
+	typedef C T;
+	static __device__ __forceinline__ C make(double2 k) { return from_d2<C>(k); }
+};
+template <> struct CoefOf<dd2> {
+	typedef dd2k T;
+	static __device__ __forceinline__ dd2k make(double2 k) { return make_dd2k(from_d2<dd2>(k)); }
+};
+template <typename C> __device__ __forceinline__ typename CoefOf<C>::T cof(double2 k) { return CoefOf<C>::make(k); }
 
 // block sum of up to 4 values; result valid in thread 0
 __device__ __forceinline__ void block_sum4(double v[4], int nv)
@@ -302,7 +312,7 @@ template <typename C> __global__ void __launch_bounds__(NT) qmr_v_init(const Rhs
 {
 	const int rr = blockIdx.y;
 	if (st[rr].done) return;
-	const C k = cof<C>(st[rr].kib);
+	const auto k = cof<C>(st[rr].kib);
 	VLOOP(n3) v[rr * n3 + i] = cmul(k, r[rr * n3 + i]);
 }
 
@@ -339,7 +349,7 @@ __global__ void __launch_bounds__(NT) qmr_v1(const RhsState *st, C *vt, const C 
 {
 	const int r = blockIdx.y;
 	if (st[r].done) return;
-	const C k0 = cof<C>(st[r].k0), k1 = cof<C>(st[r].k1);
+	const auto k0 = cof<C>(st[r].k0), k1 = cof<C>(st[r].k1);
 	typename AccOf<C>::T s[4] = {};
 	VLOOP(n3) {
 		const size_t j = r * n3 + i;
@@ -397,7 +407,7 @@ __global__ void __launch_bounds__(NT) qmr_v2(const RhsState *st, C *po, const C 
 	const int r = blockIdx.y;
 	if (st[r].done) return;
 	const RhsState &S = st[r];
-	const C k0 = cof<C>(S.k0), k1 = cof<C>(S.k1), k2 = cof<C>(S.k2), k3 = cof<C>(S.k3), kib = cof<C>(S.kib),
+	const auto k0 = cof<C>(S.k0), k1 = cof<C>(S.k1), k2 = cof<C>(S.k2), k3 = cof<C>(S.k3), kib = cof<C>(S.kib),
 		kr = cof<C>(S.kr);
 	const auto d0 = rof<C>(S.d0);
 	typename AccOf<C>::T s[4] = {};
@@ -478,7 +488,7 @@ __global__ void __launch_bounds__(NT) bs_v1(const RhsState *st, C *p, const C *v
 {
 	const int r = blockIdx.y;
 	if (st[r].done) return;
-	const C k0 = cof<C>(st[r].k0), k1 = cof<C>(st[r].k1);
+	const auto k0 = cof<C>(st[r].k0), k1 = cof<C>(st[r].k1);
 	VLOOP(n3) {
 		const size_t j = r * n3 + i;
 		p[j] = cadd(cadd(cmul(k0, p[j]), cmul(k1, v[j])), rv[j]);
@@ -512,7 +522,7 @@ __global__ void __launch_bounds__(NT) bs_v2(const RhsState *st, C *sv, const C *
 {
 	const int r = blockIdx.y;
 	if (st[r].done) return;
-	const C k0 = cof<C>(st[r].k0);
+	const auto k0 = cof<C>(st[r].k0);
 	typename AccOf<C>::T s[4] = {};
 	VLOOP(n3) {
 		const size_t j = r * n3 + i;
@@ -555,7 +565,7 @@ __global__ void __launch_bounds__(NT) bs_v3(const RhsState *st, C *x, const C *p
 	const int r = blockIdx.y;
 	if (st[r].done) return;
 	const RhsState &S = st[r];
-	const C a = cof<C>(S.balpha), om = cof<C>(S.omega), mom = cof<C>(dc(-S.omega.x, -S.omega.y));
+	const auto a = cof<C>(S.balpha), om = cof<C>(S.omega), mom = cof<C>(dc(-S.omega.x, -S.omega.y));
 	const bool half = S.half != 0;
 	typename AccOf<C>::T s[4] = {};
 	VLOOP(n3) {
@@ -601,7 +611,7 @@ template <typename C> __global__ void __launch_bounds__(NT) bg_v1(const RhsState
 	const int r = blockIdx.y;
 	if (st[r].done) return;
 	const bool first = st[r].niter == 1;
-	const C k0 = cof<C>(st[r].k0);
+	const auto k0 = cof<C>(st[r].k0);
 	VLOOP(n3) {
 		const size_t j = r * n3 + i;
 		p[j] = first ? rv[j] : cadd(cmul(k0, p[j]), rv[j]);
@@ -635,7 +645,7 @@ __global__ void __launch_bounds__(NT) bg_v2(const RhsState *st, C *x, const C *p
 {
 	const int r = blockIdx.y;
 	if (st[r].done) return;
-	const C a = cof<C>(st[r].balpha), ma = cof<C>(dc(-st[r].balpha.x, -st[r].balpha.y));
+	const auto a = cof<C>(st[r].balpha), ma = cof<C>(dc(-st[r].balpha.x, -st[r].balpha.y));
 	typename AccOf<C>::T s[4] = {};
 	VLOOP(n3) {
 		const size_t j = r * n3 + i;
@@ -763,7 +773,7 @@ __global__ void __launch_bounds__(NT) cs_v1(const RhsState *st, C *qo, const C *
 	const int r = blockIdx.y;
 	if (st[r].done) return;
 	const bool first = st[r].niter == 1;
-	const C k0 = cof<C>(st[r].k0);
+	const auto k0 = cof<C>(st[r].k0);
 	const auto k1 = rof<C>(st[r].k1.x);
 	typename AccOf<C>::T s[4] = {};
 	VLOOP(n3) {
@@ -834,7 +844,7 @@ __global__ void __launch_bounds__(NT) cs_v2(const RhsState *st, C *po, const C *
 	if (st[r].done) return;
 	const RhsState &S = st[r];
 	const int it = S.niter;
-	const C k1 = cof<C>(S.k1), k2 = cof<C>(S.k2), k3 = cof<C>(S.k3), kr = cof<C>(S.kr);
+	const auto k1 = cof<C>(S.k1), k2 = cof<C>(S.k2), k3 = cof<C>(S.k3), kr = cof<C>(S.kr);
 	const auto kib = rof<C>(S.kib.x);
 	VLOOP(n3) {
 		const size_t j = r * n3 + i;
@@ -900,7 +910,7 @@ template <typename C> __global__ void __launch_bounds__(NT) q2_v1(const RhsState
 	if (st[r].done) return;
 	const bool first = st[r].niter == 1;
 	const auto ir = rof<C>(st[r].kib.x);
-	const C k0 = cof<C>(st[r].k0);
+	const auto k0 = cof<C>(st[r].k0);
 	VLOOP(n3) {
 		const size_t j = r * n3 + i;
 		const C vv = cscale(v[j], ir);
@@ -935,7 +945,7 @@ __global__ void __launch_bounds__(NT) q2_v2(const RhsState *st, C *v, const C *A
 {
 	const int r = blockIdx.y;
 	if (st[r].done) return;
-	const C k1 = cof<C>(st[r].k1);
+	const auto k1 = cof<C>(st[r].k1);
 	typename AccOf<C>::T s[4] = {};
 	VLOOP(n3) {
 		const size_t j = r * n3 + i;
@@ -983,7 +993,7 @@ __global__ void __launch_bounds__(NT) q2_v3(const RhsState *st, C *d, const C *p
 	if (st[r].done) return;
 	const RhsState &S = st[r];
 	const bool first = S.niter == 1;
-	const C eta = cof<C>(S.k2), me = cof<C>(S.kr);
+	const auto eta = cof<C>(S.k2), me = cof<C>(S.kr);
 	const auto d0 = rof<C>(S.d0), sa = rof<C>(S.k3.x);
 	typename AccOf<C>::T s[4] = {};
 	VLOOP(n3) {
@@ -1041,7 +1051,7 @@ __global__ void __launch_bounds__(NT) b2_vu(const RhsState *st, C *u0, const C *
 	const int r = blockIdx.y;
 	if (st[r].done) return;
 	const bool copy = st[r].niter == 1 && j == 0;
-	const C k0 = cof<C>(st[r].k0);
+	const auto k0 = cof<C>(st[r].k0);
 	VLOOP(n3) {
 		const size_t q = r * n3 + i;
 		u0[q] = copy ? r0[q] : cadd(cmul(k0, u0[q]), r0[q]);
@@ -1075,7 +1085,7 @@ __global__ void __launch_bounds__(NT) b2_vx(const RhsState *st, C *x, const C *u
 {
 	const int r = blockIdx.y;
 	if (st[r].done) return;
-	const C a = cof<C>(st[r].b2_alpha), ma = cof<C>(dc(-st[r].b2_alpha.x, -st[r].b2_alpha.y));
+	const auto a = cof<C>(st[r].b2_alpha), ma = cof<C>(dc(-st[r].b2_alpha.x, -st[r].b2_alpha.y));
 	typename AccOf<C>::T s[4] = {};
 	VLOOP(n3) {
 		const size_t q = r * n3 + i;
@@ -1194,8 +1204,8 @@ __global__ void __launch_bounds__(NT) b2_vfinal(const RhsState *st, C *u0, const
 {
 	const int r = blockIdx.y;
 	if (st[r].done) return;
-	const C y1 = cof<C>(st[r].b2_y1), y2 = cof<C>(st[r].b2_y2);
-	const C my1 = cof<C>(dc(-st[r].b2_y1.x, -st[r].b2_y1.y)), my2 = cof<C>(dc(-st[r].b2_y2.x, -st[r].b2_y2.y));
+	const auto y1 = cof<C>(st[r].b2_y1), y2 = cof<C>(st[r].b2_y2);
+	const auto my1 = cof<C>(dc(-st[r].b2_y1.x, -st[r].b2_y1.y)), my2 = cof<C>(dc(-st[r].b2_y2.x, -st[r].b2_y2.y));
 	typename AccOf<C>::T s[4] = {};
 	VLOOP(n3) {
 		const size_t q = r * n3 + i;
