@@ -32,10 +32,15 @@ class Problem(ctypes.Structure):
                 ("gridX", ctypes.c_int), ("gridY", ctypes.c_int), ("gridZ", ctypes.c_int),
                 ("ndip", ctypes.c_size_t), ("position", ctypes.c_void_p), ("material", ctypes.c_void_p),
                 ("gridspace", ctypes.c_double), ("wavenum", ctypes.c_double), ("nrhs_max", ctypes.c_int),
-                ("device", ctypes.c_int), ("interaction", ctypes.c_int), ("nloc_rp", ctypes.c_double)]
+                ("device", ctypes.c_int), ("interaction", ctypes.c_int), ("nloc_rp", ctypes.c_double),
+                ("surface", ctypes.c_int), ("zsum_shift", ctypes.c_double), ("msub_re", ctypes.c_double),
+                ("msub_im", ctypes.c_double), ("msub_inf", ctypes.c_int), ("refl", ctypes.c_int),
+                ("refl_data", ctypes.c_void_p)]
 
 
 INTERACTIONS = {"poi": 0, "fcd": 1, "fcd_st": 2, "nloc": 3, "nloc_av": 4}
+# -int_surf: image dipole (GPU), image + Sommerfeld integrals from a table, or a tensor supplied by the caller
+REFL = {"img": 0, "som": 1, "host": 2}
 
 
 class SolveParams(ctypes.Structure):
@@ -89,13 +94,14 @@ class RhsStats(ctypes.Structure):
 
 
 EXPORTS = ["adda_gb300_fft_fit", "adda_gb300_fit_box", "adda_gb300_make_particle", "adda_gb300_rotation",
-           "adda_gb300_plane_wave", "adda_gb300_wkb_field", "adda_gb300_polarizability",
+           "adda_gb300_plane_wave", "adda_gb300_plane_wave_surf", "adda_gb300_wkb_field", "adda_gb300_polarizability",
            "adda_gb300_polarizability_dchi", "adda_gb300_polarizability_nloc",
            "adda_gb300_create", "adda_gb300_destroy",
            "adda_gb300_get_grid", "adda_gb300_init_dmatrix", "adda_gb300_dmatrix_len", "adda_gb300_get_dmatrix",
            "adda_gb300_set_cc", "adda_gb300_set_cc_sqrt", "adda_gb300_set_cc_dipole", "adda_gb300_matvec", "adda_gb300_matvec_device",
            "adda_gb300_solve", "adda_gb300_solve_device", "adda_gb300_solve_many", "adda_gb300_vjp_chi",
            "adda_gb300_chpoint_size", "adda_gb300_chpoint_save", "adda_gb300_chpoint_load",
+           "adda_gb300_rmatrix_len", "adda_gb300_get_rmatrix", "adda_gb300_cross_sections_beam",
            "adda_gb300_cross_sections", "adda_gb300_scattered_fields", "adda_gb300_integr_points",
            "adda_gb300_romberg2d", "adda_gb300_romberg2d_ex", "adda_gb300_scattering_integrals",
            "adda_gb300_cross_sections_noalloc", "adda_gb300_time_matvec",
@@ -132,6 +138,10 @@ def load_library(path):
         "adda_gb300_make_particle": ([I, P, I, I, I, P, P], SZ),
         "adda_gb300_rotation": ([P, D, D, D, P, P, P], None),
         "adda_gb300_plane_wave": ([SZ, P, I, I, I, D, D, P, P, P], None),
+        "adda_gb300_plane_wave_surf": ([SZ, P, I, I, I, D, D, P, P, P, I, D, D, D, I, P, P], I),
+        "adda_gb300_rmatrix_len": ([P], SZ),
+        "adda_gb300_get_rmatrix": ([P, P], I),
+        "adda_gb300_cross_sections_beam": ([P, I, P, D, P, P], I),
         "adda_gb300_wkb_field": ([I, I, I, SZ, P, P, I, P, D, P, P], I),
         "adda_gb300_polarizability": ([I, D, D, D, D, P, P, I, P], I),
         "adda_gb300_polarizability_dchi": ([I, D, D, D, D, P, P, I, P], I),
@@ -223,6 +233,19 @@ def plane_wave(box, pos, gridspace, wavenum, prop, pol):
     return e
 
 
+def plane_wave_surf(box, pos, gridspace, wavenum, prop, incpol_y, incpol_x, which, hsub, msub):
+    """the incident field of a particle whose centre is hsub above a substrate of index msub (None: perfectly
+    reflecting), which = 0 (Y, s-polarised) or 1 (X, p-polarised); returns (einc, inc_scale)"""
+    e = np.zeros(len(pos) * 3, np.complex128)
+    pos = np.ascontiguousarray(pos, dtype=np.uint16)
+    sc = np.zeros(1)
+    f = [_p(np.ascontiguousarray(v, float)) for v in (prop, incpol_y, incpol_x)]
+    m = complex(0 if msub is None else msub)
+    _check(lib().adda_gb300_plane_wave_surf(len(pos), _p(pos), *box, gridspace, wavenum, *f, which, hsub, m.real,
+                                            m.imag, 1 if msub is None else 0, _p(e), _p(sc)), "plane_wave_surf")
+    return e, float(sc[0])
+
+
 def polarizability(m, kd, gridspace, prop, incpol, relation="ldr", avgpol=False, rp=0.0):
     """CoupleConstant: the three diagonal components; rp is the Gaussian width of -pol nloc|nloc_av <Rp>"""
     cc = np.zeros(3, np.complex128)
@@ -283,7 +306,7 @@ class Setup:
     Order of the RHS: Y polarisation first, then X (calculator.c:309-330)."""
 
     def __init__(self, grid=16, shape="sphere", pars=None, m=1.5, dpl=None, size=None, pol="ldr", orient=(0, 0, 0),
-                 avgpol=False, prop=None, lam=2 * math.pi, interaction="poi", nloc_rp=0.0, pol_rp=0.0):
+                 avgpol=False, prop=None, lam=2 * math.pi, interaction="poi", nloc_rp=0.0, pol_rp=0.0, surface=None):
         self.interaction = interaction
         self.nloc_rp = float(nloc_rp)
         self.pol, self.avgpol, self.pol_rp, self.prop0 = pol, avgpol, pol_rp, prop
@@ -304,6 +327,19 @@ class Setup:
         self.cc = [polarizability(self.m, self.kd, self.gridspace, self.prop, e, pol, avgpol, pol_rp)
                    for e in self.incpol]
         self.einc = [plane_wave(self.box, self.pos, self.gridspace, self.wavenum, self.prop, e) for e in self.incpol]
+        # -surf h msub | -surf h inf with -int_surf img|som (table: the Sommerfeld integrals, see Context)
+        self.surface = None
+        self.inc_scale = 1.0
+        if surface is not None:
+            h, msub = float(surface["h"]), surface.get("msub")
+            rel = surface.get("relation", "img" if msub is None else "som")
+            zsum = 2 * (h / self.gridspace - (self.box[2] - 1) / 2.0)
+            self.surface = dict(zsum_shift=zsum, msub=None if msub is None else complex(msub), relation=rel,
+                                data=surface.get("table"))
+            beams = [plane_wave_surf(self.box, self.pos, self.gridspace, self.wavenum, self.prop, py, px, w, h, msub)
+                     for w in (0, 1)]
+            self.einc = [b[0] for b in beams]
+            self.inc_scale = beams[0][1]
 
 
 # ---------------------------------------------------------------------------------------------------------------------
@@ -374,7 +410,7 @@ class Context:
     """One particle lattice on one GPU: the interaction matrix, FP64/FP32 matvecs, solver and cross sections."""
 
     def __init__(self, box, pos, mat, gridspace, wavenum, grid=(0, 0, 0), nrhs_max=2, device=0, interaction="poi",
-                 nloc_rp=0.0, library=None):
+                 nloc_rp=0.0, library=None, surface=None):
         self.L = library or lib()
         self.pos = np.ascontiguousarray(pos, dtype=np.uint16).reshape(-1, 3)
         self.mat = None if mat is None else np.ascontiguousarray(mat, dtype=np.uint8)
@@ -383,6 +419,15 @@ class Context:
         pr = Problem(box[0], box[1], box[2], grid[0], grid[1], grid[2], self.n, _p(self.pos).value,
                      None if self.mat is None else _p(self.mat).value, gridspace, wavenum, nrhs_max, device,
                      INTERACTIONS[interaction], nloc_rp)
+        # surface: dict(zsum_shift, msub (None = perfect reflector), relation img|som|host, data (complex array))
+        self._refl = None
+        if surface is not None:
+            m = surface.get("msub")
+            pr.surface, pr.zsum_shift, pr.refl = 1, surface["zsum_shift"], REFL[surface.get("relation", "img")]
+            pr.msub_re, pr.msub_im, pr.msub_inf = (0.0, 0.0, 1) if m is None else (complex(m).real, complex(m).imag, 0)
+            if surface.get("data") is not None:
+                self._refl = np.ascontiguousarray(surface["data"], dtype=np.complex128)
+                pr.refl_data = _p(self._refl).value
         self.h = ctypes.c_void_p()
         _check(self.L.adda_gb300_create(ctypes.byref(pr), ctypes.byref(self.h)), "create")
         g = (ctypes.c_int * 3)()
@@ -392,7 +437,7 @@ class Context:
     @classmethod
     def from_setup(cls, s, nrhs_max=2, device=0, library=None):
         c = cls(s.box, s.pos, s.mat, s.gridspace, s.wavenum, s.grid, nrhs_max, device, s.interaction,
-                getattr(s, "nloc_rp", 0.0), library)
+                getattr(s, "nloc_rp", 0.0), library, getattr(s, "surface", None))
         c.init_dmatrix()
         for r in range(min(nrhs_max, len(s.cc))):
             c.set_cc(r, s.cc[r].reshape(1, 3))
@@ -416,6 +461,13 @@ class Context:
         n = self.L.adda_gb300_dmatrix_len(self.h)
         out = np.empty(n, np.complex128)
         _check(self.L.adda_gb300_get_dmatrix(self.h, _p(out)), "get_dmatrix")
+        return out
+
+    def rmatrix(self):
+        """surface mode: the FP64 reflected interaction matrix [x][z][y<gY/2+1][6]"""
+        n = self.L.adda_gb300_rmatrix_len(self.h)
+        out = np.empty(n, np.complex128)
+        _check(self.L.adda_gb300_get_rmatrix(self.h, _p(out)), "get_rmatrix")
         return out
 
     def set_cc(self, rhs, cc):
@@ -540,6 +592,15 @@ class Context:
         R = prop.shape[0]
         ce, ca = np.zeros(R), np.zeros(R)
         _check(self.L.adda_gb300_cross_sections(self.h, R, _p(prop), _p(inc), _p(ce), _p(ca)), "cross_sections")
+        return ce, ca
+
+    def cross_sections_beam(self, einc, inc_scale=1.0):
+        """Cext (general incident field, the surface-mode formula) and Cabs of the last solve; einc [nrhs, n*3]"""
+        e = np.ascontiguousarray(einc, dtype=np.complex128).reshape(-1, 3 * self.n)
+        R = e.shape[0]
+        ce, ca = np.zeros(R), np.zeros(R)
+        _check(self.L.adda_gb300_cross_sections_beam(self.h, R, _p(e), inc_scale, _p(ce), _p(ca)),
+               "cross_sections_beam")
         return ce, ca
 
     def scattered_fields(self, dirs, nrhs=1):

@@ -126,6 +126,28 @@ static int create_impl(const adda_gb300_problem *p, adda_gb300_ctx *c)
 	}
 	c->interaction = p->interaction;
 	c->nloc_rp = p->nloc_rp;
+	if (p->surface) {
+		if (p->refl < ADDA_REFL_IMG || p->refl > ADDA_REFL_HOST || (p->refl != ADDA_REFL_IMG && !p->refl_data) ||
+			(p->msub_inf && p->refl != ADDA_REFL_IMG && p->refl != ADDA_REFL_HOST) || !std::isfinite(p->zsum_shift)) {
+			set_error("create: surface mode needs a known reflection relation (with its data for SOM/HOST, image "
+				"relation for a perfect reflector) and a finite zsum_shift");
+			return ADDA_GB300_EINVAL;
+		}
+		c->surface = 1;
+		c->refl = p->refl;
+		c->msub_inf = p->msub_inf;
+		c->msub = make_double2(p->msub_re, p->msub_im);
+		c->zsum_shift = p->zsum_shift;
+		const size_t nk = 2 * (size_t)c->bZ - 1;
+		if (p->refl == ADDA_REFL_SOM) {
+			const size_t n = nk * c->bY * c->bX * 4;
+			c->refl_host.assign((const double2 *)p->refl_data, (const double2 *)p->refl_data + n);
+		}
+		else if (p->refl == ADDA_REFL_HOST) {
+			const size_t n = nk * c->bY * (2 * (size_t)c->bX - 1) * 6;
+			c->refl_host.assign((const double2 *)p->refl_data, (const double2 *)p->refl_data + n);
+		}
+	}
 	const int g3[3] = {c->gX, c->gY, c->gZ};
 	FftPlan *pl[3] = {c->px, c->py, c->pz};
 	for (int d = 0; d < 3; d++) {
@@ -161,6 +183,12 @@ static int create_impl(const adda_gb300_problem *p, adda_gb300_ctx *c)
 		xy[i] = (uint32_t)x | ((uint32_t)y << 16);
 	}
 	for (size_t l = 1; l < ls.size(); l++) ls[l] += ls[l - 1];
+	// the particle must lie entirely above the substrate (make_particle.c:2282): the lowest dipole layer zmin above
+	// its own image, zsum_shift + 2*zmin > 0 (positions are z-major, so the first dipole is in the lowest layer)
+	if (c->surface && N && !(c->zsum_shift + 2.0 * c->pos[2] > 0)) {
+		set_error("create: the particle must be entirely above the substrate (zsum_shift + 2*zmin > 0)");
+		return ADDA_GB300_EINVAL;
+	}
 	if (N > 0xffffffffu / 3) {
 		set_error("too many dipoles");
 		return ADDA_GB300_EINVAL;
@@ -179,6 +207,11 @@ static int create_impl(const adda_gb300_problem *p, adda_gb300_ctx *c)
 	const size_t dlen = (size_t)c->gX * c->DsZ * c->DsY * 6;
 	ADDA_CUDA(cudaMalloc(&c->D64, sizeof(double2) * dlen));
 	ADDA_CUDA(cudaMalloc(&c->D32, sizeof(float2) * dlen));
+	if (c->surface) {
+		const size_t rlen = (size_t)c->gX * c->gZ * (c->gY / 2 + 1) * 6;
+		ADDA_CUDA(cudaMalloc(&c->R64, sizeof(double2) * rlen));
+		ADDA_CUDA(cudaMalloc(&c->R32, sizeof(float2) * rlen));
+	}
 	// matvec work: Xf for Rmax RHS in FP64; the z-chunk buffer is sized to ~48 MB so that it stays in L2
 	const size_t R = c->Rmax;
 	ADDA_CUDA(cudaMalloc(&c->Xf, sizeof(double2) * R * c->gX * 3 * (size_t)c->bZ * c->bY));
@@ -200,6 +233,7 @@ static int create_impl(const adda_gb300_problem *p, adda_gb300_ctx *c)
 		: (int)std::max<size_t>(1, std::min<size_t>(c->gX, ((size_t)CHUNK_TUNE_MAX_MB << 20) / (slab * sizeof(float2))));
 	const size_t tz = std::max(c->CK64 * sizeof(double2), c->CK32max * sizeof(float2)) * slab;
 	ADDA_CUDA(cudaMalloc(&c->Tz, tz));
+	if (c->surface) ADDA_CUDA(cudaMalloc(&c->TzR, tz));
 	c->partial_len = R * matvec_partial_blocks(c, true) * 4;
 	ADDA_CUDA(cudaMalloc(&c->partial, sizeof(double) * c->partial_len));
 	ADDA_CUDA(cudaMalloc(&c->d_red, sizeof(double) * R * 4));
@@ -216,7 +250,7 @@ int adda_gb300_destroy(adda_gb300_ctx *c)
 	if (c->stream) cudaStreamSynchronize(c->stream);
 	solver_free(c);
 	void *bufs[] = {c->d_line_start, c->d_xy, c->d_mat, c->d_pos, c->D64, c->D32, c->cc64, c->ccs64, c->ccs32,
-		c->Xf, c->Tz, c->partial, c->d_red, c->vin, c->vout, c->pvec64, c->tw64[0], c->tw64[1], c->tw64[2],
+		c->Xf, c->Tz, c->TzR, c->R64, c->R32, c->partial, c->d_red, c->vin, c->vout, c->pvec64, c->tw64[0], c->tw64[1], c->tw64[2],
 		c->tw32[0], c->tw32[1], c->tw32[2]};
 	for (void *b : bufs)
 		if (b) cudaFree(b);
@@ -332,6 +366,23 @@ int adda_gb300_get_dmatrix(adda_gb300_ctx *c, double *out)
 	}
 	ADDA_CUDA(cudaSetDevice(c->device));
 	ADDA_CUDA(cudaMemcpy(out, c->D64, sizeof(double2) * adda_gb300_dmatrix_len(c), cudaMemcpyDeviceToHost));
+	return ADDA_GB300_OK;
+}
+
+size_t adda_gb300_rmatrix_len(const adda_gb300_ctx *c)
+{
+	return (c && c->surface) ? (size_t)c->gX * c->gZ * (c->gY / 2 + 1) * 6 : 0;
+}
+
+int adda_gb300_get_rmatrix(adda_gb300_ctx *c, double *out)
+{
+	if (!c || !out) return ADDA_GB300_EINVAL;
+	if (!c->surface || !c->dready) {
+		set_error("R matrix not initialised (no substrate, or adda_gb300_init_dmatrix not called)");
+		return ADDA_GB300_ESTATE;
+	}
+	ADDA_CUDA(cudaSetDevice(c->device));
+	ADDA_CUDA(cudaMemcpy(out, c->R64, sizeof(double2) * adda_gb300_rmatrix_len(c), cudaMemcpyDeviceToHost));
 	return ADDA_GB300_OK;
 }
 
@@ -689,6 +740,17 @@ int adda_gb300_cross_sections(adda_gb300_ctx *c, int nrhs, const double *prop, c
 	}
 	ADDA_CUDA(cudaSetDevice(c->device));
 	return cross_sections(c, nrhs, prop, incpol, cext, cabs);
+}
+
+int adda_gb300_cross_sections_beam(adda_gb300_ctx *c, int nrhs, const double *einc, double inc_scale, double *cext,
+	double *cabs)
+{
+	if (!c || !einc || nrhs < 1 || nrhs > c->last_nrhs || !c->pvec64 || !(inc_scale > 0)) {
+		set_error("cross_sections_beam: no solution available for that many RHS, or invalid arguments");
+		return ADDA_GB300_ESTATE;
+	}
+	ADDA_CUDA(cudaSetDevice(c->device));
+	return cross_sections_beam(c, nrhs, einc, inc_scale, cext, cabs);
 }
 
 int adda_gb300_scattering_integrals(adda_gb300_ctx *c, int nrhs, const adda_gb300_integr_parms p[2],

@@ -60,6 +60,13 @@ struct adda_gb300_ctx {
 	int Rmax = 1;
 	int interaction = 0; // enum adda_gb300_inter
 	double nloc_rp = 0;  // Gaussian width of the non-local interaction
+	// particle near a substrate: reflected interaction R~, layout [gX][gZ][gY/2+1][6]
+	int surface = 0, refl = 0, msub_inf = 0;
+	double zsum_shift = 0;
+	double2 msub = {0, 0};
+	std::vector<double2> refl_host;   // SOM table or HOST tensor (see enum adda_gb300_refl)
+	double2 *R64 = nullptr;
+	float2 *R32 = nullptr;
 	double gridspace = 0, k = 0;
 	// lattice (host and device)
 	std::vector<uint16_t> pos;
@@ -84,6 +91,7 @@ struct adda_gb300_ctx {
 	// matvec work
 	void *Xf = nullptr;               // [R][gX][3][bZ][bY] after the X transform
 	void *Tz = nullptr;               // [R][CK][3][gZ][bY] chunk of x-slabs after the Z transform
+	void *TzR = nullptr;              // surface: the same chunk transformed along z with the inverse sign
 	int CK64 = 1, CK32 = 1;           // x-slabs per chunk (sized to stay resident in L2)
 	int CK32max = 1;                  // largest FP32 chunk the Tz buffer holds
 	bool chunk_fixed = false;         // chunk size set by the environment: no tuning
@@ -124,6 +132,8 @@ int solver_solve_dev(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int n
 	double2 *d_xvec, double2 *d_pvec, adda_gb300_rhs_stats *stats);
 void solver_free(adda_gb300_ctx *c);
 int cross_sections(adda_gb300_ctx *c, int nrhs, const double *prop, const double *incpol, double *cext, double *cabs);
+int cross_sections_beam(adda_gb300_ctx *c, int nrhs, const double *einc, double inc_scale, double *cext,
+	double *cabs);
 size_t solver_chpoint_size(const adda_gb300_ctx *c, int method);
 int solver_chpoint_save(adda_gb300_ctx *c, int rhs, void *buf, size_t size);
 int solver_chpoint_load(adda_gb300_ctx *c, int rhs, const void *buf, size_t size);

@@ -9,6 +9,10 @@
 //                        fft_lines along z then y, and d_extract keeps y<=gY/2, z<=gZ/2 scaled by -1/Ngrid into the
 //                        reduced layout [x][z][y][6] (fft.c:144-150, 1310-1314)
 //   4. an FP32 copy for the single-precision matvec.
+//   5. surface mode (InitRmatrix, src/fft.c:818-887): refl_fill evaluates the reflected tensor for every in-plane
+//      offset and height sum k in [0, 2bZ-1) (image dipole on the GPU, plus the Sommerfeld integrals of a host table,
+//      or the caller's own tensor), the same x/z/y transforms follow with the y mirror only (heights are not
+//      mirrored), and r_extract keeps y <= gY/2 and every z: R = -FFT(GR)/Ngrid in [x][z][y][6].
 // This runs once per particle; it is written for clarity over speed (it costs a few FP64 3-D FFTs).
 #include "ctx.cuh"
 
@@ -263,6 +267,113 @@ __global__ void d_extract(double2 *D, const double2 *S, int a, int gX, int gY, i
 	}
 }
 
+// reflected Green's tensor of offset (i, j) and height sum k (lattice units, the probe minus the image of the source):
+// ReflParams + ReflTerm_core (interaction.c:1092-1134: the point-dipole term scaled by the normal-incidence reflection
+// coefficient rcn, z components inverted), for SOM plus CombineSomTensor of the table's four integrals at
+// rho = |(i,j)| (interaction.c:1229-1301); HOST copies the caller's tensor. Stored per component as [k][j][i mod gX].
+__global__ void refl_fill(double2 *G, int bX, int bY, int bZ, int gX, double gridspace, double k, double zshift,
+	double2 rcn, int refl, const double2 *data)
+{
+	const int nk = 2 * bZ - 1;
+	const size_t total = (size_t)nk * bY * gX;
+	for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+		const int x = (int)(t % gX);
+		const size_t l = t / gX;
+		const int j = (int)(l % bY), kk = (int)(l / bY);
+		double2 g[6];
+		for (int a = 0; a < 6; a++) g[a] = make_double2(0, 0);
+		const bool inside = x < bX || x > gX - bX;
+		const int i = x < bX ? x : x - gX;
+		if (inside && refl == ADDA_REFL_HOST) {
+			const double2 *v = data + (((size_t)kk * bY + j) * (2 * bX - 1) + (i + bX - 1)) * 6;
+			for (int a = 0; a < 6; a++) g[a] = v[a];
+		}
+		else if (inside && !(i == 0 && j == 0 && kk + zshift == 0)) {
+			// (the zero distance itself is left 0: no pair of dipoles above the substrate has that height sum)
+			const double q0 = i, q1 = j, q2 = kk + zshift;
+			double rr = sqrt(q0 * q0 + q1 * q1 + q2 * q2);
+			const double inv = 1 / rr, v0 = q0 * inv, v1 = q1 * inv, v2 = q2 * inv;
+			const double qm[6] = {v0 * v0, v0 * v1, v0 * v2, v1 * v1, v1 * v2, v2 * v2};
+			rr *= gridspace;
+			const double invr3 = 1 / (rr * rr * rr), kr = k * rr, kr2 = kr * kr;
+			const double t1 = 3 - kr2, t2 = -3 * kr, t3 = kr2 - 1;
+			double sn, cs;
+			sincos(kr, &sn, &cs);
+			const double2 sc = make_double2(invr3 * (rcn.x * cs - rcn.y * sn), invr3 * (rcn.x * sn + rcn.y * cs));
+			for (int a = 0; a < 6; a++) {
+				double re, im;
+				if (a == 0 || a == 3 || a == 5) {
+					re = t1 * qm[a] + t3;
+					im = kr + t2 * qm[a];
+				}
+				else {
+					re = t1 * qm[a];
+					im = t2 * qm[a];
+				}
+				g[a] = make_double2(re * sc.x - im * sc.y, re * sc.y + im * sc.x);
+			}
+			g[2] = make_double2(-g[2].x, -g[2].y);
+			g[4] = make_double2(-g[4].x, -g[4].y);
+			g[5] = make_double2(-g[5].x, -g[5].y);
+			if (refl == ADDA_REFL_SOM) {
+				const double2 *v = data + (((size_t)kk * bY + j) * bX + (i < 0 ? -i : i)) * 4;
+				const double2 Irv = v[0], Izv = v[1], Irh = v[2], Iph = v[3];
+				const double rho = hypot((double)i, (double)j);
+				if (rho == 0) {
+					g[0] = make_double2(g[0].x + Irh.x, g[0].y + Irh.y);
+					g[3] = make_double2(g[3].x + Irh.x, g[3].y + Irh.y);
+				}
+				else {
+					const double xr = i / rho, yr = j / rho;
+					const double a2 = xr * xr, b2 = yr * yr, ab = xr * yr;
+					g[0] = make_double2(g[0].x + a2 * Irh.x - b2 * Iph.x, g[0].y + a2 * Irh.y - b2 * Iph.y);
+					g[1] = make_double2(g[1].x + ab * (Irh.x + Iph.x), g[1].y + ab * (Irh.y + Iph.y));
+					g[2] = make_double2(g[2].x + xr * Irv.x, g[2].y + xr * Irv.y);
+					g[3] = make_double2(g[3].x + b2 * Irh.x - a2 * Iph.x, g[3].y + b2 * Irh.y - a2 * Iph.y);
+					g[4] = make_double2(g[4].x + yr * Irv.x, g[4].y + yr * Irv.y);
+				}
+				g[5] = make_double2(g[5].x + Izv.x, g[5].y + Izv.y);
+			}
+		}
+		for (int a = 0; a < 6; a++) G[(size_t)a * total + t] = g[a];
+	}
+}
+
+// the (j, k) half-plane of one reflected component into the full (y, z) plane of every kx: y mirrored with the
+// component's parity (xy and yz odd in y, fft.c:859-865), heights k < nk at z = k, zero elsewhere
+__global__ void slice_fill_r(double2 *S, const double2 *Ga, int bY, int nk, int gX, int gY, int gZ, double sy)
+{
+	const size_t total = (size_t)gX * gY * gZ;
+	for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+		const int z = (int)(t % gZ);
+		const size_t xy = t / gZ;
+		const int y = (int)(xy % gY), x = (int)(xy / gY);
+		int j;
+		double s = 1;
+		if (y < bY) j = y;
+		else if (y > gY - bY) { j = gY - y; s = sy; }
+		else j = -1;
+		double2 v = make_double2(0, 0);
+		if (j >= 0 && z < nk) {
+			const double2 g = Ga[((size_t)z * bY + j) * gX + x];
+			v = make_double2(s * g.x, s * g.y);
+		}
+		S[t] = v;
+	}
+}
+
+__global__ void r_extract(double2 *Rm, const double2 *S, int a, int gX, int gY, int gZ, int RsY, double invN)
+{
+	const size_t total = (size_t)gX * gZ * RsY;
+	for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+		const int y = (int)(t % RsY);
+		const size_t xz = t / RsY;
+		const int z = (int)(xz % gZ), x = (int)(xz / gZ);
+		const double2 v = S[((size_t)x * gY + y) * gZ + z];
+		Rm[t * 6 + a] = make_double2(-invN * v.x, -invN * v.y);
+	}
+}
+
 __global__ void to_f32(float2 *dst, const double2 *src, size_t n)
 {
 	for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
@@ -289,6 +400,65 @@ int fft_lines_run(adda_gb300_ctx *c, double2 *data, const FftPlan &p, const doub
 	fft_lines<double2><<<g, 256, smem, c->stream>>>(data, p, tw, inv ? 1 : 0, es, ls, nl_inner, od, TL);
 	ADDA_LAUNCHED();
 	return ADDA_GB300_OK;
+}
+
+int rmatrix_build(adda_gb300_ctx *c)
+{
+	const int bX = c->bX, bY = c->bY, bZ = c->bZ, gX = c->gX, gY = c->gY, gZ = c->gZ;
+	const int nk = 2 * bZ - 1, RsY = gY / 2 + 1;
+	const size_t lines = (size_t)nk * bY;
+	const size_t gsz = lines * gX;
+	const size_t ssz = (size_t)gX * gY * gZ;
+	const size_t rlen = (size_t)gX * gZ * RsY * 6;
+	double2 *G = nullptr, *S = nullptr, *data = nullptr;
+	int rc = ADDA_GB300_OK;
+	if (cudaMalloc(&G, sizeof(double2) * 6 * gsz) != cudaSuccess ||
+		cudaMalloc(&S, sizeof(double2) * ssz) != cudaSuccess ||
+		(!c->refl_host.empty() && cudaMalloc(&data, sizeof(double2) * c->refl_host.size()) != cudaSuccess)) {
+		cudaFree(G);
+		cudaFree(S);
+		set_error("cannot allocate the R-matrix build buffers");
+		return ADDA_GB300_ENOMEM;
+	}
+	// surfRCn, interaction.c:1411
+	double2 rcn = make_double2(-1, 0);
+	if (!c->msub_inf) {
+		const double mr = c->msub.x, mi = c->msub.y;
+		const double m2r = mr * mr - mi * mi, m2i = 2 * mr * mi;
+		const double nr = 1 - m2r, ni = -m2i, dr = 1 + m2r, di = m2i, dd = dr * dr + di * di;
+		rcn = make_double2((nr * dr + ni * di) / dd, (ni * dr - nr * di) / dd);
+	}
+	const double invN = 1.0 / (gX * ((double)gY * gZ));
+	do {
+		if (data && cudaMemcpyAsync(data, c->refl_host.data(), sizeof(double2) * c->refl_host.size(),
+				cudaMemcpyHostToDevice, c->stream) != cudaSuccess) { rc = ADDA_GB300_ECUDA; break; }
+		refl_fill<<<grid_for(gsz), 256, 0, c->stream>>>(G, bX, bY, bZ, gX, c->gridspace, c->k, c->zsum_shift, rcn,
+			c->refl, data);
+		count_launch();
+		if (cudaGetLastError() != cudaSuccess) { rc = ADDA_GB300_ECUDA; break; }
+		if ((rc = fft_lines_run(c, G, c->px[0], c->tw64[0], false, 1, gX, (int)(6 * lines), 0, 1))) break;
+		for (int a = 0; a < 6 && !rc; a++) {
+			const double sy = (a == 1 || a == 4) ? -1 : 1;
+			slice_fill_r<<<grid_for(ssz), 256, 0, c->stream>>>(S, G + (size_t)a * gsz, bY, nk, gX, gY, gZ, sy);
+			count_launch();
+			if (cudaGetLastError() != cudaSuccess) { rc = ADDA_GB300_ECUDA; break; }
+			if ((rc = fft_lines_run(c, S, c->pz[0], c->tw64[2], false, 1, gZ, gX * gY, 0, 1))) break;
+			if ((rc = fft_lines_run(c, S, c->py[0], c->tw64[1], false, gZ, 1, gZ, (size_t)gY * gZ, gX))) break;
+			r_extract<<<grid_for((size_t)gX * gZ * RsY), 256, 0, c->stream>>>(c->R64, S, a, gX, gY, gZ, RsY, invN);
+			count_launch();
+			if (cudaGetLastError() != cudaSuccess) { rc = ADDA_GB300_ECUDA; break; }
+		}
+		if (rc) break;
+		to_f32<<<grid_for(rlen), 256, 0, c->stream>>>(c->R32, c->R64, rlen);
+		count_launch();
+		if (cudaGetLastError() != cudaSuccess) { rc = ADDA_GB300_ECUDA; break; }
+		if (cudaStreamSynchronize(c->stream) != cudaSuccess) { rc = ADDA_GB300_ECUDA; break; }
+	} while (0);
+	if (rc == ADDA_GB300_ECUDA) set_error(std::string("R-matrix build: ") + cudaGetErrorString(cudaGetLastError()));
+	cudaFree(G);
+	cudaFree(S);
+	cudaFree(data);
+	return rc;
 }
 
 } // namespace
@@ -339,6 +509,7 @@ int dmatrix_build(adda_gb300_ctx *c)
 	if (rc == ADDA_GB300_ECUDA) set_error(std::string("D-matrix build: ") + cudaGetErrorString(cudaGetLastError()));
 	cudaFree(G);
 	cudaFree(S);
+	if (!rc && c->surface) rc = rmatrix_build(c);
 	if (!rc) c->dready = true;
 	return rc;
 }

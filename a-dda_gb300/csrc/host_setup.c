@@ -6,6 +6,7 @@
  *   adda_gb300_make_particle    <- MakeParticle box loop                    src/make_particle.c:1984-2230
  *   adda_gb300_rotation         <- InitRotation (zyz Euler angles)          src/crosssec.c:82-139
  *   adda_gb300_plane_wave       <- GenerateB, free-space plane wave         src/GenerateB.c:324-328
+ *   adda_gb300_plane_wave_surf  <- GenerateB, plane wave near a substrate   src/GenerateB.c:96-140, 257-323
  *   adda_gb300_polarizability   <- CoupleConstant (CM, LDR, RRC, DGF)        src/calculator.c:100-262
  * All functions are pure host code: no GPU is touched.
  */
@@ -134,6 +135,99 @@ void adda_gb300_plane_wave(size_t ndip, const uint16_t *position, int boxX, int 
 			einc[6 * i + 2 * a + 1] = s * pol[a];
 		}
 	}
+}
+
+/* normal component of the transmitted wavevector with the branch cut on the negative real axis handled explicitly
+ * (cSqrtCut, src/cmplx.h:58-80) */
+static double complex sqrt_cut(double complex a)
+{
+	if (cimag(a) == 0) return creal(a) >= 0 ? sqrt(creal(a)) : I * sqrt(-creal(a));
+	return csqrt(a);
+}
+
+int adda_gb300_plane_wave_surf(size_t ndip, const uint16_t *position, int boxX, int boxY, int boxZ,
+	double gridspace, double wavenum, const double prop[3], const double incPolY[3], const double incPolX[3],
+	int which, double hsub, double msub_re, double msub_im, int msub_inf, double *einc, double *inc_scale)
+{
+	const double round_err = 1e-15, sqrt_rnd_err = 3e-8; // const.h:337-338
+	if (prop[2] == 0 || (msub_inf && prop[2] > 0) || (which != 0 && which != 1)) return ADDA_GB300_EINVAL;
+	const double complex msub = msub_re + I * msub_im;
+	const double cX = (boxX - 1) / 2.0, cY = (boxY - 1) / 2.0, cZ = (boxZ - 1) / 2.0;
+	const double k = wavenum;
+	// beam frame: ex = the incident polarisation, ey completes it (GenerateB.c:245-252)
+	double ex[3], ey[3];
+	for (int a = 0; a < 3; a++) {
+		ex[a] = which == 0 ? incPolY[a] : incPolX[a];
+		ey[a] = which == 0 ? -incPolX[a] : incPolY[a];
+	}
+	const double tr2 = prop[0] * prop[0] + prop[1] * prop[1];
+	double complex eRefl[3], eTran[3], ktVec[3] = {0, 0, 0}, ki, kt = 0;
+	if (prop[2] > 0) { // from the substrate (below): only the transmitted wave reaches the particle
+		*inc_scale = 1 / msub_re;
+		ki = msub * prop[2];
+		kt = (cabs(msub - 1) < round_err && cabs(ki) < sqrt_rnd_err) ? ki : sqrt_cut(1 - msub * msub * tr2);
+		ktVec[0] = msub * prop[0];
+		ktVec[1] = msub * prop[1];
+		ktVec[2] = kt;
+		double complex tc;
+		if (which == 0) { // s-polarised: FresnelTS
+			for (int a = 0; a < 3; a++) eTran[a] = ex[a];
+			tc = 2 * ki / (ki + kt);
+		}
+		else { // p-polarised: eTran = ey x ktVec, FresnelTP with mr = 1/msub
+			eTran[0] = ey[1] * ktVec[2] - ey[2] * ktVec[1];
+			eTran[1] = ey[2] * ktVec[0] - ey[0] * ktVec[2];
+			eTran[2] = ey[0] * ktVec[1] - ey[1] * ktVec[0];
+			const double complex mr = 1 / msub;
+			tc = 2 * mr * ki / (mr * mr * ki + kt);
+		}
+		const double complex f = tc * cexp(I * k * (kt - ki) * hsub);
+		for (int a = 0; a < 3; a++) eTran[a] *= f;
+		for (size_t i = 0; i < ndip; i++) {
+			const double r[3] = {(position[3 * i] - cX) * gridspace, (position[3 * i + 1] - cY) * gridspace,
+				(position[3 * i + 2] - cZ) * gridspace};
+			const double complex ph = cexp(I * k * (ktVec[0] * r[0] + ktVec[1] * r[1] + ktVec[2] * r[2]));
+			for (int a = 0; a < 3; a++) {
+				const double complex v = ph * eTran[a];
+				einc[6 * i + 2 * a] = creal(v);
+				einc[6 * i + 2 * a + 1] = cimag(v);
+			}
+		}
+		return ADDA_GB300_OK;
+	}
+	// from above: the incident wave plus the wave reflected by the substrate
+	*inc_scale = 1;
+	const double prRefl[3] = {prop[0], prop[1], -prop[2]};
+	ki = -prop[2];
+	if (!msub_inf) kt = (cabs(msub - 1) < round_err && fabs(creal(ki)) < sqrt_rnd_err) ? ki
+		: sqrt_cut(msub * msub - tr2);
+	double complex rc;
+	if (which == 0) { // s-polarised: FresnelRS
+		for (int a = 0; a < 3; a++) eRefl[a] = ex[a];
+		rc = msub_inf ? -1 : (ki - kt) / (ki + kt);
+	}
+	else { // p-polarised: ex reflected about the z axis, FresnelRP with mr = msub
+		eRefl[0] = -ex[0];
+		eRefl[1] = -ex[1];
+		eRefl[2] = ex[2];
+		rc = msub_inf ? 1 : (msub * msub * ki - kt) / (msub * msub * ki + kt);
+	}
+	const double ph2 = 2 * k * creal(ki) * hsub;
+	const double complex f = rc * (cos(ph2) + I * sin(ph2));
+	for (int a = 0; a < 3; a++) eRefl[a] *= f;
+	for (size_t i = 0; i < ndip; i++) {
+		const double r[3] = {(position[3 * i] - cX) * gridspace, (position[3 * i + 1] - cY) * gridspace,
+			(position[3 * i + 2] - cZ) * gridspace};
+		const double p1 = k * (r[0] * prop[0] + r[1] * prop[1] + r[2] * prop[2]);
+		const double p2 = k * (r[0] * prRefl[0] + r[1] * prRefl[1] + r[2] * prRefl[2]);
+		const double complex e1 = cos(p1) + I * sin(p1), e2 = cos(p2) + I * sin(p2);
+		for (int a = 0; a < 3; a++) {
+			const double complex v = e1 * ex[a] + e2 * eRefl[a];
+			einc[6 * i + 2 * a] = creal(v);
+			einc[6 * i + 2 * a + 1] = cimag(v);
+		}
+	}
+	return ADDA_GB300_OK;
 }
 
 /* polCM, polM, polMplusRR, pol3coef: src/calculator.c:100-132 */

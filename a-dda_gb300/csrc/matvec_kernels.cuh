@@ -54,6 +54,11 @@ template <typename T, typename V> struct MvP {
 	int her;
 	int KB, RG;      // K2b: kz per block, RHS per block (KB*RG <= Tiles<T>::PAIRS)
 	const int *done; // per-RHS done flags (may be null): every kernel returns at once when all are set
+	// particle near a substrate: the slab transformed along z with the opposite sign (height sums) and the
+	// reflected interaction matrix R~, layout [gX][gZ][RsY][6] (fft.c:196-201)
+	C *TzR;
+	const C *Rm;
+	int RsY;
 };
 
 template <typename To, typename From> __device__ __forceinline__ To cvt(From a) { return from_d2<To>(to_d2(a)); }
@@ -138,11 +143,14 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T,
 	}
 }
 
-// K2a/K2c: FFT along z of W consecutive y-lines of one (rhs, kx, comp). Forward reads Xf (z<bZ, zero padded) and
-// writes Tz (all kz); inverse reads Tz and writes z<bZ back to Xf.
-template <typename T, typename V, int W, bool INV, int NS>
+// K2a/K2c: FFT along z of W consecutive y-lines of one (rhs, kx, comp). MODE 0 (forward) reads Xf (z<bZ, zero
+// padded) and writes Tz (all kz); MODE 1 (inverse) reads Tz and writes z<bZ back to Xf; MODE 2 (surface) reads Xf
+// like MODE 0 but transforms with the inverse sign into TzR, so that the product with R~ sums heights instead of
+// differences (planZRf, fft.c:396-403, matvec.c:249).
+template <typename T, typename V, int W, int MODE, int NS>
 __global__ void __launch_bounds__(col_threads<T, NS, W>(), (col_minblocks<T, NS, W>())) mv_fftz(MvP<T, V> p)
 {
+	constexpr bool INV = MODE == 1, SGN = MODE != 0;
 	typedef typename CxT<T>::type C;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	if (all_done(p)) return;
@@ -158,7 +166,7 @@ __global__ void __launch_bounds__(col_threads<T, NS, W>(), (col_minblocks<T, NS,
 	const int wy = min(W, p.bY - y0);
 	const size_t plane = (size_t)p.bZ * p.bY;
 	C *xf = p.Xf + (((size_t)r * p.gX + kx) * 3 + comp) * plane + y0;
-	C *tz = p.Tz + (((size_t)r * p.CK + kxl) * 3 + comp) * (size_t)n * p.bY + y0;
+	C *tz = (MODE == 2 ? p.TzR : p.Tz) + (((size_t)r * p.CK + kxl) * 3 + comp) * (size_t)n * p.bY + y0;
 	// NT is a multiple of W: each thread keeps one y-line and walks z with a constant stride
 	constexpr int ZS = NT / W;
 	const int yy = threadIdx.x % W, z0 = threadIdx.x / W;
@@ -177,8 +185,8 @@ __global__ void __launch_bounds__(col_threads<T, NS, W>(), (col_minblocks<T, NS,
 	cp_async_wait<0>();
 	__syncthreads();
 	C *o = a;
-	if constexpr (RC) tile_cols_fft<C, NS, W, LS, NT, INV>(a, p.twz);
-	else o = tile_fft<C, NS, W, LS, INV>(a, b, p.pz, p.twz);
+	if constexpr (RC) tile_cols_fft<C, NS, W, LS, NT, SGN>(a, p.twz);
+	else o = tile_fft<C, NS, W, LS, SGN>(a, b, p.pz, p.twz);
 	const int zmax = INV ? p.bZ : n;
 	if (yok) {
 		C *dst = (INV ? xf : tz) + (size_t)z0 * p.bY + yy;
@@ -253,6 +261,87 @@ template <typename T, typename V, int NS> __global__ void __launch_bounds__(256)
 		const int kz = kz0 + kk;
 		if (!(kk < KB && rg0 + rr < p.R && kz < p.gZ)) continue;
 		C *dst = p.Tz + (((size_t)(rg0 + rr) * p.CK + kxl) * 3 + comp) * lz + (size_t)kz * p.bY;
+		for (int y = lane; y < p.bY; y += 32) dst[y] = o2[y * LS + l];
+	}
+}
+
+// K2b for a particle near a substrate (matvec.c:255-305): per (kx, KB kz, RG RHS) with KB*RG <= PAIRS/2, six lines
+// per pair: the 3 components of Tz and of TzR. All are transformed along y; then yv = D~.xv + R~.xvR with D's
+// reduced-FFT signs and R's (reduced in y only: xy and yz change sign for ky > gY/2) and R's product
+// M21 = M12, M31 = -M13, M32 = -M23 (cReflMatrVec, cmplx.h:391-401); the result goes back through the inverse y
+// transform into Tz. Line l = pair*6 + c6, c6 < 3 from Tz, c6 >= 3 from TzR.
+template <typename T, typename V, int NS> __global__ void __launch_bounds__(256) mv_fft_y_surf(MvP<T, V> p)
+{
+	typedef typename CxT<T>::type C;
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	if (all_done(p)) return;
+	constexpr int NL = 3 * Tiles<T>::PAIRS, LS = tile_ls(NL);
+	const int n = NS ? NS : p.gY;
+	C *a = reinterpret_cast<C *>(smem_raw);
+	C *b = a + (size_t)n * LS;
+	const int KB = p.KB, RG = p.RG;
+	const int rg0 = blockIdx.z * RG;
+	const int kxl = blockIdx.y, kx = p.kx0 + kxl;
+	const int kz0 = blockIdx.x * KB;
+	const size_t lz = (size_t)p.gZ * p.bY;
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	for (int l = warp; l < NL; l += 8) {
+		const int pair = l / 6, c6 = l - 6 * pair, comp = c6 % 3;
+		const int kk = pair / RG, rr = pair - kk * RG;
+		const int kz = kz0 + kk;
+		const bool ok = kk < KB && rg0 + rr < p.R && kz < p.gZ;
+		const C *src = (c6 < 3 ? p.Tz : p.TzR) + (((size_t)(rg0 + rr) * p.CK + kxl) * 3 + comp) * lz +
+			(size_t)kz * p.bY;
+#pragma unroll 4
+		for (int y = lane; y < n; y += 32) a[y * LS + l] = (ok && y < p.bY) ? src[y] : cx<C>(0, 0);
+	}
+	__syncthreads();
+	C *o = tile_fft<C, NS, NL, LS, false>(a, b, p.py, p.twy);
+	C *s = (o == a) ? b : a;
+	for (int t = threadIdx.x; t < KB * n; t += 256) {
+		const int ky = t % n, kk = t / n;
+		const int kz = kz0 + kk;
+		if (kz >= p.gZ) continue;
+		const bool ry = ky >= p.DsY, rz = kz >= p.DsZ;
+		const int yy = ry ? p.gY - ky : ky, zz = rz ? p.gZ - kz : kz;
+		const C *f = p.D + (((size_t)kx * p.DsZ + zz) * p.DsY + yy) * 6;
+		C m0 = f[0], m1 = f[1], m2 = f[2], m3 = f[3], m4 = f[4], m5 = f[5];
+		if (ry) {
+			m1 = cneg(m1);
+			if (rz) m2 = cneg(m2);
+			else m4 = cneg(m4);
+		}
+		else if (rz) {
+			m2 = cneg(m2);
+			m4 = cneg(m4);
+		}
+		const bool qy = ky >= p.RsY;
+		const C *g = p.Rm + (((size_t)kx * p.gZ + kz) * p.RsY + (qy ? p.gY - ky : ky)) * 6;
+		C q0 = g[0], q1 = g[1], q2 = g[2], q3 = g[3], q4 = g[4], q5 = g[5];
+		if (qy) {
+			q1 = cneg(q1);
+			q4 = cneg(q4);
+		}
+		const int rgn = min(RG, p.R - rg0);
+		for (int rr = 0; rr < rgn; rr++) {
+			C *row = o + ky * LS + (kk * RG + rr) * 6;
+			const C v0 = row[0], v1 = row[1], v2 = row[2], u0 = row[3], u1 = row[4], u2 = row[5];
+			const C w0 = cfma(q0, u0, cfma(q1, u1, cmul(q2, u2)));
+			const C w1 = cfma(q1, u0, cfma(q3, u1, cmul(q4, u2)));
+			const C w2 = cfma(q5, u2, cneg(cfma(q2, u0, cmul(q4, u1))));
+			row[0] = cadd(w0, cfma(m0, v0, cfma(m1, v1, cmul(m2, v2))));
+			row[1] = cadd(w1, cfma(m1, v0, cfma(m3, v1, cmul(m4, v2))));
+			row[2] = cadd(w2, cfma(m2, v0, cfma(m4, v1, cmul(m5, v2))));
+		}
+	}
+	__syncthreads();
+	C *o2 = tile_fft<C, NS, NL, LS, true>(o, s, p.py, p.twy);
+	for (int l = warp; l < NL; l += 8) {
+		const int pair = l / 6, c6 = l - 6 * pair;
+		const int kk = pair / RG, rr = pair - kk * RG;
+		const int kz = kz0 + kk;
+		if (c6 >= 3 || !(kk < KB && rg0 + rr < p.R && kz < p.gZ)) continue;
+		C *dst = p.Tz + (((size_t)(rg0 + rr) * p.CK + kxl) * 3 + c6) * lz + (size_t)kz * p.bY;
 		for (int y = lane; y < p.bY; y += 32) dst[y] = o2[y * LS + l];
 	}
 }
@@ -485,9 +574,11 @@ template <typename T, typename V> int set_attrs_tv()
 #define ADDA_SET_ALL(NS)                                                                                            \
 	ADDA_SET((mv_scatter_fftx<T, V, W1, NS>));                                                                      \
 	ADDA_SET((mv_fftx_gather<T, V, W1, NS>));                                                                       \
-	ADDA_SET((mv_fftz<T, V, W2, false, NS>));                                                                       \
-	ADDA_SET((mv_fftz<T, V, W2, true, NS>));                                                                        \
-	ADDA_SET((mv_fft_y_dmul<T, V, NS>))
+	ADDA_SET((mv_fftz<T, V, W2, 0, NS>));                                                                           \
+	ADDA_SET((mv_fftz<T, V, W2, 1, NS>));                                                                           \
+	ADDA_SET((mv_fftz<T, V, W2, 2, NS>));                                                                           \
+	ADDA_SET((mv_fft_y_dmul<T, V, NS>));                                                                            \
+	ADDA_SET((mv_fft_y_surf<T, V, NS>))
 	if constexpr (sizeof(T) == 4) {
 		ADDA_SET((mv_fft_y_reg<V, 64, 128>));
 		ADDA_SET((mv_fft_y_reg<V, 128, 128>));
@@ -537,6 +628,10 @@ int launch_matvec(adda_gb300_ctx *c, int R, const V *arg, V *res, int her, const
 	p.kx0 = 0;
 	p.RG = std::min(R, Tiles<T>::PAIRS);
 	p.KB = std::max(1, Tiles<T>::PAIRS / p.RG);
+	const bool surf = c->surface;
+	p.TzR = (C *)c->TzR;
+	p.Rm = dbl ? (const C *)c->R64 : (const C *)c->R32;
+	p.RsY = c->gY / 2 + 1;
 	cudaStream_t st = c->stream;
 	const dim3 blk(256);
 	const dim3 g1((c->bY + W1 - 1) / W1, c->bZ, R);
@@ -547,9 +642,18 @@ int launch_matvec(adda_gb300_ctx *c, int R, const V *arg, V *res, int her, const
 		p.kx0 = kx0;
 		const int ck = std::min(p.CK, c->gX - kx0);
 		const dim3 g2((c->bY + W2 - 1) / W2, 3 * ck, R);
-		ADDA_NS_SWITCH(c->gZ, (mv_fftz<T, V, W2, false, NS><<<g2, col_threads<T, NS, W2>(), smem_k2s<T, NS>(c->gZ), st>>>(p)));
+		ADDA_NS_SWITCH(c->gZ, (mv_fftz<T, V, W2, 0, NS><<<g2, col_threads<T, NS, W2>(), smem_k2s<T, NS>(c->gZ), st>>>(p)));
 		ADDA_LAUNCHED();
-		if (use_k2b_reg<T>(c->gY)) {
+		if (surf) {
+			ADDA_NS_SWITCH(c->gZ, (mv_fftz<T, V, W2, 2, NS><<<g2, col_threads<T, NS, W2>(), smem_k2s<T, NS>(c->gZ), st>>>(p)));
+			ADDA_LAUNCHED();
+			MvP<T, V> q = p;
+			q.RG = std::min(R, Tiles<T>::PAIRS / 2);
+			q.KB = std::max(1, Tiles<T>::PAIRS / 2 / q.RG);
+			const dim3 g2b((c->gZ + q.KB - 1) / q.KB, ck, (R + q.RG - 1) / q.RG);
+			ADDA_NS_SWITCH(c->gY, (mv_fft_y_surf<T, V, NS><<<g2b, blk, smem_k2b<T>(c->gY), st>>>(q)));
+		}
+		else if (use_k2b_reg<T>(c->gY)) {
 			if constexpr (sizeof(T) == 4) {
 				constexpr int NT = 128;
 				switch (c->gY) {
@@ -571,7 +675,7 @@ int launch_matvec(adda_gb300_ctx *c, int R, const V *arg, V *res, int her, const
 			ADDA_NS_SWITCH(c->gY, (mv_fft_y_dmul<T, V, NS><<<g2b, blk, smem_k2b<T>(c->gY), st>>>(p)));
 		}
 		ADDA_LAUNCHED();
-		ADDA_NS_SWITCH(c->gZ, (mv_fftz<T, V, W2, true, NS><<<g2, col_threads<T, NS, W2>(), smem_k2s<T, NS>(c->gZ), st>>>(p)));
+		ADDA_NS_SWITCH(c->gZ, (mv_fftz<T, V, W2, 1, NS><<<g2, col_threads<T, NS, W2>(), smem_k2s<T, NS>(c->gZ), st>>>(p)));
 		ADDA_LAUNCHED();
 	}
 	ADDA_NS_SWITCH(c->gX, (mv_fftx_gather<T, V, W1, NS>

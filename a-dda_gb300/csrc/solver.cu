@@ -1310,6 +1310,41 @@ __global__ void __launch_bounds__(NT) k_cross(const double2 *P, const uint16_t *
 	}
 }
 
+// general-beam cross-section sums per RHS: sum_j Im(P_j . conj(Einc_j)) (ExtCross, crosssec.c:823-830) and the AbsCross
+// sum of k_cross
+__global__ void __launch_bounds__(NT) k_cross_beam(const double2 *P, const double2 *E, const double2 *cc, int per_dip,
+	int nmat, const uint8_t *mat, size_t N, double k3, double *part, int nbv)
+{
+	const int r = blockIdx.y;
+	double s[2] = {0, 0};
+	for (size_t d = blockIdx.x * (size_t)blockDim.x + threadIdx.x; d < N; d += (size_t)gridDim.x * blockDim.x) {
+		for (int c = 0; c < 3; c++) {
+			const size_t j = ((size_t)r * N + d) * 3 + c;
+			const double2 p = P[j], e = E[j];
+			s[0] += p.y * e.x - p.x * e.y;
+			const double2 a = per_dip ? cc[((size_t)r * N + d) * 3 + c] : cc[((size_t)r * nmat + mat[d]) * 3 + c];
+			const double im_inv = -a.y / (a.x * a.x + a.y * a.y);
+			s[1] += (-im_inv - 2 * k3 / 3) * (p.x * p.x + p.y * p.y);
+		}
+	}
+	__shared__ double sh[2][NT / 32];
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	for (int j = 0; j < 2; j++) {
+		double v = s[j];
+		for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+		if (lane == 0) sh[j][wid] = v;
+	}
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		double *o = part + ((size_t)r * nbv + blockIdx.x) * 8;
+		for (int j = 0; j < 2; j++) {
+			double v = 0;
+			for (int w = 0; w < NT / 32; w++) v += sh[j][w];
+			o[j] = v;
+		}
+	}
+}
+
 // scattering amplitudes (CalcFieldFree, crosssec.c:506-596), first stage: per block partial sums of
 // P_j exp(-i kd n.pos_j) for direction blockIdx.y and RHS blockIdx.z (6 doubles: Re/Im of the 3 components)
 __global__ void __launch_bounds__(NT) k_field(const double2 *P, const uint16_t *pos, size_t N, const double *dirs,
@@ -2542,6 +2577,45 @@ int cross_sections(adda_gb300_ctx *c, int R, const double *prop, const double *i
 		}
 		if (cext) cext[r] = sumc * 4 * PI / (c->k * c->k);
 		if (cabs) cabs[r] = 4 * PI * c->k * sm[6];
+	}
+	return ADDA_GB300_OK;
+}
+
+int cross_sections_beam(adda_gb300_ctx *c, int R, const double *einc, double inc_scale, double *cext, double *cabs)
+{
+	int rc = ensure_work(c, R, 1);
+	if (rc) return rc;
+	SolverWork *w = c->sw;
+	cudaStream_t s = c->stream;
+	double2 *d_e = nullptr;
+	const size_t n = (size_t)R * c->N * 3;
+	ADDA_CUDA(cudaMalloc(&d_e, sizeof(double2) * std::max<size_t>(n, 1)));
+	cudaError_t e = cudaMemcpyAsync(d_e, einc, sizeof(double2) * n, cudaMemcpyHostToDevice, s);
+	std::vector<double> part((size_t)R * w->nbv * 8);
+	if (e == cudaSuccess) {
+		const dim3 g(w->nbv, R);
+		k_cross_beam<<<g, NT, 0, s>>>(c->pvec64, d_e, c->cc64, c->per_dip, c->nmat, c->d_mat, c->N,
+			c->k * c->k * c->k, w->xpart, w->nbv);
+		count_launch();
+		e = cudaGetLastError();
+	}
+	if (e == cudaSuccess) e = cudaMemcpyAsync(part.data(), w->xpart, sizeof(double) * part.size(),
+		cudaMemcpyDeviceToHost, s);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+	cudaFree(d_e);
+	if (e != cudaSuccess) {
+		set_error(std::string("cross_sections_beam: ") + cudaGetErrorString(e));
+		return ADDA_GB300_ECUDA;
+	}
+	const double PI = 3.14159265358979323846;
+	for (int r = 0; r < R; r++) {
+		double s0 = 0, s1 = 0;
+		for (int b = 0; b < w->nbv; b++) {
+			s0 += part[((size_t)r * w->nbv + b) * 8];
+			s1 += part[((size_t)r * w->nbv + b) * 8 + 1];
+		}
+		if (cext) cext[r] = s0 * 4 * PI * c->k * inc_scale;
+		if (cabs) cabs[r] = 4 * PI * c->k * s1 * inc_scale;
 	}
 	return ADDA_GB300_OK;
 }

@@ -91,6 +91,16 @@ enum adda_gb300_init_field { ADDA_IF_AUTO = 0, ADDA_IF_ZERO = 1, ADDA_IF_INC = 2
 /* ADDA_IF_CHPOINT: every right-hand side resumes from the state given to adda_gb300_chpoint_load (the reference's
  * -chp_load, LoadIterChpoint, iterative.c:222-278); FP64 only */
 
+/* reflected Green's tensor of a particle near a substrate (-int_surf, interaction.c:1082-1345):
+ * IMG  image-dipole approximation, computed on the GPU (ReflTerm_img);
+ * SOM  image dipole plus the Sommerfeld-integral correction; refl_data holds the four integrals Irv, Izv, Irh, Iph
+ *      (complex) for every in-plane offset (i < boxX, j < boxY) and height sum k < 2*boxZ-1, layout [k][j][i][4],
+ *      evaluated at rho = hypot(i,j)*d, z = (k + zsum_shift)*d (the table of CalcSomTable, interaction.c:1176-1224,
+ *      on the full rectangle); they are combined with the image term on the GPU (ReflTerm_som_int);
+ * HOST the reflected tensor itself from the caller (e.g. the reference's own ReflTerm_int): refl_data [k][j][i'][6]
+ *      complex for k < 2*boxZ-1, j < boxY, i' = i + boxX - 1 < 2*boxX-1 (components xx,xy,xz,yy,yz,zz). */
+enum adda_gb300_refl { ADDA_REFL_IMG = 0, ADDA_REFL_SOM = 1, ADDA_REFL_HOST = 2 };
+
 typedef struct adda_gb300_ctx adda_gb300_ctx;
 
 /* The particle lattice: replaces the globals the reference sets in ParSetup/MakeParticle (comm.c:481-535,
@@ -107,6 +117,14 @@ typedef struct {
 	int device;                  /* CUDA device ordinal */
 	int interaction;             /* enum adda_gb300_inter (-int); 0 = point dipoles */
 	double nloc_rp;              /* Gaussian width Rp of -int nloc|nloc_av <Rp> (same length unit as gridspace) */
+	/* particle near a substrate (-surf <h> <m_re> <m_im> | -surf <h> inf); all ignored when surface == 0 */
+	int surface;
+	double zsum_shift;           /* ZsumShift (make_particle.c:2309): 2*(h/d - (boxZ-1)/2), in lattice units; the
+	                                lowest dipole layer zmin must be above the substrate: zsum_shift + 2*zmin > 0 */
+	double msub_re, msub_im;     /* substrate refractive index */
+	int msub_inf;                /* perfectly reflecting substrate (reflection coefficient -1, image relation) */
+	int refl;                    /* enum adda_gb300_refl */
+	const double *refl_data;     /* SOM / HOST data (copied by adda_gb300_create), NULL for IMG */
 } adda_gb300_problem;
 
 typedef struct {
@@ -150,6 +168,13 @@ void adda_gb300_rotation(const double prop0[3], double alpha_deg, double beta_de
 /* GenerateB, free-space plane wave, src/GenerateB.c:324-328: einc[i] = pol * exp(i k r_i.prop) */
 void adda_gb300_plane_wave(size_t ndip, const uint16_t *position, int boxX, int boxY, int boxZ, double gridspace,
 	double wavenum, const double prop[3], const double pol[3], double *einc);
+/* GenerateB, plane wave for a particle whose centre is hsub above a substrate of index msub (msub_inf: perfectly
+ * reflecting), src/GenerateB.c:96-140, 257-323. which: 0 = the Y polarisation (s), 1 = X (p). From above (prop[2] <
+ * 0) the incident plus the Fresnel-reflected wave; from below (prop[2] > 0, finite msub only) the transmitted wave.
+ * inc_scale receives the cross-section factor (1/Re(msub) from below, else 1). EINVAL for prop[2] == 0. */
+int adda_gb300_plane_wave_surf(size_t ndip, const uint16_t *position, int boxX, int boxY, int boxZ,
+	double gridspace, double wavenum, const double prop[3], const double incPolY[3], const double incPolX[3],
+	int which, double hsub, double msub_re, double msub_im, int msub_inf, double *einc, double *inc_scale);
 
 /* CalcFieldWKB (iterative.c:1227-1322): the internal field in the WKB approximation for incidence along +z:
  * E_j = Einc_j exp(phi_j), phi accumulated along each z column of the box with i(m-1)kd/2 per half cell (void cells
@@ -185,6 +210,11 @@ int adda_gb300_init_dmatrix(adda_gb300_ctx *ctx);
 /* copy the FP64 D matrix to the host: layout [x][z<gZ/2+1][y<gY/2+1][6] complex (fft.c:144-150) */
 size_t adda_gb300_dmatrix_len(const adda_gb300_ctx *ctx);
 int adda_gb300_get_dmatrix(adda_gb300_ctx *ctx, double *out);
+/* surface mode: InitRmatrix, src/fft.c:818-887, built with D by adda_gb300_init_dmatrix: R = -FFT(GR)/Ngrid with the
+ * height sums along z, reduced in y only; copy of the FP64 R: layout [x][z<gZ][y<gY/2+1][6] complex (fft.c:196-201);
+ * length 0 without a substrate */
+size_t adda_gb300_rmatrix_len(const adda_gb300_ctx *ctx);
+int adda_gb300_get_rmatrix(adda_gb300_ctx *ctx, double *out);
 
 /* InitCC, src/calculator.c:266-289, for right-hand side rhs: cc per material [nmat][3] complex */
 int adda_gb300_set_cc(adda_gb300_ctx *ctx, int rhs, int nmat, const double *cc);
@@ -242,6 +272,11 @@ int adda_gb300_solve_many(int nctx, adda_gb300_ctx *const *ctxs, const adda_gb30
 /* ExtCross (plane wave) and AbsCross (Draine), src/crosssec.c:811-917, in FP64 on the device from the
  * polarisations left by the last solve: prop/incpol per RHS [nrhs][3]; cext/cabs per RHS. */
 int adda_gb300_cross_sections(adda_gb300_ctx *ctx, int nrhs, const double *prop, const double *incpol,
+	double *cext, double *cabs);
+/* ExtCross for a general incident field, the branch the reference takes in surface mode (src/crosssec.c:823-846):
+ * Cext = 4 pi k sum_j Im(P_j . conj(Einc_j)) * inc_scale, and AbsCross * inc_scale (inc_scale from
+ * adda_gb300_plane_wave_surf), from the polarisations of the last solve; einc [nrhs][ndip][3] complex (host). */
+int adda_gb300_cross_sections_beam(adda_gb300_ctx *ctx, int nrhs, const double *einc, double inc_scale,
 	double *cext, double *cabs);
 
 /* ---- integrals over scattering directions (host code; fields from the GPU) ------------------------------------- */

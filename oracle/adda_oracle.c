@@ -34,6 +34,13 @@ struct or_ctx {
 	cfft_plan px, py, pz;
 	cplx *X;             // expanded grid after the X transform: [3][bZ][bY][gX]
 	int nthreads;
+	// particle near a substrate (src/interaction.c:1082-1345, src/fft.c:818-887)
+	int surf;
+	double zshift;       // ZsumShift: distance from the lowest dipole layer to its image (lattice units)
+	cplx rcn;            // surfRCn: reflection coefficient at normal incidence
+	cplx *somt;          // Sommerfeld integrals [2bZ-1][bY][bX][4] (NULL: image-dipole relation)
+	size_t RsY;          // reduced R size along y (gY/2+1)
+	cplx *R;             // [gX][gZ][RsY][6]
 };
 
 /* fftFit, src/fft.c:528-562 (FFTW3 branch, weird_nprocs=false): smallest even x' >= x divisible by divis whose prime
@@ -81,7 +88,7 @@ void or_free(or_ctx *c)
 	cfft_plan_free(&c->px);
 	cfft_plan_free(&c->py);
 	cfft_plan_free(&c->pz);
-	free(c->pos); free(c->mat); free(c->D); free(c->X); free(c->ccd); free(c->ccsd);
+	free(c->pos); free(c->mat); free(c->D); free(c->X); free(c->ccd); free(c->ccsd); free(c->somt); free(c->R);
 	free(c);
 }
 
@@ -231,6 +238,8 @@ size_t or_dmatrix_len(const or_ctx *c)
 	return (size_t)c->gX * c->DsZ * c->DsY * 6;
 }
 
+static void init_rmatrix(or_ctx *c);
+
 /* InitDmatrix, src/fft.c:918-1322 (sequential, reduced_FFT): D = -FFT(G)/Ngrid, stored for y<=gY/2, z<=gZ/2 only;
  * the remaining octants follow from the reflection symmetries of G (components xy,yz odd in y; xz,yz odd in z). */
 void or_init_dmatrix(or_ctx *c)
@@ -286,11 +295,133 @@ void or_init_dmatrix(or_ctx *c)
 		}
 	}
 	free(G);
+	if (c->surf) init_rmatrix(c);
 }
 
 void or_get_dmatrix(const or_ctx *c, double *out)
 {
 	memcpy(out, c->D, sizeof(cplx) * or_dmatrix_len(c));
+}
+
+/* surfRCn, src/interaction.c:1411: (1 - msub^2)/(1 + msub^2), -1 for a perfectly reflecting substrate */
+void or_set_surface(or_ctx *c, double zsum_shift, double msub_re, double msub_im, int msub_inf,
+	const double *som_table)
+{
+	const cplx m = msub_re + I * msub_im;
+	c->surf = 1;
+	c->zshift = zsum_shift;
+	c->rcn = msub_inf ? -1 : (1 - m * m) / (1 + m * m);
+	free(c->somt);
+	c->somt = NULL;
+	if (som_table) {
+		const size_t len = (size_t)4 * (2 * c->bZ - 1) * c->bY * c->bX;
+		c->somt = malloc(sizeof(cplx) * len);
+		memcpy(c->somt, som_table, sizeof(cplx) * len);
+	}
+}
+
+/* Reflected Green's tensor for the lattice offset (i, j) and height sum k (lattice units, probe minus image of the
+ * source): ReflParams + ReflTerm_core (image dipole scaled by surfRCn, z components inverted),
+ * src/interaction.c:1092-1134, plus with a Sommerfeld table CombineSomTensor of the four integrals at rho = |(i,j)|,
+ * src/interaction.c:1229-1301. Component order xx,xy,xz,yy,yz,zz. */
+static void green_refl(const or_ctx *c, int i, int j, int k, cplx g[6])
+{
+	const double q[3] = {i, j, k + c->zshift};
+	double rr = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+	const double qv[3] = {q[0] / rr, q[1] / rr, q[2] / rr};
+	const double qm[6] = {qv[0] * qv[0], qv[0] * qv[1], qv[0] * qv[2], qv[1] * qv[1], qv[1] * qv[2], qv[2] * qv[2]};
+	rr *= c->gridspace;
+	const double invr3 = 1 / (rr * rr * rr), kr = c->k * rr, kr2 = kr * kr;
+	const double t1 = 3 - kr2, t2 = -3 * kr, t3 = kr2 - 1;
+	const cplx scale = c->rcn * (invr3 * (cos(kr) + I * sin(kr)));
+	for (int a = 0; a < 6; a++) {
+		if (a == 0 || a == 3 || a == 5) g[a] = ((t1 * qm[a] + t3) + I * (kr + t2 * qm[a])) * scale;
+		else g[a] = (t1 + I * t2) * qm[a] * scale;
+	}
+	g[2] = -g[2];
+	g[4] = -g[4];
+	g[5] = -g[5];
+	if (c->somt) {
+		const int iT = i < 0 ? -i : i, jT = j < 0 ? -j : j;
+		const cplx *v = c->somt + 4 * (((size_t)k * c->bY + jT) * c->bX + iT);
+		const cplx Irv = v[0], Izv = v[1], Irh = v[2], Iph = v[3];
+		const double x = i, y = j, rho = hypot(x, y);
+		if (rho == 0) {
+			g[0] += Irh;
+			g[3] += Irh;
+			g[5] += Izv;
+		}
+		else {
+			const double xr = x / rho, yr = y / rho;
+			g[0] += xr * xr * Irh - yr * yr * Iph;
+			g[1] += xr * yr * (Irh + Iph);
+			g[2] += xr * Irv;
+			g[3] += yr * yr * Irh - xr * xr * Iph;
+			g[4] += yr * Irv;
+			g[5] += Izv;
+		}
+	}
+}
+
+size_t or_rmatrix_len(const or_ctx *c)
+{
+	return c->surf ? (size_t)c->gX * c->gZ * (c->gY / 2 + 1) * 6 : 0;
+}
+
+void or_get_rmatrix(const or_ctx *c, double *out)
+{
+	if (c->R) memcpy(out, c->R, sizeof(cplx) * or_rmatrix_len(c));
+}
+
+/* InitRmatrix, src/fft.c:818-887 (sequential, reduced_FFT): R = -FFT(GR)/Ngrid with GR(i,j,k) for i in (-bX,bX),
+ * j in [0,bY) mirrored to negative y (xy and yz odd in y), height sums k in [0, 2bZ-1) placed at z = k without
+ * mirroring; stored for y <= gY/2 and every z. */
+static void init_rmatrix(or_ctx *c)
+{
+	const int bX = c->bX, bY = c->bY, bZ = c->bZ, gX = c->gX, gY = c->gY, gZ = c->gZ;
+	const int nk = 2 * bZ - 1;
+	c->RsY = gY / 2 + 1;
+	free(c->R);
+	c->R = calloc(or_rmatrix_len(c), sizeof(cplx));
+	const double invN = 1.0 / (gX * ((double)gY * gZ));
+	const size_t lines = (size_t)nk * bY;
+	cplx *G = calloc(6 * lines * gX, sizeof(cplx)); // [comp][k][j][x mod gX]
+	#pragma omp parallel for num_threads(c->nthreads) schedule(dynamic)
+	for (int k = 0; k < nk; k++)
+		for (int j = 0; j < bY; j++)
+			for (int i = 1 - bX; i < bX; i++) {
+				cplx g[6];
+				green_refl(c, i, j, k, g);
+				size_t idx = ((size_t)k * bY + j) * gX + (i < 0 ? i + gX : i);
+				for (int a = 0; a < 6; a++) G[a * lines * gX + idx] = g[a];
+			}
+	for (int a = 0; a < 6; a++) {
+		cplx *Ga = G + a * lines * gX;
+		const double sy = (a == 1 || a == 4) ? -1 : 1;
+		#pragma omp parallel num_threads(c->nthreads)
+		{
+			cplx *work = malloc(sizeof(cplx) * (gX > gY ? (gX > gZ ? gX : gZ) : (gY > gZ ? gY : gZ)));
+			cplx *s = malloc(sizeof(cplx) * (size_t)gY * gZ); // [y][z]
+			#pragma omp for
+			for (size_t l = 0; l < lines; l++) cfft_exec(&c->px, Ga + l * gX, work, -1);
+			#pragma omp for
+			for (int x = 0; x < gX; x++) {
+				memset(s, 0, sizeof(cplx) * (size_t)gY * gZ);
+				for (int j = 0; j < bY; j++)
+					for (int k = 0; k < nk; k++) s[(size_t)j * gZ + k] = Ga[((size_t)k * bY + j) * gX + x];
+				for (int j = 1; j < bY; j++) // mirror along y (fft.c:859-865)
+					for (int k = 0; k < nk; k++) s[(size_t)(gY - j) * gZ + k] = sy * s[(size_t)j * gZ + k];
+				for (int y = 0; y < gY; y++) cfft_exec(&c->pz, s + (size_t)y * gZ, work, -1);
+				cfft_exec_strided(&c->py, s, gZ, 1, (size_t)gZ, -1);
+				for (size_t z = 0; z < (size_t)gZ; z++)
+					for (size_t y = 0; y < c->RsY; y++)
+						c->R[(((size_t)x * gZ + z) * c->RsY + y) * 6 + a] = -invN * s[y * gZ + z];
+			}
+			free(work);
+			free(s);
+		}
+	}
+	free(G);
 }
 
 /* InitCC, src/calculator.c:266-289: cc_sqrt = csqrt(cc) */
@@ -355,6 +486,10 @@ void or_matvec(or_ctx *c, const double *argv, double *resv, double *inprod, int 
 		cplx *work = malloc(sizeof(cplx) * gmax);
 		cplx *col = malloc(sizeof(cplx) * 3 * gY);
 		cplx *s = malloc(sizeof(cplx) * 3 * (size_t)gY * gZ); // [comp][y][z]
+		// surface: the same slab transformed along z with the opposite sign (height sums instead of differences,
+		// fft.c:396-399 planZRf), then along y (matvec.c:249, fft.c:366-367)
+		cplx *sR = c->surf ? malloc(sizeof(cplx) * 3 * (size_t)gY * gZ) : NULL;
+		cplx *colR = c->surf ? malloc(sizeof(cplx) * 3 * gY) : NULL;
 		#pragma omp for
 		for (size_t l = 0; l < 3 * (size_t)bZ * bY; l++) cfft_exec(&c->px, X + l * gX, work, -1);
 		#pragma omp for schedule(dynamic)
@@ -364,6 +499,11 @@ void or_matvec(or_ctx *c, const double *argv, double *resv, double *inprod, int 
 				for (int y = 0; y < bY; y++)
 					for (int z = 0; z < bZ; z++)
 						s[((size_t)a * gY + y) * gZ + z] = X[a * plane + ((size_t)z * bY + y) * gX + x];
+			if (sR) {
+				memcpy(sR, s, sizeof(cplx) * 3 * (size_t)gY * gZ);
+				for (int a = 0; a < 3; a++)
+					for (int y = 0; y < bY; y++) cfft_exec(&c->pz, sR + ((size_t)a * gY + y) * gZ, work, 1);
+			}
 			for (int a = 0; a < 3; a++)
 				for (int y = 0; y < bY; y++) cfft_exec(&c->pz, s + ((size_t)a * gY + y) * gZ, work, -1);
 			for (int z = 0; z < gZ; z++) {
@@ -371,6 +511,11 @@ void or_matvec(or_ctx *c, const double *argv, double *resv, double *inprod, int 
 					cplx *ln = col + a * gY;
 					for (int y = 0; y < gY; y++) ln[y] = s[((size_t)a * gY + y) * gZ + z];
 					cfft_exec(&c->py, ln, work, -1);
+					if (sR) {
+						cplx *lr = colR + a * gY;
+						for (int y = 0; y < gY; y++) lr[y] = sR[((size_t)a * gY + y) * gZ + z];
+						cfft_exec(&c->py, lr, work, -1);
+					}
 				}
 				// D~.X~ with the reduced-FFT sign flips (matvec.c:271-305)
 				for (int y = 0; y < gY; y++) {
@@ -391,6 +536,19 @@ void or_matvec(or_ctx *c, const double *argv, double *resv, double *inprod, int 
 					col[y] = m[0] * v0 + m[1] * v1 + m[2] * v2;
 					col[gY + y] = m[1] * v0 + m[3] * v1 + m[4] * v2;
 					col[2 * gY + y] = m[2] * v0 + m[4] * v1 + m[5] * v2;
+					if (sR) { // yv += R~.X'~ with R's reduced-y signs (matvec.c:288-302, cReflMatrVec cmplx.h:391-401)
+						const size_t ry = (size_t)y < c->RsY ? (size_t)y : (size_t)(gY - y);
+						const cplx *r = c->R + (((size_t)x * gZ + z) * c->RsY + ry) * 6;
+						cplx q[6] = {r[0], r[1], r[2], r[3], r[4], r[5]};
+						if ((size_t)y >= c->RsY) {
+							q[1] = -q[1];
+							q[4] = -q[4];
+						}
+						const cplx u0 = colR[y], u1 = colR[gY + y], u2 = colR[2 * gY + y];
+						col[y] += q[0] * u0 + q[1] * u1 + q[2] * u2;
+						col[gY + y] += q[1] * u0 + q[3] * u1 + q[4] * u2;
+						col[2 * gY + y] += -q[2] * u0 - q[4] * u1 + q[5] * u2;
+					}
 				}
 				for (int a = 0; a < 3; a++) {
 					cplx *ln = col + a * gY;
@@ -407,7 +565,7 @@ void or_matvec(or_ctx *c, const double *argv, double *resv, double *inprod, int 
 		}
 		#pragma omp for
 		for (size_t l = 0; l < 3 * (size_t)bZ * bY; l++) cfft_exec(&c->px, X + l * gX, work, 1);
-		free(work); free(col); free(s);
+		free(work); free(col); free(s); free(sR); free(colR);
 	}
 	// gather y = x + S.X (matvec.c:352-364)
 	double sum = 0;
@@ -1206,4 +1364,24 @@ void or_cross(or_ctx *c, const double *pvec, const double prop[3], const double 
 			sa += mult * (creal(p) * creal(p) + cimag(p) * cimag(p));
 		}
 	*cabs = 4 * M_PI * c->k * sa;
+}
+
+/* ExtCross for a general incident field (the branch taken in surface mode), src/crosssec.c:823-845:
+ * Cext = 4 pi k sum_j Im(P_j . conj(Einc_j)), times inc_scale (1/Re(msub) for a beam from the substrate, 1 otherwise,
+ * GenerateB.c:104,117); AbsCross (Draine) times the same factor, src/crosssec.c:852-917 */
+void or_cross_beam(or_ctx *c, const double *pvec, const double *einc, double inc_scale, double *cext, double *cabs)
+{
+	const cplx *P = (const cplx *)pvec, *E = (const cplx *)einc;
+	double s = 0;
+	for (size_t j = 0; j < 3 * c->n; j++) s += cimag(P[j]) * creal(E[j]) - creal(P[j]) * cimag(E[j]);
+	*cext = s * 4 * M_PI * c->k * inc_scale;
+	const double t1 = 2 * c->k * c->k * c->k / 3;
+	double sa = 0;
+	for (size_t j = 0; j < c->n; j++)
+		for (int i = 0; i < 3; i++) {
+			double mult = -cimag(1 / cc_of(c, j, i)) - t1;
+			cplx p = P[3 * j + i];
+			sa += mult * (creal(p) * creal(p) + cimag(p) * cimag(p));
+		}
+	*cabs = 4 * M_PI * c->k * sa * inc_scale;
 }

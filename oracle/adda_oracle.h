@@ -12,6 +12,9 @@
  *   or_solve_chp     <- SaveIterChpoint / LoadIterChpoint  src/iterative.c:165-278
  *   or_cross         <- ExtCross / AbsCross      src/crosssec.c:811-917 (plane wave, free space, Draine)
  *   or_field         <- CalcFieldFree            src/crosssec.c:506-596 (scattering amplitude in one direction)
+ *   or_set_surface   <- particle near a substrate: ReflTerm_img / ReflTerm_som (src/interaction.c:1082-1345),
+ *                       InitRmatrix (src/fft.c:818-887), the reflected part of MatVec (src/matvec.c:249-303)
+ *   or_cross_beam    <- ExtCross for a general incident field (src/crosssec.c:823-845), AbsCross
  * Complex vectors are interleaved (re,im) doubles, dipole-major [dipole][3], like the reference's doublecomplex.
  */
 #ifndef ADDA_ORACLE_H
@@ -59,5 +62,13 @@ int or_solve_chp(or_ctx *c, int method, const double *einc, double eps, int maxi
 void or_cross(or_ctx *c, const double *pvec, const double prop[3], const double incpol[3], double *cext,
 	double *cabs);
 void or_field(const or_ctx *c, const double *pvec, const double n[3], double *ebuff);
+/* surface mode, set before or_init_dmatrix (which then also builds R): ZsumShift (lattice units), the substrate's
+ * refractive index (msub_inf: perfectly reflecting), and the Sommerfeld integrals Irv, Izv, Irh, Iph per
+ * (k < 2bZ-1, j < bY, i < bX) at rho = hypot(i,j) d, z = (k + ZsumShift) d (NULL: image-dipole relation) */
+void or_set_surface(or_ctx *c, double zsum_shift, double msub_re, double msub_im, int msub_inf,
+	const double *som_table);
+size_t or_rmatrix_len(const or_ctx *c);        // complex elements, layout [x][z<gridZ][y<gridY/2+1][6]
+void or_get_rmatrix(const or_ctx *c, double *out);
+void or_cross_beam(or_ctx *c, const double *pvec, const double *einc, double inc_scale, double *cext, double *cabs);
 
 #endif

@@ -63,6 +63,11 @@ def lib():
         L.or_cisi.argtypes = [ctypes.c_double, c_p, c_p]
         L.or_cross.argtypes = [c_p, c_p, c_p, c_p, c_p, c_p]
         L.or_field.argtypes = [c_p, c_p, c_p, c_p]
+        L.or_set_surface.argtypes = [c_p, c_d, c_d, c_d, c_i, c_p]
+        L.or_rmatrix_len.argtypes = [c_p]
+        L.or_rmatrix_len.restype = c_sz
+        L.or_get_rmatrix.argtypes = [c_p, c_p]
+        L.or_cross_beam.argtypes = [c_p, c_p, c_p, c_d, c_p, c_p]
         _lib = L
     return _lib
 
@@ -74,7 +79,8 @@ def _ptr(a):
 class Oracle:
     """One particle lattice on the CPU: D matrix, matvec, QMR_CS/BiCGStab and Cext/Cabs in double precision."""
 
-    def __init__(self, box, grid, position, material, gridspace, wavenum, nthreads=0, interaction="poi", nloc_rp=0.0):
+    def __init__(self, box, grid, position, material, gridspace, wavenum, nthreads=0, interaction="poi", nloc_rp=0.0,
+                 surface=None):
         self.L = lib()
         self.position = np.ascontiguousarray(position, dtype=np.uint16).reshape(-1, 3)
         self.material = np.ascontiguousarray(material if material is not None
@@ -85,6 +91,13 @@ class Oracle:
                                   gridspace, wavenum, nthreads)
         self.L.or_set_interaction(self.h, {"poi": 0, "fcd": 1, "fcd_st": 2, "nloc": 3, "nloc_av": 4}[interaction])
         self.L.or_set_nloc_rp(self.h, nloc_rp)
+        if surface is not None:  # dict(zsum_shift, msub (None: perfect reflector), relation img|som, data: som table)
+            m = surface.get("msub")
+            tab = surface.get("data") if surface.get("relation", "img") == "som" else None
+            tab = None if tab is None else np.ascontiguousarray(tab, dtype=np.complex128)
+            mm = complex(0 if m is None else m)
+            self.L.or_set_surface(self.h, surface["zsum_shift"], mm.real, mm.imag, 1 if m is None else 0,
+                                  None if tab is None else _ptr(tab))
         self.L.or_init_dmatrix(self.h)
 
     def close(self):
@@ -97,6 +110,19 @@ class Oracle:
             self.close()
         except Exception:
             pass
+
+    def rmatrix(self):
+        n = self.L.or_rmatrix_len(self.h)
+        out = np.empty(n, dtype=np.complex128)
+        self.L.or_get_rmatrix(self.h, _ptr(out))
+        return out
+
+    def cross_beam(self, p, einc, inc_scale=1.0):
+        ce, ca = ctypes.c_double(), ctypes.c_double()
+        p = np.ascontiguousarray(p, dtype=np.complex128)
+        e = np.ascontiguousarray(einc, dtype=np.complex128)
+        self.L.or_cross_beam(self.h, _ptr(p), _ptr(e), inc_scale, ctypes.byref(ce), ctypes.byref(ca))
+        return ce.value, ca.value
 
     def dmatrix(self):
         n = self.L.or_dmatrix_len(self.h)

@@ -39,7 +39,8 @@ def solver_opts(kw):
 def oracle_for(s, nthreads=0):
     from oracle import oracle as O
     o = O.Oracle(s.box, s.grid, s.pos, s.mat, s.gridspace, s.wavenum, nthreads,
-                 interaction=getattr(s, "interaction", "poi"), nloc_rp=getattr(s, "nloc_rp", 0.0))
+                 interaction=getattr(s, "interaction", "poi"), nloc_rp=getattr(s, "nloc_rp", 0.0),
+                 surface=getattr(s, "surface", None))
     return o
 
 
