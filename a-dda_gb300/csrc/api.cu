@@ -723,6 +723,11 @@ int adda_gb300_time_matvec(adda_gb300_ctx *c, int prec, int nrhs, int iters, siz
 int adda_gb300_vjp_chi(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int rhs, const double prop[3],
 	const double incpol[3], const double *dinv_alpha, double *grad_cext, double *grad_cabs)
 {
+	if (c && c->surface) {
+		set_error("vjp_chi: free-space formula; in surface mode the reference scatters through CalcFieldSurf "
+			"(crosssec.c:601-800), which is not provided (Cext/Cabs: adda_gb300_cross_sections_beam)");
+		return ADDA_GB300_ESTATE;
+	}
 	if (!c || !sp || !prop || !incpol || !dinv_alpha || !grad_cext || !grad_cabs) {
 		set_error("vjp_chi: invalid arguments");
 		return ADDA_GB300_EINVAL;
@@ -734,6 +739,11 @@ int adda_gb300_vjp_chi(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int
 int adda_gb300_cross_sections(adda_gb300_ctx *c, int nrhs, const double *prop, const double *incpol, double *cext,
 	double *cabs)
 {
+	if (c && c->surface) {
+		set_error("cross_sections: free-space formula; in surface mode the reference scatters through CalcFieldSurf "
+			"(crosssec.c:601-800), which is not provided (Cext/Cabs: adda_gb300_cross_sections_beam)");
+		return ADDA_GB300_ESTATE;
+	}
 	if (!c || !prop || !incpol || nrhs < 1 || nrhs > c->last_nrhs || !c->pvec64) {
 		set_error("cross_sections: no solution available for that many RHS");
 		return ADDA_GB300_ESTATE;
@@ -756,6 +766,11 @@ int adda_gb300_cross_sections_beam(adda_gb300_ctx *c, int nrhs, const double *ei
 int adda_gb300_scattering_integrals(adda_gb300_ctx *c, int nrhs, const adda_gb300_integr_parms p[2],
 	const double prop[3], const double incpolx[3], const double incpoly[3], double *csca, double *csca_g)
 {
+	if (c && c->surface) {
+		set_error("scattering_integrals: free-space formula; in surface mode the reference scatters through CalcFieldSurf "
+			"(crosssec.c:601-800), which is not provided (Cext/Cabs: adda_gb300_cross_sections_beam)");
+		return ADDA_GB300_ESTATE;
+	}
 	if (!c || !p || !prop || !incpolx || !incpoly || !csca || !csca_g || nrhs < 1 || nrhs > c->last_nrhs ||
 		!c->pvec64) {
 		set_error("scattering_integrals: invalid arguments or no solution available for that many RHS");
@@ -813,6 +828,11 @@ int adda_gb300_scattering_integrals(adda_gb300_ctx *c, int nrhs, const adda_gb30
 
 int adda_gb300_scattered_fields(adda_gb300_ctx *c, int nrhs, int ndir, const double *dirs, double *ebuff)
 {
+	if (c && c->surface) {
+		set_error("scattered_fields: free-space formula; in surface mode the reference scatters through CalcFieldSurf "
+			"(crosssec.c:601-800), which is not provided (Cext/Cabs: adda_gb300_cross_sections_beam)");
+		return ADDA_GB300_ESTATE;
+	}
 	if (!c || !dirs || !ebuff || ndir < 1 || nrhs < 1 || nrhs > c->last_nrhs || !c->pvec64) {
 		set_error("scattered_fields: invalid arguments or no solution available for that many RHS");
 		return ADDA_GB300_ESTATE;

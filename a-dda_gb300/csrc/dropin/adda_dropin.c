@@ -39,6 +39,11 @@ extern size_t gridX, gridY, gridZ, gridYZ, local_Nsmall, local_nvoid_Ndip, local
 extern double gridspace, WaveNum, memory;
 extern bool prognosis, reduced_FFT, surface, orient_avg, ipr_required;
 extern enum inter IntRelation;
+extern bool msubInf;                                                  /* vars.c:128 */
+extern doublecomplex msub;                                            /* vars.c:126 */
+extern double ZsumShift;                                              /* make_particle.c:68 */
+/* the reflected Green's tensor of the -int_surf relation chosen by InitInteraction (interaction.h:39) */
+extern void (*ReflTerm_int)(const int i, const int j, const int k, doublecomplex result[static restrict 6]);
 extern const double nloc_Rp; /* param.c:132 */
 extern FILE *logfile;
 extern unsigned short *position;
@@ -99,7 +104,6 @@ void CheckNprocs(void)
 void InitDmatrix(void)
 {
 	clock_t start = clock();
-	if (surface) ERR("The GPU build does not support -surf");
 	int inter = ADDA_INT_POI;
 	if (IntRelation == G_POINT_DIP) inter = ADDA_INT_POI;
 	else if (IntRelation == G_FCD) inter = ADDA_INT_FCD;
@@ -128,7 +132,28 @@ void InitDmatrix(void)
 	p.device = getenv("ADDA_GB300_DEVICE") ? atoi(getenv("ADDA_GB300_DEVICE")) : 0;
 	p.interaction = inter;
 	p.nloc_rp = nloc_Rp;
-	if (adda_gb300_create(&p, &g_ctx)) ERR("GPU initialisation failed: %s", adda_gb300_last_error());
+	doublecomplex *gr = NULL;
+	if (surface) {
+		/* the reflected tensor of every in-plane offset and height sum, from the reference's own ReflTerm_int (image
+		 * dipole or Sommerfeld integrals, as InitRmatrix evaluates it, fft.c:846-850); the GPU transforms it */
+		const size_t nk = 2 * (size_t)boxZ - 1, ni = 2 * (size_t)boxX - 1;
+		gr = malloc(sizeof(doublecomplex) * 6 * nk * boxY * ni);
+		if (!gr) ERR("cannot allocate the reflected Green's tensor (%zu MB)", 96 * nk * boxY * ni >> 20);
+		for (int k = 0; k < (int)nk; k++)
+			for (int j = 0; j < boxY; j++)
+				for (int i = 1 - boxX; i < boxX; i++)
+					(*ReflTerm_int)(i, j, k, gr + 6 * (((size_t)k * boxY + j) * ni + (size_t)(i + boxX - 1)));
+		p.surface = 1;
+		p.zsum_shift = ZsumShift;
+		p.msub_re = creal(msub);
+		p.msub_im = cimag(msub);
+		p.msub_inf = msubInf;
+		p.refl = ADDA_REFL_HOST;
+		p.refl_data = (const double *)gr;
+	}
+	const int crc = adda_gb300_create(&p, &g_ctx);
+	free(gr);
+	if (crc) ERR("GPU initialisation failed: %s", adda_gb300_last_error());
 	if (adda_gb300_init_dmatrix(g_ctx)) ERR("GPU D-matrix initialisation failed: %s", adda_gb300_last_error());
 	g_ccs_valid = 0;
 	g_pvec_valid = 0;

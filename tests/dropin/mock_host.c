@@ -31,6 +31,29 @@ size_t gridX, gridY, gridZ, gridYZ, local_Nsmall, local_nvoid_Ndip, local_nRows;
 double gridspace, WaveNum, memory;
 bool prognosis = false, reduced_FFT = true, surface = false, orient_avg = false, ipr_required = false;
 enum inter IntRelation = G_POINT_DIP;
+/* surface mode: the substrate and the image-dipole relation (ReflTerm_img, interaction.c:1092-1153), stand-ins for
+ * vars.c:126-129, make_particle.c:68 and InitInteraction */
+bool msubInf = false;
+doublecomplex msub;
+double ZsumShift, hsub;
+static doublecomplex surfRCn;
+static void refl_img(const int i, const int j, const int k, doublecomplex g[static restrict 6])
+{
+	const double q[3] = {i, j, k + ZsumShift};
+	double rr = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+	const double v[3] = {q[0] / rr, q[1] / rr, q[2] / rr};
+	const double qm[6] = {v[0] * v[0], v[0] * v[1], v[0] * v[2], v[1] * v[1], v[1] * v[2], v[2] * v[2]};
+	rr *= gridspace;
+	const double kr = WaveNum * rr, kr2 = kr * kr, t1 = 3 - kr2, t2 = -3 * kr, t3 = kr2 - 1;
+	const doublecomplex scale = surfRCn * cexp(I * kr) / (rr * rr * rr);
+	for (int a = 0; a < 6; a++)
+		g[a] = (a == 0 || a == 3 || a == 5) ? ((t1 * qm[a] + t3) + I * (kr + t2 * qm[a])) * scale
+			: (t1 + I * t2) * qm[a] * scale;
+	g[2] = -g[2];
+	g[4] = -g[4];
+	g[5] = -g[5];
+}
+void (*ReflTerm_int)(const int i, const int j, const int k, doublecomplex result[static restrict 6]) = refl_img;
 double nloc_Rp = 0;
 FILE *logfile;
 unsigned short *position;
@@ -170,6 +193,13 @@ int main(int argc, char **argv)
 		chp_time = atoi(argv[11]) > 0 ? atoi(argv[11]) : -1;
 		if (argc > 12) maxiter = atoi(argv[12]);
 	}
+	if (argc > 11 && !strcmp(argv[8], "surf")) { /* -surf <h> <m_re> <m_im> -int_surf img */
+		surface = true;
+		hsub = atof(argv[9]);
+		msub = atof(argv[10]) + I * atof(argv[11]);
+		surfRCn = (1 - msub * msub) / (1 + msub * msub);
+		ZsumShift = 2 * (hsub / gridspace - (boxZ - 1) / 2.0);
+	}
 	if (argc > 9 && !strcmp(argv[8], "chp_load")) {
 		chp_dir = argv[9];
 		load_chpoint = true;
@@ -178,7 +208,13 @@ int main(int argc, char **argv)
 	Einc = malloc(sizeof(doublecomplex) * local_nRows);
 	xvec = malloc(sizeof(doublecomplex) * local_nRows);
 	pvec = malloc(sizeof(doublecomplex) * local_nRows);
-	adda_gb300_plane_wave(local_nvoid_Ndip, position, boxX, boxY, boxZ, gridspace, WaveNum, prop, py, (double *)Einc);
+	if (surface) {
+		double sc;
+		if (adda_gb300_plane_wave_surf(local_nvoid_Ndip, position, boxX, boxY, boxZ, gridspace, WaveNum, prop, py, px,
+				0, hsub, creal(msub), cimag(msub), 0, (double *)Einc, &sc)) return 4;
+	}
+	else adda_gb300_plane_wave(local_nvoid_Ndip, position, boxX, boxY, boxZ, gridspace, WaveNum, prop, py,
+		(double *)Einc);
 	InitDmatrix();
 	int niter = IterativeSolver(method, INCPOL_Y);
 	if (niter == -2) printf("mock host: exit after checkpoint\n"); /* CHP_EXIT: Calculator returns (calculator.c:312) */
@@ -194,6 +230,12 @@ int main(int argc, char **argv)
 	fwrite(&ip, sizeof(ip), 1, f);
 	fwrite(pvec, sizeof(doublecomplex), local_nRows, f);
 	fwrite(y, sizeof(doublecomplex), local_nRows, f);
+	if (surface) { /* the reference scatters through CalcFieldSurf in surface mode: no scattering output here */
+		fclose(f);
+		Free_FFT_Dmat();
+		printf("mock host: %lld dipoles, %d iterations, %zu matvecs\n", n, niter, TotalMatVec);
+		return 0;
+	}
 	/* scattered fields through the reference's CalcField call (wrapped at link time): forward and two more */
 	const double dirs[3][3] = {{prop[0], prop[1], prop[2]}, {0.6, 0.0, 0.8}, {0.0, -1.0, 0.0}};
 	for (int d = 0; d < 3; d++) {

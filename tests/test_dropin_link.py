@@ -28,6 +28,13 @@ def test_reference_host_links_with_dropin(tmp_path, adda):
                            cwd=tmp_path)
         assert p.returncode != 0
         assert "GPU initialisation failed" in p.stdout + p.stderr
+        # surface mode: the drop-in evaluates the reflected tensor with the reference's ReflTerm_int (Sommerfeld
+        # integrals of the reference's somnec) on the host before it reaches the GPU
+        p = subprocess.run([exe, "-grid", "8", "-surf", "2", "2", "0.5", "-dir", str(tmp_path / "surf")],
+                           capture_output=True, text=True, cwd=tmp_path)
+        assert p.returncode != 0
+        assert "GPU initialisation failed" in p.stdout + p.stderr
+        assert "Reflected Green's tensor formulae: 'Sommerfeld integrals'" in open(tmp_path / "surf" / "log").read()
     # unsupported options stop with the reference's error path
     p = subprocess.run([exe, "-grid", "8", "-iter", "cgnr", "-prognosis", "-dir", str(tmp_path / "c")],
                        capture_output=True, text=True, cwd=tmp_path)

@@ -127,3 +127,28 @@ def test_dropin_init_field_read(tmp_path):
     assert "x_0 = from file " + str(f) in out
     assert niter == 0, out
     assert np.linalg.norm(pv - r["p"]) <= 1e-10 * np.linalg.norm(r["p"])
+
+
+def test_dropin_surface(tmp_path):
+    """-surf 2 2 0.5 -int_surf img through the drop-in: the reflected tensor comes from the host's ReflTerm_int
+    (HOST relation); pvec and the surface matvec equal the oracle's (Y polarisation, beam from the substrate)"""
+    import adda_gb300 as A
+    A.lib()
+    exe = build_mock()
+    out = tmp_path / "res.bin"
+    p = subprocess.run([exe, "8", "1.5", "0.1", "15", "qmr", "10", str(out), "surf", "2", "2", "0.5"],
+                       capture_output=True, text=True)
+    assert p.returncode == 0, p.stdout + p.stderr
+    raw = open(out, "rb").read()
+    n = int(np.frombuffer(raw[:8], np.int64)[0])
+    vec = np.frombuffer(raw[20:], np.complex128)
+    pv, y = vec[:3 * n], vec[3 * n:6 * n]
+    s = A.Setup(grid=8, m=1.5 + 0.1j, dpl=15, surface=dict(h=2.0, msub=2 + 0.5j, relation="img"))
+    assert n == s.n
+    o = oracle_for(s)
+    r = oracle_solve(o, s, 0, eps=1e-10)
+    assert np.linalg.norm(pv - r["p"]) / np.linalg.norm(r["p"]) < 1e-9
+    o.set_cc(s.cc[0].reshape(1, 3))
+    yr, _ = o.matvec(s.einc[0])
+    assert np.linalg.norm(y - yr) / np.linalg.norm(yr) < 1e-13
+

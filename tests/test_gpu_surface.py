@@ -145,3 +145,18 @@ def test_surface_create_errors():
                 dict(s.surface, msub=None, relation="som", data=np.zeros(4))):
         with pytest.raises(A.AddaError):
             A.Context(s.box, s.pos, s.mat, s.gridspace, s.wavenum, s.grid, 1, surface=bad)
+
+
+def test_free_space_post_processing_refused_in_surface_mode():
+    """the free-space scattering formulas (CalcFieldFree) do not apply near a substrate: those entry points refuse"""
+    import adda_gb300 as A
+    s = surface_setup(BY["img_above"])
+    ctx = context(s, 2)
+    ctx.solve(np.stack(s.einc), prec="fp64", eps=1e-6)
+    with pytest.raises(A.AddaError):
+        ctx.cross_sections(np.stack([s.prop, s.prop]), np.stack(s.incpol))
+    with pytest.raises(A.AddaError):
+        ctx.scattered_fields(np.array([[0.0, 0.0, 1.0]]))
+    with pytest.raises(A.AddaError):
+        ctx.vjp_chi(0, s.prop, s.incpol[0], np.zeros(s.n, np.complex128))
+
