@@ -234,6 +234,12 @@ def run_ours(args):
     st64 = ctx.solve_device(d_e.data_ptr(), R, d_x.data_ptr(), d_p.data_ptr(), prec="fp64", **opts)
     t64 = allmax(world, ctx.last_solve_ms() / 1e3)
     ce64, ca64 = ctx.cross_sections(np.stack([s.prop, s.prop]), np.stack(s.incpol))
+    # the configuration's other method (BiCGStab or QMR_CS), mixed, one warm-up and one timed solve
+    other = "bicgstab" if args.method == "qmr" else "qmr"
+    for _ in range(2):
+        sto = ctx.solve_device(d_e.data_ptr(), R, d_x.data_ptr(), d_p.data_ptr(), prec="mixed", method=other,
+                               eps=EPS)
+    t_other = allmax(world, ctx.last_solve_ms() / 1e3)
     # end to end through the host-pointer C ABI: Einc from pinned host memory, x and p back to host
     pin_e = torch.from_numpy(einc.view(np.float64)).pin_memory()
     pin_x = torch.empty_like(pin_e).pin_memory()
@@ -274,6 +280,8 @@ def run_ours(args):
         "mixed_f64vec_time_to_solution_s": t_f64vec,
         "mixed_f64vec_iterations": [x["niter"] for x in st64v],
         "speedup_mixed_vs_fp64": t64 / t_solve,
+        "other_method": {"method": other, "mixed_time_to_solution_s": t_other,
+                         "iterations": [x["niter"] for x in sto]},
         "iterations": {"mixed": [x["niter"] for x in stats], "fp64": [x["niter"] for x in st64],
                        "fp64_matvecs_in_mixed": [x["matvecs_fp64"] for x in stats],
                        "refinements": [x["refinements"] for x in stats]},
