@@ -353,10 +353,16 @@ template <typename T, typename V, int NS> __global__ void __launch_bounds__(256)
 // registers; the 6-component D product at every ky the lane holds (matvec.c:271-305 incl. the reduced-FFT signs)
 // writes back to the same places, then each component is transformed back and stored for y < bY. Groups of one block
 // cover consecutive (kz, rhs) units with the RHS fastest, so the D rows a block reads are shared through L1.
-template <typename V, int NS, int NT> __global__ void __launch_bounds__(NT, 4) mv_fft_y_reg(MvP<float, V> p)
+// SURF (particle near a substrate): after the D product the three TzR lines of the column follow one at a time
+// through a fourth slot (the next one loading into the free third slot meanwhile); each spectrum u_c adds column c of
+// the reflected product R~.u (M21 = M12, M31 = -M13, M32 = -M23, cReflMatrVec cmplx.h:391-401; R reduced in y only)
+// to the three result components before the inverse transforms.
+template <typename V, int NS, int NT, bool SURF = false>
+__global__ void __launch_bounds__(NT, SURF ? 3 : 4) mv_fft_y_reg(MvP<float, V> p)
 {
 	typedef float2 C;
 	constexpr int T = RegShape<NS>::T, E = RegShape<NS>::E, BUF = RegShape<NS>::BUF, G = NT / T;
+	constexpr int NSLOT = SURF ? 4 : 3;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	if (all_done(p)) return;
 	const int g = threadIdx.x / T, j1 = threadIdx.x % T;
@@ -365,7 +371,7 @@ template <typename V, int NS, int NT> __global__ void __launch_bounds__(NT, 4) m
 	if (kz >= p.gZ) return; // whole groups leave together
 	const unsigned gmask = ((1u << T) - 1u) << ((threadIdx.x & 31) & ~(T - 1));
 	const int kxl = blockIdx.y, kx = p.kx0 + kxl;
-	C *slot = reinterpret_cast<C *>(smem_raw) + (size_t)g * 3 * BUF; // slots c*BUF, c = 0..2
+	C *slot = reinterpret_cast<C *>(smem_raw) + (size_t)g * NSLOT * BUF; // slots c*BUF, c = 0..NSLOT-1
 	const size_t lz = (size_t)p.gZ * p.bY;
 	C *col = p.Tz + (((size_t)r * p.CK + kxl) * 3) * lz + (size_t)kz * p.bY;
 	// the three component lines go to their slots asynchronously (lane j1 writes and later reads only its own
@@ -379,12 +385,21 @@ template <typename V, int NS, int NT> __global__ void __launch_bounds__(NT, 4) m
 		}
 		cp_async_commit();
 	}
+	const C *colR = SURF ? p.TzR + (((size_t)r * p.CK + kxl) * 3) * lz + (size_t)kz * p.bY : nullptr;
+	if constexpr (SURF) { // u_0 into slot 3
+#pragma unroll
+		for (int j = 0; j < E; j++) {
+			const int y = j1 + T * j;
+			if (y < p.bY) cp_async_elem(slot + 3 * BUF + j * T + j1, colR + y, true);
+		}
+		cp_async_commit();
+	}
 	C v[E];
 #pragma unroll
 	for (int c = 0; c < 3; c++) {
-		if (c == 0) cp_async_wait<2>();
-		else if (c == 1) cp_async_wait<1>();
-		else cp_async_wait<0>();
+		if (c == 0) cp_async_wait<SURF ? 3 : 2>();
+		else if (c == 1) cp_async_wait<SURF ? 2 : 1>();
+		else cp_async_wait<SURF ? 1 : 0>();
 #pragma unroll
 		for (int j = 0; j < E; j++) {
 			const int y = j1 + T * j;
@@ -417,6 +432,67 @@ template <typename V, int NS, int NT> __global__ void __launch_bounds__(NT, 4) m
 		slot[j * T + j1] = cfma(m0, v0, cfma(m1, v1, cmul(m2, v2)));
 		slot[BUF + j * T + j1] = cfma(m1, v0, cfma(m3, v1, cmul(m4, v2)));
 		v[j] = cfma(m2, v0, cfma(m4, v1, cmul(m5, v2)));
+	}
+	if constexpr (SURF) {
+		const float4 *rrow = reinterpret_cast<const float4 *>(p.Rm + ((size_t)kx * p.gZ + kz) * p.RsY * 6);
+#pragma unroll 1
+		for (int c = 0; c < 3; c++) {
+			C *ub = slot + (c == 1 ? 2 : 3) * BUF; // u_0 and u_2 in slot 3, u_1 in slot 2 (free after component 2)
+			if (c < 2) {
+				// the next line into the other slot: slot 2 is free, slot 3 once u_0's transform is done
+				__syncwarp(gmask);
+				C *nb = slot + (c == 0 ? 2 : 3) * BUF;
+#pragma unroll
+				for (int j = 0; j < E; j++) {
+					const int y = j1 + T * j;
+					if (y < p.bY) cp_async_elem(nb + j * T + j1, colR + (size_t)(c + 1) * lz + y, true);
+				}
+				cp_async_commit();
+				cp_async_wait<1>();
+			}
+			else cp_async_wait<0>();
+			C u[E];
+#pragma unroll
+			for (int j = 0; j < E; j++) {
+				const int y = j1 + T * j;
+				u[j] = (y < p.bY) ? ub[j * T + j1] : make_float2(0.f, 0.f);
+			}
+			reg_fft<C, NS, false>(u, ub, j1, gmask, p.twy);
+			reg_natural<C, NS>(u);
+#pragma unroll
+			for (int j = 0; j < E; j++) {
+				const int ky = j1 + T * j;
+				const bool qy = ky >= p.RsY;
+				const float4 *f = rrow + (size_t)(qy ? p.gY - ky : ky) * 3;
+				const float4 d0 = __ldg(f), d1 = __ldg(f + 1), d2 = __ldg(f + 2);
+				C a0, a1, a2; // column c of R~ with the reduced-y signs of xy and yz
+				if (c == 0) {
+					a0 = make_float2(d0.x, d0.y);
+					a1 = make_float2(d0.z, d0.w);
+					a2 = make_float2(-d1.x, -d1.y);
+					if (qy) a1 = cneg(a1);
+				}
+				else if (c == 1) {
+					a0 = make_float2(d0.z, d0.w);
+					a1 = make_float2(d1.z, d1.w);
+					a2 = make_float2(-d2.x, -d2.y);
+					if (qy) {
+						a0 = cneg(a0);
+						a2 = cneg(a2);
+					}
+				}
+				else {
+					a0 = make_float2(d1.x, d1.y);
+					a1 = make_float2(d2.x, d2.y);
+					a2 = make_float2(d2.z, d2.w);
+					if (qy) a1 = cneg(a1);
+				}
+				slot[j * T + j1] = cfma(a0, u[j], slot[j * T + j1]);
+				slot[BUF + j * T + j1] = cfma(a1, u[j], slot[BUF + j * T + j1]);
+				v[j] = cfma(a2, u[j], v[j]);
+			}
+		}
+		__syncwarp(gmask);
 	}
 #pragma unroll 1
 	for (int c = 2; c >= 0; c--) {
@@ -583,6 +659,9 @@ template <typename T, typename V> int set_attrs_tv()
 		ADDA_SET((mv_fft_y_reg<V, 64, 128>));
 		ADDA_SET((mv_fft_y_reg<V, 128, 128>));
 		ADDA_SET((mv_fft_y_reg<V, 256, 128>));
+		ADDA_SET((mv_fft_y_reg<V, 64, 128, true>));
+		ADDA_SET((mv_fft_y_reg<V, 128, 128, true>));
+		ADDA_SET((mv_fft_y_reg<V, 256, 128, true>));
 	}
 	ADDA_SET_ALL(0);
 	ADDA_SET_ALL(64);
@@ -647,6 +726,25 @@ int launch_matvec(adda_gb300_ctx *c, int R, const V *arg, V *res, int her, const
 		if (surf) {
 			ADDA_NS_SWITCH(c->gZ, (mv_fftz<T, V, W2, 2, NS><<<g2, col_threads<T, NS, W2>(), smem_k2s<T, NS>(c->gZ), st>>>(p)));
 			ADDA_LAUNCHED();
+		}
+		if (surf && use_k2b_reg<T>(c->gY)) {
+			if constexpr (sizeof(T) == 4) {
+				constexpr int NT = 128;
+				switch (c->gY) {
+#define ADDA_K2B_REG_S(NS)                                                                                          \
+	case NS: {                                                                                                      \
+		constexpr int G = NT / RegShape<NS>::T;                                                                     \
+		const dim3 g((c->gZ * R + G - 1) / G, ck);                                                                  \
+		mv_fft_y_reg<V, NS, NT, true><<<g, NT, G * 4 * RegShape<NS>::BUF * sizeof(float2), st>>>(p);               \
+	} break;
+					ADDA_K2B_REG_S(64)
+					ADDA_K2B_REG_S(128)
+					ADDA_K2B_REG_S(256)
+#undef ADDA_K2B_REG_S
+				}
+			}
+		}
+		else if (surf) {
 			MvP<T, V> q = p;
 			q.RG = std::min(R, Tiles<T>::PAIRS / 2);
 			q.KB = std::max(1, Tiles<T>::PAIRS / 2 / q.RG);

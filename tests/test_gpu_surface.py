@@ -106,6 +106,22 @@ def test_matvec_power_of_two_grid_and_small_chunks():
             assert rel(y32[r], want) < 3e-6
 
 
+@pytest.mark.parametrize("grid", [64, 128])
+def test_matvec_register_k2b_surface(grid):
+    """FP32 surface matvec through the register-form K2b (gY = 128 and 256, the bench lattice) against the oracle"""
+    import adda_gb300 as A
+    s = A.Setup(grid=grid, m=1.33 + 0.01j, dpl=15, prop=[0, 0, -1],
+                surface=dict(h=0.6 * grid * 2 * np.pi / 15, msub=1.5, relation="img"))
+    ctx = context(s, 2)
+    o = oracle_for(s)
+    x = random_vec(s.n, 2, 13)
+    y32, _ = ctx.matvec(x, "fp32")
+    for r in range(2):
+        o.set_cc(s.cc[r].reshape(1, 3))
+        want, _ = o.matvec(x[r])
+        assert rel(y32[r], want) < 3e-6, (grid, r, rel(y32[r], want))
+
+
 @pytest.mark.parametrize("name", list(BY))
 def test_solve_gives_reference_cross_sections(name):
     c = BY[name]
