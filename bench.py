@@ -439,10 +439,12 @@ def run_batch(args):
 
 def run_profile(args):
     """small, fixed workloads for ncu: 'solve' = one warm-up + one mixed solve of the bench workload;
-    'matvec' = three FP32 matvecs (2 RHS) of the bench workload"""
+    'matvec' = three FP32 matvecs (2 RHS) of the bench workload; 'surface' = three FP32 matvecs (2 RHS) of the
+    bench workload's substrate variant"""
     import torch
     import adda_gb300 as A
-    s = A.Setup(grid=args.grid, m=M_REF, dpl=DPL)
+    surf = dict(h=30.0 * args.grid / 128, msub=1.5, relation="img") if args.mode == "profile-surface" else None
+    s = A.Setup(grid=args.grid, m=M_REF, dpl=DPL, prop=[0, 0, -1] if surf else None, surface=surf)
     ctx = A.Context.from_setup(s, nrhs_max=2)
     torch.cuda.synchronize()
     if args.mode == "profile-solve":
@@ -471,7 +473,7 @@ def main():
                     help="also time BASELINE configuration 3 on this many of its 64 seeded particles")
     ap.add_argument("--batch-maxiter", type=int, default=3000, help="iteration cap per particle in configuration 3")
     ap.add_argument("--scale-maxiter", type=int, default=1000, help="iteration cap of configuration 5")
-    ap.add_argument("--mode", default="bench", choices=["bench", "profile-solve", "profile-matvec"])
+    ap.add_argument("--mode", default="bench", choices=["bench", "profile-solve", "profile-matvec", "profile-surface"])
     ap.add_argument("--grid", type=int, default=GRID, help="sphere box size for the profile modes")
     ap.add_argument("--maxiter", type=int, default=100000, help="iteration cap of the profile-solve mode")
     args = ap.parse_args()
