@@ -1,4 +1,4 @@
-"""Benchmark: time-to-solution of the DDA solve on the 128^3 sphere (BASELINE configuration 2) on one GB300.
+"""Benchmark: time-to-solution of the DDA solve on the 128^3 sphere (N = 1,099,136, grid 256^3) on one GB300.
 
 One step = one complete solve of both incident polarisations (2 right-hand sides) of the 128^3 sphere (1,099,136
 dipoles, FFT grid 256^3, m = 1.33+0.01i, 15 dipoles per wavelength) with QMR_CS to relative residual 1e-5 in the
@@ -306,9 +306,9 @@ def run_ours(args):
         except Exception as ex:  # reported, never fatal for the headline line
             line["surface"] = {"error": str(ex)}
     if args.with_scale:
-        line["scale_config5"] = run_scale(args)
+        line["scale_256sphere"] = run_scale(args)
     if args.batch_particles:
-        line["batch_config3"] = run_batch(args)
+        line["batch_ellipsoids"] = run_batch(args)
     if rank == 0 and world == 1 and not args.no_cpu:
         t_it, desc = cpu_sample(args.method, os.cpu_count() or 1, s)
         iters = REF_ITERS.get(args.method) or [x["niter"] for x in st64]
@@ -356,7 +356,7 @@ def run_surface(args):
 
 
 def run_scale(args):
-    """BASELINE configuration 5: sphere on a 256^3 box (N = 8,783,848), FFT grid 512^3, m = 1.2, dpl 10, mixed QMR_CS
+    """the scale workload: sphere on a 256^3 box (N = 8,783,848), FFT grid 512^3, m = 1.2, dpl 10, mixed QMR_CS
     to 1e-5, both polarisations as 2 RHS, device-resident, capped at --scale-maxiter iterations: QMR_CS converges
     slowly on this non-absorbing x = 80 sphere (relative residual ~1e-2 after 4000 iterations), so the line reports
     the time per iteration and the residual reached as well as the time"""
@@ -369,7 +369,7 @@ def run_scale(args):
     t_init = time.perf_counter() - t0
     einc = np.ascontiguousarray(np.stack(s.einc))
     d_e = torch.from_numpy(einc.view(np.float64)).cuda()
-    log("config 5: context + D matrix %.2f s, solving (maxiter %d)" % (t_init, args.scale_maxiter))
+    log("scale workload: context + D matrix %.2f s, solving (maxiter %d)" % (t_init, args.scale_maxiter))
     st = ctx.solve_device(d_e.data_ptr(), 2, None, None, method=args.method, prec="mixed", eps=EPS,
                           maxiter=args.scale_maxiter)
     t_solve = ctx.last_solve_ms() / 1e3
@@ -389,7 +389,7 @@ def run_scale(args):
 
 
 def run_batch(args):
-    """BASELINE configuration 3: seeded ellipsoids (numpy default_rng(20261203): box from {24,32,48,64,96}, aspect
+    """the batching workload: seeded ellipsoids (numpy default_rng(20261203): box from {24,32,48,64,96}, aspect
     ratios U[0.5,1], m_re U[1.2,1.7], m_im U[0,0.05], dpl 10|m|), each with 16 orientations (zyz: alpha, gamma
     U[0,360), beta = arccos U[-1,1]) x 2 polarisations = 32 RHS solved together (mixed QMR_CS to 1e-5). Timed per
     particle with CUDA events (solve) and wall clock (lattice + D matrix + solve)."""
@@ -420,7 +420,7 @@ def run_batch(args):
                               maxiter=args.batch_maxiter)
         torch.cuda.synchronize()
         total_s += time.perf_counter() - t0
-        log("config 3 particle: box %s grid %s N %d: %.2f s, iterations <= %d, %d/%d converged"
+        log("batch particle: box %s grid %s N %d: %.2f s, iterations <= %d, %d/%d converged"
             % (s.box, s.grid, s.n, ctx.last_solve_ms() / 1e3, max(x["niter"] for x in st),
                sum(x["status"] == "ok" for x in st), nrhs))
         unconverged += sum(x["status"] != "ok" for x in st)
@@ -468,11 +468,11 @@ def main():
     ap.add_argument("--method", default="qmr", choices=["qmr", "bicgstab"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-surface", action="store_true", help="skip the substrate variant of the workload")
-    ap.add_argument("--with-scale", action="store_true", help="also time BASELINE configuration 5 (512^3 grid)")
+    ap.add_argument("--with-scale", action="store_true", help="also time the scale workload (256^3 sphere, 512^3 grid)")
     ap.add_argument("--batch-particles", type=int, default=0,
-                    help="also time BASELINE configuration 3 on this many of its 64 seeded particles")
-    ap.add_argument("--batch-maxiter", type=int, default=3000, help="iteration cap per particle in configuration 3")
-    ap.add_argument("--scale-maxiter", type=int, default=1000, help="iteration cap of configuration 5")
+                    help="also time the batching workload (64 seeded ellipsoids x 16 orientations) on this many particles")
+    ap.add_argument("--batch-maxiter", type=int, default=3000, help="iteration cap per particle of the batching workload")
+    ap.add_argument("--scale-maxiter", type=int, default=1000, help="iteration cap of the scale workload")
     ap.add_argument("--mode", default="bench", choices=["bench", "profile-solve", "profile-matvec", "profile-surface"])
     ap.add_argument("--grid", type=int, default=GRID, help="sphere box size for the profile modes")
     ap.add_argument("--maxiter", type=int, default=100000, help="iteration cap of the profile-solve mode")

@@ -313,7 +313,7 @@ def test_large_matvec_properties():
 
 def test_solve_many_equals_individual():
     """several particles with uneven grids solved concurrently (one stream each) give the same results as one at a
-    time (BASELINE configuration 3 pattern: ellipsoids of different sizes, orientations, both polarisations)"""
+    time (the batching pattern: ellipsoids of different sizes, orientations, both polarisations)"""
     import adda_gb300 as A
     specs = [dict(grid=8, shape="ellipsoid", pars=(0.6, 0.9), m=1.3 + 0.02j, orient=(10, 40, 70)),
              dict(grid=12, shape="ellipsoid", pars=(0.8, 0.5), m=1.6 + 0.01j, orient=(200, 100, 15)),

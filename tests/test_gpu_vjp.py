@@ -1,4 +1,4 @@
-"""Adjoint VJP of Cext and Cabs with respect to per-dipole susceptibility (BASELINE configuration 4 at small size):
+"""Adjoint VJP of Cext and Cabs with respect to per-dipole susceptibility (the inhomogeneous-cube differentiation workload at small size):
 checked against central finite differences of GPU FP64 solves (step 1e-6 on chi) and against perturbed solves of
 the CPU oracle, and through a torch.autograd.Function wrapper."""
 import numpy as np
