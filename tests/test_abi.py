@@ -33,7 +33,7 @@ def test_fftfit_matches_reference_rule(adda):
 
 
 def test_particle_counts(adda):
-    # occupied-dipole counts printed by the reference for the BASELINE configurations (log / prognosis)
+    # occupied-dipole counts printed by the reference for the benchmark workloads (log / prognosis)
     for shape, grid, pars, n in [("sphere", 16, None, 2176), ("sphere", 128, None, 1099136),
                                  ("ellipsoid", 24, (0.7, 0.8), 4032), ("box", 48, None, 110592)]:
         box, pos, mat = adda.make_particle(shape, grid, pars)
