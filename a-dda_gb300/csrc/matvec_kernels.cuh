@@ -13,6 +13,9 @@
 //   K2c mv_fftz (inv)  : inverse FFT along z, keep z<boxZ  ->  Xf
 //   K3 mv_fftx_gather  : inverse FFT along x, y = x + S.X for the dipoles of the lines, optional Krylov reductions
 //                        (|y|^2, x.y, y.u*, x.y*) as deterministic per-block partial sums.
+// A particle near a substrate adds, per chunk, K2a in its third mode (the same slab transformed along z with the
+// inverse sign into TzR, so that the product sums heights) and K2b in its surface forms (mv_fft_y_surf, or
+// mv_fft_y_reg<..., true>): D~.X~ + R~.X'~ before the inverse y transform (matvec.c:249-303).
 // The reference's explicit transposes (TransposeYZ), slice zeroing and copies (Arith2/Arith4) do not exist here:
 // every tile is loaded along the contiguous axis of its buffer and transformed in element-major shared memory.
 // Every kernel is instantiated with a compile-time FFT length NS for the power-of-two grids (all index arithmetic
