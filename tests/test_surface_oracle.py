@@ -114,3 +114,22 @@ def test_oracle_rmatrix_matches_numpy_construction():
     want = np.transpose(rf[:, :gY // 2 + 1, :, :], (0, 2, 1, 3)).reshape(-1)  # [x][z][y<gY/2+1][6]
     got = oracle_for(s).rmatrix()
     assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-12
+
+
+def test_substrate_of_index_one_vanishes():
+    """msub = 1: no reflected wave from above, full transmission from below (the beam is the free plane wave), and a
+    zero reflection coefficient (the operator is the free-space one)"""
+    import adda_gb300 as A
+    for prop in ([1, 2, -3], [0.3, -0.2, 1]):
+        s = A.Setup(grid=8, m=1.5 + 0.1j, prop=prop, surface=dict(h=2.0, msub=1.0, relation="img"))
+        free = A.Setup(grid=8, m=1.5 + 0.1j, prop=prop)
+        for k in range(2):
+            assert np.max(np.abs(s.einc[k] - free.einc[k])) < 1e-14
+        assert s.inc_scale == 1.0
+    o_s, o_f = oracle_for(s), oracle_for(free)
+    for o in (o_s, o_f):
+        o.set_cc(s.cc[0].reshape(1, 3))
+    x = np.random.default_rng(6).standard_normal(3 * s.n) + 0j
+    ys, _ = o_s.matvec(x)
+    yf, _ = o_f.matvec(x)
+    assert np.linalg.norm(ys - yf) < 1e-14 * np.linalg.norm(yf)
