@@ -47,7 +47,7 @@ class SolveParams(ctypes.Structure):
     _fields_ = [("method", ctypes.c_int), ("precision", ctypes.c_int), ("eps", ctypes.c_double),
                 ("maxiter", ctypes.c_int), ("init_field", ctypes.c_int), ("check_every", ctypes.c_int),
                 ("inner_eps", ctypes.c_double), ("max_refine", ctypes.c_int), ("chp_time", ctypes.c_double),
-                ("full_steps", ctypes.c_int)]
+                ("full_steps", ctypes.c_int), ("final_eps", ctypes.c_double)]
 
 
 class IntegrParms(ctypes.Structure):
@@ -489,13 +489,15 @@ class Context:
         return (y[0], ip[0]) if one else (y, ip)
 
     def solve(self, einc, method="qmr", prec="fp64", eps=1e-5, maxiter=100000, init="auto", check_every=0,
-              inner_eps=0.0, max_refine=0, hist_cap=0, x0=None, chp_time=0.0, full_steps=False, out=None):
+              inner_eps=0.0, max_refine=0, hist_cap=0, x0=None, chp_time=0.0, full_steps=False, out=None,
+              final_eps=0.0):
         """einc: [nrhs, 3N] complex. Returns dict with x, p [nrhs,3N], stats per RHS and residual histories
         (hist[r][k] = RE_k). init="x0" starts from x0 [nrhs, 3N] (see field_to_x0 for a field read from file or from
         wkb_field); init="chpoint" resumes every RHS from chpoint_load. chp_time > 0 stops after that many seconds
         (status "chpoint", state kept for chpoint_save); full_steps: BiCGStab without its half-step exit.
         out: optional (x, p) complex128 [nrhs, 3N] C-contiguous host arrays (e.g. views of pinned memory) that receive
-        the solution and the polarisations directly."""
+        the solution and the polarisations directly. final_eps (mixed): the FP64 residual the refinement stops at (0:
+        0.3*eps, 0.1*eps for BiCGStab/BCGS2, for cross sections within about 1e-6 of the converged ones)."""
         e = np.ascontiguousarray(einc, dtype=np.complex128).reshape(-1, 3 * self.n)
         R = e.shape[0]
         if out is not None:
@@ -514,7 +516,7 @@ class Context:
         st = (RhsStats * R)()
         hist = np.zeros((R, hist_cap)) if hist_cap else None
         sp = SolveParams(ITERS[method], PREC[prec], eps, maxiter, INIT[init], check_every, inner_eps, max_refine,
-                         chp_time, int(full_steps))
+                         chp_time, int(full_steps), final_eps)
         _check(self.L.adda_gb300_solve(self.h, ctypes.byref(sp), R, _p(e), _p(x), _p(p), st, _p(hist), hist_cap),
                "solve")
         stats = [dict(niter=s.niter, status=STATUS.get(s.status, s.status), resid=s.resid,
@@ -523,11 +525,11 @@ class Context:
         return dict(x=x, p=p, stats=stats, hist=hist)
 
     def solve_device(self, d_einc, nrhs, d_x=None, d_p=None, method="qmr", prec="mixed", eps=1e-5, maxiter=100000,
-                     init="auto", check_every=0, inner_eps=0.0, max_refine=0):
+                     init="auto", check_every=0, inner_eps=0.0, max_refine=0, final_eps=0.0):
         """solve on device-resident buffers (raw CUDA pointers as ints, double2 [nrhs][3N])"""
         st = (RhsStats * nrhs)()
         sp = SolveParams(ITERS[method], PREC[prec], eps, maxiter, INIT[init], check_every, inner_eps, max_refine,
-                         0.0, 0)
+                         0.0, 0, final_eps)
         _check(self.L.adda_gb300_solve_device(self.h, ctypes.byref(sp), nrhs, ctypes.c_void_p(d_einc),
                                               ctypes.c_void_p(d_x) if d_x else None,
                                               ctypes.c_void_p(d_p) if d_p else None, st), "solve_device")

@@ -12,8 +12,10 @@
  * Environment (the reference's command line is left unchanged):
  *   ADDA_GB300_PREC=fp64|mixed   arithmetic of IterativeSolver (default fp64, the reference's)
  *   ADDA_GB300_DEVICE=<n>        CUDA device (default 0)
- * Supported: -int poi, reduced FFT, no -surf, -iter qmr|bicgstab, -init_field auto|zero|inc. Anything else stops
- * with the reference's LogError.
+ * Supported: -int poi|fcd|fcd_st|nloc|nloc_av (with every -pol the host computes), -surf with -int_surf img|som
+ * (the reflected tensor comes from the host's ReflTerm_int), every -iter method, -init_field auto|zero|inc|read|wkb,
+ * -chpoint/-chp_load (FP64), and the scattered fields of CalcField, CalcAlldir and CalcScatGrid (free space).
+ * Refused with the reference's LogError: -int igt|igt_so|so, -no_reduced_fft, more than one MPI process.
  */
 #include "adda_gb300.h"
 #include "adda_dropin.h"

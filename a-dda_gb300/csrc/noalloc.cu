@@ -1,17 +1,19 @@
 // noalloc.cu - an allocation-free variant of the cross-section reduction (adda_gb300_cross_sections_noalloc).
 //
 // Who needs it: callers that cannot call cudaMalloc at the point where they want the cross sections -- code running
-// inside a framework that owns all device memory through its own pool, a plugin whose host forbids allocation
-// after start-up, or a sequence being recorded into a CUDA graph. The context-based adda_gb300_cross_sections gets
-// its per-block partial sums from the context's solver work buffers (allocated on first use); this variant keeps
-// them in one file-scope __device__ array instead, so a call only launches two kernels and allocates nothing.
+// inside a framework that owns all device memory through its own pool allocator (a cudaMalloc behind its back
+// fragments or over-commits the pool it manages), or a plugin whose host forbids device allocation after start-up.
+// The context-based adda_gb300_cross_sections gets its per-block partial sums from the context's solver work
+// buffers (allocated on first use); this variant keeps them in one file-scope __device__ array instead, so a call
+// only launches two kernels and allocates nothing. It applies the free-space plane-wave formulas (ExtCross with the
+// forward amplitude, AbsCross); it is not valid for a particle near a substrate.
 //
 // The array (g_noalloc_scratch, 1 MiB) is part of the library image: every GPU that loads the library holds it until
-// the process exits. Its device address is looked up once per device with cudaGetSymbolAddress by the first call on
-// that device (with that device current); make that first call before any stream capture. All calls share the
-// array and it keeps the last call's contents, so calls that overlap on the GPU (different streams, or different
-// host threads on the same device) race and must be serialised by the caller; each call rewrites every slot it
-// reads before reading it.
+// the process exits. Its device address is looked up with cudaGetSymbolAddress by the first call on each device
+// (with that device current); make that first call before any stream capture. A failed lookup is not remembered:
+// the next call tries again. All calls share the array and it keeps the last call's contents, so calls that
+// overlap on the GPU (different streams, or different host threads on the same device) race and must be
+// serialised by the caller; each call rewrites every slot it reads before reading it.
 #include "ctx.cuh"
 
 #include <cmath>
@@ -28,8 +30,7 @@ __device__ __align__(256) double g_noalloc_scratch[NOALLOC_DOUBLES];
 
 constexpr int MAX_DEVICES = 64;
 double *g_ptr[MAX_DEVICES];
-std::once_flag g_once[MAX_DEVICES];
-cudaError_t g_err[MAX_DEVICES];
+std::mutex g_mutex;
 
 // per-dipole sums of one RHS: sum_j P_j exp(-i kd n.pos_j) (CalcFieldFree, crosssec.c:506-586) and
 // sum_j sum_c (-Im(1/cc) - 2k^3/3)|P_jc|^2 (AbsCross, crosssec.c:866-882)
@@ -48,6 +49,10 @@ __global__ void __launch_bounds__(256) cross_partials(double *scratch, const dou
 			s[2 * c] += p.x * cs - p.y * sn;
 			s[2 * c + 1] += p.x * sn + p.y * cs;
 			const int m = mat ? mat[d] : 0;
+			if (!per_dip && m >= nmat) { // a material index without a polarisability: Cabs of this RHS becomes NaN
+				s[6] = nan("");
+				continue;
+			}
 			const double2 a = per_dip ? cc[((size_t)r * N + d) * 3 + c] : cc[((size_t)r * nmat + m) * 3 + c];
 			const double mult = a.y / (a.x * a.x + a.y * a.y) - 2 * k3 / 3; // -Im(1/cc) - 2k^3/3
 			s[6] += mult * (p.x * p.x + p.y * p.y);
@@ -102,13 +107,6 @@ __global__ void cross_finish(const double *scratch, int R, const double *prop, c
 	cabs[r] = 4 * PI * k * sm[6];
 }
 
-void setup_device(int dev)
-{
-	void *p = nullptr;
-	g_err[dev] = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-	g_ptr[dev] = (g_err[dev] == cudaSuccess) ? static_cast<double *>(p) : nullptr;
-}
-
 int fail(const char *msg, cudaError_t e = cudaSuccess)
 {
 	adda::set_error(e != cudaSuccess ? std::string(msg) + ": " + cudaGetErrorString(e) : std::string(msg));
@@ -133,14 +131,25 @@ extern "C" int adda_gb300_cross_sections_noalloc(int nrhs, size_t ndip, const vo
 	cudaError_t e = cudaGetDevice(&dev);
 	if (e != cudaSuccess) return fail("cross_sections_noalloc: cudaGetDevice", e);
 	if (dev < 0 || dev >= MAX_DEVICES) return fail("cross_sections_noalloc: device ordinal out of range");
-	std::call_once(g_once[dev], setup_device, dev);
-	if (!g_ptr[dev]) return fail("cross_sections_noalloc: cudaGetSymbolAddress", g_err[dev]);
+	double *scratch = nullptr;
+	{
+		// the device address of the static array, looked up on the first call on this device (retried after a
+		// failure); host code must not pass g_noalloc_scratch itself, which names a host-side stand-in
+		std::lock_guard<std::mutex> lock(g_mutex);
+		if (!g_ptr[dev]) {
+			void *p = nullptr;
+			e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+			if (e != cudaSuccess) return fail("cross_sections_noalloc: cudaGetSymbolAddress", e);
+			g_ptr[dev] = static_cast<double *>(p);
+		}
+		scratch = g_ptr[dev];
+	}
 	cudaStream_t st = static_cast<cudaStream_t>(stream);
 	const dim3 grid(NOALLOC_BLOCKS, nrhs);
-	cross_partials<<<grid, 256, 0, st>>>(g_ptr[dev], static_cast<const double2 *>(d_pvec), d_position,
+	cross_partials<<<grid, 256, 0, st>>>(scratch, static_cast<const double2 *>(d_pvec), d_position,
 		static_cast<const double2 *>(d_cc), per_dipole, nmat, per_dipole ? nullptr : d_material, ndip, d_prop,
 		wavenum * gridspace, wavenum * wavenum * wavenum);
-	cross_finish<<<(nrhs + 63) / 64, 64, 0, st>>>(g_ptr[dev], nrhs, d_prop, d_incpol, wavenum, gridspace, boxX, boxY,
+	cross_finish<<<(nrhs + 63) / 64, 64, 0, st>>>(scratch, nrhs, d_prop, d_incpol, wavenum, gridspace, boxX, boxY,
 		boxZ, d_cext, d_cabs);
 	adda::count_launch(2);
 	e = cudaGetLastError();

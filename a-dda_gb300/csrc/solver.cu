@@ -1783,6 +1783,17 @@ static int krylov(adda_gb300_ctx *c, SolverWork *w, int method, int R, int K, un
 	return ADDA_GB300_OK;
 }
 
+// FP64 residual at which the mixed solver's refinement stops. A solution that only just meets eps carries a
+// cross-section error of several times eps/10 (the 128^3 sphere at eps 1e-5: 6e-6 in Cabs, FP64 and the reference
+// alike); the measured margins bring mixed solves within 1e-6 of the converged cross sections there: QMR_CS at
+// 0.3 eps (2e-7, 5 % more iterations), BiCGStab, whose cross sections converge less regularly, at 0.1 eps (7e-7).
+static double final_eps_of(const adda_gb300_solve_params *sp)
+{
+	if (sp->final_eps > 0) return std::min(sp->final_eps, sp->eps);
+	const bool erratic = sp->method == ADDA_ITER_BICGSTAB || sp->method == ADDA_ITER_BCGS2;
+	return (erratic ? 0.1 : 0.3) * sp->eps;
+}
+
 // MIXED / MIXED_F32VEC: FP32 matvec (and, for float2, FP32 Krylov vectors) inside FP64 iterative refinement
 template <typename C>
 static int solve_mixed(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int R, adda_gb300_rhs_stats *st_out,
@@ -1806,14 +1817,17 @@ static int solve_mixed(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int
 		std::vector<double> red(4 * R);
 		ADDA_CUDA(cudaMemcpyAsync(red.data(), c->d_red, sizeof(double) * 4 * R, cudaMemcpyDeviceToHost, s));
 		ADDA_CUDA(cudaStreamSynchronize(s));
+		// the refinement drives the FP64 residual to final_eps (below eps, for the accuracy of the cross sections);
+		// the solve succeeds at eps
+		const double target = final_eps_of(sp);
 		for (int r = 0; r < R; r++) {
 			temp[r] = red[4 * r];
-			epsB64[r] = sp->eps * sp->eps * temp[r];
+			epsB64[r] = target * target * temp[r];
 		}
 		// inner right-hand side: b (step 0) in float, kept in k.v3
 		k_from64<C><<<(int)std::min<size_t>((R * n3 + NT - 1) / NT, 8192), NT, 0, s>>>(k.v3, w->b64, R * n3);
 		ADDA_LAUNCHED();
-		double inner_eps0 = sp->inner_eps > 0 ? sp->inner_eps : 0.5 * sp->eps;
+		double inner_eps0 = sp->inner_eps > 0 ? sp->inner_eps : 0.5 * target;
 		int *d_odone = w->done; // reused below as skip flags after the inner solve (copied from host)
 		// caller-supplied x_0 (staged in x64): start like a refinement step from r = b - A.x_0 in FP64
 		const bool x0mode = sp->init_field == ADDA_IF_X0;
@@ -1940,7 +1954,9 @@ static int solve_mixed(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int
 			st[r].niter = iters[r];
 			st[r].status = status[r];
 			st[r].resid = sqrt(inprod64[r] / temp[r]);
-			if (!st[r].status && inprod64[r] > epsB64[r]) st[r].status = ADDA_GB300_EMAXITER;
+			// maxiter reached on the way to final_eps after the residual met eps: converged
+			if (st[r].status == ADDA_GB300_EMAXITER && st[r].resid <= sp->eps) st[r].status = ADDA_GB300_OK;
+			if (!st[r].status && !(st[r].resid <= sp->eps)) st[r].status = ADDA_GB300_EMAXITER;
 			st[r].refinements = nref[r];
 			st[r].matvecs_fp32 = nmv32[r];
 			st[r].matvecs_fp64 = nmv64[r];
@@ -1955,7 +1971,8 @@ static int check_params(const adda_gb300_solve_params *sp)
 		(sp->precision != ADDA_PREC_FP64 && sp->precision != ADDA_PREC_MIXED &&
 			sp->precision != ADDA_PREC_MIXED_F32VEC && sp->precision != ADDA_PREC_MIXED_F64VEC) || !(sp->eps > 0) || sp->maxiter < 0 ||
 			(sp->init_field != ADDA_IF_AUTO && sp->init_field != ADDA_IF_ZERO && sp->init_field != ADDA_IF_INC &&
-			sp->init_field != ADDA_IF_X0 && sp->init_field != ADDA_IF_CHPOINT) || !(sp->chp_time >= 0)) {
+			sp->init_field != ADDA_IF_X0 && sp->init_field != ADDA_IF_CHPOINT) || !(sp->chp_time >= 0) ||
+			!(sp->final_eps >= 0)) {
 		set_error("solve: unsupported parameters");
 		return ADDA_GB300_EINVAL;
 	}

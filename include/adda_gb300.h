@@ -141,6 +141,13 @@ typedef struct {
 	                                sides still running (-chpoint <time>); 0 = none */
 	int full_steps;              /* BiCGStab: no exit at the half step (the reference with -chp_type always,
 	                                iterative.c:703), so that the final state is a complete iteration */
+	double final_eps;            /* MIXED: FP64 relative residual at which the refinement loop stops, 0 < final_eps
+	                                <= eps; 0 = the default, 0.3*eps (0.1*eps for BiCGStab and BCGS2). The solve
+	                                succeeds once the residual meets eps; the margin below eps makes the cross
+	                                sections as accurate as a converged FP64 solve's to about 1e-6, which a solution
+	                                that only just meets a residual of 1e-5 is not (on the 128^3 sphere the FP64
+	                                solve at eps 1e-5 is 6e-6 off the converged Cabs, and the reference's own run
+	                                too) */
 } adda_gb300_solve_params;
 
 typedef struct {
@@ -337,14 +344,17 @@ int adda_gb300_vjp_chi(adda_gb300_ctx *ctx, const adda_gb300_solve_params *sp, i
 
 /* Allocation-free variant of adda_gb300_cross_sections; it has no counterpart in the reference (whose host never
  * runs where allocation is forbidden). For callers that cannot call cudaMalloc at this point: code running inside a
- * framework that owns all device memory through its own pool, or a sequence being recorded into a CUDA graph.
+ * framework that owns all device memory through its own pool allocator, or a plugin whose host forbids device
+ * allocation after start-up. Free space only (plane-wave ExtCross and AbsCross, crosssec.c:811-822,866-882): for a
+ * particle near a substrate use adda_gb300_cross_sections_beam.
  * Everything is passed as device pointers: polarisations d_pvec [nrhs][ndip][3] double2, d_position [ndip][3],
- * d_material [ndip] (or NULL for one material), polarisabilities d_cc [nrhs][nmat][3] (per_dipole=0) or
- * [nrhs][ndip][3] (per_dipole=1) double2, d_prop/d_incpol [nrhs][3]; results to d_cext/d_cabs [nrhs]. The call is
- * asynchronous on `stream` (a cudaStream_t, or NULL) and allocates nothing: its partial sums live in a 1 MiB static
- * device array (256 partials x 8 doubles x ADDA_GB300_NOALLOC_MAX_RHS) that every GPU loading the library holds until
- * exit. The first call on a device looks up that array's address (do it before any stream capture). All calls share
- * the array: calls that overlap on the GPU race. nrhs > ADDA_GB300_NOALLOC_MAX_RHS is rejected (ADDA_GB300_EINVAL). */
+ * d_material [ndip] (or NULL for one material; every index must be below nmat, else that RHS's Cabs is NaN),
+ * polarisabilities d_cc [nrhs][nmat][3] (per_dipole=0) or [nrhs][ndip][3] (per_dipole=1) double2,
+ * d_prop/d_incpol [nrhs][3]; results to d_cext/d_cabs [nrhs]. The call is asynchronous on `stream` (a cudaStream_t,
+ * or NULL) and allocates nothing: its partial sums live in a 1 MiB static device array (256 partials x 8 doubles x
+ * ADDA_GB300_NOALLOC_MAX_RHS) that every GPU loading the library holds until exit. The first call on a device looks
+ * up that array's address (make it before any stream capture). All calls share the array: calls that overlap on the
+ * GPU race. nrhs > ADDA_GB300_NOALLOC_MAX_RHS is rejected (ADDA_GB300_EINVAL). */
 #define ADDA_GB300_NOALLOC_MAX_RHS 64
 int adda_gb300_cross_sections_noalloc(int nrhs, size_t ndip, const void *d_pvec, const uint16_t *d_position,
 	const uint8_t *d_material, const void *d_cc, int nmat, int per_dipole, int boxX, int boxY, int boxZ,

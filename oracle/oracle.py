@@ -27,8 +27,15 @@ def build(force=False):
     return LIB_PATH
 
 
-def build_reference(ref_src="/root/reference/src"):
+def ref_src_dir():
+    """Where the reference's sources are read: $ADDA_REF_SRC, else a reference checkout beside this repository
+    (<repository>/../reference/src)."""
+    return os.environ.get("ADDA_REF_SRC") or os.path.normpath(os.path.join(HERE, "..", "..", "reference", "src"))
+
+
+def build_reference(ref_src=None):
     """Compile the unmodified reference sequential build with the FFTW-subset shim into oracle/_ref/adda."""
+    ref_src = ref_src or ref_src_dir()
     if not os.path.isdir(ref_src):
         return None
     subprocess.run(["make", "-s", "-C", HERE, "ref", "REF_SRC=" + ref_src, "-j8"], check=True)

@@ -37,11 +37,11 @@ def cross(rundir):
     return {q: float(re.search(q + r"\s*=\s*([-+0-9.eE]+)", txt).group(1)) for q in ("Cext", "Cabs")}
 
 
-def main(ref_src="/root/reference/src"):
+def main(ref_src=None):
     from oracle import oracle as O
     binp = O.build_reference(ref_src)
     if not binp:
-        raise SystemExit("reference sources not found at " + ref_src)
+        raise SystemExit("reference sources not found at " + (ref_src or O.ref_src_dir()))
     out_dir = os.path.join(HERE, "chpoint")
     os.makedirs(out_dir, exist_ok=True)
     cases = []

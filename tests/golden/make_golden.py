@@ -192,11 +192,11 @@ def parse_run(rundir, stdout):
     return out
 
 
-def main(ref_src="/root/reference/src"):
+def main(ref_src=None):
     from oracle import oracle as O
     binp = O.build_reference(ref_src)
     if not binp:
-        raise SystemExit("reference sources not found at " + ref_src)
+        raise SystemExit("reference sources not found at " + (ref_src or O.ref_src_dir()))
     results = []
     with tempfile.TemporaryDirectory() as tmp:
         for name, args, kw in CASES:

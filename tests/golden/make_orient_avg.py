@@ -40,11 +40,11 @@ def avg_file(path, kind):
                 name, lo, hi, jmin, jmax, eps, "true" if eq else "false", "true" if per else "false"))
 
 
-def main(ref_src="/root/reference/src"):
+def main(ref_src=None):
     from oracle import oracle as O
     binp = O.build_reference(ref_src)
     if not binp:
-        raise SystemExit("reference sources not found at " + ref_src)
+        raise SystemExit("reference sources not found at " + (ref_src or O.ref_src_dir()))
     out = []
     with tempfile.TemporaryDirectory() as tmp:
         for name, args, setup, kind in CASES:

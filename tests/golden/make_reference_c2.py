@@ -52,7 +52,7 @@ def main(argv):
         write({"qmr": parse(argv[1]), "bicgstab": parse(argv[2])})
         return
     from oracle import oracle as O
-    binp = O.build_reference(argv[0] if argv else "/root/reference/src")
+    binp = O.build_reference(argv[0] if argv else None)
     if not binp:
         raise SystemExit("reference sources not found")
     with tempfile.TemporaryDirectory() as tmp:

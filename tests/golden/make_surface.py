@@ -74,13 +74,13 @@ def read_beam(path):
     return (a[:, 4::2] + 1j * a[:, 5::2]), a[:, :3]
 
 
-def main(ref_src="/root/reference/src"):
+def main(ref_src=None):
     from oracle import oracle as O
     import adda_gb300 as A
     binp = O.build_reference(ref_src)
     if not binp:
-        raise SystemExit("reference sources not found at " + ref_src)
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "som", "REF_SRC=" + ref_src], check=True)
+        raise SystemExit("reference sources not found at " + (ref_src or O.ref_src_dir()))
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "som", "REF_SRC=" + (ref_src or O.ref_src_dir())], check=True)
     somlib = os.path.join(ROOT, "oracle", "_ref", "libsomnec.so")
     out = []
     with tempfile.TemporaryDirectory() as tmp:

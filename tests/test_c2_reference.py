@@ -2,9 +2,12 @@
 made by tests/golden/make_reference_c2.py): inputs on the CPU, solves on the GPU.
 
 At eps = 1e-5 a solution is only determined to the residual: the reference's two methods themselves differ by up to
-4e-6 in Cext for the X polarisation (5377.4954 QMR_CS against 5377.4755 BiCGStab). The solves here are compared at
-1e-5 relative in Cext and Cabs, must meet the FP64 residual, and their iteration counts must be within 15 % of the
-reference's (QMR_CS sits on a residual plateau near 1e-5 for tens of iterations, so rounding moves its exit point).
+4e-6 in Cext and 1e-5 in Cabs for the X polarisation (5377.4954 QMR_CS against 5377.4755 BiCGStab), and its QMR_CS
+run is 6e-6 from the converged Cabs. The mixed solves are therefore held to two bars: within 1e-6 of the converged
+cross sections of the reference's own solve to residual 1e-8 (reference_c2_converged.json, the spec accuracy
+bar), and within 1e-5 of its runs at eps 1e-5. They must meet the FP64 residual, and take between 0.85 and 1.3 times
+the reference's iterations to 1e-5 (the mixed refinement stops at 0.3 eps for QMR_CS and 0.1 eps for BiCGStab, for
+the accuracy of the cross sections).
 """
 import json
 import os
@@ -50,5 +53,11 @@ def test_c2_mixed_solve_matches_reference(method):
         assert st[r]["status"] == "ok" and st[r]["resid"] <= 1e-5
         assert abs(ce[r] / ref["cross"][pol]["Cext"] - 1) < 1e-5, (pol, ce[r], ref["cross"][pol])
         assert abs(ca[r] / ref["cross"][pol]["Cabs"] - 1) < 1e-5, (pol, ca[r], ref["cross"][pol])
-        assert abs(st[r]["niter"] / ref["niter"][pol] - 1) < 0.15, (pol, st[r]["niter"], ref["niter"][pol])
+        assert 0.85 < st[r]["niter"] / ref["niter"][pol] < 1.3, (pol, st[r]["niter"], ref["niter"][pol])
+    conv = os.path.join(HERE, "golden", "reference_c2_converged.json")
+    if os.path.exists(conv):
+        c = json.load(open(conv))["converged"]
+        for r in range(2):
+            assert abs(ce[r] / c["Cext"] - 1) < 1e-6, (r, ce[r], c["Cext"])
+            assert abs(ca[r] / c["Cabs"] - 1) < 1e-6, (r, ca[r], c["Cabs"])
     ctx.close()

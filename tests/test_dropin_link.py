@@ -7,8 +7,9 @@ import subprocess
 import pytest
 
 from conftest import ROOT, have_gpu
+from oracle.oracle import ref_src_dir
 
-REF_SRC = "/root/reference/src"
+REF_SRC = ref_src_dir()
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference sources not present")

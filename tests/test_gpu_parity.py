@@ -9,8 +9,8 @@ Tolerances:
     near the threshold (checked on the CPU: 1e-16 noise moves the 16^3 sphere between 43 and 49 iterations). So
     cross sections are compared with 2e-6 relative, iteration counts within +-6, and residual histories while the
     residual is above 1e-2.
-  - Mixed precision: the FP64-recomputed residual meets eps, and Cext/Cabs are within 2e-6 of the converged
-    (eps=1e-10) FP64 oracle and within 3e-6 of the FP64 oracle at the same eps.
+  - Mixed precision: the FP64-recomputed residual meets eps, and Cext/Cabs are within 1e-6 of the converged
+    (eps=1e-10) FP64 oracle (the refinement stops below eps for that, see final_eps in the C ABI).
 """
 import numpy as np
 import pytest
@@ -200,8 +200,8 @@ def test_solve_fp64_vs_oracle_tight(method):
 @pytest.mark.parametrize("method", ["qmr", "bicgstab"])
 @pytest.mark.parametrize("name", ["c1_qmr", "ell24", "c2_small"])
 def test_solve_mixed(name, method, prec):
-    """mixed precision: the FP64 recomputed residual meets eps; cross sections within 2e-6 of the converged FP64
-    oracle and within 3e-6 of the FP64 oracle at the same eps"""
+    """mixed precision: the FP64 recomputed residual meets eps; cross sections within 1e-6 of the converged FP64
+    oracle (Cabs relative to max(Cabs, Cext): for a real index it is zero up to rounding)"""
     import adda_gb300 as A
     c0 = case(name)
     s = setup_for(c0["setup"])
@@ -214,11 +214,9 @@ def test_solve_mixed(name, method, prec):
         assert st["status"] == "ok", st
         assert st["resid"] <= 1e-5
         assert st["matvecs_fp64"] >= 1
-        ro = oracle_solve(o, s, r, method=method, eps=1e-5)
         rc = oracle_solve(o, s, r, method=method, eps=1e-10)
-        assert abs(ce[r] / rc["Cext"] - 1) < 2e-6, (ce[r], rc["Cext"])
-        assert abs(ca[r] - rc["Cabs"]) < 2e-6 * max(abs(rc["Cabs"]), abs(rc["Cext"]))
-        assert abs(ce[r] / ro["Cext"] - 1) < 3e-6, (ce[r], ro["Cext"])
+        assert abs(ce[r] / rc["Cext"] - 1) < 1e-6, (ce[r], rc["Cext"])
+        assert abs(ca[r] - rc["Cabs"]) < 1e-6 * max(abs(rc["Cabs"]), abs(rc["Cext"])), (ca[r], rc["Cabs"])
 
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
@@ -245,8 +243,8 @@ def test_solve_from_x0(prec):
 @pytest.mark.parametrize("method", ["bicg", "cgnr", "csym", "qmr2", "bcgs2"])
 @pytest.mark.parametrize("name", ["c1_qmr", "ell24"])
 def test_solve_mixed_other_methods(name, method):
-    """BiCG_CS, CGNR and CSYM in mixed precision (double-float vectors): FP64 residual meets eps, cross sections within
-    2e-6 of the converged FP64 oracle"""
+    """BiCG_CS, CGNR, CSYM, QMR_CS_2 and BCGS2 in mixed precision (double-float vectors): FP64 residual meets eps,
+    cross sections within 1e-6 of the converged FP64 oracle"""
     import adda_gb300 as A
     s = setup_for(case(name)["setup"])
     o = oracle_for(s)
@@ -257,8 +255,8 @@ def test_solve_mixed_other_methods(name, method):
         st = res["stats"][r]
         assert st["status"] == "ok" and st["resid"] <= 1e-5, st
         rc = oracle_solve(o, s, r, method="qmr", eps=1e-10)
-        assert abs(ce[r] / rc["Cext"] - 1) < 2e-6, (ce[r], rc["Cext"])
-        assert abs(ca[r] - rc["Cabs"]) < 2e-6 * max(abs(rc["Cabs"]), abs(rc["Cext"]))
+        assert abs(ce[r] / rc["Cext"] - 1) < 1e-6, (ce[r], rc["Cext"])
+        assert abs(ca[r] - rc["Cabs"]) < 1e-6 * max(abs(rc["Cabs"]), abs(rc["Cext"])), (ca[r], rc["Cabs"])
 
 
 def test_cross_sections_from_pvec():
