@@ -35,10 +35,12 @@ class Problem(ctypes.Structure):
                 ("device", ctypes.c_int), ("interaction", ctypes.c_int), ("nloc_rp", ctypes.c_double),
                 ("surface", ctypes.c_int), ("zsum_shift", ctypes.c_double), ("msub_re", ctypes.c_double),
                 ("msub_im", ctypes.c_double), ("msub_inf", ctypes.c_int), ("refl", ctypes.c_int),
-                ("refl_data", ctypes.c_void_p)]
+                ("refl_data", ctypes.c_void_p), ("int_tables", ctypes.c_void_p), ("so_m_re", ctypes.c_double),
+                ("so_m_im", ctypes.c_double)]
 
 
-INTERACTIONS = {"poi": 0, "fcd": 1, "fcd_st": 2, "nloc": 3, "nloc_av": 4}
+INTERACTIONS = {"poi": 0, "fcd": 1, "fcd_st": 2, "nloc": 3, "nloc_av": 4, "igt_so": 5, "so": 6}
+INT_TABLES = 11928  # doubles of the igt_so / so integral tables
 # -int_surf: image dipole (GPU), image + Sommerfeld integrals from a table, or a tensor supplied by the caller
 REFL = {"img": 0, "som": 1, "host": 2}
 
@@ -104,7 +106,7 @@ EXPORTS = ["adda_gb300_fft_fit", "adda_gb300_fit_box", "adda_gb300_make_particle
            "adda_gb300_rmatrix_len", "adda_gb300_get_rmatrix", "adda_gb300_cross_sections_beam",
            "adda_gb300_cross_sections", "adda_gb300_scattered_fields", "adda_gb300_integr_points",
            "adda_gb300_romberg2d", "adda_gb300_romberg2d_ex", "adda_gb300_scattering_integrals",
-           "adda_gb300_cross_sections_noalloc", "adda_gb300_time_matvec",
+           "adda_gb300_cross_sections_noalloc", "adda_gb300_time_matvec", "adda_gb300_read_int_tables",
            "adda_gb300_last_solve_ms", "adda_gb300_last_error", "adda_gb300_kernel_launches"]
 
 _lib = None
@@ -172,6 +174,7 @@ def load_library(path):
         "adda_gb300_cross_sections": ([P, I, P, P, P, P], I),
         "adda_gb300_scattered_fields": ([P, I, I, P, P], I),
         "adda_gb300_cross_sections_noalloc": ([I, SZ, P, P, P, P, I, I, I, I, I, D, D, P, P, P, P, P], I),
+        "adda_gb300_read_int_tables": ([ctypes.c_char_p, P], I),
         "adda_gb300_last_error": ([], ctypes.c_char_p),
         "adda_gb300_last_solve_ms": ([P], D),
         "adda_gb300_kernel_launches": ([], ctypes.c_uint64),
@@ -198,6 +201,14 @@ def kernel_launches():
 
 # ---------------------------------------------------------------------------------------------------------------------
 # host-side inputs (no GPU)
+
+def read_int_tables(directory):
+    """the integral tables of -int igt_so / so (the reference's input/tables/t1f.dat .. t10f.dat) as one array"""
+    out = np.zeros(INT_TABLES)
+    if lib().adda_gb300_read_int_tables(os.fsencode(directory), _p(out)):
+        raise AddaError("read_int_tables: missing or short table files in " + str(directory))
+    return out
+
 
 def fft_fit(x, divis=1):
     return lib().adda_gb300_fft_fit(int(x), int(divis))
@@ -306,8 +317,10 @@ class Setup:
     Order of the RHS: Y polarisation first, then X (calculator.c:309-330)."""
 
     def __init__(self, grid=16, shape="sphere", pars=None, m=1.5, dpl=None, size=None, pol="ldr", orient=(0, 0, 0),
-                 avgpol=False, prop=None, lam=2 * math.pi, interaction="poi", nloc_rp=0.0, pol_rp=0.0, surface=None):
+                 avgpol=False, prop=None, lam=2 * math.pi, interaction="poi", nloc_rp=0.0, pol_rp=0.0, surface=None,
+                 int_tables=None):
         self.interaction = interaction
+        self.int_tables = int_tables  # -int igt_so | so: the integral tables (read_int_tables)
         self.nloc_rp = float(nloc_rp)
         self.pol, self.avgpol, self.pol_rp, self.prop0 = pol, avgpol, pol_rp, prop
         self.box, self.pos, self.mat = make_particle(shape, grid, pars)
@@ -410,7 +423,7 @@ class Context:
     """One particle lattice on one GPU: the interaction matrix, FP64/FP32 matvecs, solver and cross sections."""
 
     def __init__(self, box, pos, mat, gridspace, wavenum, grid=(0, 0, 0), nrhs_max=2, device=0, interaction="poi",
-                 nloc_rp=0.0, library=None, surface=None):
+                 nloc_rp=0.0, library=None, surface=None, int_tables=None, so_m=0.0):
         self.L = library or lib()
         self.pos = np.ascontiguousarray(pos, dtype=np.uint16).reshape(-1, 3)
         self.mat = None if mat is None else np.ascontiguousarray(mat, dtype=np.uint8)
@@ -419,6 +432,12 @@ class Context:
         pr = Problem(box[0], box[1], box[2], grid[0], grid[1], grid[2], self.n, _p(self.pos).value,
                      None if self.mat is None else _p(self.mat).value, gridspace, wavenum, nrhs_max, device,
                      INTERACTIONS[interaction], nloc_rp)
+        # igt_so / so: the integral tables and (so) the refractive index of the second-order terms
+        self._tables = None
+        if int_tables is not None:
+            self._tables = np.ascontiguousarray(int_tables, dtype=np.float64)
+            pr.int_tables = _p(self._tables).value
+            pr.so_m_re, pr.so_m_im = complex(so_m).real, complex(so_m).imag
         # surface: dict(zsum_shift, msub (None = perfect reflector), relation img|som|host, data (complex array))
         self._refl = None
         if surface is not None:
@@ -437,7 +456,8 @@ class Context:
     @classmethod
     def from_setup(cls, s, nrhs_max=2, device=0, library=None):
         c = cls(s.box, s.pos, s.mat, s.gridspace, s.wavenum, s.grid, nrhs_max, device, s.interaction,
-                getattr(s, "nloc_rp", 0.0), library, getattr(s, "surface", None))
+                getattr(s, "nloc_rp", 0.0), library, getattr(s, "surface", None), getattr(s, "int_tables", None),
+                getattr(s, "m", 0.0))
         c.init_dmatrix()
         for r in range(min(nrhs_max, len(s.cc))):
             c.set_cc(r, s.cc[r].reshape(1, 3))

@@ -115,9 +115,17 @@ static int create_impl(const adda_gb300_problem *p, adda_gb300_ctx *c)
 	c->Rmax = p->nrhs_max > 0 ? p->nrhs_max : 1;
 	c->gridspace = p->gridspace;
 	c->k = p->wavenum;
-	if (p->interaction < ADDA_INT_POI || p->interaction > ADDA_INT_NLOC_AV || !(p->nloc_rp >= 0)) {
+	if (p->interaction < ADDA_INT_POI || p->interaction > ADDA_INT_SO || !(p->nloc_rp >= 0)) {
 		set_error("create: unknown interaction term or negative Gaussian width");
 		return ADDA_GB300_EINVAL;
+	}
+	if (p->interaction == ADDA_INT_IGT_SO || p->interaction == ADDA_INT_SO) {
+		if (!p->int_tables) {
+			set_error("create: the igt_so and so interaction terms need the integral tables (problem.int_tables)");
+			return ADDA_GB300_EINVAL;
+		}
+		c->int_tables.assign(p->int_tables, p->int_tables + ADDA_GB300_INT_TABLES);
+		c->so_m = make_double2(p->so_m_re, p->so_m_im);
 	}
 	if ((p->interaction == ADDA_INT_FCD || p->interaction == ADDA_INT_FCD_ST) &&
 		!(p->wavenum * p->gridspace < 3.14159265358979323846)) {

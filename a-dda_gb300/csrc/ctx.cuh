@@ -60,6 +60,8 @@ struct adda_gb300_ctx {
 	int Rmax = 1;
 	int interaction = 0; // enum adda_gb300_inter
 	double nloc_rp = 0;  // Gaussian width of the non-local interaction
+	std::vector<double> int_tables; // IGT_SO / SO: the integral tables t1..t10 back to back
+	double2 so_m = {0, 0};          // SO: refractive index of the second-order terms
 	// particle near a substrate: reflected interaction R~, layout [gX][gZ][gY/2+1][6]
 	int surface = 0, refl = 0, msub_inf = 0;
 	double zsum_shift = 0;

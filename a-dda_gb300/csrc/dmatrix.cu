@@ -16,6 +16,9 @@
 // This runs once per particle; it is written for clarity over speed (it costs a few FP64 3-D FFTs).
 #include "ctx.cuh"
 
+#include <cmath>
+#include <vector>
+
 namespace adda {
 
 namespace {
@@ -97,8 +100,119 @@ __device__ double average_gauss_cube(double x, double d, double rp)
 	return dif / d;
 }
 
+// ---- the tabulated terms IGT_SO and SO (InterTerm_igt_so_int, InterTerm_so_int; interaction.c:431-579, 711-941) ----
+
+constexpr int TAB_RMAX = 10, TAB_SIZE = 142;
+// start of t1..t10 in the flat table array (values per entry 1, 6, 3, 18, 6, 36, 1, 6, 1, 6)
+__constant__ int TAB_OFF[10] = {0, 142, 994, 1420, 3976, 4828, 9940, 10082, 10934, 11076};
+
+struct IgtTables {
+	const double *t;  // the flat tables (device)
+	const int *index; // [TAB_RMAX+1][TAB_RMAX+1]: entry of (i, j, 0), i >= j
+	double2 m;        // SO: refractive index of the m^2 terms
+};
+
+__device__ __forceinline__ double2 zmul(double2 a, double2 b)
+{
+	return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// g holds the point-dipole tensor of offset (i,j,k) on entry. Pairs with kd*rn^2 < 1 and rn <= 10 take the tabulated
+// integrals of the Green's tensor over the two cubes: the offset is mapped onto i >= j >= k >= 0 (a sign per axis,
+// the axes ordered by decreasing coordinate with the reference's tie order) and each component (mu,nu) reads the
+// table entries of the mapped axes; SO adds its orientation-averaged m^2 term. Other pairs: the point-dipole tensor
+// times 1 - kd^2/24 (SO: 1 - (1+m^2) kd^2/24) plus, for kr < 1, the median correction
+// (-1 + ikr) 7/(64 rn^4) [qq(33 q4 - 7 - 12(q_mu^2 + q_nu^2)) + delta(1 - 3 q4 + 4 q_mu^2)] exp(ikr)/r^3.
+__device__ void green_igt(double2 g[6], int i, int j, int k, double rn, const double q[3], const double qm[6], double kr,
+	double kd, double2 ev, bool so, const IgtTables &tb)
+{
+	const int cmu[6] = {0, 0, 0, 1, 1, 2}, cnu[6] = {0, 1, 2, 1, 2, 2};
+	const double kr2 = kr * kr, kd2 = kd * kd;
+	const double2 m2 = zmul(tb.m, tb.m);
+	if (kr * rn < 1 && rn <= TAB_RMAX) {
+		int v[3] = {i, j, k};
+		double s[3], qa[3];
+		for (int a = 0; a < 3; a++) {
+			s[a] = v[a] < 0 ? -1 : 1;
+			v[a] = abs(v[a]);
+			qa[a] = q[a] * s[a];
+		}
+		int o0, o1, o2; // axis of the largest, middle and smallest coordinate
+		if (v[0] >= v[1]) {
+			if (v[0] >= v[2]) { o0 = 0; if (v[1] >= v[2]) { o1 = 1; o2 = 2; } else { o1 = 2; o2 = 1; } }
+			else { o0 = 2; o1 = 0; o2 = 1; }
+		}
+		else {
+			if (v[0] >= v[2]) { o0 = 1; o1 = 0; o2 = 2; }
+			else { o2 = 0; if (v[1] >= v[2]) { o0 = 1; o1 = 2; } else { o0 = 2; o1 = 1; } }
+		}
+		int rank[3];
+		rank[o0] = 0; rank[o1] = 1; rank[o2] = 2;
+		const double qp0 = qa[o0], qp1 = qa[o1], qp2 = qa[o2];
+		const int e0 = tb.index[v[o0] * (TAB_RMAX + 1) + v[o1]] + v[o2];
+		const double *t = tb.t;
+		const double *t3 = t + TAB_OFF[2] + 3 * e0, *t5 = t + TAB_OFF[4] + 6 * e0;
+		const double t3q = qp0 * t3[0] + qp1 * t3[1] + qp2 * t3[2];
+		const double t5tr = t5[0] + t5[2] + t5[5];
+		for (int a = 0; a < 6; a++) {
+			const int mu = cmu[a], nu = cnu[a];
+			const bool diag = mu == nu;
+			const double sig = s[mu] * s[nu];
+			const int r1 = rank[mu], r2 = rank[nu];
+			const int e2 = 6 * e0 + r1 + r2 + ((r1 == 2 || r2 == 2) ? 1 : 0); // symmetric order xx,xy,yy,xz,yz,zz
+			const double *t4 = t + TAB_OFF[3] + 3 * e2, *t6 = t + TAB_OFF[5] + 6 * e2;
+			const double t4q = qp0 * t4[0] + qp1 * t4[1] + qp2 * t4[2];
+			const double t6tr = t6[0] + t6[2] + t6[5];
+			// kd^2 [sig (3 (I10/2 + I8) - 2 t4q - t6tr) + (kr/24) qq (kr + 3i) + delta (2 t3q + t5tr - (kr/24)(kr + i)
+			//       - I9/2 - I7)] + sig I2 (3 - 3i kr - kr^2) + delta I1 (-1 + i kr + kr^2)
+			double br = sig * (3 * (t[TAB_OFF[9] + e2] / 2 + t[TAB_OFF[7] + e2]) - 2 * t4q - t6tr) + kr * kr * qm[a] / 24;
+			double bi = kr * 3 * qm[a] / 24;
+			if (diag) {
+				br += 2 * t3q + t5tr - kr * kr / 24 - t[TAB_OFF[8] + e0] / 2 - t[TAB_OFF[6] + e0];
+				bi -= kr / 24;
+			}
+			br *= kd2;
+			bi *= kd2;
+			const double i2 = sig * t[TAB_OFF[1] + e2];
+			br += i2 * (3 - kr2);
+			bi -= i2 * 3 * kr;
+			if (diag) {
+				const double i1 = t[TAB_OFF[0] + e0];
+				br += i1 * (kr2 - 1);
+				bi += i1 * kr;
+			}
+			g[a] = zmul(ev, make_double2(br, bi));
+			if (so) { // (kd^2/2) m^2 [delta t5tr/3 - sig t6tr + (kr/12)((kr + 3i) qq - delta (kr + i))]
+				double cr = kr * (kr * qm[a]) / 12 - sig * t6tr, ci = kr * 3 * qm[a] / 12;
+				if (diag) {
+					cr += t5tr / 3 - kr * kr / 12;
+					ci -= kr / 12;
+				}
+				const double2 w = zmul(zmul(ev, m2), make_double2(kd2 / 2 * cr, kd2 / 2 * ci));
+				g[a] = make_double2(g[a].x + w.x, g[a].y + w.y);
+			}
+		}
+		return;
+	}
+	const double2 f = so ? make_double2(1 - (1 + m2.x) * kd2 / 24, -m2.y * kd2 / 24) : make_double2(1 - kd2 / 24, 0);
+	for (int a = 0; a < 6; a++) g[a] = zmul(g[a], f);
+	if (kr < 1) {
+		const double q2[3] = {q[0] * q[0], q[1] * q[1], q[2] * q[2]};
+		const double q4 = q2[0] * q2[0] + q2[1] * q2[1] + q2[2] * q2[2];
+		const double invrn4 = 1 / (rn * rn * rn * rn);
+		const double2 em = zmul(ev, make_double2(-1, kr));
+		for (int a = 0; a < 6; a++) {
+			const int mu = cmu[a], nu = cnu[a];
+			double tt = qm[a] * (33 * q4 - 7 - 12 * (q2[mu] + q2[nu]));
+			if (mu == nu) tt += 1 - 3 * q4 + 4 * q2[mu];
+			tt *= 7 * invrn4 / 64;
+			g[a] = make_double2(g[a].x + em.x * tt, g[a].y + em.y * tt);
+		}
+	}
+}
+
 __global__ void green_fill(double2 *G, int bX, int bY, int bZ, int gX, double gridspace, double k, int inter,
-	double rp)
+	double rp, IgtTables tb)
 {
 	const size_t lines = (size_t)bZ * bY;
 	const size_t total = lines * gX;
@@ -163,6 +277,10 @@ __global__ void green_fill(double2 *G, int bX, int bY, int bZ, int gX, double gr
 					if (a == 0 || a == 3 || a == 5) re -= t1 + t2;
 					g[a] = make_double2(re, 0);
 				}
+			}
+			else if (inter == ADDA_INT_IGT_SO || inter == ADDA_INT_SO) {
+				const double q[3] = {q0, q1, q2};
+				green_igt(g, i, j, kk, rn, q, qm, kr, k * gridspace, make_double2(evr, evi), inter == ADDA_INT_SO, tb);
 			}
 			else if (inter) {
 				// FCD corrections of the real part (InterTerm_fcd / _fcd_st, interaction.c:335-411): k_F = pi/d
@@ -479,9 +597,39 @@ int dmatrix_build(adda_gb300_ctx *c)
 		return ADDA_GB300_ENOMEM;
 	}
 	const double invN = 1.0 / (gX * ((double)gY * gZ));
+	// IGT_SO / SO: the integral tables and the entry index of (i, j, 0) (ReadTables, interaction.c:1051-1061: row
+	// (i, j) holds k = 0..min(j, floor(sqrt(RMAX^2 - i^2 - j^2))))
+	IgtTables tb{nullptr, nullptr, c->so_m};
+	double *d_tabs = nullptr;
+	int *d_index = nullptr;
+	if (!c->int_tables.empty()) {
+		std::vector<int> index((TAB_RMAX + 1) * (TAB_RMAX + 1), 0);
+		int next = 0;
+		for (int i = 1; i <= TAB_RMAX; i++)
+			for (int j = 0; j <= i && i * i + j * j <= TAB_RMAX * TAB_RMAX; j++) {
+				index[i * (TAB_RMAX + 1) + j] = next;
+				next += std::min(j, (int)std::floor(std::sqrt((double)(TAB_RMAX * TAB_RMAX - i * i - j * j)))) + 1;
+			}
+		if (next != TAB_SIZE || cudaMalloc(&d_tabs, sizeof(double) * c->int_tables.size()) != cudaSuccess ||
+			cudaMalloc(&d_index, sizeof(int) * index.size()) != cudaSuccess ||
+			cudaMemcpyAsync(d_tabs, c->int_tables.data(), sizeof(double) * c->int_tables.size(),
+				cudaMemcpyHostToDevice, c->stream) != cudaSuccess ||
+			cudaMemcpyAsync(d_index, index.data(), sizeof(int) * index.size(), cudaMemcpyHostToDevice, c->stream) !=
+				cudaSuccess ||
+			cudaStreamSynchronize(c->stream) != cudaSuccess) {
+			cudaFree(G);
+			cudaFree(S);
+			cudaFree(d_tabs);
+			cudaFree(d_index);
+			set_error("cannot stage the integral tables of the interaction term");
+			return ADDA_GB300_ENOMEM;
+		}
+		tb.t = d_tabs;
+		tb.index = d_index;
+	}
 	do {
 		green_fill<<<grid_for(gsz), 256, 0, c->stream>>>(G, bX, bY, bZ, gX, c->gridspace, c->k, c->interaction,
-			c->nloc_rp);
+			c->nloc_rp, tb);
 		count_launch();
 		if (cudaGetLastError() != cudaSuccess) { rc = ADDA_GB300_ECUDA; break; }
 		// x transform of all 6*bZ*bY lines (contiguous, length gX)
@@ -509,6 +657,8 @@ int dmatrix_build(adda_gb300_ctx *c)
 	if (rc == ADDA_GB300_ECUDA) set_error(std::string("D-matrix build: ") + cudaGetErrorString(cudaGetLastError()));
 	cudaFree(G);
 	cudaFree(S);
+	cudaFree(d_tabs);
+	cudaFree(d_index);
 	if (!rc && c->surface) rc = rmatrix_build(c);
 	if (!rc) c->dready = true;
 	return rc;

@@ -12,10 +12,10 @@
  * Environment (the reference's command line is left unchanged):
  *   ADDA_GB300_PREC=fp64|mixed   arithmetic of IterativeSolver (default fp64, the reference's)
  *   ADDA_GB300_DEVICE=<n>        CUDA device (default 0)
- * Supported: -int poi|fcd|fcd_st|nloc|nloc_av (with every -pol the host computes), -surf with -int_surf img|som
+ * Supported: -int poi|fcd|fcd_st|nloc|nloc_av|igt_so|so (with every -pol the host computes), -surf with -int_surf img|som
  * (the reflected tensor comes from the host's ReflTerm_int), every -iter method, -init_field auto|zero|inc|read|wkb,
  * -chpoint/-chp_load (FP64), and the scattered fields of CalcField, CalcAlldir and CalcScatGrid (free space).
- * Refused with the reference's LogError: -int igt|igt_so|so, -no_reduced_fft, more than one MPI process.
+ * Refused with the reference's LogError: -int igt, -no_reduced_fft, more than one MPI process.
  */
 #include "adda_gb300.h"
 #include "adda_dropin.h"
@@ -112,8 +112,12 @@ void InitDmatrix(void)
 	else if (IntRelation == G_FCD_ST) inter = ADDA_INT_FCD_ST;
 	else if (IntRelation == G_NLOC) inter = ADDA_INT_NLOC;
 	else if (IntRelation == G_NLOC_AV) inter = ADDA_INT_NLOC_AV;
-	else ERR("The GPU build supports the interaction terms -int poi|fcd|fcd_st|nloc|nloc_av only");
-	if (!reduced_FFT) ERR("The GPU build requires the reduced FFT (do not use -no_reduced_fft)");
+	else if (IntRelation == G_IGT_SO) inter = ADDA_INT_IGT_SO;
+	else if (IntRelation == G_SO) inter = ADDA_INT_SO;
+	else ERR("The GPU build supports the interaction terms -int poi|fcd|fcd_st|nloc|nloc_av|igt_so|so only");
+	/* -int so turns the reduced FFT off in the reference (param.c:1992-1996) for its general, non-averaged form; the
+	 * averaged form it uses has the point-dipole reflection symmetries, so the GPU keeps the reduced D for it */
+	if (!reduced_FFT && inter != ADDA_INT_SO) ERR("The GPU build requires the reduced FFT (do not use -no_reduced_fft)");
 	local_Nsmall = (gridX / 2) * (gridYZ / 2); /* fft.c:975 with nprocs=1 */
 	if (logfile) fprintf(logfile, "The FFT grid is: %zux%zux%zu\n", gridX, gridY, gridZ);
 	/* device memory of the matvec (D in FP64+FP32, expanded grid, chunk buffer) for the log */
@@ -133,6 +137,13 @@ void InitDmatrix(void)
 	p.nrhs_max = 1;
 	p.device = getenv("ADDA_GB300_DEVICE") ? atoi(getenv("ADDA_GB300_DEVICE")) : 0;
 	p.interaction = inter;
+	static double tables[ADDA_GB300_INT_TABLES];
+	if (inter == ADDA_INT_IGT_SO || inter == ADDA_INT_SO) { /* the reference reads tables/t*f.dat (const.h:274) */
+		if (adda_gb300_read_int_tables("tables", tables)) ERR("cannot read the integral tables tables/t1f.dat..t10f.dat");
+		p.int_tables = tables;
+		p.so_m_re = creal(ref_index[0]);
+		p.so_m_im = cimag(ref_index[0]);
+	}
 	p.nloc_rp = nloc_Rp;
 	doublecomplex *gr = NULL;
 	if (surface) {

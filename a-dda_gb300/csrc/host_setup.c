@@ -8,12 +8,14 @@
  *   adda_gb300_plane_wave       <- GenerateB, free-space plane wave         src/GenerateB.c:324-328
  *   adda_gb300_plane_wave_surf  <- GenerateB, plane wave near a substrate   src/GenerateB.c:96-140, 257-323
  *   adda_gb300_polarizability   <- CoupleConstant (CM, LDR, RRC, DGF)        src/calculator.c:100-262
+ *   adda_gb300_read_int_tables  <- ReadTables / ReadTableFile                src/interaction.c:1004-1063
  * All functions are pure host code: no GPU is touched.
  */
 #include "adda_gb300.h"
 
 #include <complex.h>
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -440,4 +442,29 @@ int adda_gb300_fft_fit(int x, int divis)
 		else if (y % 13 == 0) y /= 13;
 		if (y == 1) return x;
 	}
+}
+
+/* the integral tables of -int igt_so / so: files t1f.dat .. t10f.dat of dir, each TAB_SIZE = 142 entries times 1, 6,
+ * 3, 18, 6, 36, 1, 6, 1, 6 values (src/const.h:274-277), read as whitespace-separated doubles like ReadTableFile;
+ * extra values after the expected count are ignored */
+int adda_gb300_read_int_tables(const char *dir, double *tables)
+{
+	static const int mult[10] = {1, 6, 3, 18, 6, 36, 1, 6, 1, 6};
+	if (!dir || !tables) return ADDA_GB300_EINVAL;
+	size_t off = 0;
+	for (int t = 0; t < 10; t++) {
+		char fname[4096];
+		if (snprintf(fname, sizeof(fname), "%s/t%df.dat", dir, t + 1) >= (int)sizeof(fname)) return ADDA_GB300_EINVAL;
+		FILE *f = fopen(fname, "r");
+		if (!f) return ADDA_GB300_EINVAL;
+		const int n = 142 * mult[t];
+		for (int i = 0; i < n; i++)
+			if (fscanf(f, "%lf", tables + off + i) != 1) {
+				fclose(f);
+				return ADDA_GB300_EINVAL;
+			}
+		fclose(f);
+		off += (size_t)n;
+	}
+	return off == ADDA_GB300_INT_TABLES ? ADDA_GB300_OK : ADDA_GB300_EINVAL;
 }

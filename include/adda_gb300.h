@@ -77,12 +77,18 @@ enum adda_gb300_prec {
 	ADDA_PREC_MIXED_F32VEC = 3,
 	ADDA_PREC_MIXED_F64VEC = 4
 };
-/* interaction terms of the reference's -int (interaction.c:290-411,589-707): point dipoles, filtered coupled dipoles
- * (FCD, Gay-Balmaz & Martin / Piller) and its static limit, and the static non-local interaction of two Gaussian
+/* interaction terms of the reference's -int (interaction.c:290-411,431-941): point dipoles, filtered coupled dipoles
+ * (FCD, Gay-Balmaz & Martin / Piller) and its static limit, the static non-local interaction of two Gaussian
  * dipole densities of width Rp (problem.nloc_rp; nloc: point value of the non-locality function, nloc_av: its average
- * over the dipole cube); igt, igt_so and so are not provided */
+ * over the dipole cube), and the two terms built on the reference's tabulated integrals of the Green's tensor over
+ * the dipole cube (problem.int_tables): the approximate integrated Green's tensor igt_so (InterTerm_igt_so_int) and
+ * the second-order formulation so (InterTerm_so_int, in the reference's orientation-averaged form; its m^2 terms use
+ * problem.so_m). igt (a cubature per lattice offset) is not provided. */
 enum adda_gb300_inter { ADDA_INT_POI = 0, ADDA_INT_FCD = 1, ADDA_INT_FCD_ST = 2, ADDA_INT_NLOC = 3,
-	ADDA_INT_NLOC_AV = 4 };
+	ADDA_INT_NLOC_AV = 4, ADDA_INT_IGT_SO = 5, ADDA_INT_SO = 6 };
+/* the integral tables of igt_so and so: the reference's input/tables/t1f.dat .. t10f.dat back to back (142 entries of
+ * 1, 6, 3, 18, 6, 36, 1, 6, 1, 6 values each: 11928 doubles; ReadTables, interaction.c:1031-1063) */
+#define ADDA_GB300_INT_TABLES 11928
 /* -init_field: auto, zero, inc (CalcInitField, iterative.c:1342-1394), and X0: the starting vector x_0 is supplied by
  * the caller in xvec (host API) or d_xvec (device API) -- the reference's "read" and "wkb" modes, which turn an
  * electric field E into x_0 = E/(cc_sqrt*chi_inv) (InitFieldfromE, iterative.c:1325-1338; see
@@ -125,6 +131,10 @@ typedef struct {
 	int msub_inf;                /* perfectly reflecting substrate (reflection coefficient -1, image relation) */
 	int refl;                    /* enum adda_gb300_refl */
 	const double *refl_data;     /* SOM / HOST data (copied by adda_gb300_create), NULL for IMG */
+	/* interaction IGT_SO / SO: the integral tables (ADDA_GB300_INT_TABLES doubles, see adda_gb300_read_int_tables;
+	 * copied by adda_gb300_create), and SO's refractive index (the reference's ref_index[0]) */
+	const double *int_tables;
+	double so_m_re, so_m_im;
 } adda_gb300_problem;
 
 typedef struct {
@@ -159,6 +169,10 @@ typedef struct {
 } adda_gb300_rhs_stats;
 
 /* ---- particle-side inputs (host code, no GPU) --------------------------------------------------------------- */
+
+/* ReadTables / ReadTableFile, src/interaction.c:1004-1063: the ten files t1f.dat .. t10f.dat of directory dir (the
+ * reference's input/tables) into tables[ADDA_GB300_INT_TABLES]; EINVAL when a file is missing or too short */
+int adda_gb300_read_int_tables(const char *dir, double *tables);
 
 /* fftFit, src/fft.c:528-562: smallest even size >= x, divisible by divis, with prime factors 2,3,5,7 (+ one 11|13) */
 int adda_gb300_fft_fit(int x, int divis);

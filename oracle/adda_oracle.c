@@ -24,8 +24,12 @@ struct or_ctx {
 	uint16_t *pos;       // [n][3] grid coordinates
 	uint8_t *mat;        // [n] material index
 	double gridspace, k;
-	int inter;           // 0 point dipoles, 1 FCD, 2 static FCD, 3 non-local, 4 non-local (cube-averaged)
+	int inter;           // 0 point dipoles, 1 FCD, 2 static FCD, 3 non-local, 4 non-local (cube-averaged),
+	                     // 5 IGT_SO, 6 SO (tabulated integrals)
 	double rp;           // Gaussian width of the non-local interaction
+	double *tabs;        // IGT_SO / SO: the ten integral tables t1..t10 back to back (OR_TAB_TOTAL doubles)
+	int tab_index[OR_TAB_RMAX + 1][OR_TAB_RMAX + 1];
+	cplx so_m;           // SO: the refractive index in the second-order terms (ref_index[0])
 	size_t DsY, DsZ;     // reduced D sizes (fft.c:955-963)
 	cplx *D;             // [gX][DsZ][DsY][6]
 	int per_dip, nmat;
@@ -89,6 +93,7 @@ void or_free(or_ctx *c)
 	cfft_plan_free(&c->py);
 	cfft_plan_free(&c->pz);
 	free(c->pos); free(c->mat); free(c->D); free(c->X); free(c->ccd); free(c->ccsd); free(c->somt); free(c->R);
+	free(c->tabs);
 	free(c);
 }
 
@@ -233,6 +238,136 @@ static void green_fcd(const or_ctx *c, int i, int j, int k, cplx g[6])
 	}
 }
 
+/* ---------------- tabulated interaction terms (IGT_SO, SO) ---------------- */
+
+// values per table entry of t1..t10
+static const int tab_mult[10] = {1, 6, 3, 18, 6, 36, 1, 6, 1, 6};
+
+void or_set_tables(or_ctx *c, const double *tables, double m_re, double m_im)
+{
+	free(c->tabs);
+	c->tabs = malloc(sizeof(double) * OR_TAB_TOTAL);
+	memcpy(c->tabs, tables, sizeof(double) * OR_TAB_TOTAL);
+	c->so_m = m_re + I * m_im;
+	/* ReadTables, src/interaction.c:1051-1061: entry (i,j,k) with i >= j >= k >= 0 and i^2+j^2+k^2 <= RMAX^2 sits at
+	 * tab_index[i][j] + k; row (i, j) holds k = 0..min(j, floor(sqrt(RMAX^2 - i^2 - j^2))) */
+	const int R2 = OR_TAB_RMAX * OR_TAB_RMAX;
+	int next = 0;
+	for (int i = 1; i <= OR_TAB_RMAX; i++)
+		for (int j = 0; j <= i && i * i + j * j <= R2; j++) {
+			c->tab_index[i][j] = next;
+			int kmax = (int)floor(sqrt((double)(R2 - i * i - j * j)));
+			next += (kmax < j ? kmax : j) + 1;
+		}
+}
+
+static const double *tab_of(const or_ctx *c, int n) // t<n>, n = 1..10
+{
+	size_t off = 0;
+	for (int t = 0; t < n - 1; t++) off += (size_t)OR_TAB_SIZE * tab_mult[t];
+	return c->tabs + off;
+}
+
+/* InterTerm_igt_so_int / InterTerm_so_int, src/interaction.c:431-579 and 711-941 (SO with its fixed
+ * orientation-averaged form, inter_avg = true: no Gc1/Gf1/Gm1 terms). Close pairs (kd*rn^2 < 1, rn <= 10): the
+ * tabulated Green's tensor integrals, after mapping the offset onto i >= j >= k >= 0 (signs flipped per axis,
+ * coordinates sorted in the reference's order); SO adds the m^2 term Gc2. Other pairs: the point-dipole tensor
+ * times 1 - kd^2/24 (SO: 1 - (1+m^2) kd^2/24), plus the median correction Gm0 where kr < 1. Component order
+ * xx,xy,xz,yy,yz,zz; the tables' symmetric-matrix order is xx,xy,yy,xz,yz,zz. */
+static void green_igt(const or_ctx *c, int i, int j, int k, cplx g[6])
+{
+	green_poi(c, i, j, k, g);
+	const int so = c->inter == 6;
+	const double rn = sqrt((double)i * i + (double)j * j + (double)k * k);
+	const double q[3] = {i / rn, j / rn, k / rn};
+	const double qm[6] = {q[0] * q[0], q[0] * q[1], q[0] * q[2], q[1] * q[1], q[1] * q[2], q[2] * q[2]};
+	const int cmu[6] = {0, 0, 0, 1, 1, 2}, cnu[6] = {0, 1, 2, 1, 2, 2};
+	const double rr = rn * c->gridspace, invr3 = 1 / (rr * rr * rr), kr = c->k * rr, kr2 = kr * kr;
+	const double kd = c->k * c->gridspace, kd2 = kd * kd;
+	const cplx ev = invr3 * (cos(kr) + I * sin(kr));
+	const cplx m2 = c->so_m * c->so_m;
+	if (kr * rn < 1 && rn <= OR_TAB_RMAX) {
+		int v[3] = {i, j, k}, sg[3];
+		double qa[3];
+		for (int a = 0; a < 3; a++) {
+			sg[a] = v[a] < 0 ? -1 : 1;
+			v[a] *= sg[a];
+			qa[a] = q[a] * sg[a];
+		}
+		// ord[n] = the axis of the n-th largest coordinate, ties resolved like the reference
+		int ord[3];
+		if (v[0] >= v[1]) {
+			if (v[0] >= v[2]) {
+				ord[0] = 0;
+				if (v[1] >= v[2]) { ord[1] = 1; ord[2] = 2; }
+				else { ord[1] = 2; ord[2] = 1; }
+			}
+			else { ord[0] = 2; ord[1] = 0; ord[2] = 1; }
+		}
+		else {
+			if (v[0] >= v[2]) { ord[0] = 1; ord[1] = 0; ord[2] = 2; }
+			else {
+				ord[2] = 0;
+				if (v[1] >= v[2]) { ord[0] = 1; ord[1] = 2; }
+				else { ord[0] = 2; ord[1] = 1; }
+			}
+		}
+		int inv[3], vp[3];
+		double qp[3];
+		for (int a = 0; a < 3; a++) {
+			inv[ord[a]] = a;
+			qp[a] = qa[ord[a]];
+			vp[a] = v[ord[a]];
+		}
+		const int e0 = c->tab_index[vp[0]][vp[1]] + vp[2];
+		const double *t1 = tab_of(c, 1), *t2 = tab_of(c, 2), *t3 = tab_of(c, 3) + 3 * e0, *t5 = tab_of(c, 5) + 6 * e0;
+		const double *t4 = tab_of(c, 4), *t6 = tab_of(c, 6), *t7 = tab_of(c, 7), *t8 = tab_of(c, 8);
+		const double *t9 = tab_of(c, 9), *t10 = tab_of(c, 10);
+		const double t3q = qp[0] * t3[0] + qp[1] * t3[1] + qp[2] * t3[2];
+		const double t5tr = t5[0] + t5[2] + t5[5];
+		for (int a = 0; a < 6; a++) {
+			const int mu = cmu[a], nu = cnu[a], diag = mu == nu;
+			const double sig = sg[mu] * sg[nu];
+			const int m1 = inv[mu], n1 = inv[nu];
+			const int e2 = 6 * e0 + m1 + n1 + ((m1 == 2 || n1 == 2) ? 1 : 0);
+			const double *t4e = t4 + 3 * e2, *t6e = t6 + 6 * e2;
+			const double t4q = qp[0] * t4e[0] + qp[1] * t4e[1] + qp[2] * t4e[2];
+			const double t6tr = t6e[0] + t6e[2] + t6e[5];
+			// Gc0: kd^2 [sig(3(I10/2 + I8) - 2 t4q - t6tr) + kr qq (kr + 3i)/24 + delta(2 t3q + t5tr - kr(kr + i)/24
+			//      - I9/2 - I7)] + sig I2 (3 - 3ikr - kr^2) + delta I1 (-1 + ikr + kr^2), times exp(ikr)/r^3
+			cplx br = sig * (3 * (t10[e2] / 2 + t8[e2]) - 2 * t4q - t6tr) + (kr / 24) * qm[a] * (kr + 3 * I);
+			if (diag) br += 2 * t3q + t5tr - (kr / 24) * (kr + I) - t9[e0] / 2 - t7[e0];
+			br *= kd2;
+			br += sig * t2[e2] * (3 - 3 * I * kr - kr2);
+			if (diag) br += t1[e0] * (-1 + I * kr + kr2);
+			g[a] = ev * br;
+			if (so) { // Gc2 with <a_mu a_nu> = delta/3: (kd^2/2) m^2 [delta t5tr/3 - sig t6tr - kr(delta(kr + i) -
+				      // qq(kr + 3i))/12]
+				cplx b2 = -(kr + 3 * I) * qm[a];
+				if (diag) b2 += kr + I;
+				b2 = -b2 * kr / 12 - sig * t6tr;
+				if (diag) b2 += t5tr / 3;
+				g[a] += ev * (kd2 / 2) * m2 * b2;
+			}
+		}
+		return;
+	}
+	const cplx f = so ? 1 - (1 + m2) * kd2 / 24 : 1 - kd2 / 24;
+	for (int a = 0; a < 6; a++) g[a] *= f;
+	if (kr < 1) { // Gm0 = exp(ikr)/r^3 (-1 + ikr) (7/(64 rn^4)) [qq(33 q4 - 7 - 12(q_mu^2 + q_nu^2)) + delta(1 - 3q4 + 4q_mu^2)]
+		const double q2[3] = {q[0] * q[0], q[1] * q[1], q[2] * q[2]};
+		const double q4 = q2[0] * q2[0] + q2[1] * q2[1] + q2[2] * q2[2];
+		const double invrn4 = 1 / (rn * rn * rn * rn);
+		for (int a = 0; a < 6; a++) {
+			const int mu = cmu[a], nu = cnu[a];
+			double t = qm[a] * (33 * q4 - 7 - 12 * (q2[mu] + q2[nu]));
+			if (mu == nu) t += 1 - 3 * q4 + 4 * q2[mu];
+			t *= 7 * invrn4 / 64;
+			g[a] += ev * (-1 + I * kr) * t;
+		}
+	}
+}
+
 size_t or_dmatrix_len(const or_ctx *c)
 {
 	return (size_t)c->gX * c->DsZ * c->DsY * 6;
@@ -258,7 +393,8 @@ void or_init_dmatrix(or_ctx *c)
 			for (int i = 1 - bX; i < bX; i++) {
 				if (!i && !j && !k) continue;
 				cplx g[6];
-				if (c->inter >= 3) green_nloc(c, i, j, k, g);
+				if (c->inter >= 5) green_igt(c, i, j, k, g);
+				else if (c->inter >= 3) green_nloc(c, i, j, k, g);
 				else if (c->inter) green_fcd(c, i, j, k, g);
 				else green_poi(c, i, j, k, g);
 				size_t idx = ((size_t)k * bY + j) * gX + (i < 0 ? i + gX : i);

@@ -4,7 +4,9 @@
  * always as the checker or the timed CPU baseline, never as part of the GPU product.
  *
  * What is restated (reference = ADDA 1.3b6, paths relative to the reference project):
- *   or_init_dmatrix  <- InitDmatrix              src/fft.c:918-1416 (point-dipole term, reduced FFT)
+ *   or_init_dmatrix  <- InitDmatrix              src/fft.c:918-1416 (reduced FFT) with the interaction terms
+ *                                               InterTerm_poi/fcd/fcd_st/nloc/nloc_av/igt_so/so
+ *                                               (src/interaction.c:290-941)
  *   or_matvec        <- MatVec                   src/matvec.c:128-425
  *   or_solve         <- IterativeSolver          src/iterative.c:1398-1530, QMR_CS :898-1032, BiCGStab :640-724,
  *                                               BiCG_CS :490-637, CGNR :729-769, CSYM :773-892,
@@ -40,6 +42,14 @@ void or_free(or_ctx *c);
 void or_set_interaction(or_ctx *c, int relation);
 /* 3 = -int nloc, 4 = -int nloc_av (src/interaction.c:589-707): their Gaussian width Rp (gridspace units) */
 void or_set_nloc_rp(or_ctx *c, double rp);
+/* 5 = -int igt_so, 6 = -int so (src/interaction.c:431-579, 711-941): the reference's integral tables t1f..t10f.dat
+ * (ReadTables, src/interaction.c:1031-1063; TAB_SIZE 142 entries of 1,6,3,18,6,36,1,6,1,6 values each, src/const.h:276)
+ * back to back, and for SO the refractive index of its second-order terms (ref_index[0]); set before
+ * or_init_dmatrix */
+#define OR_TAB_RMAX 10
+#define OR_TAB_SIZE 142
+#define OR_TAB_TOTAL (OR_TAB_SIZE * 84)
+void or_set_tables(or_ctx *c, const double *tables, double m_re, double m_im);
 /* cosine and sine integrals Ci(x), Si(x) for x > 0 (the reference's cisi, sinint.c) */
 void or_cisi(double x, double *ci, double *si);
 void or_init_dmatrix(or_ctx *c);

@@ -67,6 +67,7 @@ def lib():
         L.or_solve_chp.restype = c_i
         L.or_set_interaction.argtypes = [c_p, ctypes.c_int]
         L.or_set_nloc_rp.argtypes = [c_p, ctypes.c_double]
+        L.or_set_tables.argtypes = [c_p, c_p, ctypes.c_double, ctypes.c_double]
         L.or_cisi.argtypes = [ctypes.c_double, c_p, c_p]
         L.or_cross.argtypes = [c_p, c_p, c_p, c_p, c_p, c_p]
         L.or_field.argtypes = [c_p, c_p, c_p, c_p]
@@ -87,7 +88,7 @@ class Oracle:
     """One particle lattice on the CPU: D matrix, matvec, QMR_CS/BiCGStab and Cext/Cabs in double precision."""
 
     def __init__(self, box, grid, position, material, gridspace, wavenum, nthreads=0, interaction="poi", nloc_rp=0.0,
-                 surface=None):
+                 surface=None, int_tables=None, so_m=0.0):
         self.L = lib()
         self.position = np.ascontiguousarray(position, dtype=np.uint16).reshape(-1, 3)
         self.material = np.ascontiguousarray(material if material is not None
@@ -96,8 +97,12 @@ class Oracle:
         self.box, self.grid = tuple(box), tuple(grid)
         self.h = self.L.or_create(*box, *grid, self.n, _ptr(self.position), _ptr(self.material),
                                   gridspace, wavenum, nthreads)
-        self.L.or_set_interaction(self.h, {"poi": 0, "fcd": 1, "fcd_st": 2, "nloc": 3, "nloc_av": 4}[interaction])
+        self.L.or_set_interaction(self.h, {"poi": 0, "fcd": 1, "fcd_st": 2, "nloc": 3, "nloc_av": 4, "igt_so": 5,
+                                           "so": 6}[interaction])
         self.L.or_set_nloc_rp(self.h, nloc_rp)
+        if int_tables is not None:
+            t = np.ascontiguousarray(int_tables, dtype=np.float64)
+            self.L.or_set_tables(self.h, _ptr(t), complex(so_m).real, complex(so_m).imag)
         if surface is not None:  # dict(zsum_shift, msub (None: perfect reflector), relation img|som, data: som table)
             m = surface.get("msub")
             tab = surface.get("data") if surface.get("relation", "img") == "som" else None

@@ -9,6 +9,12 @@ GOLDEN = os.path.join(HERE, "golden", "reference_runs.json")
 
 SETUP_KEYS = ("grid", "shape", "pars", "m", "dpl", "size", "pol", "orient", "avgpol", "prop", "interaction", "nloc_rp",
               "pol_rp")
+INT_TABLES = os.path.join(HERE, "golden", "int_tables.npy")
+
+
+def int_tables():
+    """the reference's igt_so / so integral tables (fixture made by golden/make_int_tables.py)"""
+    return np.load(INT_TABLES)
 
 
 def golden():
@@ -28,6 +34,8 @@ def setup_for(kw):
     args = {k: v for k, v in kw.items() if k in SETUP_KEYS}
     if isinstance(args.get("m"), list):
         args["m"] = complex(*args["m"])
+    if args.get("interaction") in ("igt_so", "so"):
+        args["int_tables"] = int_tables()
     return A.Setup(**args)
 
 
@@ -40,7 +48,8 @@ def oracle_for(s, nthreads=0):
     from oracle import oracle as O
     o = O.Oracle(s.box, s.grid, s.pos, s.mat, s.gridspace, s.wavenum, nthreads,
                  interaction=getattr(s, "interaction", "poi"), nloc_rp=getattr(s, "nloc_rp", 0.0),
-                 surface=getattr(s, "surface", None))
+                 surface=getattr(s, "surface", None), int_tables=getattr(s, "int_tables", None),
+                 so_m=getattr(s, "m", 0.0))
     return o
 
 
