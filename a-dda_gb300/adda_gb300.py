@@ -107,6 +107,7 @@ EXPORTS = ["adda_gb300_fft_fit", "adda_gb300_fit_box", "adda_gb300_make_particle
            "adda_gb300_cross_sections", "adda_gb300_scattered_fields", "adda_gb300_integr_points",
            "adda_gb300_romberg2d", "adda_gb300_romberg2d_ex", "adda_gb300_scattering_integrals",
            "adda_gb300_cross_sections_noalloc", "adda_gb300_time_matvec", "adda_gb300_read_int_tables",
+           "adda_gb300_get_fft_shape", "adda_gb300_set_fft_shape",
            "adda_gb300_last_solve_ms", "adda_gb300_last_error", "adda_gb300_kernel_launches"]
 
 _lib = None
@@ -175,6 +176,8 @@ def load_library(path):
         "adda_gb300_scattered_fields": ([P, I, I, P, P], I),
         "adda_gb300_cross_sections_noalloc": ([I, SZ, P, P, P, P, I, I, I, I, I, D, D, P, P, P, P, P], I),
         "adda_gb300_read_int_tables": ([ctypes.c_char_p, P], I),
+        "adda_gb300_get_fft_shape": ([P, I, P], I),
+        "adda_gb300_set_fft_shape": ([P, I, P], I),
         "adda_gb300_last_error": ([], ctypes.c_char_p),
         "adda_gb300_last_solve_ms": ([P], D),
         "adda_gb300_kernel_launches": ([], ctypes.c_uint64),
@@ -584,6 +587,16 @@ class Context:
         """keep checkpoint bytes (the reference's chp.<ringid> file) for the next solve with init="chpoint" """
         data = bytes(data)
         _check(self.L.adda_gb300_chpoint_load(self.h, rhs, data, len(data)), "chpoint_load")
+
+    def fft_shape(self, prec="fp32"):
+        """the matvec's tile shape (w1, w2, pairs, threads) for fp32 or fp64"""
+        v = (ctypes.c_int * 4)()
+        _check(self.L.adda_gb300_get_fft_shape(self.h, PREC[prec], v), "get_fft_shape")
+        return tuple(v)
+
+    def set_fft_shape(self, shape, prec="fp32"):
+        """fix the matvec's tile shape (fp32: no tuning of it)"""
+        _check(self.L.adda_gb300_set_fft_shape(self.h, PREC[prec], (ctypes.c_int * 4)(*shape)), "set_fft_shape")
 
     def last_solve_ms(self):
         """device milliseconds of the last solve (CUDA events on the context stream)"""

@@ -17,7 +17,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libadda_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-CU = ["api.cu", "matvec.cu", "matvec_f32.cu", "dmatrix.cu", "solver.cu", "noalloc.cu"]
+CU = ["api.cu", "matvec.cu", "matvec_f32.cu", "matvec_yz.cu", "dmatrix.cu", "solver.cu", "noalloc.cu"]
 C = ["host_setup.c", "integrate.c"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -1,6 +1,8 @@
 // api.cu - context management and the C-ABI entry points of include/adda_gb300.h.
 #include "ctx.cuh"
 
+#include <cstdio>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -101,6 +103,9 @@ static int create_impl(const adda_gb300_problem *p, adda_gb300_ctx *c)
 	c->device = p->device;
 	ADDA_CUDA(cudaSetDevice(p->device));
 	ADDA_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+	ADDA_CUDA(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
+	ADDA_CUDA(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+	ADDA_CUDA(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
 	c->bX = p->boxX; c->bY = p->boxY; c->bZ = p->boxZ;
 	c->gX = p->gridX > 0 ? p->gridX : adda_gb300_fft_fit(2 * p->boxX, 1);
 	c->gY = p->gridY > 0 ? p->gridY : adda_gb300_fft_fit(2 * p->boxY, 1);
@@ -241,15 +246,28 @@ static int create_impl(const adda_gb300_problem *p, adda_gb300_ctx *c)
 		: (int)std::max<size_t>(1, std::min<size_t>(c->gX, ((size_t)CHUNK_TUNE_MAX_MB << 20) / (slab * sizeof(float2))));
 	const size_t tz = std::max(c->CK64 * sizeof(double2), c->CK32max * sizeof(float2)) * slab;
 	ADDA_CUDA(cudaMalloc(&c->Tz, tz));
-	if (c->surface) ADDA_CUDA(cudaMalloc(&c->TzR, tz));
-	c->partial_len = R * matvec_partial_blocks(c, true) * 4;
+	ADDA_CUDA(cudaMalloc(&c->Tz2, tz));
+	if (c->surface) {
+		ADDA_CUDA(cudaMalloc(&c->TzR, tz));
+		ADDA_CUDA(cudaMalloc(&c->TzR2, tz));
+	}
+	c->partial_len = (size_t)R * c->bY * c->bZ * 4; // K3 partial sums for the narrowest tile (one y-line per block)
 	ADDA_CUDA(cudaMalloc(&c->partial, sizeof(double) * c->partial_len));
 	ADDA_CUDA(cudaMalloc(&c->d_red, sizeof(double) * R * 4));
 	ADDA_CUDA(cudaMalloc(&c->vin, sizeof(double2) * R * 3 * std::max<size_t>(N, 1)));
 	ADDA_CUDA(cudaMalloc(&c->vout, sizeof(double2) * R * 3 * std::max<size_t>(N, 1)));
 	c->cc_set.assign(R, 0);
 	c->nmat = 0;
-	return matvec_setup(c);
+	int rc = matvec_setup(c);
+	if (rc) return rc;
+	// ADDA_GB300_FFT_SHAPE="w1,w2,pairs,nt" fixes the FP32 tile shape (no tuning of it)
+	if (const char *e = getenv("ADDA_GB300_FFT_SHAPE")) {
+		int v[4];
+		if (sscanf(e, "%d,%d,%d,%d", v, v + 1, v + 2, v + 3) == 4 &&
+			!matvec_set_shape(c, true, MvShape{v[0], v[1], v[2], v[3]}))
+			c->shape_fixed = true;
+	}
+	return ADDA_GB300_OK;
 }
 
 int adda_gb300_destroy(adda_gb300_ctx *c)
@@ -258,10 +276,14 @@ int adda_gb300_destroy(adda_gb300_ctx *c)
 	if (c->stream) cudaStreamSynchronize(c->stream);
 	solver_free(c);
 	void *bufs[] = {c->d_line_start, c->d_xy, c->d_mat, c->d_pos, c->D64, c->D32, c->cc64, c->ccs64, c->ccs32,
-		c->Xf, c->Tz, c->TzR, c->R64, c->R32, c->partial, c->d_red, c->vin, c->vout, c->pvec64, c->tw64[0], c->tw64[1], c->tw64[2],
-		c->tw32[0], c->tw32[1], c->tw32[2]};
+		c->Xf, c->Tz, c->TzR, c->Tz2, c->TzR2, c->R64, c->R32, c->partial, c->d_red, c->vin, c->vout, c->pvec64,
+		c->tw64[0], c->tw64[1], c->tw64[2], c->tw32[0], c->tw32[1], c->tw32[2]};
+	if (c->stream2) cudaStreamSynchronize(c->stream2);
 	for (void *b : bufs)
 		if (b) cudaFree(b);
+	if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+	if (c->ev_join) cudaEventDestroy(c->ev_join);
+	if (c->stream2) cudaStreamDestroy(c->stream2);
 	if (c->stream) cudaStreamDestroy(c->stream);
 	delete c;
 	return ADDA_GB300_OK;
@@ -296,15 +318,19 @@ int adda_gb300_create(const adda_gb300_problem *p, adda_gb300_ctx **out)
 __global__ void fill_k(double2 *v, size_t n, unsigned seed);
 __global__ void d2f_k(float2 *dst, const double2 *src, size_t n);
 
-// The FP32 matvec's chunk (x-slabs whose z-transformed data pass through L2 between K2a, K2b and K2c) trades L2
-// residency against launch count and tail waves; its best size depends on the grid and the RHS count. Measured once
-// per context on its own data sizes: balanced splits of the x-slabs into chunks of 24..CHUNK_TUNE_MAX_MB, one
-// warm-up and two timed matvecs each with
-// Rmax RHS of random data (CUDA events on the context stream); the fastest is kept. Runs from check_ready, i.e.
-// only once the D matrix and the polarisability buffers a matvec reads exist, and before any graph capture.
+// The FP32 matvec's autotuner. The tile shape (threads per register-K2b block, y-lines per K2a/K2c and per K1/K3
+// block) sets occupancy and shared memory per block; the chunk (x-slabs whose z-transformed data pass through L2
+// between K2a, K2b and K2c) trades L2 residency against launch count and tail waves; the best of both depends on
+// the grid and the RHS count. Measured once per context on its own data sizes: the shape by coordinate descent over
+// the alternatives the build holds (kept when 2 % faster), then balanced splits of the x-slabs into chunks of
+// 24..CHUNK_TUNE_MAX_MB; one warm-up and two timed matvecs each with Rmax RHS of random data (CUDA events on the
+// context stream). Runs from check_ready, i.e. only once the D matrix and the polarisability buffers a matvec reads
+// exist, and before any graph capture. ADDA_GB300_CHUNK_MB / ADDA_GB300_FFT_SHAPE (or adda_gb300_set_fft_shape)
+// fix either part.
 static int tune_chunks(adda_gb300_ctx *c)
 {
-	if (c->chunk_fixed || c->chunk_tuned || c->N == 0 || !c->dready || !c->ccs32) return ADDA_GB300_OK;
+	if (c->chunk_tuned || c->N == 0 || !c->dready || !c->ccs32 || (c->chunk_fixed && c->shape_fixed))
+		return ADDA_GB300_OK;
 	ADDA_CUDA(cudaSetDevice(c->device));
 	cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
 	ADDA_CUDA(cudaStreamIsCapturing(c->stream, &cap));
@@ -322,34 +348,88 @@ static int tune_chunks(adda_gb300_ctx *c)
 	cudaEvent_t e0, e1;
 	ADDA_CUDA(cudaEventCreate(&e0));
 	ADDA_CUDA(cudaEventCreate(&e1));
-	// candidates: the gX x-slabs split into nc balanced chunks (no small tail chunk), from the largest chunk that
-	// fits the Tz buffer down to about 24 MB
-	int best_ck = c->CK32, last = -1, rc = ADDA_GB300_OK;
-	float best = 1e30f;
-	const size_t min_ck = std::max<size_t>(1, ((size_t)24 << 20) / (slab * sizeof(float2)));
-	for (int nc = 1; nc <= c->gX; nc++) {
-		const int ck = (c->gX + nc - 1) / nc;
-		if (ck > c->CK32max) continue;
-		if (last > 0 && 5 * ck > 4 * last) continue; // next candidate at least 20 % smaller
-		if ((size_t)ck < min_ck && last > 0) break;
-		last = ck;
-		c->CK32 = ck;
-		if ((rc = matvec_run<float>(c, c->Rmax, in, out, 0, e, nullptr))) break;
+	int rc = ADDA_GB300_OK;
+	// one warm-up and two timed FP32 matvecs of Rmax RHS with the current settings
+	auto time_mv = [&](float &t) {
+		if ((rc = matvec_run<float>(c, c->Rmax, in, out, 0, e, nullptr))) return false;
 		cudaEventRecord(e0, c->stream);
 		for (int i = 0; i < 2 && !rc; i++) rc = matvec_run<float>(c, c->Rmax, in, out, 0, e, nullptr);
 		cudaEventRecord(e1, c->stream);
-		if (cudaEventSynchronize(e1) != cudaSuccess) rc = ADDA_GB300_ECUDA;
-		if (rc) break;
-		float t = 0;
+		if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = ADDA_GB300_ECUDA;
+		if (rc) return false;
 		cudaEventElapsedTime(&t, e0, e1);
-		if (t < best) {
-			best = t;
-			best_ck = ck;
+		return true;
+	};
+	// 1. the tile shape, one dimension at a time over the alternatives the build holds (register-K2b threads per
+	// block, then y-lines per K2a/K2c block, then per K1/K3 block), each kept when faster; candidates that do not
+	// fit the axis lengths are skipped
+	if (!c->shape_fixed) {
+		float best = 1e30f;
+		if (!time_mv(best)) goto done;
+		for (int dim = 0; dim < 3; dim++) {
+			static const int cand[3][3] = {{64, 128, 256}, {8, 16, 32}, {4, 8, 8}};
+			for (int k = 0; k < 3; k++) {
+				MvShape sh = c->shape[1], keep = sh;
+				int &field = dim == 0 ? sh.nt : dim == 1 ? sh.w2 : sh.w1;
+				if (field == cand[dim][k] || (dim == 0 && !matvec_k2b_reg(c))) continue;
+				field = cand[dim][k];
+				if (!matvec_shape_ok(c, true, sh)) continue;
+				c->shape[1] = sh;
+				float t = 0;
+				if (!time_mv(t)) goto done;
+				if (t < 0.98f * best) best = t;
+				else c->shape[1] = keep;
+			}
 		}
 	}
+	// 2. the chunk: the gX x-slabs split into nc balanced chunks (no small tail chunk), from the largest chunk that
+	// fits the Tz buffer down to about 24 MB
+	if (!c->chunk_fixed) {
+		int best_ck = c->CK32, last = -1;
+		float best = 1e30f;
+		const size_t min_ck = std::max<size_t>(1, ((size_t)24 << 20) / (slab * sizeof(float2)));
+		for (int nc = 1; nc <= c->gX; nc++) {
+			const int ck = (c->gX + nc - 1) / nc;
+			if (ck > c->CK32max) continue;
+			if (last > 0 && 5 * ck > 4 * last) continue; // next candidate at least 20 % smaller
+			if ((size_t)ck < min_ck && last > 0) break;
+			last = ck;
+			c->CK32 = ck;
+			float t = 0;
+			if (!time_mv(t)) break;
+			if (t < best) {
+				best = t;
+				best_ck = ck;
+			}
+		}
+		c->CK32 = best_ck;
+	}
+done:
 	cudaEventDestroy(e0);
 	cudaEventDestroy(e1);
-	c->CK32 = best_ck;
+	return rc;
+}
+
+int adda_gb300_get_fft_shape(const adda_gb300_ctx *c, int prec, int shape[4])
+{
+	if (!c || !shape || (prec != ADDA_PREC_FP64 && prec != ADDA_PREC_FP32)) return ADDA_GB300_EINVAL;
+	const MvShape &s = c->shape[prec == ADDA_PREC_FP32 ? 1 : 0];
+	shape[0] = s.w1;
+	shape[1] = s.w2;
+	shape[2] = s.pairs;
+	shape[3] = s.nt;
+	return ADDA_GB300_OK;
+}
+
+int adda_gb300_set_fft_shape(adda_gb300_ctx *c, int prec, const int shape[4])
+{
+	if (!c || !shape || (prec != ADDA_PREC_FP64 && prec != ADDA_PREC_FP32)) {
+		set_error("set_fft_shape: invalid arguments");
+		return ADDA_GB300_EINVAL;
+	}
+	const bool f32 = prec == ADDA_PREC_FP32;
+	int rc = matvec_set_shape(c, f32, MvShape{shape[0], shape[1], shape[2], f32 ? shape[3] : 128});
+	if (!rc && f32) c->shape_fixed = true;
 	return rc;
 }
 

@@ -50,6 +50,12 @@ struct MvEpi {
 
 struct SolverWork; // solver.cu
 
+// tile shape of the matvec kernels (per arithmetic): y-lines per K1/K3 block, y-lines per K2a/K2c block, (kz, RHS)
+// pairs per generic K2b block, threads per register-K2b block
+struct MvShape {
+	int w1, w2, pairs, nt;
+};
+
 } // namespace adda
 
 struct adda_gb300_ctx {
@@ -94,10 +100,17 @@ struct adda_gb300_ctx {
 	void *Xf = nullptr;               // [R][gX][3][bZ][bY] after the X transform
 	void *Tz = nullptr;               // [R][CK][3][gZ][bY] chunk of x-slabs after the Z transform
 	void *TzR = nullptr;              // surface: the same chunk transformed along z with the inverse sign
+	// the odd chunks' buffers and stream: two chunks of the y/z stage run at once (one's K2a/K2b/K2c filling the
+	// other's tail), joined before K3 by events (also inside a stream capture)
+	void *Tz2 = nullptr, *TzR2 = nullptr;
+	cudaStream_t stream2 = nullptr;
+	cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 	int CK64 = 1, CK32 = 1;           // x-slabs per chunk (sized to stay resident in L2)
 	int CK32max = 1;                  // largest FP32 chunk the Tz buffer holds
 	bool chunk_fixed = false;         // chunk size set by the environment: no tuning
 	bool chunk_tuned = false;         // FP32 chunk size measured (tune_chunks)
+	adda::MvShape shape[2] = {{4, 8, 4, 128}, {8, 16, 8, 128}}; // [0] FP64, [1] FP32 tile shapes
+	bool shape_fixed = false;         // FP32 shape set by the caller or the environment: not tuned
 	double *partial = nullptr;        // epilogue partial sums
 	size_t partial_len = 0;
 	double *d_red = nullptr;          // reduced per-RHS results [Rmax][4]
@@ -120,7 +133,10 @@ FftPlan make_plan(int n, int max_radix);
 int dmatrix_build(adda_gb300_ctx *c);
 
 // matvec.cu
-int matvec_setup(adda_gb300_ctx *c); // kernel attributes, chunk sizes
+int matvec_setup(adda_gb300_ctx *c); // tile shapes, kernel attributes
+int matvec_set_shape(adda_gb300_ctx *c, bool f32, const MvShape &s); // a tile shape the build holds and that fits
+bool matvec_shape_ok(const adda_gb300_ctx *c, bool f32, const MvShape &s);
+bool matvec_k2b_reg(const adda_gb300_ctx *c); // the FP32 matvec uses the register K2b (its thread count is tunable)
 size_t matvec_partial_blocks(const adda_gb300_ctx *c, bool dbl); // partial-sum blocks per RHS of the epilogue
 // T = FFT/D arithmetic (float or double), V = dipole-vector type (float2 or double2)
 template <typename T, typename V>

@@ -36,7 +36,9 @@ namespace mv {
 // caller passes (float2, double2 or double-float dd2). With T=float and V=double2 or dd2 (the MIXED solvers) the
 // inputs are rounded on the fly and y = x + S.X is accumulated in the vector's precision, so the identity part of A
 // keeps that precision.
-template <typename T, typename V> struct MvP {
+// Everything but the dipole vectors: the y/z stage (K2a, K2b, K2c) never touches them, so its kernels are compiled
+// once per arithmetic type T.
+template <typename T> struct MvGeom {
 	typedef typename CxT<T>::type C;
 	int bX, bY, bZ, gX, gY, gZ, DsY, DsZ;
 	int R;
@@ -46,8 +48,6 @@ template <typename T, typename V> struct MvP {
 	const uint8_t *mat;
 	const C *ccs;   // per-RHS cc_sqrt: [R][nmat][3] or [R][N][3]
 	int nmat, per_dip;
-	const V *arg;
-	V *res;
 	C *Xf;
 	C *Tz;
 	int CK, kx0;
@@ -62,6 +62,11 @@ template <typename T, typename V> struct MvP {
 	C *TzR;
 	const C *Rm;
 	int RsY;
+};
+
+template <typename T, typename V> struct MvP : MvGeom<T> {
+	const V *arg;
+	V *res;
 };
 
 template <typename To, typename From> __device__ __forceinline__ To cvt(From a) { return from_d2<To>(to_d2(a)); }
@@ -150,8 +155,8 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T,
 // padded) and writes Tz (all kz); MODE 1 (inverse) reads Tz and writes z<bZ back to Xf; MODE 2 (surface) reads Xf
 // like MODE 0 but transforms with the inverse sign into TzR, so that the product with R~ sums heights instead of
 // differences (planZRf, fft.c:396-403, matvec.c:249).
-template <typename T, typename V, int W, int MODE, int NS>
-__global__ void __launch_bounds__(col_threads<T, NS, W>(), (col_minblocks<T, NS, W>())) mv_fftz(MvP<T, V> p)
+template <typename T, int W, int MODE, int NS>
+__global__ void __launch_bounds__(col_threads<T, NS, W>(), (col_minblocks<T, NS, W>())) mv_fftz(MvGeom<T> p)
 {
 	constexpr bool INV = MODE == 1, SGN = MODE != 0;
 	typedef typename CxT<T>::type C;
@@ -199,15 +204,15 @@ __global__ void __launch_bounds__(col_threads<T, NS, W>(), (col_minblocks<T, NS,
 	}
 }
 
-// K2b: per (kx, KB kz, RG RHS) with KB*RG <= PAIRS: y-FFT of the 3 components, D product (matvec.c:271-305 incl. the
+// K2b: per (kx, KB kz, RG RHS) with KB*RG <= P pairs: y-FFT of the 3 components, D product (matvec.c:271-305 incl. the
 // reduced-FFT signs), inverse y-FFT. Line l = pair*3 + comp, pair = kk*RG + rr. Warp w loads/stores lines w, w+8, w+16
 // with its 32 lanes along y (coalesced rows of Tz, odd tile stride: conflict-free).
-template <typename T, typename V, int NS> __global__ void __launch_bounds__(256) mv_fft_y_dmul(MvP<T, V> p)
+template <typename T, int NS, int P> __global__ void __launch_bounds__(256) mv_fft_y_dmul(MvGeom<T> p)
 {
 	typedef typename CxT<T>::type C;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	if (all_done(p)) return;
-	constexpr int NL = 3 * Tiles<T>::PAIRS, LS = tile_ls(NL);
+	constexpr int NL = 3 * P, LS = tile_ls(NL);
 	const int n = NS ? NS : p.gY;
 	C *a = reinterpret_cast<C *>(smem_raw);
 	C *b = a + (size_t)n * LS;
@@ -268,17 +273,17 @@ template <typename T, typename V, int NS> __global__ void __launch_bounds__(256)
 	}
 }
 
-// K2b for a particle near a substrate (matvec.c:255-305): per (kx, KB kz, RG RHS) with KB*RG <= PAIRS/2, six lines
+// K2b for a particle near a substrate (matvec.c:255-305): per (kx, KB kz, RG RHS) with KB*RG <= P/2, six lines
 // per pair: the 3 components of Tz and of TzR. All are transformed along y; then yv = D~.xv + R~.xvR with D's
 // reduced-FFT signs and R's (reduced in y only: xy and yz change sign for ky > gY/2) and R's product
 // M21 = M12, M31 = -M13, M32 = -M23 (cReflMatrVec, cmplx.h:391-401); the result goes back through the inverse y
 // transform into Tz. Line l = pair*6 + c6, c6 < 3 from Tz, c6 >= 3 from TzR.
-template <typename T, typename V, int NS> __global__ void __launch_bounds__(256) mv_fft_y_surf(MvP<T, V> p)
+template <typename T, int NS, int P> __global__ void __launch_bounds__(256) mv_fft_y_surf(MvGeom<T> p)
 {
 	typedef typename CxT<T>::type C;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	if (all_done(p)) return;
-	constexpr int NL = 3 * Tiles<T>::PAIRS, LS = tile_ls(NL);
+	constexpr int NL = 3 * P, LS = tile_ls(NL);
 	const int n = NS ? NS : p.gY;
 	C *a = reinterpret_cast<C *>(smem_raw);
 	C *b = a + (size_t)n * LS;
@@ -360,8 +365,8 @@ template <typename T, typename V, int NS> __global__ void __launch_bounds__(256)
 // through a fourth slot (the next one loading into the free third slot meanwhile); each spectrum u_c adds column c of
 // the reflected product R~.u (M21 = M12, M31 = -M13, M32 = -M23, cReflMatrVec cmplx.h:391-401; R reduced in y only)
 // to the three result components before the inverse transforms.
-template <typename V, int NS, int NT, bool SURF = false>
-__global__ void __launch_bounds__(NT, SURF ? 3 : 4) mv_fft_y_reg(MvP<float, V> p)
+template <int NS, int NT, bool SURF = false>
+__global__ void __launch_bounds__(NT, (SURF ? 3 : 4) * 128 / NT) mv_fft_y_reg(MvGeom<float> p)
 {
 	typedef float2 C;
 	constexpr int T = RegShape<NS>::T, E = RegShape<NS>::E, BUF = RegShape<NS>::BUF, G = NT / T;
@@ -613,16 +618,6 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T,
 // ---------------------------------------------------------------------------------------------------------------
 // host side
 
-// shared memory of K1/K3 and K2a/K2c: two tiles for the Stockham form, one for the column form (NS known)
-template <typename T> size_t smem_k1(int gX) { return 2 * sizeof(typename CxT<T>::type) * (size_t)gX * tile_ls(3 * Tiles<T>::W1); }
-template <typename T> size_t smem_k2(int gZ) { return 2 * sizeof(typename CxT<T>::type) * (size_t)gZ * tile_ls(Tiles<T>::W2); }
-template <typename T, int NS> size_t smem_k1s(int gX) { return (reg_cols<T, NS>() ? 1 : 2) * smem_k1<T>(gX) / 2; }
-template <typename T, int NS> size_t smem_k2s(int gZ) { return (reg_cols<T, NS>() ? 1 : 2) * smem_k2<T>(gZ) / 2; }
-template <typename T> size_t smem_k2b(int gY)
-{
-	return 2 * sizeof(typename CxT<T>::type) * (size_t)gY * tile_ls(3 * Tiles<T>::PAIRS);
-}
-
 // compile-time length for the power-of-two grids the kernels are instantiated for, 0 otherwise
 inline int static_len(int n)
 {
@@ -635,6 +630,56 @@ template <typename T> inline bool use_k2b_reg(int gY)
 	return sizeof(T) == 4 && (gY == 64 || gY == 128 || gY == 256);
 }
 
+// shared memory of a tile kernel for nl lines of length n: one tile in the column form (FP32, compile-time length),
+// two for the Stockham passes
+template <typename T> inline size_t tile_smem(int n, int nl)
+{
+	const bool one = sizeof(T) == 4 && static_len(n) != 0;
+	return (one ? 1 : 2) * sizeof(typename CxT<T>::type) * (size_t)n * tile_ls(nl);
+}
+// register K2b: NSLOT slots of BUF complex per lane group of T lanes
+inline size_t k2b_reg_smem(int gY, int nt, bool surf)
+{
+	int lg = 0;
+	while ((1 << lg) < gY) lg++;
+	const int T = 1 << (lg / 2), E = gY / T;
+	return (size_t)(nt / T) * (surf ? 4 : 3) * E * (T + 1) * sizeof(float2);
+}
+constexpr size_t SMEM_CAP = 216 * 1024; // dynamic shared memory of one block (the opt-in limit is 227 KB)
+
+// Tile widths the build instantiates. The defaults (Tiles<T>) everywhere; for FP32 the tuner's alternatives (K1/K3 4
+// y-lines; K2a/K2c 8 or 32; register K2b 64 or 256 threads) for every length; and, for the runtime-plan lengths
+// (above 512 or not a power of two), the narrow tiles of long axes (1 y-line per K1/K3 block, 2 per K2a/K2c block,
+// one (kz, RHS) pair per generic K2b block), whose shared memory fits axes up to 2048 (FP64) / 4096 (FP32).
+template <typename T, int NS, int W> constexpr bool has_w1()
+{
+	return W == Tiles<T>::W1 || (sizeof(T) == 4 && W == 4) || (NS == 0 && W == 1);
+}
+template <typename T, int NS, int W> constexpr bool has_w2()
+{
+	return W == Tiles<T>::W2 || (sizeof(T) == 4 && (W == 8 || W == 32)) || (NS == 0 && W == 2);
+}
+template <typename T, int NS, int P> constexpr bool has_pairs()
+{
+	return P == Tiles<T>::PAIRS || (NS == 0 && P == 1);
+}
+inline bool shape_instantiated(bool f32, int n1, int n2, int ny, const MvShape &s)
+{
+	const bool w1ok = s.w1 == (f32 ? 8 : 4) || (f32 && s.w1 == 4) || (static_len(n1) == 0 && s.w1 == 1);
+	const bool w2ok = s.w2 == (f32 ? 16 : 8) || (f32 && (s.w2 == 8 || s.w2 == 32)) || (static_len(n2) == 0 && s.w2 == 2);
+	const bool pok = s.pairs == (f32 ? 8 : 4) || (static_len(ny) == 0 && s.pairs == 1);
+	const bool ntok = !f32 || s.nt == 64 || s.nt == 128 || s.nt == 256;
+	return w1ok && w2ok && pok && ntok;
+}
+// the shared memory every kernel of the shape needs fits one block
+template <typename T> inline bool shape_fits(const adda_gb300_ctx *c, const MvShape &s)
+{
+	if (tile_smem<T>(c->gX, 3 * s.w1) > SMEM_CAP || tile_smem<T>(c->gZ, s.w2) > SMEM_CAP) return false;
+	if (use_k2b_reg<T>(c->gY)) return k2b_reg_smem(c->gY, s.nt, c->surface) <= SMEM_CAP;
+	return 2 * sizeof(typename CxT<T>::type) * (size_t)c->gY * tile_ls(3 * s.pairs) <= SMEM_CAP && (!c->surface ||
+		s.pairs >= 2);
+}
+
 #define ADDA_NS_SWITCH(n, CALL)                                                                                   \
 	switch (static_len(n)) {                                                                                        \
 		case 64: { constexpr int NS = 64; CALL; } break;                                                            \
@@ -643,45 +688,133 @@ template <typename T> inline bool use_k2b_reg(int gY)
 		case 512: { constexpr int NS = 512; CALL; } break;                                                          \
 		default: { constexpr int NS = 0; CALL; } break;                                                             \
 	}
+// one case per candidate width; CALL sees the width as the constant W (instantiated widths only)
+#define ADDA_W_CASE(HAS, w, CALL)                                                                                   \
+	case w: {                                                                                                       \
+		if constexpr (HAS<T, NS, w>()) { constexpr int W = w; CALL; }                                               \
+	} break;
+#define ADDA_W_SWITCH(HAS, wv, CALL)                                                                                \
+	switch (wv) {                                                                                                   \
+		ADDA_W_CASE(HAS, 1, CALL) ADDA_W_CASE(HAS, 2, CALL) ADDA_W_CASE(HAS, 4, CALL) ADDA_W_CASE(HAS, 8, CALL)     \
+		ADDA_W_CASE(HAS, 16, CALL) ADDA_W_CASE(HAS, 32, CALL)                                                       \
+		default: break;                                                                                             \
+	}
+
+#define ADDA_SET(kern) ADDA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP))
+// shared-memory opt-in of the kernels that touch the dipole vectors (K1, K3)
+template <typename T, typename V, int NS> int set_attrs_k13()
+{
+	for (int w : {1, 4, 8}) {
+		ADDA_W_SWITCH(has_w1, w, ADDA_SET((mv_scatter_fftx<T, V, W, NS>)); ADDA_SET((mv_fftx_gather<T, V, W, NS>)))
+	}
+	return ADDA_GB300_OK;
+}
+// ... and of the y/z stage (K2a, K2b, K2c)
+template <typename T, int NS> int set_attrs_yz()
+{
+	for (int w : {1, 2, 4, 8, 16, 32}) {
+		ADDA_W_SWITCH(has_w2, w, ADDA_SET((mv_fftz<T, W, 0, NS>)); ADDA_SET((mv_fftz<T, W, 1, NS>));
+			ADDA_SET((mv_fftz<T, W, 2, NS>)))
+		ADDA_W_SWITCH(has_pairs, w, ADDA_SET((mv_fft_y_dmul<T, NS, W>)); ADDA_SET((mv_fft_y_surf<T, NS, W>)))
+	}
+	if constexpr (sizeof(T) == 4 && NS >= 64 && NS <= 256) {
+		ADDA_SET((mv_fft_y_reg<NS, 64>));
+		ADDA_SET((mv_fft_y_reg<NS, 128>));
+		ADDA_SET((mv_fft_y_reg<NS, 256>));
+		ADDA_SET((mv_fft_y_reg<NS, 64, true>));
+		ADDA_SET((mv_fft_y_reg<NS, 128, true>));
+		ADDA_SET((mv_fft_y_reg<NS, 256, true>));
+	}
+	return ADDA_GB300_OK;
+}
+#undef ADDA_SET
 
 template <typename T, typename V> int set_attrs_tv()
 {
-	constexpr int W1 = Tiles<T>::W1, W2 = Tiles<T>::W2;
-	// the opt-in limit (227 KB) covers static + dynamic shared memory; the largest tile is 208 KB
-	const int mx = 216 * 1024;
-#define ADDA_SET(kern) ADDA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))
-#define ADDA_SET_ALL(NS)                                                                                            \
-	ADDA_SET((mv_scatter_fftx<T, V, W1, NS>));                                                                      \
-	ADDA_SET((mv_fftx_gather<T, V, W1, NS>));                                                                       \
-	ADDA_SET((mv_fftz<T, V, W2, 0, NS>));                                                                           \
-	ADDA_SET((mv_fftz<T, V, W2, 1, NS>));                                                                           \
-	ADDA_SET((mv_fftz<T, V, W2, 2, NS>));                                                                           \
-	ADDA_SET((mv_fft_y_dmul<T, V, NS>));                                                                            \
-	ADDA_SET((mv_fft_y_surf<T, V, NS>))
-	if constexpr (sizeof(T) == 4) {
-		ADDA_SET((mv_fft_y_reg<V, 64, 128>));
-		ADDA_SET((mv_fft_y_reg<V, 128, 128>));
-		ADDA_SET((mv_fft_y_reg<V, 256, 128>));
-		ADDA_SET((mv_fft_y_reg<V, 64, 128, true>));
-		ADDA_SET((mv_fft_y_reg<V, 128, 128, true>));
-		ADDA_SET((mv_fft_y_reg<V, 256, 128, true>));
-	}
-	ADDA_SET_ALL(0);
-	ADDA_SET_ALL(64);
-	ADDA_SET_ALL(128);
-	ADDA_SET_ALL(256);
-	ADDA_SET_ALL(512);
-#undef ADDA_SET_ALL
-#undef ADDA_SET
+	int rc;
+	if ((rc = set_attrs_k13<T, V, 0>()) || (rc = set_attrs_k13<T, V, 64>()) || (rc = set_attrs_k13<T, V, 128>()) ||
+		(rc = set_attrs_k13<T, V, 256>()) || (rc = set_attrs_k13<T, V, 512>()))
+		return rc;
 	return ADDA_GB300_OK;
 }
+
+template <typename T> int setup_yz()
+{
+	int rc;
+	if ((rc = set_attrs_yz<T, 0>()) || (rc = set_attrs_yz<T, 64>()) || (rc = set_attrs_yz<T, 128>()) ||
+		(rc = set_attrs_yz<T, 256>()) || (rc = set_attrs_yz<T, 512>()))
+		return rc;
+	return ADDA_GB300_OK;
+}
+
+// the y/z stage of one chunk of x-slabs (K2a, [K2a surface], K2b, K2c) with the context's tile shape, on stream st
+template <typename T> int launch_yz(adda_gb300_ctx *c, MvGeom<T> p, int ck, const MvShape &sh, cudaStream_t st)
+{
+	const int R = p.R;
+	const bool surf = c->surface;
+	const dim3 g2((c->bY + sh.w2 - 1) / sh.w2, 3 * ck, R);
+	ADDA_NS_SWITCH(c->gZ, ADDA_W_SWITCH(has_w2, sh.w2, (mv_fftz<T, W, 0, NS><<<g2, col_threads<T, NS, W>(),
+		tile_smem<T>(c->gZ, W), st>>>(p))));
+	ADDA_LAUNCHED();
+	if (surf) {
+		ADDA_NS_SWITCH(c->gZ, ADDA_W_SWITCH(has_w2, sh.w2, (mv_fftz<T, W, 2, NS><<<g2, col_threads<T, NS, W>(),
+			tile_smem<T>(c->gZ, W), st>>>(p))));
+		ADDA_LAUNCHED();
+	}
+	if (use_k2b_reg<T>(c->gY)) {
+		if constexpr (sizeof(T) == 4) {
+			const int nt = sh.nt;
+			const int Tl = c->gY == 256 ? 16 : 8; // lanes per line, RegShape<gY>::T
+			const int G = nt / Tl;
+			const dim3 g((c->gZ * R + G - 1) / G, ck);
+			const size_t sm = k2b_reg_smem(c->gY, nt, surf);
+#define ADDA_K2B_REG(NS_, NT_)                                                                                      \
+	if (c->gY == NS_ && nt == NT_) {                                                                                \
+		if (surf) mv_fft_y_reg<NS_, NT_, true><<<g, NT_, sm, st>>>(p);                                            \
+		else mv_fft_y_reg<NS_, NT_><<<g, NT_, sm, st>>>(p);                                                       \
+	}
+			ADDA_K2B_REG(64, 64) ADDA_K2B_REG(64, 128) ADDA_K2B_REG(64, 256)
+			ADDA_K2B_REG(128, 64) ADDA_K2B_REG(128, 128) ADDA_K2B_REG(128, 256)
+			ADDA_K2B_REG(256, 64) ADDA_K2B_REG(256, 128) ADDA_K2B_REG(256, 256)
+#undef ADDA_K2B_REG
+		}
+	}
+	else {
+		// generic K2b: KB kz x RG RHS per block, KB*RG <= pairs (surface: pairs/2 six-line pairs)
+		const int pairs = surf ? sh.pairs / 2 : sh.pairs;
+		MvGeom<T> q = p;
+		q.RG = std::min(R, pairs);
+		q.KB = std::max(1, pairs / q.RG);
+		const dim3 g2b((c->gZ + q.KB - 1) / q.KB, ck, (R + q.RG - 1) / q.RG);
+		const size_t sm = 2 * sizeof(typename CxT<T>::type) * (size_t)c->gY * tile_ls(3 * sh.pairs);
+		if (surf) {
+			ADDA_NS_SWITCH(c->gY, ADDA_W_SWITCH(has_pairs, sh.pairs, (mv_fft_y_surf<T, NS, W><<<g2b, 256, sm, st>>>(q))));
+		}
+		else {
+			ADDA_NS_SWITCH(c->gY, ADDA_W_SWITCH(has_pairs, sh.pairs, (mv_fft_y_dmul<T, NS, W><<<g2b, 256, sm, st>>>(q))));
+		}
+	}
+	ADDA_LAUNCHED();
+	ADDA_NS_SWITCH(c->gZ, ADDA_W_SWITCH(has_w2, sh.w2, (mv_fftz<T, W, 1, NS><<<g2, col_threads<T, NS, W>(),
+		tile_smem<T>(c->gZ, W), st>>>(p))));
+	ADDA_LAUNCHED();
+	return ADDA_GB300_OK;
+}
+
+// the y/z stage and its set-up are compiled once per arithmetic, in matvec_yz.cu
+#ifndef ADDA_MATVEC_YZ_TU
+extern template int launch_yz<float>(adda_gb300_ctx *, MvGeom<float>, int, const MvShape &, cudaStream_t);
+extern template int launch_yz<double>(adda_gb300_ctx *, MvGeom<double>, int, const MvShape &, cudaStream_t);
+extern template int setup_yz<float>();
+extern template int setup_yz<double>();
+#endif
 
 template <typename T, typename V>
 int launch_matvec(adda_gb300_ctx *c, int R, const V *arg, V *res, int her, const MvEpi &epi, const int *done)
 {
 	typedef typename CxT<T>::type C;
 	constexpr bool dbl = sizeof(T) == 8;
-	constexpr int W1 = Tiles<T>::W1, W2 = Tiles<T>::W2;
+	const MvShape sh = c->shape[dbl ? 0 : 1];
 	MvP<T, V> p;
 	p.bX = c->bX; p.bY = c->bY; p.bZ = c->bZ;
 	p.gX = c->gX; p.gY = c->gY; p.gZ = c->gZ;
@@ -708,79 +841,39 @@ int launch_matvec(adda_gb300_ctx *c, int R, const V *arg, V *res, int her, const
 	p.her = her;
 	p.done = done;
 	p.kx0 = 0;
-	p.RG = std::min(R, Tiles<T>::PAIRS);
-	p.KB = std::max(1, Tiles<T>::PAIRS / p.RG);
-	const bool surf = c->surface;
+	p.RG = p.KB = 1;
 	p.TzR = (C *)c->TzR;
 	p.Rm = dbl ? (const C *)c->R64 : (const C *)c->R32;
 	p.RsY = c->gY / 2 + 1;
 	cudaStream_t st = c->stream;
-	const dim3 blk(256);
-	const dim3 g1((c->bY + W1 - 1) / W1, c->bZ, R);
-	ADDA_NS_SWITCH(c->gX, (mv_scatter_fftx<T, V, W1, NS>
-		<<<g1, col_threads<T, NS, 3 * W1>(), smem_k1s<T, NS>(c->gX), st>>>(p)));
+	const dim3 g1((c->bY + sh.w1 - 1) / sh.w1, c->bZ, R);
+	ADDA_NS_SWITCH(c->gX, ADDA_W_SWITCH(has_w1, sh.w1, (mv_scatter_fftx<T, V, W, NS><<<g1, col_threads<T, NS, 3 * W>(),
+		tile_smem<T>(c->gX, 3 * W), st>>>(p))));
 	ADDA_LAUNCHED();
-	for (int kx0 = 0; kx0 < c->gX; kx0 += p.CK) {
-		p.kx0 = kx0;
-		const int ck = std::min(p.CK, c->gX - kx0);
-		const dim3 g2((c->bY + W2 - 1) / W2, 3 * ck, R);
-		ADDA_NS_SWITCH(c->gZ, (mv_fftz<T, V, W2, 0, NS><<<g2, col_threads<T, NS, W2>(), smem_k2s<T, NS>(c->gZ), st>>>(p)));
-		ADDA_LAUNCHED();
-		if (surf) {
-			ADDA_NS_SWITCH(c->gZ, (mv_fftz<T, V, W2, 2, NS><<<g2, col_threads<T, NS, W2>(), smem_k2s<T, NS>(c->gZ), st>>>(p)));
-			ADDA_LAUNCHED();
-		}
-		if (surf && use_k2b_reg<T>(c->gY)) {
-			if constexpr (sizeof(T) == 4) {
-				constexpr int NT = 128;
-				switch (c->gY) {
-#define ADDA_K2B_REG_S(NS)                                                                                          \
-	case NS: {                                                                                                      \
-		constexpr int G = NT / RegShape<NS>::T;                                                                     \
-		const dim3 g((c->gZ * R + G - 1) / G, ck);                                                                  \
-		mv_fft_y_reg<V, NS, NT, true><<<g, NT, G * 4 * RegShape<NS>::BUF * sizeof(float2), st>>>(p);               \
-	} break;
-					ADDA_K2B_REG_S(64)
-					ADDA_K2B_REG_S(128)
-					ADDA_K2B_REG_S(256)
-#undef ADDA_K2B_REG_S
-				}
-			}
-		}
-		else if (surf) {
-			MvP<T, V> q = p;
-			q.RG = std::min(R, Tiles<T>::PAIRS / 2);
-			q.KB = std::max(1, Tiles<T>::PAIRS / 2 / q.RG);
-			const dim3 g2b((c->gZ + q.KB - 1) / q.KB, ck, (R + q.RG - 1) / q.RG);
-			ADDA_NS_SWITCH(c->gY, (mv_fft_y_surf<T, V, NS><<<g2b, blk, smem_k2b<T>(c->gY), st>>>(q)));
-		}
-		else if (use_k2b_reg<T>(c->gY)) {
-			if constexpr (sizeof(T) == 4) {
-				constexpr int NT = 128;
-				switch (c->gY) {
-#define ADDA_K2B_REG(NS)                                                                                            \
-	case NS: {                                                                                                      \
-		constexpr int G = NT / RegShape<NS>::T;                                                                     \
-		const dim3 g((c->gZ * R + G - 1) / G, ck);                                                                  \
-		mv_fft_y_reg<V, NS, NT><<<g, NT, G * 3 * RegShape<NS>::BUF * sizeof(float2), st>>>(p);                      \
-	} break;
-					ADDA_K2B_REG(64)
-					ADDA_K2B_REG(128)
-					ADDA_K2B_REG(256)
-#undef ADDA_K2B_REG
-				}
-			}
-		}
-		else {
-			const dim3 g2b((c->gZ + p.KB - 1) / p.KB, ck, (R + p.RG - 1) / p.RG);
-			ADDA_NS_SWITCH(c->gY, (mv_fft_y_dmul<T, V, NS><<<g2b, blk, smem_k2b<T>(c->gY), st>>>(p)));
-		}
-		ADDA_LAUNCHED();
-		ADDA_NS_SWITCH(c->gZ, (mv_fftz<T, V, W2, 1, NS><<<g2, col_threads<T, NS, W2>(), smem_k2s<T, NS>(c->gZ), st>>>(p)));
-		ADDA_LAUNCHED();
+	// the y/z stage chunk by chunk, even chunks on the context stream with Tz, odd ones on the second stream with Tz2
+	// (a chunk reuses its buffer only after the chunk two before it, on the same stream, has finished with it), so
+	// that one chunk's kernels fill the other's tail; joined before K3
+	int rc;
+	const bool two = c->gX > p.CK;
+	if (two) {
+		ADDA_CUDA(cudaEventRecord(c->ev_fork, st));
+		ADDA_CUDA(cudaStreamWaitEvent(c->stream2, c->ev_fork, 0));
 	}
-	ADDA_NS_SWITCH(c->gX, (mv_fftx_gather<T, V, W1, NS>
-		<<<g1, col_threads<T, NS, 3 * W1>(), smem_k1s<T, NS>(c->gX), st>>>(p, epi)));
+	for (int kx0 = 0, i = 0; kx0 < c->gX; kx0 += p.CK, i++) {
+		MvGeom<T> q = p;
+		q.kx0 = kx0;
+		if (i & 1) {
+			q.Tz = (C *)c->Tz2;
+			q.TzR = (C *)c->TzR2;
+		}
+		if ((rc = launch_yz<T>(c, q, std::min(p.CK, c->gX - kx0), sh, (i & 1) ? c->stream2 : st))) return rc;
+	}
+	if (two) {
+		ADDA_CUDA(cudaEventRecord(c->ev_join, c->stream2));
+		ADDA_CUDA(cudaStreamWaitEvent(st, c->ev_join, 0));
+	}
+	ADDA_NS_SWITCH(c->gX, ADDA_W_SWITCH(has_w1, sh.w1, (mv_fftx_gather<T, V, W, NS><<<g1, col_threads<T, NS, 3 * W>(),
+		tile_smem<T>(c->gX, 3 * W), st>>>(p, epi))));
 	ADDA_LAUNCHED();
 	return ADDA_GB300_OK;
 }

@@ -319,6 +319,7 @@ def run_ours(args):
     t_other = allmax(world, ctx.last_solve_ms() / 1e3)
     # FP32 matvec roofline (R=2 RHS sharing D), and the FP64 matvec time
     mv32 = ctx.time_matvec("fp32", R, iters=20)
+    shape32 = list(ctx.fft_shape("fp32"))
     mv64 = ctx.time_matvec("fp64", R, iters=3)
     bts = matvec_bytes(s.n, s.grid, s.box, 8, R)
     hbm, src = peaks()
@@ -353,7 +354,7 @@ def run_ours(args):
         "Cext": {"mixed": list(map(float, ce)), "fp64": list(map(float, ce64))},
         "Cabs": {"mixed": list(map(float, ca)), "fp64": list(map(float, ca64))},
         "matvec": {"fp32_ms": mv32, "fp64_ms": mv64, "fp32_GBps": achieved, "rhs": R,
-                   "algorithmic_bytes": bts},
+                   "algorithmic_bytes": bts, "fp32_tile_shape (w1, w2, pairs, threads; tuned)": shape32},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "traffic_source": traffic_src,
                      "kernel": "FP32 matvec (K1..K3 sequence, 2 RHS)",
@@ -369,10 +370,16 @@ def run_ours(args):
             line["surface"] = run_surface(args)
         except Exception as ex:  # reported, never fatal for the headline line
             line["surface"] = {"error": str(ex)}
-    if args.with_scale:
-        line["scale_256sphere"] = run_scale(args)
+    if not args.no_scale:
+        try:
+            line["scale_256sphere"] = run_scale(args)
+        except Exception as ex:  # reported, never fatal for the headline line
+            line["scale_256sphere"] = {"error": str(ex)}
     if args.batch_particles:
-        line["batch_ellipsoids"] = run_batch(args)
+        try:
+            line["batch_ellipsoids"] = run_batch(args)
+        except Exception as ex:
+            line["batch_ellipsoids"] = {"error": str(ex)}
     if rank == 0 and world == 1 and not args.no_cpu:
         arm = CpuArm(args.method, os.cpu_count() or 1)
         arm.sample()
@@ -422,10 +429,11 @@ def run_surface(args):
 
 
 def run_scale(args):
-    """the scale workload: sphere on a 256^3 box (N = 8,783,848), FFT grid 512^3, m = 1.2, dpl 10, mixed QMR_CS
-    to 1e-5, both polarisations as 2 RHS, device-resident, capped at --scale-maxiter iterations: QMR_CS converges
-    slowly on this non-absorbing x = 80 sphere (relative residual ~1e-2 after 4000 iterations), so the line reports
-    the time per iteration and the residual reached as well as the time"""
+    """the scale workload: sphere on a 256^3 box (N = 8,783,848), FFT grid 512^3, m = 1.2, dpl 10, mixed solve to
+    1e-5 (BiCGStab by default), both polarisations as 2 RHS, device-resident, capped at --scale-maxiter iterations:
+    the Krylov methods converge slowly on this non-absorbing x = 80 sphere (BiCGStab: relative residual 1.5e-3 after
+    3000 iterations, 1.8e-4 after 9000), so the line reports the time per iteration, the residual reached and the
+    FP32 matvec at 512^3 rather than a time-to-solution"""
     import torch
     import adda_gb300 as A
     s = A.Setup(grid=256, m=1.2, dpl=10)
@@ -436,20 +444,22 @@ def run_scale(args):
     einc = np.ascontiguousarray(np.stack(s.einc))
     d_e = torch.from_numpy(einc.view(np.float64)).cuda()
     log("scale workload: context + D matrix %.2f s, solving (maxiter %d)" % (t_init, args.scale_maxiter))
-    st = ctx.solve_device(d_e.data_ptr(), 2, None, None, method=args.method, prec="mixed", eps=EPS,
+    st = ctx.solve_device(d_e.data_ptr(), 2, None, None, method=args.scale_method, prec="mixed", eps=EPS,
                           maxiter=args.scale_maxiter)
     t_solve = ctx.last_solve_ms() / 1e3
     ce, ca = ctx.cross_sections(np.stack([s.prop, s.prop]), np.stack(s.incpol))
     mv32 = ctx.time_matvec("fp32", 2, iters=5)
     bts = matvec_bytes(s.n, s.grid, s.box, 8, 2)
+    hbm, _ = peaks()
     out = {"workload": "sphere 256^3 box, N=%d, FFT grid %s, m=1.2, dpl=10, mixed %s to 1e-5, 2 RHS"
-           % (s.n, "x".join(map(str, s.grid)), args.method),
+           % (s.n, "x".join(map(str, s.grid)), args.scale_method),
            "solve_s": t_solve, "init_s (D matrix + setup)": t_init, "maxiter": args.scale_maxiter,
            "converged": all(x["status"] == "ok" for x in st), "status": [x["status"] for x in st],
            "ms_per_iteration": 1e3 * t_solve / max(1, max(x["niter"] for x in st)),
            "iterations": [x["niter"] for x in st], "residual": [x["resid"] for x in st],
            "Cext": list(map(float, ce)), "Cabs": list(map(float, ca)),
-           "fp32_matvec_ms": mv32, "fp32_matvec_GBps": bts / (mv32 * 1e-3) / 1e9}
+           "fp32_matvec_ms": mv32, "fp32_matvec_GBps": bts / (mv32 * 1e-3) / 1e9,
+           "fp32_matvec_roofline_frac": bts / (mv32 * 1e-3) / 1e9 / hbm, "fp32_tile_shape": list(ctx.fft_shape())}
     ctx.close()
     return out
 
@@ -482,7 +492,7 @@ def run_batch(args):
                 ctx.set_cc(2 * k + j, A.polarizability(s.m, s.kd, s.gridspace, prop, e).reshape(1, 3))
                 einc.append(A.plane_wave(s.box, s.pos, s.gridspace, s.wavenum, prop, e))
         d_e = torch.from_numpy(np.ascontiguousarray(np.stack(einc)).view(np.float64)).cuda()
-        st = ctx.solve_device(d_e.data_ptr(), nrhs, None, None, method=args.method, prec="mixed", eps=EPS,
+        st = ctx.solve_device(d_e.data_ptr(), nrhs, None, None, method=args.batch_method, prec="mixed", eps=EPS,
                               maxiter=args.batch_maxiter)
         torch.cuda.synchronize()
         total_s += time.perf_counter() - t0
@@ -495,8 +505,8 @@ def run_batch(args):
         boxes.append(box)
         nrhs_done += nrhs
         ctx.close()
-    return {"workload": "%d seeded ellipsoids x 16 orientations x 2 polarisations (%d RHS), mixed %s to 1e-5"
-                        % (args.batch_particles, nrhs_done, args.method),
+    return {"workload": "the first %d of the 64 seeded ellipsoids x 16 orientations x 2 polarisations (%d RHS), "
+                        "mixed %s to 1e-5" % (args.batch_particles, nrhs_done, args.batch_method),
             "solve_s": solve_s, "total_s (lattice + D matrix + solve)": total_s,
             "rhs_per_s_solve": nrhs_done / solve_s, "rhs_per_s_total": nrhs_done / total_s,
             "maxiter": args.batch_maxiter, "rhs_not_converged": unconverged,
@@ -534,11 +544,14 @@ def main():
     ap.add_argument("--method", default="qmr", choices=["qmr", "bicgstab"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-surface", action="store_true", help="skip the substrate variant of the workload")
-    ap.add_argument("--with-scale", action="store_true", help="also time the scale workload (256^3 sphere, 512^3 grid)")
-    ap.add_argument("--batch-particles", type=int, default=0,
-                    help="also time the batching workload (64 seeded ellipsoids x 16 orientations) on this many particles")
-    ap.add_argument("--batch-maxiter", type=int, default=3000, help="iteration cap per particle of the batching workload")
-    ap.add_argument("--scale-maxiter", type=int, default=1000, help="iteration cap of the scale workload")
+    ap.add_argument("--no-scale", action="store_true", help="skip the scale workload (256^3 sphere, 512^3 grid)")
+    ap.add_argument("--batch-particles", type=int, default=4,
+                    help="time the batching workload (64 seeded ellipsoids x 16 orientations) on this many particles "
+                         "(0: skip)")
+    ap.add_argument("--batch-maxiter", type=int, default=4000, help="iteration cap per particle of the batching workload")
+    ap.add_argument("--batch-method", default="bicgstab", choices=["qmr", "bicgstab"])
+    ap.add_argument("--scale-maxiter", type=int, default=300, help="iteration cap of the scale workload")
+    ap.add_argument("--scale-method", default="bicgstab", choices=["qmr", "bicgstab"])
     ap.add_argument("--mode", default="bench", choices=["bench", "profile-solve", "profile-matvec", "profile-surface"])
     ap.add_argument("--grid", type=int, default=GRID, help="sphere box size for the profile modes")
     ap.add_argument("--maxiter", type=int, default=100000, help="iteration cap of the profile-solve mode")

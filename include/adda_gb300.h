@@ -343,6 +343,18 @@ int adda_gb300_scattered_fields(adda_gb300_ctx *ctx, int nrhs, int ndir, const d
  * scratch buffer between launches so every launch starts with a cold L2 */
 int adda_gb300_time_matvec(adda_gb300_ctx *ctx, int prec, int nrhs, int iters, size_t flush_bytes, double *ms);
 
+/* The matvec's tile shape for one arithmetic (prec ADDA_PREC_FP64 or ADDA_PREC_FP32): shape[0] y-lines per block of
+ * the scatter + x-FFT and inverse x-FFT + gather kernels, [1] y-lines per block of the z-FFT kernels, [2] (kz, RHS)
+ * pairs per block of the generic y-FFT + D kernel, [3] threads per block of the register y-FFT + D kernel (FP32).
+ * The library picks the defaults, narrows them for axes longer than 512 (up to 2048 per axis), and tunes the FP32
+ * shape at the first FP32 matvec or solve of a context together with its L2 chunk (the reference plans its FFTs
+ * with FFTW_MEASURE likewise, fft.c:739-815). No counterpart call in the reference: its FFTs are FFTW's. */
+int adda_gb300_get_fft_shape(const adda_gb300_ctx *ctx, int prec, int shape[4]);
+/* set a shape (FP32: the tuner then keeps it; the L2 chunk is still tuned); EINVAL for a shape this build does not
+ * hold for the context's axis lengths or one whose shared memory does not fit a block. The environment variable
+ * ADDA_GB300_FFT_SHAPE="w1,w2,pairs,threads" does the same for every FP32 context. */
+int adda_gb300_set_fft_shape(adda_gb300_ctx *ctx, int prec, const int shape[4]);
+
 /* device time in milliseconds of the last solve on this context: CUDA events recorded on the context's stream at
  * the first and the last kernel of the solve (host-device copies of the host-pointer API excluded) */
 double adda_gb300_last_solve_ms(const adda_gb300_ctx *ctx);
