@@ -26,6 +26,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 NB = 512        # perturbed right-hand sides per batched solve
 TOL_ABS = 1e-5  # |VJP - FD| <= TOL_ABS * max|gradient| + TOL_REL * |gradient|
 TOL_REL = 1e-4
+FD_TOL = 1e-6   # the perturbed solves stop at this fraction of their starting residual
 
 
 def lattice():
@@ -113,7 +114,7 @@ def fd_batch(c, dirs):
     # the starting residuals (relative residual after one iteration from x0) set the tolerance
     st = ctx.solve_device(d_e.data_ptr(), R, d_x.data_ptr(), None, method="qmr", prec="fp64", eps=1e-300,
                           maxiter=1, init="x0")
-    eps = 1e-6 * min(x["resid"] for x in st)
+    eps = FD_TOL * min(x["resid"] for x in st)
     d_x = x0.repeat(R)
     st = ctx.solve_device(d_e.data_ptr(), R, d_x.data_ptr(), None, method="qmr", prec="fp64", eps=eps,
                           maxiter=3000, init="x0")

@@ -1,7 +1,10 @@
 """The FP32 transforms add and subtract complex float2 values with Blackwell's packed add/sub.rn.f32x2; a library
 built with -DADDA_NO_F32X2 does the same sums with scalar round-to-nearest adds. Both must give the same bits: the
 FP32 matvec (power-of-two grids through the register K2b, grids with radices 3/5/7 through the shared-memory
-transforms, the her variant) and a mixed-precision solve are compared bit for bit between the two builds."""
+transforms, the her variant) and a mixed-precision solve are compared bit for bit between the two builds. Both
+contexts get the same FP32 tile shape: the tuner picks it per context by timing, and the y-lines per K3 block set
+the partition of the fused reductions (the sums of |y|^2 would differ in their last bits otherwise)."""
+SHAPE = (8, 16, 8, 128)
 import numpy as np
 import pytest
 
@@ -34,6 +37,8 @@ def test_fp32_matvec_bit_identical(name, scalar_lib):
     s = SETUPS[name]()
     packed = A.Context.from_setup(s, nrhs_max=2)
     scalar = A.Context.from_setup(s, nrhs_max=2, library=scalar_lib)
+    packed.set_fft_shape(SHAPE)
+    scalar.set_fft_shape(SHAPE)
     x = random_vec(s.n, 2, 5)
     for her in (False, True):
         y1, ip1 = packed.matvec(x, "fp32", her)
@@ -50,6 +55,7 @@ def test_mixed_solve_bit_identical(scalar_lib):
     res = []
     for L in (None, scalar_lib):
         ctx = A.Context.from_setup(s, nrhs_max=2, library=L)
+        ctx.set_fft_shape(SHAPE)
         res.append(ctx.solve(np.stack(s.einc), prec="mixed", eps=1e-8))
         ctx.close()
     assert [st["niter"] for st in res[0]["stats"]] == [st["niter"] for st in res[1]["stats"]]
