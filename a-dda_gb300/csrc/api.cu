@@ -318,8 +318,8 @@ int adda_gb300_create(const adda_gb300_problem *p, adda_gb300_ctx **out)
 __global__ void fill_k(double2 *v, size_t n, unsigned seed);
 __global__ void d2f_k(float2 *dst, const double2 *src, size_t n);
 
-// The FP32 matvec's autotuner. The tile shape (threads per register-K2b block, y-lines per K2a/K2c and per K1/K3
-// block) sets occupancy and shared memory per block; the chunk (x-slabs whose z-transformed data pass through L2
+// The FP32 matvec's autotuner. The tile shape (threads per register-K2b block or (kz, RHS) pairs per generic-K2b
+// block, y-lines per K2a/K2c and per K1/K3 block) sets occupancy and shared memory per block; the chunk (x-slabs whose z-transformed data pass through L2
 // between K2a, K2b and K2c) trades L2 residency against launch count and tail waves; the best of both depends on
 // the grid and the RHS count. Measured once per context on its own data sizes: the shape by coordinate descent over
 // the alternatives the build holds (kept when 2 % faster), then balanced splits of the x-slabs into chunks of
@@ -361,17 +361,18 @@ static int tune_chunks(adda_gb300_ctx *c)
 		return true;
 	};
 	// 1. the tile shape, one dimension at a time over the alternatives the build holds (register-K2b threads per
-	// block, then y-lines per K2a/K2c block, then per K1/K3 block), each kept when faster; candidates that do not
-	// fit the axis lengths are skipped
+	// block or generic-K2b pairs per block, then y-lines per K2a/K2c block, then per K1/K3 block), each kept when
+	// faster; candidates that do not fit the axis lengths are skipped
 	if (!c->shape_fixed) {
 		float best = 1e30f;
 		if (!time_mv(best)) goto done;
-		for (int dim = 0; dim < 3; dim++) {
-			static const int cand[3][3] = {{64, 128, 256}, {8, 16, 32}, {4, 8, 8}};
+		for (int dim = 0; dim < 4; dim++) {
+			static const int cand[4][3] = {{64, 128, 256}, {2, 4, 8}, {8, 16, 32}, {4, 8, 8}};
 			for (int k = 0; k < 3; k++) {
 				MvShape sh = c->shape[1], keep = sh;
-				int &field = dim == 0 ? sh.nt : dim == 1 ? sh.w2 : sh.w1;
-				if (field == cand[dim][k] || (dim == 0 && !matvec_k2b_reg(c))) continue;
+				int &field = dim == 0 ? sh.nt : dim == 1 ? sh.pairs : dim == 2 ? sh.w2 : sh.w1;
+				if (field == cand[dim][k] || (dim == 0 && !matvec_k2b_reg(c)) || (dim == 1 && matvec_k2b_reg(c)))
+					continue;
 				field = cand[dim][k];
 				if (!matvec_shape_ok(c, true, sh)) continue;
 				c->shape[1] = sh;

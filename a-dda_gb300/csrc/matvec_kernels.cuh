@@ -648,8 +648,9 @@ inline size_t k2b_reg_smem(int gY, int nt, bool surf)
 constexpr size_t SMEM_CAP = 216 * 1024; // dynamic shared memory of one block (the opt-in limit is 227 KB)
 
 // Tile widths the build instantiates. The defaults (Tiles<T>) everywhere; for FP32 the tuner's alternatives (K1/K3 4
-// y-lines; K2a/K2c 8 or 32; register K2b 64 or 256 threads) for every length; and, for the runtime-plan lengths
-// (above 512 or not a power of two), the narrow tiles of long axes (1 y-line per K1/K3 block, 2 per K2a/K2c block,
+// y-lines; K2a/K2c 8 or 32; register K2b 64 or 256 threads; generic K2b 2 or 4 pairs) for every length; and, for the
+// runtime-plan lengths
+// (above 512 or not a power of two) the narrow tiles of long axes (1 y-line per K1/K3 block, 2 per K2a/K2c block,
 // one (kz, RHS) pair per generic K2b block), whose shared memory fits axes up to 2048 (FP64) / 4096 (FP32).
 template <typename T, int NS, int W> constexpr bool has_w1()
 {
@@ -661,13 +662,14 @@ template <typename T, int NS, int W> constexpr bool has_w2()
 }
 template <typename T, int NS, int P> constexpr bool has_pairs()
 {
-	return P == Tiles<T>::PAIRS || (NS == 0 && P == 1);
+	return P == Tiles<T>::PAIRS || (sizeof(T) == 4 && (P == 2 || P == 4)) || (NS == 0 && P == 1);
 }
 inline bool shape_instantiated(bool f32, int n1, int n2, int ny, const MvShape &s)
 {
 	const bool w1ok = s.w1 == (f32 ? 8 : 4) || (f32 && s.w1 == 4) || (static_len(n1) == 0 && s.w1 == 1);
 	const bool w2ok = s.w2 == (f32 ? 16 : 8) || (f32 && (s.w2 == 8 || s.w2 == 32)) || (static_len(n2) == 0 && s.w2 == 2);
-	const bool pok = s.pairs == (f32 ? 8 : 4) || (static_len(ny) == 0 && s.pairs == 1);
+	const bool pok = s.pairs == (f32 ? 8 : 4) || (f32 && (s.pairs == 2 || s.pairs == 4)) ||
+		(static_len(ny) == 0 && s.pairs == 1);
 	const bool ntok = !f32 || s.nt == 64 || s.nt == 128 || s.nt == 256;
 	return w1ok && w2ok && pok && ntok;
 }

@@ -295,11 +295,12 @@ def run_ours(args):
     for _ in range(args.warmup):
         host_step()
     torch.cuda.synchronize()
-    e2e = []
+    e2e, e2e_dev = [], []
     for _ in range(args.steps):
         t0 = time.perf_counter()
         host_step()  # x and p go straight into the pinned host buffers (the C ABI's xvec/pvec)
         e2e.append(time.perf_counter() - t0)
+        e2e_dev.append(ctx.last_solve_ms() / 1e3)
     t_e2e = allmax(world, statistics.mean(e2e))
     # the variants with FP32 and with FP64 Krylov vectors, once each, for comparison
     st32 = ctx.solve_device(d_e.data_ptr(), R, d_x.data_ptr(), d_p.data_ptr(), prec="mixed_f32vec", **opts)
@@ -360,7 +361,9 @@ def run_ours(args):
                      "kernel": "FP32 matvec (K1..K3 sequence, 2 RHS)",
                      "peak_source": src},
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": einc.nbytes,
-                "d2h_bytes_per_step": 2 * einc.nbytes + 16 * R},
+                "d2h_bytes_per_step": 2 * einc.nbytes + 16 * R,
+                "device_solve_s_mean": statistics.mean(e2e_dev),
+                "iterations_last_step": [rst[r].niter for r in range(R)]},
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }

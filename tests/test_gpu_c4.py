@@ -5,7 +5,7 @@ dipoles, grid 96^3), every dipole with its own refractive index from the seeded 
   ctypes-loaded torch.autograd.Function (tests/autograd_dda.py), against central finite differences (step 1e-6 on
   chi, its real and imaginary part) at the 256 seeded dipoles. The 1024 perturbed FP64 solves run as right-hand
   sides of batched solves, each with its own per-dipole polarisabilities, and start from the unperturbed solution:
-  they solve for the solution's change, to 1e-6 of the size of their own starting residual (a solve from zero to a
+  they solve for the solution's change, to 1e-9 of the size of their own starting residual (a solve from zero to a
   residual of 1e-12 would leave errors comparable to the change itself); the cross-section differences are formed
   from the difference of the two polarisation vectors before summing (two full FP64 sums over 110,592 dipoles
   differ by rounding more than a step of 1e-6 at one dipole changes them).
@@ -26,7 +26,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 NB = 512        # perturbed right-hand sides per batched solve
 TOL_ABS = 1e-5  # |VJP - FD| <= TOL_ABS * max|gradient| + TOL_REL * |gradient|
 TOL_REL = 1e-4
-FD_TOL = 1e-6   # the perturbed solves stop at this fraction of their starting residual
+FD_TOL = 1e-9   # the perturbed solves stop at this fraction of their starting residual
 
 
 def lattice():
@@ -98,7 +98,7 @@ def cross_differences(xp, xm, S0, w0, E, k, sp_j, sm_j, wp_j, wm_j, j):
 
 def fd_batch(c, dirs):
     """central differences (dCext, dCabs)/(2h) for dirs = [(j, +dz), (j, -dz), ...] (pairs adjacent): the perturbed
-    solves as right-hand sides of one FP64 solve from the unperturbed solution, to 1e-6 of the smallest starting
+    solves as right-hand sides of one FP64 solve from the unperturbed solution, to FD_TOL of the smallest starting
     residual, and the differences of their polarisations"""
     import torch
     s, ctx, n = c["s"], c["ctx"], c["s"].n
@@ -115,6 +115,7 @@ def fd_batch(c, dirs):
     st = ctx.solve_device(d_e.data_ptr(), R, d_x.data_ptr(), None, method="qmr", prec="fp64", eps=1e-300,
                           maxiter=1, init="x0")
     eps = FD_TOL * min(x["resid"] for x in st)
+    c["last_eps"] = eps
     d_x = x0.repeat(R)
     st = ctx.solve_device(d_e.data_ptr(), R, d_x.data_ptr(), None, method="qmr", prec="fp64", eps=eps,
                           maxiter=3000, init="x0")

@@ -1,6 +1,6 @@
 """Tile shapes of the matvec kernels: every FP32 shape the autotuner can pick (register-K2b threads 64/128/256 x
 z-FFT y-lines 8/16/32 x x-FFT y-lines 4/8) gives the oracle's matvec on lattices whose y axis takes the register K2b
-with 8 and with 16 lanes per line; axes longer than 512 (600 along each axis, 1024 along x) run with the narrow
+with 8 and with 16 lanes per line, and so does the generic K2b with 2, 4 and 8 pairs per block; axes longer than 512 (600 along each axis, 1024 along x) run with the narrow
 tiles the library picks for them, in FP64 and FP32, against the oracle; an unsupported shape is refused; and the
 tuner leaves a shape the build holds."""
 import itertools
@@ -69,6 +69,19 @@ def test_long_axes_match_oracle(box):
     res = ctx.solve(np.stack(s.einc), prec="fp64", eps=1e-8)
     o.set_cc(s.cc[0].reshape(1, 3))
     assert rel(res["p"][0], o.solve(s.einc[0], eps=1e-8)["p"]) < 1e-7
+    o.close()
+    ctx.close()
+
+
+@pytest.mark.parametrize("pairs", [2, 4, 8])
+def test_generic_k2b_pairs_match_oracle(pairs):
+    """the generic K2b (y axis not 64/128/256: here 40) with every pair count the tuner can pick"""
+    import adda_gb300 as A
+    s = box_setup((16, 20, 12))
+    o = oracle_for(s)
+    ctx = A.Context.from_setup(s, nrhs_max=2)
+    ctx.set_fft_shape((8, 16, pairs, 128))
+    check_matvec(s, ctx, o, precs=("fp32",))
     o.close()
     ctx.close()
 
