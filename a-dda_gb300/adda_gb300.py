@@ -107,7 +107,7 @@ EXPORTS = ["adda_gb300_fft_fit", "adda_gb300_fit_box", "adda_gb300_make_particle
            "adda_gb300_cross_sections", "adda_gb300_scattered_fields", "adda_gb300_integr_points",
            "adda_gb300_romberg2d", "adda_gb300_romberg2d_ex", "adda_gb300_scattering_integrals",
            "adda_gb300_cross_sections_noalloc", "adda_gb300_time_matvec", "adda_gb300_read_int_tables",
-           "adda_gb300_get_fft_shape", "adda_gb300_set_fft_shape",
+           "adda_gb300_get_fft_shape", "adda_gb300_set_fft_shape", "adda_gb300_get_l2_chunk", "adda_gb300_set_stream",
            "adda_gb300_last_solve_ms", "adda_gb300_last_error", "adda_gb300_kernel_launches"]
 
 _lib = None
@@ -178,6 +178,8 @@ def load_library(path):
         "adda_gb300_read_int_tables": ([ctypes.c_char_p, P], I),
         "adda_gb300_get_fft_shape": ([P, I, P], I),
         "adda_gb300_set_fft_shape": ([P, I, P], I),
+        "adda_gb300_get_l2_chunk": ([P, I], I),
+        "adda_gb300_set_stream": ([P, P], I),
         "adda_gb300_last_error": ([], ctypes.c_char_p),
         "adda_gb300_last_solve_ms": ([P], D),
         "adda_gb300_kernel_launches": ([], ctypes.c_uint64),
@@ -549,7 +551,8 @@ class Context:
 
     def solve_device(self, d_einc, nrhs, d_x=None, d_p=None, method="qmr", prec="mixed", eps=1e-5, maxiter=100000,
                      init="auto", check_every=0, inner_eps=0.0, max_refine=0, final_eps=0.0):
-        """solve on device-resident buffers (raw CUDA pointers as ints, double2 [nrhs][3N])"""
+        """solve on device-resident buffers (raw CUDA pointers as ints, double2 [nrhs][3N]); the solve reads them after
+        the work queued on the stream of set_stream (by default the legacy default stream, torch's default)"""
         st = (RhsStats * nrhs)()
         sp = SolveParams(ITERS[method], PREC[prec], eps, maxiter, INIT[init], check_every, inner_eps, max_refine,
                          0.0, 0, final_eps)
@@ -594,9 +597,19 @@ class Context:
         _check(self.L.adda_gb300_get_fft_shape(self.h, PREC[prec], v), "get_fft_shape")
         return tuple(v)
 
+    def l2_chunk(self, prec="fp32"):
+        """x-slabs per chunk of the matvec's y/z stage"""
+        return self.L.adda_gb300_get_l2_chunk(self.h, PREC[prec])
+
     def set_fft_shape(self, shape, prec="fp32"):
         """fix the matvec's tile shape (fp32: no tuning of it)"""
         _check(self.L.adda_gb300_set_fft_shape(self.h, PREC[prec], (ctypes.c_int * 4)(*shape)), "set_fft_shape")
+
+    def set_stream(self, stream=None):
+        """the caller's stream the device-buffer calls order themselves with: a torch.cuda.Stream, a raw
+        cudaStream_t as int, or None for the legacy default stream"""
+        ptr = getattr(stream, "cuda_stream", stream)
+        _check(self.L.adda_gb300_set_stream(self.h, ctypes.c_void_p(ptr) if ptr else None), "set_stream")
 
     def last_solve_ms(self):
         """device milliseconds of the last solve (CUDA events on the context stream)"""

@@ -106,6 +106,8 @@ static int create_impl(const adda_gb300_problem *p, adda_gb300_ctx *c)
 	ADDA_CUDA(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
 	ADDA_CUDA(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
 	ADDA_CUDA(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+	ADDA_CUDA(cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming));
+	ADDA_CUDA(cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming));
 	c->bX = p->boxX; c->bY = p->boxY; c->bZ = p->boxZ;
 	c->gX = p->gridX > 0 ? p->gridX : adda_gb300_fft_fit(2 * p->boxX, 1);
 	c->gY = p->gridY > 0 ? p->gridY : adda_gb300_fft_fit(2 * p->boxY, 1);
@@ -283,6 +285,8 @@ int adda_gb300_destroy(adda_gb300_ctx *c)
 		if (b) cudaFree(b);
 	if (c->ev_fork) cudaEventDestroy(c->ev_fork);
 	if (c->ev_join) cudaEventDestroy(c->ev_join);
+	if (c->ev_in) cudaEventDestroy(c->ev_in);
+	if (c->ev_out) cudaEventDestroy(c->ev_out);
 	if (c->stream2) cudaStreamDestroy(c->stream2);
 	if (c->stream) cudaStreamDestroy(c->stream);
 	delete c;
@@ -420,6 +424,12 @@ int adda_gb300_get_fft_shape(const adda_gb300_ctx *c, int prec, int shape[4])
 	shape[2] = s.pairs;
 	shape[3] = s.nt;
 	return ADDA_GB300_OK;
+}
+
+int adda_gb300_get_l2_chunk(const adda_gb300_ctx *c, int prec)
+{
+	if (!c || (prec != ADDA_PREC_FP64 && prec != ADDA_PREC_FP32)) return ADDA_GB300_EINVAL;
+	return prec == ADDA_PREC_FP32 ? c->CK32 : c->CK64;
 }
 
 int adda_gb300_set_fft_shape(adda_gb300_ctx *c, int prec, const int shape[4])
@@ -589,6 +599,32 @@ __global__ void f2d_k(double2 *dst, const float2 *src, size_t n)
 		dst[t] = make_double2(src[t].x, src[t].y);
 }
 
+// the context's stream waits for the work queued on the caller's stream so far (inputs a caller filled there)
+static int after_caller(adda_gb300_ctx *c)
+{
+	ADDA_CUDA(cudaEventRecord(c->ev_in, c->order));
+	ADDA_CUDA(cudaStreamWaitEvent(c->stream, c->ev_in, 0));
+	return ADDA_GB300_OK;
+}
+
+// the caller's stream waits for the work queued on the context's stream so far (results the caller reads there)
+static int caller_after(adda_gb300_ctx *c)
+{
+	ADDA_CUDA(cudaEventRecord(c->ev_out, c->stream));
+	ADDA_CUDA(cudaStreamWaitEvent(c->order, c->ev_out, 0));
+	return ADDA_GB300_OK;
+}
+
+int adda_gb300_set_stream(adda_gb300_ctx *c, void *stream)
+{
+	if (!c) {
+		set_error("set_stream: invalid arguments");
+		return ADDA_GB300_EINVAL;
+	}
+	c->order = stream ? (cudaStream_t)stream : cudaStreamLegacy;
+	return ADDA_GB300_OK;
+}
+
 int adda_gb300_matvec_device(adda_gb300_ctx *c, int prec, int nrhs, const void *d_arg, void *d_res, double *d_inprod,
 	int her)
 {
@@ -598,6 +634,8 @@ int adda_gb300_matvec_device(adda_gb300_ctx *c, int prec, int nrhs, const void *
 	}
 	int rc = check_ready(c, nrhs);
 	if (rc) return rc;
+	ADDA_CUDA(cudaSetDevice(c->device));
+	if ((rc = after_caller(c))) return rc;
 	const bool dbl = prec == ADDA_PREC_FP64;
 	MvEpi e{d_inprod ? (int)EPI_NORM : (int)EPI_NONE, nullptr, c->partial};
 	if (dbl) rc = matvec_run<double>(c, nrhs, (const double2 *)d_arg, (double2 *)d_res, her, e, nullptr);
@@ -610,7 +648,7 @@ int adda_gb300_matvec_device(adda_gb300_ctx *c, int prec, int nrhs, const void *
 		ADDA_CUDA(cudaMemcpy2DAsync(d_inprod, sizeof(double), c->d_red, 4 * sizeof(double), sizeof(double), nrhs,
 			cudaMemcpyDeviceToDevice, c->stream));
 	}
-	return ADDA_GB300_OK;
+	return caller_after(c);
 }
 
 int adda_gb300_matvec(adda_gb300_ctx *c, int prec, int nrhs, const double *argvec, double *resultvec, double *inprod,
@@ -740,6 +778,7 @@ int adda_gb300_solve_device(adda_gb300_ctx *c, const adda_gb300_solve_params *sp
 	int rc = check_ready(c, nrhs);
 	if (rc) return rc;
 	ADDA_CUDA(cudaSetDevice(c->device));
+	if ((rc = after_caller(c))) return rc;
 	return solver_solve_dev(c, sp, nrhs, (const double2 *)d_einc, (double2 *)d_xvec, (double2 *)d_pvec, stats);
 }
 

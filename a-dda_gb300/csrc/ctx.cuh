@@ -105,6 +105,9 @@ struct adda_gb300_ctx {
 	void *Tz2 = nullptr, *TzR2 = nullptr;
 	cudaStream_t stream2 = nullptr;
 	cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+	// the caller's stream the device-buffer entry points order themselves with (legacy default stream unless set)
+	cudaStream_t order = cudaStreamLegacy;
+	cudaEvent_t ev_in = nullptr, ev_out = nullptr;
 	int CK64 = 1, CK32 = 1;           // x-slabs per chunk (sized to stay resident in L2)
 	int CK32max = 1;                  // largest FP32 chunk the Tz buffer holds
 	bool chunk_fixed = false;         // chunk size set by the environment: no tuning

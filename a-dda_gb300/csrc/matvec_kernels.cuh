@@ -354,7 +354,7 @@ template <typename T, int NS, int P> __global__ void __launch_bounds__(256) mv_f
 	}
 }
 
-// K2b, register form for FP32 and power-of-two gY <= 256: one group of T lanes per (kx, kz, rhs) column; each
+// K2b, register form for FP32 and power-of-two gY <= 512: one group of T lanes per (kx, kz, rhs) column; each
 // component line goes from Tz straight into registers (lane j1 holds y = j1 + T*j: half-warp rows of 128 B) and is
 // transformed by reg_fft (one transpose through a slot of the group's shared memory, no block barrier). The spectra
 // of components 0 and 1 are parked in their slots (lane-interleaved: conflict-free) while component 2 stays in
@@ -366,7 +366,8 @@ template <typename T, int NS, int P> __global__ void __launch_bounds__(256) mv_f
 // the reflected product R~.u (M21 = M12, M31 = -M13, M32 = -M23, cReflMatrVec cmplx.h:391-401; R reduced in y only)
 // to the three result components before the inverse transforms.
 template <int NS, int NT, bool SURF = false>
-__global__ void __launch_bounds__(NT, (SURF ? 3 : 4) * 128 / NT) mv_fft_y_reg(MvGeom<float> p)
+__global__ void __launch_bounds__(NT, NS >= 512 ? (NT >= 256 ? 1 : 256 / NT) : (SURF ? 3 : 4) * 128 / NT)
+	mv_fft_y_reg(MvGeom<float> p)
 {
 	typedef float2 C;
 	constexpr int T = RegShape<NS>::T, E = RegShape<NS>::E, BUF = RegShape<NS>::BUF, G = NT / T;
@@ -624,10 +625,11 @@ inline int static_len(int n)
 	return (n == 64 || n == 128 || n == 256 || n == 512) ? n : 0;
 }
 
-// K2b in register form (mv_fft_y_reg): FP32 arithmetic, power-of-two gY up to 256 (E <= 16 registers per component)
+// K2b in register form (mv_fft_y_reg): FP32 arithmetic, power-of-two gY up to 512 (E = 32 complex registers per
+// component at 512, compiled for fewer resident blocks)
 template <typename T> inline bool use_k2b_reg(int gY)
 {
-	return sizeof(T) == 4 && (gY == 64 || gY == 128 || gY == 256);
+	return sizeof(T) == 4 && (gY == 64 || gY == 128 || gY == 256 || gY == 512);
 }
 
 // shared memory of a tile kernel for nl lines of length n: one tile in the column form (FP32, compile-time length),
@@ -719,7 +721,7 @@ template <typename T, int NS> int set_attrs_yz()
 			ADDA_SET((mv_fftz<T, W, 2, NS>)))
 		ADDA_W_SWITCH(has_pairs, w, ADDA_SET((mv_fft_y_dmul<T, NS, W>)); ADDA_SET((mv_fft_y_surf<T, NS, W>)))
 	}
-	if constexpr (sizeof(T) == 4 && NS >= 64 && NS <= 256) {
+	if constexpr (sizeof(T) == 4 && NS >= 64) {
 		ADDA_SET((mv_fft_y_reg<NS, 64>));
 		ADDA_SET((mv_fft_y_reg<NS, 128>));
 		ADDA_SET((mv_fft_y_reg<NS, 256>));
@@ -766,7 +768,7 @@ template <typename T> int launch_yz(adda_gb300_ctx *c, MvGeom<T> p, int ck, cons
 	if (use_k2b_reg<T>(c->gY)) {
 		if constexpr (sizeof(T) == 4) {
 			const int nt = sh.nt;
-			const int Tl = c->gY == 256 ? 16 : 8; // lanes per line, RegShape<gY>::T
+			const int Tl = c->gY >= 256 ? 16 : 8; // lanes per line, RegShape<gY>::T
 			const int G = nt / Tl;
 			const dim3 g((c->gZ * R + G - 1) / G, ck);
 			const size_t sm = k2b_reg_smem(c->gY, nt, surf);
@@ -778,6 +780,7 @@ template <typename T> int launch_yz(adda_gb300_ctx *c, MvGeom<T> p, int ck, cons
 			ADDA_K2B_REG(64, 64) ADDA_K2B_REG(64, 128) ADDA_K2B_REG(64, 256)
 			ADDA_K2B_REG(128, 64) ADDA_K2B_REG(128, 128) ADDA_K2B_REG(128, 256)
 			ADDA_K2B_REG(256, 64) ADDA_K2B_REG(256, 128) ADDA_K2B_REG(256, 256)
+			ADDA_K2B_REG(512, 64) ADDA_K2B_REG(512, 128) ADDA_K2B_REG(512, 256)
 #undef ADDA_K2B_REG
 		}
 	}

@@ -320,7 +320,7 @@ def run_ours(args):
     t_other = allmax(world, ctx.last_solve_ms() / 1e3)
     # FP32 matvec roofline (R=2 RHS sharing D), and the FP64 matvec time
     mv32 = ctx.time_matvec("fp32", R, iters=20)
-    shape32 = list(ctx.fft_shape("fp32"))
+    shape32 = list(ctx.fft_shape("fp32")) + ["chunk %d x-slabs" % ctx.l2_chunk("fp32")]
     mv64 = ctx.time_matvec("fp64", R, iters=3)
     bts = matvec_bytes(s.n, s.grid, s.box, 8, R)
     hbm, src = peaks()
@@ -535,7 +535,9 @@ def run_profile(args):
         print(json.dumps({"mode": args.mode, "ms": ctx.last_solve_ms(), "stats": st}))
     else:
         ms = ctx.time_matvec("fp32", 2, iters=3)
-        print(json.dumps({"mode": args.mode, "fp32_matvec_ms": ms}))
+        slab_mb = 2 * 3 * s.grid[2] * s.box[1] * 8 / 2 ** 20
+        print(json.dumps({"mode": args.mode, "fp32_matvec_ms": ms, "shape": list(ctx.fft_shape("fp32")),
+                          "chunk_slabs": ctx.l2_chunk("fp32"), "chunk_mb": ctx.l2_chunk("fp32") * slab_mb}))
 
 
 def main():

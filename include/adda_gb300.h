@@ -250,7 +250,9 @@ int adda_gb300_set_cc_dipole(adda_gb300_ctx *ctx, int rhs, const double *cc);
  * RHS. prec = ADDA_PREC_FP64 or ADDA_PREC_FP32 (the FP32 path rounds the inputs to complex float). */
 int adda_gb300_matvec(adda_gb300_ctx *ctx, int prec, int nrhs, const double *argvec, double *resultvec,
 	double *inprod, int her);
-/* same, on DEVICE buffers (double2 for FP64, float2 for FP32) on the context's stream; no host synchronisation */
+/* same, on DEVICE buffers (double2 for FP64, float2 for FP32) on the context's stream; no host synchronisation.
+ * The call starts after the work queued before it on the caller's stream (adda_gb300_set_stream) and work queued on
+ * that stream after the call runs after the results are written. */
 int adda_gb300_matvec_device(adda_gb300_ctx *ctx, int prec, int nrhs, const void *d_argvec, void *d_resultvec,
 	double *d_inprod, int her);
 
@@ -278,9 +280,17 @@ int adda_gb300_chpoint_save(adda_gb300_ctx *ctx, int rhs, void *buf, size_t size
 int adda_gb300_chpoint_load(adda_gb300_ctx *ctx, int rhs, const void *buf, size_t size);
 
 /* same as adda_gb300_solve with DEVICE buffers (double2 [nrhs][ndip][3]) for einc and the optional d_xvec/d_pvec:
- * nothing crosses PCIe/C2C except the per-RHS stats and the convergence flags polled between graph launches */
+ * nothing crosses PCIe/C2C except the per-RHS stats and the convergence flags polled between graph launches. The
+ * solve reads d_einc and d_xvec after the work queued before the call on the caller's stream (adda_gb300_set_stream)
+ * and returns when d_xvec and d_pvec are written. */
 int adda_gb300_solve_device(adda_gb300_ctx *ctx, const adda_gb300_solve_params *sp, int nrhs, const void *d_einc,
 	void *d_xvec, void *d_pvec, adda_gb300_rhs_stats *stats);
+
+/* The caller's stream for the device-buffer calls (adda_gb300_matvec_device, adda_gb300_solve_device): a cudaStream_t
+ * of the context's device, or NULL for the legacy default stream (the default). The context computes on streams of
+ * its own that do not synchronise with other streams, so buffers a caller fills on a stream must be ordered before
+ * the call through this stream (or be complete: e.g. after a cudaStreamSynchronize). */
+int adda_gb300_set_stream(adda_gb300_ctx *ctx, void *stream);
 
 /* Several particles at once (uneven grids): solves context i for nrhs[i] right-hand sides einc[i] (host), writing
  * xvec[i]/pvec[i] (host, may be NULL) and stats[i] (nrhs[i] entries, may be NULL). The contexts run concurrently, each
@@ -350,6 +360,8 @@ int adda_gb300_time_matvec(adda_gb300_ctx *ctx, int prec, int nrhs, int iters, s
  * shape at the first FP32 matvec or solve of a context together with its L2 chunk (the reference plans its FFTs
  * with FFTW_MEASURE likewise, fft.c:739-815). No counterpart call in the reference: its FFTs are FFTW's. */
 int adda_gb300_get_fft_shape(const adda_gb300_ctx *ctx, int prec, int shape[4]);
+/* x-slabs per chunk of the y/z stage (the L2 chunk; FP32: tuned with the shape), or EINVAL */
+int adda_gb300_get_l2_chunk(const adda_gb300_ctx *ctx, int prec);
 /* set a shape (FP32: the tuner then keeps it; the L2 chunk is still tuned); EINVAL for a shape this build does not
  * hold for the context's axis lengths or one whose shared memory does not fit a block. The environment variable
  * ADDA_GB300_FFT_SHAPE="w1,w2,pairs,threads" does the same for every FP32 context. */

@@ -1,6 +1,6 @@
 """Tile shapes of the matvec kernels: every FP32 shape the autotuner can pick (register-K2b threads 64/128/256 x
 z-FFT y-lines 8/16/32 x x-FFT y-lines 4/8) gives the oracle's matvec on lattices whose y axis takes the register K2b
-with 8 and with 16 lanes per line, and so does the generic K2b with 2, 4 and 8 pairs per block; axes longer than 512 (600 along each axis, 1024 along x) run with the narrow
+with 8 and with 16 lanes per line (y axes of 64, 256 and 512), and so does the generic K2b with 2, 4 and 8 pairs per block; axes longer than 512 (600 along each axis, 1024 along x) run with the narrow
 tiles the library picks for them, in FP64 and FP32, against the oracle; an unsupported shape is refused; and the
 tuner leaves a shape the build holds."""
 import itertools
@@ -37,7 +37,8 @@ def check_matvec(s, ctx, o, precs=("fp64", "fp32")):
                 assert rel(ys["fp32"][r], yr) < 5e-6
 
 
-@pytest.mark.parametrize("box", [(32, 32, 32), (8, 128, 8)], ids=["grid64_lanes8", "gridY256_lanes16"])
+@pytest.mark.parametrize("box", [(32, 32, 32), (8, 128, 8), (4, 256, 4)],
+                         ids=["grid64_lanes8", "gridY256_lanes16", "gridY512_lanes16"])
 def test_every_tuner_shape_matches_oracle(box):
     import adda_gb300 as A
     s = box_setup(box)

@@ -122,6 +122,24 @@ def test_matvec_register_k2b_surface(grid):
         assert rel(y32[r], want) < 3e-6, (grid, r, rel(y32[r], want))
 
 
+def test_matvec_register_k2b_surface_y512():
+    """the same through the register-form K2b with a 512-point y axis (a 4 x 256 x 4 box), plain and Hermitian"""
+    import adda_gb300 as A
+    d = 2 * np.pi / 15
+    s = A.Setup(grid=4, shape="box", pars=(64, 1), m=1.33 + 0.01j, dpl=15, prop=[0, 0, -1],
+                surface=dict(h=3 * d, msub=1.5, relation="img"))
+    assert s.grid[1] == 512
+    ctx = context(s, 2)
+    o = oracle_for(s)
+    x = random_vec(s.n, 2, 17)
+    for her in (False, True):
+        y32, _ = ctx.matvec(x, "fp32", her)
+        for r in range(2):
+            o.set_cc(s.cc[r].reshape(1, 3))
+            want, _ = o.matvec(x[r], her)
+            assert rel(y32[r], want) < 3e-6, (her, r, rel(y32[r], want))
+
+
 @pytest.mark.parametrize("name", list(BY))
 def test_solve_gives_reference_cross_sections(name):
     c = BY[name]
