@@ -726,6 +726,11 @@ template <typename C> __device__ __forceinline__ void cp_async_elem(C *dst, cons
 	else
 		asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(n) : "memory");
 }
+// bulk prefetch of bytes (a multiple of 16) at a 16-byte aligned global address into L2 (no completion to wait for)
+__device__ __forceinline__ void prefetch_l2_bulk(const void *src, unsigned bytes)
+{
+	asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(src), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 

@@ -383,6 +383,13 @@ __global__ void __launch_bounds__(NT, NS >= 512 ? (NT >= 256 ? 1 : 256 / NT) : (
 	C *slot = reinterpret_cast<C *>(smem_raw) + (size_t)g * NSLOT * BUF; // slots c*BUF, c = 0..NSLOT-1
 	const size_t lz = (size_t)p.gZ * p.bY;
 	C *col = p.Tz + (((size_t)r * p.CK + kxl) * 3) * lz + (size_t)kz * p.bY;
+	// the column's D row (and R row) start moving into L2 now, so that the product after the forward transforms
+	// finds them there; one lane of the first RHS's group asks (rows of 6 complex per ky: multiples of 48 bytes)
+	if (j1 == 0 && r == 0) {
+		prefetch_l2_bulk(p.D + ((size_t)kx * p.DsZ + (kz >= p.DsZ ? p.gZ - kz : kz)) * p.DsY * 6,
+			(unsigned)(p.DsY * 6 * sizeof(C)));
+		if constexpr (SURF) prefetch_l2_bulk(p.Rm + ((size_t)kx * p.gZ + kz) * p.RsY * 6, (unsigned)(p.RsY * 6 * sizeof(C)));
+	}
 	// the three component lines go to their slots asynchronously (lane j1 writes and later reads only its own
 	// elements, at j*T + j1), one commit group each, so components 1 and 2 arrive during component 0's transform
 #pragma unroll
