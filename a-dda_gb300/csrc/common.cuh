@@ -566,6 +566,42 @@ template <typename C, int R> __device__ __forceinline__ void dft(C *v, bool inv,
 	else if constexpr (R == 5 || R == 7 || R == 11 || R == 13) dft_odd<C, R>(v, inv);
 }
 
+// v * exp(-/+ i k pi/16) (forward / inverse), k in [0, 16): k is a constant after unrolling, so every branch folds
+template <typename C> __device__ __forceinline__ C rot_pi16(C v, int k, bool inv)
+{
+	// cos(k pi/16), k = 0..8
+	const double c[9] = {1.0, 0.98078528040323044913, 0.92387953251128675613, 0.83146961230254523708,
+		0.70710678118654752440, 0.55557023301960222474, 0.38268343236508977173, 0.19509032201612826785, 0.0};
+	const double sg = inv ? 1.0 : -1.0;
+	if (k == 0) return v;
+	if (k == 8) return cmi(v, inv);
+	const double cs = k < 8 ? c[k] : -c[16 - k];
+	const double sn = k < 8 ? c[8 - k] : c[k - 8];
+	return crot(v, cs, sg * sn);
+}
+
+// DFT of length R (8, 16 or 32) of a line whose upper half is zero (v[j] = 0 for j >= R/2; those registers are not
+// read): X[2m] = DFT_(R/2)(x)[m] and X[2m+1] = DFT_(R/2)(x_j W_R^j)[m]. Every zero-padded transform of the matvec
+// starts like this (an axis of the FFT grid is at least twice the particle's), and it saves the R complex sums of
+// the full transform's last stage.
+template <typename C, int R> __device__ __forceinline__ void dft_half_in(C *v, bool inv)
+{
+	constexpr int H = R / 2;
+	C e[H], o[H];
+#pragma unroll
+	for (int j = 0; j < H; j++) {
+		e[j] = v[j];
+		o[j] = rot_pi16(v[j], j * (32 / R), inv);
+	}
+	dft<C, H>(e, inv, nullptr, R);
+	dft<C, H>(o, inv, nullptr, R);
+#pragma unroll
+	for (int m = 0; m < H; m++) {
+		v[2 * m] = e[m];
+		v[2 * m + 1] = o[m];
+	}
+}
+
 // One Stockham pass over all lines of an element-major tile: x -> y.
 template <typename C, int R>
 __device__ __forceinline__ void fft_pass(const C *__restrict__ x, C *__restrict__ y, int n, int nl, int ls, int m,
@@ -747,11 +783,13 @@ template <int N> struct RegShape {
 	static constexpr int BUF = E * (T + 1);             // complex elements of a line's transpose buffer
 };
 
-template <typename C, int N, bool INV>
+// HALF_IN: the line's upper half is zero (v[j] for j >= E/2 is not read).
+template <typename C, int N, bool INV, bool HALF_IN = false>
 __device__ __forceinline__ void reg_fft(C *v, C *buf, int j1, unsigned gmask, const C *__restrict__ tw)
 {
 	constexpr int T = RegShape<N>::T, E = RegShape<N>::E;
-	dft<C, E>(v, INV, tw, N);
+	if constexpr (HALF_IN) dft_half_in<C, E>(v, INV);
+	else dft<C, E>(v, INV, tw, N);
 #pragma unroll
 	for (int k2 = 1; k2 < E; k2++) {
 		C t = __ldg(tw + j1 * k2);
@@ -779,15 +817,17 @@ __device__ __forceinline__ void reg_fft(C *v, C *buf, int j1, unsigned gmask, co
 // Y[j1][k2] goes to element k2*T + ((j1 + k2) mod T): for a fixed k2 the T lanes write T consecutive elements, and
 // the step-2 reads (lane j1 takes column k2 = j1 + i*T, rows q) hit T consecutive elements modulo T too, so with an
 // odd LS both phases are bank-conflict-free. The result is written back in natural order. The caller synchronises
-// the block before (tile filled) and after (tile read by other lanes).
-template <typename C, int N, int LS, bool INV>
+// the block before (tile filled) and after (tile read by other lanes). HALF_IN: elements N/2.. of the column are zero
+// and not read; HALF_OUT: only elements 0..N/2-1 of the result are written back.
+template <typename C, int N, int LS, bool INV, bool HALF_IN = false, bool HALF_OUT = false>
 __device__ __forceinline__ void col_fft(C *a, int l, int j1, unsigned gmask, const C *__restrict__ tw)
 {
 	constexpr int T = RegShape<N>::T, E = RegShape<N>::E;
 	C v[E];
 #pragma unroll
-	for (int j = 0; j < E; j++) v[j] = a[(j1 + T * j) * LS + l];
-	dft<C, E>(v, INV, tw, N);
+	for (int j = 0; j < (HALF_IN ? E / 2 : E); j++) v[j] = a[(j1 + T * j) * LS + l];
+	if constexpr (HALF_IN) dft_half_in<C, E>(v, INV);
+	else dft<C, E>(v, INV, tw, N);
 #pragma unroll
 	for (int k2 = 1; k2 < E; k2++) {
 		C t = __ldg(tw + j1 * k2);
@@ -812,17 +852,17 @@ __device__ __forceinline__ void col_fft(C *a, int l, int j1, unsigned gmask, con
 #pragma unroll
 	for (int i = 0; i < E / T; i++)
 #pragma unroll
-		for (int k1 = 0; k1 < T; k1++) a[(j1 + i * T + E * k1) * LS + l] = v[i * T + k1];
+		for (int k1 = 0; k1 < (HALF_OUT ? T / 2 : T); k1++) a[(j1 + i * T + E * k1) * LS + l] = v[i * T + k1];
 }
 
 // FFT of all NL columns of an element-major tile by NT threads in groups of T lanes (line l = group, group + G, ...)
-template <typename C, int N, int NL, int LS, int NT, bool INV>
+template <typename C, int N, int NL, int LS, int NT, bool INV, bool HALF_IN = false, bool HALF_OUT = false>
 __device__ __forceinline__ void tile_cols_fft(C *a, const C *__restrict__ tw)
 {
 	constexpr int T = RegShape<N>::T, G = NT / T;
 	const int g = threadIdx.x / T, j1 = threadIdx.x % T;
 	const unsigned gmask = ((1u << T) - 1u) << ((threadIdx.x & 31) & ~(T - 1));
-	for (int l = g; l < NL; l += G) col_fft<C, N, LS, INV>(a, l, j1, gmask, tw);
+	for (int l = g; l < NL; l += G) col_fft<C, N, LS, INV, HALF_IN, HALF_OUT>(a, l, j1, gmask, tw);
 	__syncthreads();
 }
 

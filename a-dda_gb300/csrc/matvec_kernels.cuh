@@ -108,7 +108,8 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T,
 	C *b = a + (size_t)n * LS; // second tile of the Stockham form only
 	const int r = blockIdx.z, z = blockIdx.y, y0 = blockIdx.x * W;
 	const int wy = min(W, p.bY - y0);
-	for (int t = threadIdx.x; t < n * LS; t += NT) a[t] = cx<C>(0, 0);
+	// the column form reads elements x < gX/2 only (gX >= 2 bX for the power-of-two lengths it is built for)
+	for (int t = threadIdx.x; t < (RC ? n / 2 : n) * LS; t += NT) a[t] = cx<C>(0, 0);
 	__syncthreads();
 	const size_t line = (size_t)z * p.bY + y0;
 	const uint32_t i0 = p.line_start[line], i1 = p.line_start[line + wy];
@@ -128,7 +129,7 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T,
 	}
 	__syncthreads();
 	C *o = a;
-	if constexpr (RC) tile_cols_fft<C, NS, NL, LS, NT, false>(a, p.twx);
+	if constexpr (RC) tile_cols_fft<C, NS, NL, LS, NT, false, true>(a, p.twx);
 	else o = tile_fft<C, NS, NL, LS, false>(a, b, p.px, p.twx);
 	const size_t plane = (size_t)p.bZ * p.bY;
 	C *xf = p.Xf + (size_t)r * p.gX * 3 * plane + (size_t)z * p.bY + y0;
@@ -155,6 +156,12 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T,
 // padded) and writes Tz (all kz); MODE 1 (inverse) reads Tz and writes z<bZ back to Xf; MODE 2 (surface) reads Xf
 // like MODE 0 but transforms with the inverse sign into TzR, so that the product with R~ sums heights instead of
 // differences (planZRf, fft.c:396-403, matvec.c:249).
+// FP32 with a power-of-two length (the column form): thread (l, j1) = (threadIdx % W, threadIdx / W) holds elements
+// z = j1 + T*j of y-line l in registers, read and written straight from and to HBM/L2 (consecutive threads =
+// consecutive y: coalesced rows, no staging tile), and the two-step FFT exchanges its intermediate through shared
+// memory laid out [k2][j1][l] (one block barrier; both phases conflict-free, a pad of W elements per k2 row group
+// for W = 8). The forward transforms read z < gZ/2 only and start with dft_half_in; the inverse keeps z < gZ/2.
+// Otherwise a staged tile and Stockham passes.
 template <typename T, int W, int MODE, int NS>
 __global__ void __launch_bounds__(col_threads<T, NS, W>(), (col_minblocks<T, NS, W>())) mv_fftz(MvGeom<T> p)
 {
@@ -175,32 +182,85 @@ __global__ void __launch_bounds__(col_threads<T, NS, W>(), (col_minblocks<T, NS,
 	const size_t plane = (size_t)p.bZ * p.bY;
 	C *xf = p.Xf + (((size_t)r * p.gX + kx) * 3 + comp) * plane + y0;
 	C *tz = (MODE == 2 ? p.TzR : p.Tz) + (((size_t)r * p.CK + kxl) * 3 + comp) * (size_t)n * p.bY + y0;
-	// NT is a multiple of W: each thread keeps one y-line and walks z with a constant stride
-	constexpr int ZS = NT / W;
-	const int yy = threadIdx.x % W, z0 = threadIdx.x / W;
-	const bool yok = yy < wy;
-	{
-		const C *src = (INV ? tz : xf) + (size_t)z0 * p.bY + yy;
-		const C *base = INV ? tz : xf;
-		const size_t step = (size_t)ZS * p.bY;
-#pragma unroll 4
-		for (int z = z0; z < n; z += ZS, src += step) {
-			const bool ok = yok && (INV || z < p.bZ);
-			cp_async_elem(a + z * LS + yy, ok ? src : base, ok);
+	if constexpr (RC) {
+		constexpr int TL = RegShape<NS>::T, E = RegShape<NS>::E;
+		constexpr int KS = TL * W + (W < 16 ? W : 0); // one k2 row group of the exchange buffer
+		const int l = threadIdx.x % W, j1 = threadIdx.x / W;
+		const bool yok = l < wy;
+		const size_t ys = (size_t)p.bY;
+		C v[E];
+		if constexpr (INV) {
+#pragma unroll
+			for (int j = 0; j < E; j++) v[j] = yok ? __ldg(tz + (size_t)(j1 + TL * j) * ys + l) : cx<C>(0, 0);
+			dft<C, E>(v, SGN, p.twz, NS);
 		}
+		else {
+#pragma unroll
+			for (int j = 0; j < E / 2; j++) {
+				const int z = j1 + TL * j;
+				v[j] = (yok && z < p.bZ) ? __ldg(xf + (size_t)z * ys + l) : cx<C>(0, 0);
+			}
+			dft_half_in<C, E>(v, SGN);
+		}
+#pragma unroll
+		for (int k2 = 1; k2 < E; k2++) {
+			C t = __ldg(p.twz + j1 * k2);
+			if (SGN) t.y = -t.y;
+			v[k2] = cmul(v[k2], t);
+		}
+#pragma unroll
+		for (int k2 = 0; k2 < E; k2++) a[k2 * KS + j1 * W + l] = v[k2];
+		__syncthreads();
+#pragma unroll
+		for (int i = 0; i < E / TL; i++) {
+			const int k2 = j1 + i * TL;
+			C u[TL];
+#pragma unroll
+			for (int q = 0; q < TL; q++) u[q] = a[k2 * KS + q * W + l];
+			dft<C, TL>(u, SGN, p.twz, NS);
+			// u[k1] = element k2 + E*k1 of the transformed line
+			if (yok) {
+				if constexpr (INV) {
+#pragma unroll
+					for (int k1 = 0; k1 < TL / 2; k1++) {
+						const int z = k2 + E * k1;
+						if (z < p.bZ) xf[(size_t)z * ys + l] = u[k1];
+					}
+				}
+				else {
+#pragma unroll
+					for (int k1 = 0; k1 < TL; k1++) tz[(size_t)(k2 + E * k1) * ys + l] = u[k1];
+				}
+			}
+		}
+		return;
 	}
-	cp_async_commit();
-	cp_async_wait<0>();
-	__syncthreads();
-	C *o = a;
-	if constexpr (RC) tile_cols_fft<C, NS, W, LS, NT, SGN>(a, p.twz);
-	else o = tile_fft<C, NS, W, LS, SGN>(a, b, p.pz, p.twz);
-	const int zmax = INV ? p.bZ : n;
-	if (yok) {
-		C *dst = (INV ? xf : tz) + (size_t)z0 * p.bY + yy;
-		const size_t step = (size_t)ZS * p.bY;
+	else {
+		// NT is a multiple of W: each thread keeps one y-line and walks z with a constant stride
+		constexpr int ZS = NT / W;
+		const int yy = threadIdx.x % W, z0 = threadIdx.x / W;
+		const bool yok = yy < wy;
+		{
+			const C *src = (INV ? tz : xf) + (size_t)z0 * p.bY + yy;
+			const C *base = INV ? tz : xf;
+			const size_t step = (size_t)ZS * p.bY;
 #pragma unroll 4
-		for (int z = z0; z < zmax; z += ZS, dst += step) *dst = o[z * LS + yy];
+			for (int z = z0; z < n; z += ZS, src += step) {
+				const bool ok = yok && (INV || z < p.bZ);
+				cp_async_elem(a + z * LS + yy, ok ? src : base, ok);
+			}
+		}
+		cp_async_commit();
+		cp_async_wait<0>();
+		__syncthreads();
+		C *o = tile_fft<C, NS, W, LS, SGN>(a, b, p.pz, p.twz);
+		const int zmax = INV ? p.bZ : n;
+		if (yok) {
+			C *dst = (INV ? xf : tz) + (size_t)z0 * p.bY + yy;
+			const size_t step = (size_t)ZS * p.bY;
+#pragma unroll 4
+			for (int z = z0; z < zmax; z += ZS, dst += step) *dst = o[z * LS + yy];
+		}
 	}
 }
 
@@ -391,11 +451,13 @@ __global__ void __launch_bounds__(NT, NS >= 512 ? (NT >= 256 ? 1 : 256 / NT) : (
 		if constexpr (SURF) prefetch_l2_bulk(p.Rm + ((size_t)kx * p.gZ + kz) * p.RsY * 6, (unsigned)(p.RsY * 6 * sizeof(C)));
 	}
 	// the three component lines go to their slots asynchronously (lane j1 writes and later reads only its own
-	// elements, at j*T + j1), one commit group each, so components 1 and 2 arrive during component 0's transform
+	// elements, at j*T + j1), one commit group each, so components 1 and 2 arrive during component 0's transform;
+	// y < bY <= gY/2, so only the first E/2 elements of a lane can be non-zero (the transforms start with
+	// dft_half_in) and only those are stored after the inverse ones
 #pragma unroll
 	for (int c = 0; c < 3; c++) {
 #pragma unroll
-		for (int j = 0; j < E; j++) {
+		for (int j = 0; j < E / 2; j++) {
 			const int y = j1 + T * j;
 			if (y < p.bY) cp_async_elem(slot + c * BUF + j * T + j1, col + c * lz + y, true);
 		}
@@ -404,7 +466,7 @@ __global__ void __launch_bounds__(NT, NS >= 512 ? (NT >= 256 ? 1 : 256 / NT) : (
 	const C *colR = SURF ? p.TzR + (((size_t)r * p.CK + kxl) * 3) * lz + (size_t)kz * p.bY : nullptr;
 	if constexpr (SURF) { // u_0 into slot 3
 #pragma unroll
-		for (int j = 0; j < E; j++) {
+		for (int j = 0; j < E / 2; j++) {
 			const int y = j1 + T * j;
 			if (y < p.bY) cp_async_elem(slot + 3 * BUF + j * T + j1, colR + y, true);
 		}
@@ -417,11 +479,11 @@ __global__ void __launch_bounds__(NT, NS >= 512 ? (NT >= 256 ? 1 : 256 / NT) : (
 		else if (c == 1) cp_async_wait<SURF ? 2 : 1>();
 		else cp_async_wait<SURF ? 1 : 0>();
 #pragma unroll
-		for (int j = 0; j < E; j++) {
+		for (int j = 0; j < E / 2; j++) {
 			const int y = j1 + T * j;
 			v[j] = (y < p.bY) ? slot[c * BUF + j * T + j1] : make_float2(0.f, 0.f);
 		}
-		reg_fft<C, NS, false>(v, slot + c * BUF, j1, gmask, p.twy);
+		reg_fft<C, NS, false, true>(v, slot + c * BUF, j1, gmask, p.twy);
 		reg_natural<C, NS>(v);
 		if (c < 2) {
 			__syncwarp(gmask);
@@ -459,7 +521,7 @@ __global__ void __launch_bounds__(NT, NS >= 512 ? (NT >= 256 ? 1 : 256 / NT) : (
 				__syncwarp(gmask);
 				C *nb = slot + (c == 0 ? 2 : 3) * BUF;
 #pragma unroll
-				for (int j = 0; j < E; j++) {
+				for (int j = 0; j < E / 2; j++) {
 					const int y = j1 + T * j;
 					if (y < p.bY) cp_async_elem(nb + j * T + j1, colR + (size_t)(c + 1) * lz + y, true);
 				}
@@ -469,11 +531,11 @@ __global__ void __launch_bounds__(NT, NS >= 512 ? (NT >= 256 ? 1 : 256 / NT) : (
 			else cp_async_wait<0>();
 			C u[E];
 #pragma unroll
-			for (int j = 0; j < E; j++) {
+			for (int j = 0; j < E / 2; j++) {
 				const int y = j1 + T * j;
 				u[j] = (y < p.bY) ? ub[j * T + j1] : make_float2(0.f, 0.f);
 			}
-			reg_fft<C, NS, false>(u, ub, j1, gmask, p.twy);
+			reg_fft<C, NS, false, true>(u, ub, j1, gmask, p.twy);
 			reg_natural<C, NS>(u);
 #pragma unroll
 			for (int j = 0; j < E; j++) {
@@ -519,7 +581,7 @@ __global__ void __launch_bounds__(NT, NS >= 512 ? (NT >= 256 ? 1 : 256 / NT) : (
 		reg_fft<C, NS, true>(v, slot + c * BUF, j1, gmask, p.twy);
 		reg_natural<C, NS>(v);
 #pragma unroll
-		for (int j = 0; j < E; j++) {
+		for (int j = 0; j < E / 2; j++) {
 			const int y = j1 + T * j;
 			if (y < p.bY) col[c * lz + y] = v[j];
 		}
@@ -579,7 +641,8 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T,
 	cp_async_wait<0>();
 	__syncthreads();
 	C *o = a;
-	if constexpr (RC) tile_cols_fft<C, NS, NL, LS, NT, true>(a, p.twx);
+	// only x < bX <= gX/2 is gathered
+	if constexpr (RC) tile_cols_fft<C, NS, NL, LS, NT, true, false, true>(a, p.twx);
 	else o = tile_fft<C, NS, NL, LS, true>(a, b, p.px, p.twx);
 	const size_t line = (size_t)z * p.bY + y0;
 	const uint32_t i0 = p.line_start[line], i1 = p.line_start[line + wy];
