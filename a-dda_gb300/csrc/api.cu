@@ -81,20 +81,33 @@ int adda_gb300_get_grid(const adda_gb300_ctx *c, int grid[3])
 	return ADDA_GB300_OK;
 }
 
+// n-th roots of unity of one axis. The FP32 table has a second part of n entries for the register FFT of the y
+// transform (reg_fft, power-of-two n = T*E up to 512): W_n^(j1*k2) at k2*T + j1, so that the T lanes of a line read
+// their step-1 twiddles from consecutive addresses.
 static int upload_twiddles(adda_gb300_ctx *c, int which, int n)
 {
 	std::vector<double2> t64(n);
-	std::vector<float2> t32(n);
+	std::vector<float2> t32(2 * (size_t)n, make_float2(0.f, 0.f));
 	for (int t = 0; t < n; t++) {
 		double cs, sn;
 		unit_root(t, n, cs, sn);
 		t64[t] = make_double2(cs, sn);
 		t32[t] = make_float2((float)cs, (float)sn);
 	}
+	int T = 0;
+	switch (n) {
+		case 64: T = RegShape<64>::T; break;
+		case 128: T = RegShape<128>::T; break;
+		case 256: T = RegShape<256>::T; break;
+		case 512: T = RegShape<512>::T; break;
+		default: break;
+	}
+	for (int k2 = 0; T && k2 < n / T; k2++)
+		for (int j1 = 0; j1 < T; j1++) t32[n + (size_t)k2 * T + j1] = t32[(size_t)j1 * k2 % n];
 	ADDA_CUDA(cudaMalloc(&c->tw64[which], sizeof(double2) * n));
-	ADDA_CUDA(cudaMalloc(&c->tw32[which], sizeof(float2) * n));
+	ADDA_CUDA(cudaMalloc(&c->tw32[which], sizeof(float2) * 2 * (size_t)n));
 	ADDA_CUDA(cudaMemcpy(c->tw64[which], t64.data(), sizeof(double2) * n, cudaMemcpyHostToDevice));
-	ADDA_CUDA(cudaMemcpy(c->tw32[which], t32.data(), sizeof(float2) * n, cudaMemcpyHostToDevice));
+	ADDA_CUDA(cudaMemcpy(c->tw32[which], t32.data(), sizeof(float2) * 2 * (size_t)n, cudaMemcpyHostToDevice));
 	return ADDA_GB300_OK;
 }
 

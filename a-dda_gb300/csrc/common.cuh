@@ -783,16 +783,17 @@ template <int N> struct RegShape {
 	static constexpr int BUF = E * (T + 1);             // complex elements of a line's transpose buffer
 };
 
-// HALF_IN: the line's upper half is zero (v[j] for j >= E/2 is not read).
+// HALF_IN: the line's upper half is zero (v[j] for j >= E/2 is not read). twl: the step-1 twiddles lane-major,
+// W_N^(j1*k2) at twl[k2*T + j1] (a line's T lanes read consecutive addresses).
 template <typename C, int N, bool INV, bool HALF_IN = false>
-__device__ __forceinline__ void reg_fft(C *v, C *buf, int j1, unsigned gmask, const C *__restrict__ tw)
+__device__ __forceinline__ void reg_fft(C *v, C *buf, int j1, unsigned gmask, const C *__restrict__ twl)
 {
 	constexpr int T = RegShape<N>::T, E = RegShape<N>::E;
 	if constexpr (HALF_IN) dft_half_in<C, E>(v, INV);
-	else dft<C, E>(v, INV, tw, N);
+	else dft<C, E>(v, INV, twl, N);
 #pragma unroll
 	for (int k2 = 1; k2 < E; k2++) {
-		C t = __ldg(tw + j1 * k2);
+		C t = __ldg(twl + k2 * T + j1);
 		if (INV) t.y = -t.y;
 		v[k2] = cmul(v[k2], t);
 	}
@@ -806,26 +807,24 @@ __device__ __forceinline__ void reg_fft(C *v, C *buf, int j1, unsigned gmask, co
 		const int k2 = j1 + i * T;
 #pragma unroll
 		for (int q = 0; q < T; q++) u[q] = buf[k2 * (T + 1) + q];
-		dft<C, T>(u, INV, tw, N);
+		dft<C, T>(u, INV, twl, N);
 #pragma unroll
 		for (int q = 0; q < T; q++) v[i * T + q] = u[q];
 	}
 }
 
-// In-place FFT of column l of an element-major tile (element e at a[e*LS + l], e < N) by the T lanes of one group
-// (lane j1, group lanes gmask): the two steps of reg_fft with the transpose done inside the column itself. Step 1's
-// Y[j1][k2] goes to element k2*T + ((j1 + k2) mod T): for a fixed k2 the T lanes write T consecutive elements, and
-// the step-2 reads (lane j1 takes column k2 = j1 + i*T, rows q) hit T consecutive elements modulo T too, so with an
-// odd LS both phases are bank-conflict-free. The result is written back in natural order. The caller synchronises
-// the block before (tile filled) and after (tile read by other lanes). HALF_IN: elements N/2.. of the column are zero
-// and not read; HALF_OUT: only elements 0..N/2-1 of the result are written back.
-template <typename C, int N, int LS, bool INV, bool HALF_IN = false, bool HALF_OUT = false>
-__device__ __forceinline__ void col_fft(C *a, int l, int j1, unsigned gmask, const C *__restrict__ tw)
+// Line-fastest two-step FFT of NL lines by NT = NL*T threads: thread (l, j1) = (threadIdx % NL, threadIdx / NL)
+// holds elements j1 + T*j of line l in v (j < E/2 with HALF_IN: the upper half is zero), so that consecutive threads
+// hold consecutive lines and the caller's loads and stores along the lines' common contiguous axis coalesce. The
+// step-1 results Y[j1][k2] go through xb laid out [k2][j1][l] (row groups of KS = T*NL + pad complex; with
+// KS = NL mod 16 a warp's accesses of either phase fall on distinct bank pairs); one block barrier. On return
+// v[i*T + k1] holds element (j1 + i*T) + E*k1 of line l. Every thread of the block must call it; the caller
+// synchronises before reusing xb.
+template <int NL, int T> __host__ __device__ constexpr int lf_ks() { return T * NL + (NL * (17 - T)) % 16; }
+template <typename C, int N, int NL, bool INV, bool HALF_IN>
+__device__ __forceinline__ void lf_fft(C *v, C *xb, int l, int j1, const C *__restrict__ tw)
 {
-	constexpr int T = RegShape<N>::T, E = RegShape<N>::E;
-	C v[E];
-#pragma unroll
-	for (int j = 0; j < (HALF_IN ? E / 2 : E); j++) v[j] = a[(j1 + T * j) * LS + l];
+	constexpr int T = RegShape<N>::T, E = RegShape<N>::E, KS = lf_ks<NL, T>();
 	if constexpr (HALF_IN) dft_half_in<C, E>(v, INV);
 	else dft<C, E>(v, INV, tw, N);
 #pragma unroll
@@ -834,40 +833,23 @@ __device__ __forceinline__ void col_fft(C *a, int l, int j1, unsigned gmask, con
 		if (INV) t.y = -t.y;
 		v[k2] = cmul(v[k2], t);
 	}
-	__syncwarp(gmask);
 #pragma unroll
-	for (int k2 = 0; k2 < E; k2++) a[(k2 * T + ((j1 + k2) & (T - 1))) * LS + l] = v[k2];
-	__syncwarp(gmask);
+	for (int k2 = 0; k2 < E; k2++) xb[k2 * KS + j1 * NL + l] = v[k2];
+	__syncthreads();
 #pragma unroll
 	for (int i = 0; i < E / T; i++) {
 		const int k2 = j1 + i * T;
 		C u[T];
 #pragma unroll
-		for (int q = 0; q < T; q++) u[q] = a[(k2 * T + ((q + k2) & (T - 1))) * LS + l];
+		for (int q = 0; q < T; q++) u[q] = xb[k2 * KS + q * NL + l];
 		dft<C, T>(u, INV, tw, N);
 #pragma unroll
 		for (int k1 = 0; k1 < T; k1++) v[i * T + k1] = u[k1];
 	}
-	__syncwarp(gmask);
-#pragma unroll
-	for (int i = 0; i < E / T; i++)
-#pragma unroll
-		for (int k1 = 0; k1 < (HALF_OUT ? T / 2 : T); k1++) a[(j1 + i * T + E * k1) * LS + l] = v[i * T + k1];
 }
 
-// FFT of all NL columns of an element-major tile by NT threads in groups of T lanes (line l = group, group + G, ...)
-template <typename C, int N, int NL, int LS, int NT, bool INV, bool HALF_IN = false, bool HALF_OUT = false>
-__device__ __forceinline__ void tile_cols_fft(C *a, const C *__restrict__ tw)
-{
-	constexpr int T = RegShape<N>::T, G = NT / T;
-	const int g = threadIdx.x / T, j1 = threadIdx.x % T;
-	const unsigned gmask = ((1u << T) - 1u) << ((threadIdx.x & 31) & ~(T - 1));
-	for (int l = g; l < NL; l += G) col_fft<C, N, LS, INV, HALF_IN, HALF_OUT>(a, l, j1, gmask, tw);
-	__syncthreads();
-}
-
-// whether a kernel of compile-time length NS and arithmetic T transforms its single tile with tile_cols_fft
-// (FP32, power-of-two 64..512) rather than with ping-pong Stockham passes, and its thread count for NL lines
+// whether a kernel of compile-time length NS and arithmetic T transforms its lines with lf_fft (FP32, power-of-two
+// 64..512) rather than with ping-pong Stockham passes over two tiles, and its thread count for NL lines
 template <typename T, int NS> __host__ __device__ constexpr bool reg_cols() { return sizeof(T) == 4 && NS >= 64 && NS <= 512; }
 template <typename T, int NS, int NL> __host__ __device__ constexpr int col_threads()
 {

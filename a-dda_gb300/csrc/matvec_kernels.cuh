@@ -20,9 +20,9 @@
 // every tile is loaded along the contiguous axis of its buffer and transformed in element-major shared memory.
 // Every kernel is instantiated with a compile-time FFT length NS for the power-of-two grids (all index arithmetic
 // folds to shifts, passes unroll) and with NS = 0 (runtime plan) for the other fftFit sizes. With FP32 arithmetic and
-// a power-of-two length the tile is transformed column by column in registers (tile_cols_fft: one tile instead of
-// two, one group of 8-16 lanes per line, warp-local synchronisation); blocks then have lines x group-size threads,
-// otherwise 256 threads and ping-pong Stockham passes.
+// a power-of-two length the lines are transformed in registers (lf_fft: 8-16 threads per line, consecutive threads
+// on consecutive lines, one exchange through shared memory, the zero half of every padded line skipped); blocks then
+// have lines x threads-per-line threads, otherwise 256 threads and ping-pong Stockham passes over two tiles.
 #pragma once
 
 #include "ctx.cuh"
@@ -128,22 +128,28 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T,
 		}
 	}
 	__syncthreads();
-	C *o = a;
-	if constexpr (RC) tile_cols_fft<C, NS, NL, LS, NT, false, true>(a, p.twx);
-	else o = tile_fft<C, NS, NL, LS, false>(a, b, p.px, p.twx);
 	const size_t plane = (size_t)p.bZ * p.bY;
 	C *xf = p.Xf + (size_t)r * p.gX * 3 * plane + (size_t)z * p.bY + y0;
 	if constexpr (RC) {
-		// NT is a multiple of NL: each thread keeps one line (comp, yy) and walks kx
-		constexpr int KS = NT / NL;
-		const int l = threadIdx.x % NL, comp = l / W, yy = l % W;
+		// line-fastest transform of the tile's lines l = comp*W + yy; each thread stores its elements kx of line l
+		// straight to Xf (consecutive threads = consecutive y)
+		constexpr int TL = RegShape<NS>::T, E = RegShape<NS>::E;
+		const int l = threadIdx.x % NL, j1 = threadIdx.x / NL, comp = l / W, yy = l % W;
+		C v[E];
+#pragma unroll
+		for (int j = 0; j < E / 2; j++) v[j] = a[(j1 + TL * j) * LS + l];
+		__syncthreads(); // the exchange buffer of lf_fft overwrites the tile
+		lf_fft<C, NS, NL, false, true>(v, a, l, j1, p.twx);
 		if (yy < wy) {
-			C *dst = xf + (size_t)comp * plane + yy + (size_t)(threadIdx.x / NL) * 3 * plane;
-#pragma unroll 4
-			for (int kx = threadIdx.x / NL; kx < NS; kx += KS, dst += (size_t)KS * 3 * plane) *dst = o[kx * LS + l];
+			C *dst = xf + (size_t)comp * plane + yy;
+#pragma unroll
+			for (int i = 0; i < E / TL; i++)
+#pragma unroll
+				for (int k1 = 0; k1 < TL; k1++) dst[(size_t)(j1 + i * TL + E * k1) * 3 * plane] = v[i * TL + k1];
 		}
 	}
 	else {
+		const C *o = tile_fft<C, NS, NL, LS, false>(a, b, p.px, p.twx);
 		for (int t = threadIdx.x; t < n * NL; t += NT) {
 			const int yy = t % W, rest = t / W;
 			const int comp = rest % 3, kx = rest / 3;
@@ -184,7 +190,6 @@ __global__ void __launch_bounds__(col_threads<T, NS, W>(), (col_minblocks<T, NS,
 	C *tz = (MODE == 2 ? p.TzR : p.Tz) + (((size_t)r * p.CK + kxl) * 3 + comp) * (size_t)n * p.bY + y0;
 	if constexpr (RC) {
 		constexpr int TL = RegShape<NS>::T, E = RegShape<NS>::E;
-		constexpr int KS = TL * W + (W < 16 ? W : 0); // one k2 row group of the exchange buffer
 		const int l = threadIdx.x % W, j1 = threadIdx.x / W;
 		const bool yok = l < wy;
 		const size_t ys = (size_t)p.bY;
@@ -192,7 +197,6 @@ __global__ void __launch_bounds__(col_threads<T, NS, W>(), (col_minblocks<T, NS,
 		if constexpr (INV) {
 #pragma unroll
 			for (int j = 0; j < E; j++) v[j] = yok ? __ldg(tz + (size_t)(j1 + TL * j) * ys + l) : cx<C>(0, 0);
-			dft<C, E>(v, SGN, p.twz, NS);
 		}
 		else {
 #pragma unroll
@@ -200,36 +204,22 @@ __global__ void __launch_bounds__(col_threads<T, NS, W>(), (col_minblocks<T, NS,
 				const int z = j1 + TL * j;
 				v[j] = (yok && z < p.bZ) ? __ldg(xf + (size_t)z * ys + l) : cx<C>(0, 0);
 			}
-			dft_half_in<C, E>(v, SGN);
 		}
+		lf_fft<C, NS, W, SGN, !INV>(v, a, l, j1, p.twz);
+		// v[i*TL + k1] = element (j1 + i*TL) + E*k1 of the transformed line
+		if (yok) {
 #pragma unroll
-		for (int k2 = 1; k2 < E; k2++) {
-			C t = __ldg(p.twz + j1 * k2);
-			if (SGN) t.y = -t.y;
-			v[k2] = cmul(v[k2], t);
-		}
-#pragma unroll
-		for (int k2 = 0; k2 < E; k2++) a[k2 * KS + j1 * W + l] = v[k2];
-		__syncthreads();
-#pragma unroll
-		for (int i = 0; i < E / TL; i++) {
-			const int k2 = j1 + i * TL;
-			C u[TL];
-#pragma unroll
-			for (int q = 0; q < TL; q++) u[q] = a[k2 * KS + q * W + l];
-			dft<C, TL>(u, SGN, p.twz, NS);
-			// u[k1] = element k2 + E*k1 of the transformed line
-			if (yok) {
+			for (int i = 0; i < E / TL; i++) {
 				if constexpr (INV) {
 #pragma unroll
 					for (int k1 = 0; k1 < TL / 2; k1++) {
-						const int z = k2 + E * k1;
-						if (z < p.bZ) xf[(size_t)z * ys + l] = u[k1];
+						const int z = j1 + i * TL + E * k1;
+						if (z < p.bZ) xf[(size_t)z * ys + l] = v[i * TL + k1];
 					}
 				}
 				else {
 #pragma unroll
-					for (int k1 = 0; k1 < TL; k1++) tz[(size_t)(k2 + E * k1) * ys + l] = u[k1];
+					for (int k1 = 0; k1 < TL; k1++) tz[(size_t)(j1 + i * TL + E * k1) * ys + l] = v[i * TL + k1];
 				}
 			}
 		}
@@ -441,14 +431,15 @@ __global__ void __launch_bounds__(NT, NS >= 512 ? (NT >= 256 ? 1 : 256 / NT) : (
 	const unsigned gmask = ((1u << T) - 1u) << ((threadIdx.x & 31) & ~(T - 1));
 	const int kxl = blockIdx.y, kx = p.kx0 + kxl;
 	C *slot = reinterpret_cast<C *>(smem_raw) + (size_t)g * NSLOT * BUF; // slots c*BUF, c = 0..NSLOT-1
+	constexpr int DY = NS / 2 + 1; // rows of D (and R) along y: gY/2 + 1, gY = NS
 	const size_t lz = (size_t)p.gZ * p.bY;
 	C *col = p.Tz + (((size_t)r * p.CK + kxl) * 3) * lz + (size_t)kz * p.bY;
 	// the column's D row (and R row) start moving into L2 now, so that the product after the forward transforms
 	// finds them there; one lane of the first RHS's group asks (rows of 6 complex per ky: multiples of 48 bytes)
 	if (j1 == 0 && r == 0) {
-		prefetch_l2_bulk(p.D + ((size_t)kx * p.DsZ + (kz >= p.DsZ ? p.gZ - kz : kz)) * p.DsY * 6,
-			(unsigned)(p.DsY * 6 * sizeof(C)));
-		if constexpr (SURF) prefetch_l2_bulk(p.Rm + ((size_t)kx * p.gZ + kz) * p.RsY * 6, (unsigned)(p.RsY * 6 * sizeof(C)));
+		prefetch_l2_bulk(p.D + ((size_t)kx * p.DsZ + (kz >= p.DsZ ? p.gZ - kz : kz)) * DY * 6,
+			(unsigned)(DY * 6 * sizeof(C)));
+		if constexpr (SURF) prefetch_l2_bulk(p.Rm + ((size_t)kx * p.gZ + kz) * DY * 6, (unsigned)(DY * 6 * sizeof(C)));
 	}
 	// the three component lines go to their slots asynchronously (lane j1 writes and later reads only its own
 	// elements, at j*T + j1), one commit group each, so components 1 and 2 arrive during component 0's transform;
@@ -483,7 +474,7 @@ __global__ void __launch_bounds__(NT, NS >= 512 ? (NT >= 256 ? 1 : 256 / NT) : (
 			const int y = j1 + T * j;
 			v[j] = (y < p.bY) ? slot[c * BUF + j * T + j1] : make_float2(0.f, 0.f);
 		}
-		reg_fft<C, NS, false, true>(v, slot + c * BUF, j1, gmask, p.twy);
+		reg_fft<C, NS, false, true>(v, slot + c * BUF, j1, gmask, p.twy + NS);
 		reg_natural<C, NS>(v);
 		if (c < 2) {
 			__syncwarp(gmask);
@@ -493,12 +484,12 @@ __global__ void __launch_bounds__(NT, NS >= 512 ? (NT >= 256 ? 1 : 256 / NT) : (
 	}
 	const bool rz = kz >= p.DsZ;
 	const int zz = rz ? p.gZ - kz : kz;
-	const float4 *drow = reinterpret_cast<const float4 *>(p.D + ((size_t)kx * p.DsZ + zz) * p.DsY * 6);
+	const float4 *drow = reinterpret_cast<const float4 *>(p.D + ((size_t)kx * p.DsZ + zz) * DY * 6);
 #pragma unroll
 	for (int j = 0; j < E; j++) {
 		const int ky = j1 + T * j;
-		const bool ry = ky >= p.DsY;
-		const int yy = ry ? p.gY - ky : ky;
+		const bool ry = ky >= DY;
+		const int yy = ry ? NS - ky : ky;
 		const float4 *f = drow + (size_t)yy * 3;
 		const float4 d0 = __ldg(f), d1 = __ldg(f + 1), d2 = __ldg(f + 2);
 		C m0 = make_float2(d0.x, d0.y), m1 = make_float2(d0.z, d0.w), m2 = make_float2(d1.x, d1.y);
@@ -512,7 +503,7 @@ __global__ void __launch_bounds__(NT, NS >= 512 ? (NT >= 256 ? 1 : 256 / NT) : (
 		v[j] = cfma(m2, v0, cfma(m4, v1, cmul(m5, v2)));
 	}
 	if constexpr (SURF) {
-		const float4 *rrow = reinterpret_cast<const float4 *>(p.Rm + ((size_t)kx * p.gZ + kz) * p.RsY * 6);
+		const float4 *rrow = reinterpret_cast<const float4 *>(p.Rm + ((size_t)kx * p.gZ + kz) * DY * 6);
 #pragma unroll 1
 		for (int c = 0; c < 3; c++) {
 			C *ub = slot + (c == 1 ? 2 : 3) * BUF; // u_0 and u_2 in slot 3, u_1 in slot 2 (free after component 2)
@@ -535,13 +526,13 @@ __global__ void __launch_bounds__(NT, NS >= 512 ? (NT >= 256 ? 1 : 256 / NT) : (
 				const int y = j1 + T * j;
 				u[j] = (y < p.bY) ? ub[j * T + j1] : make_float2(0.f, 0.f);
 			}
-			reg_fft<C, NS, false, true>(u, ub, j1, gmask, p.twy);
+			reg_fft<C, NS, false, true>(u, ub, j1, gmask, p.twy + NS);
 			reg_natural<C, NS>(u);
 #pragma unroll
 			for (int j = 0; j < E; j++) {
 				const int ky = j1 + T * j;
-				const bool qy = ky >= p.RsY;
-				const float4 *f = rrow + (size_t)(qy ? p.gY - ky : ky) * 3;
+				const bool qy = ky >= DY;
+				const float4 *f = rrow + (size_t)(qy ? NS - ky : ky) * 3;
 				const float4 d0 = __ldg(f), d1 = __ldg(f + 1), d2 = __ldg(f + 2);
 				C a0, a1, a2; // column c of R~ with the reduced-y signs of xy and yz
 				if (c == 0) {
@@ -578,7 +569,7 @@ __global__ void __launch_bounds__(NT, NS >= 512 ? (NT >= 256 ? 1 : 256 / NT) : (
 #pragma unroll
 			for (int j = 0; j < E; j++) v[j] = slot[c * BUF + j * T + j1];
 		}
-		reg_fft<C, NS, true>(v, slot + c * BUF, j1, gmask, p.twy);
+		reg_fft<C, NS, true>(v, slot + c * BUF, j1, gmask, p.twy + NS);
 		reg_natural<C, NS>(v);
 #pragma unroll
 		for (int j = 0; j < E / 2; j++) {
@@ -619,14 +610,24 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T,
 	const int wy = min(W, p.bY - y0);
 	const size_t plane = (size_t)p.bZ * p.bY;
 	const C *xf = p.Xf + (size_t)r * p.gX * 3 * plane + (size_t)z * p.bY + y0;
+	C *o = a;
 	if constexpr (RC) {
-		constexpr int KS = NT / NL;
-		const int l = threadIdx.x % NL, comp = l / W, yy = l % W;
+		// line-fastest transform of lines l = comp*W + yy read straight from Xf (consecutive threads = consecutive
+		// y); the result rows x < bX <= gX/2, the only ones gathered, go to the tile in natural order
+		constexpr int TL = RegShape<NS>::T, E = RegShape<NS>::E;
+		const int l = threadIdx.x % NL, j1 = threadIdx.x / NL, comp = l / W, yy = l % W;
 		const bool ok = yy < wy;
-		const C *src = xf + (size_t)comp * plane + yy + (size_t)(threadIdx.x / NL) * 3 * plane;
-#pragma unroll 4
-		for (int kx = threadIdx.x / NL; kx < NS; kx += KS, src += (size_t)KS * 3 * plane)
-			cp_async_elem(a + kx * LS + l, ok ? src : xf, ok);
+		const C *src = xf + (size_t)comp * plane + yy;
+		C v[E];
+#pragma unroll
+		for (int j = 0; j < E; j++) v[j] = ok ? __ldg(src + (size_t)(j1 + TL * j) * 3 * plane) : cx<C>(0, 0);
+		lf_fft<C, NS, NL, true, false>(v, a, l, j1, p.twx);
+		__syncthreads(); // every exchange read is done before the result rows overwrite the buffer
+#pragma unroll
+		for (int i = 0; i < E / TL; i++)
+#pragma unroll
+			for (int k1 = 0; k1 < TL / 2; k1++) a[(j1 + i * TL + E * k1) * LS + l] = v[i * TL + k1];
+		__syncthreads();
 	}
 	else {
 #pragma unroll 4
@@ -636,14 +637,11 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T,
 			const bool ok = yy < wy;
 			cp_async_elem(a + kx * LS + comp * W + yy, ok ? xf + ((size_t)kx * 3 + comp) * plane + yy : xf, ok);
 		}
+		cp_async_commit();
+		cp_async_wait<0>();
+		__syncthreads();
+		o = tile_fft<C, NS, NL, LS, true>(a, b, p.px, p.twx);
 	}
-	cp_async_commit();
-	cp_async_wait<0>();
-	__syncthreads();
-	C *o = a;
-	// only x < bX <= gX/2 is gathered
-	if constexpr (RC) tile_cols_fft<C, NS, NL, LS, NT, true, false, true>(a, p.twx);
-	else o = tile_fft<C, NS, NL, LS, true>(a, b, p.px, p.twx);
 	const size_t line = (size_t)z * p.bY + y0;
 	const uint32_t i0 = p.line_start[line], i1 = p.line_start[line + wy];
 	const V *arg = p.arg + (size_t)r * p.N * 3;
@@ -707,7 +705,9 @@ template <typename T> inline bool use_k2b_reg(int gY)
 template <typename T> inline size_t tile_smem(int n, int nl)
 {
 	const bool one = sizeof(T) == 4 && static_len(n) != 0;
-	return (one ? 1 : 2) * sizeof(typename CxT<T>::type) * (size_t)n * tile_ls(nl);
+	// the column form's exchange buffer (lf_fft) needs E*(T*nl + pad) <= n*nl + 2n complex (pad < 16, E <= n/8)
+	return one ? sizeof(typename CxT<T>::type) * (size_t)n * (tile_ls(nl) + 2)
+		: 2 * sizeof(typename CxT<T>::type) * (size_t)n * tile_ls(nl);
 }
 // register K2b: NSLOT slots of BUF complex per lane group of T lanes
 inline size_t k2b_reg_smem(int gY, int nt, bool surf)

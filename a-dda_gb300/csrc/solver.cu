@@ -1786,11 +1786,14 @@ static int krylov(adda_gb300_ctx *c, SolverWork *w, int method, int R, int K, un
 // FP64 residual at which the mixed solver's refinement stops. A solution that only just meets eps carries a
 // cross-section error of several times eps/10 (the 128^3 sphere at eps 1e-5: 6e-6 in Cabs, FP64 and the reference
 // alike); the measured margins bring mixed solves within 1e-6 of the converged cross sections there: QMR_CS at
-// 0.3 eps (2e-7, 5 % more iterations), BiCGStab, whose cross sections converge less regularly, at 0.1 eps (7e-7).
+// 0.3 eps (2e-7, 5 % more iterations), BiCGStab, whose cross sections converge less regularly, at 0.1 eps (7e-7);
+// so do the inner solves with FP32 Krylov vectors (MIXED_F32VEC: at 0.3 eps a 32^3 sphere's QMR_CS solve ended 1.005e-6
+// off the converged Cext), which therefore stop at 0.1 eps too.
 static double final_eps_of(const adda_gb300_solve_params *sp)
 {
 	if (sp->final_eps > 0) return std::min(sp->final_eps, sp->eps);
-	const bool erratic = sp->method == ADDA_ITER_BICGSTAB || sp->method == ADDA_ITER_BCGS2;
+	const bool erratic = sp->method == ADDA_ITER_BICGSTAB || sp->method == ADDA_ITER_BCGS2 ||
+		sp->precision == ADDA_PREC_MIXED_F32VEC;
 	return (erratic ? 0.1 : 0.3) * sp->eps;
 }
 

@@ -152,7 +152,8 @@ typedef struct {
 	int full_steps;              /* BiCGStab: no exit at the half step (the reference with -chp_type always,
 	                                iterative.c:703), so that the final state is a complete iteration */
 	double final_eps;            /* MIXED: FP64 relative residual at which the refinement loop stops, 0 < final_eps
-	                                <= eps; 0 = the default, 0.3*eps (0.1*eps for BiCGStab and BCGS2). The solve
+	                                <= eps; 0 = the default, 0.3*eps (0.1*eps for BiCGStab, BCGS2 and FP32 Krylov
+	                                vectors, ADDA_PREC_MIXED_F32VEC). The solve
 	                                succeeds once the residual meets eps; the margin below eps makes the cross
 	                                sections as accurate as a converged FP64 solve's to about 1e-6, which a solution
 	                                that only just meets a residual of 1e-5 is not (on the 128^3 sphere the FP64
