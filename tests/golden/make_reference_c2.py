@@ -14,7 +14,7 @@ polarisations, and the reference's own total wall time (single thread, x86 host 
 
 With --converged it writes tests/golden/reference_c2_converged.json instead: the same workload solved by the
 reference to relative residual 1e-8 with both methods (-eps 8, the reference's default symmetry handling: the sphere
-is symmetric, so it solves the Y polarisation and X equals it), about three hours per method on one core, and their
+is symmetric, so it solves the Y polarisation and X equals it), 1.6-1.7 hours per method on one core, and their
 mean as the converged cross sections:
 
     python tests/golden/make_reference_c2.py --converged [/path/to/reference/src]
