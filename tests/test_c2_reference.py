@@ -26,13 +26,31 @@ def setup():
 
 def test_c2_inputs_match_reference():
     s = setup()
-    for run in REF["runs"].values():
+    runs = list(REF["runs"].values())
+    conv = os.path.join(HERE, "golden", "reference_c2_converged.json")
+    if os.path.exists(conv):
+        runs += list(json.load(open(conv))["runs"].values())
+    for run in runs:
         assert run["ndip"] == s.n
         assert tuple(run["box"]) == tuple(s.box)
         assert tuple(run["grid"]) == tuple(s.grid)
         for pol, cc in zip("YX", run["cc"]):
             got = s.cc[0 if pol == "Y" else 1][0]
             assert abs(got - complex(*cc)) <= 1e-9 * abs(got)
+
+
+def test_c2_converged_reference_is_converged():
+    """the two methods of the reference's residual-1e-8 runs agree to 1e-8 (so their mean is a converged bar for 1e-6
+    checks), and each is within 1e-5 of the same method's eps-1e-5 run"""
+    conv = os.path.join(HERE, "golden", "reference_c2_converged.json")
+    if not os.path.exists(conv):
+        pytest.skip("no converged fixture")
+    c = json.load(open(conv))
+    assert c["converged"]["spread"]["Cext"] < 1e-8 and c["converged"]["spread"]["Cabs"] < 1e-8
+    for m, run in c["runs"].items():
+        assert run["resid_final"]["Y"] <= 1e-8
+        for q in ("Cext", "Cabs"):
+            assert abs(run["cross"]["Y"][q] / REF["runs"][m]["cross"]["Y"][q] - 1) < 1e-5
 
 
 @pytest.mark.gpu
