@@ -81,6 +81,9 @@ template <typename P> __device__ __forceinline__ bool all_done(const P &p)
 		if (!p.done[r]) return false;
 	return true;
 }
+// a right-hand side the solver has finished (converged, broken down or stopped): the matvec skips its blocks, since
+// every vector kernel and scalar kernel of the solver leaves a finished RHS alone and nothing reads its products
+template <typename P> __device__ __forceinline__ bool rhs_done(const P &p, int r) { return p.done && p.done[r]; }
 
 template <typename C> __device__ __forceinline__ C ccs_of(const C *ccs, int per_dip, int nmat, size_t N, int r,
 	size_t i, uint8_t m, int comp)
@@ -100,7 +103,7 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T,
 {
 	typedef typename CxT<T>::type C;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
-	if (all_done(p)) return;
+	if (rhs_done(p, blockIdx.z)) return; // blockIdx.z = RHS
 	constexpr int NL = 3 * W, LS = tile_ls(3 * W), NT = col_threads<T, NS, 3 * W>();
 	constexpr bool RC = reg_cols<T, NS>();
 	const int n = NS ? NS : p.gX;
@@ -174,7 +177,7 @@ __global__ void __launch_bounds__(col_threads<T, NS, W>(), (col_minblocks<T, NS,
 	constexpr bool INV = MODE == 1, SGN = MODE != 0;
 	typedef typename CxT<T>::type C;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
-	if (all_done(p)) return;
+	if (rhs_done(p, blockIdx.z)) return; // blockIdx.z = RHS
 	constexpr int LS = tile_ls(W), NT = col_threads<T, NS, W>();
 	constexpr bool RC = reg_cols<T, NS>();
 	const int n = NS ? NS : p.gZ;
@@ -268,6 +271,11 @@ template <typename T, int NS, int P> __global__ void __launch_bounds__(256) mv_f
 	C *b = a + (size_t)n * LS;
 	const int KB = p.KB, RG = p.RG;
 	const int rg0 = blockIdx.z * RG;
+	{
+		bool live = false; // any of the block's RHS still running
+		for (int rr = rg0; rr < min(rg0 + RG, p.R); rr++) live = live || !rhs_done(p, rr);
+		if (!live) return;
+	}
 	const int kxl = blockIdx.y, kx = p.kx0 + kxl;
 	const int kz0 = blockIdx.x * KB;
 	const size_t lz = (size_t)p.gZ * p.bY; // one (rhs, kx, comp) block of Tz
@@ -339,6 +347,11 @@ template <typename T, int NS, int P> __global__ void __launch_bounds__(256) mv_f
 	C *b = a + (size_t)n * LS;
 	const int KB = p.KB, RG = p.RG;
 	const int rg0 = blockIdx.z * RG;
+	{
+		bool live = false; // any of the block's RHS still running
+		for (int rr = rg0; rr < min(rg0 + RG, p.R); rr++) live = live || !rhs_done(p, rr);
+		if (!live) return;
+	}
 	const int kxl = blockIdx.y, kx = p.kx0 + kxl;
 	const int kz0 = blockIdx.x * KB;
 	const size_t lz = (size_t)p.gZ * p.bY;
@@ -427,7 +440,7 @@ __global__ void __launch_bounds__(NT, NS >= 512 ? (NT >= 256 ? 1 : 256 / NT) : (
 	const int g = threadIdx.x / T, j1 = threadIdx.x % T;
 	const int unit = blockIdx.x * G + g;
 	const int r = unit % p.R, kz = unit / p.R;
-	if (kz >= p.gZ) return; // whole groups leave together
+	if (kz >= p.gZ || rhs_done(p, r)) return; // whole groups leave together
 	const unsigned gmask = ((1u << T) - 1u) << ((threadIdx.x & 31) & ~(T - 1));
 	const int kxl = blockIdx.y, kx = p.kx0 + kxl;
 	C *slot = reinterpret_cast<C *>(smem_raw) + (size_t)g * NSLOT * BUF; // slots c*BUF, c = 0..NSLOT-1
@@ -600,7 +613,7 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T,
 	typedef typename CxT<T>::type C;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	__shared__ double red[32];
-	if (all_done(p)) return;
+	if (rhs_done(p, blockIdx.z)) return; // blockIdx.z = RHS
 	constexpr int NL = 3 * W, LS = tile_ls(3 * W), NT = col_threads<T, NS, 3 * W>();
 	constexpr bool RC = reg_cols<T, NS>();
 	const int n = NS ? NS : p.gX;
