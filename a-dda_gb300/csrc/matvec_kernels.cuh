@@ -5,19 +5,20 @@
 //                        the dipole vector (no zeroed expanded grid, the reference's Xmatrix fill + Arith1), pad to
 //                        gridX in shared memory, forward FFT along x  ->  Xf[r][kx][comp][z][y]
 //   then per chunk of CK x-slabs (chunk buffer Tz sized to stay in L2):
-//   K2a mv_fftz        : forward FFT along z of each y-line block (zero padding z>=boxZ in shared memory)
+//   K2a mv_fftz        : forward FFT along z of each y-line block (z>=boxZ zero: only z<gZ/2 is read)
 //   K2b mv_fft_y_dmul  : per (kx, kz block, RHS group): forward FFT along y, 6-component symmetric D~ x X~ product
 //                        (D read once per grid point and reused by every RHS of the block), inverse FFT along y;
-//       mv_fft_y_reg   : the same in register form (FP32, power-of-two gY <= 256): one lane group per column, lines
+//       mv_fft_y_reg   : the same in register form (FP32, power-of-two gY <= 512): one lane group per column, lines
 //                        straight from Tz into registers, in-register two-step FFT, no block barrier
 //   K2c mv_fftz (inv)  : inverse FFT along z, keep z<boxZ  ->  Xf
 //   K3 mv_fftx_gather  : inverse FFT along x, y = x + S.X for the dipoles of the lines, optional Krylov reductions
 //                        (|y|^2, x.y, y.u*, x.y*) as deterministic per-block partial sums.
+// Every kernel skips the right-hand sides the solver has finished (rhs_done).
 // A particle near a substrate adds, per chunk, K2a in its third mode (the same slab transformed along z with the
 // inverse sign into TzR, so that the product sums heights) and K2b in its surface forms (mv_fft_y_surf, or
 // mv_fft_y_reg<..., true>): D~.X~ + R~.X'~ before the inverse y transform (matvec.c:249-303).
 // The reference's explicit transposes (TransposeYZ), slice zeroing and copies (Arith2/Arith4) do not exist here:
-// every tile is loaded along the contiguous axis of its buffer and transformed in element-major shared memory.
+// every line is read and written along the contiguous axis of its buffer (y), whichever axis it transforms.
 // Every kernel is instantiated with a compile-time FFT length NS for the power-of-two grids (all index arithmetic
 // folds to shifts, passes unroll) and with NS = 0 (runtime plan) for the other fftFit sizes. With FP32 arithmetic and
 // a power-of-two length the lines are transformed in registers (lf_fft: 8-16 threads per line, consecutive threads
