@@ -98,7 +98,7 @@ class RhsStats(ctypes.Structure):
 EXPORTS = ["adda_gb300_fft_fit", "adda_gb300_fit_box", "adda_gb300_make_particle", "adda_gb300_rotation",
            "adda_gb300_plane_wave", "adda_gb300_plane_wave_surf", "adda_gb300_wkb_field", "adda_gb300_polarizability",
            "adda_gb300_polarizability_dchi", "adda_gb300_polarizability_nloc",
-           "adda_gb300_create", "adda_gb300_destroy",
+           "adda_gb300_create", "adda_gb300_create_group", "adda_gb300_destroy",
            "adda_gb300_get_grid", "adda_gb300_init_dmatrix", "adda_gb300_dmatrix_len", "adda_gb300_get_dmatrix",
            "adda_gb300_set_cc", "adda_gb300_set_cc_sqrt", "adda_gb300_set_cc_dipole", "adda_gb300_matvec", "adda_gb300_matvec_device",
            "adda_gb300_solve", "adda_gb300_solve_device", "adda_gb300_solve_many", "adda_gb300_vjp_chi",
@@ -151,6 +151,7 @@ def load_library(path):
         "adda_gb300_polarizability_nloc": ([I, D, D, D, D, P], I),
         "adda_gb300_vjp_chi": ([P, P, I, P, P, P, P, P], I),
         "adda_gb300_create": ([P, P], I),
+        "adda_gb300_create_group": ([P, I, P, P, P, P], I),
         "adda_gb300_destroy": ([P], I),
         "adda_gb300_get_grid": ([P, P], I),
         "adda_gb300_init_dmatrix": ([P], I),
@@ -457,6 +458,59 @@ class Context:
         g = (ctypes.c_int * 3)()
         self.L.adda_gb300_get_grid(self.h, g)
         self.grid = tuple(g)
+
+    @classmethod
+    def group(cls, setups, rhs_per_particle=2, device=0, library=None):
+        """several particles (Setup objects of the same lattice spacing, wavelength and interaction term) solved as
+        one batch: one context in the smallest box that holds every particle, rhs_per_particle RHS each (RHS
+        r belongs to particle r // rhs_per_particle). Vectors are [R][3 * n] with n the largest particle's dipole count
+        (group_pad pads a particle's field); set_cc per RHS, D built, the first rhs_per_particle of each particle's
+        cc set. The phase reference of incident and scattered fields is the centre of the common box (self.box):
+        incident fields come from group_plane_wave."""
+        s0 = setups[0]
+        for s in setups:
+            if s.gridspace != s0.gridspace or s.wavenum != s0.wavenum or s.interaction != s0.interaction:
+                raise ValueError("group: particles need the same lattice spacing, wavelength and interaction term")
+        box = tuple(max(s.box[d] for s in setups) for d in range(3))
+        c = cls.__new__(cls)
+        c.L = library or lib()
+        c._lat = [(np.ascontiguousarray(s.pos, dtype=np.uint16).reshape(-1, 3),
+                   None if s.mat is None else np.ascontiguousarray(s.mat, dtype=np.uint8)) for s in setups]
+        c.counts = [len(p) for p, _ in c._lat]
+        c.n = max(c.counts)
+        c.pos, c.mat = None, None
+        c.nparticles, c.rpp = len(setups), rhs_per_particle
+        c.box, c.gridspace, c.wavenum = box, s0.gridspace, s0.wavenum
+        c.nrhs_max = len(setups) * rhs_per_particle
+        c._tables, c._refl = None, None
+        pr = Problem(box[0], box[1], box[2], 0, 0, 0, 0, None, None, s0.gridspace, s0.wavenum, c.nrhs_max, device,
+                     INTERACTIONS[s0.interaction], getattr(s0, "nloc_rp", 0.0))
+        P_ = len(setups)
+        nd = (ctypes.c_size_t * P_)(*c.counts)
+        pp = (ctypes.c_void_p * P_)(*[_p(p).value for p, _ in c._lat])
+        mm = (ctypes.c_void_p * P_)(*[None if m is None else _p(m).value for _, m in c._lat])
+        c.h = ctypes.c_void_p()
+        _check(c.L.adda_gb300_create_group(ctypes.byref(pr), P_, nd, pp, mm, ctypes.byref(c.h)), "create_group")
+        g = (ctypes.c_int * 3)()
+        c.L.adda_gb300_get_grid(c.h, g)
+        c.grid = tuple(g)
+        c.init_dmatrix()
+        for q, s in enumerate(setups):
+            for k in range(min(rhs_per_particle, len(s.cc))):
+                c.set_cc(q * rhs_per_particle + k, s.cc[k].reshape(1, 3))
+        return c
+
+    def group_plane_wave(self, q, prop, pol):
+        """the incident plane wave at particle q's dipoles, phase reference the common box's centre, padded"""
+        pos = self._lat[q][0]
+        return self.group_pad(plane_wave(self.box, pos, self.gridspace, self.wavenum, prop, pol), q)
+
+    def group_pad(self, field, q):
+        """particle q's [..., 3 * n_q] complex field padded with zeros to the group's vector length"""
+        f = np.asarray(field, dtype=np.complex128)
+        out = np.zeros(f.shape[:-1] + (3 * self.n,), np.complex128)
+        out[..., :f.shape[-1]] = f
+        return out
 
     @classmethod
     def from_setup(cls, s, nrhs_max=2, device=0, library=None):

@@ -111,7 +111,14 @@ static int upload_twiddles(adda_gb300_ctx *c, int which, int n)
 	return ADDA_GB300_OK;
 }
 
-static int create_impl(const adda_gb300_problem *p, adda_gb300_ctx *c)
+// one particle's lattice inside the context's box
+struct Lat {
+	size_t n;
+	const uint16_t *pos;
+	const uint8_t *mat;
+};
+
+static int create_impl(const adda_gb300_problem *p, adda_gb300_ctx *c, const std::vector<Lat> &lats)
 {
 	c->device = p->device;
 	ADDA_CUDA(cudaSetDevice(p->device));
@@ -131,8 +138,15 @@ static int create_impl(const adda_gb300_problem *p, adda_gb300_ctx *c)
 	}
 	c->DsY = c->gY / 2 + 1;
 	c->DsZ = c->gZ / 2 + 1;
-	c->N = p->ndip;
+	c->P = (int)lats.size();
+	c->N = 0;
+	for (const Lat &l : lats) c->N = std::max(c->N, l.n);
 	c->Rmax = p->nrhs_max > 0 ? p->nrhs_max : 1;
+	if (c->P > 1 && (c->Rmax % c->P || p->surface)) {
+		set_error("create_group: nrhs_max must be a multiple of the number of particles (and no substrate)");
+		return ADDA_GB300_EINVAL;
+	}
+	c->rpp = c->Rmax / c->P;
 	c->gridspace = p->gridspace;
 	c->k = p->wavenum;
 	if (p->interaction < ADDA_INT_POI || p->interaction > ADDA_INT_SO || !(p->nloc_rp >= 0)) {
@@ -188,29 +202,41 @@ static int create_impl(const adda_gb300_problem *p, adda_gb300_ctx *c)
 		int rc = upload_twiddles(c, d, g3[d]);
 		if (rc) return rc;
 	}
-	// lattice: check order (z, y, x ascending), build per-line dipole ranges
-	const size_t N = c->N;
-	c->pos.assign(p->position, p->position + 3 * N);
-	c->mat.assign(N, 0);
-	if (p->material) std::copy(p->material, p->material + N, c->mat.begin());
-	std::vector<uint32_t> ls((size_t)c->bZ * c->bY + 1, 0), xy(N);
-	long prev = -1;
-	for (size_t i = 0; i < N; i++) {
-		const int x = c->pos[3 * i], y = c->pos[3 * i + 1], z = c->pos[3 * i + 2];
-		if (x >= c->bX || y >= c->bY || z >= c->bZ) {
-			set_error("dipole position outside the box");
+	// lattices: check order (z, y, x ascending), build per-line dipole ranges. Particle q of a group occupies slot q
+	// of every lattice array: line starts [q][bZ*bY+1] (indices into its own dipoles), xy/material [q][N], positions
+	// [q][N][3], N the largest particle (the other slots padded with zeros)
+	const size_t N = c->N, nl = (size_t)c->bZ * c->bY + 1;
+	c->pos.assign(3 * N * c->P, 0);
+	c->mat.assign(N * c->P, 0);
+	std::vector<uint32_t> ls(nl * c->P, 0), xy(std::max<size_t>(N * c->P, 1), 0);
+	for (int q = 0; q < c->P; q++) {
+		const Lat &L = lats[q];
+		if (L.n && !L.pos) {
+			set_error("create: a particle without positions");
 			return ADDA_GB300_EINVAL;
 		}
-		const long key = ((long)z * c->bY + y) * c->bX + x;
-		if (key <= prev) {
-			set_error("dipole positions must be unique and sorted z-major, then y, then x");
-			return ADDA_GB300_EINVAL;
+		std::copy(L.pos, L.pos + 3 * L.n, c->pos.begin() + 3 * N * q);
+		if (L.mat) std::copy(L.mat, L.mat + L.n, c->mat.begin() + N * q);
+		uint32_t *lq = ls.data() + nl * q;
+		long prev = -1;
+		for (size_t i = 0; i < L.n; i++) {
+			const int x = L.pos[3 * i], y = L.pos[3 * i + 1], z = L.pos[3 * i + 2];
+			if (x >= c->bX || y >= c->bY || z >= c->bZ) {
+				set_error("dipole position outside the box");
+				return ADDA_GB300_EINVAL;
+			}
+			const long key = ((long)z * c->bY + y) * c->bX + x;
+			if (key <= prev) {
+				set_error("dipole positions must be unique and sorted z-major, then y, then x");
+				return ADDA_GB300_EINVAL;
+			}
+			prev = key;
+			lq[(size_t)z * c->bY + y + 1]++;
+			xy[N * q + i] = (uint32_t)x | ((uint32_t)y << 16);
 		}
-		prev = key;
-		ls[(size_t)z * c->bY + y + 1]++;
-		xy[i] = (uint32_t)x | ((uint32_t)y << 16);
+		for (size_t l = 1; l < nl; l++) lq[l] += lq[l - 1];
 	}
-	for (size_t l = 1; l < ls.size(); l++) ls[l] += ls[l - 1];
+	c->lat_stride = N;
 	// the particle must lie entirely above the substrate (make_particle.c:2282): the lowest dipole layer zmin above
 	// its own image, zsum_shift + 2*zmin > 0 (positions are z-major, so the first dipole is in the lowest layer)
 	if (c->surface && N && !(c->zsum_shift + 2.0 * c->pos[2] > 0)) {
@@ -221,15 +247,16 @@ static int create_impl(const adda_gb300_problem *p, adda_gb300_ctx *c)
 		set_error("too many dipoles");
 		return ADDA_GB300_EINVAL;
 	}
+	const size_t NP = std::max<size_t>(N * c->P, 1);
 	ADDA_CUDA(cudaMalloc(&c->d_line_start, sizeof(uint32_t) * ls.size()));
-	ADDA_CUDA(cudaMalloc(&c->d_xy, sizeof(uint32_t) * std::max<size_t>(N, 1)));
-	ADDA_CUDA(cudaMalloc(&c->d_mat, std::max<size_t>(N, 1)));
-	ADDA_CUDA(cudaMalloc(&c->d_pos, sizeof(uint16_t) * 3 * std::max<size_t>(N, 1)));
+	ADDA_CUDA(cudaMalloc(&c->d_xy, sizeof(uint32_t) * NP));
+	ADDA_CUDA(cudaMalloc(&c->d_mat, NP));
+	ADDA_CUDA(cudaMalloc(&c->d_pos, sizeof(uint16_t) * 3 * NP));
 	ADDA_CUDA(cudaMemcpy(c->d_line_start, ls.data(), sizeof(uint32_t) * ls.size(), cudaMemcpyHostToDevice));
 	if (N) {
-		ADDA_CUDA(cudaMemcpy(c->d_xy, xy.data(), sizeof(uint32_t) * N, cudaMemcpyHostToDevice));
-		ADDA_CUDA(cudaMemcpy(c->d_mat, c->mat.data(), N, cudaMemcpyHostToDevice));
-		ADDA_CUDA(cudaMemcpy(c->d_pos, c->pos.data(), sizeof(uint16_t) * 3 * N, cudaMemcpyHostToDevice));
+		ADDA_CUDA(cudaMemcpy(c->d_xy, xy.data(), sizeof(uint32_t) * N * c->P, cudaMemcpyHostToDevice));
+		ADDA_CUDA(cudaMemcpy(c->d_mat, c->mat.data(), N * c->P, cudaMemcpyHostToDevice));
+		ADDA_CUDA(cudaMemcpy(c->d_pos, c->pos.data(), sizeof(uint16_t) * 3 * N * c->P, cudaMemcpyHostToDevice));
 	}
 	// interaction matrix
 	const size_t dlen = (size_t)c->gX * c->DsZ * c->DsY * 6;
@@ -271,6 +298,10 @@ static int create_impl(const adda_gb300_problem *p, adda_gb300_ctx *c)
 	ADDA_CUDA(cudaMalloc(&c->d_red, sizeof(double) * R * 4));
 	ADDA_CUDA(cudaMalloc(&c->vin, sizeof(double2) * R * 3 * std::max<size_t>(N, 1)));
 	ADDA_CUDA(cudaMalloc(&c->vout, sizeof(double2) * R * 3 * std::max<size_t>(N, 1)));
+	if (c->P > 1) { // padded dipoles of smaller particles: the gather never writes them
+		ADDA_CUDA(cudaMemset(c->vin, 0, sizeof(double2) * R * 3 * N));
+		ADDA_CUDA(cudaMemset(c->vout, 0, sizeof(double2) * R * 3 * N));
+	}
 	c->cc_set.assign(R, 0);
 	c->nmat = 0;
 	int rc = matvec_setup(c);
@@ -321,7 +352,36 @@ int adda_gb300_create(const adda_gb300_problem *p, adda_gb300_ctx **out)
 		return ADDA_GB300_ECUDA;
 	}
 	adda_gb300_ctx *c = new adda_gb300_ctx();
-	int rc = create_impl(p, c);
+	int rc = create_impl(p, c, {Lat{p->ndip, p->position, p->material}});
+	if (rc) {
+		std::string keep = g_err;
+		adda_gb300_destroy(c);
+		g_err = keep;
+		return rc;
+	}
+	*out = c;
+	return ADDA_GB300_OK;
+}
+
+int adda_gb300_create_group(const adda_gb300_problem *p, int nparticles, const size_t *ndip,
+	const uint16_t *const *position, const uint8_t *const *material, adda_gb300_ctx **out)
+{
+	if (!p || !out || nparticles < 1 || !ndip || !position || p->boxX < 1 || p->boxY < 1 || p->boxZ < 1 ||
+		p->boxX > 65535 || p->boxY > 65535 || p->boxZ > 65535 || !(p->gridspace > 0) || !(p->wavenum > 0)) {
+		set_error("adda_gb300_create_group: invalid problem description");
+		return ADDA_GB300_EINVAL;
+	}
+	*out = nullptr;
+	int ndev = 0;
+	if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= p->device || p->device < 0) {
+		cudaGetLastError();
+		set_error("adda_gb300_create_group: no usable CUDA device");
+		return ADDA_GB300_ECUDA;
+	}
+	std::vector<Lat> lats(nparticles);
+	for (int q = 0; q < nparticles; q++) lats[q] = Lat{ndip[q], position[q], material ? material[q] : nullptr};
+	adda_gb300_ctx *c = new adda_gb300_ctx();
+	int rc = create_impl(p, c, lats);
 	if (rc) {
 		std::string keep = g_err;
 		adda_gb300_destroy(c);
@@ -532,7 +592,7 @@ static int set_cc_impl(adda_gb300_ctx *c, int rhs, int per_dip, int nmat, const 
 		return ADDA_GB300_EINVAL;
 	}
 	if (!per_dip)
-		for (size_t i = 0; i < c->N; i++)
+		for (size_t i = 0; i < c->mat.size(); i++)
 			if (c->mat[i] >= nmat) {
 				set_error("set_cc: a dipole's material index exceeds nmat");
 				return ADDA_GB300_EINVAL;
@@ -677,6 +737,8 @@ int adda_gb300_matvec(adda_gb300_ctx *c, int prec, int nrhs, const double *argve
 	const size_t n = (size_t)nrhs * 3 * c->N;
 	double *d_ip = c->d_red + 4 * (size_t)c->Rmax - 0; // not used directly; inprod goes through d_red
 	(void)d_ip;
+	// group contexts: the gather writes only real dipoles, so the padding of the result comes back as zeros
+	if (c->P > 1) ADDA_CUDA(cudaMemsetAsync(c->vout, 0, sizeof(double2) * n, c->stream));
 	if (prec == ADDA_PREC_FP64) {
 		ADDA_CUDA(cudaMemcpyAsync(c->vin, argvec, sizeof(double2) * n, cudaMemcpyHostToDevice, c->stream));
 		MvEpi e{inprod ? (int)EPI_NORM : (int)EPI_NONE, nullptr, c->partial};
@@ -737,6 +799,10 @@ size_t adda_gb300_chpoint_size(const adda_gb300_ctx *c, int method)
 
 int adda_gb300_chpoint_save(adda_gb300_ctx *c, int rhs, void *buf, size_t size)
 {
+	if (c && c->P > 1) {
+		set_error("chpoint_save: checkpoints hold one particle's vectors (not a group context)");
+		return ADDA_GB300_ESTATE;
+	}
 	if (!c) {
 		set_error("chpoint_save: invalid arguments");
 		return ADDA_GB300_EINVAL;
@@ -747,6 +813,10 @@ int adda_gb300_chpoint_save(adda_gb300_ctx *c, int rhs, void *buf, size_t size)
 
 int adda_gb300_chpoint_load(adda_gb300_ctx *c, int rhs, const void *buf, size_t size)
 {
+	if (c && c->P > 1) {
+		set_error("chpoint_load: checkpoints hold one particle's vectors (not a group context)");
+		return ADDA_GB300_ESTATE;
+	}
 	if (!c) {
 		set_error("chpoint_load: invalid arguments");
 		return ADDA_GB300_EINVAL;
@@ -867,6 +937,10 @@ int adda_gb300_vjp_chi(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int
 	if (c && c->surface) {
 		set_error("vjp_chi: free-space formula; in surface mode the reference scatters through CalcFieldSurf "
 			"(crosssec.c:601-800), which is not provided (Cext/Cabs: adda_gb300_cross_sections_beam)");
+		return ADDA_GB300_ESTATE;
+	}
+	if (c && c->P > 1) {
+		set_error("vjp_chi: one particle per context (not a group context)");
 		return ADDA_GB300_ESTATE;
 	}
 	if (!c || !sp || !prop || !incpol || !dinv_alpha || !grad_cext || !grad_cabs) {

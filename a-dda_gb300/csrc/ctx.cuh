@@ -76,7 +76,11 @@ struct adda_gb300_ctx {
 	double2 *R64 = nullptr;
 	float2 *R32 = nullptr;
 	double gridspace = 0, k = 0;
-	// lattice (host and device)
+	// lattice (host and device). A group context (adda_gb300_create_group) holds P particles in one box: particle q's
+	// arrays are slot q of each lattice array (stride lat_stride = N, the largest particle; line starts stride
+	// bZ*bY+1), and RHS r belongs to particle r / rpp. A single lattice: P = 1, rpp = Rmax.
+	int P = 1, rpp = 1;
+	size_t lat_stride = 0;
 	std::vector<uint16_t> pos;
 	std::vector<uint8_t> mat;
 	uint32_t *d_line_start = nullptr; // [bZ*bY+1]: index of the first dipole of x-line (y,z), lines z-major

@@ -63,6 +63,8 @@ template <typename T> struct MvGeom {
 	C *TzR;
 	const C *Rm;
 	int RsY;
+	int rpp;           // RHS per particle: RHS r uses lattice slot r / rpp (a group context, adda_gb300_create_group)
+	size_t lat_stride; // dipoles per lattice slot
 };
 
 template <typename T, typename V> struct MvP : MvGeom<T> {
@@ -116,18 +118,22 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T,
 	C *a = reinterpret_cast<C *>(smem_raw);
 	C *b = a + (size_t)n * LS; // second tile of the Stockham form only
 	const int r = blockIdx.z, z = blockIdx.y, y0 = blockIdx.x * W;
+	// the lattice of RHS r's particle (a single-lattice context has one)
+	const size_t lq = (size_t)(r / p.rpp);
+	const uint32_t *lstart = p.line_start + lq * ((size_t)p.bZ * p.bY + 1), *lxy = p.xy + lq * p.lat_stride;
+	const uint8_t *lmat = p.mat + lq * p.lat_stride;
 	const int wy = min(W, p.bY - y0);
 	// the column form reads elements x < gX/2 only (gX >= 2 bX for the power-of-two lengths it is built for)
 	for (int t = threadIdx.x; t < (RC ? n / 2 : n) * LS; t += NT) a[t] = cx<C>(0, 0);
 	__syncthreads();
 	const size_t line = (size_t)z * p.bY + y0;
-	const uint32_t i0 = p.line_start[line], i1 = p.line_start[line + wy];
+	const uint32_t i0 = lstart[line], i1 = lstart[line + wy];
 	const V *arg = p.arg + (size_t)r * p.N * 3;
 #pragma unroll 2
 	for (uint32_t i = i0 + threadIdx.x; i < i1; i += NT) {
-		const uint32_t q = p.xy[i];
+		const uint32_t q = lxy[i];
 		const int x = q & 0xffff, y = q >> 16;
-		const uint8_t m = p.mat[i];
+		const uint8_t m = lmat[i];
 #pragma unroll
 		for (int comp = 0; comp < 3; comp++) {
 			C v = cvt<C>(arg[(size_t)i * 3 + comp]);
@@ -626,6 +632,10 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T,
 	C *a = reinterpret_cast<C *>(smem_raw);
 	C *b = a + (size_t)n * LS;
 	const int r = blockIdx.z, z = blockIdx.y, y0 = blockIdx.x * W;
+	// the lattice of RHS r's particle (a single-lattice context has one)
+	const size_t lq = (size_t)(r / p.rpp);
+	const uint32_t *lstart = p.line_start + lq * ((size_t)p.bZ * p.bY + 1), *lxy = p.xy + lq * p.lat_stride;
+	const uint8_t *lmat = p.mat + lq * p.lat_stride;
 	const int wy = min(W, p.bY - y0);
 	const size_t plane = (size_t)p.bZ * p.bY;
 	const C *xf = p.Xf + (size_t)r * p.gX * 3 * plane + (size_t)z * p.bY + y0;
@@ -662,15 +672,15 @@ __global__ void __launch_bounds__(col_threads<T, NS, 3 * W>(), (col_minblocks<T,
 		o = tile_fft<C, NS, NL, LS, true>(a, b, p.px, p.twx);
 	}
 	const size_t line = (size_t)z * p.bY + y0;
-	const uint32_t i0 = p.line_start[line], i1 = p.line_start[line + wy];
+	const uint32_t i0 = lstart[line], i1 = lstart[line + wy];
 	const V *arg = p.arg + (size_t)r * p.N * 3;
 	V *res = p.res + (size_t)r * p.N * 3;
 	const V *u = e.u ? reinterpret_cast<const V *>(e.u) + (size_t)r * p.N * 3 : nullptr;
 	typename AccOf<V>::T s0{}, s1r{}, s1i{};
 	for (uint32_t i = i0 + threadIdx.x; i < i1; i += NT) {
-		const uint32_t q = p.xy[i];
+		const uint32_t q = lxy[i];
 		const int x = q & 0xffff, y = q >> 16;
-		const uint8_t m = p.mat[i];
+		const uint8_t m = lmat[i];
 #pragma unroll
 		for (int comp = 0; comp < 3; comp++) {
 			const size_t j = (size_t)i * 3 + comp;
@@ -939,6 +949,8 @@ int launch_matvec(adda_gb300_ctx *c, int R, const V *arg, V *res, int her, const
 	p.TzR = (C *)c->TzR;
 	p.Rm = dbl ? (const C *)c->R64 : (const C *)c->R32;
 	p.RsY = c->gY / 2 + 1;
+	p.rpp = c->rpp;
+	p.lat_stride = c->lat_stride;
 	cudaStream_t st = c->stream;
 	const dim3 g1((c->bY + sh.w1 - 1) / sh.w1, c->bZ, R);
 	ADDA_NS_SWITCH(c->gX, ADDA_W_SWITCH(has_w1, sh.w1, (mv_scatter_fftx<T, V, W, NS><<<g1, col_threads<T, NS, 3 * W>(),

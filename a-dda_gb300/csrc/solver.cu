@@ -176,9 +176,10 @@ __device__ __forceinline__ void sum_part(const double *part, size_t nblk, int r,
 
 // b = S.E (nMult_mat, linalg.c:549); partial |b|^2. E, b FP64.
 __global__ void __launch_bounds__(NT) k_mult_cc(const double2 *E, double2 *b, const double2 *ccs, int per_dip, int nmat,
-	const uint8_t *mat, size_t N, double *part, int nbv)
+	const uint8_t *mat, size_t N, double *part, int nbv, int rpp, size_t lst)
 {
 	const int r = blockIdx.y;
+	mat += (size_t)(r / rpp) * lst; // RHS r's particle (group contexts)
 	const size_t n3 = 3 * N;
 	double v[4] = {0, 0, 0, 0};
 	VLOOP(n3) {
@@ -1258,9 +1259,10 @@ template <typename C> __global__ void __launch_bounds__(NT) k_from64(C *dst, con
 
 // p = S.x (iterative.c:1527)
 __global__ void __launch_bounds__(NT) k_pvec(const double2 *x, double2 *p, const double2 *ccs, int per_dip, int nmat,
-	const uint8_t *mat, size_t N)
+	const uint8_t *mat, size_t N, int rpp, size_t lst)
 {
 	const int r = blockIdx.y;
+	mat += (size_t)(r / rpp) * lst; // RHS r's particle (group contexts)
 	const size_t n3 = 3 * N;
 	VLOOP(n3) {
 		const size_t d = i / 3;
@@ -1273,9 +1275,12 @@ __global__ void __launch_bounds__(NT) k_pvec(const double2 *x, double2 *p, const
 // cross-section sums per RHS: sum_j P_j exp(-i kd n.pos_j) (CalcFieldFree, crosssec.c:506-586) and
 // sum_j sum_c (-Im(1/cc) - 2k^3/3)|P_jc|^2 (AbsCross, crosssec.c:866-882)
 __global__ void __launch_bounds__(NT) k_cross(const double2 *P, const uint16_t *pos, const double2 *cc, int per_dip,
-	int nmat, const uint8_t *mat, size_t N, const double *prop, double kd, double k3, double *part, int nbv)
+	int nmat, const uint8_t *mat, size_t N, const double *prop, double kd, double k3, double *part, int nbv, int rpp,
+	size_t lst)
 {
 	const int r = blockIdx.y;
+	mat += (size_t)(r / rpp) * lst; // RHS r's particle (group contexts)
+	pos += (size_t)(r / rpp) * lst * 3;
 	const double n0 = prop[3 * r], n1 = prop[3 * r + 1], n2 = prop[3 * r + 2];
 	double s[7] = {0, 0, 0, 0, 0, 0, 0};
 	for (size_t d = blockIdx.x * (size_t)blockDim.x + threadIdx.x; d < N; d += (size_t)gridDim.x * blockDim.x) {
@@ -1313,9 +1318,10 @@ __global__ void __launch_bounds__(NT) k_cross(const double2 *P, const uint16_t *
 // general-beam cross-section sums per RHS: sum_j Im(P_j . conj(Einc_j)) (ExtCross, crosssec.c:823-830) and the AbsCross
 // sum of k_cross
 __global__ void __launch_bounds__(NT) k_cross_beam(const double2 *P, const double2 *E, const double2 *cc, int per_dip,
-	int nmat, const uint8_t *mat, size_t N, double k3, double *part, int nbv)
+	int nmat, const uint8_t *mat, size_t N, double k3, double *part, int nbv, int rpp, size_t lst)
 {
 	const int r = blockIdx.y;
+	mat += (size_t)(r / rpp) * lst; // RHS r's particle (group contexts)
 	double s[2] = {0, 0};
 	for (size_t d = blockIdx.x * (size_t)blockDim.x + threadIdx.x; d < N; d += (size_t)gridDim.x * blockDim.x) {
 		for (int c = 0; c < 3; c++) {
@@ -1348,9 +1354,10 @@ __global__ void __launch_bounds__(NT) k_cross_beam(const double2 *P, const doubl
 // scattering amplitudes (CalcFieldFree, crosssec.c:506-596), first stage: per block partial sums of
 // P_j exp(-i kd n.pos_j) for direction blockIdx.y and RHS blockIdx.z (6 doubles: Re/Im of the 3 components)
 __global__ void __launch_bounds__(NT) k_field(const double2 *P, const uint16_t *pos, size_t N, const double *dirs,
-	double kd, double *part)
+	double kd, double *part, int rpp, size_t lst)
 {
 	const int d = blockIdx.y, r = blockIdx.z, nb = gridDim.x;
+	pos += (size_t)(r / rpp) * lst * 3; // RHS r's particle (group contexts)
 	const double n0 = dirs[3 * d], n1 = dirs[3 * d + 1], n2 = dirs[3 * d + 2];
 	double s[6] = {0, 0, 0, 0, 0, 0};
 	for (size_t j = blockIdx.x * (size_t)NT + threadIdx.x; j < N; j += (size_t)nb * NT) {
@@ -1471,6 +1478,13 @@ static int ensure_work(adda_gb300_ctx *c, int R, int hist_cap)
 		ADDA_CUDA(cudaMalloc(&w->vpart, sizeof(double) * Rm * w->nbv * 4));
 		ADDA_CUDA(cudaMalloc(&w->xpart, sizeof(double) * Rm * w->nbv * 8));
 		if (!c->pvec64) ADDA_CUDA(cudaMalloc(&c->pvec64, vb));
+		if (c->P > 1) {
+			// group contexts: the vectors of a smaller particle are padded to the largest particle's length; the gather
+			// writes only real dipoles, so the padding starts at zero and every update keeps it there
+			void *bufs[] = {w->x64, w->r64, w->b64, w->av64, w->kv[0], w->kv[1], w->kv[2], w->kv[3], w->kv[4], w->kv[5],
+				w->kv[6], w->kv[7], c->pvec64};
+			for (void *b : bufs) ADDA_CUDA(cudaMemset(b, 0, vb));
+		}
 	}
 	if (hist_cap > w->hist_cap) {
 		if (w->hist) cudaFree(w->hist);
@@ -2133,7 +2147,8 @@ static int solve_core_impl(adda_gb300_ctx *c, const adda_gb300_solve_params *sp,
 	for (auto &x : st) memset(&x, 0, sizeof(x));
 	std::vector<RhsState> hs(R);
 	// b = S.Einc in FP64
-	k_mult_cc<<<gv, NT, 0, s>>>(d_einc, w->b64, c->ccs64, c->per_dip, c->nmat, c->d_mat, c->N, w->vpart, w->nbv);
+	k_mult_cc<<<gv, NT, 0, s>>>(d_einc, w->b64, c->ccs64, c->per_dip, c->nmat, c->d_mat, c->N, w->vpart, w->nbv, c->rpp,
+		c->lat_stride);
 	ADDA_LAUNCHED();
 	ADDA_CUDA(cudaMemsetAsync(w->hist, 0, sizeof(double) * R * w->hist_cap, s));
 	for (int i = 0; i < 8; i++) ADDA_CUDA(cudaMemsetAsync(w->kv[i], 0, sizeof(double2) * R * n3, s));
@@ -2266,7 +2281,7 @@ static int solve_core_impl(adda_gb300_ctx *c, const adda_gb300_solve_params *sp,
 		if ((rc = solve_mixed<float2>(c, sp, R, st.data(), mc, K))) return rc;
 	}
 	// polarisations p = S.x (FP64) stay on the device (iterative.c:1527)
-	k_pvec<<<gv, NT, 0, s>>>(w->x64, c->pvec64, c->ccs64, c->per_dip, c->nmat, c->d_mat, c->N);
+	k_pvec<<<gv, NT, 0, s>>>(w->x64, c->pvec64, c->ccs64, c->per_dip, c->nmat, c->d_mat, c->N, c->rpp, c->lat_stride);
 	ADDA_LAUNCHED();
 	c->last_nrhs = R;
 	if (stats)
@@ -2463,7 +2478,9 @@ int vjp_chi(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int rhs, const
 	const double ph0 = -c->k * (r0[0] * prop[0] + r0[1] * prop[1] + r0[2] * prop[2]);
 	const double2 *ccr = c->cc64 + per * rhs;
 	const int gN = (int)std::max<size_t>(1, std::min<size_t>((N + NT - 1) / NT, 152 * 16));
-	k_adj_rhs<<<gN, NT, 0, s>>>(w->av64, save_p + n3 * rhs, c->d_pos, ccr, c->per_dip, c->nmat, c->d_mat, N, prop[0],
+	const size_t lq = (size_t)(rhs / c->rpp) * c->lat_stride; // the RHS's particle (group contexts)
+	k_adj_rhs<<<gN, NT, 0, s>>>(w->av64, save_p + n3 * rhs, c->d_pos + 3 * lq, ccr, c->per_dip, c->nmat, c->d_mat + lq, N,
+		prop[0],
 		prop[1], prop[2], incpol[0], incpol[1], incpol[2], kd, c->k, ph0);
 	ADDA_LAUNCHED();
 	adda_gb300_rhs_stats st[2];
@@ -2528,7 +2545,8 @@ int scattered_fields(adda_gb300_ctx *c, int R, int ndir, const double *dirs, dou
 	if (cudaMemcpyAsync(d_dirs, dirs, sizeof(double) * 3 * ndir, cudaMemcpyHostToDevice, s) != cudaSuccess)
 		rc = ADDA_GB300_ECUDA;
 	if (!rc && N) {
-		k_field<<<dim3(nb, ndir, R), NT, 0, s>>>(c->pvec64, c->d_pos, N, d_dirs, c->k * c->gridspace, d_part);
+		k_field<<<dim3(nb, ndir, R), NT, 0, s>>>(c->pvec64, c->d_pos, N, d_dirs, c->k * c->gridspace, d_part, c->rpp,
+			c->lat_stride);
 		if (cudaGetLastError() != cudaSuccess) rc = ADDA_GB300_ECUDA;
 		else count_launch();
 	}
@@ -2566,7 +2584,7 @@ int cross_sections(adda_gb300_ctx *c, int R, const double *prop, const double *i
 	const dim3 g(w->nbv, R);
 	const double kd = c->k * c->gridspace, k3 = c->k * c->k * c->k;
 	k_cross<<<g, NT, 0, s>>>(c->pvec64, c->d_pos, c->cc64, c->per_dip, c->nmat, c->d_mat, c->N, d_prop, kd, k3,
-		w->xpart, w->nbv);
+		w->xpart, w->nbv, c->rpp, c->lat_stride);
 	ADDA_LAUNCHED();
 	std::vector<double> part((size_t)R * w->nbv * 8);
 	ADDA_CUDA(cudaMemcpyAsync(part.data(), w->xpart, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, s));
@@ -2615,7 +2633,7 @@ int cross_sections_beam(adda_gb300_ctx *c, int R, const double *einc, double inc
 	if (e == cudaSuccess) {
 		const dim3 g(w->nbv, R);
 		k_cross_beam<<<g, NT, 0, s>>>(c->pvec64, d_e, c->cc64, c->per_dip, c->nmat, c->d_mat, c->N,
-			c->k * c->k * c->k, w->xpart, w->nbv);
+			c->k * c->k * c->k, w->xpart, w->nbv, c->rpp, c->lat_stride);
 		count_launch();
 		e = cudaGetLastError();
 	}

@@ -221,6 +221,19 @@ int adda_gb300_polarizability_dchi(int relation, double m_re, double m_im, doubl
 /* ParSetup + allocation half of InitDmatrix (comm.c:481-535, fft.c:1164-1209): validates the lattice, uploads it
  * and allocates every device buffer. Fails with ADDA_GB300_ECUDA when no GPU is usable. */
 int adda_gb300_create(const adda_gb300_problem *p, adda_gb300_ctx **out);
+/* Several particles solved as one batch (no counterpart in the reference, which solves particles one after another,
+ * calculator.c:348-358): nparticles lattices of ndip[q] dipoles (positions[q], materials[q] or NULL) in the common box
+ * and grid of p (every particle inside it; p->ndip, p->position and p->material are ignored), sharing D; p->nrhs_max
+ * = nparticles x the RHS per particle, and RHS r belongs to particle r / (nrhs_max / nparticles). Vectors have the
+ * largest particle's length ndip_max per RHS, [nrhs][ndip_max][3]: the entries past a smaller particle's ndip[q] are
+ * padding, which the incident field must leave at zero and the solve keeps at zero (adda_gb300_matvec returns zeros
+ * there, adda_gb300_matvec_device leaves the padding of d_res as it was); set_cc per RHS gives each
+ * particle its own polarizabilities. The phase reference of the incident field, the cross sections and the scattered
+ * fields is the centre of the common box (a particle's own box centre only shifts the phase of its solution). Every matvec stage, vector update and reduction then runs once for all
+ * particles' RHS (one launch per stage, one CUDA graph per batch of iterations), and a particle whose RHS have all
+ * converged costs no more FFT work. Free space only; checkpoints and the VJP take single-lattice contexts. */
+int adda_gb300_create_group(const adda_gb300_problem *p, int nparticles, const size_t *ndip,
+	const uint16_t *const *positions, const uint8_t *const *materials, adda_gb300_ctx **out);
 /* Free_FFT_Dmat, src/fft.c:1420-1493 */
 int adda_gb300_destroy(adda_gb300_ctx *ctx);
 /* grid actually used (after fftFit) */
