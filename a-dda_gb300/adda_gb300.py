@@ -460,18 +460,22 @@ class Context:
         self.grid = tuple(g)
 
     @classmethod
-    def group(cls, setups, rhs_per_particle=2, device=0, library=None):
+    def group(cls, setups, rhs_per_particle=2, device=0, library=None, box=None):
         """several particles (Setup objects of the same lattice spacing, wavelength and interaction term) solved as
         one batch: one context in the smallest box that holds every particle, rhs_per_particle RHS each (RHS
         r belongs to particle r // rhs_per_particle). Vectors are [R][3 * n] with n the largest particle's dipole count
         (group_pad pads a particle's field); set_cc per RHS, D built, the first rhs_per_particle of each particle's
         cc set. The phase reference of incident and scattered fields is the centre of the common box (self.box):
-        incident fields come from group_plane_wave."""
+        incident fields come from group_plane_wave. box: a larger common box (e.g. one whose FFT grid is a power of
+        two, for the compile-time transforms)."""
         s0 = setups[0]
         for s in setups:
             if s.gridspace != s0.gridspace or s.wavenum != s0.wavenum or s.interaction != s0.interaction:
                 raise ValueError("group: particles need the same lattice spacing, wavelength and interaction term")
-        box = tuple(max(s.box[d] for s in setups) for d in range(3))
+        fit = tuple(max(s.box[d] for s in setups) for d in range(3))
+        box = fit if box is None else tuple(int(b) for b in box)
+        if any(b < f for b, f in zip(box, fit)):
+            raise ValueError("group: the common box must hold every particle")
         c = cls.__new__(cls)
         c.L = library or lib()
         c._lat = [(np.ascontiguousarray(s.pos, dtype=np.uint16).reshape(-1, 3),

@@ -383,6 +383,11 @@ def run_ours(args):
             line["batch_ellipsoids"] = run_batch(args)
         except Exception as ex:
             line["batch_ellipsoids"] = {"error": str(ex)}
+        if args.group_particles > 0:
+            try:
+                line["batch_grouped"] = run_group(args)
+            except Exception as ex:
+                line["batch_grouped"] = {"error": str(ex)}
     if rank == 0 and world == 1 and not args.no_cpu:
         arm = CpuArm(args.method, os.cpu_count() or 1)
         arm.sample()
@@ -516,6 +521,73 @@ def run_batch(args):
             "boxes": boxes, "max_iterations_per_particle": iters}
 
 
+def run_group(args):
+    """grouped batching: the first --group-particles of the seeded ellipsoids (run_batch's sequence) whose box is 24 or 32,
+    at one lattice spacing (dpl 17 = 10 x the largest |m|, so that all share D), 16 orientations x 2 polarisations
+    each, solved (mixed, --batch-method, to 1e-5) once one context per particle, once as one group context (all
+    particles' RHS in every launch; the common box is the largest particle's cube, so the FFT grid is a power of two).
+    CUDA-event solve times."""
+    import torch
+    import adda_gb300 as A
+    rng = np.random.default_rng(20261203)
+    nrhs, dpl = 32, 17.0
+    parts = []
+    while len(parts) < args.group_particles:
+        box = int(rng.choice([24, 32, 48, 64, 96]))
+        r1, r2 = (float(v) for v in rng.uniform(0.5, 1.0, 2))
+        m = complex(rng.uniform(1.2, 1.7), rng.uniform(0.0, 0.05))
+        orients = [(rng.uniform(0, 360), math.degrees(math.acos(rng.uniform(-1, 1))), rng.uniform(0, 360))
+                   for _ in range(nrhs // 2)]
+        if box <= 32:
+            parts.append((A.Setup(grid=box, shape="ellipsoid", pars=(r1, r2), m=m, dpl=dpl), orients))
+
+    def rhs(s, orients, box):
+        cc, e = [], []
+        for o in orients:
+            prop, py, px = A.rotation(*o)
+            for pol in (py, px):
+                cc.append(A.polarizability(s.m, s.kd, s.gridspace, prop, pol).reshape(1, 3))
+                e.append(A.plane_wave(box, s.pos, s.gridspace, s.wavenum, prop, pol))
+        return cc, e
+    seq_s, seq_it, unconv = 0.0, [], 0
+    for s, orients in parts:
+        ctx = A.Context(s.box, s.pos, s.mat, s.gridspace, s.wavenum, s.grid, nrhs_max=nrhs)
+        ctx.init_dmatrix()
+        cc, e = rhs(s, orients, s.box)
+        for r in range(nrhs):
+            ctx.set_cc(r, cc[r])
+        d_e = torch.from_numpy(np.ascontiguousarray(np.stack(e)).view(np.float64)).cuda()
+        st = ctx.solve_device(d_e.data_ptr(), nrhs, None, None, method=args.batch_method, prec="mixed", eps=EPS,
+                              maxiter=args.batch_maxiter)
+        seq_s += ctx.last_solve_ms() / 1e3
+        seq_it.append(max(x["niter"] for x in st))
+        unconv += sum(x["status"] != "ok" for x in st)
+        ctx.close()
+    # the common box rounded up to the power-of-two FFT grid of the largest particle class (compile-time transforms)
+    gb = max(max(s.box) for s, _ in parts)
+    g = A.Context.group([s for s, _ in parts], rhs_per_particle=nrhs, box=(gb, gb, gb))
+    es = []
+    for q, (s, orients) in enumerate(parts):
+        cc, e = rhs(s, orients, g.box)
+        for k in range(nrhs):
+            g.set_cc(q * nrhs + k, cc[k])
+        es.append(g.group_pad(np.stack(e), q))
+    d_e = torch.from_numpy(np.ascontiguousarray(np.concatenate(es)).view(np.float64)).cuda()
+    st = g.solve_device(d_e.data_ptr(), nrhs * len(parts), None, None, method=args.batch_method, prec="mixed",
+                        eps=EPS, maxiter=args.batch_maxiter)
+    grp_s = g.last_solve_ms() / 1e3
+    gunconv = sum(x["status"] != "ok" for x in st)
+    out = {"workload": "%d seeded ellipsoids with boxes of 24 or 32 (dpl 17) x 16 orientations x 2 polarisations "
+                       "(%d RHS), mixed %s to 1e-5" % (len(parts), nrhs * len(parts), args.batch_method),
+           "boxes": [list(s.box) for s, _ in parts], "group_box": list(g.box), "group_grid": list(g.grid),
+           "one_context_per_particle": {"solve_s": seq_s, "rhs_per_s": nrhs * len(parts) / seq_s,
+                                        "max_iterations_per_particle": seq_it, "rhs_not_converged": unconv},
+           "group_context": {"solve_s": grp_s, "rhs_per_s": nrhs * len(parts) / grp_s,
+                             "max_iterations": max(x["niter"] for x in st), "rhs_not_converged": gunconv}}
+    g.close()
+    return out
+
+
 def run_profile(args):
     """small, fixed workloads for ncu: 'solve' = one warm-up + one mixed solve of the bench workload;
     'matvec' = three FP32 matvecs (2 RHS) of the bench workload; 'surface' = three FP32 matvecs (2 RHS) of the
@@ -550,6 +622,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-surface", action="store_true", help="skip the substrate variant of the workload")
     ap.add_argument("--no-scale", action="store_true", help="skip the scale workload (256^3 sphere, 512^3 grid)")
+    ap.add_argument("--group-particles", type=int, default=8,
+                    help="small seeded ellipsoids solved one context each and as one group context (0 skips)")
     ap.add_argument("--batch-particles", type=int, default=4,
                     help="time the batching workload (64 seeded ellipsoids x 16 orientations) on this many particles "
                          "(0: skip)")
