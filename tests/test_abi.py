@@ -61,6 +61,21 @@ def test_create_fails_loudly_without_gpu(adda):
         adda.Context(box, pos, mat, 0.5, 1.0)
 
 
+def test_create_group_rejects_bad_arguments(adda):
+    """adda_gb300_create_group checks its description before touching a device (EINVAL = -1)"""
+    L = adda.lib()
+    box, pos, mat = adda.make_particle("sphere", 8)
+    pr = adda.Problem(box[0], box[1], box[2], 0, 0, 0, 0, None, None, 0.5, 1.0, 2, 0, 0, 0.0)
+    nd = (ctypes.c_size_t * 1)(len(pos))
+    pp = (ctypes.c_void_p * 1)(pos.ctypes.data)
+    h = ctypes.c_void_p()
+    assert L.adda_gb300_create_group(ctypes.byref(pr), 0, nd, pp, None, ctypes.byref(h)) == -1    # no particle
+    assert L.adda_gb300_create_group(ctypes.byref(pr), 1, None, pp, None, ctypes.byref(h)) == -1  # no counts
+    bad = adda.Problem(0, box[1], box[2], 0, 0, 0, 0, None, None, 0.5, 1.0, 2, 0, 0, 0.0)
+    assert L.adda_gb300_create_group(ctypes.byref(bad), 1, nd, pp, None, ctypes.byref(h)) == -1   # empty box
+    assert not h.value
+
+
 def test_host_functions_reject_bad_arguments(adda):
     """the host-side entry points return the reference's error cases as status codes instead of aborting"""
     L = adda.lib()
