@@ -1948,9 +1948,11 @@ static int solve_mixed(adda_gb300_ctx *c, const adda_gb300_solve_params *sp, int
 			ADDA_CUDA(cudaMemcpyAsync(d_odone, w->h_done, sizeof(int) * R, cudaMemcpyHostToDevice, s));
 			k_accum<C><<<gv, NT, 0, s>>>(w->x64, k.x, n3, refine ? 1 : 0, d_odone);
 			ADDA_LAUNCHED();
-			// true residual in FP64: r64 = b - A64.x64, |r64|^2; float copy into k.v3 for the next inner solve
+			// true residual in FP64: r64 = b - A64.x64, |r64|^2; float copy into k.v3 for the next inner solve. The
+			// RHS that had finished before this step keep their x64, so their A64.x64 in av64 is still current: the
+			// matvec skips them
 			MvEpi e{EPI_NONE, nullptr, c->partial};
-			if ((rc = matvec_run<double>(c, R, w->x64, w->av64, 0, e, nullptr))) return rc;
+			if ((rc = matvec_run<double>(c, R, w->x64, w->av64, 0, e, d_odone))) return rc;
 			k_resid64<C><<<gv, NT, 0, s>>>(w->b64, w->av64, w->r64, k.v3, n3, w->vpart, w->nbv);
 			ADDA_LAUNCHED();
 			if ((rc = reduce_partials(c, R, w->vpart, w->nbv, c->d_red))) return rc;
