@@ -735,8 +735,6 @@ int adda_gb300_matvec(adda_gb300_ctx *c, int prec, int nrhs, const double *argve
 	if (rc) return rc;
 	ADDA_CUDA(cudaSetDevice(c->device));
 	const size_t n = (size_t)nrhs * 3 * c->N;
-	double *d_ip = c->d_red + 4 * (size_t)c->Rmax - 0; // not used directly; inprod goes through d_red
-	(void)d_ip;
 	// group contexts: the gather writes only real dipoles, so the padding of the result comes back as zeros
 	if (c->P > 1) ADDA_CUDA(cudaMemsetAsync(c->vout, 0, sizeof(double2) * n, c->stream));
 	if (prec == ADDA_PREC_FP64) {
@@ -747,10 +745,10 @@ int adda_gb300_matvec(adda_gb300_ctx *c, int prec, int nrhs, const double *argve
 		ADDA_CUDA(cudaMemcpyAsync(resultvec, c->vout, sizeof(double2) * n, cudaMemcpyDeviceToHost, c->stream));
 	}
 	else if (prec == ADDA_PREC_FP32) {
-		// stage the double host vector, round it on the device, compute, widen the result back
+		// stage the double host vector, round it on the device, compute, widen the result back (vout holds the 2n
+		// float2 of the rounded input and the FP32 result: n double2)
 		double2 *din = (double2 *)c->vin;
 		float2 *fin = (float2 *)c->vout, *fout = (float2 *)c->vout + n;
-		if (2 * n * sizeof(float2) > sizeof(double2) * n + 0) { /* vout holds 2n float2 == n double2 */ }
 		ADDA_CUDA(cudaMemcpyAsync(din, argvec, sizeof(double2) * n, cudaMemcpyHostToDevice, c->stream));
 		d2f_k<<<(int)std::min<size_t>((n + 255) / 256, 8192), 256, 0, c->stream>>>(fin, din, n);
 		ADDA_LAUNCHED();
